@@ -1,0 +1,144 @@
+/* lh2g_types.h - wire formats of the GB300 wavefront render core.
+ *
+ * Plain C structs shared by the C-ABI (lh2g.h), the CUDA kernels and the CPU oracle.
+ * Every struct here is laid out byte-for-byte like the Lighthouse 2 type it stands for, so that
+ * arrays built by the Lighthouse 2 RenderSystem can be handed over without conversion:
+ *
+ *   lh2g_core_tri      <-> CoreTri            lib/RenderSystem/common_classes.h:57-97   (208 B)
+ *   lh2g_light_tri     <-> CoreLightTri       lib/RenderSystem/common_classes.h:365-385 (96 B)
+ *   lh2g_point_light   <-> CorePointLight     lib/RenderSystem/common_classes.h:392-404 (32 B)
+ *   lh2g_spot_light    <-> CoreSpotLight      lib/RenderSystem/common_classes.h:411-426 (48 B)
+ *   lh2g_dir_light     <-> CoreDirectionalLight lib/RenderSystem/common_classes.h:433-445 (32 B)
+ *   lh2g_view          <-> ViewPyramid        lib/RenderSystem/common_classes.h:452-475 (68 B)
+ *   lh2g_texture       <-> CoreTexDesc (host) lib/RenderSystem/common_classes.h:336-359 (40 B)
+ *   lh2g_ray           <-> Ray (OptiX Prime ORIGIN_TMIN_DIRECTION_TMAX)
+ *                                             lib/RenderCore_PrimeRef/core_settings.h:151 (32 B)
+ *   lh2g_hit           <-> hit float4 {u|v<<16, inst, prim, t}
+ *                                             lib/rendercore_optix7/optix/.optix.cu:180-183 (16 B)
+ *   lh2g_gpu_material  <-> CUDAMaterial       lib/rendercore_optix7/core_settings.h:136-185 (128 B)
+ */
+#ifndef LH2G_TYPES_H
+#define LH2G_TYPES_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* One triangle with all shading attributes (CoreTri). Vertex positions are in object space. */
+typedef struct lh2g_core_tri {
+    float u0, u1, u2; int32_t ltriIdx;      /* texture u per vertex; light index for emissive tris */
+    float v0, v1, v2; uint32_t material;    /* texture v per vertex; material index */
+    float vN0[3]; float Nx;                 /* vertex normal 0; face normal x */
+    float vN1[3]; float Ny;
+    float vN2[3]; float Nz;
+    float T[3]; float area;                 /* tangent; area */
+    float B[3]; float invArea;              /* bitangent */
+    float alpha[3]; float LOD;              /* consistent-normal alphas; texture LOD bias */
+    float vertex0[3]; float dummy0;
+    float vertex1[3]; float dummy1;
+    float vertex2[3]; float dummy2;
+    float u1_0, u1_1, u1_2; float dummy3;   /* second uv layer */
+    float v1_0, v1_1, v1_2; float dummy4;
+} lh2g_core_tri;
+
+typedef struct lh2g_light_tri {
+    float centre[3]; float energy;
+    float N[3]; float area;
+    float radiance[3]; int32_t dummy2;
+    float vertex0[3]; int32_t triIdx;
+    float vertex1[3]; int32_t instIdx;
+    float vertex2[3]; int32_t dummy1;
+} lh2g_light_tri;
+
+typedef struct lh2g_point_light {
+    float position[3]; float energy;
+    float radiance[3]; int32_t dummy;
+} lh2g_point_light;
+
+typedef struct lh2g_spot_light {
+    float position[3]; float cosInner;
+    float radiance[3]; float cosOuter;
+    float direction[3]; int32_t dummy;
+} lh2g_spot_light;
+
+typedef struct lh2g_dir_light {
+    float direction[3]; float energy;
+    float radiance[3]; int32_t dummy;
+} lh2g_dir_light;
+
+/* Camera: eye position and three corners of the screen plane (p1 top-left, p2 top-right, p3 bottom-left). */
+typedef struct lh2g_view {
+    float pos[3], p1[3], p2[3], p3[3];
+    float aperture, spreadAngle, imagePlane, focalDistance, distortion;
+} lh2g_view;
+
+/* Texture descriptor (host layout of CoreTexDesc). texels points at pixelCount ARGB32 words holding every
+ * MIP level back to back; firstPixel is filled in by the core. */
+typedef struct lh2g_texture {
+    const uint32_t* texels;
+    uint32_t width, height, flags, pixelCount, firstPixel, MIPlevels;
+    int32_t storage;                        /* 0 = ARGB32 (the only storage this core reads) */
+} lh2g_texture;
+
+/* Ray query formats. */
+typedef struct lh2g_ray { float ox, oy, oz, tmin, dx, dy, dz, tmax; } lh2g_ray;
+typedef struct lh2g_hit { uint32_t bary; int32_t inst; int32_t prim; float t; } lh2g_hit;
+
+/* Host-side material description: the value fields of CoreMaterial (common_classes.h:219-328) that the
+ * Lambert shading path reads, plus the texture slots it samples. Textures are indices into the array given
+ * to lh2g_set_textures (-1 = none). */
+typedef struct lh2g_map_ref { int32_t texture; float uvscale[2]; float uvoffset[2]; } lh2g_map_ref;
+typedef struct lh2g_material {
+    float color[3];                         /* base colour; any channel > 1 marks an emitter */
+    float absorption[3];                    /* transmittance = 1 - absorption */
+    float metallic, subsurface, specular, roughness;
+    float specularTint, anisotropic, sheen, sheenTint;
+    float clearcoat, clearcoatGloss, transmission, eta;
+    uint32_t flags;                         /* 1 = smooth normals, 2 = alpha tested */
+    lh2g_map_ref color_map, detail_color_map, normal_map, detail_normal_map, specular_map, roughness_map;
+} lh2g_material;
+
+/* Packed device material (128 bytes): half diffuse rgb + half transmittance rgb + flags, 16 8-bit
+ * parameters (eta as float bits in the last word), six 16-byte texture maps
+ * {short w, h; half uscale, vscale, uoffs, voffs; uint addr}. */
+typedef struct lh2g_gpu_material { uint32_t base[4]; uint32_t params[4]; uint32_t maps[6][4]; } lh2g_gpu_material;
+
+/* Material flag bits (core_settings.h:160-171 of the OptiX7 core). */
+#define LH2G_MAT_ISDIELECTRIC     (1u << 0)
+#define LH2G_MAT_DIFFUSEMAPISHDR  (1u << 1)
+#define LH2G_MAT_HASDIFFUSEMAP    (1u << 2)
+#define LH2G_MAT_HASNORMALMAP     (1u << 3)
+#define LH2G_MAT_HASSPECULARITYMAP (1u << 4)
+#define LH2G_MAT_HASROUGHNESSMAP  (1u << 5)
+#define LH2G_MAT_HAS2NDNORMALMAP  (1u << 7)
+#define LH2G_MAT_HAS2NDDIFFUSEMAP (1u << 9)
+#define LH2G_MAT_HASSMOOTHNORMALS (1u << 11)
+#define LH2G_MAT_HASALPHA         (1u << 12)
+
+/* Per-frame estimator parameters. The defaults reproduce the PrimeRef reference path tracer
+ * (lib/RenderCore_PrimeRef/kernels/pathtracer.h:45-168): uniform xorshift numbers, NEE without MIS,
+ * Russian roulette from the first bounce. */
+typedef struct lh2g_render_params {
+    int32_t width, height, spp;
+    int32_t maxDepth;                       /* MAXPATHLENGTH: paths stop after this many segments */
+    int32_t rrStartDepth;                   /* Russian roulette applies from this path length on (1 = always) */
+    int32_t samplesTaken;                   /* samples already accumulated (the 'pass' of the reference) */
+    uint32_t cameraR0;                      /* R0 of the primary-ray kernel (RandomUInt(camRNGseed)) */
+    float geometryEpsilon;                  /* ray offset / tmin, 'epsilon' setting (rendersystem.h:67) */
+    float clampValue;                       /* 'clampValue' setting (kept for the settings interface) */
+    int32_t flags;                          /* LH2G_RP_* */
+} lh2g_render_params;
+
+#define LH2G_RP_NEE        1                /* next-event estimation (connections buffer present) */
+#define LH2G_RP_DEPTH_W    2                /* add the primary hit distance to accumulator.w (DOF data) */
+
+/* Per-path, per-depth capture used by the parity tests: the hit record each path saw at each depth and
+ * its RNG state after shading. Entries of paths that were no longer alive carry prim = -2. */
+typedef struct lh2g_capture { lh2g_hit* hits; uint32_t* seeds; } lh2g_capture;
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LH2G_TYPES_H */

@@ -1,0 +1,269 @@
+"""ctypes bindings of the CPU oracle (oracle/lh2o.cpp) and of the reference-kernel harness (oracle/ref).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from lighthouse2_gb300 import scenes as S
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liblh2o.so")
+REF_LIB = os.path.join(HERE, "_ref", "libref.so")
+REFERENCE_TREE = os.environ.get("LH2_REFERENCE", "/root/reference")
+
+PARAMS_DTYPE = np.dtype([("width", "<i4"), ("height", "<i4"), ("spp", "<i4"), ("maxDepth", "<i4"),
+                         ("rrStartDepth", "<i4"), ("samplesTaken", "<i4"), ("cameraR0", "<u4"),
+                         ("geometryEpsilon", "<f4"), ("clampValue", "<f4"), ("flags", "<i4")])
+RP_NEE, RP_DEPTH_W = 1, 2
+
+
+def build_oracle():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB
+
+
+def build_ref():
+    """Compile the reference's own kernels for the host (only where the reference tree exists)."""
+    if not os.path.isdir(os.path.join(REFERENCE_TREE, "lib", "RenderCore_PrimeRef")):
+        return None
+    build_oracle()
+    subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), "REF=" + REFERENCE_TREE], check=True)
+    return REF_LIB
+
+
+def make_params(width, height, spp=1, max_depth=3, rr_start=1, samples_taken=0, camera_r0=0, eps=1e-3,
+                clamp=10.0, flags=RP_NEE):
+    p = np.zeros((), PARAMS_DTYPE)
+    p["width"], p["height"], p["spp"], p["maxDepth"] = width, height, spp, max_depth
+    p["rrStartDepth"], p["samplesTaken"], p["cameraR0"] = rr_start, samples_taken, camera_r0
+    p["geometryEpsilon"], p["clampValue"], p["flags"] = eps, clamp, flags
+    return p
+
+
+def camera_r0(frame_index_since_restart):
+    """R0 of the primary-ray kernel: RandomUInt(camRNGseed) with camRNGseed reset to 0x12345678 on Restart
+    (lib/RenderCore_PrimeRef/rendercore.cpp:548,556; lib/platform/system.cpp:50)."""
+    s = 0x12345678
+    for _ in range(frame_index_since_restart + 1):
+        s ^= (s << 13) & 0xFFFFFFFF
+        s ^= s >> 17
+        s ^= (s << 5) & 0xFFFFFFFF
+    return s
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+class _Capture(C.Structure):
+    _fields_ = [("hits", C.c_void_p), ("seeds", C.c_void_p)]
+
+
+class Oracle:
+    def __init__(self):
+        if not os.path.exists(LIB):
+            build_oracle()
+        self.lib = C.CDLL(LIB)
+        L = self.lib
+        L.lh2o_create.restype = C.c_void_p
+        L.lh2o_destroy.argtypes = [C.c_void_p]
+        L.lh2o_set_geometry.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+        L.lh2o_set_instance.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+        L.lh2o_set_materials.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+        L.lh2o_set_textures.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+        L.lh2o_set_lights.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int]
+        L.lh2o_set_sky.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+        L.lh2o_finalize.argtypes = [C.c_void_p]
+        L.lh2o_trace.argtypes = [C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int]
+        L.lh2o_render.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        self.s = L.lh2o_create()
+        self._keep = []
+
+    def __del__(self):
+        try:
+            self.lib.lh2o_destroy(self.s)
+        except Exception:
+            pass
+
+    def set_scene(self, sc: S.Scene):
+        L, s = self.lib, self.s
+        for i, m in enumerate(sc.meshes):
+            assert L.lh2o_set_geometry(s, i, _p(m.vertices), len(m.vertices), len(m.tris), _p(m.tris)) == 0
+        for i, (mi, T) in enumerate(sc.instances):
+            T = np.ascontiguousarray(T, np.float32)
+            assert L.lh2o_set_instance(s, i, mi, _p(T)) == 0
+        texdesc = texture_descs(sc.textures)
+        self._keep.append(texdesc)
+        assert L.lh2o_set_textures(s, _p(texdesc[0]) if len(sc.textures) else None, len(sc.textures)) == 0
+        assert L.lh2o_set_materials(s, _p(sc.materials), len(sc.materials)) == 0
+        assert L.lh2o_set_lights(s, _p(sc.tri_lights), len(sc.tri_lights), _p(sc.point_lights), len(sc.point_lights),
+                                 _p(sc.spot_lights), len(sc.spot_lights), _p(sc.dir_lights), len(sc.dir_lights)) == 0
+        if sc.sky is not None:
+            rgb, w, h = sc.sky
+            rgb = np.ascontiguousarray(rgb, np.float32)
+            assert L.lh2o_set_sky(s, _p(rgb), w, h, None) == 0
+        assert L.lh2o_finalize(s) == 0
+
+    def trace(self, rays, mode=0, brute=False, nthreads=0):
+        n = len(rays)
+        if mode == 0:
+            hits = np.zeros(n, S.HIT_DTYPE)
+            assert self.lib.lh2o_trace(self.s, _p(rays), n, 0, int(brute), _p(hits), None, nthreads) == 0
+            return hits
+        occ = np.zeros(n, np.uint32)
+        assert self.lib.lh2o_trace(self.s, _p(rays), n, 1, int(brute), None, _p(occ), nthreads) == 0
+        return occ
+
+    def render(self, view, params, accum=None, accum64=False, capture=False, nthreads=0):
+        W, H, spp, D = int(params["width"]), int(params["height"]), int(params["spp"]), int(params["maxDepth"])
+        if accum is None:
+            accum = np.zeros((H * W, 4), np.float32)
+        a64 = np.zeros((H * W, 4), np.float64) if accum64 else None
+        counters = np.zeros((D, 2), np.uint32)
+        cap = None
+        hits = seeds = None
+        if capture:
+            hits = np.zeros(D * W * H * spp, S.HIT_DTYPE)
+            seeds = np.zeros(D * W * H * spp, np.uint32)
+            cap = _Capture(hits.ctypes.data, seeds.ctypes.data)
+        rc = self.lib.lh2o_render(self.s, _p(view), _p(params), _p(accum), _p(a64), _p(counters),
+                                  C.byref(cap) if cap is not None else None, nthreads)
+        assert rc == 0
+        out = {"accum": accum, "counters": counters}
+        if accum64:
+            out["accum64"] = a64
+        if capture:
+            out["hits"] = hits.reshape(D, -1)
+            out["seeds"] = seeds.reshape(D, -1)
+        return out
+
+
+TEXDESC_DTYPE = np.dtype([("texels", "<u8"), ("width", "<u4"), ("height", "<u4"), ("flags", "<u4"),
+                          ("pixelCount", "<u4"), ("firstPixel", "<u4"), ("MIPlevels", "<u4"), ("storage", "<i4"),
+                          ("pad", "<i4")])
+assert TEXDESC_DTYPE.itemsize == 40
+
+
+def texture_descs(textures):
+    d = np.zeros(max(1, len(textures)), TEXDESC_DTYPE)
+    keep = []
+    for i, t in enumerate(textures):
+        arr = np.ascontiguousarray(t.texels, np.uint32)
+        keep.append(arr)
+        d[i]["texels"] = arr.ctypes.data
+        d[i]["width"], d[i]["height"] = t.width, t.height
+        d[i]["pixelCount"] = len(arr)
+        d[i]["MIPlevels"] = 5
+    return d, keep
+
+
+class RefKernels:
+    """The reference's PrimeRef kernels compiled for the host (oracle/ref), driven through its own wave loop
+    (lib/RenderCore_PrimeRef/rendercore.cpp:551-611) with the oracle answering the ray queries."""
+
+    def __init__(self):
+        if build_ref() is None:
+            raise FileNotFoundError("reference tree not available")
+        self.lib = C.CDLL(REF_LIB)
+        L = self.lib
+        L.ref_set_scene.argtypes = [C.c_void_p] * 2 + [C.c_void_p, C.c_int] * 4 + [C.c_void_p, C.c_float, C.c_int]
+        L.ref_generate.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_float, C.c_void_p, C.c_int, C.c_int, C.c_int]
+        L.ref_shade.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, C.c_int]
+        L.ref_finalize_connections.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.ref_next_counters.argtypes = [C.c_void_p]
+        L.ref_init_counters.argtypes = [C.c_int]
+        L.ref_wanghash.restype = C.c_uint32
+        L.ref_random_float.restype = C.c_float
+        L.ref_random_float.argtypes = [C.c_void_p]
+        L.ref_pack_normal.restype = C.c_uint32
+        L.ref_pack_normal.argtypes = [C.c_void_p]
+        L.ref_unpack_normal.argtypes = [C.c_uint32, C.c_void_p]
+        L.ref_random_barycentrics.argtypes = [C.c_float, C.c_void_p]
+        L.ref_diffuse_cos.argtypes = [C.c_float, C.c_float, C.c_void_p]
+        L.ref_tangent2world.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.ref_consistent_normal.argtypes = [C.c_void_p, C.c_void_p, C.c_float, C.c_void_p]
+        L.ref_invert4x4.argtypes = [C.c_void_p, C.c_void_p]
+
+    def render(self, oracle: Oracle, sc: S.Scene, view, params):
+        """One frame through the reference's kernels; returns per-pixel accumulator and per-depth counters.
+        Connections of the last wave are traced too (as the OptiX7 core's final shadow pass does,
+        lib/rendercore_optix7/rendercore.cpp:919-922); the PrimeRef loop leaves them untraced only because its
+        compile-time MAXPATHLENGTH of 64 is never reached."""
+        L = self.lib
+        W, H, spp, D = int(params["width"]), int(params["height"]), int(params["spp"]), int(params["maxDepth"])
+        eps = float(params["geometryEpsilon"])
+        nee = int(params["flags"]) & RP_NEE
+        inst = np.zeros((len(sc.instances), 20), np.float32)
+        keep = []
+        for i, (mi, T) in enumerate(sc.instances):
+            tris = sc.meshes[mi].tris
+            inv = np.zeros(16, np.float32)
+            L.ref_invert4x4(_p(np.ascontiguousarray(T, np.float32).reshape(-1)), _p(inv))
+            inst[i].view(np.uint64)[0] = tris.ctypes.data
+            inst[i, 4:] = inv
+        packed = pack_materials(oracle, sc)
+        texels = np.concatenate([t.texels for t in sc.textures]).astype(np.uint32) if sc.textures else np.zeros(16, np.uint32)
+        keep += [inst, packed, texels]
+        self._keep = keep
+        L.ref_set_scene(_p(inst), _p(packed), _p(sc.tri_lights), len(sc.tri_lights), _p(sc.point_lights), len(sc.point_lights),
+                        _p(sc.spot_lights), len(sc.spot_lights), _p(sc.dir_lights), len(sc.dir_lights), _p(texels), eps, D)
+        P = W * H * spp
+        rays = [np.zeros((P, 8), np.float32), np.zeros((P, 8), np.float32)]
+        ps = [np.zeros((2 * P, 4), np.float32), np.zeros((2 * P, 4), np.float32)]
+        conn = np.zeros((P, 8), np.float32)
+        pot = np.zeros((P, 4), np.float32)
+        acc = np.zeros((W * H, 4), np.float32)
+        v = view
+        right = (v["p2"] - v["p1"]).astype(np.float32)
+        up = (v["p3"] - v["p1"]).astype(np.float32)
+        L.ref_generate(_p(rays[0]), _p(ps[0]), int(params["cameraR0"]), int(params["samplesTaken"]), _p(v["pos"].copy()),
+                       _p(right), _p(up), float(v["aperture"]), _p(v["p1"].copy()), W, H, spp)
+        L.ref_init_counters(P)
+        count, cin = P, 0
+        counters = np.zeros((D, 2), np.uint32)
+        tt = np.zeros(P, np.float32); ii = np.zeros(P, np.int32); pp = np.zeros(P, np.int32)
+        uu = np.zeros(P, np.float32); vv = np.zeros(P, np.float32)
+        isect = np.zeros(P, np.dtype([("t", "<f4"), ("triid", "<i4"), ("instid", "<i4"), ("u", "<f4"), ("v", "<f4")]))
+        for pl in range(1, D + 1):
+            r = np.ascontiguousarray(rays[cin][:count])
+            oracle.lib.lh2o_trace_raw(oracle.s, _p(r), count, _p(tt), _p(ii), _p(pp), _p(uu), _p(vv), 0)
+            isect["t"][:count], isect["triid"][:count], isect["instid"][:count] = tt[:count], pp[:count], ii[:count]
+            isect["u"][:count], isect["v"][:count] = uu[:count], vv[:count]
+            R0 = (int(params["samplesTaken"]) * 7907 + pl * 91771) & 0xFFFFFFFF
+            L.ref_shade(count, _p(acc), _p(rays[cin]), _p(ps[cin]), _p(isect), _p(rays[1 - cin]), _p(ps[1 - cin]),
+                        _p(conn), _p(pot), R0, int(params["samplesTaken"]), pl, W, H, float(v["spreadAngle"]), nee)
+            c3 = np.zeros(3, np.uint32)
+            L.ref_next_counters(_p(c3))
+            counters[pl - 1] = c3[:2]
+            if c3[1] > 0:
+                occ = oracle.trace(np.ascontiguousarray(conn[:c3[1]]).view(S.RAY_DTYPE).reshape(-1), mode=1)
+                bits = np.zeros((c3[1] + 31) // 32, np.uint32)
+                idx = np.nonzero(occ)[0]
+                np.bitwise_or.at(bits, idx >> 5, (np.uint32(1) << (idx & 31).astype(np.uint32)))
+                L.ref_finalize_connections(int(c3[1]), _p(acc), _p(bits), _p(pot))
+            count, cin = int(c3[0]), 1 - cin
+            if count == 0:
+                break
+        return {"accum": acc, "counters": counters}
+
+
+def pack_materials(oracle: Oracle, sc: S.Scene):
+    first, wh, off = [], [], 0
+    for t in sc.textures:
+        first.append(off); wh += [t.width, t.height]; off += len(t.texels)
+    first = np.array(first or [0], np.uint32); wh = np.array(wh or [0, 0], np.uint32)
+    out = np.zeros((len(sc.materials), 32), np.uint32)
+    fn = oracle.lib.lh2o_pack_material
+    fn.argtypes = [C.c_void_p] * 4
+    for i in range(len(sc.materials)):
+        m = np.ascontiguousarray(sc.materials[i:i + 1])
+        fn(_p(m), _p(first), _p(wh), out[i].ctypes.data_as(C.c_void_p))
+    return out

@@ -1,0 +1,85 @@
+/* lh2o.h - CPU ORACLE of the GB300 wavefront render core.
+ *
+ * TEST INFRASTRUCTURE ONLY. This library is the checker that the CUDA path is compared against, and the
+ * timed CPU baseline of the benchmark. Nothing in the product links, loads or calls it; only tests/,
+ * __graft_entry__.smoke() and bench.py (its CPU-baseline leg and --impl reference arm) may.
+ *
+ * It restates, in plain C++ on the host, the reference's path for one frame:
+ *   - primary rays        lib/RenderCore_PrimeRef/kernels/camera.h:39-68
+ *   - shading             lib/RenderCore_PrimeRef/kernels/pathtracer.h:45-168 with the BSDF of
+ *                         lib/sharedBSDFs/lambert.h:32-125, lights of lib/CUDA/shared_kernel_code/lights_shared.h,
+ *                         materials of lib/CUDA/shared_kernel_code/material_shared.h:42-206
+ *   - shadow connections  lib/RenderCore_PrimeRef/kernels/connections.h:22-34
+ *   - the wave loop       lib/RenderCore_PrimeRef/rendercore.cpp:535-632, run per path depth-first, which is
+ *                         equivalent because every random number depends only on (path, depth).
+ * Ray traversal in the reference is closed NVIDIA code (OptiX / OptiX Prime), so the oracle brings its own
+ * scalar binned-SAH BVH2 and a brute-force intersector; both return the closest hit with ties broken by the
+ * lowest (instance, primitive).
+ */
+#ifndef LH2O_H
+#define LH2O_H
+
+#include "../include/lh2g_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct lh2o_scene lh2o_scene;
+
+lh2o_scene* lh2o_create(void);
+void lh2o_destroy(lh2o_scene* s);
+
+/* Scene setters: same meaning as the core's CoreAPI_Base setters (core_api_base.h:103-118). */
+int lh2o_set_geometry(lh2o_scene* s, int meshIdx, const float* vertices4, int vertexCount, int triangleCount,
+                      const lh2g_core_tri* tris);
+int lh2o_set_instance(lh2o_scene* s, int instIdx, int meshIdx, const float* transform16);
+int lh2o_set_materials(lh2o_scene* s, const lh2g_material* mats, int count);
+int lh2o_set_textures(lh2o_scene* s, const lh2g_texture* tex, int count);
+int lh2o_set_lights(lh2o_scene* s, const lh2g_light_tri* tri, int ntri, const lh2g_point_light* pt, int npt,
+                    const lh2g_spot_light* spot, int nspot, const lh2g_dir_light* dir, int ndir);
+int lh2o_set_sky(lh2o_scene* s, const float* rgb, int width, int height, const float* worldToSky16);
+/* Builds the BVHs (BVH2 per mesh + BVH2 over instances). Must follow the setters, precede tracing. */
+int lh2o_finalize(lh2o_scene* s);
+
+/* Ray queries. mode 0: closest hit into hits (prim = -1 on miss); mode 1: any hit, occluded[i] = 0/1.
+ * brute != 0 tests every triangle of every instance (the judge of the BVH). */
+int lh2o_trace(lh2o_scene* s, const lh2g_ray* rays, long long n, int mode, int brute, lh2g_hit* hits,
+               uint32_t* occluded, int nthreads);
+
+/* Closest hit with unquantised barycentrics (t, instance, primitive, u, v per ray; prim = -1 on a miss). */
+int lh2o_trace_raw(lh2o_scene* s, const lh2g_ray* rays, long long n, float* t, int* inst, int* prim, float* u, float* v,
+                   int nthreads);
+
+/* One frame of the path tracer. pixelAccum (W*H float4) receives += the sum over the frame's samples of each
+ * path's radiance (rgb; w = primary hit distance when LH2G_RP_DEPTH_W). pixelAccum64 (optional, W*H*4
+ * doubles) receives the same sums accumulated in FP64. counters (optional, 2*maxDepth) receive per path
+ * length the number of extension rays and shadow rays written. capture (optional) receives per-path,
+ * per-depth hits and RNG states (maxDepth * W*H*spp entries each). Returns 0 on success. */
+int lh2o_render(lh2o_scene* s, const lh2g_view* view, const lh2g_render_params* p, float* pixelAccum,
+                double* pixelAccum64, uint32_t* counters, lh2g_capture* capture, int nthreads);
+
+/* Small pure functions exported for the pinning tests against the reference's own headers. */
+uint32_t lh2o_wanghash(uint32_t s);
+float lh2o_random_float(uint32_t* seed);
+void lh2o_random_barycentrics(float r0, float* out3);
+uint32_t lh2o_pack_normal(const float* n3);
+void lh2o_unpack_normal(uint32_t p, float* out3);
+void lh2o_diffuse_cos(float r0, float r1, float* out3);
+void lh2o_tangent2world(const float* v3, const float* n3, float* out3);
+void lh2o_consistent_normal(const float* d3, const float* in3, float alpha, float* out3);
+void lh2o_sincos(float x, float* s, float* c);
+float lh2o_expf(float x);
+float lh2o_log2f(float x);
+float lh2o_atan2f(float y, float x);
+float lh2o_acosf(float x);
+uint16_t lh2o_float2half(float f);
+float lh2o_half2float(uint16_t h);
+void lh2o_pack_material(const lh2g_material* m, const uint32_t* texFirstPixel, const uint32_t* texWH,
+                        lh2g_gpu_material* out);
+void lh2o_invert4x4(const float* m16, float* out16);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
