@@ -1,0 +1,102 @@
+/* lh2g.h - C ABI of the GB300 wavefront render core (libRenderCore_GB300.so).
+ *
+ * A flat, allocation-owning C interface under the core's CoreAPI_Base plugin (lh2_core_api.h). Every entry
+ * point returns an int status (LH2G_OK on success) and never aborts the host; the message of the last failure
+ * is available from lh2g_last_error(). One context owns one CUDA stream on one device; calls on a context
+ * must come from one host thread at a time.
+ *
+ * Each entry point names the reference interface it replaces (lib/RenderSystem/core_api_base.h of
+ * Lighthouse 2, where the plugin API is a C++ vtable; the reference has no C ABI of its own).
+ */
+#ifndef LH2G_H
+#define LH2G_H
+
+#include "lh2g_types.h"
+
+#if defined(__GNUC__)
+#define LH2G_API __attribute__((visibility("default")))
+#else
+#define LH2G_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LH2G_OK 0
+#define LH2G_ERR_INVALID 1     /* bad argument or call order */
+#define LH2G_ERR_CUDA 2        /* a CUDA call failed */
+#define LH2G_ERR_OOM 3         /* device allocation failed */
+#define LH2G_ERR_STATE 4       /* scene not finalized / no target */
+#define LH2G_ERR_OVERFLOW 5    /* a device capacity was exceeded (traversal stack, node pool) */
+
+typedef struct lh2g_context lh2g_context;
+
+/* Per-frame statistics, the fields of CoreStats (core_api_base.h:30-64) this core fills. */
+typedef struct lh2g_stats {
+    uint32_t totalRays, totalExtensionRays, totalShadowRays, primaryRayCount, bounce1RayCount, deepRayCount;
+    float renderTime, traceTime0, traceTime1, traceTimeX, shadowTraceTime, shadeTime, filterTime, bvhBuildTime;
+    uint32_t SMcount, ccMajor, ccMinor, VRAM;
+    int32_t probedInstid, probedTriid;
+    float probedDist;
+    uint32_t deviceStatus;          /* LH2G_STATUS_* bits reported by the kernels */
+} lh2g_stats;
+
+/* Context: replaces CreateCore (lib/rendercore_optix7/core_api.cpp:18-22) + RenderCore::Init (rendercore.cpp:219-278). */
+LH2G_API int lh2g_create(int device, lh2g_context** out);
+/* RenderCore::Shutdown (rendercore.cpp:984-1003). */
+LH2G_API int lh2g_destroy(lh2g_context* ctx);
+LH2G_API const char* lh2g_last_error(lh2g_context* ctx);
+
+/* SetGeometry (core_api_base.h:114): 3 float4 vertices per triangle + CoreTri records; meshes in index order. */
+LH2G_API int lh2g_set_geometry(lh2g_context* ctx, int meshIdx, const float* vertices4, int vertexCount, int triangleCount, const lh2g_core_tri* tris);
+/* SetInstance (core_api_base.h:116): 4x4 row-major object-to-world transform; meshIdx -1 truncates the list. */
+LH2G_API int lh2g_set_instance(lh2g_context* ctx, int instIdx, int meshIdx, const float* transform16);
+/* FinalizeInstances (core_api_base.h:118): builds every dirty BLAS and the TLAS on the device. */
+LH2G_API int lh2g_finalize_instances(lh2g_context* ctx);
+/* SetMaterials (core_api_base.h:105); textures must be set first. */
+LH2G_API int lh2g_set_materials(lh2g_context* ctx, const lh2g_material* materials, int count);
+/* Packs materials into the 128-byte device format without a context (for inspection and tests). */
+LH2G_API int lh2g_pack_materials(const lh2g_material* materials, int count, const lh2g_texture* textures, int textureCount, lh2g_gpu_material* out);
+/* SetTextures (core_api_base.h:103): ARGB32 texels, MIP levels back to back. */
+LH2G_API int lh2g_set_textures(lh2g_context* ctx, const lh2g_texture* textures, int count);
+/* SetLights (core_api_base.h:107-110); at most 64 lights in total. */
+LH2G_API int lh2g_set_lights(lh2g_context* ctx, const lh2g_light_tri* tri, int ntri, const lh2g_point_light* point, int npoint,
+                    const lh2g_spot_light* spot, int nspot, const lh2g_dir_light* dir, int ndir);
+/* SetSkyData (core_api_base.h:112): width*height RGB floats; worldToSky16 may be NULL (identity). */
+LH2G_API int lh2g_set_sky(lh2g_context* ctx, const float* rgb, int width, int height, const float* worldToSky16);
+/* Setting (core_api_base.h:95): "epsilon", "clampValue", "maxDepth", "rrStartDepth", "nee". */
+LH2G_API int lh2g_setting(lh2g_context* ctx, const char* name, float value);
+/* SetTarget (core_api_base.h:93), headless: the output is a device float4 buffer of width*height pixels. */
+LH2G_API int lh2g_set_target(lh2g_context* ctx, int width, int height, int spp);
+/* SetProbePos (core_api_base.h:91). */
+LH2G_API int lh2g_set_probe(lh2g_context* ctx, int x, int y);
+/* Render (core_api_base.h:97): converge 0 = Converge (accumulate), 1 = Restart. */
+LH2G_API int lh2g_render(lh2g_context* ctx, const lh2g_view* view, int converge);
+/* Render one frame with explicit estimator parameters (used by the parity tests): accumulate != 0 adds to the
+ * accumulator, else it is cleared first. captureHits / captureSeeds (host, maxDepth * W*H*spp entries, may be
+ * NULL) receive per-path, per-depth hit records and RNG states; counters (host, 2 * maxDepth, may be NULL)
+ * receive per path length the extension and connection counts. */
+LH2G_API int lh2g_render_ex(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* params, int accumulate,
+                   lh2g_hit* captureHits, uint32_t* captureSeeds, uint32_t* counters);
+/* WaitForRender (core_api_base.h:99): blocks until the context's stream is idle. */
+LH2G_API int lh2g_wait(lh2g_context* ctx);
+/* GetCoreStats (core_api_base.h:87). */
+LH2G_API int lh2g_get_stats(lh2g_context* ctx, lh2g_stats* out);
+/* Headless output: device pointer of the W*H float4 frame (accumulator / samples), and host read-backs. */
+LH2G_API int lh2g_get_framebuffer(lh2g_context* ctx, void** devicePtr);
+LH2G_API int lh2g_read_framebuffer(lh2g_context* ctx, float* host);
+LH2G_API int lh2g_read_accumulator(lh2g_context* ctx, float* host);
+
+/* Ray queries over the scene (the OptiX Prime query interface of lib/RenderCore_PrimeRef/rendercore.cpp:569-605,
+ * formats RTP_BUFFER_FORMAT_RAY_ORIGIN_TMIN_DIRECTION_TMAX / hit float4 {u|v<<16, inst, prim, t}).
+ * mode 0: closest hit into lh2g_hit[n] (prim = -1 on a miss); mode 1: any hit into uint32 occluded[n].
+ * lh2g_trace takes device pointers and a CUDA stream (NULL = the context's stream) and returns without waiting;
+ * lh2g_trace_host takes host buffers and returns when the results are back on the host. */
+LH2G_API int lh2g_trace(lh2g_context* ctx, const lh2g_ray* rays, void* out, long long n, int mode, void* stream);
+LH2G_API int lh2g_trace_host(lh2g_context* ctx, const lh2g_ray* rays, void* out, long long n, int mode);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

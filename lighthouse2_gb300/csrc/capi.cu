@@ -1,0 +1,700 @@
+/* capi.cu - host side of the GB300 render core: context, scene upload, device BVH finalisation, frame
+ * orchestration and ray queries behind the C ABI of include/lh2g.h.
+ *
+ * Host-side semantics follow the reference core:
+ *   scene setters        lib/RenderCore_PrimeRef/rendercore.cpp:214-478 (meshes appended in index order,
+ *                        SetInstance(n, -1) truncates, textures before materials, lights <= 64)
+ *   material packing     rendercore.cpp:360-402 (half colours, 8-bit parameters, 16-byte texture maps)
+ *   instance inverse     mat4::Inverted, lib/RenderSystem/common_types.h:559-604
+ *   Render               rendercore.cpp:535-632 (Restart resets the accumulator, samplesTaken and the camera
+ *                        seed 0x12345678; R0 = RandomUInt(camRNGseed); shading R0 = samplesTaken * 7907 +
+ *                        pathLength * 91771; output = accumulator / samplesTaken)
+ * No stage of a frame waits for the host: queue sizes stay on the device.
+ */
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "bvh_build.cuh"
+#include "kernels.cuh"
+#include "lh2g.h"
+
+using namespace lh2g;
+
+namespace {
+
+struct MeshDev {
+    float4* verts = nullptr;   /* 3 per triangle */
+    float4* tris = nullptr;    /* CoreTri4, 13 float4 per triangle */
+    uint32_t n = 0;
+    float bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0};
+};
+
+struct InstHost { int mesh; float T[16]; float inv[16]; };
+
+uint16_t f2h(float f) {   /* round-to-nearest-even float -> half */
+    uint32_t x;
+    memcpy(&x, &f, 4);
+    const uint32_t sign = (x >> 16) & 0x8000u, ax = x & 0x7fffffffu;
+    if (ax >= 0x7f800000u) return (uint16_t)(sign | 0x7c00u | (ax > 0x7f800000u ? 0x200u : 0u));
+    if (ax >= 0x477ff000u) return (uint16_t)(sign | 0x7c00u);
+    if (ax < 0x38800000u) {
+        const uint32_t e = ax >> 23;
+        if (e < 102) return (uint16_t)sign;
+        const uint32_t m = (ax & 0x7fffffu) | 0x800000u, shift = 126 - e;
+        uint32_t h = m >> shift;
+        const uint32_t rem = m & ((1u << shift) - 1u), half = 1u << (shift - 1u);
+        if (rem > half || (rem == half && (h & 1u))) h++;
+        return (uint16_t)(sign | h);
+    }
+    uint32_t h = (ax >> 13) - (112u << 10);
+    const uint32_t rem = ax & 0x1fffu;
+    if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) h++;
+    return (uint16_t)(sign | h);
+}
+
+uint32_t f2u_sat(float x) { if (!(x > 0.0f)) return 0u; if (x >= 4294967296.0f) return 0xffffffffu; return (uint32_t)x; }
+uint32_t tochar(float a) { return f2u_sat(a * 255.0f); }
+uint32_t touint4(float a, float b, float c, float d) { return tochar(a) + (tochar(b) << 8) + (tochar(c) << 16) + (tochar(d) << 24); }
+uint32_t fbits(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
+
+void pack_material(const lh2g_material& m, const std::vector<uint32_t>& first, const std::vector<uint32_t>& wh, lh2g_gpu_material& g) {
+    memset(&g, 0, sizeof(g));
+    g.base[0] = (uint32_t)f2h(m.color[0]) | ((uint32_t)f2h(m.color[1]) << 16);
+    g.base[1] = (uint32_t)f2h(m.color[2]) | ((uint32_t)f2h(1 - m.absorption[0]) << 16);
+    g.base[2] = (uint32_t)f2h(1 - m.absorption[1]) | ((uint32_t)f2h(1 - m.absorption[2]) << 16);
+    g.params[0] = touint4(m.metallic, m.subsurface, m.specular, m.roughness);
+    g.params[1] = touint4(m.specularTint, m.anisotropic, m.sheen, m.sheenTint);
+    g.params[2] = touint4(m.clearcoat, m.clearcoatGloss, m.transmission, 0);
+    g.params[3] = fbits(m.eta);
+    const lh2g_map_ref* refs[6] = {&m.color_map, &m.detail_color_map, &m.normal_map, &m.detail_normal_map, &m.specular_map, &m.roughness_map};
+    for (int i = 0; i < 6; i++) {
+        const lh2g_map_ref& r = *refs[i];
+        if (r.texture < 0) continue;
+        g.maps[i][0] = (wh[2 * r.texture] & 0xffffu) | ((wh[2 * r.texture + 1] & 0xffffu) << 16);
+        g.maps[i][1] = (uint32_t)f2h(r.uvscale[0]) | ((uint32_t)f2h(r.uvscale[1]) << 16);
+        g.maps[i][2] = (uint32_t)f2h(r.uvoffset[0]) | ((uint32_t)f2h(r.uvoffset[1]) << 16);
+        g.maps[i][3] = first[r.texture];
+    }
+    uint32_t flags = m.eta < 1 ? 1u : 0u;
+    flags += m.color_map.texture >= 0 ? LH2G_MAT_HASDIFFUSEMAP : 0u;
+    flags += m.normal_map.texture >= 0 ? LH2G_MAT_HASNORMALMAP : 0u;
+    flags += m.specular_map.texture >= 0 ? LH2G_MAT_HASSPECULARITYMAP : 0u;
+    flags += m.roughness_map.texture >= 0 ? LH2G_MAT_HASROUGHNESSMAP : 0u;
+    flags += m.detail_normal_map.texture >= 0 ? LH2G_MAT_HAS2NDNORMALMAP : 0u;
+    flags += m.detail_color_map.texture >= 0 ? LH2G_MAT_HAS2NDDIFFUSEMAP : 0u;
+    flags += (m.flags & 1) ? LH2G_MAT_HASSMOOTHNORMALS : 0u;
+    flags += (m.flags & 2) ? LH2G_MAT_HASALPHA : 0u;
+    g.base[3] = flags;
+}
+
+/* mat4::Inverted, cofactor expansion (common_types.h:559-604). */
+void invert4x4(const float* cell, float* out) {
+    const float inv[16] = {
+        cell[5] * cell[10] * cell[15] - cell[5] * cell[11] * cell[14] - cell[9] * cell[6] * cell[15] + cell[9] * cell[7] * cell[14] + cell[13] * cell[6] * cell[11] - cell[13] * cell[7] * cell[10],
+        -cell[1] * cell[10] * cell[15] + cell[1] * cell[11] * cell[14] + cell[9] * cell[2] * cell[15] - cell[9] * cell[3] * cell[14] - cell[13] * cell[2] * cell[11] + cell[13] * cell[3] * cell[10],
+        cell[1] * cell[6] * cell[15] - cell[1] * cell[7] * cell[14] - cell[5] * cell[2] * cell[15] + cell[5] * cell[3] * cell[14] + cell[13] * cell[2] * cell[7] - cell[13] * cell[3] * cell[6],
+        -cell[1] * cell[6] * cell[11] + cell[1] * cell[7] * cell[10] + cell[5] * cell[2] * cell[11] - cell[5] * cell[3] * cell[10] - cell[9] * cell[2] * cell[7] + cell[9] * cell[3] * cell[6],
+        -cell[4] * cell[10] * cell[15] + cell[4] * cell[11] * cell[14] + cell[8] * cell[6] * cell[15] - cell[8] * cell[7] * cell[14] - cell[12] * cell[6] * cell[11] + cell[12] * cell[7] * cell[10],
+        cell[0] * cell[10] * cell[15] - cell[0] * cell[11] * cell[14] - cell[8] * cell[2] * cell[15] + cell[8] * cell[3] * cell[14] + cell[12] * cell[2] * cell[11] - cell[12] * cell[3] * cell[10],
+        -cell[0] * cell[6] * cell[15] + cell[0] * cell[7] * cell[14] + cell[4] * cell[2] * cell[15] - cell[4] * cell[3] * cell[14] - cell[12] * cell[2] * cell[7] + cell[12] * cell[3] * cell[6],
+        cell[0] * cell[6] * cell[11] - cell[0] * cell[7] * cell[10] - cell[4] * cell[2] * cell[11] + cell[4] * cell[3] * cell[10] + cell[8] * cell[2] * cell[7] - cell[8] * cell[3] * cell[6],
+        cell[4] * cell[9] * cell[15] - cell[4] * cell[11] * cell[13] - cell[8] * cell[5] * cell[15] + cell[8] * cell[7] * cell[13] + cell[12] * cell[5] * cell[11] - cell[12] * cell[7] * cell[9],
+        -cell[0] * cell[9] * cell[15] + cell[0] * cell[11] * cell[13] + cell[8] * cell[1] * cell[15] - cell[8] * cell[3] * cell[13] - cell[12] * cell[1] * cell[11] + cell[12] * cell[3] * cell[9],
+        cell[0] * cell[5] * cell[15] - cell[0] * cell[7] * cell[13] - cell[4] * cell[1] * cell[15] + cell[4] * cell[3] * cell[13] + cell[12] * cell[1] * cell[7] - cell[12] * cell[3] * cell[5],
+        -cell[0] * cell[5] * cell[11] + cell[0] * cell[7] * cell[9] + cell[4] * cell[1] * cell[11] - cell[4] * cell[3] * cell[9] - cell[8] * cell[1] * cell[7] + cell[8] * cell[3] * cell[5],
+        -cell[4] * cell[9] * cell[14] + cell[4] * cell[10] * cell[13] + cell[8] * cell[5] * cell[14] - cell[8] * cell[6] * cell[13] - cell[12] * cell[5] * cell[10] + cell[12] * cell[6] * cell[9],
+        cell[0] * cell[9] * cell[14] - cell[0] * cell[10] * cell[13] - cell[8] * cell[1] * cell[14] + cell[8] * cell[2] * cell[13] + cell[12] * cell[1] * cell[10] - cell[12] * cell[2] * cell[9],
+        -cell[0] * cell[5] * cell[14] + cell[0] * cell[6] * cell[13] + cell[4] * cell[1] * cell[14] - cell[4] * cell[2] * cell[13] - cell[12] * cell[1] * cell[6] + cell[12] * cell[2] * cell[5],
+        cell[0] * cell[5] * cell[10] - cell[0] * cell[6] * cell[9] - cell[4] * cell[1] * cell[10] + cell[4] * cell[2] * cell[9] + cell[8] * cell[1] * cell[6] - cell[8] * cell[2] * cell[5]};
+    const float det = cell[0] * inv[0] + cell[1] * inv[4] + cell[2] * inv[8] + cell[3] * inv[12];
+    for (int i = 0; i < 16; i++) out[i] = (i % 5 == 0) ? 1.0f : 0.0f;
+    if (det != 0) {
+        const float invdet = 1.0f / det;
+        for (int i = 0; i < 16; i++) out[i] = inv[i] * invdet;
+    }
+}
+
+uint32_t xorshift(uint32_t& s) { s ^= s << 13; s ^= s >> 17; s ^= s << 5; return s; }
+
+}  // namespace
+
+struct lh2g_context {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    std::string err;
+    std::vector<MeshDev> meshes;
+    std::vector<InstHost> inst;
+    std::vector<lh2g_material> hostMats;
+    uint4* mats = nullptr;
+    uint32_t* texels = nullptr;
+    std::vector<uint32_t> texFirst, texWH;
+    float4 *triL = nullptr, *ptL = nullptr, *spL = nullptr, *dirL = nullptr;
+    int nTri = 0, nPt = 0, nSpot = 0, nDir = 0;
+    float4* sky = nullptr;
+    int skyW = 0, skyH = 0;
+    float w2s[16];
+    /* acceleration structure */
+    uint4* pool = nullptr;
+    float4* triData = nullptr;
+    InstanceGPU* instGPU = nullptr;
+    uint32_t* tlasPrims = nullptr;
+    uint32_t tlasRoot = 0xffffffffu;
+    const float4** instTris = nullptr;
+    float4* instInvRows = nullptr;
+    bool finalized = false;
+    /* target */
+    int W = 0, H = 0, spp = 1;
+    int64_t cap = 0;
+    WaveBuffers B;
+    /* settings and accumulation state (RenderCore_PrimeRef/rendercore.cpp:535-550) */
+    float eps = 1e-3f, clampValue = 10.0f;
+    int maxDepth = 3, rrStart = 1, nee = 1;
+    int samplesTaken = 0;
+    uint32_t camSeed = 0x12345678u;
+    bool firstConverging = true;
+    int probeX = -1, probeY = -1;
+    lh2g_stats stats;
+    Counters* hostCounters = nullptr;   /* pinned copy of the frame's counters */
+    int lastDepth = 0;
+    int64_t lastP = 0;
+    bool statsPending = false;
+    uint32_t* traceFetch = nullptr;     /* 64-bit fetch counter + status word */
+    lh2g_ray* hostRaysDev = nullptr;
+    void* hostOutDev = nullptr;
+    long long hostCap = 0;
+    cudaEvent_t ev[2];
+    int blocksExtend = 0, blocksConnect = 0, blocksShade = 0;
+};
+
+namespace {
+
+int fail(lh2g_context* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+int cuda_check(lh2g_context* c, cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return LH2G_OK;
+    return fail(c, e == cudaErrorMemoryAllocation ? LH2G_ERR_OOM : LH2G_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                                      \
+    do {                                                              \
+        const int _r = cuda_check(ctx, (call), #call);                \
+        if (_r != LH2G_OK) return _r;                                 \
+    } while (0)
+
+template <typename T>
+void dfree(T*& p) { if (p) cudaFree((void*)p); p = nullptr; }
+
+template <typename T>
+cudaError_t dalloc(T*& p, size_t count) {
+    dfree(p);
+    return cudaMalloc((void**)&p, std::max<size_t>(1, count) * sizeof(T));
+}
+
+void free_target(lh2g_context* ctx) {
+    WaveBuffers& B = ctx->B;
+    for (int k = 0; k < 2; k++) dfree(B.O[k]), dfree(B.D[k]), dfree(B.T[k]);
+    dfree(B.hits), dfree(B.shO), dfree(B.shD), dfree(B.shE), dfree(B.pathAcc), dfree(B.accum), dfree(B.frame), dfree(B.counters);
+    ctx->cap = 0;
+}
+
+SceneGPU scene_of(const lh2g_context* c) {
+    SceneGPU S;
+    memset(&S, 0, sizeof(S));
+    S.nodes = c->pool, S.triData = c->triData, S.inst = c->instGPU, S.tlasPrims = c->tlasPrims, S.tlasRoot = c->tlasRoot;
+    S.instCount = (int)c->inst.size();
+    S.instTris = c->instTris, S.instInvRows = c->instInvRows;
+    S.materials = c->mats, S.texels = c->texels;
+    S.nMaterials = (int)std::max<size_t>(c->hostMats.size(), 1);
+    S.triLights = c->triL, S.pointLights = c->ptL, S.spotLights = c->spL, S.dirLights = c->dirL;
+    S.nTri = c->nTri, S.nPoint = c->nPt, S.nSpot = c->nSpot, S.nDir = c->nDir;
+    S.skyPixels = c->sky, S.skyW = c->skyW, S.skyH = c->skyH;
+    for (int r = 0; r < 3; r++) S.worldToSky[r] = make_float4(c->w2s[4 * r], c->w2s[4 * r + 1], c->w2s[4 * r + 2], c->w2s[4 * r + 3]);
+    return S;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lh2g_create(int device, lh2g_context** out) {
+    if (!out) return LH2G_ERR_INVALID;
+    *out = nullptr;
+    lh2g_context* ctx = new lh2g_context();
+    memset(&ctx->B, 0, sizeof(ctx->B));
+    memset(&ctx->stats, 0, sizeof(ctx->stats));
+    for (int i = 0; i < 16; i++) ctx->w2s[i] = (i % 5 == 0) ? 1.0f : 0.0f;
+    ctx->device = device;
+    int r = cuda_check(ctx, cudaSetDevice(device), "cudaSetDevice");
+    if (r == LH2G_OK) r = cuda_check(ctx, cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking), "cudaStreamCreate");
+    if (r == LH2G_OK) r = cuda_check(ctx, cudaMallocHost((void**)&ctx->hostCounters, sizeof(Counters)), "cudaMallocHost");
+    if (r == LH2G_OK) r = cuda_check(ctx, cudaMalloc((void**)&ctx->traceFetch, 16), "cudaMalloc");
+    if (r == LH2G_OK) r = cuda_check(ctx, cudaEventCreate(&ctx->ev[0]), "cudaEventCreate");
+    if (r == LH2G_OK) r = cuda_check(ctx, cudaEventCreate(&ctx->ev[1]), "cudaEventCreate");
+    if (r != LH2G_OK) {
+        fprintf(stderr, "lh2g_create: %s\n", ctx->err.c_str());
+        delete ctx;
+        return r;
+    }
+    cudaDeviceProp prop;
+    cudaGetDeviceProperties(&prop, device);
+    ctx->stats.SMcount = (uint32_t)prop.multiProcessorCount;
+    ctx->stats.ccMajor = (uint32_t)prop.major, ctx->stats.ccMinor = (uint32_t)prop.minor;
+    ctx->stats.VRAM = (uint32_t)(prop.totalGlobalMem >> 20);
+    ctx->stats.probedTriid = -1;
+    ctx->blocksExtend = persistent_blocks_wave(0);
+    ctx->blocksConnect = persistent_blocks_wave(1);
+    ctx->blocksShade = persistent_blocks_wave(2);
+    *out = ctx;
+    return LH2G_OK;
+}
+
+int lh2g_destroy(lh2g_context* ctx) {
+    if (!ctx) return LH2G_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->st);
+    for (MeshDev& m : ctx->meshes) dfree(m.verts), dfree(m.tris);
+    dfree(ctx->mats), dfree(ctx->texels), dfree(ctx->triL), dfree(ctx->ptL), dfree(ctx->spL), dfree(ctx->dirL), dfree(ctx->sky);
+    dfree(ctx->pool), dfree(ctx->triData), dfree(ctx->instGPU), dfree(ctx->tlasPrims), dfree(ctx->instTris), dfree(ctx->instInvRows);
+    dfree(ctx->traceFetch), dfree(ctx->hostRaysDev), dfree(ctx->hostOutDev);
+    dfree(ctx->B.capHits), dfree(ctx->B.capSeeds);
+    free_target(ctx);
+    if (ctx->hostCounters) cudaFreeHost(ctx->hostCounters);
+    cudaEventDestroy(ctx->ev[0]), cudaEventDestroy(ctx->ev[1]);
+    cudaStreamDestroy(ctx->st);
+    delete ctx;
+    return LH2G_OK;
+}
+
+const char* lh2g_last_error(lh2g_context* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int lh2g_set_geometry(lh2g_context* ctx, int meshIdx, const float* v4, int vertexCount, int triangleCount, const lh2g_core_tri* tris) {
+    if (!ctx) return LH2G_ERR_INVALID;
+    if (meshIdx < 0 || meshIdx > (int)ctx->meshes.size() || triangleCount < 0 || vertexCount != 3 * triangleCount || (triangleCount && (!v4 || !tris)))
+        return fail(ctx, LH2G_ERR_INVALID, "set_geometry: meshes must arrive in index order with 3 vertices per triangle");
+    if (triangleCount >= (1 << 28)) return fail(ctx, LH2G_ERR_INVALID, "set_geometry: at most 2^28 triangles per mesh");
+    cudaSetDevice(ctx->device);
+    if (meshIdx == (int)ctx->meshes.size()) ctx->meshes.emplace_back();
+    MeshDev& m = ctx->meshes[meshIdx];
+    m.n = (uint32_t)triangleCount;
+    CK(dalloc(m.verts, (size_t)3 * triangleCount));
+    CK(dalloc(m.tris, (size_t)13 * triangleCount));
+    CK(cudaMemcpyAsync(m.verts, v4, sizeof(float4) * 3 * (size_t)triangleCount, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(m.tris, tris, sizeof(lh2g_core_tri) * (size_t)triangleCount, cudaMemcpyHostToDevice, ctx->st));
+    for (int k = 0; k < 3; k++) m.bmin[k] = 1e30f, m.bmax[k] = -1e30f;
+    for (size_t i = 0; i < (size_t)vertexCount; i++)
+        for (int k = 0; k < 3; k++) m.bmin[k] = std::min(m.bmin[k], v4[4 * i + k]), m.bmax[k] = std::max(m.bmax[k], v4[4 * i + k]);
+    CK(cudaStreamSynchronize(ctx->st));   /* the caller may free its arrays on return */
+    ctx->finalized = false;
+    return LH2G_OK;
+}
+
+int lh2g_set_instance(lh2g_context* ctx, int instIdx, int meshIdx, const float* T) {
+    if (!ctx || instIdx < 0) return LH2G_ERR_INVALID;
+    if (meshIdx == -1) {
+        if ((int)ctx->inst.size() > instIdx) ctx->inst.resize(instIdx);
+        ctx->finalized = false;
+        return LH2G_OK;
+    }
+    if (instIdx > (int)ctx->inst.size() || meshIdx < 0 || !T) return fail(ctx, LH2G_ERR_INVALID, "set_instance: instances must arrive in index order");
+    if (instIdx == (int)ctx->inst.size()) ctx->inst.emplace_back();
+    InstHost& in = ctx->inst[instIdx];
+    in.mesh = meshIdx;
+    memcpy(in.T, T, 64);
+    invert4x4(T, in.inv);
+    ctx->finalized = false;
+    return LH2G_OK;
+}
+
+int lh2g_finalize_instances(lh2g_context* ctx) {
+    if (!ctx) return LH2G_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    for (const InstHost& in : ctx->inst)
+        if (in.mesh >= (int)ctx->meshes.size()) return fail(ctx, LH2G_ERR_INVALID, "finalize: instance of a mesh that was never set");
+    const auto t0 = std::chrono::high_resolution_clock::now();
+    const uint32_t M = (uint32_t)ctx->meshes.size(), I = (uint32_t)ctx->inst.size();
+    std::vector<uint32_t> segStart(M + 1, 0);
+    for (uint32_t m = 0; m < M; m++) segStart[m + 1] = segStart[m] + ctx->meshes[m].n;
+    const uint32_t N = segStart[M];
+    float4 *triIn = nullptr, *lo = nullptr, *hi = nullptr;
+    uint32_t *segOf = nullptr, *leafPrim = nullptr;
+    auto cleanup = [&]() { dfree(triIn), dfree(lo), dfree(hi), dfree(segOf), dfree(leafPrim); };
+    if (dalloc(triIn, (size_t)3 * N) || dalloc(lo, std::max(N, I)) || dalloc(hi, std::max(N, I)) || dalloc(segOf, std::max(N, I)) ||
+        dalloc(leafPrim, std::max(N, I))) {
+        cleanup();
+        return fail(ctx, LH2G_ERR_OOM, "finalize: out of device memory for the BVH build");
+    }
+    for (uint32_t m = 0; m < M; m++)
+        launch_tri_prep(ctx->meshes[m].verts, ctx->meshes[m].n, m, triIn + 3 * (size_t)segStart[m], lo + segStart[m], hi + segStart[m],
+                        segOf + segStart[m], ctx->st);
+    const uint32_t cap = N + M + 2 * (I + 1) + 64;
+    if (dalloc(ctx->pool, (size_t)5 * cap) || dalloc(ctx->triData, (size_t)3 * std::max(N, 1u))) {
+        cleanup();
+        return fail(ctx, LH2G_ERR_OOM, "finalize: out of device memory for the node pool");
+    }
+    std::vector<uint32_t> meshRoot(M);
+    uint32_t used = 0, slots = 0;
+    int r = build_bvh8(lo, hi, segOf, N, segStart, ctx->pool, 0, cap, leafPrim, 3, meshRoot.data(), &used, &slots, ctx->st);
+    if (r != 0) { cleanup(); return fail(ctx, r == 3 ? LH2G_ERR_OOM : (r == 5 ? LH2G_ERR_OVERFLOW : LH2G_ERR_CUDA), "finalize: BLAS build failed"); }
+    launch_gather_tris(triIn, leafPrim, N, ctx->triData, ctx->st);
+    /* TLAS over instance world boxes (8 transformed corners of the mesh box, widened) */
+    std::vector<float4> ilo(std::max(I, 1u)), ihi(std::max(I, 1u));
+    std::vector<uint32_t> iseg(std::max(I, 1u), 0);
+    for (uint32_t i = 0; i < I; i++) {
+        const InstHost& in = ctx->inst[i];
+        const MeshDev& m = ctx->meshes[in.mesh];
+        float mn[3] = {1e30f, 1e30f, 1e30f}, mx[3] = {-1e30f, -1e30f, -1e30f};
+        for (int c = 0; c < 8; c++) {
+            const float p[3] = {(c & 1) ? m.bmax[0] : m.bmin[0], (c & 2) ? m.bmax[1] : m.bmin[1], (c & 4) ? m.bmax[2] : m.bmin[2]};
+            for (int k = 0; k < 3; k++) {
+                const float w = in.T[4 * k] * p[0] + in.T[4 * k + 1] * p[1] + in.T[4 * k + 2] * p[2] + in.T[4 * k + 3];
+                mn[k] = std::min(mn[k], w), mx[k] = std::max(mx[k], w);
+            }
+        }
+        for (int k = 0; k < 3; k++) {
+            const float pad = (mx[k] - mn[k]) * 1e-5f + (fabsf(mn[k]) + fabsf(mx[k])) * 1e-6f + 1e-30f;
+            mn[k] -= pad, mx[k] += pad;
+        }
+        ilo[i] = make_float4(mn[0], mn[1], mn[2], 0), ihi[i] = make_float4(mx[0], mx[1], mx[2], 0);
+    }
+    std::vector<InstanceGPU> ig(std::max(I, 1u));
+    std::vector<const float4*> itris(std::max(I, 1u), nullptr);
+    std::vector<float4> irows(3 * std::max(I, 1u));
+    for (uint32_t i = 0; i < I; i++) {
+        const InstHost& in = ctx->inst[i];
+        memset(&ig[i], 0, sizeof(InstanceGPU));
+        memcpy(ig[i].inv, in.inv, 48);
+        ig[i].blasRoot = meshRoot[in.mesh];
+        ig[i].mesh = (uint32_t)in.mesh;
+        itris[i] = ctx->meshes[in.mesh].tris;
+        for (int k = 0; k < 3; k++) irows[3 * i + k] = make_float4(in.inv[4 * k], in.inv[4 * k + 1], in.inv[4 * k + 2], in.inv[4 * k + 3]);
+    }
+    if (dalloc(ctx->instGPU, std::max(I, 1u)) || dalloc(ctx->instTris, std::max(I, 1u)) || dalloc(ctx->instInvRows, 3 * (size_t)std::max(I, 1u)) ||
+        dalloc(ctx->tlasPrims, std::max(I, 1u))) {
+        cleanup();
+        return fail(ctx, LH2G_ERR_OOM, "finalize: out of device memory for instances");
+    }
+    CK(cudaMemcpyAsync(ctx->instGPU, ig.data(), sizeof(InstanceGPU) * ig.size(), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync((void*)ctx->instTris, itris.data(), sizeof(void*) * itris.size(), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->instInvRows, irows.data(), sizeof(float4) * irows.size(), cudaMemcpyHostToDevice, ctx->st));
+    ctx->tlasRoot = 0xffffffffu;
+    if (I > 0) {
+        CK(cudaMemcpyAsync(lo, ilo.data(), sizeof(float4) * I, cudaMemcpyHostToDevice, ctx->st));
+        CK(cudaMemcpyAsync(hi, ihi.data(), sizeof(float4) * I, cudaMemcpyHostToDevice, ctx->st));
+        CK(cudaMemcpyAsync(segOf, iseg.data(), sizeof(uint32_t) * I, cudaMemcpyHostToDevice, ctx->st));
+        std::vector<uint32_t> tseg = {0, I};
+        uint32_t troot = 0, tused = 0, tslots = 0;
+        r = build_bvh8(lo, hi, segOf, I, tseg, ctx->pool, used, cap, ctx->tlasPrims, 1, &troot, &tused, &tslots, ctx->st);
+        if (r != 0) { cleanup(); return fail(ctx, LH2G_ERR_CUDA, "finalize: TLAS build failed"); }
+        ctx->tlasRoot = troot;
+    }
+    CK(cudaStreamSynchronize(ctx->st));
+    cleanup();
+    ctx->finalized = true;
+    ctx->stats.bvhBuildTime = std::chrono::duration<float, std::milli>(std::chrono::high_resolution_clock::now() - t0).count();
+    return LH2G_OK;
+}
+
+int lh2g_pack_materials(const lh2g_material* mats, int count, const lh2g_texture* tex, int ntex, lh2g_gpu_material* out) {
+    if (count < 0 || ntex < 0 || (count && (!mats || !out))) return LH2G_ERR_INVALID;
+    std::vector<uint32_t> first, wh;
+    uint32_t off = 0;
+    for (int i = 0; i < ntex; i++) first.push_back(off), wh.push_back(tex[i].width), wh.push_back(tex[i].height), off += tex[i].pixelCount;
+    for (int i = 0; i < count; i++) {
+        const lh2g_map_ref* refs[6] = {&mats[i].color_map, &mats[i].detail_color_map, &mats[i].normal_map, &mats[i].detail_normal_map, &mats[i].specular_map, &mats[i].roughness_map};
+        for (const lh2g_map_ref* r : refs) if (r->texture >= ntex) return LH2G_ERR_INVALID;
+        pack_material(mats[i], first, wh, out[i]);
+    }
+    return LH2G_OK;
+}
+
+int lh2g_set_textures(lh2g_context* ctx, const lh2g_texture* tex, int count) {
+    if (!ctx || count < 0 || (count && !tex)) return LH2G_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    ctx->texFirst.clear(), ctx->texWH.clear();
+    size_t total = 0, slack = 64;
+    for (int i = 0; i < count; i++) {
+        slack = std::max(slack, (size_t)tex[i].width * tex[i].height + 64);   /* MIP reads past a short chain stay in bounds */
+        if (tex[i].storage != 0) return fail(ctx, LH2G_ERR_INVALID, "set_textures: only ARGB32 storage is supported");
+        ctx->texFirst.push_back((uint32_t)total), ctx->texWH.push_back(tex[i].width), ctx->texWH.push_back(tex[i].height);
+        total += tex[i].pixelCount;
+    }
+    CK(dalloc(ctx->texels, total + slack));
+    CK(cudaMemsetAsync(ctx->texels, 0, sizeof(uint32_t) * (total + slack), ctx->st));
+    for (int i = 0; i < count; i++)
+        CK(cudaMemcpyAsync(ctx->texels + ctx->texFirst[i], tex[i].texels, sizeof(uint32_t) * tex[i].pixelCount, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return LH2G_OK;
+}
+
+int lh2g_set_materials(lh2g_context* ctx, const lh2g_material* mats, int count) {
+    if (!ctx || count < 0 || (count && !mats)) return LH2G_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    std::vector<lh2g_gpu_material> packed(std::max(count, 1));
+    for (int i = 0; i < count; i++) {
+        const lh2g_map_ref* refs[6] = {&mats[i].color_map, &mats[i].detail_color_map, &mats[i].normal_map, &mats[i].detail_normal_map, &mats[i].specular_map, &mats[i].roughness_map};
+        for (const lh2g_map_ref* r : refs)
+            if (r->texture >= (int)ctx->texFirst.size()) return fail(ctx, LH2G_ERR_INVALID, "set_materials: texture index out of range (set textures first)");
+        pack_material(mats[i], ctx->texFirst, ctx->texWH, packed[i]);
+    }
+    ctx->hostMats.assign(mats, mats + count);
+    CK(dalloc(ctx->mats, (size_t)8 * packed.size()));
+    CK(cudaMemcpyAsync(ctx->mats, packed.data(), sizeof(lh2g_gpu_material) * packed.size(), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return LH2G_OK;
+}
+
+int lh2g_set_lights(lh2g_context* ctx, const lh2g_light_tri* tri, int ntri, const lh2g_point_light* pt, int npt, const lh2g_spot_light* spot, int nspot,
+                    const lh2g_dir_light* dir, int ndir) {
+    if (!ctx || ntri < 0 || npt < 0 || nspot < 0 || ndir < 0) return LH2G_ERR_INVALID;
+    if (ntri + npt + nspot + ndir > 64) return fail(ctx, LH2G_ERR_INVALID, "set_lights: at most 64 lights (MAXISLIGHTS)");
+    cudaSetDevice(ctx->device);
+    CK(dalloc(ctx->triL, (size_t)6 * std::max(ntri, 1)));
+    CK(dalloc(ctx->ptL, (size_t)2 * std::max(npt, 1)));
+    CK(dalloc(ctx->spL, (size_t)3 * std::max(nspot, 1)));
+    CK(dalloc(ctx->dirL, (size_t)2 * std::max(ndir, 1)));
+    if (ntri) CK(cudaMemcpyAsync(ctx->triL, tri, sizeof(lh2g_light_tri) * ntri, cudaMemcpyHostToDevice, ctx->st));
+    if (npt) CK(cudaMemcpyAsync(ctx->ptL, pt, sizeof(lh2g_point_light) * npt, cudaMemcpyHostToDevice, ctx->st));
+    if (nspot) CK(cudaMemcpyAsync(ctx->spL, spot, sizeof(lh2g_spot_light) * nspot, cudaMemcpyHostToDevice, ctx->st));
+    if (ndir) CK(cudaMemcpyAsync(ctx->dirL, dir, sizeof(lh2g_dir_light) * ndir, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->nTri = ntri, ctx->nPt = npt, ctx->nSpot = nspot, ctx->nDir = ndir;
+    return LH2G_OK;
+}
+
+int lh2g_set_sky(lh2g_context* ctx, const float* rgb, int w, int h, const float* m16) {
+    if (!ctx || w < 0 || h < 0 || ((size_t)w * h && !rgb)) return LH2G_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    std::vector<float4> px((size_t)std::max(1, w * h));
+    for (size_t i = 0; i < (size_t)w * h; i++) px[i] = make_float4(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2], 0.0f);
+    CK(dalloc(ctx->sky, px.size()));
+    CK(cudaMemcpyAsync(ctx->sky, px.data(), sizeof(float4) * px.size(), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->skyW = w, ctx->skyH = h;
+    for (int i = 0; i < 16; i++) ctx->w2s[i] = m16 ? m16[i] : ((i % 5 == 0) ? 1.0f : 0.0f);
+    return LH2G_OK;
+}
+
+int lh2g_setting(lh2g_context* ctx, const char* name, float value) {
+    if (!ctx || !name) return LH2G_ERR_INVALID;
+    if (!strcmp(name, "epsilon")) ctx->eps = value;
+    else if (!strcmp(name, "clampValue")) ctx->clampValue = value;
+    else if (!strcmp(name, "maxDepth")) {
+        if (value < 1 || value > 64) return fail(ctx, LH2G_ERR_INVALID, "setting maxDepth: 1..64");
+        ctx->maxDepth = (int)value;
+    } else if (!strcmp(name, "rrStartDepth")) ctx->rrStart = (int)value;
+    else if (!strcmp(name, "nee")) ctx->nee = value != 0.0f;
+    /* other names (the filter core's clampDirect, clampIndirect, filter, TAA) are accepted and ignored,
+     * as the reference cores ignore settings they do not know (rendercore.cpp:484-502) */
+    return LH2G_OK;
+}
+
+int lh2g_set_target(lh2g_context* ctx, int w, int h, int spp) {
+    if (!ctx || w <= 0 || h <= 0 || spp <= 0 || w > 16384 || h > 16384) return fail(ctx, LH2G_ERR_INVALID, "set_target: bad size");
+    const int64_t P = (int64_t)w * h * spp;
+    if (P >= (1ll << 31)) return fail(ctx, LH2G_ERR_INVALID, "set_target: more than 2^31 paths");
+    cudaSetDevice(ctx->device);
+    CK(cudaStreamSynchronize(ctx->st));
+    if (P > ctx->cap || (int64_t)w * h != (int64_t)ctx->W * ctx->H) {
+        free_target(ctx);
+        WaveBuffers& B = ctx->B;
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < 2 && e == cudaSuccess; k++) {
+            if ((e = dalloc(B.O[k], P))) break;
+            if ((e = dalloc(B.D[k], P))) break;
+            e = dalloc(B.T[k], P);
+        }
+        if (!e) e = dalloc(B.hits, P);
+        if (!e) e = dalloc(B.shO, P);
+        if (!e) e = dalloc(B.shD, P);
+        if (!e) e = dalloc(B.shE, P);
+        if (!e) e = dalloc(B.pathAcc, P);
+        if (!e) e = dalloc(B.accum, (size_t)w * h);
+        if (!e) e = dalloc(B.frame, (size_t)w * h);
+        if (!e) e = dalloc(B.counters, 1);
+        if (e) { free_target(ctx); return cuda_check(ctx, e, "set_target allocation"); }
+        ctx->cap = P;
+        CK(cudaMemsetAsync(B.accum, 0, sizeof(float4) * (size_t)w * h, ctx->st));
+        CK(cudaMemsetAsync(B.frame, 0, sizeof(float4) * (size_t)w * h, ctx->st));
+    }
+    ctx->W = w, ctx->H = h, ctx->spp = spp;
+    ctx->samplesTaken = 0;
+    ctx->firstConverging = true;
+    return LH2G_OK;
+}
+
+int lh2g_set_probe(lh2g_context* ctx, int x, int y) {
+    if (!ctx) return LH2G_ERR_INVALID;
+    ctx->probeX = x, ctx->probeY = y;
+    return LH2G_OK;
+}
+
+int lh2g_render_ex(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* p, int accumulate, lh2g_hit* capHits, uint32_t* capSeeds,
+                   uint32_t* countersOut) {
+    if (!ctx || !view || !p) return LH2G_ERR_INVALID;
+    if (!ctx->finalized) return fail(ctx, LH2G_ERR_STATE, "render: scene not finalized (call lh2g_finalize_instances)");
+    if (!ctx->cap) return fail(ctx, LH2G_ERR_STATE, "render: no target (call lh2g_set_target)");
+    if (p->width != ctx->W || p->height != ctx->H || p->spp != ctx->spp || p->maxDepth < 1 || p->maxDepth > 64)
+        return fail(ctx, LH2G_ERR_INVALID, "render: parameters do not match the target");
+    if (!ctx->mats) return fail(ctx, LH2G_ERR_STATE, "render: no materials");
+    cudaSetDevice(ctx->device);
+    FrameGPU F;
+    memset(&F, 0, sizeof(F));
+    F.W = p->width, F.H = p->height, F.spp = p->spp, F.maxDepth = p->maxDepth, F.rrStart = p->rrStartDepth, F.samplesTaken = p->samplesTaken;
+    F.cameraR0 = p->cameraR0, F.eps = p->geometryEpsilon, F.flags = p->flags;
+    F.spreadAngle = view->spreadAngle, F.aperture = view->aperture;
+    F.pos = make_float3(view->pos[0], view->pos[1], view->pos[2]);
+    F.p1 = make_float3(view->p1[0], view->p1[1], view->p1[2]);
+    F.right = make_float3(view->p2[0] - view->p1[0], view->p2[1] - view->p1[1], view->p2[2] - view->p1[2]);
+    F.up = make_float3(view->p3[0] - view->p1[0], view->p3[1] - view->p1[1], view->p3[2] - view->p1[2]);
+    F.P = (int64_t)F.W * F.H * F.spp;
+    F.stride = ctx->cap;
+    WaveBuffers B = ctx->B;
+    B.capHits = nullptr, B.capSeeds = nullptr;
+    const size_t capN = (size_t)F.maxDepth * F.P;
+    if (capHits || capSeeds) {
+        CK(dalloc(ctx->B.capHits, capN));
+        CK(dalloc(ctx->B.capSeeds, capN));
+        std::vector<lh2g_hit> init(capN, lh2g_hit{0u, -1, -2, 0.0f});
+        CK(cudaMemcpyAsync(ctx->B.capHits, init.data(), sizeof(lh2g_hit) * capN, cudaMemcpyHostToDevice, ctx->st));
+        CK(cudaMemsetAsync(ctx->B.capSeeds, 0, sizeof(uint32_t) * capN, ctx->st));
+        B.capHits = ctx->B.capHits, B.capSeeds = ctx->B.capSeeds;
+    }
+    const SceneGPU S = scene_of(ctx);
+    if (!accumulate) CK(cudaMemsetAsync(B.accum, 0, sizeof(float4) * (size_t)F.W * F.H, ctx->st));
+    CK(cudaMemsetAsync(B.counters, 0, sizeof(Counters), ctx->st));
+    CK(cudaEventRecord(ctx->ev[0], ctx->st));
+    launch_generate(F, B, ctx->st);
+    for (int d = 1; d <= F.maxDepth; d++) {
+        launch_extend(S, F, B, d, ctx->blocksExtend, ctx->st);
+        launch_shade(S, F, B, d, ctx->blocksShade, ctx->st);
+        launch_connect(S, F, B, d, ctx->blocksConnect, ctx->st);
+    }
+    const int after = p->samplesTaken + F.spp;
+    launch_finalize(F, B, 1.0f / (float)after, ctx->st);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev[1], ctx->st));
+    CK(cudaMemcpyAsync(ctx->hostCounters, B.counters, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->st));
+    ctx->statsPending = true, ctx->lastDepth = F.maxDepth, ctx->lastP = F.P;
+    if (capHits || capSeeds || countersOut) {
+        CK(cudaStreamSynchronize(ctx->st));
+        if (capHits) CK(cudaMemcpy(capHits, ctx->B.capHits, sizeof(lh2g_hit) * capN, cudaMemcpyDeviceToHost));
+        if (capSeeds) CK(cudaMemcpy(capSeeds, ctx->B.capSeeds, sizeof(uint32_t) * capN, cudaMemcpyDeviceToHost));
+        if (countersOut)
+            for (int d = 0; d < F.maxDepth; d++) countersOut[2 * d] = ctx->hostCounters->extension[d], countersOut[2 * d + 1] = ctx->hostCounters->shadow[d];
+        if (ctx->hostCounters->status) return fail(ctx, LH2G_ERR_OVERFLOW, "render: traversal stack overflow or step limit");
+    }
+    return LH2G_OK;
+}
+
+int lh2g_render(lh2g_context* ctx, const lh2g_view* view, int converge) {
+    if (!ctx || !view) return LH2G_ERR_INVALID;
+    if (converge == 1 || ctx->firstConverging) {
+        ctx->samplesTaken = 0;
+        ctx->firstConverging = true;
+        ctx->camSeed = 0x12345678u;
+    }
+    if (converge == 0) ctx->firstConverging = false;
+    lh2g_render_params p;
+    memset(&p, 0, sizeof(p));
+    p.width = ctx->W, p.height = ctx->H, p.spp = ctx->spp, p.maxDepth = ctx->maxDepth, p.rrStartDepth = ctx->rrStart;
+    p.samplesTaken = ctx->samplesTaken;
+    p.cameraR0 = xorshift(ctx->camSeed);
+    p.geometryEpsilon = ctx->eps, p.clampValue = ctx->clampValue;
+    p.flags = (ctx->nee ? LH2G_RP_NEE : 0) | LH2G_RP_DEPTH_W;
+    const int r = lh2g_render_ex(ctx, view, &p, ctx->samplesTaken > 0 ? 1 : 0, nullptr, nullptr, nullptr);
+    if (r == LH2G_OK) ctx->samplesTaken += ctx->spp;
+    return r;
+}
+
+int lh2g_wait(lh2g_context* ctx) {
+    if (!ctx) return LH2G_ERR_INVALID;
+    CK(cudaStreamSynchronize(ctx->st));
+    return LH2G_OK;
+}
+
+int lh2g_get_stats(lh2g_context* ctx, lh2g_stats* out) {
+    if (!ctx || !out) return LH2G_ERR_INVALID;
+    if (ctx->statsPending) {
+        CK(cudaStreamSynchronize(ctx->st));
+        const Counters& C = *ctx->hostCounters;
+        uint32_t ext = (uint32_t)ctx->lastP, sh = 0;
+        for (int d = 0; d < ctx->lastDepth; d++) ext += C.extension[d], sh += C.shadow[d];
+        ctx->stats.totalExtensionRays = ext, ctx->stats.totalShadowRays = sh, ctx->stats.totalRays = ext + sh;
+        ctx->stats.primaryRayCount = (uint32_t)ctx->lastP;
+        ctx->stats.bounce1RayCount = ctx->lastDepth > 1 ? C.extension[0] : 0;
+        uint32_t deep = 0;
+        for (int d = 1; d < ctx->lastDepth - 1; d++) deep += C.extension[d];
+        ctx->stats.deepRayCount = deep;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+        ctx->stats.renderTime = ms;
+        ctx->stats.deviceStatus = C.status;
+        ctx->statsPending = false;
+    }
+    *out = ctx->stats;
+    return LH2G_OK;
+}
+
+int lh2g_get_framebuffer(lh2g_context* ctx, void** dev) {
+    if (!ctx || !dev) return LH2G_ERR_INVALID;
+    if (!ctx->cap) return fail(ctx, LH2G_ERR_STATE, "no target");
+    *dev = ctx->B.frame;
+    return LH2G_OK;
+}
+
+int lh2g_read_framebuffer(lh2g_context* ctx, float* host) {
+    if (!ctx || !host) return LH2G_ERR_INVALID;
+    if (!ctx->cap) return fail(ctx, LH2G_ERR_STATE, "no target");
+    CK(cudaMemcpyAsync(host, ctx->B.frame, sizeof(float4) * (size_t)ctx->W * ctx->H, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return LH2G_OK;
+}
+
+int lh2g_read_accumulator(lh2g_context* ctx, float* host) {
+    if (!ctx || !host) return LH2G_ERR_INVALID;
+    if (!ctx->cap) return fail(ctx, LH2G_ERR_STATE, "no target");
+    CK(cudaMemcpyAsync(host, ctx->B.accum, sizeof(float4) * (size_t)ctx->W * ctx->H, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return LH2G_OK;
+}
+
+int lh2g_trace(lh2g_context* ctx, const lh2g_ray* rays, void* out, long long n, int mode, void* stream) {
+    if (!ctx || n < 0 || (n && (!rays || !out)) || (mode != 0 && mode != 1)) return LH2G_ERR_INVALID;
+    if (!ctx->finalized) return fail(ctx, LH2G_ERR_STATE, "trace: scene not finalized");
+    if (n == 0) return LH2G_OK;
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->st;
+    CK(cudaMemsetAsync(ctx->traceFetch, 0, 16, st));
+    launch_trace(scene_of(ctx), rays, out, n, mode, ctx->traceFetch, ctx->traceFetch + 2, persistent_blocks_trace(mode), st);
+    CK(cudaGetLastError());
+    return LH2G_OK;
+}
+
+int lh2g_trace_host(lh2g_context* ctx, const lh2g_ray* rays, void* out, long long n, int mode) {
+    if (!ctx || n < 0 || (n && (!rays || !out)) || (mode != 0 && mode != 1)) return LH2G_ERR_INVALID;
+    if (n == 0) return LH2G_OK;
+    cudaSetDevice(ctx->device);
+    if (n > ctx->hostCap) {
+        CK(dalloc(ctx->hostRaysDev, (size_t)n));
+        CK(cudaMalloc(&ctx->hostOutDev, sizeof(lh2g_hit) * (size_t)n));
+        ctx->hostCap = n;
+    }
+    const size_t outBytes = (mode == 0 ? sizeof(lh2g_hit) : sizeof(uint32_t)) * (size_t)n;
+    CK(cudaMemcpyAsync(ctx->hostRaysDev, rays, sizeof(lh2g_ray) * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
+    const int r = lh2g_trace(ctx, ctx->hostRaysDev, ctx->hostOutDev, n, mode, nullptr);
+    if (r != LH2G_OK) return r;
+    CK(cudaMemcpyAsync(out, ctx->hostOutDev, outBytes, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    uint32_t status = 0;
+    CK(cudaMemcpy(&status, ctx->traceFetch + 2, 4, cudaMemcpyDeviceToHost));
+    if (status) return fail(ctx, LH2G_ERR_OVERFLOW, "trace: traversal stack overflow or step limit");
+    return LH2G_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,369 @@
+/* kernels.cu - wavefront path-tracing stages and ray-query kernels of the GB300 render core.
+ *
+ * Stage structure of the reference's wave loop (lib/RenderCore_PrimeRef/rendercore.cpp:551-611,
+ * lib/rendercore_optix7/rendercore.cpp:878-922), rebuilt for one GB300:
+ *   generate  primary rays (lib/RenderCore_PrimeRef/kernels/camera.h:39-68)
+ *   extend    closest hit of every ray in the current queue (persistent warps fetching 32 rays at a time)
+ *   shade     one thread per path (lib/RenderCore_PrimeRef/kernels/pathtracer.h:45-168); extension rays and
+ *             connections are compacted into the next queues by warp ballot + popc with one atomic per warp
+ *   connect   any hit of every connection; unoccluded ones add their contribution (connections.h:22-34)
+ *   finalize  per-pixel sum of the frame's samples in sample order, scaled by 1 / samples (finalize_shared.h:29-45)
+ * Queue sizes live in device counters; no stage waits for the host, so a frame is a fixed launch sequence.
+ * Radiance is accumulated per path (each path is owned by exactly one thread per stage), so the result does
+ * not depend on the order in which the queues were filled.
+ */
+#include "kernels.cuh"
+#include "shading.cuh"
+#include "traverse.cuh"
+
+namespace lh2g {
+
+namespace {
+
+constexpr int WAVE_BLOCK = 128;
+
+__device__ __forceinline__ uint32_t lanemask_lt() { uint32_t m; asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m)); return m; }
+
+/* -------------------------------------------------------------------------------------------------- */
+__global__ void __launch_bounds__(256) k_generate(const FrameGPU F, const WaveBuffers B) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= F.P) return;
+    const uint32_t jobIndex = (uint32_t)i;
+    const uint32_t x = jobIndex % (uint32_t)F.W;
+    uint32_t y = jobIndex / (uint32_t)F.W;
+    y %= (uint32_t)F.H;
+    uint32_t seed = WangHash(jobIndex + F.cameraR0);
+    const float r0 = RandomFloat(seed), r1 = RandomFloat(seed);
+    const float r2 = RandomFloat(seed), r3 = RandomFloat(seed);
+    const float3 posOnPixel = F.p1 + ((float)x + r0) * (F.right / (float)F.W) + ((float)y + r1) * (F.up / (float)F.H);
+    float3 posOnLens;
+    {
+        const float blade = (float)f2i(r2 * 9);
+        float rr2 = (r2 - blade * (1.0f / 9.0f)) * 9.0f, rr1 = r3;
+        float x1, y1, x2, y2;
+        sincos_cw(blade * PI / 4.5f, &x1, &y1);
+        sincos_cw((blade + 1.0f) * PI / 4.5f, &x2, &y2);
+        if ((rr1 + rr2) > 1) rr1 = 1.0f - rr1, rr2 = 1.0f - rr2;
+        const float xr = x1 * rr1 + x2 * rr2;
+        const float yr = y1 * rr1 + y2 * rr2;
+        posOnLens = F.pos + F.aperture * (F.right * xr + F.up * yr);
+    }
+    const float3 D = normalize(posOnPixel - posOnLens);
+    B.O[0][i] = make_float4(posOnLens.x, posOnLens.y, posOnLens.z, __uint_as_float(jobIndex));
+    B.D[0][i] = make_float4(D.x, D.y, D.z, __uint_as_float(S_SPECULAR));
+    B.T[0][i] = make_float4(1.0f, 1.0f, 1.0f, F.eps);
+    B.pathAcc[i] = make_float4(0, 0, 0, 0);
+}
+
+__device__ __forceinline__ uint32_t queue_count(const FrameGPU& F, const Counters* C, int depth) {
+    return depth == 1 ? (uint32_t)F.P : C->extension[depth - 2];
+}
+
+/* -------------------------------------------------------------------------------------------------- */
+__global__ void __launch_bounds__(128) k_extend(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int depth) {
+    Counters* C = B.counters;
+    const uint32_t count = queue_count(F, C, depth);
+    const int q = (depth - 1) & 1;
+    const float4* __restrict__ O4 = B.O[q];
+    const float4* __restrict__ D4 = B.D[q];
+    const float4* __restrict__ T4 = B.T[q];
+    const int lane = threadIdx.x & 31;
+    uint32_t status = 0;
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&C->fetch[depth - 1], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= count) break;
+        const uint32_t i = base + lane;
+        if (i >= count) continue;
+        const float4 o = O4[i], d = D4[i];
+        const float tmin = T4[i].w;
+        HitRec h;
+        const bool found = trace_ray<false>(S, xyz(o), xyz(d), tmin, 1e34f, h, status);
+        float4 rec;
+        if (found) rec = make_float4(__uint_as_float(f2u(65535.0f * h.u) + (f2u(65535.0f * h.v) << 16)), __int_as_float(h.inst), __int_as_float(h.prim), h.t);
+        else rec = make_float4(__uint_as_float(0u), __int_as_float(0), __int_as_float(NOHIT), 1e34f);
+        B.hits[i] = rec;
+        if (B.capHits) {
+            const uint32_t pathIdx = __float_as_uint(o.w);
+            lh2g_hit c;
+            c.bary = __float_as_uint(rec.x), c.inst = __float_as_int(rec.y), c.prim = __float_as_int(rec.z), c.t = rec.w;
+            B.capHits[(size_t)(depth - 1) * F.P + pathIdx] = c;
+        }
+    }
+    if (status) atomicOr(&C->status, status);
+}
+
+/* -------------------------------------------------------------------------------------------------- */
+struct ShadeOut {
+    bool ext, shadow;
+    float4 eO, eD, eT;
+    float4 sO, sD, sE;
+};
+
+__device__ __forceinline__ void shade_path(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, const int depth, const uint32_t i, ShadeOut& out) {
+    const int q = (depth - 1) & 1;
+    const float4 o4 = B.O[q][i], d4 = B.D[q][i], t4 = B.T[q][i], hit = B.hits[i];
+    const uint32_t pathIdx = __float_as_uint(o4.w);
+    uint32_t FLAGS = __float_as_uint(d4.w);
+    const float3 O = xyz(o4), D = xyz(d4);
+    float3 throughput = xyz(t4);
+    const int PRIM = __float_as_int(hit.z), INST = __float_as_int(hit.y);
+    const float HIT_T = hit.w;
+    const size_t capIdx = (size_t)(depth - 1) * F.P + pathIdx;
+    const uint32_t R0 = (uint32_t)F.samplesTaken * 7907u + (uint32_t)depth * 91771u;
+    float4 acc = B.pathAcc[pathIdx];
+    if ((F.flags & LH2G_RP_DEPTH_W) && depth == 1) acc.w += PRIM == NOHIT ? 10000.0f : HIT_T;
+    if (PRIM == NOHIT) {
+        const float3 c = throughput * SampleSkydome(S, D);
+        acc.x += c.x, acc.y += c.y, acc.z += c.z;
+        B.pathAcc[pathIdx] = acc;
+        if (B.capSeeds) B.capSeeds[capIdx] = 0;
+        return;
+    }
+    const uint32_t bary = __float_as_uint(hit.x);
+    const float HIT_U = (float)(bary & 65535u) * (1.0f / 65535.0f);
+    const float HIT_V = (float)(bary >> 16) * (1.0f / 65535.0f);
+    Shading sd;
+    float3 N, iN, fN, T;
+    const float3 I = O + HIT_T * D;
+    const float coneWidth = F.spreadAngle * HIT_T;
+    GetShadingData(S, D, HIT_U, HIT_V, coneWidth, INST, PRIM, sd, N, iN, fN, T);
+    const bool nee = (F.flags & LH2G_RP_NEE) != 0;
+    if (IsEmissive(sd)) {
+        const float DdotNL = -dot(D, N);
+        if (DdotNL > 0) {
+            const float3 c = throughput * sd.color;
+            if (depth == 1 || (FLAGS & S_SPECULAR) || !nee) acc.x += c.x, acc.y += c.y, acc.z += c.z;
+        }
+        B.pathAcc[pathIdx] = acc;
+        if (B.capSeeds) B.capSeeds[capIdx] = 0;
+        return;
+    }
+    if (depth == 1 && B.counters) {
+        /* probe: nothing to do here unless requested; kept out of the hot path */
+    }
+    B.pathAcc[pathIdx] = acc;
+    if (ROUGHNESS(sd) <= 0.001f || TRANSMISSION(sd) > 0.999f) FLAGS |= S_SPECULAR; else FLAGS &= ~S_SPECULAR;
+    uint32_t seed = WangHash(pathIdx * 17u + R0);
+    const float faceDir = (dot(D, N) > 0) ? -1.0f : 1.0f;
+    if (faceDir == 1) sd.transmittance = mk3(0);
+    if ((FLAGS & S_SPECULAR) == 0 && nee) {
+        const float q0 = RandomFloat(seed), q1 = RandomFloat(seed);
+        float pickProb = 0, lightPdf = 0;
+        float3 lightColor = mk3(0);
+        float3 L = RandomPointOnLight(S, q0, q1, I, fN * faceDir, pickProb, lightPdf, lightColor) - I;
+        const float dist = length(L);
+        L = L * (1.0f / dist);
+        const float NdotL = dot(L, fN * faceDir);
+        if (NdotL > 0 && lightPdf > 0) {
+            float bsdfPdf;
+            const float3 sampledBSDF = EvaluateBSDF(sd, fN, L, bsdfPdf) * ROUGHNESS(sd);
+            const float3 contribution = throughput * sampledBSDF * lightColor * (NdotL / (pickProb * lightPdf));
+            const float3 SO = SafeOrigin(I, L, N, F.eps);
+            out.shadow = true;
+            out.sO = make_float4(SO.x, SO.y, SO.z, __uint_as_float(pathIdx));
+            out.sD = make_float4(L.x, L.y, L.z, dist - 2 * F.eps);
+            out.sE = make_float4(contribution.x, contribution.y, contribution.z, 0.0f);
+        }
+    }
+    float3 R;
+    float newBsdfPdf;
+    bool specular = false;
+    const float q3 = RandomFloat(seed), q4 = RandomFloat(seed), q5 = RandomFloat(seed);
+    const float3 bsdf = SampleBSDF(sd, fN, N, D * -1.0f, HIT_T, q3, q4, R, newBsdfPdf, specular);
+    if (B.capSeeds) B.capSeeds[capIdx] = seed;
+    if (newBsdfPdf < EPSILON || isnan(newBsdfPdf)) return;
+    if (specular) FLAGS |= S_SPECULAR;
+    const float pr = depth == F.maxDepth ? 0.0f : (((FLAGS & S_SPECULAR) || depth < F.rrStart) ? 1.0f : SurvivalProbability(bsdf));
+    if (pr <= q5) return;
+    throughput = throughput * (bsdf * fabsf(dot(fN, R)) / (pr * newBsdfPdf));
+    const float3 EO = SafeOrigin(I, R, N, F.eps);
+    out.ext = true;
+    out.eO = make_float4(EO.x, EO.y, EO.z, __uint_as_float(pathIdx));
+    out.eD = make_float4(R.x, R.y, R.z, __uint_as_float(FLAGS));
+    out.eT = make_float4(throughput.x, throughput.y, throughput.z, 0.0f);
+}
+
+__global__ void __launch_bounds__(WAVE_BLOCK) k_shade(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int depth) {
+    Counters* C = B.counters;
+    const uint32_t count = queue_count(F, C, depth);
+    const int nq = depth & 1;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        ShadeOut out;
+        out.ext = out.shadow = false;
+        if (i < count) shade_path(S, F, B, depth, i, out);
+        const uint32_t em = __ballot_sync(0xffffffffu, out.ext);
+        if (em) {
+            const int leader = __ffs(em) - 1;
+            uint32_t slot = 0;
+            if ((int)lane == leader) slot = atomicAdd(&C->extension[depth - 1], (uint32_t)__popc(em));
+            slot = __shfl_sync(0xffffffffu, slot, leader) + __popc(em & lanemask_lt());
+            if (out.ext) B.O[nq][slot] = out.eO, B.D[nq][slot] = out.eD, B.T[nq][slot] = out.eT;
+        }
+        const uint32_t sm = __ballot_sync(0xffffffffu, out.shadow);
+        if (sm) {
+            const int leader = __ffs(sm) - 1;
+            uint32_t slot = 0;
+            if ((int)lane == leader) slot = atomicAdd(&C->shadow[depth - 1], (uint32_t)__popc(sm));
+            slot = __shfl_sync(0xffffffffu, slot, leader) + __popc(sm & lanemask_lt());
+            if (out.shadow) B.shO[slot] = out.sO, B.shD[slot] = out.sD, B.shE[slot] = out.sE;
+        }
+    }
+}
+
+/* -------------------------------------------------------------------------------------------------- */
+__global__ void __launch_bounds__(128) k_connect(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int depth) {
+    Counters* C = B.counters;
+    const uint32_t count = C->shadow[depth - 1];
+    const int lane = threadIdx.x & 31;
+    uint32_t status = 0;
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&C->fetch[64 + depth - 1], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= count) break;
+        const uint32_t i = base + lane;
+        if (i >= count) continue;
+        const float4 o = B.shO[i], d = B.shD[i];
+        HitRec h;
+        if (trace_ray<true>(S, xyz(o), xyz(d), 0.0f, d.w, h, status)) continue;
+        const float4 e = B.shE[i];
+        const uint32_t pathIdx = __float_as_uint(o.w);
+        float4 acc = B.pathAcc[pathIdx];
+        acc.x += e.x, acc.y += e.y, acc.z += e.z;
+        B.pathAcc[pathIdx] = acc;
+    }
+    if (status) atomicOr(&C->status, status);
+}
+
+/* -------------------------------------------------------------------------------------------------- */
+__global__ void k_finalize(const FrameGPU F, const WaveBuffers B, const float scale) {
+    const int64_t px = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t WH = (int64_t)F.W * F.H;
+    if (px >= WH) return;
+    float4 acc = B.accum[px];
+    for (int s = 0; s < F.spp; s++) {
+        const float4 v = B.pathAcc[s * WH + px];
+        acc.x += v.x, acc.y += v.y, acc.z += v.z, acc.w += v.w;
+    }
+    B.accum[px] = acc;
+    B.frame[px] = make_float4(acc.x * scale, acc.y * scale, acc.z * scale, acc.w * scale);
+}
+
+/* -------------------------------------------------------------------------------------------------- */
+template <int MODE>
+__global__ void __launch_bounds__(128) k_trace(const SceneGPU S, const lh2g_ray* __restrict__ rays, void* __restrict__ out, const long long n,
+                                               uint32_t* fetch, uint32_t* statusOut) {
+    const int lane = threadIdx.x & 31;
+    uint32_t status = 0;
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd((unsigned long long*)fetch, 32ull);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= (unsigned long long)n) break;
+        const unsigned long long i = base + lane;
+        if (i >= (unsigned long long)n) continue;
+        const float4* r = (const float4*)(rays + i);
+        const float4 a = __ldg(r), b = __ldg(r + 1);
+        HitRec h;
+        const bool hit = trace_ray<MODE == 1>(S, xyz(a), xyz(b), a.w, b.w, h, status);
+        if (MODE == 1) ((uint32_t*)out)[i] = hit ? 1u : 0u;
+        else {
+            uint4 rec;
+            if (hit) rec = make_uint4(f2u(65535.0f * h.u) + (f2u(65535.0f * h.v) << 16), (uint32_t)h.inst, (uint32_t)h.prim, __float_as_uint(h.t));
+            else rec = make_uint4(0u, 0u, (uint32_t)NOHIT, __float_as_uint(1e34f));
+            ((uint4*)out)[i] = rec;
+        }
+    }
+    if (status) atomicOr(statusOut, status);
+}
+
+/* -------------------------------------------------------------------------------------------------- */
+__global__ void k_tri_prep(const float4* __restrict__ verts, uint32_t n, uint32_t seg, float4* __restrict__ triData, float4* __restrict__ lo,
+                           float4* __restrict__ hi, uint32_t* __restrict__ segOf) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 a = verts[3 * i], b = verts[3 * i + 1], c = verts[3 * i + 2];
+    const float3 v0 = xyz(a), e1 = xyz(b) - v0, e2 = xyz(c) - v0;
+    triData[3 * i] = make_float4(v0.x, v0.y, v0.z, __int_as_float((int)i));
+    triData[3 * i + 1] = make_float4(e1.x, e1.y, e1.z, 0.0f);
+    triData[3 * i + 2] = make_float4(e2.x, e2.y, e2.z, 0.0f);
+    const float3 v1 = v0 + e1, v2 = v0 + e2;
+    float3 mn = make_float3(fminf(fminf(v0.x, v1.x), v2.x), fminf(fminf(v0.y, v1.y), v2.y), fminf(fminf(v0.z, v1.z), v2.z));
+    float3 mx = make_float3(fmaxf(fmaxf(v0.x, v1.x), v2.x), fmaxf(fmaxf(v0.y, v1.y), v2.y), fmaxf(fmaxf(v0.z, v1.z), v2.z));
+    /* widen by 2^-20 of the magnitude (covers the rounding of v0 + e1 and of dequantised planes) */
+    const float k = 9.5367431640625e-07f;
+    mn = make_float3(mn.x - (fabsf(mn.x) * k + 1e-30f), mn.y - (fabsf(mn.y) * k + 1e-30f), mn.z - (fabsf(mn.z) * k + 1e-30f));
+    mx = make_float3(mx.x + (fabsf(mx.x) * k + 1e-30f), mx.y + (fabsf(mx.y) * k + 1e-30f), mx.z + (fabsf(mx.z) * k + 1e-30f));
+    lo[i] = make_float4(mn.x, mn.y, mn.z, 0.0f);
+    hi[i] = make_float4(mx.x, mx.y, mx.z, 0.0f);
+    segOf[i] = seg;
+}
+
+__global__ void k_gather_tris(const float4* __restrict__ triIn, const uint32_t* __restrict__ leafPrim, uint32_t n, float4* __restrict__ triOut) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t p = leafPrim[i];
+    triOut[3 * i] = triIn[3 * p], triOut[3 * i + 1] = triIn[3 * p + 1], triOut[3 * i + 2] = triIn[3 * p + 2];
+}
+
+int sm_count() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+}  // namespace
+
+int persistent_blocks_trace(int mode) {
+    int per = 0;
+    if (mode == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_trace<1>, 128, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_trace<0>, 128, 0);
+    return sm_count() * (per > 0 ? per : 1);
+}
+
+int persistent_blocks_wave(int which) {
+    int per = 0;
+    if (which == 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_extend, 128, 0);
+    else if (which == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_connect, 128, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_shade, WAVE_BLOCK, 0);
+    return sm_count() * (per > 0 ? per : 1);
+}
+
+void launch_generate(const FrameGPU& F, const WaveBuffers& B, cudaStream_t st) {
+    k_generate<<<(unsigned)((F.P + 255) / 256), 256, 0, st>>>(F, B);
+}
+void launch_extend(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int blocks, cudaStream_t st) {
+    k_extend<<<blocks, 128, 0, st>>>(S, F, B, depth);
+}
+void launch_shade(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int blocks, cudaStream_t st) {
+    k_shade<<<blocks, WAVE_BLOCK, 0, st>>>(S, F, B, depth);
+}
+void launch_connect(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int blocks, cudaStream_t st) {
+    k_connect<<<blocks, 128, 0, st>>>(S, F, B, depth);
+}
+void launch_finalize(const FrameGPU& F, const WaveBuffers& B, float scale, cudaStream_t st) {
+    const int64_t WH = (int64_t)F.W * F.H;
+    k_finalize<<<(unsigned)((WH + 255) / 256), 256, 0, st>>>(F, B, scale);
+}
+void launch_trace(const SceneGPU& S, const lh2g_ray* rays, void* out, long long n, int mode, uint32_t* fetch, uint32_t* status, int blocks, cudaStream_t st) {
+    if (mode == 1) k_trace<1><<<blocks, 128, 0, st>>>(S, rays, out, n, fetch, status);
+    else k_trace<0><<<blocks, 128, 0, st>>>(S, rays, out, n, fetch, status);
+}
+void launch_tri_prep(const float4* verts, uint32_t n, uint32_t seg, float4* triData, float4* lo, float4* hi, uint32_t* segOf, cudaStream_t st) {
+    if (n) k_tri_prep<<<(n + 255) / 256, 256, 0, st>>>(verts, n, seg, triData, lo, hi, segOf);
+}
+void launch_gather_tris(const float4* triIn, const uint32_t* leafPrim, uint32_t n, float4* triOut, cudaStream_t st) {
+    if (n) k_gather_tris<<<(n + 255) / 256, 256, 0, st>>>(triIn, leafPrim, n, triOut);
+}
+
+}  // namespace lh2g

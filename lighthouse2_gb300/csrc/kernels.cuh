@@ -1,0 +1,40 @@
+/* kernels.cuh - the wavefront stages and ray-query kernels of the GB300 render core. */
+#pragma once
+#include "core_types.cuh"
+#include "lh2g_types.h"
+
+namespace lh2g {
+
+/* Path-state buffers of one render target (capacity = W * H * spp paths). */
+struct WaveBuffers {
+    float4* O[2];          /* ping-pong queues: O4 (w = path index), D4 (w = flags), T4 (w = tmin) */
+    float4* D[2];
+    float4* T[2];
+    float4* hits;          /* OptiX-style hit record per queue slot */
+    float4* shO;           /* connections: origin (w = path index), direction (w = tmax), contribution */
+    float4* shD;
+    float4* shE;
+    float4* pathAcc;       /* per-path radiance (w = primary distance) */
+    float4* accum;         /* per-pixel accumulator across frames */
+    float4* frame;         /* finalized output: accum / samplesTaken */
+    Counters* counters;
+    lh2g_hit* capHits;     /* optional per-(depth, path) capture */
+    uint32_t* capSeeds;
+};
+
+void launch_generate(const FrameGPU& F, const WaveBuffers& B, cudaStream_t st);
+void launch_extend(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int persistentBlocks, cudaStream_t st);
+void launch_shade(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int blocks, cudaStream_t st);
+void launch_connect(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int persistentBlocks, cudaStream_t st);
+void launch_finalize(const FrameGPU& F, const WaveBuffers& B, float scale, cudaStream_t st);
+void launch_trace(const SceneGPU& S, const lh2g_ray* rays, void* out, long long n, int mode, uint32_t* fetch, uint32_t* status,
+                  int persistentBlocks, cudaStream_t st);
+
+/* scene preparation */
+void launch_tri_prep(const float4* verts, uint32_t n, uint32_t seg, float4* triData, float4* lo, float4* hi, uint32_t* segOf, cudaStream_t st);
+void launch_gather_tris(const float4* triIn, const uint32_t* leafPrim, uint32_t n, float4* triOut, cudaStream_t st);
+
+int persistent_blocks_trace(int mode);
+int persistent_blocks_wave(int which);
+
+}  // namespace lh2g
