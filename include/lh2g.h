@@ -88,6 +88,14 @@ LH2G_API int lh2g_get_framebuffer(lh2g_context* ctx, void** devicePtr);
 LH2G_API int lh2g_read_framebuffer(lh2g_context* ctx, float* host);
 LH2G_API int lh2g_read_accumulator(lh2g_context* ctx, float* host);
 
+/* The context's CUDA stream (cudaStream_t), for callers that bracket frames with their own events. */
+LH2G_API int lh2g_get_stream(lh2g_context* ctx, void** stream);
+/* Per-launch device timing of the next frames (enable != 0): lh2g_get_launch_times fills ms[k] with the
+ * duration of launch k of the last frame, in launch order [generate, (extend, shade, connect) x maxDepth,
+ * finalize], and *count with the number of launches. Timing adds one event pair per launch. */
+LH2G_API int lh2g_enable_launch_timing(lh2g_context* ctx, int enable);
+LH2G_API int lh2g_get_launch_times(lh2g_context* ctx, float* ms, int capacity, int* count);
+
 /* Ray queries over the scene (the OptiX Prime query interface of lib/RenderCore_PrimeRef/rendercore.cpp:569-605,
  * formats RTP_BUFFER_FORMAT_RAY_ORIGIN_TMIN_DIRECTION_TMAX / hit float4 {u|v<<16, inst, prim, t}).
  * mode 0: closest hit into lh2g_hit[n] (prim = -1 on a miss); mode 1: any hit into uint32 occluded[n].

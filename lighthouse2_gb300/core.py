@@ -34,7 +34,8 @@ RP_NEE, RP_DEPTH_W = 1, 2
 C_API = ["lh2g_create", "lh2g_destroy", "lh2g_last_error", "lh2g_set_geometry", "lh2g_set_instance", "lh2g_finalize_instances",
          "lh2g_set_materials", "lh2g_pack_materials", "lh2g_set_textures", "lh2g_set_lights", "lh2g_set_sky", "lh2g_setting",
          "lh2g_set_target", "lh2g_set_probe", "lh2g_render", "lh2g_render_ex", "lh2g_wait", "lh2g_get_stats",
-         "lh2g_get_framebuffer", "lh2g_read_framebuffer", "lh2g_read_accumulator", "lh2g_trace", "lh2g_trace_host"]
+         "lh2g_get_framebuffer", "lh2g_read_framebuffer", "lh2g_read_accumulator", "lh2g_trace", "lh2g_trace_host",
+         "lh2g_get_stream", "lh2g_enable_launch_timing", "lh2g_get_launch_times"]
 
 _lib = None
 
@@ -77,6 +78,9 @@ def load_library(path: str | None = None):
     lib.lh2g_read_accumulator.argtypes = [vp, vp]
     lib.lh2g_trace.argtypes = [vp, vp, vp, C.c_longlong, i, vp]
     lib.lh2g_trace_host.argtypes = [vp, vp, vp, C.c_longlong, i]
+    lib.lh2g_get_stream.argtypes = [vp, C.POINTER(vp)]
+    lib.lh2g_enable_launch_timing.argtypes = [vp, i]
+    lib.lh2g_get_launch_times.argtypes = [vp, vp, i, C.POINTER(i)]
     if path is None:
         _lib = lib
     return lib
@@ -240,6 +244,23 @@ class RenderCore:
         p = C.c_void_p()
         self._check(self.lib.lh2g_get_framebuffer(self.ctx, C.byref(p)), "get_framebuffer")
         return p.value
+
+    def stream_ptr(self):
+        p = C.c_void_p()
+        self._check(self.lib.lh2g_get_stream(self.ctx, C.byref(p)), "get_stream")
+        return p.value or 0
+
+    def enable_launch_timing(self, on=True):
+        self._check(self.lib.lh2g_enable_launch_timing(self.ctx, int(on)), "enable_launch_timing")
+
+    def launch_times(self):
+        buf = np.zeros(256, np.float32)
+        n = C.c_int(0)
+        self._check(self.lib.lh2g_get_launch_times(self.ctx, _p(buf), len(buf), C.byref(n)), "get_launch_times")
+        return buf[:n.value].copy()
+
+    def read_framebuffer_into(self, host_ptr):
+        self._check(self.lib.lh2g_read_framebuffer(self.ctx, C.c_void_p(host_ptr)), "read_framebuffer")
 
     def trace_host(self, rays, mode=0):
         rays = np.ascontiguousarray(rays)

@@ -166,6 +166,9 @@ struct lh2g_context {
     void* hostOutDev = nullptr;
     long long hostCap = 0;
     cudaEvent_t ev[2];
+    bool launchTiming = false;
+    std::vector<cudaEvent_t> lev;   /* 2 per launch */
+    int lastLaunches = 0;
     int blocksExtend = 0, blocksConnect = 0, blocksShade = 0;
 };
 
@@ -266,6 +269,7 @@ int lh2g_destroy(lh2g_context* ctx) {
     free_target(ctx);
     if (ctx->hostCounters) cudaFreeHost(ctx->hostCounters);
     cudaEventDestroy(ctx->ev[0]), cudaEventDestroy(ctx->ev[1]);
+    for (cudaEvent_t e : ctx->lev) cudaEventDestroy(e);
     cudaStreamDestroy(ctx->st);
     delete ctx;
     return LH2G_OK;
@@ -568,15 +572,26 @@ int lh2g_render_ex(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_p
     const SceneGPU S = scene_of(ctx);
     if (!accumulate) CK(cudaMemsetAsync(B.accum, 0, sizeof(float4) * (size_t)F.W * F.H, ctx->st));
     CK(cudaMemsetAsync(B.counters, 0, sizeof(Counters), ctx->st));
+    const int launches = 2 + 3 * F.maxDepth;
+    const bool timing = ctx->launchTiming;
+    if (timing)
+        while ((int)ctx->lev.size() < 2 * launches) {
+            cudaEvent_t e;
+            CK(cudaEventCreate(&e));
+            ctx->lev.push_back(e);
+        }
+    int li = 0;
+    auto mark = [&]() { if (timing) cudaEventRecord(ctx->lev[li++], ctx->st); };
     CK(cudaEventRecord(ctx->ev[0], ctx->st));
-    launch_generate(F, B, ctx->st);
+    mark(), launch_generate(F, B, ctx->st), mark();
     for (int d = 1; d <= F.maxDepth; d++) {
-        launch_extend(S, F, B, d, ctx->blocksExtend, ctx->st);
-        launch_shade(S, F, B, d, ctx->blocksShade, ctx->st);
-        launch_connect(S, F, B, d, ctx->blocksConnect, ctx->st);
+        mark(), launch_extend(S, F, B, d, ctx->blocksExtend, ctx->st), mark();
+        mark(), launch_shade(S, F, B, d, ctx->blocksShade, ctx->st), mark();
+        mark(), launch_connect(S, F, B, d, ctx->blocksConnect, ctx->st), mark();
     }
     const int after = p->samplesTaken + F.spp;
-    launch_finalize(F, B, 1.0f / (float)after, ctx->st);
+    mark(), launch_finalize(F, B, 1.0f / (float)after, ctx->st), mark();
+    ctx->lastLaunches = timing ? launches : 0;
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev[1], ctx->st));
     CK(cudaMemcpyAsync(ctx->hostCounters, B.counters, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->st));
@@ -661,6 +676,30 @@ int lh2g_read_accumulator(lh2g_context* ctx, float* host) {
     if (!ctx->cap) return fail(ctx, LH2G_ERR_STATE, "no target");
     CK(cudaMemcpyAsync(host, ctx->B.accum, sizeof(float4) * (size_t)ctx->W * ctx->H, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
+    return LH2G_OK;
+}
+
+int lh2g_get_stream(lh2g_context* ctx, void** stream) {
+    if (!ctx || !stream) return LH2G_ERR_INVALID;
+    *stream = (void*)ctx->st;
+    return LH2G_OK;
+}
+
+int lh2g_enable_launch_timing(lh2g_context* ctx, int enable) {
+    if (!ctx) return LH2G_ERR_INVALID;
+    ctx->launchTiming = enable != 0;
+    return LH2G_OK;
+}
+
+int lh2g_get_launch_times(lh2g_context* ctx, float* ms, int capacity, int* count) {
+    if (!ctx || !count || (capacity > 0 && !ms)) return LH2G_ERR_INVALID;
+    CK(cudaStreamSynchronize(ctx->st));
+    *count = ctx->lastLaunches;
+    for (int k = 0; k < ctx->lastLaunches && k < capacity; k++) {
+        float t = 0;
+        CK(cudaEventElapsedTime(&t, ctx->lev[2 * k], ctx->lev[2 * k + 1]));
+        ms[k] = t;
+    }
     return LH2G_OK;
 }
 

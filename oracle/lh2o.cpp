@@ -1160,22 +1160,29 @@ int lh2o_set_sky(lh2o_scene* s, const float* rgb, int w, int h, const float* m16
 
 int lh2o_finalize(lh2o_scene* s) {
     if (!s) return 1;
-    for (Mesh& m : s->meshes) {
-        std::vector<BuildPrim> prims(m.v0.size());
-        for (size_t i = 0; i < m.v0.size(); i++) {
-            const f3 a = m.v0[i], b = a + m.e1[i], c = a + m.e2[i];
-            /* box of the exact vertices (v0 + e1 may differ from v1 by rounding: take the union) */
-            const f3 ps[3] = {a, b, c};
-            BuildPrim& p = prims[i];
-            for (int k = 0; k < 3; k++) p.bmin[k] = 1e30f, p.bmax[k] = -1e30f;
-            for (const f3& q : ps) {
-                const float qq[3] = {q.x, q.y, q.z};
-                for (int k = 0; k < 3; k++) p.bmin[k] = std::min(p.bmin[k], qq[k]), p.bmax[k] = std::max(p.bmax[k], qq[k]);
+    parallel_for((long long)s->meshes.size(), 0, 1, [&](long long b, long long e) {
+        for (long long mi = b; mi < e; mi++) {
+            Mesh& m = s->meshes[mi];
+            std::vector<BuildPrim> prims(m.v0.size());
+            for (size_t i = 0; i < m.v0.size(); i++) {
+                const f3 a = m.v0[i], bb = a + m.e1[i], c = a + m.e2[i];
+                const f3 ps[3] = {a, bb, c};
+                BuildPrim& p = prims[i];
+                for (int k = 0; k < 3; k++) p.bmin[k] = 1e30f, p.bmax[k] = -1e30f;
+                for (const f3& q : ps) {
+                    const float qq[3] = {q.x, q.y, q.z};
+                    for (int k = 0; k < 3; k++) p.bmin[k] = std::min(p.bmin[k], qq[k]), p.bmax[k] = std::max(p.bmax[k], qq[k]);
+                }
+                /* widen by 2^-20 of the magnitude: v0 + e1 is not exactly the vertex the test uses */
+                for (int k = 0; k < 3; k++) {
+                    p.bmin[k] -= fabsf(p.bmin[k]) * 9.5367431640625e-07f + 1e-30f;
+                    p.bmax[k] += fabsf(p.bmax[k]) * 9.5367431640625e-07f + 1e-30f;
+                    p.c[k] = (p.bmin[k] + p.bmax[k]) * 0.5f;
+                }
             }
-            for (int k = 0; k < 3; k++) p.c[k] = (p.bmin[k] + p.bmax[k]) * 0.5f;
+            build_bvh2(prims, m.bvh);
         }
-        build_bvh2(prims, m.bvh);
-    }
+    });
     std::vector<BuildPrim> ip(s->inst.size());
     for (size_t i = 0; i < s->inst.size(); i++) {
         Instance& in = s->inst[i];
