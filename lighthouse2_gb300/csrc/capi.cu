@@ -709,8 +709,15 @@ int lh2g_trace(lh2g_context* ctx, const lh2g_ray* rays, void* out, long long n, 
     if (n == 0) return LH2G_OK;
     cudaSetDevice(ctx->device);
     cudaStream_t st = stream ? (cudaStream_t)stream : ctx->st;
-    CK(cudaMemsetAsync(ctx->traceFetch, 0, 16, st));
-    launch_trace(scene_of(ctx), rays, out, n, mode, ctx->traceFetch, ctx->traceFetch + 2, persistent_blocks_trace(mode), st);
+    const long long chunk = 1ll << 31;   /* the work counter is 32-bit */
+    const int blocks = persistent_blocks_trace(mode);
+    CK(cudaMemsetAsync(ctx->traceFetch + 2, 0, 4, st));
+    for (long long b = 0; b < n; b += chunk) {
+        const long long m = std::min(chunk, n - b);
+        CK(cudaMemsetAsync(ctx->traceFetch, 0, 4, st));
+        void* o = (char*)out + (size_t)b * (mode == 0 ? sizeof(lh2g_hit) : sizeof(uint32_t));
+        launch_trace(scene_of(ctx), rays + b, o, m, mode, ctx->traceFetch, ctx->traceFetch + 2, blocks, st);
+    }
     CK(cudaGetLastError());
     return LH2G_OK;
 }
@@ -737,3 +744,4 @@ int lh2g_trace_host(lh2g_context* ctx, const lh2g_ray* rays, void* out, long lon
 }
 
 }  // extern "C"
+

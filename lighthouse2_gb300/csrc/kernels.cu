@@ -67,30 +67,24 @@ __global__ void __launch_bounds__(128) k_extend(const SceneGPU S, const FrameGPU
     const float4* __restrict__ O4 = B.O[q];
     const float4* __restrict__ D4 = B.D[q];
     const float4* __restrict__ T4 = B.T[q];
-    const int lane = threadIdx.x & 31;
     uint32_t status = 0;
-    for (;;) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(&C->fetch[depth - 1], 32u);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= count) break;
-        const uint32_t i = base + lane;
-        if (i >= count) continue;
-        const float4 o = O4[i], d = D4[i];
-        const float tmin = T4[i].w;
-        HitRec h;
-        const bool found = trace_ray<false>(S, xyz(o), xyz(d), tmin, 1e34f, h, status);
-        float4 rec;
-        if (found) rec = make_float4(__uint_as_float(f2u(65535.0f * h.u) + (f2u(65535.0f * h.v) << 16)), __int_as_float(h.inst), __int_as_float(h.prim), h.t);
-        else rec = make_float4(__uint_as_float(0u), __int_as_float(0), __int_as_float(NOHIT), 1e34f);
-        B.hits[i] = rec;
-        if (B.capHits) {
-            const uint32_t pathIdx = __float_as_uint(o.w);
-            lh2g_hit c;
-            c.bary = __float_as_uint(rec.x), c.inst = __float_as_int(rec.y), c.prim = __float_as_int(rec.z), c.t = rec.w;
-            B.capHits[(size_t)(depth - 1) * F.P + pathIdx] = c;
-        }
-    }
+    trace_queue<false>(S, &C->fetch[depth - 1], count, status,
+        [&](uint32_t i, float3& o, float3& d, float& t0, float& t1) {
+            o = xyz(O4[i]), d = xyz(D4[i]), t0 = T4[i].w, t1 = 1e34f;
+        },
+        [&](uint32_t i, const Traversal& tr, bool) {
+            float4 rec;
+            if (tr.found) rec = make_float4(__uint_as_float(f2u(65535.0f * tr.best.u) + (f2u(65535.0f * tr.best.v) << 16)), __int_as_float(tr.best.inst),
+                                            __int_as_float(tr.best.prim), tr.best.t);
+            else rec = make_float4(__uint_as_float(0u), __int_as_float(0), __int_as_float(NOHIT), 1e34f);
+            B.hits[i] = rec;
+            if (B.capHits) {
+                const uint32_t pathIdx = __float_as_uint(O4[i].w);
+                lh2g_hit c;
+                c.bary = __float_as_uint(rec.x), c.inst = __float_as_int(rec.y), c.prim = __float_as_int(rec.z), c.t = rec.w;
+                B.capHits[(size_t)(depth - 1) * F.P + pathIdx] = c;
+            }
+        });
     if (status) atomicOr(&C->status, status);
 }
 
@@ -219,24 +213,20 @@ __global__ void __launch_bounds__(WAVE_BLOCK) k_shade(const SceneGPU S, const Fr
 __global__ void __launch_bounds__(128) k_connect(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int depth) {
     Counters* C = B.counters;
     const uint32_t count = C->shadow[depth - 1];
-    const int lane = threadIdx.x & 31;
     uint32_t status = 0;
-    for (;;) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(&C->fetch[64 + depth - 1], 32u);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= count) break;
-        const uint32_t i = base + lane;
-        if (i >= count) continue;
-        const float4 o = B.shO[i], d = B.shD[i];
-        HitRec h;
-        if (trace_ray<true>(S, xyz(o), xyz(d), 0.0f, d.w, h, status)) continue;
-        const float4 e = B.shE[i];
-        const uint32_t pathIdx = __float_as_uint(o.w);
-        float4 acc = B.pathAcc[pathIdx];
-        acc.x += e.x, acc.y += e.y, acc.z += e.z;
-        B.pathAcc[pathIdx] = acc;
-    }
+    trace_queue<true>(S, &C->fetch[64 + depth - 1], count, status,
+        [&](uint32_t i, float3& o, float3& d, float& t0, float& t1) {
+            const float4 d4 = B.shD[i];
+            o = xyz(B.shO[i]), d = xyz(d4), t0 = 0.0f, t1 = d4.w;
+        },
+        [&](uint32_t i, const Traversal&, bool occluded) {
+            if (occluded) return;
+            const float4 e = B.shE[i];
+            const uint32_t pathIdx = __float_as_uint(B.shO[i].w);
+            float4 acc = B.pathAcc[pathIdx];
+            acc.x += e.x, acc.y += e.y, acc.z += e.z;
+            B.pathAcc[pathIdx] = acc;
+        });
     if (status) atomicOr(&C->status, status);
 }
 
@@ -258,27 +248,24 @@ __global__ void k_finalize(const FrameGPU F, const WaveBuffers B, const float sc
 template <int MODE>
 __global__ void __launch_bounds__(128) k_trace(const SceneGPU S, const lh2g_ray* __restrict__ rays, void* __restrict__ out, const long long n,
                                                uint32_t* fetch, uint32_t* statusOut) {
-    const int lane = threadIdx.x & 31;
     uint32_t status = 0;
-    for (;;) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd((unsigned long long*)fetch, 32ull);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= (unsigned long long)n) break;
-        const unsigned long long i = base + lane;
-        if (i >= (unsigned long long)n) continue;
-        const float4* r = (const float4*)(rays + i);
-        const float4 a = __ldg(r), b = __ldg(r + 1);
-        HitRec h;
-        const bool hit = trace_ray<MODE == 1>(S, xyz(a), xyz(b), a.w, b.w, h, status);
-        if (MODE == 1) ((uint32_t*)out)[i] = hit ? 1u : 0u;
-        else {
-            uint4 rec;
-            if (hit) rec = make_uint4(f2u(65535.0f * h.u) + (f2u(65535.0f * h.v) << 16), (uint32_t)h.inst, (uint32_t)h.prim, __float_as_uint(h.t));
-            else rec = make_uint4(0u, 0u, (uint32_t)NOHIT, __float_as_uint(1e34f));
-            ((uint4*)out)[i] = rec;
-        }
-    }
+    /* queries of more than 2^32 - 2^16 rays are processed in chunks by the host */
+    trace_queue<MODE == 1>(S, fetch, (uint32_t)n, status,
+        [&](uint32_t i, float3& o, float3& d, float& t0, float& t1) {
+            const float4* r = (const float4*)(rays + i);
+            const float4 a = __ldg(r), b = __ldg(r + 1);
+            o = xyz(a), d = xyz(b), t0 = a.w, t1 = b.w;
+        },
+        [&](uint32_t i, const Traversal& tr, bool any) {
+            if (MODE == 1) ((uint32_t*)out)[i] = any ? 1u : 0u;
+            else {
+                uint4 rec;
+                if (tr.found) rec = make_uint4(f2u(65535.0f * tr.best.u) + (f2u(65535.0f * tr.best.v) << 16), (uint32_t)tr.best.inst, (uint32_t)tr.best.prim,
+                                               __float_as_uint(tr.best.t));
+                else rec = make_uint4(0u, 0u, (uint32_t)NOHIT, __float_as_uint(1e34f));
+                ((uint4*)out)[i] = rec;
+            }
+        });
     if (status) atomicOr(statusOut, status);
 }
 

@@ -55,28 +55,37 @@ LH2G_DEV bool isect_tri(const float3 O, const float3 D, const float4 a, const fl
 
 LH2G_DEV uint32_t byte_of(uint32_t w0, uint32_t w1, int i) { return ((i < 4 ? w0 : w1) >> ((i & 3) * 8)) & 255u; }
 
-template <bool ANYHIT>
-LH2G_DEV bool trace_ray(const SceneGPU& S, const float3 Ow, const float3 Dw, const float tmin, const float tmax,
-                        HitRec& best, uint32_t& status) {
-    best.t = tmax, best.u = best.v = 0.0f, best.inst = -1, best.prim = NOHIT;
-    bool found = false;
-    if (S.tlasRoot == 0xffffffffu) return false;
+/* Resumable traversal state of one ray (one lane). step() processes the current stack entry and pops the
+ * next one; it returns false once the ray is finished. Kernels interleave step() with per-lane refills of
+ * finished rays, so a warp keeps all lanes busy instead of waiting for its slowest ray. */
+struct Traversal {
     uint2 stack[LH2G_STACK];
-    int sp = 0;
-    float3 O = Ow, D = Dw;
-    float3 invD = make_float3(safe_rcp(Dw.x), safe_rcp(Dw.y), safe_rcp(Dw.z));
-    int curInst = -1;
-    uint32_t entry = S.tlasRoot;
-    uint32_t steps = 0;
-    for (;;) {
-        if (++steps > MAX_STEPS) { status |= LH2G_STATUS_TRAVERSAL_LIMIT; return found; }
+    float3 Ow, Dw, O, D, invD;
+    float tmin, tmax;
+    int sp, curInst;
+    uint32_t entry, steps;
+    bool found;
+    HitRec best;
+
+    __device__ __forceinline__ void begin(const SceneGPU& S, const float3 o, const float3 d, const float t0, const float t1) {
+        Ow = O = o, Dw = D = d, tmin = t0, tmax = t1;
+        invD = make_float3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
+        best.t = t1, best.u = best.v = 0.0f, best.inst = -1, best.prim = NOHIT;
+        found = false, sp = 0, curInst = -1, steps = 0;
+        entry = S.tlasRoot;
+    }
+
+    /* returns true while the ray has work left; anyHitDone is set when an any-hit query found an occluder */
+    template <bool ANYHIT>
+    __device__ __forceinline__ bool step(const SceneGPU& S, uint32_t& status, bool& anyHitDone) {
+        if (entry == 0xffffffffu && sp == 0 && curInst < 0 && steps == 0) return false;   /* empty scene */
+        if (++steps > MAX_STEPS) { status |= LH2G_STATUS_TRAVERSAL_LIMIT; return false; }
         const uint32_t kind = entry >> 30;
         if (entry == ENTRY_MARKER) {
             O = Ow, D = Dw;
             invD = make_float3(safe_rcp(Dw.x), safe_rcp(Dw.y), safe_rcp(Dw.z));
             curInst = -1;
         } else if (kind == 0u) {
-            /* ---- interior node: test the 8 children ---- */
             const uint4* np = S.nodes + (size_t)entry * 5;
             const uint4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3), n4 = __ldg(np + 4);
             const float px = __uint_as_float(n0.x), py = __uint_as_float(n0.y), pz = __uint_as_float(n0.z);
@@ -112,22 +121,29 @@ LH2G_DEV bool trace_ray(const SceneGPU& S, const float3 Ow, const float3 Dw, con
                 }
             }
             const int nh = __popc(hitmask);
-            if (sp + nh > LH2G_STACK) { status |= LH2G_STATUS_STACK_OVERFLOW; }
+            if (sp + nh > LH2G_STACK) status |= LH2G_STATUS_STACK_OVERFLOW;
+            if (ANYHIT) {
+                /* any hit: order does not matter */
 #pragma unroll
-            for (int i = 0; i < 8; i++) {
-                if (!(hitmask & (1u << i))) continue;
-                int rank = 0;
+                for (int i = 0; i < 8; i++)
+                    if ((hitmask & (1u << i)) && sp < LH2G_STACK) stack[sp++] = make_uint2(codes[i], keys[i]);
+            } else {
+                /* closest hit: nearest child on top */
 #pragma unroll
-                for (int j = 0; j < 8; j++) {
-                    if (j == i || !(hitmask & (1u << j))) continue;
-                    rank += (keys[j] < keys[i] || (keys[j] == keys[i] && j < i)) ? 1 : 0;
+                for (int i = 0; i < 8; i++) {
+                    if (!(hitmask & (1u << i))) continue;
+                    int rank = 0;
+#pragma unroll
+                    for (int j = 0; j < 8; j++) {
+                        if (j == i || !(hitmask & (1u << j))) continue;
+                        rank += (keys[j] < keys[i] || (keys[j] == keys[i] && j < i)) ? 1 : 0;
+                    }
+                    const int slot = sp + (nh - 1 - rank);
+                    if (slot < LH2G_STACK) stack[slot] = make_uint2(codes[i], keys[i]);
                 }
-                const int slot = sp + (nh - 1 - rank);
-                if (slot < LH2G_STACK) stack[slot] = make_uint2(codes[i], keys[i]);
+                sp = min(sp + nh, LH2G_STACK);
             }
-            sp = min(sp + nh, LH2G_STACK);
         } else if (kind == 1u) {
-            /* ---- leaf: 1..3 triangles of the current instance ---- */
             const uint32_t first = entry & 0x0fffffffu, cnt = ((entry >> 28) & 3u) + 1u;
             for (uint32_t k = 0; k < cnt; k++) {
                 const float4* td = S.triData + (size_t)(first + k) * 3;
@@ -135,7 +151,7 @@ LH2G_DEV bool trace_ray(const SceneGPU& S, const float3 Ow, const float3 Dw, con
                 float t, u, v;
                 if (!isect_tri(O, D, a, b, c, t, u, v)) continue;
                 if (!(t > tmin && t < tmax)) continue;
-                if (ANYHIT) return true;
+                if (ANYHIT) { anyHitDone = true; return false; }
                 const int prim = __float_as_int(a.w);
                 if (!found || t < best.t || (t == best.t && (curInst < best.inst || (curInst == best.inst && prim < best.prim)))) {
                     best.t = t, best.u = u, best.v = v, best.inst = curInst, best.prim = prim;
@@ -143,7 +159,6 @@ LH2G_DEV bool trace_ray(const SceneGPU& S, const float3 Ow, const float3 Dw, con
                 }
             }
         } else {
-            /* ---- TLAS leaf: instance list; descend into the first, keep the rest ---- */
             const uint32_t first = entry & 0x0fffffffu, cnt = ((entry >> 28) & 3u) + 1u;
             if (cnt > 1u && sp < LH2G_STACK) stack[sp++] = make_uint2(0x80000000u | ((cnt - 2u) << 28) | (first + 1u), 0u);
             const int ii = (int)__ldg(S.tlasPrims + first);
@@ -158,16 +173,88 @@ LH2G_DEV bool trace_ray(const SceneGPU& S, const float3 Ow, const float3 Dw, con
                 curInst = ii;
                 stack[sp++] = make_uint2(ENTRY_MARKER, 0u);
                 entry = root;
-                continue;
+                return true;
             }
         }
-        /* ---- pop the next entry that can still hold a closer hit ---- */
         for (;;) {
-            if (sp == 0) return found;
+            if (sp == 0) return false;
             const uint2 e = stack[--sp];
             entry = e.x;
-            if (entry == ENTRY_MARKER || ANYHIT || (entry >> 30) == 2u) break;
-            if (!found || __uint_as_float(e.y) <= best.t) break;
+            if (entry == ENTRY_MARKER || ANYHIT || (entry >> 30) == 2u) return true;
+            if (!found || __uint_as_float(e.y) <= best.t) return true;
+        }
+    }
+};
+
+/* Single-ray form (used where lanes do not refill). */
+template <bool ANYHIT>
+LH2G_DEV bool trace_ray(const SceneGPU& S, const float3 Ow, const float3 Dw, const float tmin, const float tmax, HitRec& best, uint32_t& status) {
+    Traversal tr;
+    tr.begin(S, Ow, Dw, tmin, tmax);
+    bool any = false;
+    if (S.tlasRoot != 0xffffffffu)
+        while (tr.step<ANYHIT>(S, status, any)) {}
+    best = tr.best;
+    return ANYHIT ? any : tr.found;
+}
+
+/* Persistent, self-refilling loop of a warp: every lane traverses its own ray; a lane whose ray finished takes
+ * the next one from the queue (one atomic per warp per refill round, ballot + popc to hand out indices).
+ * fetch is a 32-bit work counter; count the number of rays; onFinish(i, tr, anyHit) writes the result. */
+template <bool ANYHIT, typename Load, typename Finish>
+LH2G_DEV void trace_queue(const SceneGPU& S, uint32_t* fetch, const uint32_t count, uint32_t& status, Load load, Finish onFinish) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t lanemask_lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lanemask_lt));
+    Traversal tr;
+    uint32_t ray = 0;
+    bool active = false, exhausted = false;
+    if (S.tlasRoot == 0xffffffffu) {
+        /* no geometry: every ray misses */
+        for (;;) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(fetch, 32u);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= count) return;
+            const uint32_t i = base + lane;
+            if (i < count) {
+                float3 o, d;
+                float t0, t1;
+                load(i, o, d, t0, t1);
+                tr.begin(S, o, d, t0, t1);
+                onFinish(i, tr, false);
+            }
+        }
+    }
+    for (;;) {
+        if (!exhausted) {
+            const uint32_t need = __ballot_sync(0xffffffffu, !active);
+            if (need) {
+                const int leader = __ffs(need) - 1;
+                uint32_t base = 0;
+                if ((int)lane == leader) base = atomicAdd(fetch, (uint32_t)__popc(need));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (base + (uint32_t)__popc(need) >= count) exhausted = true;
+                if (!active) {
+                    const uint32_t i = base + __popc(need & lanemask_lt);
+                    if (i < count) {
+                        float3 o, d;
+                        float t0, t1;
+                        load(i, o, d, t0, t1);
+                        tr.begin(S, o, d, t0, t1);
+                        ray = i;
+                        active = true;
+                    }
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) return;
+        if (active) {
+            bool anyHit = false;
+            if (!tr.step<ANYHIT>(S, status, anyHit)) {
+                onFinish(ray, tr, anyHit);
+                active = false;
+            }
         }
     }
 }

@@ -396,7 +396,7 @@ def _rotation(rng):
                      [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]], np.float64)
 
 
-def spheres_2m(seed=7, n_spheres=64, slices=160, stacks=101, tex_size=1024, with_textures=True):
+def spheres_2m(seed=7, n_spheres=64, slices=160, stacks=101, tex_size=1024, with_textures=True, sky_size=(64, 32)):
     """64 distinct noise-displaced UV spheres (32,000 tris each) over a 1000x1000 ground."""
     rng = np.random.default_rng(seed)
     s = Scene()
@@ -458,7 +458,7 @@ def spheres_2m(seed=7, n_spheres=64, slices=160, stacks=101, tex_size=1024, with
     s.point_lights = pl
     s.spot_lights = np.zeros(0, SPOT_LIGHT_DTYPE)
     s.dir_lights = np.zeros(0, DIR_LIGHT_DTYPE)
-    sw, sh = 64, 32
+    sw, sh = sky_size
     yy = (np.arange(sh) + 0.5) / sh
     sky = np.zeros((sh, sw, 3), np.float32)
     sky[..., 0] = (0.25 + 0.5 * (1 - yy))[:, None]

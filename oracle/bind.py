@@ -172,7 +172,7 @@ class RefKernels:
             raise FileNotFoundError("reference tree not available")
         self.lib = C.CDLL(REF_LIB)
         L = self.lib
-        L.ref_set_scene.argtypes = [C.c_void_p] * 2 + [C.c_void_p, C.c_int] * 4 + [C.c_void_p, C.c_float, C.c_int]
+        L.ref_set_scene.argtypes = [C.c_void_p] * 2 + [C.c_void_p, C.c_int] * 4 + [C.c_void_p, C.c_float, C.c_int, C.c_void_p, C.c_int, C.c_int]
         L.ref_generate.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_float, C.c_void_p, C.c_int, C.c_int, C.c_int]
         L.ref_shade.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -211,10 +211,16 @@ class RefKernels:
             inst[i, 4:] = inv
         packed = pack_materials(oracle, sc)
         texels = np.concatenate([t.texels for t in sc.textures]).astype(np.uint32) if sc.textures else np.zeros(16, np.uint32)
-        keep += [inst, packed, texels]
+        sky4, sw, sh = None, 0, 0
+        if sc.sky is not None:
+            rgb, sw, sh = sc.sky
+            sky4 = np.zeros((sw * sh, 4), np.float32)
+            sky4[:, :3] = np.asarray(rgb, np.float32).reshape(-1, 3)
+        keep += [inst, packed, texels, sky4]
         self._keep = keep
         L.ref_set_scene(_p(inst), _p(packed), _p(sc.tri_lights), len(sc.tri_lights), _p(sc.point_lights), len(sc.point_lights),
-                        _p(sc.spot_lights), len(sc.spot_lights), _p(sc.dir_lights), len(sc.dir_lights), _p(texels), eps, D)
+                        _p(sc.spot_lights), len(sc.spot_lights), _p(sc.dir_lights), len(sc.dir_lights), _p(texels), eps, D,
+                        _p(sky4), sw, sh)
         P = W * H * spp
         rays = [np.zeros((P, 8), np.float32), np.zeros((P, 8), np.float32)]
         ps = [np.zeros((2 * P, 4), np.float32), np.zeros((2 * P, 4), np.float32)]

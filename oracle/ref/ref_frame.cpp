@@ -98,13 +98,13 @@ extern "C" {
 
 /* scene: all pointers stay owned by the caller */
 void ref_set_scene(void* instDescs, void* mats, void* tri, int ntri, void* pt, int npt, void* spot, int nspot, void* dir, int ndir,
-                   uint32_t* texels, float geoEps, int maxPathLength) {
+                   uint32_t* texels, float geoEps, int maxPathLength, float* sky4, int skyW, int skyH) {
     instanceDescriptors = (CoreInstanceDesc*)instDescs;
     materials = (CUDAMaterial4*)mats;
     triLights = (CoreLightTri*)tri, pointLights = (CorePointLight*)pt, spotLights = (CoreSpotLight*)spot, directionalLights = (CoreDirectionalLight*)dir;
     lightCounts = make_int4(ntri, npt, nspot, ndir);
     argb32 = (uchar4*)texels;
-    skywidth = skyheight = 0, skyPixels = 0;
+    skywidth = skyW, skyheight = skyH, skyPixels = (float4*)sky4;
     geometryEpsilon = geoEps;
     MAXPATHLENGTH_RT = maxPathLength;
 }
