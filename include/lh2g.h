@@ -104,6 +104,22 @@ LH2G_API int lh2g_get_launch_times(lh2g_context* ctx, float* ms, int capacity, i
 LH2G_API int lh2g_trace(lh2g_context* ctx, const lh2g_ray* rays, void* out, long long n, int mode, void* stream);
 LH2G_API int lh2g_trace_host(lh2g_context* ctx, const lh2g_ray* rays, void* out, long long n, int mode);
 
+/* Allocation-free frame render. No counterpart in the reference (its cores always allocate their buffers).
+ * For callers that cannot call cudaMalloc when they render: a host with a fixed device-memory budget and its
+ * own allocator (a game engine or plugin host that owns all device memory), or a process that must not grow
+ * its device footprint after start-up. It renders one frame like lh2g_render_ex
+ * (same kernels, same results) with all scratch memory of the wavefront stages in a static device array
+ * compiled into the library (about 6 MB, held by every GPU that loads it until the process exits), and adds
+ * the frame's per-pixel sums to accumDevice (caller-owned device memory, width*height float4).
+ * Limit: width * height * spp <= LH2G_NOALLOC_MAX_PATHS, else LH2G_ERR_OVERFLOW. The scene comes from ctx,
+ * which must be finalized; no render target is needed. stream may be NULL (legacy default stream). The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress); make that first call before
+ * any stream capture. All calls share the array and it keeps the last call's contents: calls whose GPU work
+ * overlaps (other streams, threads or contexts on the same device) race. */
+#define LH2G_NOALLOC_MAX_PATHS 32768
+LH2G_API int lh2g_render_noalloc(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* params, float* accumDevice,
+                                 void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -745,3 +745,15 @@ int lh2g_trace_host(lh2g_context* ctx, const lh2g_ray* rays, void* out, long lon
 
 }  // extern "C"
 
+namespace lh2g {
+/* Scene and persistent-grid sizes of a finalized context (for the allocation-free render in noalloc.cu). */
+int context_scene(lh2g_context* ctx, SceneGPU* scene, int* device, int* blocks3) {
+    if (!ctx || !scene || !device || !blocks3) return LH2G_ERR_INVALID;
+    if (!ctx->finalized) return fail(ctx, LH2G_ERR_STATE, "render: scene not finalized (call lh2g_finalize_instances)");
+    if (!ctx->mats) return fail(ctx, LH2G_ERR_STATE, "render: no materials");
+    *scene = scene_of(ctx);
+    *device = ctx->device;
+    blocks3[0] = ctx->blocksExtend, blocks3[1] = ctx->blocksConnect, blocks3[2] = ctx->blocksShade;
+    return LH2G_OK;
+}
+}  // namespace lh2g
