@@ -211,12 +211,17 @@ def run_gb300(args):
     rays = 0
     per_kind = {"extend": [0.0, 0, 0], "shade": [0.0, 0, 0], "connect": [0.0, 0, 0], "generate": [0.0, 0, 0], "finalize": [0.0, 0, 0]}
     launches = 0
+    trav = np.zeros(4, np.float64)
+    ext_rays = shadow_rays = 0
     for k in range(args.steps):
         out = core.render_ex(*frames[k % 8], counters=True)   # counters: the per-depth queue sizes of this frame
         c = out["counters"]
         n_in = [W * H] + [int(x) for x in c[:-1, 0]]
         rays += W * H + int(c[:, 0].sum()) + int(c[:, 1].sum())
         lt = [float(x) for x in core.launch_times()]
+        trav += core.traversal_stats()
+        ext_rays += W * H + int(c[:-1, 0].sum())
+        shadow_rays += int(c[:, 1].sum())
         launches += len(lt)
         per_kind["generate"][0] += lt[0]
         per_kind["finalize"][0] += lt[-1]
@@ -275,7 +280,11 @@ def run_gb300(args):
                        "bvh_build_ms": round(build_ms, 2), "scene_generation_s": round(gen_s, 1),
                        "rays_per_frame": rays / args.steps / world,
                        "kernel_ms_per_frame": {k: round(v[0] / args.steps, 4) for k, v in per_kind.items()},
-                       "kernel_share": {k: round(v[0] / frame_ms, 4) for k, v in per_kind.items()}},
+                       "kernel_share": {k: round(v[0] / frame_ms, 4) for k, v in per_kind.items()},
+                       "traversal": {"closest_nodes_per_ray": trav[0] / max(ext_rays, 1), "closest_tris_per_ray": trav[1] / max(ext_rays, 1),
+                                     "any_nodes_per_ray": trav[2] / max(shadow_rays, 1), "any_tris_per_ray": trav[3] / max(shadow_rays, 1),
+                                     "traversal_bytes_per_closest_ray": (trav[0] * 80 + trav[1] * 48) / max(ext_rays, 1),
+                                     "extend_traversal_GBps": (trav[0] * 80 + trav[1] * 48) / max(per_kind["extend"][0], 1e-9) / 1e6}},
             "roofline": {"kernel": "k_" + dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                          "note": "traversal/shading are latency and issue bound; algorithmic bytes count queue traffic only"},

@@ -96,6 +96,10 @@ LH2G_API int lh2g_get_stream(lh2g_context* ctx, void** stream);
 LH2G_API int lh2g_enable_launch_timing(lh2g_context* ctx, int enable);
 LH2G_API int lh2g_get_launch_times(lh2g_context* ctx, float* ms, int capacity, int* count);
 
+/* Traversal work of the last frame: out[0..3] = interior nodes visited and triangles tested by the closest-hit
+ * (extend) stage, then by the any-hit (connect) stage. */
+LH2G_API int lh2g_get_traversal_stats(lh2g_context* ctx, unsigned long long* out4);
+
 /* Ray queries over the scene (the OptiX Prime query interface of lib/RenderCore_PrimeRef/rendercore.cpp:569-605,
  * formats RTP_BUFFER_FORMAT_RAY_ORIGIN_TMIN_DIRECTION_TMAX / hit float4 {u|v<<16, inst, prim, t}).
  * mode 0: closest hit into lh2g_hit[n] (prim = -1 on a miss); mode 1: any hit into uint32 occluded[n].

@@ -35,7 +35,7 @@ C_API = ["lh2g_create", "lh2g_destroy", "lh2g_last_error", "lh2g_set_geometry", 
          "lh2g_set_materials", "lh2g_pack_materials", "lh2g_set_textures", "lh2g_set_lights", "lh2g_set_sky", "lh2g_setting",
          "lh2g_set_target", "lh2g_set_probe", "lh2g_render", "lh2g_render_ex", "lh2g_wait", "lh2g_get_stats",
          "lh2g_get_framebuffer", "lh2g_read_framebuffer", "lh2g_read_accumulator", "lh2g_trace", "lh2g_trace_host",
-         "lh2g_get_stream", "lh2g_enable_launch_timing", "lh2g_get_launch_times"]
+         "lh2g_get_stream", "lh2g_enable_launch_timing", "lh2g_get_launch_times", "lh2g_get_traversal_stats"]
 
 _lib = None
 
@@ -81,6 +81,7 @@ def load_library(path: str | None = None):
     lib.lh2g_get_stream.argtypes = [vp, C.POINTER(vp)]
     lib.lh2g_enable_launch_timing.argtypes = [vp, i]
     lib.lh2g_get_launch_times.argtypes = [vp, vp, i, C.POINTER(i)]
+    lib.lh2g_get_traversal_stats.argtypes = [vp, vp]
     if path is None:
         _lib = lib
     return lib
@@ -258,6 +259,11 @@ class RenderCore:
         n = C.c_int(0)
         self._check(self.lib.lh2g_get_launch_times(self.ctx, _p(buf), len(buf), C.byref(n)), "get_launch_times")
         return buf[:n.value].copy()
+
+    def traversal_stats(self):
+        out = np.zeros(4, np.uint64)
+        self._check(self.lib.lh2g_get_traversal_stats(self.ctx, _p(out)), "get_traversal_stats")
+        return out
 
     def read_framebuffer_into(self, host_ptr):
         self._check(self.lib.lh2g_read_framebuffer(self.ctx, C.c_void_p(host_ptr)), "read_framebuffer")

@@ -679,6 +679,13 @@ int lh2g_read_accumulator(lh2g_context* ctx, float* host) {
     return LH2G_OK;
 }
 
+int lh2g_get_traversal_stats(lh2g_context* ctx, unsigned long long* out4) {
+    if (!ctx || !out4) return LH2G_ERR_INVALID;
+    CK(cudaStreamSynchronize(ctx->st));
+    for (int k = 0; k < 4; k++) out4[k] = ctx->hostCounters->travStats[k];
+    return LH2G_OK;
+}
+
 int lh2g_get_stream(lh2g_context* ctx, void** stream) {
     if (!ctx || !stream) return LH2G_ERR_INVALID;
     *stream = (void*)ctx->st;

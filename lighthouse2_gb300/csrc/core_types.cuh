@@ -83,6 +83,7 @@ struct Counters {
     uint32_t status;
     uint32_t probeInst, probePrim;
     float probeDist;
+    unsigned long long travStats[4];   /* extend: nodes, triangles; connect: nodes, triangles */
 };
 
 #define LH2G_STATUS_STACK_OVERFLOW 1u

@@ -68,23 +68,27 @@ __global__ void __launch_bounds__(128) k_extend(const SceneGPU S, const FrameGPU
     const float4* __restrict__ D4 = B.D[q];
     const float4* __restrict__ T4 = B.T[q];
     uint32_t status = 0;
-    trace_queue<false>(S, &C->fetch[depth - 1], count, status,
+    __shared__ uint2 stackBase[LH2G_COOP ? 128 / COOP * COOP_STACK : 1];
+    auto write = [&](uint32_t i, bool found, const HitRec& best) {
+        float4 rec;
+        if (found) rec = make_float4(__uint_as_float(f2u(65535.0f * best.u) + (f2u(65535.0f * best.v) << 16)), __int_as_float(best.inst),
+                                     __int_as_float(best.prim), best.t);
+        else rec = make_float4(__uint_as_float(0u), __int_as_float(0), __int_as_float(NOHIT), 1e34f);
+        B.hits[i] = rec;
+        if (B.capHits) {
+            const uint32_t pathIdx = __float_as_uint(O4[i].w);
+            lh2g_hit c;
+            c.bary = __float_as_uint(rec.x), c.inst = __float_as_int(rec.y), c.prim = __float_as_int(rec.z), c.t = rec.w;
+            B.capHits[(size_t)(depth - 1) * F.P + pathIdx] = c;
+        }
+    };
+    trace_queue_any<false>(S, &C->fetch[depth - 1], count, status, stackBase,
         [&](uint32_t i, float3& o, float3& d, float& t0, float& t1) {
             o = xyz(O4[i]), d = xyz(D4[i]), t0 = T4[i].w, t1 = 1e34f;
         },
-        [&](uint32_t i, const Traversal& tr, bool) {
-            float4 rec;
-            if (tr.found) rec = make_float4(__uint_as_float(f2u(65535.0f * tr.best.u) + (f2u(65535.0f * tr.best.v) << 16)), __int_as_float(tr.best.inst),
-                                            __int_as_float(tr.best.prim), tr.best.t);
-            else rec = make_float4(__uint_as_float(0u), __int_as_float(0), __int_as_float(NOHIT), 1e34f);
-            B.hits[i] = rec;
-            if (B.capHits) {
-                const uint32_t pathIdx = __float_as_uint(O4[i].w);
-                lh2g_hit c;
-                c.bary = __float_as_uint(rec.x), c.inst = __float_as_int(rec.y), c.prim = __float_as_int(rec.z), c.t = rec.w;
-                B.capHits[(size_t)(depth - 1) * F.P + pathIdx] = c;
-            }
-        });
+        [&](uint32_t i, const Traversal& tr, bool) { write(i, tr.found, tr.best); },
+        [&](uint32_t i, const CoopRay& tr, bool) { if ((threadIdx.x & (COOP - 1)) == 0) write(i, tr.found, tr.best); },
+        C->travStats);
     if (status) atomicOr(&C->status, status);
 }
 
@@ -95,7 +99,8 @@ struct ShadeOut {
     float4 sO, sD, sE;
 };
 
-__device__ __forceinline__ void shade_path(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, const int depth, const uint32_t i, ShadeOut& out) {
+__device__ __forceinline__ void shade_path(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, const int depth, const uint32_t i, ShadeOut& out,
+                                           float* pot) {
     const int q = (depth - 1) & 1;
     const float4 o4 = B.O[q][i], d4 = B.D[q][i], t4 = B.T[q][i], hit = B.hits[i];
     const uint32_t pathIdx = __float_as_uint(o4.w);
@@ -134,9 +139,6 @@ __device__ __forceinline__ void shade_path(const SceneGPU& S, const FrameGPU& F,
         if (B.capSeeds) B.capSeeds[capIdx] = 0;
         return;
     }
-    if (depth == 1 && B.counters) {
-        /* probe: nothing to do here unless requested; kept out of the hot path */
-    }
     B.pathAcc[pathIdx] = acc;
     if (ROUGHNESS(sd) <= 0.001f || TRANSMISSION(sd) > 0.999f) FLAGS |= S_SPECULAR; else FLAGS &= ~S_SPECULAR;
     uint32_t seed = WangHash(pathIdx * 17u + R0);
@@ -146,7 +148,7 @@ __device__ __forceinline__ void shade_path(const SceneGPU& S, const FrameGPU& F,
         const float q0 = RandomFloat(seed), q1 = RandomFloat(seed);
         float pickProb = 0, lightPdf = 0;
         float3 lightColor = mk3(0);
-        float3 L = RandomPointOnLight(S, q0, q1, I, fN * faceDir, pickProb, lightPdf, lightColor) - I;
+        float3 L = RandomPointOnLight(S, q0, q1, I, fN * faceDir, pickProb, lightPdf, lightColor, pot, WAVE_BLOCK) - I;
         const float dist = length(L);
         L = L * (1.0f / dist);
         const float NdotL = dot(L, fN * faceDir);
@@ -185,11 +187,12 @@ __global__ void __launch_bounds__(WAVE_BLOCK) k_shade(const SceneGPU S, const Fr
     const int nq = depth & 1;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t stride = gridDim.x * blockDim.x;
+    __shared__ float potential[64 * WAVE_BLOCK];   /* light-selection potentials, 64 lights x 128 threads */
     for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += stride) {
         const uint32_t i = base + threadIdx.x;
         ShadeOut out;
         out.ext = out.shadow = false;
-        if (i < count) shade_path(S, F, B, depth, i, out);
+        if (i < count) shade_path(S, F, B, depth, i, out, potential + threadIdx.x);
         const uint32_t em = __ballot_sync(0xffffffffu, out.ext);
         if (em) {
             const int leader = __ffs(em) - 1;
@@ -214,19 +217,22 @@ __global__ void __launch_bounds__(128) k_connect(const SceneGPU S, const FrameGP
     Counters* C = B.counters;
     const uint32_t count = C->shadow[depth - 1];
     uint32_t status = 0;
-    trace_queue<true>(S, &C->fetch[64 + depth - 1], count, status,
+    __shared__ uint2 stackBase[LH2G_COOP ? 128 / COOP * COOP_STACK : 1];
+    auto add = [&](uint32_t i) {
+        const float4 e = B.shE[i];
+        const uint32_t pathIdx = __float_as_uint(B.shO[i].w);
+        float4 acc = B.pathAcc[pathIdx];
+        acc.x += e.x, acc.y += e.y, acc.z += e.z;
+        B.pathAcc[pathIdx] = acc;
+    };
+    trace_queue_any<true>(S, &C->fetch[64 + depth - 1], count, status, stackBase,
         [&](uint32_t i, float3& o, float3& d, float& t0, float& t1) {
             const float4 d4 = B.shD[i];
             o = xyz(B.shO[i]), d = xyz(d4), t0 = 0.0f, t1 = d4.w;
         },
-        [&](uint32_t i, const Traversal&, bool occluded) {
-            if (occluded) return;
-            const float4 e = B.shE[i];
-            const uint32_t pathIdx = __float_as_uint(B.shO[i].w);
-            float4 acc = B.pathAcc[pathIdx];
-            acc.x += e.x, acc.y += e.y, acc.z += e.z;
-            B.pathAcc[pathIdx] = acc;
-        });
+        [&](uint32_t i, const Traversal&, bool occluded) { if (!occluded) add(i); },
+        [&](uint32_t i, const CoopRay&, bool occluded) { if (!occluded && (threadIdx.x & (COOP - 1)) == 0) add(i); },
+        C->travStats + 2);
     if (status) atomicOr(&C->status, status);
 }
 
@@ -249,23 +255,27 @@ template <int MODE>
 __global__ void __launch_bounds__(128) k_trace(const SceneGPU S, const lh2g_ray* __restrict__ rays, void* __restrict__ out, const long long n,
                                                uint32_t* fetch, uint32_t* statusOut) {
     uint32_t status = 0;
-    /* queries of more than 2^32 - 2^16 rays are processed in chunks by the host */
-    trace_queue<MODE == 1>(S, fetch, (uint32_t)n, status,
+    __shared__ uint2 stackBase[LH2G_COOP ? 128 / COOP * COOP_STACK : 1];
+    auto write = [&](uint32_t i, bool found, const HitRec& best, bool any) {
+        if (MODE == 1) ((uint32_t*)out)[i] = any ? 1u : 0u;
+        else {
+            uint4 rec;
+            if (found) rec = make_uint4(f2u(65535.0f * best.u) + (f2u(65535.0f * best.v) << 16), (uint32_t)best.inst, (uint32_t)best.prim,
+                                        __float_as_uint(best.t));
+            else rec = make_uint4(0u, 0u, (uint32_t)NOHIT, __float_as_uint(1e34f));
+            ((uint4*)out)[i] = rec;
+        }
+    };
+    /* queries of more than 2^31 rays are processed in chunks by the host */
+    trace_queue_any<MODE == 1>(S, fetch, (uint32_t)n, status, stackBase,
         [&](uint32_t i, float3& o, float3& d, float& t0, float& t1) {
             const float4* r = (const float4*)(rays + i);
             const float4 a = __ldg(r), b = __ldg(r + 1);
             o = xyz(a), d = xyz(b), t0 = a.w, t1 = b.w;
         },
-        [&](uint32_t i, const Traversal& tr, bool any) {
-            if (MODE == 1) ((uint32_t*)out)[i] = any ? 1u : 0u;
-            else {
-                uint4 rec;
-                if (tr.found) rec = make_uint4(f2u(65535.0f * tr.best.u) + (f2u(65535.0f * tr.best.v) << 16), (uint32_t)tr.best.inst, (uint32_t)tr.best.prim,
-                                               __float_as_uint(tr.best.t));
-                else rec = make_uint4(0u, 0u, (uint32_t)NOHIT, __float_as_uint(1e34f));
-                ((uint4*)out)[i] = rec;
-            }
-        });
+        [&](uint32_t i, const Traversal& tr, bool any) { write(i, tr.found, tr.best, any); },
+        [&](uint32_t i, const CoopRay& tr, bool any) { if ((threadIdx.x & (COOP - 1)) == 0) write(i, tr.found, tr.best, any); },
+        nullptr);
     if (status) atomicOr(statusOut, status);
 }
 

@@ -287,20 +287,27 @@ LH2G_DEV float Potential(const SceneGPU& S, int i, const float3& I, const float3
     return PotentialDir(S, i - S.nSpot, N);
 }
 
-LH2G_DEV float3 RandomPointOnLight(const SceneGPU& S, float r0, float r1, const float3& I, const float3& N, float& pickProb, float& lightPdf, float3& lightColor) {
+/* pot: this thread's slice of a potential array (entry i at pot[i * stride]), as the reference's local
+ * potential[MAXISLIGHTS] array (lights_shared.h:232); it lives in shared memory. */
+LH2G_DEV float3 RandomPointOnLight(const SceneGPU& S, float r0, float r1, const float3& I, const float3& N, float& pickProb, float& lightPdf, float3& lightColor,
+                                   float* pot, const int stride) {
     const int lights = S.nTri + S.nPoint + S.nSpot + S.nDir;
     const float lightCount = (float)lights;
     const float3 bary = RandomBarycentrics(r0);
     float sum = 0, total = 0;
     int lightIdx = 0;
-    for (int i = 0; i < lights; i++) sum += Potential(S, i, I, N, bary);
+    for (int i = 0; i < lights; i++) {
+        const float c = Potential(S, i, I, N, bary);
+        pot[i * stride] = c;
+        sum += c;
+    }
     if (sum <= 0) { lightPdf = 0; return mk3(1); }
     r1 *= sum;
     for (int i = 0; i < lights; i++) {
-        total += Potential(S, i, I, N, bary);
+        total += pot[i * stride];
         if (total >= r1) { lightIdx = i; break; }
     }
-    pickProb = Potential(S, lightIdx, I, N, bary) / sum;
+    pickProb = pot[lightIdx * stride] / sum;
     lightIdx = max(0, min(lightIdx, f2i(lightCount) - 1));
     if (lightIdx < S.nTri) {
         const float4* l = S.triLights + (size_t)lightIdx * 6;

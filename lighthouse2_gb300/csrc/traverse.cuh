@@ -20,6 +20,19 @@ namespace lh2g {
 #ifndef LH2G_STACK
 #define LH2G_STACK 80
 #endif
+/* Traversal strategy (tuning switches, all give identical results):
+ *   LH2G_COOP        1: 8 lanes per ray (warp-cooperative), 0: one lane per ray
+ *   LH2G_WHILE_WHILE 1: a lane descends interior nodes until it holds a leaf before leaf work; 0: one entry per step
+ *   LH2G_REFILL      1: a lane takes a new ray as soon as its ray finishes; 0: a warp takes 32 rays at a time */
+#ifndef LH2G_COOP
+#define LH2G_COOP 0
+#endif
+#ifndef LH2G_WHILE_WHILE
+#define LH2G_WHILE_WHILE 0
+#endif
+#ifndef LH2G_REFILL
+#define LH2G_REFILL 0
+#endif
 constexpr float BOX_MARGIN = 1.52587890625e-05f;
 constexpr uint32_t ENTRY_MARKER = 0xffffffffu;
 constexpr uint32_t MAX_STEPS = 1u << 20;   /* far beyond any traversal of a well-formed tree */
@@ -55,15 +68,19 @@ LH2G_DEV bool isect_tri(const float3 O, const float3 D, const float4 a, const fl
 
 LH2G_DEV uint32_t byte_of(uint32_t w0, uint32_t w1, int i) { return ((i < 4 ? w0 : w1) >> ((i & 3) * 8)) & 255u; }
 
-/* Resumable traversal state of one ray (one lane). step() processes the current stack entry and pops the
- * next one; it returns false once the ray is finished. Kernels interleave step() with per-lane refills of
- * finished rays, so a warp keeps all lanes busy instead of waiting for its slowest ray. */
+/* Compare-exchange for the sorting network. */
+LH2G_DEV void cx(uint32_t& a, uint32_t& b) { const uint32_t lo = min(a, b), hi = max(a, b); a = lo, b = hi; }
+
+/* Resumable traversal state of one ray (one lane). step() runs the interior-node loop until the lane holds a
+ * leaf, an instance or a return marker (so a warp executes node work and leaf work in separate phases), handles
+ * that entry and pops the next; it returns false once the ray is finished. Kernels interleave step() with
+ * per-lane refills of finished rays. */
 struct Traversal {
     uint2 stack[LH2G_STACK];
     float3 Ow, Dw, O, D, invD;
     float tmin, tmax;
     int sp, curInst;
-    uint32_t entry, steps;
+    uint32_t entry, steps, nodes, tris;
     bool found;
     HitRec best;
 
@@ -71,84 +88,115 @@ struct Traversal {
         Ow = O = o, Dw = D = d, tmin = t0, tmax = t1;
         invD = make_float3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
         best.t = t1, best.u = best.v = 0.0f, best.inst = -1, best.prim = NOHIT;
-        found = false, sp = 0, curInst = -1, steps = 0;
+        found = false, sp = 0, curInst = -1, steps = 0, nodes = 0, tris = 0;
         entry = S.tlasRoot;
+    }
+
+    /* pops the next entry that can still hold a closer hit; false when the stack is empty */
+    template <bool ANYHIT>
+    __device__ __forceinline__ bool pop() {
+        for (;;) {
+            if (sp == 0) return false;
+            const uint2 e = stack[--sp];
+            entry = e.x;
+            if (entry == ENTRY_MARKER || ANYHIT || (entry >> 30) == 2u) return true;
+            if (!found || __uint_as_float(e.y) <= best.t) return true;
+        }
+    }
+
+    /* tests the 8 children of interior node `entry` and pushes the hit ones, nearest on top */
+    template <bool ANYHIT>
+    __device__ __forceinline__ void visit_node(const SceneGPU& S, uint32_t& status) {
+        const uint4* np = S.nodes + (size_t)entry * 5;
+        const uint4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3), n4 = __ldg(np + 4);
+        /* slab distances in the form t(q) = q * a + b, a = 2^e * invD (exact), b = (p - O) * invD */
+        const float ax = __uint_as_float((n0.w & 255u) << 23) * invD.x, ay = __uint_as_float(((n0.w >> 8) & 255u) << 23) * invD.y,
+                    az = __uint_as_float(((n0.w >> 16) & 255u) << 23) * invD.z;
+        const float bx = (__uint_as_float(n0.x) - O.x) * invD.x, by = (__uint_as_float(n0.y) - O.y) * invD.y,
+                    bz = (__uint_as_float(n0.z) - O.z) * invD.z;
+        /* absolute rounding bound of the three distances (a few ulp of the operands, taken with margin 2^-20) */
+        const float err = (fmaxf(fmaxf(fabsf(bx), fabsf(by)), fabsf(bz)) + 255.0f * fmaxf(fmaxf(fabsf(ax), fabsf(ay)), fabsf(az))) * 9.5367431640625e-07f;
+        /* near / far plane words per axis, swapped for negative directions */
+        const bool nx = invD.x < 0.0f, ny = invD.y < 0.0f, nz = invD.z < 0.0f;
+        const uint32_t nlx0 = nx ? n3.z : n2.x, nlx1 = nx ? n3.w : n2.y, nhx0 = nx ? n2.x : n3.z, nhx1 = nx ? n2.y : n3.w;
+        const uint32_t nly0 = ny ? n4.x : n2.z, nly1 = ny ? n4.y : n2.w, nhy0 = ny ? n2.z : n4.x, nhy1 = ny ? n2.w : n4.y;
+        const uint32_t nlz0 = nz ? n4.z : n3.x, nlz1 = nz ? n4.w : n3.y, nhz0 = nz ? n3.x : n4.z, nhz1 = nz ? n3.y : n4.w;
+        const float limit = (!ANYHIT && found) ? best.t : tmax;
+        uint32_t key[8];
+        const uint32_t metaLo = n1.z, metaHi = n1.w;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const uint32_t sel = 0x4440u | (uint32_t)(i & 3);
+            const uint32_t meta = __byte_perm(i < 4 ? metaLo : metaHi, 0u, sel);
+            const float txn = fmaf((float)__byte_perm(i < 4 ? nlx0 : nlx1, 0u, sel), ax, bx);
+            const float txf = fmaf((float)__byte_perm(i < 4 ? nhx0 : nhx1, 0u, sel), ax, bx);
+            const float tyn = fmaf((float)__byte_perm(i < 4 ? nly0 : nly1, 0u, sel), ay, by);
+            const float tyf = fmaf((float)__byte_perm(i < 4 ? nhy0 : nhy1, 0u, sel), ay, by);
+            const float tzn = fmaf((float)__byte_perm(i < 4 ? nlz0 : nlz1, 0u, sel), az, bz);
+            const float tzf = fmaf((float)__byte_perm(i < 4 ? nhz0 : nhz1, 0u, sel), az, bz);
+            float tn = fmaxf(fmaxf(txn, tyn), tzn);
+            float tf = fminf(fminf(txf, tyf), tzf);
+            tn = fmaf(-fabsf(tn), BOX_MARGIN, tn) - err;
+            tf = fmaf(fabsf(tf), BOX_MARGIN, tf) + err;
+            tn = fmaxf(tn, tmin);
+            tf = fminf(tf, limit);
+            const bool hit = meta != 0u && tn <= tf;
+            /* key: distance with the low 3 bits replaced by the slot (rounded down: culling stays conservative) */
+            key[i] = hit ? ((__float_as_uint(fmaxf(tn, 0.0f)) & ~7u) | (uint32_t)i) : 0xffffffffu;
+        }
+        if (!ANYHIT) {
+            cx(key[0], key[1]), cx(key[2], key[3]), cx(key[4], key[5]), cx(key[6], key[7]);
+            cx(key[0], key[2]), cx(key[1], key[3]), cx(key[4], key[6]), cx(key[5], key[7]);
+            cx(key[1], key[2]), cx(key[5], key[6]);
+            cx(key[0], key[4]), cx(key[1], key[5]), cx(key[2], key[6]), cx(key[3], key[7]);
+            cx(key[2], key[4]), cx(key[3], key[5]);
+            cx(key[1], key[2]), cx(key[3], key[4]), cx(key[5], key[6]);
+        }
+#pragma unroll
+        for (int k = 7; k >= 0; k--) {
+            const uint32_t kk = key[k];
+            if (kk == 0xffffffffu) continue;
+            const uint32_t slot = kk & 7u;
+            const uint32_t meta = ((slot < 4 ? metaLo : metaHi) >> ((slot & 3u) * 8u)) & 255u;
+            uint32_t code;
+            if (meta & 0x80u) code = n1.x + (meta & 7u);
+            else code = (curInst < 0 ? 0x80000000u : 0x40000000u) | (((meta >> 5) - 1u) << 28) | (n1.y + (meta & 31u));
+            if (sp < LH2G_STACK) stack[sp++] = make_uint2(code, kk & ~7u);
+            else status |= LH2G_STATUS_STACK_OVERFLOW;
+        }
+        nodes++;
     }
 
     /* returns true while the ray has work left; anyHitDone is set when an any-hit query found an occluder */
     template <bool ANYHIT>
     __device__ __forceinline__ bool step(const SceneGPU& S, uint32_t& status, bool& anyHitDone) {
-        if (entry == 0xffffffffu && sp == 0 && curInst < 0 && steps == 0) return false;   /* empty scene */
+#if LH2G_WHILE_WHILE
+        /* node phase: descend until the current entry is a leaf, an instance or a marker */
+        while ((entry >> 30) == 0u) {
+            if (++steps > MAX_STEPS) { status |= LH2G_STATUS_TRAVERSAL_LIMIT; return false; }
+            visit_node<ANYHIT>(S, status);
+            if (!pop<ANYHIT>()) return false;
+        }
+#else
+        if ((entry >> 30) == 0u) {
+            if (++steps > MAX_STEPS) { status |= LH2G_STATUS_TRAVERSAL_LIMIT; return false; }
+            visit_node<ANYHIT>(S, status);
+            return pop<ANYHIT>();
+        }
+#endif
         if (++steps > MAX_STEPS) { status |= LH2G_STATUS_TRAVERSAL_LIMIT; return false; }
         const uint32_t kind = entry >> 30;
         if (entry == ENTRY_MARKER) {
             O = Ow, D = Dw;
             invD = make_float3(safe_rcp(Dw.x), safe_rcp(Dw.y), safe_rcp(Dw.z));
             curInst = -1;
-        } else if (kind == 0u) {
-            const uint4* np = S.nodes + (size_t)entry * 5;
-            const uint4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3), n4 = __ldg(np + 4);
-            const float px = __uint_as_float(n0.x), py = __uint_as_float(n0.y), pz = __uint_as_float(n0.z);
-            const float sx = __uint_as_float((n0.w & 255u) << 23), sy = __uint_as_float(((n0.w >> 8) & 255u) << 23),
-                        sz = __uint_as_float(((n0.w >> 16) & 255u) << 23);
-            const float limit = (!ANYHIT && found) ? best.t : tmax;
-            uint32_t keys[8], codes[8];
-            uint32_t hitmask = 0;
-#pragma unroll
-            for (int i = 0; i < 8; i++) {
-                const uint32_t meta = byte_of(n1.z, n1.w, i);
-                keys[i] = 0xffffffffu, codes[i] = 0;
-                if (meta == 0u) continue;
-                const float lx = fmaf((float)byte_of(n2.x, n2.y, i), sx, px), hx = fmaf((float)byte_of(n3.z, n3.w, i), sx, px);
-                const float ly = fmaf((float)byte_of(n2.z, n2.w, i), sy, py), hy = fmaf((float)byte_of(n4.x, n4.y, i), sy, py);
-                const float lz = fmaf((float)byte_of(n3.x, n3.y, i), sz, pz), hz = fmaf((float)byte_of(n4.z, n4.w, i), sz, pz);
-                const float tx0 = (lx - O.x) * invD.x, tx1 = (hx - O.x) * invD.x;
-                const float ty0 = (ly - O.y) * invD.y, ty1 = (hy - O.y) * invD.y;
-                const float tz0 = (lz - O.z) * invD.z, tz1 = (hz - O.z) * invD.z;
-                float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
-                float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
-                tn = fmaf(-fabsf(tn), BOX_MARGIN, tn);
-                tf = fmaf(fabsf(tf), BOX_MARGIN, tf);
-                tn = fmaxf(tn, tmin);
-                tf = fminf(tf, limit);
-                if (!(tn <= tf)) continue;
-                hitmask |= 1u << i;
-                keys[i] = __float_as_uint(fmaxf(tn, 0.0f));
-                if (meta & 0x80u) codes[i] = n1.x + (meta & 7u);
-                else {
-                    const uint32_t first = n1.y + (meta & 31u), cnt = meta >> 5;
-                    codes[i] = (curInst < 0 ? 0x80000000u : 0x40000000u) | ((cnt - 1u) << 28) | first;
-                }
-            }
-            const int nh = __popc(hitmask);
-            if (sp + nh > LH2G_STACK) status |= LH2G_STATUS_STACK_OVERFLOW;
-            if (ANYHIT) {
-                /* any hit: order does not matter */
-#pragma unroll
-                for (int i = 0; i < 8; i++)
-                    if ((hitmask & (1u << i)) && sp < LH2G_STACK) stack[sp++] = make_uint2(codes[i], keys[i]);
-            } else {
-                /* closest hit: nearest child on top */
-#pragma unroll
-                for (int i = 0; i < 8; i++) {
-                    if (!(hitmask & (1u << i))) continue;
-                    int rank = 0;
-#pragma unroll
-                    for (int j = 0; j < 8; j++) {
-                        if (j == i || !(hitmask & (1u << j))) continue;
-                        rank += (keys[j] < keys[i] || (keys[j] == keys[i] && j < i)) ? 1 : 0;
-                    }
-                    const int slot = sp + (nh - 1 - rank);
-                    if (slot < LH2G_STACK) stack[slot] = make_uint2(codes[i], keys[i]);
-                }
-                sp = min(sp + nh, LH2G_STACK);
-            }
         } else if (kind == 1u) {
             const uint32_t first = entry & 0x0fffffffu, cnt = ((entry >> 28) & 3u) + 1u;
             for (uint32_t k = 0; k < cnt; k++) {
                 const float4* td = S.triData + (size_t)(first + k) * 3;
                 const float4 a = __ldg(td), b = __ldg(td + 1), c = __ldg(td + 2);
                 float t, u, v;
+                tris++;
                 if (!isect_tri(O, D, a, b, c, t, u, v)) continue;
                 if (!(t > tmin && t < tmax)) continue;
                 if (ANYHIT) { anyHitDone = true; return false; }
@@ -176,15 +224,199 @@ struct Traversal {
                 return true;
             }
         }
-        for (;;) {
-            if (sp == 0) return false;
-            const uint2 e = stack[--sp];
-            entry = e.x;
-            if (entry == ENTRY_MARKER || ANYHIT || (entry >> 30) == 2u) return true;
-            if (!found || __uint_as_float(e.y) <= best.t) return true;
-        }
+        return pop<ANYHIT>();
     }
 };
+
+/* ======================================================================================================
+ * Warp-cooperative traversal: a group of 8 lanes traces one ray, lane g testing child slot g of the current
+ * 8-wide node (and triangle g of a leaf). The ray state is replicated in the group's lanes (identical
+ * arithmetic, so all 8 copies agree and the group's control flow is uniform); the stack is shared by the group
+ * and lives in shared memory. A finished group takes the next ray from the queue (one atomic per group).
+ * ==================================================================================================== */
+constexpr int COOP = 8;                      /* lanes per ray */
+constexpr int COOP_STACK = 64;               /* shared-memory stack entries per group */
+
+struct CoopRay {
+    float3 Ow, Dw, O, D, invD, invDw;
+    float tmin, tmax;
+    int sp, curInst;
+    uint32_t entry, steps, nodes, tris;
+    bool found;
+    HitRec best;
+};
+
+template <bool ANYHIT>
+LH2G_DEV bool coop_pop(CoopRay& r, const uint2* stk) {
+    for (;;) {
+        if (r.sp == 0) return false;
+        const uint2 e = stk[--r.sp];
+        r.entry = e.x;
+        if (e.x == ENTRY_MARKER || ANYHIT || (e.x >> 30) == 2u) return true;
+        if (!r.found || __uint_as_float(e.y) <= r.best.t) return true;
+    }
+}
+
+/* One entry of the group's ray. g = lane within the group, gmask = the group's lanes. Returns false when the ray
+ * is finished (anyHit set when an any-hit query found an occluder). */
+template <bool ANYHIT>
+LH2G_DEV bool coop_step(const SceneGPU& S, CoopRay& r, uint2* stk, const int g, const uint32_t gmask, uint32_t& status, bool& anyHit) {
+    if (++r.steps > MAX_STEPS) { status |= LH2G_STATUS_TRAVERSAL_LIMIT; return false; }
+    const uint32_t entry = r.entry, kind = entry >> 30;
+    if (entry == ENTRY_MARKER) {
+        r.O = r.Ow, r.D = r.Dw, r.invD = r.invDw, r.curInst = -1;
+    } else if (kind == 0u) {
+        const uint4* np = S.nodes + (size_t)entry * 5;
+        const uint4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3), n4 = __ldg(np + 4);
+        const float3 invD = r.invD, O = r.O;
+        const float ax = __uint_as_float((n0.w & 255u) << 23) * invD.x, ay = __uint_as_float(((n0.w >> 8) & 255u) << 23) * invD.y,
+                    az = __uint_as_float(((n0.w >> 16) & 255u) << 23) * invD.z;
+        const float bx = (__uint_as_float(n0.x) - O.x) * invD.x, by = (__uint_as_float(n0.y) - O.y) * invD.y,
+                    bz = (__uint_as_float(n0.z) - O.z) * invD.z;
+        const float err = (fmaxf(fmaxf(fabsf(bx), fabsf(by)), fabsf(bz)) + 255.0f * fmaxf(fmaxf(fabsf(ax), fabsf(ay)), fabsf(az))) * 9.5367431640625e-07f;
+        const uint32_t sel = 0x4440u | (uint32_t)(g & 3), hi = g >= 4;
+        const uint32_t meta = __byte_perm(hi ? n1.w : n1.z, 0u, sel);
+        const float qlx = (float)__byte_perm(hi ? n2.y : n2.x, 0u, sel), qhx = (float)__byte_perm(hi ? n3.w : n3.z, 0u, sel);
+        const float qly = (float)__byte_perm(hi ? n2.w : n2.z, 0u, sel), qhy = (float)__byte_perm(hi ? n4.y : n4.x, 0u, sel);
+        const float qlz = (float)__byte_perm(hi ? n3.y : n3.x, 0u, sel), qhz = (float)__byte_perm(hi ? n4.w : n4.z, 0u, sel);
+        const float tx0 = fmaf(qlx, ax, bx), tx1 = fmaf(qhx, ax, bx);
+        const float ty0 = fmaf(qly, ay, by), ty1 = fmaf(qhy, ay, by);
+        const float tz0 = fmaf(qlz, az, bz), tz1 = fmaf(qhz, az, bz);
+        float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
+        float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+        tn = fmaf(-fabsf(tn), BOX_MARGIN, tn) - err;
+        tf = fmaf(fabsf(tf), BOX_MARGIN, tf) + err;
+        tn = fmaxf(tn, r.tmin);
+        tf = fminf(tf, (!ANYHIT && r.found) ? r.best.t : r.tmax);
+        const bool hit = meta != 0u && tn <= tf;
+        const uint32_t key = hit ? ((__float_as_uint(fmaxf(tn, 0.0f)) & ~7u) | (uint32_t)g) : 0xffffffffu;
+        const uint32_t bal = __ballot_sync(gmask, hit);
+        const int nh = __popc(bal);
+        int rank;
+        if (ANYHIT) {
+            rank = __popc(bal & gmask & ((1u << (threadIdx.x & 31)) - 1u));
+        } else {
+            rank = 0;
+#pragma unroll
+            for (int j = 0; j < COOP; j++) rank += __shfl_sync(gmask, key, j, COOP) < key ? 1 : 0;
+        }
+        if (r.sp + nh > COOP_STACK) status |= LH2G_STATUS_STACK_OVERFLOW;
+        if (hit) {
+            uint32_t code;
+            if (meta & 0x80u) code = n1.x + (meta & 7u);
+            else code = (r.curInst < 0 ? 0x80000000u : 0x40000000u) | (((meta >> 5) - 1u) << 28) | (n1.y + (meta & 31u));
+            const int slot = r.sp + nh - 1 - rank;
+            if (slot < COOP_STACK) stk[slot] = make_uint2(code, key & ~7u);
+        }
+        __syncwarp(gmask);
+        r.sp = min(r.sp + nh, COOP_STACK);
+        r.nodes++;
+    } else if (kind == 1u) {
+        const uint32_t first = entry & 0x0fffffffu, cnt = ((entry >> 28) & 3u) + 1u;
+        float t = 0.0f, u = 0.0f, v = 0.0f;
+        bool ok = false;
+        int prim = 0x7fffffff;
+        if ((uint32_t)g < cnt) {
+            const float4* td = S.triData + (size_t)(first + g) * 3;
+            const float4 a = __ldg(td), b = __ldg(td + 1), c = __ldg(td + 2);
+            ok = isect_tri(r.O, r.D, a, b, c, t, u, v) && t > r.tmin && t < r.tmax;
+            prim = __float_as_int(a.w);
+        }
+        r.tris += cnt;
+        if (ANYHIT) {
+            if (__ballot_sync(gmask, ok)) { anyHit = true; return false; }
+        } else {
+            /* closest among the group's triangles (t, then primitive), then against the best so far */
+            if (!ok) t = __int_as_float(0x7f800000), prim = 0x7fffffff;
+#pragma unroll
+            for (int off = 1; off < COOP; off <<= 1) {
+                const float ot = __shfl_xor_sync(gmask, t, off, COOP), ou = __shfl_xor_sync(gmask, u, off, COOP), ov = __shfl_xor_sync(gmask, v, off, COOP);
+                const int op = __shfl_xor_sync(gmask, prim, off, COOP);
+                const bool ook = __shfl_xor_sync(gmask, ok ? 1 : 0, off, COOP) != 0;
+                if (ook && (!ok || ot < t || (ot == t && op < prim))) t = ot, u = ou, v = ov, prim = op, ok = true;
+            }
+            if (ok && (!r.found || t < r.best.t || (t == r.best.t && (r.curInst < r.best.inst || (r.curInst == r.best.inst && prim < r.best.prim))))) {
+                r.best.t = t, r.best.u = u, r.best.v = v, r.best.inst = r.curInst, r.best.prim = prim;
+                r.found = true;
+            }
+        }
+    } else {
+        const uint32_t first = entry & 0x0fffffffu, cnt = ((entry >> 28) & 3u) + 1u;
+        if (cnt > 1u && r.sp < COOP_STACK) {
+            if (g == 0) stk[r.sp] = make_uint2(0x80000000u | ((cnt - 2u) << 28) | (first + 1u), 0u);
+            __syncwarp(gmask);
+            r.sp++;
+        }
+        const int ii = (int)__ldg(S.tlasPrims + first);
+        const InstanceGPU* in = S.inst + ii;
+        const uint32_t root = __ldg(&in->blasRoot);
+        if (root != 0xffffffffu && r.sp < COOP_STACK) {
+            float m[12];
+#pragma unroll
+            for (int k = 0; k < 12; k++) m[k] = __ldg(&in->inv[k]);
+            r.O = xform_point(m, r.Ow), r.D = xform_vector(m, r.Dw);
+            r.invD = make_float3(safe_rcp(r.D.x), safe_rcp(r.D.y), safe_rcp(r.D.z));
+            r.curInst = ii;
+            if (g == 0) stk[r.sp] = make_uint2(ENTRY_MARKER, 0u);
+            __syncwarp(gmask);
+            r.sp++;
+            r.entry = root;
+            return true;
+        }
+    }
+    return coop_pop<ANYHIT>(r, stk);
+}
+
+/* Persistent queue loop of a warp with 4 cooperative groups. stackBase: the block's shared stack storage
+ * (COOP_STACK entries per group). load(i, o, d, t0, t1) reads ray i; onFinish(i, r, anyHit) is called by every
+ * lane of the group (write from one lane). */
+template <bool ANYHIT, typename Load, typename Finish>
+LH2G_DEV void trace_queue_coop(const SceneGPU& S, uint32_t* fetch, const uint32_t count, uint32_t& status, uint2* stackBase, Load load,
+                               Finish onFinish, unsigned long long* stats = nullptr) {
+    const int lane = threadIdx.x & 31, g = lane & (COOP - 1), grp = lane / COOP;
+    const uint32_t gmask = 0xffu << (grp * COOP);
+    uint2* stk = stackBase + (threadIdx.x / COOP) * COOP_STACK;
+    unsigned long long nodeSum = 0, triSum = 0;
+    CoopRay r;
+    uint32_t ray = 0;
+    bool active = false, exhausted = false;
+    for (;;) {
+        if (!active && !exhausted) {
+            uint32_t i = 0;
+            if (g == 0) i = atomicAdd(fetch, 1u);
+            i = __shfl_sync(gmask, i, 0, COOP);
+            if (i < count) {
+                float3 o, d;
+                float t0, t1;
+                load(i, o, d, t0, t1);
+                r.Ow = r.O = o, r.Dw = r.D = d, r.tmin = t0, r.tmax = t1;
+                r.invDw = r.invD = make_float3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
+                r.best.t = t1, r.best.u = r.best.v = 0.0f, r.best.inst = -1, r.best.prim = NOHIT;
+                r.found = false, r.sp = 0, r.curInst = -1, r.steps = 0, r.nodes = 0, r.tris = 0;
+                r.entry = S.tlasRoot;
+                ray = i;
+                active = true;
+                if (S.tlasRoot == 0xffffffffu) { onFinish(ray, r, false); active = false; }
+            } else {
+                exhausted = true;
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) break;
+        if (active) {
+            bool anyHit = false;
+            if (!coop_step<ANYHIT>(S, r, stk, g, gmask, status, anyHit)) {
+                onFinish(ray, r, anyHit);
+                if (g == 0) nodeSum += r.nodes, triSum += r.tris;
+                active = false;
+            }
+        }
+    }
+    if (stats) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) nodeSum += __shfl_xor_sync(0xffffffffu, nodeSum, off), triSum += __shfl_xor_sync(0xffffffffu, triSum, off);
+        if (lane == 0) atomicAdd(stats, nodeSum), atomicAdd(stats + 1, triSum);
+    }
+}
 
 /* Single-ray form (used where lanes do not refill). */
 template <bool ANYHIT>
@@ -202,15 +434,17 @@ LH2G_DEV bool trace_ray(const SceneGPU& S, const float3 Ow, const float3 Dw, con
  * the next one from the queue (one atomic per warp per refill round, ballot + popc to hand out indices).
  * fetch is a 32-bit work counter; count the number of rays; onFinish(i, tr, anyHit) writes the result. */
 template <bool ANYHIT, typename Load, typename Finish>
-LH2G_DEV void trace_queue(const SceneGPU& S, uint32_t* fetch, const uint32_t count, uint32_t& status, Load load, Finish onFinish) {
+LH2G_DEV void trace_queue(const SceneGPU& S, uint32_t* fetch, const uint32_t count, uint32_t& status, Load load, Finish onFinish,
+                          unsigned long long* stats = nullptr) {
+    unsigned long long nodeSum = 0, triSum = 0;
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t lanemask_lt;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lanemask_lt));
     Traversal tr;
     uint32_t ray = 0;
     bool active = false, exhausted = false;
-    if (S.tlasRoot == 0xffffffffu) {
-        /* no geometry: every ray misses */
+    if (S.tlasRoot == 0xffffffffu || !LH2G_REFILL) {
+        /* a warp takes 32 rays at a time and traces each to the end (also used when there is no geometry) */
         for (;;) {
             uint32_t base = 0;
             if (lane == 0) base = atomicAdd(fetch, 32u);
@@ -222,9 +456,19 @@ LH2G_DEV void trace_queue(const SceneGPU& S, uint32_t* fetch, const uint32_t cou
                 float t0, t1;
                 load(i, o, d, t0, t1);
                 tr.begin(S, o, d, t0, t1);
-                onFinish(i, tr, false);
+                bool anyHit = false;
+                if (S.tlasRoot != 0xffffffffu)
+                    while (tr.step<ANYHIT>(S, status, anyHit)) {}
+                onFinish(i, tr, anyHit);
+                nodeSum += tr.nodes, triSum += tr.tris;
             }
         }
+        if (stats) {
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) nodeSum += __shfl_xor_sync(0xffffffffu, nodeSum, off), triSum += __shfl_xor_sync(0xffffffffu, triSum, off);
+            if (lane == 0) atomicAdd(stats, nodeSum), atomicAdd(stats + 1, triSum);
+        }
+        return;
     }
     for (;;) {
         if (!exhausted) {
@@ -248,15 +492,32 @@ LH2G_DEV void trace_queue(const SceneGPU& S, uint32_t* fetch, const uint32_t cou
                 }
             }
         }
-        if (!__any_sync(0xffffffffu, active)) return;
+        if (!__any_sync(0xffffffffu, active)) break;
         if (active) {
             bool anyHit = false;
             if (!tr.step<ANYHIT>(S, status, anyHit)) {
                 onFinish(ray, tr, anyHit);
+                nodeSum += tr.nodes, triSum += tr.tris;
                 active = false;
             }
         }
     }
+    if (stats) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) nodeSum += __shfl_xor_sync(0xffffffffu, nodeSum, off), triSum += __shfl_xor_sync(0xffffffffu, triSum, off);
+        if (lane == 0) atomicAdd(stats, nodeSum), atomicAdd(stats + 1, triSum);
+    }
+}
+
+/* The queue loop of the configured strategy. */
+template <bool ANYHIT, typename Load, typename FinishT, typename FinishC>
+LH2G_DEV void trace_queue_any(const SceneGPU& S, uint32_t* fetch, const uint32_t count, uint32_t& status, uint2* stackBase, Load load,
+                              FinishT finishThread, FinishC finishCoop, unsigned long long* stats) {
+#if LH2G_COOP
+    trace_queue_coop<ANYHIT>(S, fetch, count, status, stackBase, load, finishCoop, stats);
+#else
+    trace_queue<ANYHIT>(S, fetch, count, status, load, finishThread, stats);
+#endif
 }
 
 }  // namespace lh2g
