@@ -1,6 +1,7 @@
 """In-tree build of the GB300 render core: nvcc for sm_103a, one shared library.
 
     python -m lighthouse2_gb300.build        # -> lighthouse2_gb300/_build/libRenderCore_GB300.so
+    LH2G_NVCC_FLAGS="-DLH2G_COOP=1" python -m lighthouse2_gb300.build -f   # another traversal strategy
 
 The library exports the C ABI of include/lh2g.h and the Lighthouse 2 plugin entry point CreateCore
 (include/lh2_core_api.h). Device code is compiled without fast-math and with --fmad=false: the shading
@@ -33,7 +34,8 @@ def nvcc():
 
 
 def _flags():
-    return ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
+    extra = os.environ.get("LH2G_NVCC_FLAGS", "").split()   # e.g. traversal strategy: -DLH2G_COOP=1 -DLH2G_REFILL=1
+    return ARCH + extra + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
                    "-Xcompiler", "-fPIC,-O2,-fvisibility=hidden,-ffp-contract=off", "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 
 
