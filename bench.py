@@ -13,6 +13,8 @@ depth 3, next-event estimation; frames follow a seeded 8-pose camera path. Seede
   roofline  the kernel with the largest share of the frame: algorithmic bytes per launch / measured launch
             duration against the measured HBM copy bandwidth.
   cpu_baseline  the CPU oracle (a restatement of the reference's path tracer) on all host cores.
+  svgf      filter-core frames of the same scene and camera path with SVGF + TAA: device time of the six filter
+            launches per frame against the measured HBM bandwidth.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 Under torchrun each rank renders its own frames on its own GPU (replicas, weak scaling); rank 0 prints.
@@ -36,6 +38,7 @@ MAX_DEPTH, RR_START = 8, 4
 WORKLOAD = "spheres_2m: 64 x 32k-tri displaced spheres + ground (2,048,002 tris, 66 instances), 16 quad + 4 point lights, " \
            "20 materials (4 textured), sky; 1920x1080 1spp, max depth 8, RR after depth 3, NEE"
 METRIC = "Mrays/s @1080p 1spp"
+VIEW_BYTES, PARAMS_BYTES = 68, 44     # lh2g_view and lh2g_render_params copied host -> device per frame
 
 
 def peaks():
@@ -172,6 +175,39 @@ def algorithmic_bytes(kind, n_in, n_ext, n_shadow):
     return n_in * 48
 
 
+# SVGF bytes per pixel and frame (own-pixel buffers; neighbourhood taps hit L1/L2): prepare reads accumulator
+# halves 32, features 16, world position 16, previous world position 16, previous moments 16 and writes shading 16,
+# motion 8, moments 16, features 16; a-trous phase 1 reads features, packed light, depth derivatives, moments
+# (4 x 16), motion 8, world positions 2 x 16, history 16 and writes 16; phases 2 and 3 read 4 x 16 and write 16;
+# TAA reads 16 + 8 + 16 and writes 16; unsharpen reads 16 and writes 16.
+SVGF_BYTES_PER_PIXEL = (96 + 56) + (64 + 56 + 16) + 2 * (64 + 16) + (40 + 16) + (16 + 16)
+
+
+def svgf_leg(core, W, H, steps, warmup):
+    """Filter-core frames with SVGF + TAA over the 8-pose camera path (Restart every frame, as a moving camera
+    does); the filter passes are timed by the core's own events (coreStats.filterTime)."""
+    from lighthouse2_gb300 import scenes as S
+    core.Setting("filter", 1)
+    core.Setting("TAA", 1)
+    for k in range(warmup):
+        core.Render(S.spheres_view(W, H, frame=k % 8), converge=1)
+        core.GetCoreStats()
+    filt, rend = [], []
+    for k in range(steps):
+        core.Render(S.spheres_view(W, H, frame=k % 8), converge=1)
+        st = core.GetCoreStats()
+        filt.append(st["filterTime"])
+        rend.append(st["renderTime"])
+    core.Setting("filter", 0)
+    ms = statistics.median(filt)
+    peak, peak_kind = peaks()
+    achieved = SVGF_BYTES_PER_PIXEL * W * H / (ms / 1e3) / 1e9
+    return {"workload": f"filter-core frames of the same scene, {W}x{H}, 8-pose camera path, Halton jitter, TAA + unsharpen",
+            "filter_ms_per_frame": ms, "filter_ms_min": min(filt), "render_ms_per_frame": statistics.median(rend),
+            "launches_per_frame": 6, "algorithmic_bytes_per_pixel": SVGF_BYTES_PER_PIXEL, "achieved_GBps": achieved,
+            "peak_GBps": peak, "frac": achieved / peak, "peak_source": peak_kind}
+
+
 def run_gb300(args):
     import numpy as np
     import torch
@@ -258,6 +294,7 @@ def run_gb300(args):
         c = out["counters"]
         e2e_rays += W * H + int(c[:, 0].sum()) + int(c[:, 1].sum())
     e2e_value = e2e_rays * world / t_e2e / 1e6
+    svgf = svgf_leg(core, W, H, max(args.steps, 8), args.warmup) if not args.no_svgf else None
     if rank != 0:
         return 0
     frame_ms = sum(v[0] for v in per_kind.values())
@@ -288,9 +325,11 @@ def run_gb300(args):
             "roofline": {"kernel": "k_" + dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                          "note": "traversal/shading are latency and issue bound; algorithmic bytes count queue traffic only"},
-            "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": 68 + 40, "d2h_bytes_per_step": W * H * 16},
+            "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": VIEW_BYTES + PARAMS_BYTES, "d2h_bytes_per_step": W * H * 16},
             "gpu_launches": launches * world,
             "clocks": clk}
+    if svgf is not None:
+        line["svgf"] = svgf
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(sc, W, H, args.cpu_seconds, os.cpu_count() or 1)
     print(json.dumps(line, default=float), flush=True)
@@ -308,6 +347,7 @@ def main():
     ap.add_argument("--height", type=int, default=H_DEFAULT)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-svgf", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

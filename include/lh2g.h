@@ -65,7 +65,10 @@ LH2G_API int lh2g_set_lights(lh2g_context* ctx, const lh2g_light_tri* tri, int n
                     const lh2g_spot_light* spot, int nspot, const lh2g_dir_light* dir, int ndir);
 /* SetSkyData (core_api_base.h:112): width*height RGB floats; worldToSky16 may be NULL (identity). */
 LH2G_API int lh2g_set_sky(lh2g_context* ctx, const float* rgb, int width, int height, const float* worldToSky16);
-/* Setting (core_api_base.h:95): "epsilon", "clampValue", "maxDepth", "rrStartDepth", "nee". */
+/* Setting (core_api_base.h:95): "epsilon", "clampValue", "maxDepth", "rrStartDepth", "nee", and the filter
+ * core's "filter" (0/1, default 0), "TAA" (0/1, default 1), "clampDirect" (2.5), "clampIndirect" (15)
+ * (lib/RenderCore_Optix7Filter/rendercore.cpp:674-677, rendercore.h:32-35). With "filter" on, lh2g_render
+ * renders filter-core frames (LH2G_RP_FILTER, Halton-jittered when TAA is on) and denoises them with SVGF. */
 LH2G_API int lh2g_setting(lh2g_context* ctx, const char* name, float value);
 /* SetTarget (core_api_base.h:93), headless: the output is a device float4 buffer of width*height pixels. */
 LH2G_API int lh2g_set_target(lh2g_context* ctx, int width, int height, int spp);
@@ -79,6 +82,18 @@ LH2G_API int lh2g_render(lh2g_context* ctx, const lh2g_view* view, int converge)
  * receive per path length the extension and connection counts. */
 LH2G_API int lh2g_render_ex(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* params, int accumulate,
                    lh2g_hit* captureHits, uint32_t* captureSeeds, uint32_t* counters);
+/* SVGF on the accumulator of the last LH2G_RP_FILTER frame (lib/RenderCore_Optix7Filter/rendercore.cpp:904-935):
+ * prepareFilter (demodulation, reprojection, luminance moments), applyFilter phases 1-3 (temporal blend,
+ * a-trous at steps 1, 2, 4, remodulation), then TAA + unsharpen or finalizeNoTAA into the frame buffer, whose
+ * border pixels keep their contents as in the reference; then the history buffers swap. lh2g_render calls
+ * this itself when the "filter" setting is on. */
+LH2G_API int lh2g_filter(lh2g_context* ctx, const lh2g_filter_params* params);
+/* Copies filter buffer slot LH2G_FB_* (W*H elements; LH2G_FB_ACCUM 2*W*H) to host memory. */
+LH2G_API int lh2g_read_filter_buffer(lh2g_context* ctx, int slot, void* host);
+/* The filter parameters lh2g_render used for its last filtered frame, and the jittered view and estimator
+ * parameters of that frame (either pointer may be NULL). */
+LH2G_API int lh2g_get_last_filter_frame(lh2g_context* ctx, lh2g_filter_params* filter, lh2g_view* jitteredView,
+                                        lh2g_render_params* params);
 /* WaitForRender (core_api_base.h:99): blocks until the context's stream is idle. */
 LH2G_API int lh2g_wait(lh2g_context* ctx);
 /* GetCoreStats (core_api_base.h:87). */

@@ -129,10 +129,45 @@ typedef struct lh2g_render_params {
     float geometryEpsilon;                  /* ray offset / tmin, 'epsilon' setting (rendersystem.h:67) */
     float clampValue;                       /* 'clampValue' setting (kept for the settings interface) */
     int32_t flags;                          /* LH2G_RP_* */
+    uint32_t frameSeed;                     /* LH2G_RP_FILTER only: shading R0 = frameSeed + pathLength * 91771 */
 } lh2g_render_params;
 
 #define LH2G_RP_NEE        1                /* next-event estimation (connections buffer present) */
 #define LH2G_RP_DEPTH_W    2                /* add the primary hit distance to accumulator.w (DOF data) */
+/* Filter-core frame (lib/RenderCore_Optix7Filter): primary rays through the pixel corner of the (jittered)
+ * view without lens sampling (optix/.optix.cu:66-100), SVGF features of sample 0 written while shading
+ * (kernels/pathtracer.h:44-57,95-232), radiance split into a direct half (accumulator[0, W*H)) and an
+ * indirect half (accumulator[W*H, 2*W*H)) at the first diffuse bounce, and a per-frame shading seed
+ * (rendercore.cpp:834: RandomUInt(camRNGseed) + pathLength * 91771). */
+#define LH2G_RP_FILTER     4
+
+/* One SVGF pass over the accumulator of a LH2G_RP_FILTER frame (lib/RenderCore_Optix7Filter/rendercore.cpp:
+ * 897-935 with the kernels of lib/CUDA/shared_kernel_code/finalize_shared.h:169-600). */
+typedef struct lh2g_filter_params {
+    lh2g_view prevView;                     /* unjittered view of the previous frame (reprojection) */
+    float j0, j1;                           /* subpixel jitter of this frame, in pixels */
+    float prevj0, prevj1;                   /* jitter of the previous filtered frame */
+    float clampDirect, clampIndirect;       /* demodulated-light clamps ('clampDirect' 2.5, 'clampIndirect' 15) */
+    int32_t samplesTaken;                   /* samples in the accumulator, this frame included (scale = 1 / this) */
+    int32_t camIsStationary;                /* 1 while converging: specular pixels keep their own position */
+    int32_t taa;                            /* 1: TAA + unsharpen (TAApassKernel, unsharpenTAAKernel); 0: finalizeNoTAA */
+} lh2g_filter_params;
+
+/* Filter buffer slots (lh2g_read_filter_buffer), named by their role at the time of the call: after
+ * lh2g_filter the history buffers have been swapped, so PREV_* hold this frame's data. */
+#define LH2G_FB_FEATURES       0            /* uint4: albedo 10:11:11, normal 10:10:10 + specular bits, depth, w = history | spec << 4 | mat << 6 */
+#define LH2G_FB_WORLDPOS       1            /* float4: first diffuse vertex, w = packed normal */
+#define LH2G_FB_PREV_WORLDPOS  2
+#define LH2G_FB_DELTADEPTH     3            /* float4: z, w = depth derivatives in x and y */
+#define LH2G_FB_MOTION         4            /* float2: position in the previous frame (+0.5) */
+#define LH2G_FB_MOMENTS        5            /* float4: luminance moments direct (x, y) and indirect (z, w) */
+#define LH2G_FB_PREV_MOMENTS   6
+#define LH2G_FB_SHADING        7            /* float4: 5:11 packed direct + indirect light; after filtering the gamma image */
+#define LH2G_FB_FILTERED_IN    8            /* float4: packed light, history of the temporal blend */
+#define LH2G_FB_FILTERED_OUT   9
+#define LH2G_FB_PREV_PIXELS    10           /* float4: the previous frame's image (TAA history) */
+#define LH2G_FB_ACCUM          11           /* float4 x 2*W*H: direct and indirect accumulators */
+#define LH2G_FB_COUNT          12
 
 /* Per-path, per-depth capture used by the parity tests: the hit record each path saw at each depth and
  * its RNG state after shading. Entries of paths that were no longer alive carry prim = -2. */

@@ -19,7 +19,10 @@ LIB_PATH = os.path.join(HERE, "_build", "libRenderCore_GB300.so")
 
 PARAMS_DTYPE = np.dtype([("width", "<i4"), ("height", "<i4"), ("spp", "<i4"), ("maxDepth", "<i4"),
                          ("rrStartDepth", "<i4"), ("samplesTaken", "<i4"), ("cameraR0", "<u4"),
-                         ("geometryEpsilon", "<f4"), ("clampValue", "<f4"), ("flags", "<i4")])
+                         ("geometryEpsilon", "<f4"), ("clampValue", "<f4"), ("flags", "<i4"), ("frameSeed", "<u4")])
+FILTER_PARAMS_DTYPE = np.dtype([("prevView", S.VIEW_DTYPE), ("j0", "<f4"), ("j1", "<f4"), ("prevj0", "<f4"), ("prevj1", "<f4"),
+                                ("clampDirect", "<f4"), ("clampIndirect", "<f4"), ("samplesTaken", "<i4"),
+                                ("camIsStationary", "<i4"), ("taa", "<i4")])
 TEXDESC_DTYPE = np.dtype([("texels", "<u8"), ("width", "<u4"), ("height", "<u4"), ("flags", "<u4"),
                           ("pixelCount", "<u4"), ("firstPixel", "<u4"), ("MIPlevels", "<u4"), ("storage", "<i4"),
                           ("pad", "<i4")])
@@ -30,12 +33,18 @@ STATS_FIELDS = ["totalRays", "totalExtensionRays", "totalShadowRays", "primaryRa
 STATS_DTYPE = np.dtype([(f, "<u4") for f in STATS_FIELDS[:6]] + [(f, "<f4") for f in STATS_FIELDS[6:14]] +
                        [(f, "<u4") for f in STATS_FIELDS[14:18]] + [("probedInstid", "<i4"), ("probedTriid", "<i4"),
                                                                     ("probedDist", "<f4"), ("deviceStatus", "<u4")])
-RP_NEE, RP_DEPTH_W = 1, 2
+RP_NEE, RP_DEPTH_W, RP_FILTER = 1, 2, 4
+# filter buffer slots (LH2G_FB_*): name -> (index, element dtype, components per pixel)
+FILTER_SLOTS = {"features": (0, np.uint32, 4), "worldPos": (1, np.float32, 4), "prevWorldPos": (2, np.float32, 4),
+                "deltaDepth": (3, np.float32, 4), "motion": (4, np.float32, 2), "moments": (5, np.float32, 4),
+                "prevMoments": (6, np.float32, 4), "shading": (7, np.float32, 4), "filteredIN": (8, np.float32, 4),
+                "filteredOUT": (9, np.float32, 4), "prevPixels": (10, np.float32, 4), "accum": (11, np.float32, 4)}
 C_API = ["lh2g_create", "lh2g_destroy", "lh2g_last_error", "lh2g_set_geometry", "lh2g_set_instance", "lh2g_finalize_instances",
          "lh2g_set_materials", "lh2g_pack_materials", "lh2g_set_textures", "lh2g_set_lights", "lh2g_set_sky", "lh2g_setting",
          "lh2g_set_target", "lh2g_set_probe", "lh2g_render", "lh2g_render_ex", "lh2g_wait", "lh2g_get_stats",
          "lh2g_get_framebuffer", "lh2g_read_framebuffer", "lh2g_read_accumulator", "lh2g_trace", "lh2g_trace_host",
-         "lh2g_get_stream", "lh2g_enable_launch_timing", "lh2g_get_launch_times", "lh2g_get_traversal_stats"]
+         "lh2g_get_stream", "lh2g_enable_launch_timing", "lh2g_get_launch_times", "lh2g_get_traversal_stats",
+         "lh2g_render_noalloc", "lh2g_filter", "lh2g_read_filter_buffer", "lh2g_get_last_filter_frame"]
 
 _lib = None
 
@@ -82,6 +91,10 @@ def load_library(path: str | None = None):
     lib.lh2g_enable_launch_timing.argtypes = [vp, i]
     lib.lh2g_get_launch_times.argtypes = [vp, vp, i, C.POINTER(i)]
     lib.lh2g_get_traversal_stats.argtypes = [vp, vp]
+    lib.lh2g_render_noalloc.argtypes = [vp, vp, vp, vp, vp]
+    lib.lh2g_filter.argtypes = [vp, vp]
+    lib.lh2g_read_filter_buffer.argtypes = [vp, i, vp]
+    lib.lh2g_get_last_filter_frame.argtypes = [vp, vp, vp, vp]
     if path is None:
         _lib = lib
     return lib
@@ -104,11 +117,12 @@ def texture_descs(textures):
     return d, keep
 
 
-def make_params(width, height, spp=1, max_depth=3, rr_start=1, samples_taken=0, camera_r0=0, eps=1e-3, clamp=10.0, flags=RP_NEE):
+def make_params(width, height, spp=1, max_depth=3, rr_start=1, samples_taken=0, camera_r0=0, eps=1e-3, clamp=10.0, flags=RP_NEE,
+                frame_seed=0):
     p = np.zeros((), PARAMS_DTYPE)
     p["width"], p["height"], p["spp"], p["maxDepth"] = width, height, spp, max_depth
     p["rrStartDepth"], p["samplesTaken"], p["cameraR0"] = rr_start, samples_taken, camera_r0
-    p["geometryEpsilon"], p["clampValue"], p["flags"] = eps, clamp, flags
+    p["geometryEpsilon"], p["clampValue"], p["flags"], p["frameSeed"] = eps, clamp, flags, frame_seed
     return p
 
 
@@ -264,6 +278,24 @@ class RenderCore:
         out = np.zeros(4, np.uint64)
         self._check(self.lib.lh2g_get_traversal_stats(self.ctx, _p(out)), "get_traversal_stats")
         return out
+
+    # --- SVGF (filter core) ----------------------------------------------------------------------------
+    def filter(self, fparams):
+        self._check(self.lib.lh2g_filter(self.ctx, _p(np.ascontiguousarray(fparams))), "filter")
+
+    def read_filter_buffer(self, name):
+        """Copy of filter buffer slot `name` (FILTER_SLOTS) as an array of (pixels, components)."""
+        idx, dt, comps = FILTER_SLOTS[name]
+        n = self.W * self.H * (2 if name == "accum" else 1)
+        out = np.zeros((n, comps), dt)
+        self._check(self.lib.lh2g_read_filter_buffer(self.ctx, idx, _p(out)), "read_filter_buffer")
+        return out
+
+    def last_filter_frame(self):
+        """(filter params, jittered view, render params) of the last filtered frame that Render produced."""
+        fp, jv, rp = np.zeros((), FILTER_PARAMS_DTYPE), np.zeros((), S.VIEW_DTYPE), np.zeros((), PARAMS_DTYPE)
+        self._check(self.lib.lh2g_get_last_filter_frame(self.ctx, _p(fp), _p(jv), _p(rp)), "get_last_filter_frame")
+        return fp, jv, rp
 
     def read_framebuffer_into(self, host_ptr):
         self._check(self.lib.lh2g_read_framebuffer(self.ctx, C.c_void_p(host_ptr)), "read_framebuffer")

@@ -9,6 +9,11 @@
  *   Render               rendercore.cpp:535-632 (Restart resets the accumulator, samplesTaken and the camera
  *                        seed 0x12345678; R0 = RandomUInt(camRNGseed); shading R0 = samplesTaken * 7907 +
  *                        pathLength * 91771; output = accumulator / samplesTaken)
+ *   Render, "filter" on  lib/RenderCore_Optix7Filter/rendercore.cpp:737-797, 897-935 (Halton subpixel jitter
+ *                        when TAA is on, aperture 0, camRNGseed never reset; then SVGF and the history swaps).
+ *                        One RandomUInt(camRNGseed) per frame seeds every wave (the reference draws one per wave,
+ *                        and its wave count depends on queue sizes read back by the host, which this core never
+ *                        reads). The first filtered frame after SetTarget reprojects onto its own view.
  * No stage of a frame waits for the host: queue sizes stay on the device.
  */
 #include <chrono>
@@ -20,6 +25,7 @@
 #include "bvh_build.cuh"
 #include "kernels.cuh"
 #include "lh2g.h"
+#include "svgf.cuh"
 
 using namespace lh2g;
 
@@ -170,6 +176,23 @@ struct lh2g_context {
     std::vector<cudaEvent_t> lev;   /* 2 per launch */
     int lastLaunches = 0;
     int blocksExtend = 0, blocksConnect = 0, blocksShade = 0;
+    /* SVGF (filter core) state: settings of lib/RenderCore_Optix7Filter/rendercore.h:32-35 (this core renders
+     * the unfiltered PrimeRef estimator unless "filter" is set) */
+    int filterEnabled = 0, taaEnabled = 1;
+    float clampDirect = 2.5f, clampIndirect = 15.0f;
+    SvgfBuffers sv;
+    bool svAlloc = false;
+    int64_t pathAccCap = 0;            /* paths that pathAcc holds (2 * cap once a filter frame was rendered) */
+    uint32_t filterSeed = 0x12345678u; /* camRNGseed of the filter core */
+    int frameCycle = 0;
+    float prevj0 = 0, prevj1 = 0;
+    lh2g_view prevView;
+    bool havePrevView = false;
+    cudaEvent_t fev[2] = {nullptr, nullptr};   /* around the filter passes: coreStats.filterTime */
+    bool filterPending = false;
+    lh2g_filter_params lastFilter;
+    lh2g_view lastJittered;
+    lh2g_render_params lastParams;
 };
 
 namespace {
@@ -199,11 +222,70 @@ cudaError_t dalloc(T*& p, size_t count) {
     return cudaMalloc((void**)&p, std::max<size_t>(1, count) * sizeof(T));
 }
 
+void free_filter(lh2g_context* ctx) {
+    SvgfBuffers& v = ctx->sv;
+    dfree(v.features), dfree(v.worldPos), dfree(v.prevWorldPos), dfree(v.deltaDepth), dfree(v.motion), dfree(v.moments);
+    dfree(v.prevMoments), dfree(v.shading), dfree(v.filteredIN), dfree(v.filteredOUT), dfree(v.prevPixels), dfree(v.taaPixels);
+    ctx->svAlloc = false;
+    ctx->havePrevView = false;
+}
+
 void free_target(lh2g_context* ctx) {
     WaveBuffers& B = ctx->B;
     for (int k = 0; k < 2; k++) dfree(B.O[k]), dfree(B.D[k]), dfree(B.T[k]);
     dfree(B.hits), dfree(B.shO), dfree(B.shD), dfree(B.shE), dfree(B.pathAcc), dfree(B.accum), dfree(B.frame), dfree(B.counters);
-    ctx->cap = 0;
+    free_filter(ctx);
+    ctx->cap = 0, ctx->pathAccCap = 0;
+}
+
+/* The filter's buffers, a second (indirect) half for the per-path radiance and the accumulator; all zeroed. */
+int ensure_filter(lh2g_context* ctx) {
+    if (ctx->svAlloc) return LH2G_OK;
+    const size_t WH = (size_t)ctx->W * ctx->H;
+    SvgfBuffers& v = ctx->sv;
+    WaveBuffers& B = ctx->B;
+    cudaError_t e = cudaSuccess;
+    CK(cudaStreamSynchronize(ctx->st));
+    if (!e) e = dalloc(B.pathAcc, 2 * (size_t)ctx->cap);
+    if (!e) e = dalloc(B.accum, 2 * WH);
+    float4** f4[] = {&v.worldPos, &v.prevWorldPos, &v.deltaDepth, &v.moments, &v.prevMoments, &v.shading, &v.filteredIN, &v.filteredOUT,
+                     &v.prevPixels, &v.taaPixels};
+    for (float4** q : f4)
+        if (!e) e = dalloc(*q, WH);
+    if (!e) e = dalloc(v.features, WH);
+    if (!e) e = dalloc(v.motion, WH);
+    if (e) { free_target(ctx); return cuda_check(ctx, e, "filter buffer allocation"); }
+    ctx->pathAccCap = 2 * ctx->cap;
+    CK(cudaMemsetAsync(B.accum, 0, sizeof(float4) * 2 * WH, ctx->st));
+    for (float4** q : f4) CK(cudaMemsetAsync(*q, 0, sizeof(float4) * WH, ctx->st));
+    CK(cudaMemsetAsync(v.features, 0, sizeof(uint4) * WH, ctx->st));
+    CK(cudaMemsetAsync(v.motion, 0, sizeof(float2) * WH, ctx->st));
+    ctx->svAlloc = true;
+    return LH2G_OK;
+}
+
+/* host part of prepareFilter (lib/CUDA/shared_kernel_code/finalize_shared.h:297-313) */
+float3 h3(const float* p) { return make_float3(p[0], p[1], p[2]); }
+float3 hsub(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
+float3 hadd(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
+float3 hmul(float3 a, float s) { return make_float3(a.x * s, a.y * s, a.z * s); }
+float hdot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+float3 hnormalize(float3 v) { const float inv = 1.0f / sqrtf(hdot(v, v)); return hmul(v, inv); }
+SvgfView svgf_view(const lh2g_view& v, int h) {
+    const float3 pos = h3(v.pos), p1 = h3(v.p1), p2 = h3(v.p2), p3 = h3(v.p3);
+    const float3 centre = make_float3(0.5f * (p2.x + p3.x), 0.5f * (p2.y + p3.y), 0.5f * (p2.z + p3.z));
+    const float3 direction = hnormalize(hsub(centre, pos));
+    const float3 right = hnormalize(hsub(p2, p1));
+    const float3 up = hnormalize(hsub(p3, p1));
+    const float screenSize = sqrtf(hdot(hsub(p3, p1), hsub(p3, p1)));
+    const float lenReci = (float)h / screenSize;
+    SvgfView r;
+    r.prevPos = make_float4(pos.x, pos.y, pos.z, -(hdot(pos, direction) - hdot(centre, direction)));
+    r.prevE = make_float4(direction.x, direction.y, direction.z, 0);
+    const float3 rr = hmul(right, lenReci), uu = hmul(up, lenReci);
+    r.prevRight = make_float4(rr.x, rr.y, rr.z, hdot(p1, right) * lenReci);
+    r.prevUp = make_float4(uu.x, uu.y, uu.z, hdot(p1, up) * lenReci);
+    return r;
 }
 
 SceneGPU scene_of(const lh2g_context* c) {
@@ -231,6 +313,11 @@ int lh2g_create(int device, lh2g_context** out) {
     lh2g_context* ctx = new lh2g_context();
     memset(&ctx->B, 0, sizeof(ctx->B));
     memset(&ctx->stats, 0, sizeof(ctx->stats));
+    memset(&ctx->sv, 0, sizeof(ctx->sv));
+    memset(&ctx->prevView, 0, sizeof(ctx->prevView));
+    memset(&ctx->lastFilter, 0, sizeof(ctx->lastFilter));
+    memset(&ctx->lastJittered, 0, sizeof(ctx->lastJittered));
+    memset(&ctx->lastParams, 0, sizeof(ctx->lastParams));
     for (int i = 0; i < 16; i++) ctx->w2s[i] = (i % 5 == 0) ? 1.0f : 0.0f;
     ctx->device = device;
     int r = cuda_check(ctx, cudaSetDevice(device), "cudaSetDevice");
@@ -239,6 +326,8 @@ int lh2g_create(int device, lh2g_context** out) {
     if (r == LH2G_OK) r = cuda_check(ctx, cudaMalloc((void**)&ctx->traceFetch, 16), "cudaMalloc");
     if (r == LH2G_OK) r = cuda_check(ctx, cudaEventCreate(&ctx->ev[0]), "cudaEventCreate");
     if (r == LH2G_OK) r = cuda_check(ctx, cudaEventCreate(&ctx->ev[1]), "cudaEventCreate");
+    if (r == LH2G_OK) r = cuda_check(ctx, cudaEventCreate(&ctx->fev[0]), "cudaEventCreate");
+    if (r == LH2G_OK) r = cuda_check(ctx, cudaEventCreate(&ctx->fev[1]), "cudaEventCreate");
     if (r != LH2G_OK) {
         fprintf(stderr, "lh2g_create: %s\n", ctx->err.c_str());
         delete ctx;
@@ -269,6 +358,8 @@ int lh2g_destroy(lh2g_context* ctx) {
     free_target(ctx);
     if (ctx->hostCounters) cudaFreeHost(ctx->hostCounters);
     cudaEventDestroy(ctx->ev[0]), cudaEventDestroy(ctx->ev[1]);
+    if (ctx->fev[0]) cudaEventDestroy(ctx->fev[0]);
+    if (ctx->fev[1]) cudaEventDestroy(ctx->fev[1]);
     for (cudaEvent_t e : ctx->lev) cudaEventDestroy(e);
     cudaStreamDestroy(ctx->st);
     delete ctx;
@@ -493,8 +584,13 @@ int lh2g_setting(lh2g_context* ctx, const char* name, float value) {
         ctx->maxDepth = (int)value;
     } else if (!strcmp(name, "rrStartDepth")) ctx->rrStart = (int)value;
     else if (!strcmp(name, "nee")) ctx->nee = value != 0.0f;
-    /* other names (the filter core's clampDirect, clampIndirect, filter, TAA) are accepted and ignored,
-     * as the reference cores ignore settings they do not know (rendercore.cpp:484-502) */
+    /* the filter core's settings (lib/RenderCore_Optix7Filter/rendercore.cpp:674-677) */
+    else if (!strcmp(name, "clampDirect")) ctx->clampDirect = value;
+    else if (!strcmp(name, "clampIndirect")) ctx->clampIndirect = value;
+    else if (!strcmp(name, "filter")) ctx->filterEnabled = value == 0 ? 0 : 1;
+    else if (!strcmp(name, "TAA")) ctx->taaEnabled = value == 0 ? 0 : 1;
+    /* other names are accepted and ignored, as the reference cores ignore settings they do not know
+     * (rendercore.cpp:484-502) */
     return LH2G_OK;
 }
 
@@ -522,10 +618,11 @@ int lh2g_set_target(lh2g_context* ctx, int w, int h, int spp) {
         if (!e) e = dalloc(B.frame, (size_t)w * h);
         if (!e) e = dalloc(B.counters, 1);
         if (e) { free_target(ctx); return cuda_check(ctx, e, "set_target allocation"); }
-        ctx->cap = P;
+        ctx->cap = P, ctx->pathAccCap = P;
         CK(cudaMemsetAsync(B.accum, 0, sizeof(float4) * (size_t)w * h, ctx->st));
         CK(cudaMemsetAsync(B.frame, 0, sizeof(float4) * (size_t)w * h, ctx->st));
     }
+    ctx->havePrevView = false;
     ctx->W = w, ctx->H = h, ctx->spp = spp;
     ctx->samplesTaken = 0;
     ctx->firstConverging = true;
@@ -547,10 +644,15 @@ int lh2g_render_ex(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_p
         return fail(ctx, LH2G_ERR_INVALID, "render: parameters do not match the target");
     if (!ctx->mats) return fail(ctx, LH2G_ERR_STATE, "render: no materials");
     cudaSetDevice(ctx->device);
+    const bool filt = (p->flags & LH2G_RP_FILTER) != 0;
+    if (filt) {
+        const int r = ensure_filter(ctx);
+        if (r != LH2G_OK) return r;
+    }
     FrameGPU F;
     memset(&F, 0, sizeof(F));
     F.W = p->width, F.H = p->height, F.spp = p->spp, F.maxDepth = p->maxDepth, F.rrStart = p->rrStartDepth, F.samplesTaken = p->samplesTaken;
-    F.cameraR0 = p->cameraR0, F.eps = p->geometryEpsilon, F.flags = p->flags;
+    F.cameraR0 = p->cameraR0, F.frameSeed = p->frameSeed, F.eps = p->geometryEpsilon, F.flags = p->flags;
     F.spreadAngle = view->spreadAngle, F.aperture = view->aperture;
     F.pos = make_float3(view->pos[0], view->pos[1], view->pos[2]);
     F.p1 = make_float3(view->p1[0], view->p1[1], view->p1[2]);
@@ -560,6 +662,9 @@ int lh2g_render_ex(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_p
     F.stride = ctx->cap;
     WaveBuffers B = ctx->B;
     B.capHits = nullptr, B.capSeeds = nullptr;
+    B.features = filt ? ctx->sv.features : nullptr;
+    B.worldPos = filt ? ctx->sv.worldPos : nullptr;
+    B.deltaDepth = filt ? ctx->sv.deltaDepth : nullptr;
     const size_t capN = (size_t)F.maxDepth * F.P;
     if (capHits || capSeeds) {
         CK(dalloc(ctx->B.capHits, capN));
@@ -570,7 +675,7 @@ int lh2g_render_ex(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_p
         B.capHits = ctx->B.capHits, B.capSeeds = ctx->B.capSeeds;
     }
     const SceneGPU S = scene_of(ctx);
-    if (!accumulate) CK(cudaMemsetAsync(B.accum, 0, sizeof(float4) * (size_t)F.W * F.H, ctx->st));
+    if (!accumulate) CK(cudaMemsetAsync(B.accum, 0, sizeof(float4) * (size_t)F.W * F.H * (filt ? 2 : 1), ctx->st));
     CK(cudaMemsetAsync(B.counters, 0, sizeof(Counters), ctx->st));
     const int launches = 2 + 3 * F.maxDepth;
     const bool timing = ctx->launchTiming;
@@ -607,8 +712,123 @@ int lh2g_render_ex(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_p
     return LH2G_OK;
 }
 
+namespace {
+
+/* RenderCore::Render + FinalizeRender of the filter core (lib/RenderCore_Optix7Filter/rendercore.cpp:737-797,
+ * 897-935) */
+int render_filtered(lh2g_context* ctx, const lh2g_view* view, int converge) {
+    if (converge == 1 || ctx->firstConverging) {
+        ctx->samplesTaken = 0;
+        ctx->firstConverging = true;   /* camRNGseed is not reset: every frame gets new noise */
+    }
+    if (converge == 0) ctx->firstConverging = false;
+    static const float haltonx[4] = {0.3f, 0.7f, 0.2f, 0.8f}, haltony[4] = {0.2f, 0.8f, 0.7f, 0.3f};
+    const float j0 = ctx->taaEnabled ? haltonx[ctx->frameCycle] : 0.0f;
+    const float j1 = ctx->taaEnabled ? haltony[ctx->frameCycle] : 0.0f;
+    ctx->frameCycle = (ctx->frameCycle + 1) & 3;
+    lh2g_view jv = *view;
+    for (int k = 0; k < 3; k++) {
+        const float right = view->p2[k] - view->p1[k], up = view->p3[k] - view->p1[k];
+        const float jitter = (j0 / (float)ctx->W) * right + (j1 / (float)ctx->H) * up;
+        jv.p1[k] += jitter, jv.p2[k] += jitter, jv.p3[k] += jitter;
+    }
+    jv.aperture = 0;
+    lh2g_render_params p;
+    memset(&p, 0, sizeof(p));
+    p.width = ctx->W, p.height = ctx->H, p.spp = ctx->spp, p.maxDepth = ctx->maxDepth, p.rrStartDepth = ctx->rrStart;
+    p.samplesTaken = ctx->samplesTaken;
+    p.frameSeed = xorshift(ctx->filterSeed);
+    p.geometryEpsilon = ctx->eps, p.clampValue = ctx->clampValue;
+    p.flags = LH2G_RP_FILTER | (ctx->nee ? LH2G_RP_NEE : 0) | LH2G_RP_DEPTH_W;
+    int r = lh2g_render_ex(ctx, &jv, &p, ctx->samplesTaken > 0 ? 1 : 0, nullptr, nullptr, nullptr);
+    if (r != LH2G_OK) return r;
+    ctx->samplesTaken += ctx->spp;
+    lh2g_filter_params fp;
+    memset(&fp, 0, sizeof(fp));
+    fp.prevView = ctx->havePrevView ? ctx->prevView : *view;
+    fp.j0 = j0, fp.j1 = j1, fp.prevj0 = ctx->prevj0, fp.prevj1 = ctx->prevj1;
+    fp.clampDirect = ctx->clampDirect, fp.clampIndirect = ctx->clampIndirect;
+    fp.samplesTaken = ctx->samplesTaken;
+    fp.camIsStationary = ctx->samplesTaken == ctx->spp ? 0 : 1;
+    fp.taa = ctx->taaEnabled;
+    r = lh2g_filter(ctx, &fp);
+    if (r != LH2G_OK) return r;
+    ctx->prevj0 = j0, ctx->prevj1 = j1;
+    ctx->prevView = *view, ctx->havePrevView = true;
+    ctx->lastFilter = fp, ctx->lastJittered = jv, ctx->lastParams = p;
+    return LH2G_OK;
+}
+
+}  // namespace
+
+int lh2g_filter(lh2g_context* ctx, const lh2g_filter_params* fp) {
+    if (!ctx || !fp) return LH2G_ERR_INVALID;
+    if (!ctx->svAlloc) return fail(ctx, LH2G_ERR_STATE, "filter: no filter-core frame rendered on this target");
+    if (fp->samplesTaken <= 0) return fail(ctx, LH2G_ERR_INVALID, "filter: samplesTaken must be positive");
+    cudaSetDevice(ctx->device);
+    SvgfBuffers b = ctx->sv;
+    b.accum = ctx->B.accum, b.target = ctx->B.frame;
+    SvgfArgs a;
+    a.W = ctx->W, a.H = ctx->H;
+    a.scale = 1.0f / (float)fp->samplesTaken;
+    a.j0 = fp->j0, a.j1 = fp->j1, a.prevj0 = fp->prevj0, a.prevj1 = fp->prevj1;
+    a.clampDirect = fp->clampDirect, a.clampIndirect = fp->clampIndirect;
+    a.camIsStationary = fp->camIsStationary;
+    a.view = svgf_view(fp->prevView, ctx->H);
+    CK(cudaEventRecord(ctx->fev[0], ctx->st));
+    launch_svgf(b, a, fp->taa != 0, ctx->st);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->fev[1], ctx->st));
+    ctx->filterPending = true;
+    SvgfBuffers& v = ctx->sv;
+    if (fp->taa) std::swap(v.taaPixels, v.prevPixels);
+    else std::swap(v.shading, v.prevPixels);
+    std::swap(v.filteredIN, v.filteredOUT);
+    std::swap(v.prevWorldPos, v.worldPos);
+    std::swap(v.moments, v.prevMoments);
+    return LH2G_OK;
+}
+
+int lh2g_read_filter_buffer(lh2g_context* ctx, int slot, void* host) {
+    if (!ctx || !host || slot < 0 || slot >= LH2G_FB_COUNT) return LH2G_ERR_INVALID;
+    if (!ctx->svAlloc) return fail(ctx, LH2G_ERR_STATE, "read_filter_buffer: no filter buffers");
+    const size_t WH = (size_t)ctx->W * ctx->H;
+    const SvgfBuffers& v = ctx->sv;
+    const void* src = nullptr;
+    size_t bytes = sizeof(float4) * WH;
+    switch (slot) {
+        case LH2G_FB_FEATURES: src = v.features; break;
+        case LH2G_FB_WORLDPOS: src = v.worldPos; break;
+        case LH2G_FB_PREV_WORLDPOS: src = v.prevWorldPos; break;
+        case LH2G_FB_DELTADEPTH: src = v.deltaDepth; break;
+        case LH2G_FB_MOTION: src = v.motion, bytes = sizeof(float2) * WH; break;
+        case LH2G_FB_MOMENTS: src = v.moments; break;
+        case LH2G_FB_PREV_MOMENTS: src = v.prevMoments; break;
+        case LH2G_FB_SHADING: src = v.shading; break;
+        case LH2G_FB_FILTERED_IN: src = v.filteredIN; break;
+        case LH2G_FB_FILTERED_OUT: src = v.filteredOUT; break;
+        case LH2G_FB_PREV_PIXELS: src = v.prevPixels; break;
+        default: src = ctx->B.accum, bytes = 2 * sizeof(float4) * WH; break;
+    }
+    CK(cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return LH2G_OK;
+}
+
+int lh2g_get_last_filter_frame(lh2g_context* ctx, lh2g_filter_params* filter, lh2g_view* jitteredView, lh2g_render_params* params) {
+    if (!ctx) return LH2G_ERR_INVALID;
+    if (filter) *filter = ctx->lastFilter;
+    if (jitteredView) *jitteredView = ctx->lastJittered;
+    if (params) *params = ctx->lastParams;
+    return LH2G_OK;
+}
+
 int lh2g_render(lh2g_context* ctx, const lh2g_view* view, int converge) {
     if (!ctx || !view) return LH2G_ERR_INVALID;
+    if (ctx->filterEnabled) {
+        if (!ctx->cap) return fail(ctx, LH2G_ERR_STATE, "render: no target (call lh2g_set_target)");
+        return render_filtered(ctx, view, converge);
+    }
     if (converge == 1 || ctx->firstConverging) {
         ctx->samplesTaken = 0;
         ctx->firstConverging = true;
@@ -652,6 +872,13 @@ int lh2g_get_stats(lh2g_context* ctx, lh2g_stats* out) {
         ctx->stats.deviceStatus = C.status;
         ctx->statsPending = false;
     }
+    if (ctx->filterPending) {   /* RenderCore_Optix7Filter/rendercore.cpp:868 */
+        CK(cudaEventSynchronize(ctx->fev[1]));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->fev[0], ctx->fev[1]);
+        ctx->stats.filterTime = ms;
+        ctx->filterPending = false;
+    }
     *out = ctx->stats;
     return LH2G_OK;
 }
@@ -674,6 +901,7 @@ int lh2g_read_framebuffer(lh2g_context* ctx, float* host) {
 int lh2g_read_accumulator(lh2g_context* ctx, float* host) {
     if (!ctx || !host) return LH2G_ERR_INVALID;
     if (!ctx->cap) return fail(ctx, LH2G_ERR_STATE, "no target");
+    /* the direct half only when filter frames split it (LH2G_FB_ACCUM reads both) */
     CK(cudaMemcpyAsync(host, ctx->B.accum, sizeof(float4) * (size_t)ctx->W * ctx->H, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     return LH2G_OK;

@@ -66,6 +66,7 @@ struct SceneGPU {
 struct FrameGPU {
     int W, H, spp, maxDepth, rrStart, samplesTaken;
     uint32_t cameraR0;
+    uint32_t frameSeed;              /* LH2G_RP_FILTER: shading R0 = frameSeed + depth * 91771 */
     float eps;
     int flags;
     float spreadAngle, aperture;

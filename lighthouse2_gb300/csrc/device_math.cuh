@@ -7,6 +7,7 @@
  */
 #pragma once
 #include <cstdint>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #define LH2G_DEV static __device__ __forceinline__

@@ -14,6 +14,7 @@
  */
 #include "kernels.cuh"
 #include "shading.cuh"
+#include "svgf.cuh"
 #include "traverse.cuh"
 
 namespace lh2g {
@@ -35,9 +36,14 @@ __global__ void __launch_bounds__(256) k_generate(const FrameGPU F, const WaveBu
     uint32_t seed = WangHash(jobIndex + F.cameraR0);
     const float r0 = RandomFloat(seed), r1 = RandomFloat(seed);
     const float r2 = RandomFloat(seed), r3 = RandomFloat(seed);
-    const float3 posOnPixel = F.p1 + ((float)x + r0) * (F.right / (float)F.W) + ((float)y + r1) * (F.up / (float)F.H);
-    float3 posOnLens;
-    {
+    float3 posOnPixel, posOnLens;
+    if (F.flags & LH2G_RP_FILTER) {
+        /* filter core: pixel corner of the jittered view, no lens (RenderCore_Optix7Filter/optix/.optix.cu:66-100) */
+        const float u = (float)x * (1.0f / (float)F.W), v = (float)y * (1.0f / (float)F.H);
+        posOnPixel = F.p1 + u * F.right + v * F.up;
+        posOnLens = F.pos;
+    } else {
+        posOnPixel = F.p1 + ((float)x + r0) * (F.right / (float)F.W) + ((float)y + r1) * (F.up / (float)F.H);
         const float blade = (float)f2i(r2 * 9);
         float rr2 = (r2 - blade * (1.0f / 9.0f)) * 9.0f, rr1 = r3;
         float x1, y1, x2, y2;
@@ -53,6 +59,7 @@ __global__ void __launch_bounds__(256) k_generate(const FrameGPU F, const WaveBu
     B.D[0][i] = make_float4(D.x, D.y, D.z, __uint_as_float(S_SPECULAR));
     B.T[0][i] = make_float4(1.0f, 1.0f, 1.0f, F.eps);
     B.pathAcc[i] = make_float4(0, 0, 0, 0);
+    if (F.flags & LH2G_RP_FILTER) B.pathAcc[i + F.P] = make_float4(0, 0, 0, 0);
 }
 
 __device__ __forceinline__ uint32_t queue_count(const FrameGPU& F, const Counters* C, int depth) {
@@ -110,13 +117,33 @@ __device__ __forceinline__ void shade_path(const SceneGPU& S, const FrameGPU& F,
     const int PRIM = __float_as_int(hit.z), INST = __float_as_int(hit.y);
     const float HIT_T = hit.w;
     const size_t capIdx = (size_t)(depth - 1) * F.P + pathIdx;
-    const uint32_t R0 = (uint32_t)F.samplesTaken * 7907u + (uint32_t)depth * 91771u;
-    float4 acc = B.pathAcc[pathIdx];
+    const bool filt = (F.flags & LH2G_RP_FILTER) != 0;
+    const uint32_t R0 = filt ? F.frameSeed + (uint32_t)depth * 91771u : (uint32_t)F.samplesTaken * 7907u + (uint32_t)depth * 91771u;
+    /* radiance goes to the indirect half once the path has bounced off a diffuse vertex */
+    const uint32_t half = filt && (FLAGS & S_BOUNCED) ? 1u : 0u;
+    float4* accP = B.pathAcc + (half ? F.P : 0) + pathIdx;
+    /* SVGF data of sample 0 (RenderCore_Optix7Filter/kernels/pathtracer.h:95-104) */
+    const uint32_t WH = (uint32_t)F.W * (uint32_t)F.H;
+    const bool firstHitToBeStored = filt && (FLAGS & S_BOUNCED) == 0 && pathIdx / WH + (uint32_t)F.samplesTaken == 0;
+    const uint32_t isSpecular = (FLAGS & S_VIASPECULAR) ? 1u : 0u;
+    if (depth == 1 && firstHitToBeStored) {
+        PackFeatures(B.features + pathIdx, 0, 0, 1e34f, 0, 0);
+        B.worldPos[pathIdx] = make_float4(0, 0, 0, __uint_as_float(0));
+        B.deltaDepth[pathIdx] = make_float4(0, 0, 0, 0);
+    }
+    float4 acc = *accP;
     if ((F.flags & LH2G_RP_DEPTH_W) && depth == 1) acc.w += PRIM == NOHIT ? 10000.0f : HIT_T;
     if (PRIM == NOHIT) {
         const float3 c = throughput * SampleSkydome(S, D);
         acc.x += c.x, acc.y += c.y, acc.z += c.z;
-        B.pathAcc[pathIdx] = acc;
+        *accP = acc;
+        if (firstHitToBeStored) {
+            const uint32_t packedNormal = PackNormal2(D * -1.0f) + isSpecular;
+            PackFeatures(B.features + pathIdx, HDRtoRGB32(c), packedNormal, HIT_T, isSpecular, 0);
+            const float3 far = O + 50000 * D;
+            B.worldPos[pathIdx] = make_float4(far.x, far.y, far.z, __uint_as_float(packedNormal));
+            B.deltaDepth[pathIdx] = make_float4(0, 0, 0, 0);
+        }
         if (B.capSeeds) B.capSeeds[capIdx] = 0;
         return;
     }
@@ -129,19 +156,44 @@ __device__ __forceinline__ void shade_path(const SceneGPU& S, const FrameGPU& F,
     const float coneWidth = F.spreadAngle * HIT_T;
     GetShadingData(S, D, HIT_U, HIT_V, coneWidth, INST, PRIM, sd, N, iN, fN, T);
     const bool nee = (F.flags & LH2G_RP_NEE) != 0;
+    auto matID = [&]() {   /* ShadingData::matID is never assigned in the reference; the material index is what it names */
+        return min(__float_as_uint(__ldg(S.instTris[INST] + (size_t)PRIM * 13 + 1).w), (uint32_t)(S.nMaterials - 1));
+    };
+    auto derivatives = [&]() {
+        return DepthDerivatives((int)(pathIdx % (uint32_t)F.W), (int)(pathIdx / (uint32_t)F.W), F.W, F.H, HIT_T, I, N, F.p1, F.right, F.up, F.pos);
+    };
     if (IsEmissive(sd)) {
         const float DdotNL = -dot(D, N);
         if (DdotNL > 0) {
             const float3 c = throughput * sd.color;
             if (depth == 1 || (FLAGS & S_SPECULAR) || !nee) acc.x += c.x, acc.y += c.y, acc.z += c.z;
         }
-        B.pathAcc[pathIdx] = acc;
+        *accP = acc;
+        if (firstHitToBeStored) {
+            const uint32_t packedNormal = PackNormal2(N) + isSpecular;
+            PackFeatures(B.features + pathIdx, HDRtoRGB32(sd.color), packedNormal, HIT_T, isSpecular, matID());
+            B.worldPos[pathIdx] = make_float4(I.x, I.y, I.z, __uint_as_float(packedNormal));
+            B.deltaDepth[pathIdx] = derivatives();
+        }
         if (B.capSeeds) B.capSeeds[capIdx] = 0;
         return;
     }
-    B.pathAcc[pathIdx] = acc;
+    *accP = acc;
     if (ROUGHNESS(sd) <= 0.001f || TRANSMISSION(sd) > 0.999f) FLAGS |= S_SPECULAR; else FLAGS &= ~S_SPECULAR;
     uint32_t seed = WangHash(pathIdx * 17u + R0);
+    if (firstHitToBeStored) {
+        if (FLAGS & S_SPECULAR) {
+            B.features[pathIdx].x = HDRtoRGB32(sd.color);   /* modulated by the first diffuse vertex later */
+        } else {
+            float3 albedo = sd.color;
+            if (FLAGS & S_VIASPECULAR) albedo = albedo * RGB32toHDR(B.features[pathIdx].x);
+            /* the reference writes flip ? -fN : fN with flip = +-1, which always takes the first branch */
+            const uint32_t packedNormal = PackNormal2(fN * -1.0f) + isSpecular;
+            PackFeatures(B.features + pathIdx, HDRtoRGB32(albedo), packedNormal, HIT_T, isSpecular, matID());
+            B.worldPos[pathIdx] = make_float4(I.x, I.y, I.z, __uint_as_float(packedNormal));
+            B.deltaDepth[pathIdx] = derivatives();
+        }
+    }
     const float faceDir = (dot(D, N) > 0) ? -1.0f : 1.0f;
     if (faceDir == 1) sd.transmittance = mk3(0);
     if ((FLAGS & S_SPECULAR) == 0 && nee) {
@@ -160,8 +212,14 @@ __device__ __forceinline__ void shade_path(const SceneGPU& S, const FrameGPU& F,
             out.shadow = true;
             out.sO = make_float4(SO.x, SO.y, SO.z, __uint_as_float(pathIdx));
             out.sD = make_float4(L.x, L.y, L.z, dist - 2 * F.eps);
-            out.sE = make_float4(contribution.x, contribution.y, contribution.z, 0.0f);
+            out.sE = make_float4(contribution.x, contribution.y, contribution.z, __uint_as_float(half));
         }
+    }
+    if (depth == F.maxDepth && firstHitToBeStored) {
+        /* the path ends before its first diffuse bounce (RenderCore_Optix7Filter/kernels/pathtracer.h:288-299) */
+        const uint32_t packedNormal = PackNormal2(N) + isSpecular;
+        PackFeatures(B.features + pathIdx, 0, packedNormal, HIT_T, isSpecular, 0);
+        B.worldPos[pathIdx] = make_float4(I.x, I.y, I.z, __uint_as_float(packedNormal));
     }
     float3 R;
     float newBsdfPdf;
@@ -174,6 +232,7 @@ __device__ __forceinline__ void shade_path(const SceneGPU& S, const FrameGPU& F,
     const float pr = depth == F.maxDepth ? 0.0f : (((FLAGS & S_SPECULAR) || depth < F.rrStart) ? 1.0f : SurvivalProbability(bsdf));
     if (pr <= q5) return;
     throughput = throughput * (bsdf * fabsf(dot(fN, R)) / (pr * newBsdfPdf));
+    if (!(FLAGS & S_SPECULAR)) FLAGS |= S_BOUNCED; else FLAGS |= S_VIASPECULAR;
     const float3 EO = SafeOrigin(I, R, N, F.eps);
     out.ext = true;
     out.eO = make_float4(EO.x, EO.y, EO.z, __uint_as_float(pathIdx));
@@ -221,9 +280,10 @@ __global__ void __launch_bounds__(128) k_connect(const SceneGPU S, const FrameGP
     auto add = [&](uint32_t i) {
         const float4 e = B.shE[i];
         const uint32_t pathIdx = __float_as_uint(B.shO[i].w);
-        float4 acc = B.pathAcc[pathIdx];
+        float4* accP = B.pathAcc + (__float_as_uint(e.w) ? F.P : 0) + pathIdx;   /* e.w: indirect half */
+        float4 acc = *accP;
         acc.x += e.x, acc.y += e.y, acc.z += e.z;
-        B.pathAcc[pathIdx] = acc;
+        *accP = acc;
     };
     trace_queue_any<true>(S, &C->fetch[64 + depth - 1], count, status, stackBase,
         [&](uint32_t i, float3& o, float3& d, float& t0, float& t1) {
@@ -241,13 +301,17 @@ __global__ void k_finalize(const FrameGPU F, const WaveBuffers B, const float sc
     const int64_t px = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t WH = (int64_t)F.W * F.H;
     if (px >= WH) return;
-    float4 acc = B.accum[px];
-    for (int s = 0; s < F.spp; s++) {
-        const float4 v = B.pathAcc[s * WH + px];
-        acc.x += v.x, acc.y += v.y, acc.z += v.z, acc.w += v.w;
+    const bool filt = (F.flags & LH2G_RP_FILTER) != 0;
+    for (int half = 0; half < (filt ? 2 : 1); half++) {
+        float4 acc = B.accum[half * WH + px];
+        for (int s = 0; s < F.spp; s++) {
+            const float4 v = B.pathAcc[half * F.P + s * WH + px];
+            acc.x += v.x, acc.y += v.y, acc.z += v.z, acc.w += v.w;
+        }
+        B.accum[half * WH + px] = acc;
+        /* LH2G_RP_FILTER frames are presented by the filter */
+        if (!filt) B.frame[px] = make_float4(acc.x * scale, acc.y * scale, acc.z * scale, acc.w * scale);
     }
-    B.accum[px] = acc;
-    B.frame[px] = make_float4(acc.x * scale, acc.y * scale, acc.z * scale, acc.w * scale);
 }
 
 /* -------------------------------------------------------------------------------------------------- */

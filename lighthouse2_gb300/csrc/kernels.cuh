@@ -14,10 +14,13 @@ struct WaveBuffers {
     float4* shO;           /* connections: origin (w = path index), direction (w = tmax), contribution */
     float4* shD;
     float4* shE;
-    float4* pathAcc;       /* per-path radiance (w = primary distance) */
+    float4* pathAcc;       /* per-path radiance (w = primary distance); LH2G_RP_FILTER frames add an indirect half at + P */
     float4* accum;         /* per-pixel accumulator across frames */
     float4* frame;         /* finalized output: accum / samplesTaken */
     Counters* counters;
+    uint4* features;       /* LH2G_RP_FILTER: SVGF features, world position and depth derivatives of sample 0 (W*H) */
+    float4* worldPos;
+    float4* deltaDepth;
     lh2g_hit* capHits;     /* optional per-(depth, path) capture */
     uint32_t* capSeeds;
 };

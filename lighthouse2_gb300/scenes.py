@@ -383,8 +383,9 @@ def cornell_sphere(seed=1, subdiv=6):
     return s
 
 
-def cornell_view(width=512, height=512):
-    return make_view((0.0, 1.0, 0.95), (0.0, 0.9, -1.0), 65.0, width, height)
+def cornell_view(width=512, height=512, frame=0):
+    """Camera in the open side of the room; frame > 0 moves it along a short seeded-free dolly (for the filter)."""
+    return make_view((0.02 * frame, 1.0 - 0.01 * frame, 0.95), (0.0, 0.9, -1.0), 65.0, width, height)
 
 
 def _rotation(rng):

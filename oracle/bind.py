@@ -19,8 +19,11 @@ REFERENCE_TREE = os.environ.get("LH2_REFERENCE", "/root/reference")
 
 PARAMS_DTYPE = np.dtype([("width", "<i4"), ("height", "<i4"), ("spp", "<i4"), ("maxDepth", "<i4"),
                          ("rrStartDepth", "<i4"), ("samplesTaken", "<i4"), ("cameraR0", "<u4"),
-                         ("geometryEpsilon", "<f4"), ("clampValue", "<f4"), ("flags", "<i4")])
-RP_NEE, RP_DEPTH_W = 1, 2
+                         ("geometryEpsilon", "<f4"), ("clampValue", "<f4"), ("flags", "<i4"), ("frameSeed", "<u4")])
+FILTER_PARAMS_DTYPE = np.dtype([("prevView", S.VIEW_DTYPE), ("j0", "<f4"), ("j1", "<f4"), ("prevj0", "<f4"), ("prevj1", "<f4"),
+                                ("clampDirect", "<f4"), ("clampIndirect", "<f4"), ("samplesTaken", "<i4"),
+                                ("camIsStationary", "<i4"), ("taa", "<i4")])
+RP_NEE, RP_DEPTH_W, RP_FILTER = 1, 2, 4
 
 
 def build_oracle():
@@ -38,11 +41,11 @@ def build_ref():
 
 
 def make_params(width, height, spp=1, max_depth=3, rr_start=1, samples_taken=0, camera_r0=0, eps=1e-3,
-                clamp=10.0, flags=RP_NEE):
+                clamp=10.0, flags=RP_NEE, frame_seed=0):
     p = np.zeros((), PARAMS_DTYPE)
     p["width"], p["height"], p["spp"], p["maxDepth"] = width, height, spp, max_depth
     p["rrStartDepth"], p["samplesTaken"], p["cameraR0"] = rr_start, samples_taken, camera_r0
-    p["geometryEpsilon"], p["clampValue"], p["flags"] = eps, clamp, flags
+    p["geometryEpsilon"], p["clampValue"], p["flags"], p["frameSeed"] = eps, clamp, flags, frame_seed
     return p
 
 
@@ -82,6 +85,8 @@ class Oracle:
         L.lh2o_finalize.argtypes = [C.c_void_p]
         L.lh2o_trace.argtypes = [C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int]
         L.lh2o_render.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        L.lh2o_render_ex.argtypes = [C.c_void_p] * 8 + [C.c_int]
+        L.lh2o_svgf_frame.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         self.s = L.lh2o_create()
         self._keep = []
 
@@ -120,11 +125,14 @@ class Oracle:
         assert self.lib.lh2o_trace(self.s, _p(rays), n, 1, int(brute), None, _p(occ), nthreads) == 0
         return occ
 
-    def render(self, view, params, accum=None, accum64=False, capture=False, nthreads=0):
+    def render(self, view, params, accum=None, accum64=False, capture=False, nthreads=0, features=None):
+        """One frame. LH2G_RP_FILTER frames accumulate 2*W*H pixels (direct, then indirect) and write the SVGF
+        features into `features` (an SvgfState, or None)."""
         W, H, spp, D = int(params["width"]), int(params["height"]), int(params["spp"]), int(params["maxDepth"])
+        halves = 2 if int(params["flags"]) & RP_FILTER else 1
         if accum is None:
-            accum = np.zeros((H * W, 4), np.float32)
-        a64 = np.zeros((H * W, 4), np.float64) if accum64 else None
+            accum = np.zeros((halves * H * W, 4), np.float32)
+        a64 = np.zeros((halves * H * W, 4), np.float64) if accum64 else None
         counters = np.zeros((D, 2), np.uint32)
         cap = None
         hits = seeds = None
@@ -132,8 +140,9 @@ class Oracle:
             hits = np.zeros(D * W * H * spp, S.HIT_DTYPE)
             seeds = np.zeros(D * W * H * spp, np.uint32)
             cap = _Capture(hits.ctypes.data, seeds.ctypes.data)
-        rc = self.lib.lh2o_render(self.s, _p(view), _p(params), _p(accum), _p(a64), _p(counters),
-                                  C.byref(cap) if cap is not None else None, nthreads)
+        feat = _Features(features.ptr("features"), features.ptr("worldPos"), features.ptr("deltaDepth")) if features is not None else None
+        rc = self.lib.lh2o_render_ex(self.s, _p(view), _p(params), _p(accum), _p(a64), _p(counters),
+                                     C.byref(cap) if cap is not None else None, C.byref(feat) if feat is not None else None, nthreads)
         assert rc == 0
         out = {"accum": accum, "counters": counters}
         if accum64:
@@ -142,6 +151,54 @@ class Oracle:
             out["hits"] = hits.reshape(D, -1)
             out["seeds"] = seeds.reshape(D, -1)
         return out
+
+
+class _Features(C.Structure):
+    _fields_ = [("features", C.c_void_p), ("worldPos", C.c_void_p), ("deltaDepth", C.c_void_p)]
+
+
+SVGF_SLOTS = ["features", "worldPos", "prevWorldPos", "deltaDepth", "motion", "moments", "prevMoments", "shading", "filteredIN",
+              "filteredOUT", "prevPixels", "taaPixels", "target"]
+
+
+class _Svgf(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int)] + [(n, C.c_void_p) for n in SVGF_SLOTS]
+
+
+class SvgfState:
+    """The oracle's SVGF buffers of one W x H target (zeroed, like the GPU core's at allocation). Slot names
+    follow the GPU core's: lh2o_svgf_frame swaps the history slots exactly as the core does."""
+
+    def __init__(self, oracle: Oracle, width, height):
+        self.oracle, self.W, self.H = oracle, width, height
+        n = width * height
+        self.arrays = {}
+        for name in SVGF_SLOTS:
+            dt, comps = (np.uint32, 4) if name == "features" else (np.float32, 2 if name == "motion" else 4)
+            self.arrays[name] = np.zeros((n, comps), dt)
+        self.slot = {name: name for name in SVGF_SLOTS}       # slot -> array key
+
+    def __getitem__(self, slot):
+        return self.arrays[self.slot[slot]]
+
+    def ptr(self, slot):
+        return self[slot].ctypes.data
+
+    def frame(self, accum, fparams, nthreads=0):
+        st = _Svgf(self.W, self.H, *[self.ptr(n) for n in SVGF_SLOTS])
+        assert self.oracle.lib.lh2o_svgf_frame(C.byref(st), _p(np.ascontiguousarray(accum)), _p(np.ascontiguousarray(fparams)),
+                                               nthreads) == 0
+        by_addr = {self.arrays[k].ctypes.data: k for k in self.arrays}
+        self.slot = {n: by_addr[getattr(st, n)] for n in SVGF_SLOTS}
+
+
+def make_filter_params(prev_view, j0, j1, prevj0, prevj1, samples_taken, cam_is_stationary, taa, clamp_direct=2.5, clamp_indirect=15.0):
+    fp = np.zeros((), FILTER_PARAMS_DTYPE)
+    fp["prevView"] = prev_view
+    fp["j0"], fp["j1"], fp["prevj0"], fp["prevj1"] = j0, j1, prevj0, prevj1
+    fp["clampDirect"], fp["clampIndirect"] = clamp_direct, clamp_indirect
+    fp["samplesTaken"], fp["camIsStationary"], fp["taa"] = samples_taken, cam_is_stationary, taa
+    return fp
 
 
 TEXDESC_DTYPE = np.dtype([("texels", "<u8"), ("width", "<u4"), ("height", "<u4"), ("flags", "<u4"),

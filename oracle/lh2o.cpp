@@ -84,6 +84,8 @@ constexpr float EPSILON = 0.0001f;                    /* common_settings.h:53 */
 constexpr int MIPLEVELCOUNT = 5;                      /* common_settings.h:57 */
 constexpr int NOHIT = -1;
 constexpr uint S_SPECULAR = 1;                        /* RenderCore_PrimeRef/kernels/pathtracer.h:29 */
+constexpr uint S_BOUNCED = 2;                         /* RenderCore_Optix7Filter/kernels/pathtracer.h:30-31 */
+constexpr uint S_VIASPECULAR = 4;
 
 /* ------------------------------------------------------------------------------------------------------
  * Transcendental functions. The reference calls the CUDA library (sincosf, __sincosf, expf, __expf,
@@ -945,9 +947,61 @@ struct Frame {
     lh2g_render_params p;
     f3 right, up;
     long long P;
+    lh2o_features feat;        /* LH2G_RP_FILTER: SVGF feature buffers (W*H entries each) */
 };
 
-struct PathOut { float rgbw[4]; };
+/* Radiance of one path: rgbw[0] = the direct half (and the primary distance in w), rgbw[1] = the indirect
+ * half (only LH2G_RP_FILTER frames route radiance there). */
+struct PathOut { float rgbw[2][4]; };
+
+/* ------------------------------------------------------------------------------------------------------
+ * SVGF feature packing (lib/CUDA/shared_kernel_code/tools_shared.h:122-136, 157-183, 282-304)
+ * ---------------------------------------------------------------------------------------------------- */
+inline uint umin(uint a, uint b) { return a < b ? a : b; }
+inline uint umax(uint a, uint b) { return a > b ? a : b; }
+/* PackNormal2: 10 bits per component at bits 2, 12, 22; bits 0-1 stay free for the specular flag */
+inline uint PackNormal2(const f3 N) {
+    const uint x = umin(f2u((N.x + 1) * 511), 1023u);
+    const uint y = umin(f2u((N.y + 1) * 511), 1023u);
+    const uint z = umin(f2u((N.z + 1) * 511), 1023u);
+    return (x << 2u) + (y << 12u) + (z << 22u);
+}
+inline f3 UnpackNormal2(const uint pi) {
+    const uint x = (pi >> 2u) & 1023u, y = (pi >> 12u) & 1023u, z = pi >> 22u;
+    return mk3((float)x * (1.0f / 511.0f) - 1, (float)y * (1.0f / 511.0f) - 1, (float)z * (1.0f / 511.0f) - 1);
+}
+/* HDRtoRGB32: 10:11:11 unsigned fixed point of min(1, c) */
+inline uint HDRtoRGB32(const f3& c) {
+    const uint r = f2u(1023.0f * fminr(1.0f, c.x));
+    const uint g = f2u(2047.0f * fminr(1.0f, c.y));
+    const uint b = f2u(2047.0f * fminr(1.0f, c.z));
+    return (r << 22) + (g << 11) + b;
+}
+inline f3 RGB32toHDR(const uint c) {
+    return mk3((float)(c >> 22) * (1.0f / 1023.0f), (float)((c >> 11) & 2047) * (1.0f / 2047.0f), (float)(c & 2047) * (1.0f / 2047.0f));
+}
+inline f3 RGB32toHDRmin1(const uint c) {
+    return mk3((float)umax(1u, c >> 22) * (1.0f / 1023.0f), (float)umax(1u, (c >> 11) & 2047) * (1.0f / 2047.0f),
+               (float)umax(1u, c & 2047) * (1.0f / 2047.0f));
+}
+/* PackFeatures (RenderCore_Optix7Filter/kernels/pathtracer.h:44-47): the history count in w & 15 survives */
+inline void PackFeatures(uint* f, const uint albedo, const uint packedNormal, const float t, const uint isSpecular, const uint matid) {
+    const uint w = (isSpecular << 4) + (matid << 6) + (f[3] & 15);
+    f[0] = albedo, f[1] = packedNormal, f[2] = fbits(t), f[3] = w;
+}
+inline void store4(float* d, float x, float y, float z, float w) { d[0] = x, d[1] = y, d[2] = z, d[3] = w; }
+/* calculateDepthDerivatives (RenderCore_Optix7Filter/kernels/pathtracer.h:48-57): depth change of the rays
+ * through the pixels right of and below (x, y) where they meet the plane of the hit. The plane is the one
+ * through the hit point I with the world-space geometric normal N; the reference takes vertex 0 and the face
+ * normal of the object-space triangle, the same plane when the instance transform is the identity. */
+inline void DepthDerivatives(const int x, const int y, const int w, const int h, const float depth, const f3& I, const f3& N,
+                             const f3& p1, const f3& p2, const f3& p3, const f3& pos, float* out) {
+    const f3 rayDXDir = normalize((p1 + (float)(x + 0.5f + 1) * (1.0f / w) * p2 + (float)(y + 0.5f) * (1.0f / h) * p3) - pos);
+    const float rayDXDepth = dot(I - pos, N) / dot(N, rayDXDir);
+    const f3 rayDYDir = normalize((p1 + (float)(x + 0.5f) * (1.0f / w) * p2 + (float)(y + 0.5f + 1) * (1.0f / h) * p3) - pos);
+    const float rayDYDepth = dot(I - pos, N) / dot(N, rayDYDir);
+    store4(out, 0, 0, rayDXDepth - depth, rayDYDepth - depth);
+}
 
 void trace_path(const Frame& F, const uint jobIndex, PathOut& out, std::vector<uint>& ext, std::vector<uint>& shad, lh2g_capture* cap) {
     const lh2o_scene* s = F.s;
@@ -955,6 +1009,8 @@ void trace_path(const Frame& F, const uint jobIndex, PathOut& out, std::vector<u
     const int W = p.width, H = p.height;
     const float eps = p.geometryEpsilon;
     const bool nee = (p.flags & LH2G_RP_NEE) != 0;
+    const bool filt = (p.flags & LH2G_RP_FILTER) != 0;
+    const uint WH = (uint)W * (uint)H;
     /* generateEyeRaysKernel */
     const uint x = jobIndex % (uint)W;
     uint y = jobIndex / (uint)W;
@@ -963,36 +1019,66 @@ void trace_path(const Frame& F, const uint jobIndex, PathOut& out, std::vector<u
     const float r0 = RandomFloat(seed), r1 = RandomFloat(seed);
     const float r2 = RandomFloat(seed), r3 = RandomFloat(seed);
     const f3 p1 = ld3(F.view.p1), pos = ld3(F.view.pos);
-    const f3 posOnPixel = p1 + ((float)x + r0) * (F.right / (float)W) + ((float)y + r1) * (F.up / (float)H);
-    f3 posOnLens;
-    {   /* RandomPointOnLens, camera.h:22-33 */
-        const float blade = (float)f2i(r2 * 9);
-        float rr2 = (r2 - blade * (1.0f / 9.0f)) * 9.0f, rr1 = r3;
-        float x1, y1, x2, y2;
-        lm_sincos(blade * PI / 4.5f, &x1, &y1);
-        lm_sincos((blade + 1.0f) * PI / 4.5f, &x2, &y2);
-        if ((rr1 + rr2) > 1) rr1 = 1.0f - rr1, rr2 = 1.0f - rr2;
-        const float xr = x1 * rr1 + x2 * rr2;
-        const float yr = y1 * rr1 + y2 * rr2;
-        posOnLens = pos + F.view.aperture * (F.right * xr + F.up * yr);
+    f3 O, D;
+    if (filt) {
+        /* filter core: pixel corner of the jittered view, no lens (RenderCore_Optix7Filter/optix/.optix.cu:66-100) */
+        const float u = (float)x * (1.0f / (float)W), v = (float)y * (1.0f / (float)H);
+        const f3 posOnPixel = p1 + u * F.right + v * F.up;
+        O = pos, D = normalize(posOnPixel - pos);
+    } else {
+        const f3 posOnPixel = p1 + ((float)x + r0) * (F.right / (float)W) + ((float)y + r1) * (F.up / (float)H);
+        f3 posOnLens;
+        {   /* RandomPointOnLens, camera.h:22-33 */
+            const float blade = (float)f2i(r2 * 9);
+            float rr2 = (r2 - blade * (1.0f / 9.0f)) * 9.0f, rr1 = r3;
+            float x1, y1, x2, y2;
+            lm_sincos(blade * PI / 4.5f, &x1, &y1);
+            lm_sincos((blade + 1.0f) * PI / 4.5f, &x2, &y2);
+            if ((rr1 + rr2) > 1) rr1 = 1.0f - rr1, rr2 = 1.0f - rr2;
+            const float xr = x1 * rr1 + x2 * rr2;
+            const float yr = y1 * rr1 + y2 * rr2;
+            posOnLens = pos + F.view.aperture * (F.right * xr + F.up * yr);
+        }
+        O = posOnLens, D = normalize(posOnPixel - posOnLens);
     }
-    f3 O = posOnLens, D = normalize(posOnPixel - posOnLens);
     float tmin = eps;
     f3 throughput = mk3(1);
     uint FLAGS = S_SPECULAR;
     const uint pathIdx = jobIndex;
-    out.rgbw[0] = out.rgbw[1] = out.rgbw[2] = out.rgbw[3] = 0;
+    for (int h = 0; h < 2; h++) out.rgbw[h][0] = out.rgbw[h][1] = out.rgbw[h][2] = out.rgbw[h][3] = 0;
+    /* filter data of sample 0 (RenderCore_Optix7Filter/kernels/pathtracer.h:95-104) */
+    const uint sampleIdx = pathIdx / WH + (uint)p.samplesTaken;
+    uint* feat = filt && sampleIdx == 0 && F.feat.features ? F.feat.features + 4 * (size_t)pathIdx : nullptr;
+    float* wpos = feat ? F.feat.worldPos + 4 * (size_t)pathIdx : nullptr;
+    float* ddep = feat ? F.feat.deltaDepth + 4 * (size_t)pathIdx : nullptr;
+    const f3 vp2 = F.right, vp3 = F.up;   /* p2 - p1, p3 - p1 of the view */
     for (int pathLength = 1; pathLength <= p.maxDepth; pathLength++) {
         HitRec h;
         trace_scene(s, O, D, tmin, 1e34f, false, false, h);
         const lh2g_hit hit = make_hit(h);
         const long long capIdx = (long long)(pathLength - 1) * F.P + pathIdx;
         if (cap && cap->hits) cap->hits[capIdx] = hit;
-        const uint R0 = (uint)p.samplesTaken * 7907u + (uint)pathLength * 91771u;
-        if ((p.flags & LH2G_RP_DEPTH_W) && pathLength == 1) out.rgbw[3] += hit.prim == NOHIT ? 10000.0f : hit.t;
+        const uint R0 = filt ? p.frameSeed + (uint)pathLength * 91771u : (uint)p.samplesTaken * 7907u + (uint)pathLength * 91771u;
+        /* radiance goes to the indirect half once the path has bounced off a diffuse vertex */
+        float* acc = out.rgbw[filt && (FLAGS & S_BOUNCED) ? 1 : 0];
+        const bool firstHitToBeStored = feat && (FLAGS & S_BOUNCED) == 0;
+        const uint isSpecular = (FLAGS & S_VIASPECULAR) ? 1 : 0;
+        if (pathLength == 1 && firstHitToBeStored) {
+            PackFeatures(feat, 0, 0, 1e34f, 0, 0);
+            store4(wpos, 0, 0, 0, bitsf(0));
+            store4(ddep, 0, 0, 0, 0);
+        }
+        if ((p.flags & LH2G_RP_DEPTH_W) && pathLength == 1) acc[3] += hit.prim == NOHIT ? 10000.0f : hit.t;
         if (hit.prim == NOHIT) {
             const f3 c = throughput * SampleSkydome(s, D);
-            out.rgbw[0] += c.x, out.rgbw[1] += c.y, out.rgbw[2] += c.z;
+            acc[0] += c.x, acc[1] += c.y, acc[2] += c.z;
+            if (firstHitToBeStored) {
+                const uint packedNormal = PackNormal2(D * -1.0f) + isSpecular;
+                PackFeatures(feat, HDRtoRGB32(c), packedNormal, hit.t, isSpecular, 0);
+                const f3 far = O + 50000 * D;
+                store4(wpos, far.x, far.y, far.z, bitsf(packedNormal));
+                store4(ddep, 0, 0, 0, 0);
+            }
             if (cap && cap->seeds) cap->seeds[capIdx] = 0;
             return;
         }
@@ -1006,17 +1092,37 @@ void trace_path(const Frame& F, const uint jobIndex, PathOut& out, std::vector<u
         const f3 I = O + HIT_T * D;
         const float coneWidth = F.view.spreadAngle * HIT_T;
         GetShadingData(s, D, HIT_U, HIT_V, coneWidth, tri, INST, sd, N, iN, fN, T);
+        const uint matID = std::min<uint>(tri.material, (uint)s->mats.size() - 1);   /* ShadingData::matID is never assigned in the reference; the material index is what it names */
         if (IsEmissive(sd)) {
             const float DdotNL = -dot(D, N);
             if (DdotNL > 0) {
                 const f3 c = throughput * sd.color;
-                if (pathLength == 1 || (FLAGS & S_SPECULAR) || !nee) out.rgbw[0] += c.x, out.rgbw[1] += c.y, out.rgbw[2] += c.z;
+                if (pathLength == 1 || (FLAGS & S_SPECULAR) || !nee) acc[0] += c.x, acc[1] += c.y, acc[2] += c.z;
+            }
+            if (firstHitToBeStored) {
+                const uint packedNormal = PackNormal2(N) + isSpecular;
+                PackFeatures(feat, HDRtoRGB32(sd.color), packedNormal, HIT_T, isSpecular, matID);
+                store4(wpos, I.x, I.y, I.z, bitsf(packedNormal));
+                DepthDerivatives((int)(pathIdx % (uint)W), (int)(pathIdx / (uint)W), W, H, HIT_T, I, N, p1, vp2, vp3, pos, ddep);
             }
             if (cap && cap->seeds) cap->seeds[capIdx] = 0;
             return;
         }
         if (ROUGHNESS(sd) <= 0.001f || TRANSMISSION(sd) > 0.999f) FLAGS |= S_SPECULAR; else FLAGS &= ~S_SPECULAR;
         seed = WangHash(pathIdx * 17u + R0);
+        if (firstHitToBeStored) {
+            if (FLAGS & S_SPECULAR) {
+                feat[0] = HDRtoRGB32(sd.color);   /* modulated by the first diffuse vertex later */
+            } else {
+                f3 albedo = sd.color;
+                if (FLAGS & S_VIASPECULAR) albedo = albedo * RGB32toHDR(feat[0]);
+                /* the reference writes flip ? -fN : fN with flip = +-1, which always takes the first branch */
+                const uint packedNormal = PackNormal2(fN * -1.0f) + isSpecular;
+                PackFeatures(feat, HDRtoRGB32(albedo), packedNormal, HIT_T, isSpecular, matID);
+                store4(wpos, I.x, I.y, I.z, bitsf(packedNormal));
+                DepthDerivatives((int)(pathIdx % (uint)W), (int)(pathIdx / (uint)W), W, H, HIT_T, I, N, p1, vp2, vp3, pos, ddep);
+            }
+        }
         const float faceDir = (dot(D, N) > 0) ? -1.0f : 1.0f;
         if (faceDir == 1) sd.transmittance = mk3(0);
         if ((FLAGS & S_SPECULAR) == 0 && nee) {
@@ -1035,8 +1141,14 @@ void trace_path(const Frame& F, const uint jobIndex, PathOut& out, std::vector<u
                 HitRec sh;
                 const f3 SO = SafeOrigin(I, L, N, eps);
                 if (!trace_scene(s, SO, L, 0.0f, dist - 2 * eps, true, false, sh))
-                    out.rgbw[0] += contribution.x, out.rgbw[1] += contribution.y, out.rgbw[2] += contribution.z;
+                    acc[0] += contribution.x, acc[1] += contribution.y, acc[2] += contribution.z;
             }
+        }
+        if (pathLength == p.maxDepth && firstHitToBeStored) {
+            /* the path ends here before its first diffuse bounce (RenderCore_Optix7Filter/kernels/pathtracer.h:288-299) */
+            const uint packedNormal = PackNormal2(N) + isSpecular;
+            PackFeatures(feat, 0, packedNormal, HIT_T, isSpecular, 0);
+            store4(wpos, I.x, I.y, I.z, bitsf(packedNormal));
         }
         f3 R;
         float newBsdfPdf;
@@ -1050,6 +1162,7 @@ void trace_path(const Frame& F, const uint jobIndex, PathOut& out, std::vector<u
         if (pr <= q5) return;
         throughput = throughput * (bsdf * fabsf(dot(fN, R)) / (pr * newBsdfPdf));
         ext[pathLength - 1]++;
+        if (!(FLAGS & S_SPECULAR)) FLAGS |= S_BOUNCED; else FLAGS |= S_VIASPECULAR;
         O = SafeOrigin(I, R, N, eps);
         D = R;
         tmin = 0.0f;
@@ -1071,6 +1184,368 @@ void parallel_for(long long n, int nthreads, long long chunk, const std::functio
     for (int i = 0; i < nthreads; i++) ts.emplace_back(worker);
     for (auto& t : ts) t.join();
 }
+
+/* ------------------------------------------------------------------------------------------------------
+ * SVGF, lib/CUDA/shared_kernel_code/finalize_shared.h:169-600, one pixel per call, in the kernels' order
+ * ---------------------------------------------------------------------------------------------------- */
+inline f4 ld4(const float* p) { return {p[0], p[1], p[2], p[3]}; }
+inline f4 operator-(f4 a, f4 b) { return {a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w}; }
+inline float dot4(f4 a, f4 b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
+inline f3 fmin3(float a, f3 b) { return mk3(fminr(a, b.x), fminr(a, b.y), fminr(a, b.z)); }
+inline f3 fmin3(f3 a, float b) { return mk3(fminr(a.x, b), fminr(a.y, b), fminr(a.z, b)); }
+inline f3 fmax3(float a, f3 b) { return mk3(fmaxr(a, b.x), fmaxr(a, b.y), fmaxr(a, b.z)); }
+inline float clampf(float f, float a, float b) { return fmaxr(a, fminr(f, b)); }
+inline f3 clamp3(f3 v, f3 a, f3 b) { return mk3(clampf(v.x, a.x, b.x), clampf(v.y, a.y, b.y), clampf(v.z, a.z, b.z)); }
+inline f3 operator+(f3 a, float b) { return {a.x + b, a.y + b, a.z + b}; }
+
+inline float Luminance(const f3 rgb) { return 0.299f * fminr(rgb.x, 10.0f) + 0.587f * fminr(rgb.y, 10.0f) + 0.114f * fminr(rgb.z, 10.0f); }
+inline f3 RGBToYCoCg(const f3 RGB) {
+    const f3 rgb = fmin3(4.0f, RGB);
+    const float Y = dot(rgb, mk3(1, 2, 1)) * 0.25f;
+    const float Co = dot(rgb, mk3(2, 0, -2)) * 0.25f + (0.5f * 256.0f / 255.0f);
+    const float Cg = dot(rgb, mk3(-1, 2, -1)) * 0.25f + (0.5f * 256.0f / 255.0f);
+    return mk3(Y, Co, Cg);
+}
+inline f3 YCoCgToRGB(const f3 c) {
+    const float Y = c.x, Co = c.y - (0.5f * 256.0f / 255.0f), Cg = c.z - (0.5f * 256.0f / 255.0f);
+    return mk3(Y + Co - Cg, Y + Cg, Y - Co - Cg);
+}
+/* two non-negative rgb triples as 5:11 unsigned fixed point in the bits of one float4 */
+inline void CombineToFloat4(const f3& A, const f3& B, float* out) {
+    const uint Ar = f2u(fminr(A.x, 31.999f) * 2048.0f), Ag = f2u(fminr(A.y, 31.999f) * 2048.0f), Ab = f2u(fminr(A.z, 31.999f) * 2048.0f);
+    const uint Br = f2u(fminr(B.x, 31.999f) * 2048.0f), Bg = f2u(fminr(B.y, 31.999f) * 2048.0f), Bb = f2u(fminr(B.z, 31.999f) * 2048.0f);
+    out[0] = bitsf((Ar << 16) + Ag), out[1] = bitsf(Ab), out[2] = bitsf((Br << 16) + Bg), out[3] = bitsf(Bb);
+}
+inline f3 GetDirect(const float* X) {
+    const uint v0 = fbits(X[0]), v1 = fbits(X[1]);
+    return mk3((float)(v0 >> 16) * (1.0f / 2048.0f), (float)(v0 & 65535) * (1.0f / 2048.0f), (float)v1 * (1.0f / 2048.0f));
+}
+inline f3 GetIndirect(const float* X) {
+    const uint v2 = fbits(X[2]), v3 = fbits(X[3]);
+    return mk3((float)(v2 >> 16) * (1.0f / 2048.0f), (float)(v2 & 65535) * (1.0f / 2048.0f), (float)v3 * (1.0f / 2048.0f));
+}
+/* 2^-p for p in [0, 126] from the exponent bits (tools_shared.h:86) */
+inline float oneoverpow2(const int p) { return bitsf((uint)(127 - p) << 23); }
+/* x^128 by seven squarings; the reference calls powf(x, 128) */
+inline float pow128(float x) { for (int i = 0; i < 7; i++) x = x * x; return x; }
+inline float MitchellNetravali(const float v) {   /* sampling_shared.h:22-27, B = C = 1/3 */
+    const float B = 1.0f / 3.0f, C = 1.0f / 3.0f, x = fabsf(v), x2 = x * x, x3 = x2 * x;
+    if (x < 1) return (1.0f / 6.0f) * ((12 - 9 * B - 6 * C) * x3 + (-18 + 12 * B + 6 * C) * x2 + (6 - 2 * B));
+    else if (x < 2) return 1.0f / 6.0f * ((-B - 6 * C) * x3 + (6 * B + 30 * C) * x2 + (-12 * B - 48 * C) * x + (8 * B + 24 * C));
+    return 0.0f;
+}
+
+struct SvgfView { f4 prevPos, prevE, prevRight, prevUp; };
+/* host part of prepareFilter (finalize_shared.h:293-314): the previous camera as a plane and two screen axes */
+SvgfView svgf_view(const lh2g_view& v, int h) {
+    const f3 pos = ld3(v.pos), p1 = ld3(v.p1), p2 = ld3(v.p2), p3 = ld3(v.p3);
+    const f3 centre = 0.5f * (p2 + p3);
+    const f3 direction = normalize(centre - pos);
+    const f3 right = normalize(p2 - p1);
+    const f3 up = normalize(p3 - p1);
+    const float screenSize = length(p3 - p1);
+    const float lenReci = (float)h / screenSize;
+    SvgfView r;
+    r.prevPos = mk4(pos.x, pos.y, pos.z, -(dot(pos, direction) - dot(centre, direction)));
+    r.prevE = mk4(direction.x, direction.y, direction.z, 0);
+    const f3 rr = right * lenReci, uu = up * lenReci;
+    r.prevRight = mk4(rr.x, rr.y, rr.z, dot(p1, right) * lenReci);
+    r.prevUp = mk4(uu.x, uu.y, uu.z, dot(p1, up) * lenReci);
+    return r;
+}
+
+struct Svgf {
+    int w, h;
+    const lh2o_svgf* b;
+    f4 world(const float* buf, int x, int y) const {   /* ReadWorldPos */
+        if (x >= 0 && y >= 0 && x < w && y < h) return ld4(buf + 4 * ((size_t)x + (size_t)y * w));
+        return mk4(1e20f, 1e20f, 1e20f, bitsf(0));
+    }
+    float WorldDistance(int px, int py, const f4& cur) const {
+        const f4 p = world(b->prevWorldPos, px, py);
+        const f3 localNormal = UnpackNormal2(fbits(cur.w)), prevNormal = UnpackNormal2(fbits(p.w));
+        if ((fbits(p.w) & 3) != 1) return 1e21f;            /* only specular pixels are searched */
+        if (dot(localNormal, prevNormal) < 0.85f) return 1e21f;
+        return length(mk3(cur - p));
+    }
+    float FineWorldDistance(const f2 pixel, const f4& cur) const {
+        const int x0 = f2i(pixel.x), y0 = f2i(pixel.y);
+        const float fx = pixel.x - floorf(pixel.x), fy = pixel.y - floorf(pixel.y);
+        const float w0 = (1 - fx) * (1 - fy), w1 = fx * (1 - fy), w2 = (1 - fx) * fy, w3 = fx * fy;
+        const float d0 = WorldDistance(x0, y0, cur), d1 = WorldDistance(x0 + 1, y0, cur);
+        const float d2 = WorldDistance(x0, y0 + 1, cur), d3 = WorldDistance(x0 + 1, y0 + 1, cur);
+        float totalWeight = 0, totalDist = 0;
+        if (d0 < 1e20f) totalDist += d0 * w0, totalWeight += w0;
+        if (d1 < 1e20f) totalDist += d1 * w1, totalWeight += w1;
+        if (d2 < 1e20f) totalDist += d2 * w2, totalWeight += w2;
+        if (d3 < 1e20f) totalDist += d3 * w3, totalWeight += w3;
+        return totalWeight == 0 ? 1e20f : totalDist / totalWeight;
+    }
+    int RefineHistoryPos(f2& pos, const f2 offset, const f4& cur, float& bestDist, const float step) const {
+        int bestTap = 0;
+        const f2 c0 = mk2(pos.x - step, pos.y), c1 = mk2(pos.x + step, pos.y), c2 = mk2(pos.x, pos.y - step), c3 = mk2(pos.x, pos.y + step);
+        float d;
+        d = FineWorldDistance(c0 + offset, cur); if (d < bestDist) bestDist = d, pos = c0, bestTap = 1;
+        d = FineWorldDistance(c1 + offset, cur); if (d < bestDist) bestDist = d, pos = c1, bestTap = 2;
+        d = FineWorldDistance(c2 + offset, cur); if (d < bestDist) bestDist = d, pos = c2, bestTap = 3;
+        d = FineWorldDistance(c3 + offset, cur); if (d < bestDist) bestDist = d, pos = c3, bestTap = 4;
+        return bestTap;
+    }
+    /* ReadTexelConsistent (sampling_shared.h:136-175): bilinear history read whose taps must agree in normal
+     * (dot >= 0.95) and specularity with the pixel; out.x = -1 when no tap qualifies */
+    f4 ReadConsistent(const float* buf, const f4& localPos, const f3& localNormal, float u, float v) const {
+        const int iu1 = f2i(floorf(u)), iv1 = f2i(floorf(v)), iu0 = imax(0, iu1 - 1), iv0 = imax(0, iv1 - 1);
+        if (iu1 >= w || iv1 >= h || iu1 < 0 || iv1 < 0) return mk4(-1, -1, -1, -1);
+        const float fu = u - floorf(u), fv = v - floorf(v);
+        const size_t a0 = (size_t)iu0 + (size_t)iv0 * w, a1 = (size_t)iu1 + (size_t)iv0 * w;
+        const size_t a2 = (size_t)iu0 + (size_t)iv1 * w, a3 = (size_t)iu1 + (size_t)iv1 * w;
+        const f4 p0 = ld4(buf + 4 * a0), p1 = ld4(buf + 4 * a1), p2 = ld4(buf + 4 * a2), p3 = ld4(buf + 4 * a3);
+        const uint n0 = fbits(b->prevWorldPos[4 * a0 + 3]), n1 = fbits(b->prevWorldPos[4 * a1 + 3]);
+        const uint n2 = fbits(b->prevWorldPos[4 * a2 + 3]), n3 = fbits(b->prevWorldPos[4 * a3 + 3]);
+        const uint spec = fbits(localPos.w) & 3;
+        float w0 = (1 - fu) * (1 - fv), w1 = fu * (1 - fv), w2 = (1 - fu) * fv, w3 = 1 - (w0 + w1 + w2);
+        if (dot(UnpackNormal2(n0), localNormal) < 0.95f || (n0 & 3) != spec) w0 = 0;
+        if (dot(UnpackNormal2(n1), localNormal) < 0.95f || (n1 & 3) != spec) w1 = 0;
+        if (dot(UnpackNormal2(n2), localNormal) < 0.95f || (n2 & 3) != spec) w2 = 0;
+        if (dot(UnpackNormal2(n3), localNormal) < 0.95f || (n3 & 3) != spec) w3 = 0;
+        const float sum = w0 + w1 + w2 + w3;
+        if (sum == 0) return mk4(-1, -1, -1, -1);
+        return (w0 * p0 + w1 * p1 + w2 * p2 + w3 * p3) * (1.0f / sum);
+    }
+    /* ReadTexelConsistent2 (sampling_shared.h:177-220): the same for packed direct + indirect light, dot >= 0.975 */
+    bool ReadConsistent2(const float* buf, const f4& localPos, const f3& localNormal, float u, float v, f3& direct, f3& indirect) const {
+        const int iu1 = f2i(floorf(u)), iv1 = f2i(floorf(v)), iu0 = imax(0, iu1 - 1), iv0 = imax(0, iv1 - 1);
+        if (iu1 >= w || iv1 >= h || iu1 < 0 || iv1 < 0) return false;
+        const float fu = u - floorf(u), fv = v - floorf(v);
+        const size_t a[4] = {(size_t)iu0 + (size_t)iv0 * w, (size_t)iu1 + (size_t)iv0 * w, (size_t)iu0 + (size_t)iv1 * w,
+                             (size_t)iu1 + (size_t)iv1 * w};
+        const uint spec = fbits(localPos.w) & 3;
+        float wt[4];
+        wt[0] = (1 - fu) * (1 - fv), wt[1] = fu * (1 - fv), wt[2] = (1 - fu) * fv, wt[3] = 1 - (wt[0] + wt[1] + wt[2]);
+        for (int k = 0; k < 4; k++) {
+            const uint n = fbits(b->prevWorldPos[4 * a[k] + 3]);
+            if (dot(UnpackNormal2(n), localNormal) < 0.975f || (n & 3) != spec) wt[k] = 0;
+        }
+        const float sum = wt[0] + wt[1] + wt[2] + wt[3];
+        if (sum == 0) return false;
+        f3 d = wt[0] * GetDirect(buf + 4 * a[0]), in = wt[0] * GetIndirect(buf + 4 * a[0]);
+        for (int k = 1; k < 4; k++) d = d + wt[k] * GetDirect(buf + 4 * a[k]), in = in + wt[k] * GetIndirect(buf + 4 * a[k]);
+        direct = d * (1.0f / sum), indirect = in * (1.0f / sum);
+        return true;
+    }
+
+    /* prepareFilterKernel (finalize_shared.h:217-291) */
+    void prepare(int x, int y, const float* accum, const SvgfView& V, const lh2g_filter_params& fp, float scale) const {
+        const size_t px = (size_t)x + (size_t)y * w, WH = (size_t)w * h;
+        uint* feature = b->features + 4 * px;
+        const f3 direct = mk3(ld4(accum + 4 * px)) * scale;
+        const f4 localWorldPos = ld4(b->worldPos + 4 * px);
+        const f3 albedo = RGB32toHDRmin1(feature[0]);
+        const f3 indirect = mk3(ld4(accum + 4 * (px + WH))) * scale;
+        const f3 reciAlbedo = mk3(1.0f / albedo.x, 1.0f / albedo.y, 1.0f / albedo.z);
+        const f3 directLight = fmin3(direct * reciAlbedo, fp.clampDirect);
+        const f3 indirectLight = fmin3(indirect * reciAlbedo, fp.clampIndirect);
+        CombineToFloat4(directLight, indirectLight, b->shading + 4 * px);
+        float lumDirect = Luminance(directLight), lumDirect2 = lumDirect * lumDirect;
+        float lumIndirect = Luminance(indirectLight), lumIndirect2 = lumIndirect * lumIndirect;
+        f2 prevPixelPos;
+        if (((feature[3] >> 4) & 3) == 0) {
+            /* diffuse: project the world position into the previous camera */
+            const f3 dd = normalize(mk3(localWorldPos - V.prevPos));
+            const f4 D = mk4(dd.x, dd.y, dd.z, 0);
+            const f3 ss = mk3(V.prevPos) + mk3(D) * (V.prevPos.w / dot4(V.prevE, D));
+            const f4 S = mk4(ss.x, ss.y, ss.z, 0);
+            prevPixelPos = mk2(dot4(S, V.prevRight) - V.prevRight.w - fp.j0, dot4(S, V.prevUp) - V.prevUp.w - fp.j1);
+        } else {
+            prevPixelPos = mk2((float)x, (float)y);
+            if (!fp.camIsStationary) {
+                /* specular: diamond search for the position in the previous frame's world positions */
+                float bestDist = length(mk3(localWorldPos - ld4(b->prevWorldPos + 4 * px))), stepSize = 5.0f;
+                const f2 offset = mk2(fp.j0 - fp.prevj0, fp.j1 - fp.prevj1);
+                int iter = 0;
+                for (;;) {
+                    const int tap = RefineHistoryPos(prevPixelPos, offset, localWorldPos, bestDist, stepSize);
+                    if (tap == 0) { stepSize *= 0.45f; if (stepSize < 0.05f) break; }
+                    if (++iter == 25) break;
+                }
+            }
+        }
+        prevPixelPos = prevPixelPos + mk2(0.5f, 0.5f);
+        const float ppx = prevPixelPos.x, ppy = prevPixelPos.y;
+        bool hit = false;
+        if (ppx >= 0 && ppx < (float)w && ppy >= 0 && ppy < (float)h) {
+            const f3 localNormal = UnpackNormal2(feature[1]);
+            const f4 history = ReadConsistent(b->prevMoments, localWorldPos, localNormal, ppx, ppy);
+            if (history.x > -1) {
+                lumDirect = 0.2f * lumDirect + 0.8f * history.x;
+                lumDirect2 = 0.2f * lumDirect2 + 0.8f * history.y;
+                lumIndirect = 0.2f * lumIndirect + 0.8f * history.z;
+                lumIndirect2 = 0.2f * lumIndirect2 + 0.8f * history.w;
+                if ((feature[3] & 15) < 15) feature[3]++;
+                hit = true;
+            }
+        }
+        if (!hit) feature[3] &= 0xfffffff0u;   /* reset the history count */
+        b->motion[2 * px] = prevPixelPos.x, b->motion[2 * px + 1] = prevPixelPos.y;
+        store4(b->moments + 4 * px, lumDirect, lumDirect2, lumIndirect, lumIndirect2);
+    }
+
+    /* applyFilterKernel (finalize_shared.h:320-476): 5x5 a-trous (corners cut) at step 2^(phase-1) with normal,
+     * depth, material and luminance stops; phase 1 blends with the clamped history, the last pass remodulates */
+    void apply(int x, int y, const float* A, const float* B, float* C, int phase, bool lastPass) const {
+        const size_t px = (size_t)x + (size_t)y * w;
+        const uint* lf = b->features + 4 * px;
+        const f4 localPos = ld4(b->worldPos + 4 * px);
+        const f3 localNormal = UnpackNormal2(lf[1]);
+        const f3 localColor = RGB32toHDR(lf[0]);
+        const uint localMatID = lf[3] >> 4;
+        float directWeightSum = 1, indirectWeightSum = 1;
+        f3 directSum = directWeightSum * GetDirect(A + 4 * px);
+        f3 indirectSum = indirectWeightSum * GetIndirect(A + 4 * px);
+        const float localDirect = Luminance(GetDirect(A + 4 * px));
+        const float localIndirect = Luminance(GetIndirect(A + 4 * px));
+        const float localDepth = bitsf(lf[2]);
+        const float localDdx = b->deltaDepth[4 * px + 2], localDdy = b->deltaDepth[4 * px + 3];
+        const float sigma = 10.0f * oneoverpow2(phase - 1);
+        const float factor = (lf[3] & 15) == 0 ? 400.0f : 1.0f;
+        const f4 m = ld4(b->moments + 4 * px);
+        const float var_dir = m.y - m.x * m.x, var_ind = m.w - m.z * m.z;
+        const float rdir = -1.0f / (sigma * factor * sqrtf(var_dir + 0.00001f) + 0.00001f);
+        const float rind = -1.0f / (sigma * factor * sqrtf(var_ind + 0.00001f) + 0.00001f);
+        const int step = 1 << (phase - 1);
+        for (int vv = -2; vv <= 2; vv++) {
+            const int v = vv * step + y;
+            const int r = (vv == 2 || vv == -2) ? 1 : 2;
+            if (v < 0 || v >= h) continue;
+            for (int uu = -r; uu <= r; uu++) {
+                if (uu == 0 && vv == 0) continue;
+                const int u = std::min(std::max(uu * step + x, 0), w - 1);
+                const size_t q = (size_t)u + (size_t)v * w;
+                const uint* nf = b->features + 4 * q;
+                const float w_dist = (float)(uu * uu + vv * vv) * (-1.0f / 7.5f);
+                const f3 nDirect = GetDirect(A + 4 * q), nIndirect = GetIndirect(A + 4 * q);
+                float w_normal = pow128(fmaxr(0.0f, dot(UnpackNormal2(nf[1]), localNormal)));
+                const float expected = localDepth + localDdx * (float)(uu * step) + localDdy * (float)(vv * step);
+                const float depthError = fabsf(expected - bitsf(nf[2]));
+                const float expectedDifference = fabsf(expected - localDepth);
+                const float w_depth = depthError / fmaxr(0.00001f, (0.5f + (float)phase * 0.5f) * expectedDifference);
+                /* the reference's ternary mixes the double literal 0.0001 with a float: the product is formed in double */
+                if ((nf[3] >> 4) != localMatID) w_normal = (float)((double)w_normal * 0.0001);
+                else w_normal = w_normal * dot(localColor, RGB32toHDR(nf[0]));
+                float w_dir = w_normal * lm_expf(fabsf(localDirect - Luminance(nDirect)) * rdir + w_dist - w_depth);
+                float w_ind = w_normal * lm_expf(fabsf(localIndirect - Luminance(nIndirect)) * rind + w_dist - w_depth);
+                if (!std::isfinite(w_dir)) w_dir = 0;
+                if (!std::isfinite(w_ind)) w_ind = 0;
+                directSum = directSum + nDirect * w_dir, directWeightSum += w_dir;
+                indirectSum = indirectSum + nIndirect * w_ind, indirectWeightSum += w_ind;
+            }
+        }
+        f3 directFiltered = directSum * (1.0f / fmaxr(0.0001f, directWeightSum));
+        f3 indirectFiltered = indirectSum * (1.0f / fmaxr(0.0001f, indirectWeightSum));
+        if (phase == 1) {
+            const float mx = b->motion[2 * px], my = b->motion[2 * px + 1];
+            const int ix = f2i(mx), iy = f2i(my);
+            f3 prevDirect, prevIndirect;
+            if (ix >= 0 && ix < w && iy >= 0 && iy < h && ReadConsistent2(B, localPos, localNormal, mx, my, prevDirect, prevIndirect)) {
+                /* neighbourhood clamp in YCoCg, +-0.75 sigma over the 3x3 block of the unfiltered input */
+                prevDirect = RGBToYCoCg(prevDirect), prevIndirect = RGBToYCoCg(prevIndirect);
+                f3 dirAvg = RGBToYCoCg(directFiltered), dirVar = dirAvg * dirAvg;
+                f3 indAvg = RGBToYCoCg(indirectFiltered), indVar = indAvg * indAvg;
+                auto add = [&](size_t q) {
+                    const f3 f = RGBToYCoCg(GetDirect(A + 4 * q)), g = RGBToYCoCg(GetIndirect(A + 4 * q));
+                    dirAvg = dirAvg + f, dirVar = dirVar + f * f, indAvg = indAvg + g, indVar = indVar + g * g;
+                };
+                if (x > 1) {
+                    if (y > 1) add(px - w - 1);
+                    add(px - 1);
+                    if (y < h - 1) add(px + w - 1);
+                }
+                if (y > 1) add(px - w);
+                if (y < h - 1) add(px + w);
+                if (x < w - 1) {
+                    if (y > 1) add(px + 1 - w);
+                    add(px + 1);
+                    if (y < h - 1) add(px + 1 + w);
+                }
+                dirAvg = dirAvg * (1.0f / 9.0f), dirVar = dirVar * (1.0f / 9.0f), indAvg = indAvg * (1.0f / 9.0f), indVar = indVar * (1.0f / 9.0f);
+                f3 sd = fmax3(0.0f, dirVar - dirAvg * dirAvg), si = fmax3(0.0f, indVar - indAvg * indAvg);
+                sd = mk3(sqrtf(sd.x), sqrtf(sd.y), sqrtf(sd.z)), si = mk3(sqrtf(si.x), sqrtf(si.y), sqrtf(si.z));
+                prevDirect = clamp3(prevDirect, dirAvg - 0.75f * sd, dirAvg + 0.75f * sd);
+                prevIndirect = clamp3(prevIndirect, indAvg - 0.75f * si, indAvg + 0.75f * si);
+                directFiltered = directFiltered * 0.1f + YCoCgToRGB(prevDirect) * 0.9f;
+                indirectFiltered = indirectFiltered * 0.1f + YCoCgToRGB(prevIndirect) * 0.9f;
+            }
+        }
+        if (lastPass) {
+            const f3 c = (directFiltered + indirectFiltered) * RGB32toHDR(lf[0]);
+            store4(C + 4 * px, sqrtf(c.x), sqrtf(c.y), sqrtf(c.z), 1);
+        } else {
+            CombineToFloat4(directFiltered, indirectFiltered, C + 4 * px);
+        }
+    }
+
+    /* TAApassKernel (finalize_shared.h:498-539); reads 'pixels', writes 'out' */
+    void taa(int x, int y, const float* pixels, const float* prev, float* out) const {
+        const size_t px = (size_t)x + (size_t)y * w;
+        f3 pixel = mk3(ld4(pixels + 4 * px));
+        const float ppx = b->motion[2 * px] - 0.5f, ppy = b->motion[2 * px + 1] - 0.5f;
+        if (ppx >= 0 && ppx < (float)w && ppy >= 0 && ppy < (float)h) {
+            const f3 newPixel = RGBToYCoCg(pixel);
+            /* ReadTexelBmitchellNetravali (sampling_shared.h:117-134) */
+            const int x1 = f2i(ppx - 2.0f), y1 = f2i(ppy - 2.0f);
+            float totalWeight = 0;
+            f4 total = mk4(0, 0, 0, 0);
+            for (int yy = y1; yy < y1 + 4; yy++)
+                for (int xx = x1; xx < x1 + 4; xx++)
+                    if (xx >= 0 && yy > 0 && xx < w && yy < h) {
+                        const float weight = MitchellNetravali((float)xx - ppx) * MitchellNetravali((float)yy - ppy);
+                        total = total + ld4(prev + 4 * ((size_t)xx + (size_t)yy * w)) * weight;
+                        totalWeight += weight;
+                    }
+            f3 history = RGBToYCoCg(mk3(total * (1.0f / totalWeight)));
+            f3 colorAvg = newPixel, colorVar = newPixel * newPixel;
+            auto add = [&](size_t q) { const f3 f = RGBToYCoCg(mk3(ld4(pixels + 4 * q))); colorAvg = colorAvg + f, colorVar = colorVar + f * f; };
+            if (x > 1) {
+                if (y > 1) add(px - w - 1);
+                add(px - 1);
+                if (y < h - 1) add(px + w - 1);
+            }
+            if (y > 1) add(px - w);
+            if (y < h - 1) add(px + w);
+            if (x < w - 1) {
+                if (y > 1) add(px + 1 - w);
+                add(px + 1);
+                if (y < h - 1) add(px + 1 + w);
+            }
+            colorAvg = colorAvg * (1.0f / 9.0f), colorVar = colorVar * (1.0f / 9.0f);
+            f3 sigma = fmax3(0.0f, colorVar - colorAvg * colorAvg);
+            sigma = mk3(sqrtf(sigma.x), sqrtf(sigma.y), sqrtf(sigma.z));
+            history = clamp3(history, colorAvg - 1.25f * sigma, colorAvg + 1.25f * sigma);
+            pixel = YCoCgToRGB(newPixel * 0.1f + history * 0.9f);
+            if (std::isnan(pixel.x + pixel.y + pixel.z)) pixel = YCoCgToRGB(newPixel);
+        }
+        const f3 c = fmin3(10.0f, pixel);
+        store4(out + 4 * px, c.x, c.y, c.z, 0);
+    }
+    /* unsharpenTAAKernel (finalize_shared.h:553-576): sharpen, then square (the gamma is applied again later) */
+    void unsharpen(int x, int y, const float* pixels, float* target) const {
+        if (x == 0 || y == 0 || x >= w - 1 || y >= h - 1) return;
+        auto P = [&](int xx, int yy) { return ld4(pixels + 4 * ((size_t)xx + (size_t)yy * w)); };
+        const f4 p0 = P(x - 1, y - 1), p1 = P(x, y - 1), p2 = P(x + 1, y - 1), p3 = P(x + 1, y);
+        const f4 p4 = P(x + 1, y + 1), p5 = P(x, y + 1), p6 = P(x - 1, y + 1), p7 = P(x - 1, y);
+        const f4 c = P(x, y);
+        const f4 blur = 0.35f * p0 + 0.5f * p1 + 0.35f * p2 + 0.5f * p3 + 0.35f * p4 + 0.5f * p5 + 0.35f * p6 + 0.5f * p7;
+        const f4 sharp = c * 2.7f - 0.5f * blur;
+        const f4 pixel = mk4(fmaxr(c.x, sharp.x), fmaxr(c.y, sharp.y), fmaxr(c.z, sharp.z), fmaxr(c.w, sharp.w));
+        store4(target + 4 * ((size_t)x + (size_t)y * w), pixel.x * pixel.x, pixel.y * pixel.y, pixel.z * pixel.z, 0);
+    }
+    /* finalizeNoTAAKernel (finalize_shared.h:587-595) */
+    void finalize_no_taa(int x, int y, const float* pixels, float* target) const {
+        if (x == 0 || y == 0 || x >= w - 1 || y >= h - 1) return;
+        const f4 p = ld4(pixels + 4 * ((size_t)x + (size_t)y * w));
+        store4(target + 4 * ((size_t)x + (size_t)y * w), sqrtf(p.x), sqrtf(p.y), sqrtf(p.z), 0);
+    }
+};
 
 }  // namespace
 
@@ -1233,13 +1708,16 @@ int lh2o_trace_raw(lh2o_scene* s, const lh2g_ray* rays, long long n, float* t, i
     return 0;
 }
 
-int lh2o_render(lh2o_scene* s, const lh2g_view* view, const lh2g_render_params* p, float* pixelAccum, double* pixelAccum64,
-                uint32_t* counters, lh2g_capture* capture, int nthreads) {
+int lh2o_render_ex(lh2o_scene* s, const lh2g_view* view, const lh2g_render_params* p, float* pixelAccum, double* pixelAccum64,
+                   uint32_t* counters, lh2g_capture* capture, const lh2o_features* feat, int nthreads) {
     if (!s || !s->finalized || !view || !p || p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->maxDepth <= 0 || p->maxDepth > 64) return 1;
+    const bool filt = (p->flags & LH2G_RP_FILTER) != 0;
     Frame F;
     F.s = s, F.view = *view, F.p = *p;
     F.right = ld3(view->p2) - ld3(view->p1);
     F.up = ld3(view->p3) - ld3(view->p1);
+    memset(&F.feat, 0, sizeof(F.feat));
+    if (filt && feat) F.feat = *feat;
     const long long WH = (long long)p->width * p->height;
     F.P = WH * p->spp;
     const int D = p->maxDepth;
@@ -1255,25 +1733,80 @@ int lh2o_render(lh2o_scene* s, const lh2g_view* view, const lh2g_render_params* 
         std::lock_guard<std::mutex> g(mtx);
         for (int d = 0; d < D; d++) extTot[d] += ext[d], shadTot[d] += shad[d];
     });
-    /* per-pixel sums in sample order (deterministic) */
-    for (long long px = 0; px < WH; px++) {
-        for (int k = 0; k < 4; k++) {
-            float acc = pixelAccum ? pixelAccum[px * 4 + k] : 0.0f;
-            double acc64 = pixelAccum64 ? pixelAccum64[px * 4 + k] : 0.0;
-            for (int smp = 0; smp < p->spp; smp++) {
-                const float v = paths[smp * WH + px].rgbw[k];
-                acc += v;
-                acc64 += (double)v;
+    /* per-pixel sums in sample order (deterministic); LH2G_RP_FILTER frames have a second, indirect half */
+    for (int half = 0; half < (filt ? 2 : 1); half++)
+        for (long long px = 0; px < WH; px++) {
+            const long long o = (half * WH + px) * 4;
+            for (int k = 0; k < 4; k++) {
+                float acc = pixelAccum ? pixelAccum[o + k] : 0.0f;
+                double acc64 = pixelAccum64 ? pixelAccum64[o + k] : 0.0;
+                for (int smp = 0; smp < p->spp; smp++) {
+                    const float v = paths[smp * WH + px].rgbw[half][k];
+                    acc += v;
+                    acc64 += (double)v;
+                }
+                if (pixelAccum) pixelAccum[o + k] = acc;
+                if (pixelAccum64) pixelAccum64[o + k] = acc64;
             }
-            if (pixelAccum) pixelAccum[px * 4 + k] = acc;
-            if (pixelAccum64) pixelAccum64[px * 4 + k] = acc64;
         }
-    }
     if (counters) for (int d = 0; d < D; d++) counters[2 * d] = extTot[d], counters[2 * d + 1] = shadTot[d];
     return 0;
 }
 
+int lh2o_render(lh2o_scene* s, const lh2g_view* view, const lh2g_render_params* p, float* pixelAccum, double* pixelAccum64,
+                uint32_t* counters, lh2g_capture* capture, int nthreads) {
+    return lh2o_render_ex(s, view, p, pixelAccum, pixelAccum64, counters, capture, nullptr, nthreads);
+}
+
+int lh2o_svgf_frame(lh2o_svgf* f, const float* accum, const lh2g_filter_params* fp, int nthreads) {
+    if (!f || !accum || !fp || f->width <= 0 || f->height <= 0 || fp->samplesTaken <= 0) return 1;
+    Svgf S;
+    S.w = f->width, S.h = f->height, S.b = f;
+    const SvgfView V = svgf_view(fp->prevView, f->height);
+    const float scale = 1.0f / (float)fp->samplesTaken;
+    auto rows = [&](const std::function<void(int, int)>& fn) {
+        parallel_for(S.h, nthreads, 4, [&](long long b, long long e) {
+            for (long long y = b; y < e; y++)
+                for (int x = 0; x < S.w; x++) fn(x, (int)y);
+        });
+    };
+    rows([&](int x, int y) { S.prepare(x, y, accum, V, *fp, scale); });
+    rows([&](int x, int y) { S.apply(x, y, f->shading, f->filteredIN, f->filteredOUT, 1, false); });
+    rows([&](int x, int y) { S.apply(x, y, f->filteredOUT, nullptr, f->filteredIN, 2, false); });
+    rows([&](int x, int y) { S.apply(x, y, f->filteredIN, nullptr, f->shading, 3, true); });
+    if (fp->taa) {
+        rows([&](int x, int y) { S.taa(x, y, f->shading, f->prevPixels, f->taaPixels); });
+        rows([&](int x, int y) { S.unsharpen(x, y, f->taaPixels, f->target); });
+        std::swap(f->taaPixels, f->prevPixels);
+    } else {
+        rows([&](int x, int y) { S.finalize_no_taa(x, y, f->shading, f->target); });
+        std::swap(f->shading, f->prevPixels);
+    }
+    std::swap(f->filteredIN, f->filteredOUT);
+    std::swap(f->prevWorldPos, f->worldPos);
+    std::swap(f->moments, f->prevMoments);
+    return 0;
+}
+
 /* pure functions for the pinning tests */
+uint32_t lh2o_pack_normal2(const float* n) { return PackNormal2(ld3(n)); }
+void lh2o_unpack_normal2(uint32_t p, float* o) { const f3 n = UnpackNormal2(p); o[0] = n.x, o[1] = n.y, o[2] = n.z; }
+uint32_t lh2o_hdr_to_rgb32(const float* c) { return HDRtoRGB32(ld3(c)); }
+void lh2o_rgb32_to_hdr(uint32_t c, int min1, float* o) { const f3 v = min1 ? RGB32toHDRmin1(c) : RGB32toHDR(c); o[0] = v.x, o[1] = v.y, o[2] = v.z; }
+void lh2o_combine_to_float4(const float* a, const float* b, float* o) { CombineToFloat4(ld3(a), ld3(b), o); }
+void lh2o_split_float4(const float* x, float* d, float* i) {
+    const f3 a = GetDirect(x), b = GetIndirect(x);
+    d[0] = a.x, d[1] = a.y, d[2] = a.z, i[0] = b.x, i[1] = b.y, i[2] = b.z;
+}
+void lh2o_rgb_to_ycocg(const float* c, float* o) { const f3 v = RGBToYCoCg(ld3(c)); o[0] = v.x, o[1] = v.y, o[2] = v.z; }
+void lh2o_ycocg_to_rgb(const float* c, float* o) { const f3 v = YCoCgToRGB(ld3(c)); o[0] = v.x, o[1] = v.y, o[2] = v.z; }
+float lh2o_luminance(const float* c) { return Luminance(ld3(c)); }
+float lh2o_mitchell_netravali(float v) { return MitchellNetravali(v); }
+void lh2o_svgf_view(const lh2g_view* v, int h, float* out16) {
+    const SvgfView r = svgf_view(*v, h);
+    const f4 q[4] = {r.prevPos, r.prevE, r.prevRight, r.prevUp};
+    for (int k = 0; k < 4; k++) out16[4 * k] = q[k].x, out16[4 * k + 1] = q[k].y, out16[4 * k + 2] = q[k].z, out16[4 * k + 3] = q[k].w;
+}
 uint32_t lh2o_wanghash(uint32_t v) { return WangHash(v); }
 float lh2o_random_float(uint32_t* seed) { return RandomFloat(*seed); }
 void lh2o_random_barycentrics(float r0, float* o) { const f3 b = RandomBarycentrics(r0); o[0] = b.x, o[1] = b.y, o[2] = b.z; }

@@ -59,6 +59,40 @@ int lh2o_trace_raw(lh2o_scene* s, const lh2g_ray* rays, long long n, float* t, i
 int lh2o_render(lh2o_scene* s, const lh2g_view* view, const lh2g_render_params* p, float* pixelAccum,
                 double* pixelAccum64, uint32_t* counters, lh2g_capture* capture, int nthreads);
 
+/* SVGF feature buffers of a LH2G_RP_FILTER frame, W*H entries each, written for the paths of sample 0 of a
+ * frame with samplesTaken == 0 (RenderCore_Optix7Filter/kernels/pathtracer.h:95-232). features: uint4;
+ * worldPos, deltaDepth: float4. The caller keeps them between frames (features.w carries the history count). */
+typedef struct lh2o_features { uint32_t* features; float* worldPos; float* deltaDepth; } lh2o_features;
+
+/* lh2o_render with feature output. For LH2G_RP_FILTER frames pixelAccum (and pixelAccum64) hold 2*W*H float4:
+ * the direct half, then the indirect half. */
+int lh2o_render_ex(lh2o_scene* s, const lh2g_view* view, const lh2g_render_params* p, float* pixelAccum,
+                   double* pixelAccum64, uint32_t* counters, lh2g_capture* capture, const lh2o_features* feat, int nthreads);
+
+/* SVGF state of one render target: the buffers of RenderCore_Optix7Filter/rendercore.cpp:350-364 (W*H entries,
+ * float4 unless noted), owned by the caller. lh2o_svgf_frame swaps the history pointers inside the struct
+ * exactly as the GPU core swaps its buffers, so the same slot names can be compared after every frame. */
+typedef struct lh2o_svgf {
+    int width, height;
+    uint32_t* features;                  /* uint4, written by lh2o_render_ex */
+    float* worldPos;                     /* written by lh2o_render_ex */
+    float* prevWorldPos;
+    float* deltaDepth;                   /* written by lh2o_render_ex */
+    float* motion;                       /* float2 */
+    float* moments;
+    float* prevMoments;
+    float* shading;
+    float* filteredIN;
+    float* filteredOUT;
+    float* prevPixels;
+    float* taaPixels;                    /* TAA output (the reference updates 'shading' in place) */
+    float* target;                       /* the frame: border pixels are never written */
+} lh2o_svgf;
+
+/* prepareFilter, applyFilter x 3, TAA + unsharpen or finalizeNoTAA, history swaps
+ * (RenderCore_Optix7Filter/rendercore.cpp:904-935). accum: 2*W*H float4 of the frame. */
+int lh2o_svgf_frame(lh2o_svgf* f, const float* accum, const lh2g_filter_params* fp, int nthreads);
+
 /* Small pure functions exported for the pinning tests against the reference's own headers. */
 uint32_t lh2o_wanghash(uint32_t s);
 float lh2o_random_float(uint32_t* seed);
@@ -78,6 +112,18 @@ float lh2o_half2float(uint16_t h);
 void lh2o_pack_material(const lh2g_material* m, const uint32_t* texFirstPixel, const uint32_t* texWH,
                         lh2g_gpu_material* out);
 void lh2o_invert4x4(const float* m16, float* out16);
+uint32_t lh2o_pack_normal2(const float* n3);
+void lh2o_unpack_normal2(uint32_t p, float* out3);
+uint32_t lh2o_hdr_to_rgb32(const float* c3);
+void lh2o_rgb32_to_hdr(uint32_t c, int min1, float* out3);
+void lh2o_combine_to_float4(const float* a3, const float* b3, float* out4);
+void lh2o_split_float4(const float* x4, float* direct3, float* indirect3);
+void lh2o_rgb_to_ycocg(const float* rgb3, float* out3);
+void lh2o_ycocg_to_rgb(const float* ycocg3, float* out3);
+float lh2o_luminance(const float* rgb3);
+float lh2o_mitchell_netravali(float v);
+/* prepareFilter's camera constants (prevPos, prevE, prevRight, prevUp as 4 float4) for a target of height h */
+void lh2o_svgf_view(const lh2g_view* v, int h, float* out16);
 
 #ifdef __cplusplus
 }

@@ -51,6 +51,13 @@ inline float __expf(float x) { return lh2o_expf(x); }
 #define sincosf(a, s, c) lh2o_sincos(a, s, c)
 #define expf(x) lh2o_expf(x)
 #define log2f(x) lh2o_log2f(x)
+/* float -> unsigned conversion with the GPU's semantics (cvt.rzi.u32.f32: truncation, saturation at the range
+ * ends, NaN -> 0). The Makefile rewrites the float casts "(uint)(...)" of tools_shared.h to it. */
+inline uint REF_F2U(float x) {
+    if (!(x > 0.0f)) return 0u;
+    if (x >= 4294967296.0f) return 0xffffffffu;
+    return (uint)x;
+}
 /* single-threaded host execution: atomics are plain read-modify-writes */
 inline uint atomicAdd(uint* p, uint v) { const uint o = *p; *p = o + v; return o; }
 struct ref_dim3 { uint x, y, z; };
