@@ -35,6 +35,7 @@ sys.path.insert(0, ROOT)
 
 W_DEFAULT, H_DEFAULT = 1920, 1080
 MAX_DEPTH, RR_START = 8, 4
+WAVE_TAIL = 4          # path lengths >= 4 run in the persistent tail kernel (setting "waveTail")
 WORKLOAD = "spheres_2m: 64 x 32k-tri displaced spheres + ground (2,048,002 tris, 66 instances), 16 quad + 4 point lights, " \
            "20 materials (4 textured), sky; 1920x1080 1spp, max depth 8, RR after depth 3, NEE"
 METRIC = "Mrays/s @1080p 1spp"
@@ -187,6 +188,8 @@ def svgf_leg(core, W, H, steps, warmup):
     """Filter-core frames with SVGF + TAA over the 8-pose camera path (Restart every frame, as a moving camera
     does); the filter passes are timed by the core's own events (coreStats.filterTime)."""
     from lighthouse2_gb300 import scenes as S
+    core.Setting("maxDepth", MAX_DEPTH)
+    core.Setting("rrStartDepth", RR_START)
     core.Setting("filter", 1)
     core.Setting("TAA", 1)
     for k in range(warmup):
@@ -228,6 +231,8 @@ def run_gb300(args):
     core.set_scene(sc)
     build_ms = core.GetCoreStats()["bvhBuildTime"]
     core.SetTarget(W, H, 1)
+    core.Setting("waveTail", args.wave_tail)
+    waves = min(MAX_DEPTH, args.wave_tail - 1) if args.wave_tail > 0 else MAX_DEPTH
     stream = torch.cuda.ExternalStream(core.stream_ptr())
     frames = [frame_params(k, W, H) for k in range(8)]
     for k in range(args.warmup):
@@ -245,7 +250,8 @@ def run_gb300(args):
     with torch.cuda.stream(stream):
         e0.record()
     rays = 0
-    per_kind = {"extend": [0.0, 0, 0], "shade": [0.0, 0, 0], "connect": [0.0, 0, 0], "generate": [0.0, 0, 0], "finalize": [0.0, 0, 0]}
+    per_kind = {"extend": [0.0, 0, 0], "shade": [0.0, 0, 0], "connect": [0.0, 0, 0], "tail": [0.0, 0, 0], "generate": [0.0, 0, 0],
+                "finalize": [0.0, 0, 0]}
     launches = 0
     trav = np.zeros(4, np.float64)
     ext_rays = shadow_rays = 0
@@ -261,7 +267,7 @@ def run_gb300(args):
         launches += len(lt)
         per_kind["generate"][0] += lt[0]
         per_kind["finalize"][0] += lt[-1]
-        for d in range(MAX_DEPTH):
+        for d in range(waves):
             te, ts, tc = lt[1 + 3 * d], lt[2 + 3 * d], lt[3 + 3 * d]
             for kind, t, b in (("extend", te, algorithmic_bytes("extend", n_in[d], 0, 0)),
                                ("shade", ts, algorithmic_bytes("shade", n_in[d], int(c[d, 0]), int(c[d, 1]))),
@@ -269,6 +275,12 @@ def run_gb300(args):
                 per_kind[kind][0] += t
                 per_kind[kind][1] += b
                 per_kind[kind][2] += 1
+        if waves < MAX_DEPTH:   # the tail kernel: every remaining path vertex is traced, shaded and connected
+            b = sum(algorithmic_bytes("extend", n_in[d], 0, 0) + algorithmic_bytes("shade", n_in[d], int(c[d, 0]), int(c[d, 1])) +
+                    algorithmic_bytes("connect", int(c[d, 1]), 0, 0) for d in range(waves, MAX_DEPTH))
+            per_kind["tail"][0] += lt[1 + 3 * waves]
+            per_kind["tail"][1] += b
+            per_kind["tail"][2] += 1
     with torch.cuda.stream(stream):
         e1.record()
     torch.cuda.synchronize()
@@ -298,7 +310,7 @@ def run_gb300(args):
     if rank != 0:
         return 0
     frame_ms = sum(v[0] for v in per_kind.values())
-    dom = max(("extend", "shade", "connect"), key=lambda k: per_kind[k][0])
+    dom = max(("extend", "shade", "connect", "tail"), key=lambda k: per_kind[k][0])
     t_dom, b_dom, n_dom = per_kind[dom]
     peak, peak_kind = peaks()
     achieved = (b_dom / n_dom) / ((t_dom / n_dom) / 1e3) / 1e9 if t_dom > 0 else 0.0
@@ -313,6 +325,7 @@ def run_gb300(args):
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": 1, "max_depth": MAX_DEPTH, "rr_start_depth": RR_START,
+                       "wave_tail": args.wave_tail,
                        "l2": "inputs larger than L2 (scene ~0.6 GB + path state ~0.36 GB resident), no flush",
                        "bvh_build_ms": round(build_ms, 2), "scene_generation_s": round(gen_s, 1),
                        "rays_per_frame": rays / args.steps / world,
@@ -348,6 +361,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-svgf", action="store_true")
+    ap.add_argument("--wave-tail", type=int, default=WAVE_TAIL, help="first path length of the persistent tail kernel (0: off)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

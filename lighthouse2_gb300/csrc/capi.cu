@@ -16,6 +16,7 @@
  *                        reads). The first filtered frame after SetTarget reprojects onto its own view.
  * No stage of a frame waits for the host: queue sizes stay on the device.
  */
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -175,7 +176,10 @@ struct lh2g_context {
     bool launchTiming = false;
     std::vector<cudaEvent_t> lev;   /* 2 per launch */
     int lastLaunches = 0;
-    int blocksExtend = 0, blocksConnect = 0, blocksShade = 0;
+    int blocksExtend = 0, blocksConnect = 0, blocksShade = 0, blocksTail = 0;
+    /* path length from which the remaining paths run to their end in one persistent kernel (0: wave loop
+     * to the end); a scheduling choice only, results are the same */
+    int tailDepth = 4;
     /* SVGF (filter core) state: settings of lib/RenderCore_Optix7Filter/rendercore.h:32-35 (this core renders
      * the unfiltered PrimeRef estimator unless "filter" is set) */
     int filterEnabled = 0, taaEnabled = 1;
@@ -342,6 +346,7 @@ int lh2g_create(int device, lh2g_context** out) {
     ctx->blocksExtend = persistent_blocks_wave(0);
     ctx->blocksConnect = persistent_blocks_wave(1);
     ctx->blocksShade = persistent_blocks_wave(2);
+    ctx->blocksTail = persistent_blocks_wave(3);
     *out = ctx;
     return LH2G_OK;
 }
@@ -584,6 +589,10 @@ int lh2g_setting(lh2g_context* ctx, const char* name, float value) {
         ctx->maxDepth = (int)value;
     } else if (!strcmp(name, "rrStartDepth")) ctx->rrStart = (int)value;
     else if (!strcmp(name, "nee")) ctx->nee = value != 0.0f;
+    else if (!strcmp(name, "waveTail")) {
+        if (value < 0 || value > 65) return fail(ctx, LH2G_ERR_INVALID, "setting waveTail: 0 (off) or 1..65");
+        ctx->tailDepth = (int)value;
+    }
     /* the filter core's settings (lib/RenderCore_Optix7Filter/rendercore.cpp:674-677) */
     else if (!strcmp(name, "clampDirect")) ctx->clampDirect = value;
     else if (!strcmp(name, "clampIndirect")) ctx->clampIndirect = value;
@@ -677,7 +686,9 @@ int lh2g_render_ex(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_p
     const SceneGPU S = scene_of(ctx);
     if (!accumulate) CK(cudaMemsetAsync(B.accum, 0, sizeof(float4) * (size_t)F.W * F.H * (filt ? 2 : 1), ctx->st));
     CK(cudaMemsetAsync(B.counters, 0, sizeof(Counters), ctx->st));
-    const int launches = 2 + 3 * F.maxDepth;
+    const int waves = ctx->tailDepth > 0 ? std::min(F.maxDepth, ctx->tailDepth - 1) : F.maxDepth;
+    const bool tail = waves < F.maxDepth;
+    const int launches = 2 + 3 * waves + (tail ? 1 : 0);
     const bool timing = ctx->launchTiming;
     if (timing)
         while ((int)ctx->lev.size() < 2 * launches) {
@@ -689,11 +700,12 @@ int lh2g_render_ex(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_p
     auto mark = [&]() { if (timing) cudaEventRecord(ctx->lev[li++], ctx->st); };
     CK(cudaEventRecord(ctx->ev[0], ctx->st));
     mark(), launch_generate(F, B, ctx->st), mark();
-    for (int d = 1; d <= F.maxDepth; d++) {
+    for (int d = 1; d <= waves; d++) {
         mark(), launch_extend(S, F, B, d, ctx->blocksExtend, ctx->st), mark();
         mark(), launch_shade(S, F, B, d, ctx->blocksShade, ctx->st), mark();
         mark(), launch_connect(S, F, B, d, ctx->blocksConnect, ctx->st), mark();
     }
+    if (tail) mark(), launch_tail(S, F, B, waves + 1, ctx->blocksTail, ctx->st), mark();
     const int after = p->samplesTaken + F.spp;
     mark(), launch_finalize(F, B, 1.0f / (float)after, ctx->st), mark();
     ctx->lastLaunches = timing ? launches : 0;
@@ -982,13 +994,14 @@ int lh2g_trace_host(lh2g_context* ctx, const lh2g_ray* rays, void* out, long lon
 
 namespace lh2g {
 /* Scene and persistent-grid sizes of a finalized context (for the allocation-free render in noalloc.cu). */
-int context_scene(lh2g_context* ctx, SceneGPU* scene, int* device, int* blocks3) {
-    if (!ctx || !scene || !device || !blocks3) return LH2G_ERR_INVALID;
+int context_scene(lh2g_context* ctx, SceneGPU* scene, int* device, int* blocks4, int* tailDepth) {
+    if (!ctx || !scene || !device || !blocks4 || !tailDepth) return LH2G_ERR_INVALID;
     if (!ctx->finalized) return fail(ctx, LH2G_ERR_STATE, "render: scene not finalized (call lh2g_finalize_instances)");
     if (!ctx->mats) return fail(ctx, LH2G_ERR_STATE, "render: no materials");
     *scene = scene_of(ctx);
     *device = ctx->device;
-    blocks3[0] = ctx->blocksExtend, blocks3[1] = ctx->blocksConnect, blocks3[2] = ctx->blocksShade;
+    blocks4[0] = ctx->blocksExtend, blocks4[1] = ctx->blocksConnect, blocks4[2] = ctx->blocksShade, blocks4[3] = ctx->blocksTail;
+    *tailDepth = ctx->tailDepth;
     return LH2G_OK;
 }
 }  // namespace lh2g

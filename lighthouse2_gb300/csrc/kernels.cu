@@ -8,6 +8,7 @@
  *             connections are compacted into the next queues by warp ballot + popc with one atomic per warp
  *   connect   any hit of every connection; unoccluded ones add their contribution (connections.h:22-34)
  *   finalize  per-pixel sum of the frame's samples in sample order, scaled by 1 / samples (finalize_shared.h:29-45)
+ *   tail      from a chosen path length on, the few remaining paths run to their end in one persistent kernel
  * Queue sizes live in device counters; no stage waits for the host, so a frame is a fixed launch sequence.
  * Radiance is accumulated per path (each path is owned by exactly one thread per stage), so the result does
  * not depend on the order in which the queues were filled.
@@ -106,10 +107,11 @@ struct ShadeOut {
     float4 sO, sD, sE;
 };
 
-__device__ __forceinline__ void shade_path(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, const int depth, const uint32_t i, ShadeOut& out,
-                                           float* pot) {
-    const int q = (depth - 1) & 1;
-    const float4 o4 = B.O[q][i], d4 = B.D[q][i], t4 = B.T[q][i], hit = B.hits[i];
+/* Shading of one path vertex (lib/RenderCore_PrimeRef/kernels/pathtracer.h:45-168, with the filter core's
+ * feature gathering for LH2G_RP_FILTER): o4, d4, t4 = the path's ray state, hit = its closest hit. Radiance goes
+ * to the path's own accumulator; a connection and an extension ray are returned in out. */
+__device__ __forceinline__ void shade_core(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, const int depth, const float4 o4,
+                                           const float4 d4, const float4 t4, const float4 hit, ShadeOut& out, float* pot) {
     const uint32_t pathIdx = __float_as_uint(o4.w);
     uint32_t FLAGS = __float_as_uint(d4.w);
     const float3 O = xyz(o4), D = xyz(d4);
@@ -240,6 +242,18 @@ __device__ __forceinline__ void shade_path(const SceneGPU& S, const FrameGPU& F,
     out.eT = make_float4(throughput.x, throughput.y, throughput.z, 0.0f);
 }
 
+__device__ __forceinline__ void shade_path(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, const int depth, const uint32_t i, ShadeOut& out,
+                                           float* pot) {
+    const int q = (depth - 1) & 1;
+    shade_core(S, F, B, depth, B.O[q][i], B.D[q][i], B.T[q][i], B.hits[i], out, pot);
+}
+
+__device__ __forceinline__ float4 hit_record(const bool found, const HitRec& best) {
+    if (found) return make_float4(__uint_as_float(f2u(65535.0f * best.u) + (f2u(65535.0f * best.v) << 16)), __int_as_float(best.inst),
+                                  __int_as_float(best.prim), best.t);
+    return make_float4(__uint_as_float(0u), __int_as_float(0), __int_as_float(NOHIT), 1e34f);
+}
+
 __global__ void __launch_bounds__(WAVE_BLOCK) k_shade(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int depth) {
     Counters* C = B.counters;
     const uint32_t count = queue_count(F, C, depth);
@@ -269,6 +283,67 @@ __global__ void __launch_bounds__(WAVE_BLOCK) k_shade(const SceneGPU S, const Fr
             if (out.shadow) B.shO[slot] = out.sO, B.shD[slot] = out.sD, B.shE[slot] = out.sE;
         }
     }
+}
+
+/* -------------------------------------------------------------------------------------------------- */
+/* The tail of the wave loop: the paths still alive when path length `startDepth` begins are few, and tracing
+ * them wave by wave would cost one launch and the latency of the slowest ray per remaining path length. Here a
+ * persistent thread takes one path at a time from the queue and runs it to its end: closest hit, shading,
+ * the connection's any-hit query and its contribution, the next segment. Every per-path quantity (RNG states,
+ * hit records, radiance and its order of accumulation, queue counts per path length) is the one the wave loop
+ * produces. */
+__global__ void __launch_bounds__(WAVE_BLOCK) k_tail(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int startDepth) {
+    Counters* C = B.counters;
+    const uint32_t count = queue_count(F, C, startDepth);
+    const int q = (startDepth - 1) & 1;
+    __shared__ float potential[64 * WAVE_BLOCK];
+    float* pot = potential + threadIdx.x;
+    uint32_t status = 0;
+    unsigned long long cn = 0, ct = 0, an = 0, at = 0;
+    /* the first path of a thread is fixed by its index; later ones come from the shared counter */
+    const uint32_t firstRound = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i = firstRound < count ? firstRound + atomicAdd(&C->fetch[3 * 64], 1u) : count) {
+        float4 o4 = B.O[q][i], d4 = B.D[q][i], t4 = B.T[q][i];
+        for (int depth = startDepth; depth <= F.maxDepth; depth++) {
+            Traversal tr;
+            tr.begin(S, xyz(o4), xyz(d4), t4.w, 1e34f);
+            bool any = false;
+            if (S.tlasRoot != 0xffffffffu)
+                while (tr.step<false>(S, status, any)) {}
+            cn += tr.nodes, ct += tr.tris;
+            const float4 hit = hit_record(tr.found, tr.best);
+            if (B.capHits) {
+                lh2g_hit c;
+                c.bary = __float_as_uint(hit.x), c.inst = __float_as_int(hit.y), c.prim = __float_as_int(hit.z), c.t = hit.w;
+                B.capHits[(size_t)(depth - 1) * F.P + __float_as_uint(o4.w)] = c;
+            }
+            ShadeOut out;
+            out.ext = out.shadow = false;
+            shade_core(S, F, B, depth, o4, d4, t4, hit, out, pot);
+            if (out.shadow) {
+                atomicAdd(&C->shadow[depth - 1], 1u);
+                Traversal sh;
+                sh.begin(S, xyz(out.sO), xyz(out.sD), 0.0f, out.sD.w);
+                bool occluded = false;
+                if (S.tlasRoot != 0xffffffffu)
+                    while (sh.step<true>(S, status, occluded)) {}
+                an += sh.nodes, at += sh.tris;
+                if (!occluded) {
+                    float4* accP = B.pathAcc + (__float_as_uint(out.sE.w) ? F.P : 0) + __float_as_uint(out.sO.w);
+                    float4 acc = *accP;
+                    acc.x += out.sE.x, acc.y += out.sE.y, acc.z += out.sE.z;
+                    *accP = acc;
+                }
+            }
+            if (!out.ext) break;
+            atomicAdd(&C->extension[depth - 1], 1u);
+            o4 = out.eO, d4 = out.eD, t4 = out.eT;
+        }
+    }
+    if (status) atomicOr(&C->status, status);
+    if (cn | ct) atomicAdd(&C->travStats[0], cn), atomicAdd(&C->travStats[1], ct);
+    if (an | at) atomicAdd(&C->travStats[2], an), atomicAdd(&C->travStats[3], at);
 }
 
 /* -------------------------------------------------------------------------------------------------- */
@@ -396,7 +471,8 @@ int persistent_blocks_wave(int which) {
     int per = 0;
     if (which == 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_extend, 128, 0);
     else if (which == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_connect, 128, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_shade, WAVE_BLOCK, 0);
+    else if (which == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_shade, WAVE_BLOCK, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_tail, WAVE_BLOCK, 0);
     return sm_count() * (per > 0 ? per : 1);
 }
 
@@ -411,6 +487,9 @@ void launch_shade(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, in
 }
 void launch_connect(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int blocks, cudaStream_t st) {
     k_connect<<<blocks, 128, 0, st>>>(S, F, B, depth);
+}
+void launch_tail(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int startDepth, int blocks, cudaStream_t st) {
+    k_tail<<<blocks, WAVE_BLOCK, 0, st>>>(S, F, B, startDepth);
 }
 void launch_finalize(const FrameGPU& F, const WaveBuffers& B, float scale, cudaStream_t st) {
     const int64_t WH = (int64_t)F.W * F.H;

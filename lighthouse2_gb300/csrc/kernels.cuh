@@ -29,6 +29,8 @@ void launch_generate(const FrameGPU& F, const WaveBuffers& B, cudaStream_t st);
 void launch_extend(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int persistentBlocks, cudaStream_t st);
 void launch_shade(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int blocks, cudaStream_t st);
 void launch_connect(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int persistentBlocks, cudaStream_t st);
+/* path lengths startDepth..maxDepth of the frame's remaining paths, one persistent launch */
+void launch_tail(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int startDepth, int persistentBlocks, cudaStream_t st);
 void launch_finalize(const FrameGPU& F, const WaveBuffers& B, float scale, cudaStream_t st);
 void launch_trace(const SceneGPU& S, const lh2g_ray* rays, void* out, long long n, int mode, uint32_t* fetch, uint32_t* status,
                   int persistentBlocks, cudaStream_t st);
@@ -38,6 +40,6 @@ void launch_tri_prep(const float4* verts, uint32_t n, uint32_t seg, float4* triD
 void launch_gather_tris(const float4* triIn, const uint32_t* leafPrim, uint32_t n, float4* triOut, cudaStream_t st);
 
 int persistent_blocks_trace(int mode);
-int persistent_blocks_wave(int which);
+int persistent_blocks_wave(int which);   /* 0 extend, 1 connect, 2 shade, 3 tail */
 
 }  // namespace lh2g

@@ -13,6 +13,7 @@
  * start of every call and every other buffer is written before it is read. Calls whose work overlaps on the GPU
  * (two streams, two threads, two contexts on one device) race on the array.
  */
+#include <algorithm>
 #include <mutex>
 
 #include "kernels.cuh"
@@ -33,7 +34,7 @@ unsigned char* g_scratch_addr[MAX_DEVICES] = {nullptr};
 
 namespace lh2g {
 /* defined in capi.cu: the scene and launch configuration of a context */
-int context_scene(lh2g_context* ctx, SceneGPU* scene, int* device, int* blocks3);
+int context_scene(lh2g_context* ctx, SceneGPU* scene, int* device, int* blocks4, int* tailDepth);
 }
 
 extern "C" LH2G_API int lh2g_render_noalloc(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* p, float* accumDevice,
@@ -45,8 +46,8 @@ extern "C" LH2G_API int lh2g_render_noalloc(lh2g_context* ctx, const lh2g_view* 
     const long long P = (long long)p->width * p->height * p->spp;
     if (P > LH2G_NOALLOC_MAX_PATHS) return LH2G_ERR_OVERFLOW;   /* width * height * spp above the static capacity */
     SceneGPU S;
-    int device = 0, blocks[3] = {0, 0, 0};
-    const int r = context_scene(ctx, &S, &device, blocks);
+    int device = 0, blocks[4] = {0, 0, 0, 0}, tailDepth = 0;
+    const int r = context_scene(ctx, &S, &device, blocks, &tailDepth);
     if (r != LH2G_OK) return r;
     if (device < 0 || (size_t)device >= MAX_DEVICES) return LH2G_ERR_INVALID;
     int current = -1;
@@ -93,11 +94,13 @@ extern "C" LH2G_API int lh2g_render_noalloc(lh2g_context* ctx, const lh2g_view* 
         return LH2G_ERR_CUDA;
     }
     launch_generate(F, B, st);
-    for (int d = 1; d <= F.maxDepth; d++) {
+    const int waves = tailDepth > 0 ? std::min(F.maxDepth, tailDepth - 1) : F.maxDepth;
+    for (int d = 1; d <= waves; d++) {
         launch_extend(S, F, B, d, blocks[0], st);
         launch_shade(S, F, B, d, blocks[2], st);
         launch_connect(S, F, B, d, blocks[1], st);
     }
+    if (waves < F.maxDepth) launch_tail(S, F, B, waves + 1, blocks[3], st);
     launch_finalize(F, B, 1.0f / (float)(p->samplesTaken + F.spp), st);
     const cudaError_t e = cudaGetLastError();
     if (current != device) cudaSetDevice(current);

@@ -444,12 +444,18 @@ LH2G_DEV void trace_queue(const SceneGPU& S, uint32_t* fetch, const uint32_t cou
     uint32_t ray = 0;
     bool active = false, exhausted = false;
     if (S.tlasRoot == 0xffffffffu || !LH2G_REFILL) {
-        /* a warp takes 32 rays at a time and traces each to the end (also used when there is no geometry) */
-        for (;;) {
-            uint32_t base = 0;
-            if (lane == 0) base = atomicAdd(fetch, 32u);
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (base >= count) return;
+        /* a warp takes 32 rays at a time and traces each to the end (also used when there is no geometry). The
+         * first 32 rays of a warp are fixed by its index, later ones come from the shared counter: a short queue
+         * costs no atomics at all, a long one is still balanced dynamically. */
+        const uint32_t firstRound = gridDim.x * blockDim.x;
+        uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
+        for (bool first = true;; first = false) {
+            if (!first) {
+                if (firstRound >= count) break;
+                if (lane == 0) base = firstRound + atomicAdd(fetch, 32u);
+                base = __shfl_sync(0xffffffffu, base, 0);
+            }
+            if (base >= count) break;   /* warp-uniform */
             const uint32_t i = base + lane;
             if (i < count) {
                 float3 o, d;

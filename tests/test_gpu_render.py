@@ -103,3 +103,20 @@ def test_render_api_matches_explicit_parameters(cornell):
         p = make_params(W, H, 1, max_depth=3, samples_taken=k, camera_r0=camera_r0(k), flags=RP_NEE | RP_DEPTH_W)
         acc = o.render(view, p, accum=acc)["accum"]
     assert np.array_equal(core.read_accumulator(), acc)
+
+
+@pytest.mark.parametrize("tail", [0, 1, 2, 5])
+def test_wave_tail_split_changes_nothing(cornell, tail):
+    """Running path lengths >= waveTail in the persistent tail kernel instead of wave by wave gives the same
+    hits, RNG states, queue counts and radiance (bit for bit) as the oracle."""
+    sc, core, o = cornell
+    W, H = 48, 40
+    core.SetTarget(W, H, 2)
+    core.Setting("waveTail", tail)
+    try:
+        view = S.cornell_view(W, H)
+        p = make_params(W, H, 2, max_depth=7, rr_start=3, camera_r0=camera_r0(0), flags=RP_NEE | RP_DEPTH_W)
+        acc = _check_frame(core, o, view, p)
+        assert np.array_equal(acc, o.render(view, p)["accum"])
+    finally:
+        core.Setting("waveTail", 4)

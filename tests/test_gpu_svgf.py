@@ -74,7 +74,9 @@ def test_filter_frame_features_and_halves(scene, oracle_lib, W, H, spp, depth):
 
 @pytest.mark.parametrize("taa", [1, 0])
 def test_filtered_render_sequence(scene, oracle_lib, taa):
-    sc, core, o = scene
+    sc, _, o = scene
+    core = RenderCore()           # a fresh core: jitter cycle, previous jitter and camera seed start from their initial values
+    core.set_scene(sc)
     W, H = 56, 40
     core.SetTarget(W, H, 1)
     core.Setting("maxDepth", 5)
@@ -86,15 +88,19 @@ def test_filtered_render_sequence(scene, oracle_lib, taa):
     seed = 0x12345678
     prev_view, pj, samples = None, (0.0, 0.0), 0
     cycle = 0
-    plan = [(0, 1), (1, 1), (2, 1), (3, 1), (3, 0), (3, 0)]       # (camera frame, converge: 1 = Restart)
+    first_converging = True
+    # (camera frame, converge: 1 = Restart); the first Converge frame after a Restart starts over as well
+    plan = [(0, 1), (1, 1), (2, 1), (3, 1), (3, 0), (3, 0), (3, 0)]
     for k, (cam, restart) in enumerate(plan):
         view = S.cornell_view(W, H, frame=cam)
         core.Render(view, converge=restart)
         fp, jv, rp = core.last_filter_frame()
-        # the filter core's bookkeeping
-        samples = 1 if restart else samples + 1
-        if restart:
-            accum = None
+        # the filter core's bookkeeping (rendercore.cpp:744-750)
+        if restart or first_converging:
+            samples, first_converging, accum = 0, True, None
+        if not restart:
+            first_converging = False
+        samples += 1
         j = (HALTON[0][cycle], HALTON[1][cycle]) if taa else (0.0, 0.0)
         cycle = (cycle + 1) & 3
         seed = xorshift(seed)
@@ -122,7 +128,7 @@ def test_filtered_render_sequence(scene, oracle_lib, taa):
     img = core.read_framebuffer().reshape(H, W, 4)[1:-1, 1:-1, :3]
     assert np.isfinite(img).all() and img.mean() > 0.01
     assert (core.read_filter_buffer("features")[:, 3] & 15).max() >= 3     # history accumulated
-    core.Setting("filter", 0)
+    core.close()
 
 
 def test_filter_requires_a_filter_frame(core_lib):
