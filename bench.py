@@ -15,6 +15,8 @@ depth 3, next-event estimation; frames follow a seeded 8-pose camera path. Seede
   cpu_baseline  the CPU oracle (a restatement of the reference's path tracer) on all host cores.
   svgf      filter-core frames of the same scene and camera path with SVGF + TAA: device time of the six filter
             launches per frame against the measured HBM bandwidth.
+  serving   the serving loop on a seeded job list over 4 resident scenes against sequential plain-core renders of
+            the same jobs: saturated throughput, and p50 / p99 latency under Poisson arrivals.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 Under torchrun each rank renders its own frames on its own GPU (replicas, weak scaling); rank 0 prints.
@@ -211,6 +213,133 @@ def svgf_leg(core, W, H, steps, warmup):
             "peak_GBps": peak, "frac": achieved / peak, "peak_source": peak_kind}
 
 
+def serving_jobs(n, n_scenes, seed=11):
+    """Seeded job list: scene, resolution in {256^2, 512^2, 1024^2, 1920x1080}, spp in {1, 4, 16}, depth 4..8,
+    a camera pose per job."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    res = [(256, 256), (512, 512), (1024, 1024), (1920, 1080)]
+    jobs = []
+    for k in range(n):
+        W, H = res[int(rng.integers(0, 4))]
+        jobs.append({"scene": int(rng.integers(0, n_scenes)), "W": W, "H": H, "spp": int(rng.choice([1, 4, 16])),
+                     "depth": int(rng.integers(4, 9)), "frame": int(rng.integers(0, 64))})
+    return jobs
+
+
+def serving_leg(args):
+    """The serving loop against sequential plain-core renders of the same job list: saturated throughput (all jobs
+    submitted at once) and latency under Poisson arrivals at a fraction of the sequential capacity."""
+    import numpy as np
+    from lighthouse2_gb300 import scenes as S
+    from lighthouse2_gb300.core import RenderCore, make_params, camera_r0, RP_NEE, RP_DEPTH_W
+    from lighthouse2_gb300.server import RenderServer
+    t0 = time.time()
+    scene_defs = [("cornell 82k", lambda: S.cornell_sphere(subdiv=6)),
+                  ("spheres 16 (512k)", lambda: S.spheres_2m(seed=3, n_spheres=16)),
+                  ("spheres 64 (2M)", lambda: S.spheres_2m(seed=7)),
+                  ("spheres 128 (4M)", lambda: S.spheres_2m(seed=9, n_spheres=128))]
+    scenes, cores = [], []
+    for name, make in scene_defs:
+        sc = make()
+        core = RenderCore(0)
+        core.set_scene(sc)
+        scenes.append(sc)
+        cores.append(core)
+    setup_s = time.time() - t0
+    jobs = serving_jobs(args.serving_jobs, len(cores))
+
+    def inputs(j):
+        view = S.cornell_view(j["W"], j["H"], frame=j["frame"] % 4) if j["scene"] == 0 else S.spheres_view(j["W"], j["H"], frame=j["frame"])
+        p = make_params(j["W"], j["H"], j["spp"], max_depth=j["depth"], rr_start=min(4, j["depth"]), camera_r0=camera_r0(0),
+                        flags=RP_NEE | RP_DEPTH_W)
+        return view, p
+
+    # sequential plain-core renders: service time of every job alone (render + image read back)
+    for c in cores:
+        c.SetTarget(64, 64, 1)
+    for j in jobs[:4]:   # warm-up
+        view, p = inputs(j)
+        cores[j["scene"]].SetTarget(j["W"], j["H"], j["spp"])
+        cores[j["scene"]].render_ex(view, p, counters=False)
+        cores[j["scene"]].read_accumulator()
+    # (SetTarget, which reallocates when the resolution changes, stays outside the service time: a plain-core
+    # deployment would keep a target per resolution)
+    service, seq_rays = [], 0
+    for j in jobs:
+        view, p = inputs(j)
+        c = cores[j["scene"]]
+        c.SetTarget(j["W"], j["H"], j["spp"])
+        c.WaitForRender()
+        t = time.perf_counter()
+        out = c.render_ex(view, p, counters=True)
+        c.read_accumulator()
+        service.append(time.perf_counter() - t)
+        cnt = out["counters"]
+        seq_rays += j["W"] * j["H"] * j["spp"] + int(cnt[:, 0].sum()) + int(cnt[:, 1].sum())
+    t_seq = float(sum(service))
+    cap = max(j["W"] * j["H"] * j["spp"] for j in jobs) * 2
+    srv = RenderServer(path_capacity=cap)
+    sids = [srv.add_scene(c) for c in cores]
+    for j in jobs[:4]:   # warm-up
+        view, p = inputs(j)
+        srv.wait(srv.submit_render(sids[j["scene"]], view, p))
+    # saturated: every job at once
+    r0 = srv.stats()["raysTraced"]
+    t = time.perf_counter()
+    ids = []
+    for j in jobs:
+        view, p = inputs(j)
+        ids.append(srv.submit_render(sids[j["scene"]], view, p))
+    for i in ids:
+        srv.wait(i)
+    t_sat = time.perf_counter() - t
+    sat_rays = srv.stats()["raysTraced"] - r0
+    for i in ids:
+        srv.release(i)
+    # Poisson arrivals at a fraction of the sequential capacity
+    rate = args.serving_load * len(jobs) / t_seq
+    rng = np.random.default_rng(5)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, len(jobs)))
+    t_start = time.perf_counter()
+    ids = []
+    for k, j in enumerate(jobs):
+        delay = arrivals[k] - (time.perf_counter() - t_start)
+        if delay > 0:
+            time.sleep(delay)
+        view, p = inputs(j)
+        ids.append(srv.submit_render(sids[j["scene"]], view, p))
+    lat = []
+    for i in ids:
+        ts, ta, td = srv.wait(i)
+        lat.append(td - ts)
+        srv.release(i)
+    srv.close()
+    for c in cores:
+        c.close()
+    # the same arrivals served by the plain core one job at a time (first come, first served), from the measured
+    # service times
+    seq_lat, free_at = [], 0.0
+    for k in range(len(jobs)):
+        start = max(arrivals[k], free_at)
+        free_at = start + service[k]
+        seq_lat.append(free_at - arrivals[k])
+    lat, seq_lat, service = np.array(lat), np.array(seq_lat), np.array(service)
+    slow = lat / service
+    pct = lambda a, q: float(np.percentile(a, q) * 1e3)
+    return {"workload": f"{len(jobs)} seeded jobs over 4 resident scenes ({', '.join(n for n, _ in scene_defs)}); resolution in "
+                        "{256^2, 512^2, 1024^2, 1920x1080}, spp in {1, 4, 16}, depth 4..8; scenes built once (" + f"{setup_s:.0f} s)",
+            "path_capacity": cap,
+            "sequential": {"jobs_per_s": len(jobs) / t_seq, "Mrays_per_s": seq_rays / t_seq / 1e6, "seconds": t_seq},
+            "saturated": {"jobs_per_s": len(jobs) / t_sat, "Mrays_per_s": sat_rays / t_sat / 1e6, "seconds": t_sat,
+                          "throughput_vs_sequential": t_seq / t_sat},
+            "poisson": {"rate_jobs_per_s": rate, "load_vs_sequential_capacity": args.serving_load,
+                        "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
+                        "sequential_fifo_latency_ms": {"p50": pct(seq_lat, 50), "p99": pct(seq_lat, 99)},
+                        "standalone_latency_ms": {"p50": pct(service, 50), "p99": pct(service, 99)},
+                        "slowdown_vs_standalone": {"p50": float(np.percentile(slow, 50)), "p99": float(np.percentile(slow, 99))}}}
+
+
 def run_gb300(args):
     import numpy as np
     import torch
@@ -307,6 +436,7 @@ def run_gb300(args):
         e2e_rays += W * H + int(c[:, 0].sum()) + int(c[:, 1].sum())
     e2e_value = e2e_rays * world / t_e2e / 1e6
     svgf = svgf_leg(core, W, H, max(args.steps, 8), args.warmup) if not args.no_svgf else None
+    serving = serving_leg(args) if (not args.no_serving and rank == 0) else None
     if rank != 0:
         return 0
     frame_ms = sum(v[0] for v in per_kind.values())
@@ -343,6 +473,8 @@ def run_gb300(args):
             "clocks": clk}
     if svgf is not None:
         line["svgf"] = svgf
+    if serving is not None:
+        line["serving"] = serving
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(sc, W, H, args.cpu_seconds, os.cpu_count() or 1)
     print(json.dumps(line, default=float), flush=True)
@@ -361,6 +493,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-svgf", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serving-jobs", type=int, default=120)
+    ap.add_argument("--serving-load", type=float, default=0.8, help="Poisson arrival rate as a fraction of the sequential capacity")
     ap.add_argument("--wave-tail", type=int, default=WAVE_TAIL, help="first path length of the persistent tail kernel (0: off)")
     args = ap.parse_args()
     if args.warmup < 3:

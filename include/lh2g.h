@@ -139,6 +139,37 @@ LH2G_API int lh2g_trace_host(lh2g_context* ctx, const lh2g_ray* rays, void* out,
 LH2G_API int lh2g_render_noalloc(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* params, float* accumDevice,
                                  void* stream);
 
+/* ---- serving loop (no counterpart in the reference, whose cores render one frame at a time) ----
+ * Render and ray-query jobs of several resident scenes, continuously batched: jobs are admitted in arrival order
+ * while their paths fit in the server's path capacity (the admission unit, 48 B x 2 + 64 B of queue memory per
+ * path plus 16 B of per-path radiance), and the paths of every admitted job share one set of wavefront queues;
+ * one CUDA graph per tick advances every in-flight path by one vertex. A job's image is the per-pixel sum of its
+ * samples (what lh2g_render_ex with accumulate = 0 leaves in the accumulator), bit for bit the same whatever else
+ * is in flight. Ray queries run concurrently on a second stream. Scenes are finalized contexts, added by
+ * reference: they must outlive the server and stay unchanged while it runs. Host buffers passed to submit must
+ * stay valid until the job is done; pinned memory makes the copies asynchronous. */
+typedef struct lh2g_server lh2g_server;
+typedef struct lh2g_job_times { double submit, admit, done; } lh2g_job_times;   /* seconds on a steady clock */
+typedef struct lh2g_server_stats {
+    unsigned long long ticks, raysTraced;
+    long long jobsDone, pathsInFlight, pending;
+    uint32_t deviceStatus;
+} lh2g_server_stats;
+LH2G_API int lh2g_server_create(int device, long long pathCapacity, lh2g_server** out);
+LH2G_API int lh2g_server_destroy(lh2g_server* server);   /* finishes the jobs it holds first */
+LH2G_API const char* lh2g_server_last_error(lh2g_server* server);
+LH2G_API int lh2g_server_add_scene(lh2g_server* server, lh2g_context* scene, int* sceneId);
+/* hostOut: width * height float4. Filter frames (LH2G_RP_FILTER) are not served. */
+LH2G_API int lh2g_server_submit_render(lh2g_server* server, int sceneId, const lh2g_view* view, const lh2g_render_params* params,
+                                       float* hostOut, long long* jobId);
+/* ray query as lh2g_trace_host: mode 0 closest hit into lh2g_hit[n], 1 any hit into uint32[n] */
+LH2G_API int lh2g_server_submit_trace(lh2g_server* server, int sceneId, const lh2g_ray* hostRays, long long n, int mode, void* hostOut,
+                                      long long* jobId);
+/* waits up to timeoutMs for a job: LH2G_OK when done (times filled), LH2G_ERR_STATE on timeout */
+LH2G_API int lh2g_server_wait(lh2g_server* server, long long jobId, int timeoutMs, lh2g_job_times* times);
+LH2G_API int lh2g_server_release(lh2g_server* server, long long jobId);   /* forgets a finished job */
+LH2G_API int lh2g_server_get_stats(lh2g_server* server, lh2g_server_stats* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -30,6 +30,10 @@
 
 using namespace lh2g;
 
+namespace lh2g {
+FrameGPU frame_of(const lh2g_view* view, const lh2g_render_params* p);
+}
+
 namespace {
 
 struct MeshDev {
@@ -658,16 +662,7 @@ int lh2g_render_ex(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_p
         const int r = ensure_filter(ctx);
         if (r != LH2G_OK) return r;
     }
-    FrameGPU F;
-    memset(&F, 0, sizeof(F));
-    F.W = p->width, F.H = p->height, F.spp = p->spp, F.maxDepth = p->maxDepth, F.rrStart = p->rrStartDepth, F.samplesTaken = p->samplesTaken;
-    F.cameraR0 = p->cameraR0, F.frameSeed = p->frameSeed, F.eps = p->geometryEpsilon, F.flags = p->flags;
-    F.spreadAngle = view->spreadAngle, F.aperture = view->aperture;
-    F.pos = make_float3(view->pos[0], view->pos[1], view->pos[2]);
-    F.p1 = make_float3(view->p1[0], view->p1[1], view->p1[2]);
-    F.right = make_float3(view->p2[0] - view->p1[0], view->p2[1] - view->p1[1], view->p2[2] - view->p1[2]);
-    F.up = make_float3(view->p3[0] - view->p1[0], view->p3[1] - view->p1[1], view->p3[2] - view->p1[2]);
-    F.P = (int64_t)F.W * F.H * F.spp;
+    FrameGPU F = frame_of(view, p);
     F.stride = ctx->cap;
     WaveBuffers B = ctx->B;
     B.capHits = nullptr, B.capSeeds = nullptr;
@@ -993,6 +988,22 @@ int lh2g_trace_host(lh2g_context* ctx, const lh2g_ray* rays, void* out, long lon
 }  // extern "C"
 
 namespace lh2g {
+/* The device frame parameters of a view and estimator parameters (shared by render_ex and the serving loop). */
+FrameGPU frame_of(const lh2g_view* view, const lh2g_render_params* p) {
+    FrameGPU F;
+    memset(&F, 0, sizeof(F));
+    F.W = p->width, F.H = p->height, F.spp = p->spp, F.maxDepth = p->maxDepth, F.rrStart = p->rrStartDepth, F.samplesTaken = p->samplesTaken;
+    F.cameraR0 = p->cameraR0, F.frameSeed = p->frameSeed, F.eps = p->geometryEpsilon, F.flags = p->flags;
+    F.spreadAngle = view->spreadAngle, F.aperture = view->aperture;
+    F.pos = make_float3(view->pos[0], view->pos[1], view->pos[2]);
+    F.p1 = make_float3(view->p1[0], view->p1[1], view->p1[2]);
+    F.right = make_float3(view->p2[0] - view->p1[0], view->p2[1] - view->p1[1], view->p2[2] - view->p1[2]);
+    F.up = make_float3(view->p3[0] - view->p1[0], view->p3[1] - view->p1[1], view->p3[2] - view->p1[2]);
+    F.P = (int64_t)F.W * F.H * F.spp;
+    F.stride = F.P;
+    return F;
+}
+
 /* Scene and persistent-grid sizes of a finalized context (for the allocation-free render in noalloc.cu). */
 int context_scene(lh2g_context* ctx, SceneGPU* scene, int* device, int* blocks4, int* tailDepth) {
     if (!ctx || !scene || !device || !blocks4 || !tailDepth) return LH2G_ERR_INVALID;

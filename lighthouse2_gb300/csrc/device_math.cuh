@@ -45,9 +45,17 @@ constexpr int MIPLEVELCOUNT = 5;
 constexpr int NOHIT = -1;
 constexpr uint32_t S_SPECULAR = 1;
 
+/* three-input minimum and maximum (one instruction on sm_100 and later; the same value as two fminf / fmaxf) */
+LH2G_DEV float fmax3f(float a, float b, float c) { float d; asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c)); return d; }
+LH2G_DEV float fmin3f(float a, float b, float c) { float d; asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c)); return d; }
+
 /* float -> integer conversions (cvt.rzi: truncation, saturation, NaN -> 0) */
 LH2G_DEV uint32_t f2u(float x) { return __float2uint_rz(x); }
 LH2G_DEV int f2i(float x) { return __float2int_rz(x); }
+/* The float of an unsigned integer v < 2^23, exactly (float)v, without the conversion pipe (a quarter of the
+ * FP32 rate and the bottleneck of code that unpacks many small fixed-point fields): 2^23 + v has the bit
+ * pattern 0x4B000000 | v, and subtracting 2^23 is exact. */
+LH2G_DEV float u2f23(uint32_t v) { return __uint_as_float(0x4B000000u | v) - 8388608.0f; }
 
 /* ---- transcendental functions: Cody-Waite reduction + truncated Taylor series; atanh series for log2 ---- */
 constexpr float CW_PIO2_1 = 1.5703125f, CW_PIO2_2 = 4.838705062866211e-4f, CW_PIO2_3 = -4.371138828673793e-8f;
@@ -73,11 +81,14 @@ LH2G_DEV float exp_cw(float x) {
     if (x != x) return x;
     if (x > 88.72283f) return __int_as_float(0x7f800000);
     if (x < -87.33654f) return 0.0f;
-    const float kf = rintf(x * LOG2E);
+    /* k = rint(x log2 e): |x log2 e| <= 128 here, so adding 1.5 * 2^23 rounds it to an integer (to nearest even,
+     * as rintf does) in the low mantissa bits; no conversion instruction is needed for kf or k */
+    const float shifted = x * LOG2E + 12582912.0f;
+    const float kf = shifted - 12582912.0f;
     float r = x - kf * LN2_HI;
     r = r - kf * LN2_LO;
     const float p = 1.0f + r * (1.0f + r * (0.5f + r * ((float)(1.0 / 6.0) + r * ((float)(1.0 / 24.0) + r * ((float)(1.0 / 120.0) + r * ((float)(1.0 / 720.0) + r * (float)(1.0 / 5040.0)))))));
-    const int k = f2i(kf);
+    const int k = __float_as_int(shifted) - 0x4B400000;
     if (k > 127) return p * __int_as_float(0x7f000000) * 2.0f;
     if (k < -126) return p * __int_as_float((k + 127 + 64) << 23) * __int_as_float(0x1f800000);
     return p * __int_as_float((k + 127) << 23);

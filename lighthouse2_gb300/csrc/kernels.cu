@@ -14,55 +14,25 @@
  * not depend on the order in which the queues were filled.
  */
 #include "kernels.cuh"
-#include "shading.cuh"
-#include "svgf.cuh"
-#include "traverse.cuh"
+#include "wavefront.cuh"
 
 namespace lh2g {
 
 namespace {
 
-constexpr int WAVE_BLOCK = 128;
-
-__device__ __forceinline__ uint32_t lanemask_lt() { uint32_t m; asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m)); return m; }
 
 /* -------------------------------------------------------------------------------------------------- */
 __global__ void __launch_bounds__(256) k_generate(const FrameGPU F, const WaveBuffers B) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= F.P) return;
-    const uint32_t jobIndex = (uint32_t)i;
-    const uint32_t x = jobIndex % (uint32_t)F.W;
-    uint32_t y = jobIndex / (uint32_t)F.W;
-    y %= (uint32_t)F.H;
-    uint32_t seed = WangHash(jobIndex + F.cameraR0);
-    const float r0 = RandomFloat(seed), r1 = RandomFloat(seed);
-    const float r2 = RandomFloat(seed), r3 = RandomFloat(seed);
-    float3 posOnPixel, posOnLens;
-    if (F.flags & LH2G_RP_FILTER) {
-        /* filter core: pixel corner of the jittered view, no lens (RenderCore_Optix7Filter/optix/.optix.cu:66-100) */
-        const float u = (float)x * (1.0f / (float)F.W), v = (float)y * (1.0f / (float)F.H);
-        posOnPixel = F.p1 + u * F.right + v * F.up;
-        posOnLens = F.pos;
-    } else {
-        posOnPixel = F.p1 + ((float)x + r0) * (F.right / (float)F.W) + ((float)y + r1) * (F.up / (float)F.H);
-        const float blade = (float)f2i(r2 * 9);
-        float rr2 = (r2 - blade * (1.0f / 9.0f)) * 9.0f, rr1 = r3;
-        float x1, y1, x2, y2;
-        sincos_cw(blade * PI / 4.5f, &x1, &y1);
-        sincos_cw((blade + 1.0f) * PI / 4.5f, &x2, &y2);
-        if ((rr1 + rr2) > 1) rr1 = 1.0f - rr1, rr2 = 1.0f - rr2;
-        const float xr = x1 * rr1 + x2 * rr2;
-        const float yr = y1 * rr1 + y2 * rr2;
-        posOnLens = F.pos + F.aperture * (F.right * xr + F.up * yr);
-    }
-    const float3 D = normalize(posOnPixel - posOnLens);
-    B.O[0][i] = make_float4(posOnLens.x, posOnLens.y, posOnLens.z, __uint_as_float(jobIndex));
+    float3 O, D;
+    primary_ray(F, (uint32_t)i, O, D);
+    B.O[0][i] = make_float4(O.x, O.y, O.z, __uint_as_float((uint32_t)i));
     B.D[0][i] = make_float4(D.x, D.y, D.z, __uint_as_float(S_SPECULAR));
     B.T[0][i] = make_float4(1.0f, 1.0f, 1.0f, F.eps);
     B.pathAcc[i] = make_float4(0, 0, 0, 0);
     if (F.flags & LH2G_RP_FILTER) B.pathAcc[i + F.P] = make_float4(0, 0, 0, 0);
 }
-
 __device__ __forceinline__ uint32_t queue_count(const FrameGPU& F, const Counters* C, int depth) {
     return depth == 1 ? (uint32_t)F.P : C->extension[depth - 2];
 }
@@ -101,157 +71,10 @@ __global__ void __launch_bounds__(128) k_extend(const SceneGPU S, const FrameGPU
 }
 
 /* -------------------------------------------------------------------------------------------------- */
-struct ShadeOut {
-    bool ext, shadow;
-    float4 eO, eD, eT;
-    float4 sO, sD, sE;
-};
-
-/* Shading of one path vertex (lib/RenderCore_PrimeRef/kernels/pathtracer.h:45-168, with the filter core's
- * feature gathering for LH2G_RP_FILTER): o4, d4, t4 = the path's ray state, hit = its closest hit. Radiance goes
- * to the path's own accumulator; a connection and an extension ray are returned in out. */
-__device__ __forceinline__ void shade_core(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, const int depth, const float4 o4,
-                                           const float4 d4, const float4 t4, const float4 hit, ShadeOut& out, float* pot) {
-    const uint32_t pathIdx = __float_as_uint(o4.w);
-    uint32_t FLAGS = __float_as_uint(d4.w);
-    const float3 O = xyz(o4), D = xyz(d4);
-    float3 throughput = xyz(t4);
-    const int PRIM = __float_as_int(hit.z), INST = __float_as_int(hit.y);
-    const float HIT_T = hit.w;
-    const size_t capIdx = (size_t)(depth - 1) * F.P + pathIdx;
-    const bool filt = (F.flags & LH2G_RP_FILTER) != 0;
-    const uint32_t R0 = filt ? F.frameSeed + (uint32_t)depth * 91771u : (uint32_t)F.samplesTaken * 7907u + (uint32_t)depth * 91771u;
-    /* radiance goes to the indirect half once the path has bounced off a diffuse vertex */
-    const uint32_t half = filt && (FLAGS & S_BOUNCED) ? 1u : 0u;
-    float4* accP = B.pathAcc + (half ? F.P : 0) + pathIdx;
-    /* SVGF data of sample 0 (RenderCore_Optix7Filter/kernels/pathtracer.h:95-104) */
-    const uint32_t WH = (uint32_t)F.W * (uint32_t)F.H;
-    const bool firstHitToBeStored = filt && (FLAGS & S_BOUNCED) == 0 && pathIdx / WH + (uint32_t)F.samplesTaken == 0;
-    const uint32_t isSpecular = (FLAGS & S_VIASPECULAR) ? 1u : 0u;
-    if (depth == 1 && firstHitToBeStored) {
-        PackFeatures(B.features + pathIdx, 0, 0, 1e34f, 0, 0);
-        B.worldPos[pathIdx] = make_float4(0, 0, 0, __uint_as_float(0));
-        B.deltaDepth[pathIdx] = make_float4(0, 0, 0, 0);
-    }
-    float4 acc = *accP;
-    if ((F.flags & LH2G_RP_DEPTH_W) && depth == 1) acc.w += PRIM == NOHIT ? 10000.0f : HIT_T;
-    if (PRIM == NOHIT) {
-        const float3 c = throughput * SampleSkydome(S, D);
-        acc.x += c.x, acc.y += c.y, acc.z += c.z;
-        *accP = acc;
-        if (firstHitToBeStored) {
-            const uint32_t packedNormal = PackNormal2(D * -1.0f) + isSpecular;
-            PackFeatures(B.features + pathIdx, HDRtoRGB32(c), packedNormal, HIT_T, isSpecular, 0);
-            const float3 far = O + 50000 * D;
-            B.worldPos[pathIdx] = make_float4(far.x, far.y, far.z, __uint_as_float(packedNormal));
-            B.deltaDepth[pathIdx] = make_float4(0, 0, 0, 0);
-        }
-        if (B.capSeeds) B.capSeeds[capIdx] = 0;
-        return;
-    }
-    const uint32_t bary = __float_as_uint(hit.x);
-    const float HIT_U = (float)(bary & 65535u) * (1.0f / 65535.0f);
-    const float HIT_V = (float)(bary >> 16) * (1.0f / 65535.0f);
-    Shading sd;
-    float3 N, iN, fN, T;
-    const float3 I = O + HIT_T * D;
-    const float coneWidth = F.spreadAngle * HIT_T;
-    GetShadingData(S, D, HIT_U, HIT_V, coneWidth, INST, PRIM, sd, N, iN, fN, T);
-    const bool nee = (F.flags & LH2G_RP_NEE) != 0;
-    auto matID = [&]() {   /* ShadingData::matID is never assigned in the reference; the material index is what it names */
-        return min(__float_as_uint(__ldg(S.instTris[INST] + (size_t)PRIM * 13 + 1).w), (uint32_t)(S.nMaterials - 1));
-    };
-    auto derivatives = [&]() {
-        return DepthDerivatives((int)(pathIdx % (uint32_t)F.W), (int)(pathIdx / (uint32_t)F.W), F.W, F.H, HIT_T, I, N, F.p1, F.right, F.up, F.pos);
-    };
-    if (IsEmissive(sd)) {
-        const float DdotNL = -dot(D, N);
-        if (DdotNL > 0) {
-            const float3 c = throughput * sd.color;
-            if (depth == 1 || (FLAGS & S_SPECULAR) || !nee) acc.x += c.x, acc.y += c.y, acc.z += c.z;
-        }
-        *accP = acc;
-        if (firstHitToBeStored) {
-            const uint32_t packedNormal = PackNormal2(N) + isSpecular;
-            PackFeatures(B.features + pathIdx, HDRtoRGB32(sd.color), packedNormal, HIT_T, isSpecular, matID());
-            B.worldPos[pathIdx] = make_float4(I.x, I.y, I.z, __uint_as_float(packedNormal));
-            B.deltaDepth[pathIdx] = derivatives();
-        }
-        if (B.capSeeds) B.capSeeds[capIdx] = 0;
-        return;
-    }
-    *accP = acc;
-    if (ROUGHNESS(sd) <= 0.001f || TRANSMISSION(sd) > 0.999f) FLAGS |= S_SPECULAR; else FLAGS &= ~S_SPECULAR;
-    uint32_t seed = WangHash(pathIdx * 17u + R0);
-    if (firstHitToBeStored) {
-        if (FLAGS & S_SPECULAR) {
-            B.features[pathIdx].x = HDRtoRGB32(sd.color);   /* modulated by the first diffuse vertex later */
-        } else {
-            float3 albedo = sd.color;
-            if (FLAGS & S_VIASPECULAR) albedo = albedo * RGB32toHDR(B.features[pathIdx].x);
-            /* the reference writes flip ? -fN : fN with flip = +-1, which always takes the first branch */
-            const uint32_t packedNormal = PackNormal2(fN * -1.0f) + isSpecular;
-            PackFeatures(B.features + pathIdx, HDRtoRGB32(albedo), packedNormal, HIT_T, isSpecular, matID());
-            B.worldPos[pathIdx] = make_float4(I.x, I.y, I.z, __uint_as_float(packedNormal));
-            B.deltaDepth[pathIdx] = derivatives();
-        }
-    }
-    const float faceDir = (dot(D, N) > 0) ? -1.0f : 1.0f;
-    if (faceDir == 1) sd.transmittance = mk3(0);
-    if ((FLAGS & S_SPECULAR) == 0 && nee) {
-        const float q0 = RandomFloat(seed), q1 = RandomFloat(seed);
-        float pickProb = 0, lightPdf = 0;
-        float3 lightColor = mk3(0);
-        float3 L = RandomPointOnLight(S, q0, q1, I, fN * faceDir, pickProb, lightPdf, lightColor, pot, WAVE_BLOCK) - I;
-        const float dist = length(L);
-        L = L * (1.0f / dist);
-        const float NdotL = dot(L, fN * faceDir);
-        if (NdotL > 0 && lightPdf > 0) {
-            float bsdfPdf;
-            const float3 sampledBSDF = EvaluateBSDF(sd, fN, L, bsdfPdf) * ROUGHNESS(sd);
-            const float3 contribution = throughput * sampledBSDF * lightColor * (NdotL / (pickProb * lightPdf));
-            const float3 SO = SafeOrigin(I, L, N, F.eps);
-            out.shadow = true;
-            out.sO = make_float4(SO.x, SO.y, SO.z, __uint_as_float(pathIdx));
-            out.sD = make_float4(L.x, L.y, L.z, dist - 2 * F.eps);
-            out.sE = make_float4(contribution.x, contribution.y, contribution.z, __uint_as_float(half));
-        }
-    }
-    if (depth == F.maxDepth && firstHitToBeStored) {
-        /* the path ends before its first diffuse bounce (RenderCore_Optix7Filter/kernels/pathtracer.h:288-299) */
-        const uint32_t packedNormal = PackNormal2(N) + isSpecular;
-        PackFeatures(B.features + pathIdx, 0, packedNormal, HIT_T, isSpecular, 0);
-        B.worldPos[pathIdx] = make_float4(I.x, I.y, I.z, __uint_as_float(packedNormal));
-    }
-    float3 R;
-    float newBsdfPdf;
-    bool specular = false;
-    const float q3 = RandomFloat(seed), q4 = RandomFloat(seed), q5 = RandomFloat(seed);
-    const float3 bsdf = SampleBSDF(sd, fN, N, D * -1.0f, HIT_T, q3, q4, R, newBsdfPdf, specular);
-    if (B.capSeeds) B.capSeeds[capIdx] = seed;
-    if (newBsdfPdf < EPSILON || isnan(newBsdfPdf)) return;
-    if (specular) FLAGS |= S_SPECULAR;
-    const float pr = depth == F.maxDepth ? 0.0f : (((FLAGS & S_SPECULAR) || depth < F.rrStart) ? 1.0f : SurvivalProbability(bsdf));
-    if (pr <= q5) return;
-    throughput = throughput * (bsdf * fabsf(dot(fN, R)) / (pr * newBsdfPdf));
-    if (!(FLAGS & S_SPECULAR)) FLAGS |= S_BOUNCED; else FLAGS |= S_VIASPECULAR;
-    const float3 EO = SafeOrigin(I, R, N, F.eps);
-    out.ext = true;
-    out.eO = make_float4(EO.x, EO.y, EO.z, __uint_as_float(pathIdx));
-    out.eD = make_float4(R.x, R.y, R.z, __uint_as_float(FLAGS));
-    out.eT = make_float4(throughput.x, throughput.y, throughput.z, 0.0f);
-}
-
 __device__ __forceinline__ void shade_path(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, const int depth, const uint32_t i, ShadeOut& out,
                                            float* pot) {
     const int q = (depth - 1) & 1;
     shade_core(S, F, B, depth, B.O[q][i], B.D[q][i], B.T[q][i], B.hits[i], out, pot);
-}
-
-__device__ __forceinline__ float4 hit_record(const bool found, const HitRec& best) {
-    if (found) return make_float4(__uint_as_float(f2u(65535.0f * best.u) + (f2u(65535.0f * best.v) << 16)), __int_as_float(best.inst),
-                                  __int_as_float(best.prim), best.t);
-    return make_float4(__uint_as_float(0u), __int_as_float(0), __int_as_float(NOHIT), 1e34f);
 }
 
 __global__ void __launch_bounds__(WAVE_BLOCK) k_shade(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int depth) {

@@ -1,0 +1,727 @@
+/* server.cu - the serving loop: render and ray-query jobs of several resident scenes, continuously batched.
+ *
+ * No counterpart in the reference, whose closest analogue is the asynchronous Render / WaitForRender of one core
+ * (lib/rendercore_optix7/rendercore.cpp:803-847, 945-957): one frame at a time per core. Here jobs of different
+ * scenes, resolutions, sample counts and depths share one set of wavefront queues:
+ *
+ *   tick      one CUDA graph, replayed: generate the primary rays of the jobs admitted since the last tick and
+ *             append them to the current queue; extend (closest hit) every ray in the queue; shade every path
+ *             vertex, compacting extension rays into the other queue and connections into the shadow queue;
+ *             connect (any hit); swap the queues; copy the per-job counts of live paths to the host.
+ *             A path carries its job slot (bits 8..15) and its own path length (bits 16..22) in its flag word,
+ *             so paths of jobs admitted at different ticks, and at different depths, are processed together.
+ *   admission a job is admitted when its paths fit in the queue capacity (path memory) and a slot is free;
+ *             jobs wait in arrival order. A job whose live-path count reached zero is finalized (its per-path
+ *             radiance summed per pixel, in sample order), its slot and memory released, and its image copied
+ *             to the caller's host buffer by a worker thread.
+ *   ray queries run on the worker thread's own stream, concurrently with the render ticks.
+ *
+ * Every per-path quantity (RNG seeds, hit records, radiance and its order of accumulation) is the one the
+ * plain core computes for the same job: a job's image does not depend on what else is in flight.
+ * Queue sizes never leave the device; the host reads only the live-path counts, one tick behind.
+ */
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <functional>
+#include <map>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "lh2g.h"
+#include "wavefront.cuh"
+
+namespace lh2g {
+int context_scene(lh2g_context* ctx, SceneGPU* scene, int* device, int* blocks4, int* tailDepth);
+FrameGPU frame_of(const lh2g_view* view, const lh2g_render_params* p);
+void launch_trace(const SceneGPU& S, const lh2g_ray* rays, void* out, long long n, int mode, uint32_t* fetch, uint32_t* status,
+                  int persistentBlocks, cudaStream_t st);
+int persistent_blocks_trace(int mode);
+}  // namespace lh2g
+
+using namespace lh2g;
+
+namespace lh2g {
+namespace srv {
+
+constexpr int MAX_SLOTS = 256;         /* job slots: 8 bits of the flag word */
+constexpr int MAX_NEW = 64;            /* jobs admitted per tick */
+constexpr uint32_t SLOT_SHIFT = 8, DEPTH_SHIFT = 16;
+
+struct JobGPU {
+    FrameGPU F;                        /* F.P = paths of the job */
+    int scene;
+    float4* pathAcc;                   /* F.P entries */
+    float4* out;                       /* W*H: per-pixel sums over the job's samples */
+};
+
+struct ServerState {
+    uint32_t cur;                      /* queue the next tick extends */
+    uint32_t qCount[2];
+    uint32_t shadowCount;
+    uint32_t fetch[4];
+    uint32_t status;
+    uint32_t newCount, newTotal;       /* jobs admitted for the next tick and their paths */
+    uint32_t newSlot[MAX_NEW];
+    uint32_t newPrefix[MAX_NEW + 1];
+    unsigned long long rays;           /* rays traced over all ticks */
+    unsigned long long ticks;
+};
+
+struct Queues {
+    float4* O[2];
+    float4* D[2];
+    float4* T[2];
+    float4* hits;
+    float4* shO;
+    float4* shD;
+    float4* shE;
+};
+
+__device__ __forceinline__ uint32_t slot_of(const float4& d4) { return (__float_as_uint(d4.w) >> SLOT_SHIFT) & 255u; }
+
+/* primary rays of the jobs admitted for this tick, appended to the current queue */
+__global__ void __launch_bounds__(256) k_srv_generate(const JobGPU* __restrict__ jobs, ServerState* st, const Queues Q) {
+    const uint32_t total = st->newTotal, n = st->newCount;
+    if (total == 0) return;
+    const uint32_t cur = st->cur, base = st->qCount[cur];
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        uint32_t j = 0;
+        while (j + 1 < n && st->newPrefix[j + 1] <= g) j++;
+        const uint32_t slot = st->newSlot[j], i = g - st->newPrefix[j];
+        const JobGPU& J = jobs[slot];
+        float3 O, D;
+        primary_ray(J.F, i, O, D);
+        Q.O[cur][base + g] = make_float4(O.x, O.y, O.z, __uint_as_float(i));
+        Q.D[cur][base + g] = make_float4(D.x, D.y, D.z, __uint_as_float(S_SPECULAR | (slot << SLOT_SHIFT) | (1u << DEPTH_SHIFT)));
+        Q.T[cur][base + g] = make_float4(1.0f, 1.0f, 1.0f, J.F.eps);
+        J.pathAcc[i] = make_float4(0, 0, 0, 0);
+    }
+}
+
+/* closest hit of every ray in the current queue, each against the scene of its job */
+__global__ void __launch_bounds__(128) k_srv_extend(const SceneGPU* __restrict__ scenes, const JobGPU* __restrict__ jobs, ServerState* st,
+                                                    const Queues Q) {
+    const uint32_t cur = st->cur, count = st->qCount[cur] + st->newTotal;
+    const uint32_t lane = threadIdx.x & 31u, firstRound = gridDim.x * blockDim.x;
+    uint32_t status = 0;
+    uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
+    for (bool first = true;; first = false) {
+        if (!first) {
+            if (firstRound >= count) break;
+            if (lane == 0) base = firstRound + atomicAdd(&st->fetch[0], 32u);
+            base = __shfl_sync(0xffffffffu, base, 0);
+        }
+        if (base >= count) break;
+        const uint32_t i = base + lane;
+        if (i < count) {
+            const float4 o4 = Q.O[cur][i], d4 = Q.D[cur][i], t4 = Q.T[cur][i];
+            const SceneGPU& S = scenes[jobs[slot_of(d4)].scene];
+            Traversal tr;
+            tr.begin(S, xyz(o4), xyz(d4), t4.w, 1e34f);
+            bool any = false;
+            if (S.tlasRoot != 0xffffffffu)
+                while (tr.step<false>(S, status, any)) {}
+            Q.hits[i] = hit_record(tr.found, tr.best);
+        }
+    }
+    if (status) atomicOr(&st->status, status);
+}
+
+/* one vertex of every path in the current queue: extension rays to the other queue, connections to the shadow
+ * queue (warp ballot + popc, one atomic per warp), finished paths leave their job's live count */
+__global__ void __launch_bounds__(WAVE_BLOCK) k_srv_shade(const SceneGPU* __restrict__ scenes, const JobGPU* __restrict__ jobs, ServerState* st,
+                                                         const Queues Q, int* alive) {
+    const uint32_t cur = st->cur, nq = cur ^ 1u, count = st->qCount[cur] + st->newTotal;
+    const uint32_t lane = threadIdx.x & 31u;
+    __shared__ float potential[64 * WAVE_BLOCK];
+    for (uint32_t b0 = blockIdx.x * blockDim.x; b0 < count; b0 += gridDim.x * blockDim.x) {
+        const uint32_t i = b0 + threadIdx.x;
+        ShadeOut out;
+        out.ext = out.shadow = false;
+        uint32_t slot = 0;
+        if (i < count) {
+            const float4 o4 = Q.O[cur][i], d4 = Q.D[cur][i], t4 = Q.T[cur][i], hit = Q.hits[i];
+            slot = slot_of(d4);
+            const int depth = (int)((__float_as_uint(d4.w) >> DEPTH_SHIFT) & 127u);
+            const JobGPU& J = jobs[slot];
+            WaveBuffers B;
+            memset(&B, 0, sizeof(B));
+            B.pathAcc = J.pathAcc;
+            shade_core(scenes[J.scene], J.F, B, depth, o4, d4, t4, hit, out, potential + threadIdx.x);
+            if (out.ext) out.eD.w = __uint_as_float(__float_as_uint(out.eD.w) + (1u << DEPTH_SHIFT));
+            else atomicSub(&alive[slot], 1);
+            if (out.shadow) out.sE.w = __uint_as_float(__float_as_uint(out.sE.w) | (slot << SLOT_SHIFT));
+        }
+        const uint32_t em = __ballot_sync(0xffffffffu, out.ext);
+        if (em) {
+            const int leader = __ffs(em) - 1;
+            uint32_t s = 0;
+            if ((int)lane == leader) s = atomicAdd(&st->qCount[nq], (uint32_t)__popc(em));
+            s = __shfl_sync(0xffffffffu, s, leader) + __popc(em & lanemask_lt());
+            if (out.ext) Q.O[nq][s] = out.eO, Q.D[nq][s] = out.eD, Q.T[nq][s] = out.eT;
+        }
+        const uint32_t sm = __ballot_sync(0xffffffffu, out.shadow);
+        if (sm) {
+            const int leader = __ffs(sm) - 1;
+            uint32_t s = 0;
+            if ((int)lane == leader) s = atomicAdd(&st->shadowCount, (uint32_t)__popc(sm));
+            s = __shfl_sync(0xffffffffu, s, leader) + __popc(sm & lanemask_lt());
+            if (out.shadow) Q.shO[s] = out.sO, Q.shD[s] = out.sD, Q.shE[s] = out.sE;
+        }
+    }
+}
+
+/* any hit of every connection; unoccluded ones add their contribution to their path */
+__global__ void __launch_bounds__(128) k_srv_connect(const SceneGPU* __restrict__ scenes, const JobGPU* __restrict__ jobs, ServerState* st,
+                                                     const Queues Q) {
+    const uint32_t count = st->shadowCount;
+    const uint32_t lane = threadIdx.x & 31u, firstRound = gridDim.x * blockDim.x;
+    uint32_t status = 0;
+    uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
+    for (bool first = true;; first = false) {
+        if (!first) {
+            if (firstRound >= count) break;
+            if (lane == 0) base = firstRound + atomicAdd(&st->fetch[1], 32u);
+            base = __shfl_sync(0xffffffffu, base, 0);
+        }
+        if (base >= count) break;
+        const uint32_t i = base + lane;
+        if (i < count) {
+            const float4 e = Q.shE[i], o4 = Q.shO[i], d4 = Q.shD[i];
+            const uint32_t tag = __float_as_uint(e.w), slot = (tag >> SLOT_SHIFT) & 255u;
+            const JobGPU& J = jobs[slot];
+            const SceneGPU& S = scenes[J.scene];
+            Traversal tr;
+            tr.begin(S, xyz(o4), xyz(d4), 0.0f, d4.w);
+            bool occluded = false;
+            if (S.tlasRoot != 0xffffffffu)
+                while (tr.step<true>(S, status, occluded)) {}
+            if (!occluded) {
+                float4* accP = J.pathAcc + ((tag & 1u) ? J.F.P : 0) + __float_as_uint(o4.w);
+                float4 acc = *accP;
+                acc.x += e.x, acc.y += e.y, acc.z += e.z;
+                *accP = acc;
+            }
+        }
+    }
+    if (status) atomicOr(&st->status, status);
+}
+
+/* closes a tick: swap the queues, count the rays, clear the per-tick state */
+__global__ void k_srv_end(ServerState* st) {
+    const uint32_t cur = st->cur;
+    st->rays += (unsigned long long)(st->qCount[cur] + st->newTotal) + st->shadowCount;
+    st->ticks++;
+    st->qCount[cur] = 0;
+    st->cur = cur ^ 1u;
+    st->shadowCount = 0;
+    st->fetch[0] = st->fetch[1] = 0;
+    st->newCount = st->newTotal = 0;
+}
+
+/* per-pixel sums of a finished job's paths in sample order (as the plain core's finalize) */
+__global__ void k_srv_finalize(const JobGPU J) {
+    const int64_t px = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t WH = (int64_t)J.F.W * J.F.H;
+    if (px >= WH) return;
+    float4 acc = make_float4(0, 0, 0, 0);
+    for (int s = 0; s < J.F.spp; s++) {
+        const float4 v = J.pathAcc[s * WH + px];
+        acc.x += v.x, acc.y += v.y, acc.z += v.z, acc.w += v.w;
+    }
+    J.out[px] = acc;
+}
+
+double now_s() {
+    static const auto t0 = std::chrono::steady_clock::now();
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+struct Job {
+    long long id = 0;
+    int kind = 0;                      /* 0 render, 1 ray query */
+    int scene = 0;
+    lh2g_view view;
+    lh2g_render_params params;
+    void* hostOut = nullptr;
+    const lh2g_ray* hostRays = nullptr;
+    long long n = 0;                   /* rays of a query */
+    int mode = 0;
+    long long paths = 0;
+    int slot = -1;
+    long long admitTick = -1;
+    int state = 0;                     /* 0 pending, 1 running, 2 finishing, 3 done, 4 failed */
+    double tSubmit = 0, tAdmit = 0, tDone = 0;
+    JobGPU gpu;
+};
+
+}  // namespace srv
+}  // namespace lh2g
+
+using namespace lh2g::srv;
+
+struct lh2g_server {
+    int device = 0;
+    cudaStream_t st = nullptr;         /* render ticks */
+    cudaStream_t io = nullptr;         /* worker: result copies, ray queries */
+    std::string err;
+    std::vector<SceneGPU> scenes;
+    SceneGPU* dScenes = nullptr;
+    JobGPU* dJobs = nullptr;
+    int* dAlive = nullptr;
+    int* hAlive = nullptr;             /* pinned snapshot, refreshed by every tick */
+    ServerState* dState = nullptr;
+    ServerState* hTick = nullptr;      /* pinned staging of the tick parameters, one per tick-event ring entry */
+    Queues Q;
+    long long capacity = 0;
+    cudaGraphExec_t tickExec = nullptr;
+    cudaGraph_t tickGraph = nullptr;
+    std::vector<cudaEvent_t> tickEv;   /* ring of tick-completion events */
+    long long ticksLaunched = 0, ticksDone = 0;
+    int blocksGen = 0, blocksExtend = 0, blocksShade = 0, blocksConnect = 0, blocksTrace0 = 0, blocksTrace1 = 0;
+    /* jobs */
+    std::mutex mu;
+    std::condition_variable cvWork, cvDone;
+    std::deque<Job*> pending;
+    std::map<long long, Job*> jobs;
+    Job* slots[MAX_SLOTS] = {};
+    long long nextId = 1;
+    long long pathsInFlight = 0;
+    bool stop = false;                 /* finish the jobs held, then exit */
+    bool abortLoop = false;            /* exit now (a drain that does not end) */
+    bool loopExited = false;
+    std::thread loop, worker;
+    std::deque<std::function<void()>> tasks;
+    std::mutex tmu;
+    std::condition_variable tcv;
+    /* statistics */
+    long long jobsDone = 0;
+    unsigned long long raysDone = 0;
+};
+
+namespace lh2g {
+namespace srv {
+
+int sfail(lh2g_server* s, int code, const std::string& m) {
+    if (s) {
+        std::lock_guard<std::mutex> g(s->mu);
+        s->err = m;
+    }
+    return code;
+}
+
+void post(lh2g_server* s, std::function<void()> f) {
+    {
+        std::lock_guard<std::mutex> g(s->tmu);
+        s->tasks.push_back(std::move(f));
+    }
+    s->tcv.notify_one();
+}
+
+void finish(lh2g_server* s, Job* j, int state) {
+    std::lock_guard<std::mutex> g(s->mu);
+    j->state = state;
+    j->tDone = now_s();
+    s->jobsDone++;
+    s->cvDone.notify_all();
+}
+
+/* the worker: copies finished images out and runs ray queries, in submission order, on its own stream */
+void worker_loop(lh2g_server* s) {
+    cudaSetDevice(s->device);
+    for (;;) {
+        std::function<void()> f;
+        {
+            std::unique_lock<std::mutex> g(s->tmu);
+            s->tcv.wait(g, [&] { return s->stop || !s->tasks.empty(); });
+            if (s->tasks.empty()) return;
+            f = std::move(s->tasks.front());
+            s->tasks.pop_front();
+        }
+        f();
+    }
+}
+
+void run_query(lh2g_server* s, Job* j) {
+    const SceneGPU S = s->scenes[j->scene];
+    lh2g_ray* dr = nullptr;
+    void* dout = nullptr;
+    uint32_t* fetch = nullptr;
+    const size_t outBytes = (size_t)j->n * (j->mode == 1 ? 4 : 16);
+    bool ok = cudaMallocAsync((void**)&dr, sizeof(lh2g_ray) * (size_t)j->n, s->io) == cudaSuccess &&
+              cudaMallocAsync(&dout, outBytes, s->io) == cudaSuccess && cudaMallocAsync((void**)&fetch, 16, s->io) == cudaSuccess;
+    if (ok) ok = cudaMemcpyAsync(dr, j->hostRays, sizeof(lh2g_ray) * (size_t)j->n, cudaMemcpyHostToDevice, s->io) == cudaSuccess;
+    if (ok) ok = cudaMemsetAsync(fetch, 0, 16, s->io) == cudaSuccess;
+    if (ok) {
+        launch_trace(S, dr, dout, j->n, j->mode, fetch, fetch + 1, j->mode == 1 ? s->blocksTrace1 : s->blocksTrace0, s->io);
+        ok = cudaGetLastError() == cudaSuccess;
+    }
+    if (ok) ok = cudaMemcpyAsync(j->hostOut, dout, outBytes, cudaMemcpyDeviceToHost, s->io) == cudaSuccess;
+    if (dr) cudaFreeAsync(dr, s->io);
+    if (dout) cudaFreeAsync(dout, s->io);
+    if (fetch) cudaFreeAsync(fetch, s->io);
+    ok = cudaStreamSynchronize(s->io) == cudaSuccess && ok;
+    {
+        std::lock_guard<std::mutex> g(s->mu);
+        s->raysDone += (unsigned long long)j->n;
+    }
+    finish(s, j, ok ? 3 : 4);
+}
+
+/* admits pending render jobs in arrival order while they fit; ray queries go to the worker */
+void admit(lh2g_server* s, std::vector<Job*>& admitted) {
+    std::lock_guard<std::mutex> g(s->mu);
+    while (!s->pending.empty() && (int)admitted.size() < MAX_NEW) {
+        Job* j = s->pending.front();
+        if (j->kind == 1) {
+            s->pending.pop_front();
+            j->state = 1, j->tAdmit = now_s();
+            post(s, [s, j] { run_query(s, j); });
+            continue;
+        }
+        if (s->pathsInFlight + j->paths > s->capacity) break;   /* wait for path memory: arrival order is kept */
+        int slot = -1;
+        for (int k = 0; k < MAX_SLOTS; k++)
+            if (!s->slots[k]) { slot = k; break; }
+        if (slot < 0) break;
+        s->pending.pop_front();
+        j->slot = slot;
+        s->slots[slot] = j;
+        s->pathsInFlight += j->paths;
+        j->state = 1, j->tAdmit = now_s();
+        admitted.push_back(j);
+    }
+}
+
+void tick_loop_body(lh2g_server* s);
+
+void tick_loop(lh2g_server* s) {
+    tick_loop_body(s);
+    cudaStreamSynchronize(s->st);
+    std::lock_guard<std::mutex> g(s->mu);
+    s->loopExited = true;
+    s->cvDone.notify_all();
+}
+
+void tick_loop_body(lh2g_server* s) {
+    cudaSetDevice(s->device);
+    const int ring = (int)s->tickEv.size();
+    std::vector<Job*> admitted;
+    for (;;) {
+        admitted.clear();
+        admit(s, admitted);
+        bool active = false;
+        {
+            std::unique_lock<std::mutex> g(s->mu);
+            if (s->abortLoop) return;
+            for (int k = 0; k < MAX_SLOTS && !active; k++) active = s->slots[k] != nullptr;
+            if (!active && admitted.empty()) {
+                if (s->stop) return;
+                s->cvWork.wait_for(g, std::chrono::milliseconds(2));
+                continue;
+            }
+        }
+        /* new jobs: device records, live counts, per-job memory (stream-ordered), tick parameters */
+        uint32_t total = 0;
+        /* staging entry of this tick: its previous user (ticksLaunched - ring) has completed, since at most two
+         * ticks are in flight */
+        ServerState& tp = s->hTick[s->ticksLaunched % ring];
+        tp.newCount = (uint32_t)admitted.size();
+        for (size_t k = 0; k < admitted.size(); k++) {
+            Job* j = admitted[k];
+            JobGPU& G = j->gpu;
+            G.F = frame_of(&j->view, &j->params);
+            G.scene = j->scene;
+            G.pathAcc = nullptr, G.out = nullptr;
+            if (cudaMallocAsync((void**)&G.pathAcc, sizeof(float4) * (size_t)j->paths, s->st) != cudaSuccess ||
+                cudaMallocAsync((void**)&G.out, sizeof(float4) * (size_t)G.F.W * G.F.H, s->st) != cudaSuccess) {
+                /* no device memory for this job: it fails, the others go on */
+                if (G.pathAcc) cudaFreeAsync(G.pathAcc, s->st);
+                {
+                    std::lock_guard<std::mutex> g(s->mu);
+                    s->slots[j->slot] = nullptr;
+                    s->pathsInFlight -= j->paths;
+                }
+                finish(s, j, 4);
+                admitted.erase(admitted.begin() + (long)k--);
+                continue;
+            }
+            cudaMemcpyAsync(s->dJobs + j->slot, &G, sizeof(JobGPU), cudaMemcpyHostToDevice, s->st);
+            const int live = (int)j->paths;
+            cudaMemcpyAsync(s->dAlive + j->slot, &live, sizeof(int), cudaMemcpyHostToDevice, s->st);
+            tp.newSlot[k] = (uint32_t)j->slot;
+            tp.newPrefix[k] = total;
+            total += (uint32_t)j->paths;
+            j->admitTick = s->ticksLaunched;
+        }
+        tp.newPrefix[admitted.size()] = total;
+        tp.newTotal = total;
+        cudaMemcpyAsync(&s->dState->newCount, &tp.newCount, offsetof(ServerState, rays) - offsetof(ServerState, newCount), cudaMemcpyHostToDevice,
+                        s->st);
+        /* the tick */
+        cudaGraphLaunch(s->tickExec, s->st);
+        cudaEventRecord(s->tickEv[s->ticksLaunched % ring], s->st);
+        s->ticksLaunched++;
+        /* at most two ticks in flight: the host prepares the next tick while the GPU runs the current one; the
+         * live counts on the host are then at least as new as the older of the two */
+        while (s->ticksLaunched - s->ticksDone > 1) {
+            cudaEventSynchronize(s->tickEv[s->ticksDone % ring]);
+            s->ticksDone++;
+        }
+        /* jobs with no live path left: finalize, release, copy out */
+        std::vector<Job*> done;
+        {
+            std::lock_guard<std::mutex> g(s->mu);
+            for (int k = 0; k < MAX_SLOTS; k++) {
+                Job* j = s->slots[k];
+                if (j && j->admitTick < s->ticksDone && s->hAlive[k] <= 0) done.push_back(j);
+            }
+        }
+        for (Job* j : done) {
+            JobGPU& G = j->gpu;
+            const int64_t WH = (int64_t)G.F.W * G.F.H;
+            k_srv_finalize<<<(unsigned)((WH + 255) / 256), 256, 0, s->st>>>(G);
+            cudaFreeAsync(G.pathAcc, s->st);
+            cudaEvent_t ev;
+            cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+            cudaEventRecord(ev, s->st);
+            {
+                std::lock_guard<std::mutex> g(s->mu);
+                s->slots[j->slot] = nullptr;
+                s->pathsInFlight -= j->paths;
+                j->state = 2;
+            }
+            post(s, [s, j, ev] {
+                JobGPU& G2 = j->gpu;
+                cudaStreamWaitEvent(s->io, ev, 0);
+                const size_t bytes = sizeof(float4) * (size_t)G2.F.W * G2.F.H;
+                bool ok = cudaMemcpyAsync(j->hostOut, G2.out, bytes, cudaMemcpyDeviceToHost, s->io) == cudaSuccess;
+                cudaFreeAsync(G2.out, s->io);
+                ok = cudaStreamSynchronize(s->io) == cudaSuccess && ok;
+                cudaEventDestroy(ev);
+                finish(s, j, ok ? 3 : 4);
+            });
+        }
+        if (!done.empty()) s->cvWork.notify_all();
+    }
+}
+
+int build_tick_graph(lh2g_server* s) {
+    if (cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return LH2G_ERR_CUDA;
+    k_srv_generate<<<s->blocksGen, 256, 0, s->st>>>(s->dJobs, s->dState, s->Q);
+    k_srv_extend<<<s->blocksExtend, 128, 0, s->st>>>(s->dScenes, s->dJobs, s->dState, s->Q);
+    k_srv_shade<<<s->blocksShade, WAVE_BLOCK, 0, s->st>>>(s->dScenes, s->dJobs, s->dState, s->Q, s->dAlive);
+    k_srv_connect<<<s->blocksConnect, 128, 0, s->st>>>(s->dScenes, s->dJobs, s->dState, s->Q);
+    k_srv_end<<<1, 1, 0, s->st>>>(s->dState);
+    cudaMemcpyAsync(s->hAlive, s->dAlive, sizeof(int) * MAX_SLOTS, cudaMemcpyDeviceToHost, s->st);
+    if (cudaStreamEndCapture(s->st, &s->tickGraph) != cudaSuccess) return LH2G_ERR_CUDA;
+    if (cudaGraphInstantiate(&s->tickExec, s->tickGraph, 0) != cudaSuccess) return LH2G_ERR_CUDA;
+    return LH2G_OK;
+}
+
+template <typename K>
+int occupancy_blocks(K kernel, int threads) {
+    int dev = 0, sms = 1, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, 0);
+    return sms * std::max(per, 1);
+}
+
+}  // namespace srv
+}  // namespace lh2g
+
+extern "C" {
+
+int lh2g_server_create(int device, long long pathCapacity, lh2g_server** out) {
+    if (!out || pathCapacity <= 0 || pathCapacity >= (1ll << 31)) return LH2G_ERR_INVALID;
+    *out = nullptr;
+    lh2g_server* s = new lh2g_server();
+    s->device = device;
+    s->capacity = pathCapacity;
+    memset(&s->Q, 0, sizeof(s->Q));
+    bool ok = cudaSetDevice(device) == cudaSuccess;
+    ok = ok && cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) == cudaSuccess;
+    ok = ok && cudaStreamCreateWithFlags(&s->io, cudaStreamNonBlocking) == cudaSuccess;
+    const size_t cap = (size_t)pathCapacity;
+    for (int k = 0; k < 2 && ok; k++)
+        ok = cudaMalloc((void**)&s->Q.O[k], 16 * cap) == cudaSuccess && cudaMalloc((void**)&s->Q.D[k], 16 * cap) == cudaSuccess &&
+             cudaMalloc((void**)&s->Q.T[k], 16 * cap) == cudaSuccess;
+    ok = ok && cudaMalloc((void**)&s->Q.hits, 16 * cap) == cudaSuccess && cudaMalloc((void**)&s->Q.shO, 16 * cap) == cudaSuccess &&
+         cudaMalloc((void**)&s->Q.shD, 16 * cap) == cudaSuccess && cudaMalloc((void**)&s->Q.shE, 16 * cap) == cudaSuccess;
+    ok = ok && cudaMalloc((void**)&s->dJobs, sizeof(JobGPU) * MAX_SLOTS) == cudaSuccess;
+    ok = ok && cudaMalloc((void**)&s->dAlive, sizeof(int) * MAX_SLOTS) == cudaSuccess;
+    ok = ok && cudaMalloc((void**)&s->dState, sizeof(ServerState)) == cudaSuccess;
+    ok = ok && cudaMalloc((void**)&s->dScenes, sizeof(SceneGPU) * 64) == cudaSuccess;
+    ok = ok && cudaMallocHost((void**)&s->hAlive, sizeof(int) * MAX_SLOTS) == cudaSuccess;
+    ok = ok && cudaMallocHost((void**)&s->hTick, sizeof(ServerState) * 4) == cudaSuccess;
+    if (ok) {
+        cudaMemset(s->dAlive, 0, sizeof(int) * MAX_SLOTS);
+        cudaMemset(s->dState, 0, sizeof(ServerState));
+        memset(s->hAlive, 0, sizeof(int) * MAX_SLOTS);
+        memset(s->hTick, 0, sizeof(ServerState) * 4);
+        /* per-job memory comes from the stream-ordered pool: keep what it holds between jobs */
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+            uint64_t keep = ~0ull;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        s->blocksGen = occupancy_blocks(k_srv_generate, 256);
+        s->blocksExtend = occupancy_blocks(k_srv_extend, 128);
+        s->blocksShade = occupancy_blocks(k_srv_shade, WAVE_BLOCK);
+        s->blocksConnect = occupancy_blocks(k_srv_connect, 128);
+        s->blocksTrace0 = persistent_blocks_trace(0);
+        s->blocksTrace1 = persistent_blocks_trace(1);
+        s->tickEv.resize(4);
+        for (auto& e : s->tickEv) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+        ok = ok && cudaDeviceSynchronize() == cudaSuccess;
+        ok = ok && build_tick_graph(s) == LH2G_OK;
+    }
+    if (!ok) {
+        lh2g_server_destroy(s);
+        return LH2G_ERR_CUDA;
+    }
+    s->loop = std::thread(tick_loop, s);
+    s->worker = std::thread(worker_loop, s);
+    *out = s;
+    return LH2G_OK;
+}
+
+int lh2g_server_destroy(lh2g_server* s) {
+    if (!s) return LH2G_ERR_INVALID;
+    {
+        std::unique_lock<std::mutex> g(s->mu);
+        s->stop = true;
+        s->cvWork.notify_all();
+        /* let the loop finish the jobs it holds; a drain longer than 30 s ends it */
+        if (s->loop.joinable() && !s->cvDone.wait_for(g, std::chrono::seconds(30), [&] { return s->loopExited; })) s->abortLoop = true;
+    }
+    s->cvWork.notify_all();
+    if (s->loop.joinable()) s->loop.join();
+    {
+        std::lock_guard<std::mutex> g(s->tmu);
+    }
+    s->tcv.notify_all();
+    if (s->worker.joinable()) s->worker.join();
+    cudaSetDevice(s->device);
+    if (s->st) cudaStreamSynchronize(s->st);
+    if (s->io) cudaStreamSynchronize(s->io);
+    if (s->tickExec) cudaGraphExecDestroy(s->tickExec);
+    if (s->tickGraph) cudaGraphDestroy(s->tickGraph);
+    for (auto& e : s->tickEv) if (e) cudaEventDestroy(e);
+    for (int k = 0; k < 2; k++) cudaFree(s->Q.O[k]), cudaFree(s->Q.D[k]), cudaFree(s->Q.T[k]);
+    cudaFree(s->Q.hits), cudaFree(s->Q.shO), cudaFree(s->Q.shD), cudaFree(s->Q.shE);
+    cudaFree(s->dJobs), cudaFree(s->dAlive), cudaFree(s->dState), cudaFree(s->dScenes);
+    if (s->hAlive) cudaFreeHost(s->hAlive);
+    if (s->hTick) cudaFreeHost(s->hTick);
+    for (auto& kv : s->jobs) delete kv.second;
+    if (s->st) cudaStreamDestroy(s->st);
+    if (s->io) cudaStreamDestroy(s->io);
+    delete s;
+    return LH2G_OK;
+}
+
+const char* lh2g_server_last_error(lh2g_server* s) { return s ? s->err.c_str() : "null server"; }
+
+int lh2g_server_add_scene(lh2g_server* s, lh2g_context* ctx, int* sceneId) {
+    if (!s || !ctx || !sceneId) return LH2G_ERR_INVALID;
+    SceneGPU S;
+    int dev = 0, blocks[4], tail = 0;
+    const int r = context_scene(ctx, &S, &dev, blocks, &tail);
+    if (r != LH2G_OK) return sfail(s, r, "add_scene: the context has no finalized scene");
+    if (dev != s->device) return sfail(s, LH2G_ERR_INVALID, "add_scene: the context is on another device");
+    std::lock_guard<std::mutex> g(s->mu);
+    if (s->scenes.size() >= 64) { s->err = "add_scene: at most 64 scenes"; return LH2G_ERR_OVERFLOW; }
+    /* a new table entry that no job refers to yet: safe to write while ticks run */
+    cudaSetDevice(s->device);
+    if (cudaMemcpy(s->dScenes + s->scenes.size(), &S, sizeof(SceneGPU), cudaMemcpyHostToDevice) != cudaSuccess) {
+        s->err = "add_scene: copy failed";
+        return LH2G_ERR_CUDA;
+    }
+    *sceneId = (int)s->scenes.size();
+    s->scenes.push_back(S);
+    return LH2G_OK;
+}
+
+int lh2g_server_submit_render(lh2g_server* s, int sceneId, const lh2g_view* view, const lh2g_render_params* p, float* hostOut, long long* jobId) {
+    if (!s || !view || !p || !hostOut || !jobId) return LH2G_ERR_INVALID;
+    if (p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->maxDepth < 1 || p->maxDepth > 64 || (p->flags & LH2G_RP_FILTER))
+        return sfail(s, LH2G_ERR_INVALID, "submit_render: bad parameters (filter frames are not served)");
+    const long long P = (long long)p->width * p->height * p->spp;
+    Job* j = new Job();
+    j->kind = 0, j->view = *view, j->params = *p, j->hostOut = hostOut, j->paths = P, j->tSubmit = now_s();
+    {
+        std::lock_guard<std::mutex> g(s->mu);
+        if (sceneId < 0 || sceneId >= (int)s->scenes.size()) { delete j; s->err = "submit_render: unknown scene"; return LH2G_ERR_INVALID; }
+        if (P > s->capacity) { delete j; s->err = "submit_render: the job has more paths than the server's capacity"; return LH2G_ERR_OVERFLOW; }
+        j->scene = sceneId;
+        j->id = s->nextId++;
+        s->jobs[j->id] = j;
+        s->pending.push_back(j);
+        *jobId = j->id;
+    }
+    s->cvWork.notify_all();
+    return LH2G_OK;
+}
+
+int lh2g_server_submit_trace(lh2g_server* s, int sceneId, const lh2g_ray* hostRays, long long n, int mode, void* hostOut, long long* jobId) {
+    if (!s || !hostRays || !hostOut || !jobId || n <= 0 || n >= (1ll << 31) || (mode != 0 && mode != 1)) return LH2G_ERR_INVALID;
+    Job* j = new Job();
+    j->kind = 1, j->hostRays = hostRays, j->n = n, j->mode = mode, j->hostOut = hostOut, j->tSubmit = now_s();
+    {
+        std::lock_guard<std::mutex> g(s->mu);
+        if (sceneId < 0 || sceneId >= (int)s->scenes.size()) { delete j; s->err = "submit_trace: unknown scene"; return LH2G_ERR_INVALID; }
+        j->scene = sceneId;
+        j->id = s->nextId++;
+        s->jobs[j->id] = j;
+        s->pending.push_back(j);
+        *jobId = j->id;
+    }
+    s->cvWork.notify_all();
+    return LH2G_OK;
+}
+
+int lh2g_server_wait(lh2g_server* s, long long jobId, int timeoutMs, lh2g_job_times* times) {
+    if (!s) return LH2G_ERR_INVALID;
+    std::unique_lock<std::mutex> g(s->mu);
+    auto it = s->jobs.find(jobId);
+    if (it == s->jobs.end()) return LH2G_ERR_INVALID;
+    Job* j = it->second;
+    const bool done = s->cvDone.wait_for(g, std::chrono::milliseconds(timeoutMs < 0 ? 0 : timeoutMs), [&] { return j->state >= 3; });
+    if (!done) return LH2G_ERR_STATE;
+    if (times) times->submit = j->tSubmit, times->admit = j->tAdmit, times->done = j->tDone;
+    return j->state == 3 ? LH2G_OK : LH2G_ERR_CUDA;
+}
+
+int lh2g_server_release(lh2g_server* s, long long jobId) {
+    if (!s) return LH2G_ERR_INVALID;
+    std::lock_guard<std::mutex> g(s->mu);
+    auto it = s->jobs.find(jobId);
+    if (it == s->jobs.end() || it->second->state < 3) return LH2G_ERR_STATE;
+    delete it->second;
+    s->jobs.erase(it);
+    return LH2G_OK;
+}
+
+int lh2g_server_get_stats(lh2g_server* s, lh2g_server_stats* out) {
+    if (!s || !out) return LH2G_ERR_INVALID;
+    ServerState st;
+    cudaSetDevice(s->device);
+    /* a plain read of two counters; the copy may overlap a running tick (values from some tick boundary) */
+    if (cudaMemcpy(&st, s->dState, sizeof(ServerState), cudaMemcpyDeviceToHost) != cudaSuccess) return LH2G_ERR_CUDA;
+    std::lock_guard<std::mutex> g(s->mu);
+    out->ticks = st.ticks;
+    out->raysTraced = st.rays + s->raysDone;
+    out->jobsDone = s->jobsDone;
+    out->pathsInFlight = s->pathsInFlight;
+    out->pending = (long long)s->pending.size();
+    out->deviceStatus = st.status;
+    return LH2G_OK;
+}
+
+}  // extern "C"

@@ -15,12 +15,17 @@
  * The TAA pass reads the phase-3 image and writes a separate buffer: the reference updates its input in place
  * while neighbouring threads still read it.
  */
+#include "fp_exact.h"
 #include "svgf.cuh"
 
 namespace lh2g {
 namespace {
 
 constexpr int BX = 32, BY = 8;
+
+/* w * 0.0001 rounded as the reference's float * double product; out of line so that only warps with a lane
+ * on a material edge execute it (inlined, it is if-converted into every tap) */
+__device__ __noinline__ float material_stop(const float w) { return mul_float_by_double(w, DBL_1EM4_MANT, DBL_1EM4_EXP); }
 
 struct Px {
     int x, y;
@@ -202,8 +207,9 @@ __global__ void __launch_bounds__(BX* BY) k_apply(const SvgfBuffers b, const Svg
             const float depthError = fabsf(expected - __uint_as_float(nf.z));
             const float expectedDifference = fabsf(expected - localDepth);
             const float w_depth = depthError / fmaxf(0.00001f, (0.5f + (float)PHASE * 0.5f) * expectedDifference);
-            /* material stop: the reference multiplies by the double literal 0.0001 here, so in double */
-            if ((nf.w >> 4) != localMatID) w_normal = (float)((double)w_normal * 0.0001);
+            /* material stop: the reference multiplies by the double literal 0.0001 here, i.e. in double; the same
+             * float comes from exact integer arithmetic (no FP64 instruction) */
+            if ((nf.w >> 4) != localMatID) w_normal = material_stop(w_normal);
             else w_normal = w_normal * dot(localColor, RGB32toHDR(nf.x));
             float w_dir = w_normal * exp_cw(fabsf(localDirect - Luminance(nDirect)) * rdir + w_dist - w_depth);
             float w_ind = w_normal * exp_cw(fabsf(localIndirect - Luminance(nIndirect)) * rind + w_dist - w_depth);

@@ -4,7 +4,10 @@
  *   normal    10 bits per component at bits 2, 12, 22 ((n + 1) * 511); bits 0-1 hold the specular flag
  *   albedo    10:11:11 unsigned fixed point of min(1, c)
  *   light     two rgb triples as 5:11 unsigned fixed point in the bits of one float4 (direct in x, y;
- *             indirect in z, w), clamped at 31.999
+ *             indirect in z, w), clamped at 31.999, so every field is below 65534 (the third field's word is
+ *             masked to 23 bits when unpacked, which keeps every word the packer writes unchanged)
+ * Fields are turned into floats with u2f23 (exact, no conversion instruction): the a-trous taps unpack ~290
+ * fields per pixel and pass.
  *   features  uint4 {albedo, normal | specular, depth bits, history (4 bits) | specular << 4 | material << 6}
  */
 #pragma once
@@ -31,7 +34,7 @@ LH2G_DEV uint32_t PackNormal2(const float3 N) {
 }
 LH2G_DEV float3 UnpackNormal2(const uint32_t pi) {
     const uint32_t x = (pi >> 2u) & 1023u, y = (pi >> 12u) & 1023u, z = pi >> 22u;
-    return make_float3((float)x * (1.0f / 511.0f) - 1, (float)y * (1.0f / 511.0f) - 1, (float)z * (1.0f / 511.0f) - 1);
+    return make_float3(u2f23(x) * (1.0f / 511.0f) - 1, u2f23(y) * (1.0f / 511.0f) - 1, u2f23(z) * (1.0f / 511.0f) - 1);
 }
 LH2G_DEV uint32_t HDRtoRGB32(const float3& c) {
     const uint32_t r = f2u(1023.0f * fminf(1.0f, c.x));
@@ -40,11 +43,11 @@ LH2G_DEV uint32_t HDRtoRGB32(const float3& c) {
     return (r << 22) + (g << 11) + b;
 }
 LH2G_DEV float3 RGB32toHDR(const uint32_t c) {
-    return make_float3((float)(c >> 22) * (1.0f / 1023.0f), (float)((c >> 11) & 2047u) * (1.0f / 2047.0f), (float)(c & 2047u) * (1.0f / 2047.0f));
+    return make_float3(u2f23(c >> 22) * (1.0f / 1023.0f), u2f23((c >> 11) & 2047u) * (1.0f / 2047.0f), u2f23(c & 2047u) * (1.0f / 2047.0f));
 }
 LH2G_DEV float3 RGB32toHDRmin1(const uint32_t c) {
-    return make_float3((float)max(1u, c >> 22) * (1.0f / 1023.0f), (float)max(1u, (c >> 11) & 2047u) * (1.0f / 2047.0f),
-                       (float)max(1u, c & 2047u) * (1.0f / 2047.0f));
+    return make_float3(u2f23(max(1u, c >> 22)) * (1.0f / 1023.0f), u2f23(max(1u, (c >> 11) & 2047u)) * (1.0f / 2047.0f),
+                       u2f23(max(1u, c & 2047u)) * (1.0f / 2047.0f));
 }
 /* PackFeatures (RenderCore_Optix7Filter/kernels/pathtracer.h:44-47); the history count in w & 15 survives */
 LH2G_DEV void PackFeatures(uint4* f, const uint32_t albedo, const uint32_t packedNormal, const float t, const uint32_t isSpecular,
@@ -83,11 +86,11 @@ LH2G_DEV float4 CombineToFloat4(const float3& A, const float3& B) {
 }
 LH2G_DEV float3 GetDirect(const float4& X) {
     const uint32_t v0 = __float_as_uint(X.x), v1 = __float_as_uint(X.y);
-    return make_float3((float)(v0 >> 16) * (1.0f / 2048.0f), (float)(v0 & 65535u) * (1.0f / 2048.0f), (float)v1 * (1.0f / 2048.0f));
+    return make_float3(u2f23(v0 >> 16) * (1.0f / 2048.0f), u2f23(v0 & 65535u) * (1.0f / 2048.0f), u2f23(v1 & 0x7fffffu) * (1.0f / 2048.0f));
 }
 LH2G_DEV float3 GetIndirect(const float4& X) {
     const uint32_t v2 = __float_as_uint(X.z), v3 = __float_as_uint(X.w);
-    return make_float3((float)(v2 >> 16) * (1.0f / 2048.0f), (float)(v2 & 65535u) * (1.0f / 2048.0f), (float)v3 * (1.0f / 2048.0f));
+    return make_float3(u2f23(v2 >> 16) * (1.0f / 2048.0f), u2f23(v2 & 65535u) * (1.0f / 2048.0f), u2f23(v3 & 0x7fffffu) * (1.0f / 2048.0f));
 }
 LH2G_DEV float oneoverpow2(const int p) { return __uint_as_float((uint32_t)(127 - p) << 23); }
 /* x^128 by seven squarings (the reference calls powf(x, 128)) */

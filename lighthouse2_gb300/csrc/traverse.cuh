@@ -67,6 +67,9 @@ LH2G_DEV bool isect_tri(const float3 O, const float3 D, const float4 a, const fl
 }
 
 LH2G_DEV uint32_t byte_of(uint32_t w0, uint32_t w1, int i) { return ((i < 4 ? w0 : w1) >> ((i & 3) * 8)) & 255u; }
+/* byte i & 3 of w as a float, exactly: one byte permute builds the bits of 2^23 + byte (0x4B0000bb), one FADD
+ * removes 2^23 (an integer-to-float conversion would run on the quarter-rate conversion pipe, 48 times per node) */
+LH2G_DEV float plane_byte(uint32_t w, int i) { return __uint_as_float(__byte_perm(w, 0x4Bu, 0x4550u | (uint32_t)(i & 3))) - 8388608.0f; }
 
 /* Compare-exchange for the sorting network. */
 LH2G_DEV void cx(uint32_t& a, uint32_t& b) { const uint32_t lo = min(a, b), hi = max(a, b); a = lo, b = hi; }
@@ -128,14 +131,14 @@ struct Traversal {
         for (int i = 0; i < 8; i++) {
             const uint32_t sel = 0x4440u | (uint32_t)(i & 3);
             const uint32_t meta = __byte_perm(i < 4 ? metaLo : metaHi, 0u, sel);
-            const float txn = fmaf((float)__byte_perm(i < 4 ? nlx0 : nlx1, 0u, sel), ax, bx);
-            const float txf = fmaf((float)__byte_perm(i < 4 ? nhx0 : nhx1, 0u, sel), ax, bx);
-            const float tyn = fmaf((float)__byte_perm(i < 4 ? nly0 : nly1, 0u, sel), ay, by);
-            const float tyf = fmaf((float)__byte_perm(i < 4 ? nhy0 : nhy1, 0u, sel), ay, by);
-            const float tzn = fmaf((float)__byte_perm(i < 4 ? nlz0 : nlz1, 0u, sel), az, bz);
-            const float tzf = fmaf((float)__byte_perm(i < 4 ? nhz0 : nhz1, 0u, sel), az, bz);
-            float tn = fmaxf(fmaxf(txn, tyn), tzn);
-            float tf = fminf(fminf(txf, tyf), tzf);
+            const float txn = fmaf(plane_byte(i < 4 ? nlx0 : nlx1, i), ax, bx);
+            const float txf = fmaf(plane_byte(i < 4 ? nhx0 : nhx1, i), ax, bx);
+            const float tyn = fmaf(plane_byte(i < 4 ? nly0 : nly1, i), ay, by);
+            const float tyf = fmaf(plane_byte(i < 4 ? nhy0 : nhy1, i), ay, by);
+            const float tzn = fmaf(plane_byte(i < 4 ? nlz0 : nlz1, i), az, bz);
+            const float tzf = fmaf(plane_byte(i < 4 ? nhz0 : nhz1, i), az, bz);
+            float tn = fmax3f(txn, tyn, tzn);
+            float tf = fmin3f(txf, tyf, tzf);
             tn = fmaf(-fabsf(tn), BOX_MARGIN, tn) - err;
             tf = fmaf(fabsf(tf), BOX_MARGIN, tf) + err;
             tn = fmaxf(tn, tmin);
@@ -276,14 +279,14 @@ LH2G_DEV bool coop_step(const SceneGPU& S, CoopRay& r, uint2* stk, const int g, 
         const float err = (fmaxf(fmaxf(fabsf(bx), fabsf(by)), fabsf(bz)) + 255.0f * fmaxf(fmaxf(fabsf(ax), fabsf(ay)), fabsf(az))) * 9.5367431640625e-07f;
         const uint32_t sel = 0x4440u | (uint32_t)(g & 3), hi = g >= 4;
         const uint32_t meta = __byte_perm(hi ? n1.w : n1.z, 0u, sel);
-        const float qlx = (float)__byte_perm(hi ? n2.y : n2.x, 0u, sel), qhx = (float)__byte_perm(hi ? n3.w : n3.z, 0u, sel);
-        const float qly = (float)__byte_perm(hi ? n2.w : n2.z, 0u, sel), qhy = (float)__byte_perm(hi ? n4.y : n4.x, 0u, sel);
-        const float qlz = (float)__byte_perm(hi ? n3.y : n3.x, 0u, sel), qhz = (float)__byte_perm(hi ? n4.w : n4.z, 0u, sel);
+        const float qlx = plane_byte(hi ? n2.y : n2.x, g), qhx = plane_byte(hi ? n3.w : n3.z, g);
+        const float qly = plane_byte(hi ? n2.w : n2.z, g), qhy = plane_byte(hi ? n4.y : n4.x, g);
+        const float qlz = plane_byte(hi ? n3.y : n3.x, g), qhz = plane_byte(hi ? n4.w : n4.z, g);
         const float tx0 = fmaf(qlx, ax, bx), tx1 = fmaf(qhx, ax, bx);
         const float ty0 = fmaf(qly, ay, by), ty1 = fmaf(qhy, ay, by);
         const float tz0 = fmaf(qlz, az, bz), tz1 = fmaf(qhz, az, bz);
-        float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
-        float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+        float tn = fmax3f(fminf(tx0, tx1), fminf(ty0, ty1), fminf(tz0, tz1));
+        float tf = fmin3f(fmaxf(tx0, tx1), fmaxf(ty0, ty1), fmaxf(tz0, tz1));
         tn = fmaf(-fabsf(tn), BOX_MARGIN, tn) - err;
         tf = fmaf(fabsf(tf), BOX_MARGIN, tf) + err;
         tn = fmaxf(tn, r.tmin);
