@@ -248,6 +248,9 @@ def serving_leg(args):
         cores.append(core)
     setup_s = time.time() - t0
     jobs = serving_jobs(args.serving_jobs, len(cores))
+    import torch
+    # pinned host images for both arms (copies back are part of each job's latency)
+    pinned = [torch.empty((j["W"] * j["H"], 4), dtype=torch.float32, pin_memory=True).numpy() for j in jobs]
 
     def inputs(j):
         view = S.cornell_view(j["W"], j["H"], frame=j["frame"] % 4) if j["scene"] == 0 else S.spheres_view(j["W"], j["H"], frame=j["frame"])
@@ -273,7 +276,7 @@ def serving_leg(args):
         c.WaitForRender()
         t = time.perf_counter()
         out = c.render_ex(view, p, counters=True)
-        c.read_accumulator()
+        c.read_accumulator_into(pinned[len(service)])
         service.append(time.perf_counter() - t)
         cnt = out["counters"]
         seq_rays += j["W"] * j["H"] * j["spp"] + int(cnt[:, 0].sum()) + int(cnt[:, 1].sum())
@@ -288,9 +291,9 @@ def serving_leg(args):
     r0 = srv.stats()["raysTraced"]
     t = time.perf_counter()
     ids = []
-    for j in jobs:
+    for k, j in enumerate(jobs):
         view, p = inputs(j)
-        ids.append(srv.submit_render(sids[j["scene"]], view, p))
+        ids.append(srv.submit_render(sids[j["scene"]], view, p, out=pinned[k]))
     for i in ids:
         srv.wait(i)
     t_sat = time.perf_counter() - t
@@ -308,7 +311,7 @@ def serving_leg(args):
         if delay > 0:
             time.sleep(delay)
         view, p = inputs(j)
-        ids.append(srv.submit_render(sids[j["scene"]], view, p))
+        ids.append(srv.submit_render(sids[j["scene"]], view, p, out=pinned[k]))
     lat = []
     for i in ids:
         ts, ta, td = srv.wait(i)

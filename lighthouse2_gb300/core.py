@@ -257,6 +257,11 @@ class RenderCore:
         self._check(self.lib.lh2g_read_accumulator(self.ctx, _p(out)), "read_accumulator")
         return out
 
+    def read_accumulator_into(self, out):
+        """Copies the accumulator (direct half) into a preallocated (W*H, 4) float32 array."""
+        assert out.dtype == np.float32 and out.size >= self.W * self.H * 4 and out.flags["C_CONTIGUOUS"]
+        self._check(self.lib.lh2g_read_accumulator(self.ctx, _p(out)), "read_accumulator")
+
     def framebuffer_ptr(self):
         p = C.c_void_p()
         self._check(self.lib.lh2g_get_framebuffer(self.ctx, C.byref(p)), "get_framebuffer")

@@ -10,10 +10,12 @@
  *             connect (any hit); swap the queues; copy the per-job counts of live paths to the host.
  *             A path carries its job slot (bits 8..15) and its own path length (bits 16..22) in its flag word,
  *             so paths of jobs admitted at different ticks, and at different depths, are processed together.
- *   admission a job is admitted when its paths fit in the queue capacity (path memory) and a slot is free;
- *             jobs wait in arrival order. A job whose live-path count reached zero is finalized (its per-path
- *             radiance summed per pixel, in sample order), its slot and memory released, and its image copied
- *             to the caller's host buffer by a worker thread.
+ *   admission a job is admitted when its paths fit in the queue capacity (path memory, reserved whole) and a
+ *             slot is free: the smallest pending job first, the oldest one once it has waited longer than a bound.
+ *             Its paths enter the queues in ranges, at most a tick budget of new paths per tick, so that a large
+ *             job does not stretch the ticks every small job needs. A job whose live-path count reached zero is
+ *             finalized (its per-path radiance summed per pixel, in sample order), its slot and memory released,
+ *             and its image copied to the caller's host buffer by a worker thread.
  *   ray queries run on the worker thread's own stream, concurrently with the render ticks.
  *
  * Every per-path quantity (RNG seeds, hit records, radiance and its order of accumulation) is the one the
@@ -49,7 +51,8 @@ namespace lh2g {
 namespace srv {
 
 constexpr int MAX_SLOTS = 256;         /* job slots: 8 bits of the flag word */
-constexpr int MAX_NEW = 64;            /* jobs admitted per tick */
+constexpr int MAX_NEW = 64;            /* path ranges admitted per tick */
+constexpr int MAX_SCENES = 16;         /* scene records travel as a kernel parameter */
 constexpr uint32_t SLOT_SHIFT = 8, DEPTH_SHIFT = 16;
 
 struct JobGPU {
@@ -65,12 +68,15 @@ struct ServerState {
     uint32_t shadowCount;
     uint32_t fetch[4];
     uint32_t status;
-    uint32_t newCount, newTotal;       /* jobs admitted for the next tick and their paths */
+    uint32_t newCount, newTotal;       /* path ranges admitted for the next tick and their paths */
     uint32_t newSlot[MAX_NEW];
+    uint32_t newStart[MAX_NEW];        /* first path (index within its job) of each range */
     uint32_t newPrefix[MAX_NEW + 1];
     unsigned long long rays;           /* rays traced over all ticks */
     unsigned long long ticks;
 };
+
+struct SceneTable { SceneGPU s[MAX_SCENES]; };
 
 struct Queues {
     float4* O[2];
@@ -92,7 +98,7 @@ __global__ void __launch_bounds__(256) k_srv_generate(const JobGPU* __restrict__
     for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
         uint32_t j = 0;
         while (j + 1 < n && st->newPrefix[j + 1] <= g) j++;
-        const uint32_t slot = st->newSlot[j], i = g - st->newPrefix[j];
+        const uint32_t slot = st->newSlot[j], i = st->newStart[j] + (g - st->newPrefix[j]);
         const JobGPU& J = jobs[slot];
         float3 O, D;
         primary_ray(J.F, i, O, D);
@@ -104,7 +110,7 @@ __global__ void __launch_bounds__(256) k_srv_generate(const JobGPU* __restrict__
 }
 
 /* closest hit of every ray in the current queue, each against the scene of its job */
-__global__ void __launch_bounds__(128) k_srv_extend(const SceneGPU* __restrict__ scenes, const JobGPU* __restrict__ jobs, ServerState* st,
+__global__ void __launch_bounds__(128) k_srv_extend(const __grid_constant__ SceneTable scenes, const JobGPU* __restrict__ jobs, ServerState* st,
                                                     const Queues Q) {
     const uint32_t cur = st->cur, count = st->qCount[cur] + st->newTotal;
     const uint32_t lane = threadIdx.x & 31u, firstRound = gridDim.x * blockDim.x;
@@ -120,7 +126,7 @@ __global__ void __launch_bounds__(128) k_srv_extend(const SceneGPU* __restrict__
         const uint32_t i = base + lane;
         if (i < count) {
             const float4 o4 = Q.O[cur][i], d4 = Q.D[cur][i], t4 = Q.T[cur][i];
-            const SceneGPU& S = scenes[jobs[slot_of(d4)].scene];
+            const SceneGPU& S = scenes.s[jobs[slot_of(d4)].scene];
             Traversal tr;
             tr.begin(S, xyz(o4), xyz(d4), t4.w, 1e34f);
             bool any = false;
@@ -134,8 +140,8 @@ __global__ void __launch_bounds__(128) k_srv_extend(const SceneGPU* __restrict__
 
 /* one vertex of every path in the current queue: extension rays to the other queue, connections to the shadow
  * queue (warp ballot + popc, one atomic per warp), finished paths leave their job's live count */
-__global__ void __launch_bounds__(WAVE_BLOCK) k_srv_shade(const SceneGPU* __restrict__ scenes, const JobGPU* __restrict__ jobs, ServerState* st,
-                                                         const Queues Q, int* alive) {
+__global__ void __launch_bounds__(WAVE_BLOCK) k_srv_shade(const __grid_constant__ SceneTable scenes, const JobGPU* __restrict__ jobs,
+                                                         ServerState* st, const Queues Q, int* alive) {
     const uint32_t cur = st->cur, nq = cur ^ 1u, count = st->qCount[cur] + st->newTotal;
     const uint32_t lane = threadIdx.x & 31u;
     __shared__ float potential[64 * WAVE_BLOCK];
@@ -152,7 +158,7 @@ __global__ void __launch_bounds__(WAVE_BLOCK) k_srv_shade(const SceneGPU* __rest
             WaveBuffers B;
             memset(&B, 0, sizeof(B));
             B.pathAcc = J.pathAcc;
-            shade_core(scenes[J.scene], J.F, B, depth, o4, d4, t4, hit, out, potential + threadIdx.x);
+            shade_core(scenes.s[J.scene], J.F, B, depth, o4, d4, t4, hit, out, potential + threadIdx.x);
             if (out.ext) out.eD.w = __uint_as_float(__float_as_uint(out.eD.w) + (1u << DEPTH_SHIFT));
             else atomicSub(&alive[slot], 1);
             if (out.shadow) out.sE.w = __uint_as_float(__float_as_uint(out.sE.w) | (slot << SLOT_SHIFT));
@@ -177,7 +183,7 @@ __global__ void __launch_bounds__(WAVE_BLOCK) k_srv_shade(const SceneGPU* __rest
 }
 
 /* any hit of every connection; unoccluded ones add their contribution to their path */
-__global__ void __launch_bounds__(128) k_srv_connect(const SceneGPU* __restrict__ scenes, const JobGPU* __restrict__ jobs, ServerState* st,
+__global__ void __launch_bounds__(128) k_srv_connect(const __grid_constant__ SceneTable scenes, const JobGPU* __restrict__ jobs, ServerState* st,
                                                      const Queues Q) {
     const uint32_t count = st->shadowCount;
     const uint32_t lane = threadIdx.x & 31u, firstRound = gridDim.x * blockDim.x;
@@ -195,7 +201,7 @@ __global__ void __launch_bounds__(128) k_srv_connect(const SceneGPU* __restrict_
             const float4 e = Q.shE[i], o4 = Q.shO[i], d4 = Q.shD[i];
             const uint32_t tag = __float_as_uint(e.w), slot = (tag >> SLOT_SHIFT) & 255u;
             const JobGPU& J = jobs[slot];
-            const SceneGPU& S = scenes[J.scene];
+            const SceneGPU& S = scenes.s[J.scene];
             Traversal tr;
             tr.begin(S, xyz(o4), xyz(d4), 0.0f, d4.w);
             bool occluded = false;
@@ -253,6 +259,7 @@ struct Job {
     long long n = 0;                   /* rays of a query */
     int mode = 0;
     long long paths = 0;
+    long long admittedPaths = 0;       /* paths generated so far (a job enters the queues in ranges) */
     int slot = -1;
     long long admitTick = -1;
     int state = 0;                     /* 0 pending, 1 running, 2 finishing, 3 done, 4 failed */
@@ -271,7 +278,7 @@ struct lh2g_server {
     cudaStream_t io = nullptr;         /* worker: result copies, ray queries */
     std::string err;
     std::vector<SceneGPU> scenes;
-    SceneGPU* dScenes = nullptr;
+    int graphScenes = -1;              /* scene count the tick graph was captured with */
     JobGPU* dJobs = nullptr;
     int* dAlive = nullptr;
     int* hAlive = nullptr;             /* pinned snapshot, refreshed by every tick */
@@ -279,6 +286,8 @@ struct lh2g_server {
     ServerState* hTick = nullptr;      /* pinned staging of the tick parameters, one per tick-event ring entry */
     Queues Q;
     long long capacity = 0;
+    long long tickBudget = 0;          /* new paths per tick */
+    double maxWaitS = 0.2;             /* a job waiting longer than this is admitted before smaller ones */
     cudaGraphExec_t tickExec = nullptr;
     cudaGraph_t tickGraph = nullptr;
     std::vector<cudaEvent_t> tickEv;   /* ring of tick-completion events */
@@ -288,6 +297,7 @@ struct lh2g_server {
     std::mutex mu;
     std::condition_variable cvWork, cvDone;
     std::deque<Job*> pending;
+    std::vector<Job*> partial;         /* admitted jobs with paths still to generate */
     std::map<long long, Job*> jobs;
     Job* slots[MAX_SLOTS] = {};
     long long nextId = 1;
@@ -373,32 +383,61 @@ void run_query(lh2g_server* s, Job* j) {
     finish(s, j, ok ? 3 : 4);
 }
 
-/* admits pending render jobs in arrival order while they fit; ray queries go to the worker */
-void admit(lh2g_server* s, std::vector<Job*>& admitted) {
+/* A path range of a job entering the queues at the next tick. */
+struct Range { Job* job; long long start, count; bool first; };
+
+/* Admission for the next tick. Ray queries go to the worker. Render jobs are admitted when their paths fit in the
+ * capacity (reserved whole) and a slot is free: the smallest pending job first, unless one has waited longer than
+ * maxWaitS (then the oldest); a job that does not fit stops admission, so no job waits forever. The paths of
+ * admitted jobs enter the queues in ranges, at most tickBudget new paths per tick, so that one large job does not
+ * stretch the ticks that every small job needs. */
+void admit(lh2g_server* s, std::vector<Range>& ranges) {
     std::lock_guard<std::mutex> g(s->mu);
-    while (!s->pending.empty() && (int)admitted.size() < MAX_NEW) {
-        Job* j = s->pending.front();
+    long long budget = s->tickBudget;
+    auto take = [&](Job* j, bool first) {
+        const long long n = std::min(j->paths - j->admittedPaths, std::max(budget, 1ll));
+        ranges.push_back({j, j->admittedPaths, n, first});
+        j->admittedPaths += n;
+        budget -= n;
+    };
+    /* ranges of jobs admitted earlier, in admission order */
+    for (size_t k = 0; k < s->partial.size() && budget > 0 && (int)ranges.size() < MAX_NEW;) {
+        Job* j = s->partial[k];
+        take(j, false);
+        if (j->admittedPaths == j->paths) s->partial.erase(s->partial.begin() + (long)k);
+        else k++;
+    }
+    const double now = now_s();
+    while (!s->pending.empty() && budget > 0 && (int)ranges.size() < MAX_NEW) {
+        size_t pick = 0;
+        if (now - s->pending.front()->tSubmit <= s->maxWaitS)
+            for (size_t k = 1; k < s->pending.size(); k++)
+                if (s->pending[k]->paths < s->pending[pick]->paths) pick = k;
+        Job* j = s->pending[pick];
         if (j->kind == 1) {
-            s->pending.pop_front();
-            j->state = 1, j->tAdmit = now_s();
+            s->pending.erase(s->pending.begin() + (long)pick);
+            j->state = 1, j->tAdmit = now;
             post(s, [s, j] { run_query(s, j); });
             continue;
         }
-        if (s->pathsInFlight + j->paths > s->capacity) break;   /* wait for path memory: arrival order is kept */
+        if (j->scene >= s->graphScenes) break;                  /* its scene is not in the tick graph yet */
+        if (s->pathsInFlight + j->paths > s->capacity) break;   /* wait for path memory */
         int slot = -1;
         for (int k = 0; k < MAX_SLOTS; k++)
             if (!s->slots[k]) { slot = k; break; }
         if (slot < 0) break;
-        s->pending.pop_front();
+        s->pending.erase(s->pending.begin() + (long)pick);
         j->slot = slot;
         s->slots[slot] = j;
         s->pathsInFlight += j->paths;
-        j->state = 1, j->tAdmit = now_s();
-        admitted.push_back(j);
+        j->state = 1, j->tAdmit = now;
+        take(j, true);
+        if (j->admittedPaths < j->paths) s->partial.push_back(j);
     }
 }
 
 void tick_loop_body(lh2g_server* s);
+int build_tick_graph(lh2g_server* s);
 
 void tick_loop(lh2g_server* s) {
     tick_loop_body(s);
@@ -411,8 +450,21 @@ void tick_loop(lh2g_server* s) {
 void tick_loop_body(lh2g_server* s) {
     cudaSetDevice(s->device);
     const int ring = (int)s->tickEv.size();
-    std::vector<Job*> admitted;
+    std::vector<Range> admitted;
     for (;;) {
+        {
+            /* scenes added since the tick graph was captured: capture it again (the scene table is a kernel
+             * parameter) */
+            int n;
+            {
+                std::lock_guard<std::mutex> g(s->mu);
+                n = (int)s->scenes.size();
+            }
+            if (n != s->graphScenes && build_tick_graph(s) != LH2G_OK) {
+                std::lock_guard<std::mutex> g(s->mu);
+                s->err = "tick graph capture failed";
+            }
+        }
         admitted.clear();
         admit(s, admitted);
         bool active = false;
@@ -433,7 +485,14 @@ void tick_loop_body(lh2g_server* s) {
         ServerState& tp = s->hTick[s->ticksLaunched % ring];
         tp.newCount = (uint32_t)admitted.size();
         for (size_t k = 0; k < admitted.size(); k++) {
-            Job* j = admitted[k];
+            Job* j = admitted[k].job;
+            if (!admitted[k].first) {   /* a further range of a job already on the device */
+                tp.newSlot[k] = (uint32_t)j->slot;
+                tp.newStart[k] = (uint32_t)admitted[k].start;
+                tp.newPrefix[k] = total;
+                total += (uint32_t)admitted[k].count;
+                continue;
+            }
             JobGPU& G = j->gpu;
             G.F = frame_of(&j->view, &j->params);
             G.scene = j->scene;
@@ -446,6 +505,7 @@ void tick_loop_body(lh2g_server* s) {
                     std::lock_guard<std::mutex> g(s->mu);
                     s->slots[j->slot] = nullptr;
                     s->pathsInFlight -= j->paths;
+                    s->partial.erase(std::remove(s->partial.begin(), s->partial.end(), j), s->partial.end());
                 }
                 finish(s, j, 4);
                 admitted.erase(admitted.begin() + (long)k--);
@@ -455,8 +515,9 @@ void tick_loop_body(lh2g_server* s) {
             const int live = (int)j->paths;
             cudaMemcpyAsync(s->dAlive + j->slot, &live, sizeof(int), cudaMemcpyHostToDevice, s->st);
             tp.newSlot[k] = (uint32_t)j->slot;
+            tp.newStart[k] = (uint32_t)admitted[k].start;
             tp.newPrefix[k] = total;
-            total += (uint32_t)j->paths;
+            total += (uint32_t)admitted[k].count;
             j->admitTick = s->ticksLaunched;
         }
         tp.newPrefix[admitted.size()] = total;
@@ -479,7 +540,7 @@ void tick_loop_body(lh2g_server* s) {
             std::lock_guard<std::mutex> g(s->mu);
             for (int k = 0; k < MAX_SLOTS; k++) {
                 Job* j = s->slots[k];
-                if (j && j->admitTick < s->ticksDone && s->hAlive[k] <= 0) done.push_back(j);
+                if (j && j->admitTick < s->ticksDone && j->admittedPaths == j->paths && s->hAlive[k] <= 0) done.push_back(j);
             }
         }
         for (Job* j : done) {
@@ -512,15 +573,26 @@ void tick_loop_body(lh2g_server* s) {
 }
 
 int build_tick_graph(lh2g_server* s) {
+    SceneTable T;
+    memset(&T, 0, sizeof(T));
+    int n;
+    {
+        std::lock_guard<std::mutex> g(s->mu);
+        n = (int)s->scenes.size();
+        for (int k = 0; k < n; k++) T.s[k] = s->scenes[k];
+    }
+    if (s->tickExec) cudaGraphExecDestroy(s->tickExec), s->tickExec = nullptr;
+    if (s->tickGraph) cudaGraphDestroy(s->tickGraph), s->tickGraph = nullptr;
     if (cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return LH2G_ERR_CUDA;
     k_srv_generate<<<s->blocksGen, 256, 0, s->st>>>(s->dJobs, s->dState, s->Q);
-    k_srv_extend<<<s->blocksExtend, 128, 0, s->st>>>(s->dScenes, s->dJobs, s->dState, s->Q);
-    k_srv_shade<<<s->blocksShade, WAVE_BLOCK, 0, s->st>>>(s->dScenes, s->dJobs, s->dState, s->Q, s->dAlive);
-    k_srv_connect<<<s->blocksConnect, 128, 0, s->st>>>(s->dScenes, s->dJobs, s->dState, s->Q);
+    k_srv_extend<<<s->blocksExtend, 128, 0, s->st>>>(T, s->dJobs, s->dState, s->Q);
+    k_srv_shade<<<s->blocksShade, WAVE_BLOCK, 0, s->st>>>(T, s->dJobs, s->dState, s->Q, s->dAlive);
+    k_srv_connect<<<s->blocksConnect, 128, 0, s->st>>>(T, s->dJobs, s->dState, s->Q);
     k_srv_end<<<1, 1, 0, s->st>>>(s->dState);
     cudaMemcpyAsync(s->hAlive, s->dAlive, sizeof(int) * MAX_SLOTS, cudaMemcpyDeviceToHost, s->st);
     if (cudaStreamEndCapture(s->st, &s->tickGraph) != cudaSuccess) return LH2G_ERR_CUDA;
     if (cudaGraphInstantiate(&s->tickExec, s->tickGraph, 0) != cudaSuccess) return LH2G_ERR_CUDA;
+    s->graphScenes = n;
     return LH2G_OK;
 }
 
@@ -544,6 +616,7 @@ int lh2g_server_create(int device, long long pathCapacity, lh2g_server** out) {
     lh2g_server* s = new lh2g_server();
     s->device = device;
     s->capacity = pathCapacity;
+    s->tickBudget = std::max(1ll << 20, std::min(pathCapacity, 1ll << 22));
     memset(&s->Q, 0, sizeof(s->Q));
     bool ok = cudaSetDevice(device) == cudaSuccess;
     ok = ok && cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) == cudaSuccess;
@@ -557,7 +630,6 @@ int lh2g_server_create(int device, long long pathCapacity, lh2g_server** out) {
     ok = ok && cudaMalloc((void**)&s->dJobs, sizeof(JobGPU) * MAX_SLOTS) == cudaSuccess;
     ok = ok && cudaMalloc((void**)&s->dAlive, sizeof(int) * MAX_SLOTS) == cudaSuccess;
     ok = ok && cudaMalloc((void**)&s->dState, sizeof(ServerState)) == cudaSuccess;
-    ok = ok && cudaMalloc((void**)&s->dScenes, sizeof(SceneGPU) * 64) == cudaSuccess;
     ok = ok && cudaMallocHost((void**)&s->hAlive, sizeof(int) * MAX_SLOTS) == cudaSuccess;
     ok = ok && cudaMallocHost((void**)&s->hTick, sizeof(ServerState) * 4) == cudaSuccess;
     if (ok) {
@@ -580,7 +652,6 @@ int lh2g_server_create(int device, long long pathCapacity, lh2g_server** out) {
         s->tickEv.resize(4);
         for (auto& e : s->tickEv) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
         ok = ok && cudaDeviceSynchronize() == cudaSuccess;
-        ok = ok && build_tick_graph(s) == LH2G_OK;
     }
     if (!ok) {
         lh2g_server_destroy(s);
@@ -616,7 +687,7 @@ int lh2g_server_destroy(lh2g_server* s) {
     for (auto& e : s->tickEv) if (e) cudaEventDestroy(e);
     for (int k = 0; k < 2; k++) cudaFree(s->Q.O[k]), cudaFree(s->Q.D[k]), cudaFree(s->Q.T[k]);
     cudaFree(s->Q.hits), cudaFree(s->Q.shO), cudaFree(s->Q.shD), cudaFree(s->Q.shE);
-    cudaFree(s->dJobs), cudaFree(s->dAlive), cudaFree(s->dState), cudaFree(s->dScenes);
+    cudaFree(s->dJobs), cudaFree(s->dAlive), cudaFree(s->dState);
     if (s->hAlive) cudaFreeHost(s->hAlive);
     if (s->hTick) cudaFreeHost(s->hTick);
     for (auto& kv : s->jobs) delete kv.second;
@@ -635,16 +706,14 @@ int lh2g_server_add_scene(lh2g_server* s, lh2g_context* ctx, int* sceneId) {
     const int r = context_scene(ctx, &S, &dev, blocks, &tail);
     if (r != LH2G_OK) return sfail(s, r, "add_scene: the context has no finalized scene");
     if (dev != s->device) return sfail(s, LH2G_ERR_INVALID, "add_scene: the context is on another device");
-    std::lock_guard<std::mutex> g(s->mu);
-    if (s->scenes.size() >= 64) { s->err = "add_scene: at most 64 scenes"; return LH2G_ERR_OVERFLOW; }
-    /* a new table entry that no job refers to yet: safe to write while ticks run */
-    cudaSetDevice(s->device);
-    if (cudaMemcpy(s->dScenes + s->scenes.size(), &S, sizeof(SceneGPU), cudaMemcpyHostToDevice) != cudaSuccess) {
-        s->err = "add_scene: copy failed";
-        return LH2G_ERR_CUDA;
+    {
+        std::lock_guard<std::mutex> g(s->mu);
+        if ((int)s->scenes.size() >= MAX_SCENES) { s->err = "add_scene: at most 16 scenes"; return LH2G_ERR_OVERFLOW; }
+        *sceneId = (int)s->scenes.size();
+        s->scenes.push_back(S);
     }
-    *sceneId = (int)s->scenes.size();
-    s->scenes.push_back(S);
+    /* the tick loop captures its graph again with the new table before it admits a job of this scene */
+    s->cvWork.notify_all();
     return LH2G_OK;
 }
 

@@ -69,11 +69,15 @@ class RenderServer:
         self._scenes.append(core)
         return sid.value
 
-    def submit_render(self, scene_id: int, view, params) -> int:
+    def submit_render(self, scene_id: int, view, params, out=None) -> int:
         """Queues a render job; returns its id. The image (width*height x 4 float32: per-pixel sums over the job's
-        samples) is available from result(id) once wait(id) returned."""
+        samples) is available from result(id) once wait(id) returned. `out` may supply the (width*height, 4)
+        float32 host array to fill (pinned memory makes the copy asynchronous)."""
         W, H = int(params["width"]), int(params["height"])
-        out = np.zeros((W * H, 4), np.float32)
+        if out is None:
+            out = np.zeros((W * H, 4), np.float32)
+        elif out.dtype != np.float32 or out.shape != (W * H, 4) or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a C-contiguous (width*height, 4) float32 array")
         view, params = np.ascontiguousarray(view), np.ascontiguousarray(params)
         jid = C.c_longlong(0)
         self._check(self.lib.lh2g_server_submit_render(self.srv, scene_id, view.ctypes.data_as(C.c_void_p), params.ctypes.data_as(C.c_void_p),
