@@ -170,6 +170,39 @@ LH2G_API int lh2g_server_wait(lh2g_server* server, long long jobId, int timeoutM
 LH2G_API int lh2g_server_release(lh2g_server* server, long long jobId);   /* forgets a finished job */
 LH2G_API int lh2g_server_get_stats(lh2g_server* server, lh2g_server_stats* out);
 
+/* ---- radiance cache (no counterpart in the reference): a hash-grid + one-blob encoded 4 x 64 ReLU MLP with
+ * bf16 weights, trained online with Adam on the relative L2 loss, inference and training on the tensor cores.
+ * A query is 16 floats: position xyz, roughness, outgoing direction xyz, 0, normal xyz, 0, albedo rgb, 0; a
+ * prediction and a training target are 4 floats (rgb, 0). Parameters: LH2G_NRC_MLP_PARAMS fp32 weights (row-major
+ * [out][in] per layer: 64x64 four times, then 3x64) and LH2G_NRC_GRID_PARAMS fp32 grid features (12 levels x 2^19
+ * entries x 2). */
+#define LH2G_NRC_MLP_PARAMS 16576
+#define LH2G_NRC_GRID_PARAMS 12582912
+typedef struct lh2g_nrc lh2g_nrc;
+typedef struct lh2g_nrc_config {
+    float sceneMin[3], sceneMax[3];   /* box the hash grid spans */
+    float learningRate;               /* Adam step (1e-3 when 0) */
+    uint32_t seed;                    /* initial parameters */
+} lh2g_nrc_config;
+LH2G_API int lh2g_nrc_create(int device, const lh2g_nrc_config* config, lh2g_nrc** out);
+LH2G_API int lh2g_nrc_destroy(lh2g_nrc* cache);
+LH2G_API const char* lh2g_nrc_last_error(lh2g_nrc* cache);
+/* encoding geometry (for CPU checkers): per-level resolution, dense flag, and bmin xyz + 1 / extent xyz */
+LH2G_API int lh2g_nrc_get_spec(lh2g_nrc* cache, int* res12, int* dense12, float* bminInv6);
+LH2G_API int lh2g_nrc_set_params(lh2g_nrc* cache, const float* mlp, const float* grid);   /* either may be NULL; resets Adam */
+LH2G_API int lh2g_nrc_get_params(lh2g_nrc* cache, float* mlp, float* grid);
+/* the accumulated gradients (a train call with update = 0 leaves them; update = 1 applies and clears them) */
+LH2G_API int lh2g_nrc_get_grads(lh2g_nrc* cache, float* mlp, float* grid);
+/* device buffers, asynchronous on stream (NULL: the cache's stream) */
+LH2G_API int lh2g_nrc_infer(lh2g_nrc* cache, const float* queries, long long n, float* out, void* stream);
+LH2G_API int lh2g_nrc_train(lh2g_nrc* cache, const float* queries, const float* targets, long long n, int update, float* lossOut,
+                            void* stream);
+/* one Adam step with the gradients accumulated by train calls with update = 0 (then cleared) */
+LH2G_API int lh2g_nrc_apply_update(lh2g_nrc* cache, void* stream);
+/* host buffers, synchronous */
+LH2G_API int lh2g_nrc_infer_host(lh2g_nrc* cache, const float* queries, long long n, float* out);
+LH2G_API int lh2g_nrc_train_host(lh2g_nrc* cache, const float* queries, const float* targets, long long n, int update, float* lossOut);
+
 #ifdef __cplusplus
 }
 #endif

@@ -46,7 +46,9 @@ C_API = ["lh2g_create", "lh2g_destroy", "lh2g_last_error", "lh2g_set_geometry", 
          "lh2g_get_stream", "lh2g_enable_launch_timing", "lh2g_get_launch_times", "lh2g_get_traversal_stats",
          "lh2g_render_noalloc", "lh2g_filter", "lh2g_read_filter_buffer", "lh2g_get_last_filter_frame",
          "lh2g_server_create", "lh2g_server_destroy", "lh2g_server_last_error", "lh2g_server_add_scene", "lh2g_server_submit_render",
-         "lh2g_server_submit_trace", "lh2g_server_wait", "lh2g_server_release", "lh2g_server_get_stats"]
+         "lh2g_server_submit_trace", "lh2g_server_wait", "lh2g_server_release", "lh2g_server_get_stats",
+         "lh2g_nrc_create", "lh2g_nrc_destroy", "lh2g_nrc_last_error", "lh2g_nrc_get_spec", "lh2g_nrc_set_params", "lh2g_nrc_get_params",
+         "lh2g_nrc_get_grads", "lh2g_nrc_infer", "lh2g_nrc_train", "lh2g_nrc_apply_update", "lh2g_nrc_infer_host", "lh2g_nrc_train_host"]
 
 _lib = None
 

@@ -153,6 +153,61 @@ class Oracle:
         return out
 
 
+class NrcSpec(C.Structure):
+    _fields_ = [("res", C.c_int * 12), ("dense", C.c_int * 12), ("bmin", C.c_float * 3), ("inv", C.c_float * 3)]
+
+
+class NrcOracle:
+    """The radiance cache's encoding, outputs and gradients restated on the CPU (oracle/lh2o.cpp)."""
+
+    def __init__(self, res, dense, bmin, inv):
+        if not os.path.exists(LIB):
+            build_oracle()
+        self.lib = C.CDLL(LIB)
+        L = self.lib
+        L.lh2o_nrc_encode.argtypes = [C.c_void_p] * 4
+        L.lh2o_nrc_forward.argtypes = [C.c_void_p] * 4 + [C.c_longlong, C.c_void_p, C.c_int, C.c_int]
+        L.lh2o_nrc_gradients.argtypes = [C.c_void_p] * 5 + [C.c_longlong, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.lh2o_nrc_adam.argtypes = [C.c_void_p] * 4 + [C.c_longlong, C.c_float, C.c_longlong]
+        L.lh2o_nrc_forward64.argtypes = [C.c_void_p] * 4 + [C.c_longlong, C.c_void_p]
+        self.spec = NrcSpec((C.c_int * 12)(*res), (C.c_int * 12)(*dense), (C.c_float * 3)(*bmin), (C.c_float * 3)(*inv))
+
+    def encode(self, grid, query):
+        e = np.zeros(64, np.float32)
+        q = np.ascontiguousarray(query, np.float32)
+        self.lib.lh2o_nrc_encode(C.byref(self.spec), _p(np.ascontiguousarray(grid, np.float32)), _p(q), _p(e))
+        return e
+
+    def forward(self, grid, mlp, queries, emulate=True):
+        q = np.ascontiguousarray(queries, np.float32).reshape(-1, 16)
+        out = np.zeros((len(q), 4), np.float32)
+        assert self.lib.lh2o_nrc_forward(C.byref(self.spec), _p(np.ascontiguousarray(grid, np.float32)), _p(np.ascontiguousarray(mlp, np.float32)),
+                                         _p(q), len(q), _p(out), int(emulate), 0) == 0
+        return out
+
+    def forward64(self, grid, mlp, queries):
+        q = np.ascontiguousarray(queries, np.float32).reshape(-1, 16)
+        out = np.zeros((len(q), 3), np.float64)
+        assert self.lib.lh2o_nrc_forward64(C.byref(self.spec), _p(np.ascontiguousarray(grid, np.float32)), _p(np.ascontiguousarray(mlp, np.float32)),
+                                           _p(q), len(q), _p(out)) == 0
+        return out
+
+    def gradients(self, grid, mlp, queries, targets, emulate=True, with_grid=True):
+        q = np.ascontiguousarray(queries, np.float32).reshape(-1, 16)
+        t = np.ascontiguousarray(targets, np.float32).reshape(-1, 4)
+        gm = np.zeros(len(mlp), np.float64)
+        gg = np.zeros(len(grid), np.float64) if with_grid else None
+        loss = C.c_double(0)
+        assert self.lib.lh2o_nrc_gradients(C.byref(self.spec), _p(np.ascontiguousarray(grid, np.float32)), _p(np.ascontiguousarray(mlp, np.float32)),
+                                           _p(q), _p(t), len(q), int(emulate), _p(gm), _p(gg), C.byref(loss)) == 0
+        return gm, gg, loss.value
+
+    def adam(self, p, m, v, g, lr, step):
+        for a in (p, m, v, g):
+            assert a.dtype == np.float32 and a.flags["C_CONTIGUOUS"]
+        self.lib.lh2o_nrc_adam(_p(p), _p(m), _p(v), _p(g), len(p), lr, step)
+
+
 class _Features(C.Structure):
     _fields_ = [("features", C.c_void_p), ("worldPos", C.c_void_p), ("deltaDepth", C.c_void_p)]
 

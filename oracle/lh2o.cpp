@@ -1547,6 +1547,88 @@ struct Svgf {
     }
 };
 
+/* ------------------------------------------------------------------------------------------------------
+ * radiance cache (no reference counterpart): the encoding, the network and its gradients with the rounding
+ * points of the GPU kernels - fp16 grid features, bf16 weights, activations and loss gradients - and sums in
+ * double; and one Adam step
+ * ---------------------------------------------------------------------------------------------------- */
+constexpr int NRC_IN = 64, NRC_HID = 64, NRC_LEVELS = 12, NRC_T = 1 << 19;
+inline float bf16r(float x) {   /* round to bfloat16, nearest even */
+    uint b = fbits(x);
+    if ((b & 0x7f800000u) == 0x7f800000u) return x;
+    b = (b + 0x7fffu + ((b >> 16) & 1u)) & 0xffff0000u;
+    return bitsf(b);
+}
+inline float f16r(float x) { return half2float(float2half(x)); }
+inline void one_blob4(float x, float* out) {
+    for (int i = 0; i < 4; i++) out[i] = fmaxr(0.0f, 1.0f - fabsf(x * 4.0f - ((float)i + 0.5f)));
+}
+inline void sph01(f3 d, float& th, float& ph) {
+    th = lm_acosf(fminr(fmaxr(d.z, -1.0f), 1.0f)) * INVPI;
+    ph = lm_atan2f(d.y, d.x) * INV2PI + 0.5f;
+}
+struct NrcCell { uint i, j, k; float fx, fy, fz; };
+inline f3 nrc_unit(const lh2o_nrc_spec& S, const float* q) {
+    float u[3];
+    for (int a = 0; a < 3; a++) u[a] = fminr(fmaxr((q[a] - S.bmin[a]) * S.inv[a], 0.0f), 1.0f);
+    return mk3(u[0], u[1], u[2]);
+}
+inline NrcCell nrc_cell(const lh2o_nrc_spec& S, int l, f3 p) {
+    const float r = (float)S.res[l];
+    const float x = p.x * r, y = p.y * r, z = p.z * r;
+    NrcCell c;
+    c.i = (uint)imin(f2i(floorf(x)), S.res[l] - 1), c.j = (uint)imin(f2i(floorf(y)), S.res[l] - 1), c.k = (uint)imin(f2i(floorf(z)), S.res[l] - 1);
+    c.fx = x - (float)c.i, c.fy = y - (float)c.j, c.fz = z - (float)c.k;
+    return c;
+}
+inline uint nrc_index(const lh2o_nrc_spec& S, int l, uint x, uint y, uint z) {
+    if (S.dense[l]) {
+        const uint r1 = (uint)S.res[l] + 1u;
+        return x + r1 * (y + r1 * z);
+    }
+    return ((x * 1u) ^ (y * 2654435761u) ^ (z * 805459861u)) & (uint)(NRC_T - 1);
+}
+inline float nrc_weight(const NrcCell& c, int corner) {
+    return ((corner & 1) ? c.fx : 1.0f - c.fx) * ((corner & 2) ? c.fy : 1.0f - c.fy) * ((corner & 4) ? c.fz : 1.0f - c.fz);
+}
+void nrc_encode(const lh2o_nrc_spec& S, const float* grid, const float* q, float* e, bool emulate = true) {
+    const f3 p = nrc_unit(S, q);
+    for (int l = 0; l < NRC_LEVELS; l++) {
+        const NrcCell c = nrc_cell(S, l, p);
+        float f0 = 0.0f, f1 = 0.0f;
+        for (int corner = 0; corner < 8; corner++) {
+            const uint idx = nrc_index(S, l, c.i + (corner & 1), c.j + ((corner >> 1) & 1), c.k + (corner >> 2));
+            const size_t at = ((size_t)l * NRC_T + idx) * 2;
+            const float w = nrc_weight(c, corner);
+            const float g0 = emulate ? f16r(grid[at]) : grid[at], g1 = emulate ? f16r(grid[at + 1]) : grid[at + 1];
+            f0 = f0 + w * g0, f1 = f1 + w * g1;
+        }
+        e[2 * l] = f0, e[2 * l + 1] = f1;
+    }
+    float th, ph;
+    sph01(mk3(q[4], q[5], q[6]), th, ph);
+    one_blob4(th, e + 24), one_blob4(ph, e + 28);
+    sph01(mk3(q[8], q[9], q[10]), th, ph);
+    one_blob4(th, e + 32), one_blob4(ph, e + 36);
+    one_blob4(fminr(fmaxr(q[3], 0.0f), 1.0f), e + 40);
+    e[44] = q[12], e[45] = q[13], e[46] = q[14], e[47] = 1.0f;
+    for (int i = 48; i < NRC_IN; i++) e[i] = 0.0f;
+}
+/* forward of one sample: act[0..4] (bf16 values when emulating), y[3] */
+void nrc_forward1(const float* mlp, const float* e, float act[5][64], double* y, bool emulate) {
+    for (int k = 0; k < NRC_IN; k++) act[0][k] = emulate ? bf16r(e[k]) : e[k];
+    for (int j = 0; j < 5; j++) {
+        const int rows = j < 4 ? NRC_HID : 3;
+        const float* W = mlp + (size_t)j * NRC_HID * NRC_IN;
+        for (int n = 0; n < rows; n++) {
+            double z = 0.0;
+            for (int k = 0; k < NRC_IN; k++) z += (double)act[j][k] * (double)(emulate ? bf16r(W[n * NRC_IN + k]) : W[n * NRC_IN + k]);
+            if (j < 4) act[j + 1][n] = emulate ? bf16r(fmaxr((float)z, 0.0f)) : (float)std::max(z, 0.0);
+            else y[n] = emulate ? (double)(float)z : z;
+        }
+    }
+}
+
 }  // namespace
 
 /* ==========================================================================================================
@@ -1786,6 +1868,100 @@ int lh2o_svgf_frame(lh2o_svgf* f, const float* accum, const lh2g_filter_params* 
     std::swap(f->prevWorldPos, f->worldPos);
     std::swap(f->moments, f->prevMoments);
     return 0;
+}
+
+void lh2o_nrc_encode(const lh2o_nrc_spec* S, const float* grid, const float* q, float* e64) { nrc_encode(*S, grid, q, e64); }
+
+int lh2o_nrc_forward(const lh2o_nrc_spec* S, const float* grid, const float* mlp, const float* queries, long long n, float* out4, int emulate,
+                     int nthreads) {
+    if (!S || !grid || !mlp || !queries || !out4 || n < 0) return 1;
+    parallel_for(n, nthreads, 256, [&](long long b, long long e) {
+        float enc[64], act[5][64];
+        double y[3];
+        for (long long i = b; i < e; i++) {
+            nrc_encode(*S, grid, queries + 16 * i, enc, emulate != 0);
+            nrc_forward1(mlp, enc, act, y, emulate != 0);
+            out4[4 * i] = (float)y[0], out4[4 * i + 1] = (float)y[1], out4[4 * i + 2] = (float)y[2], out4[4 * i + 3] = 0.0f;
+        }
+    });
+    return 0;
+}
+
+int lh2o_nrc_forward64(const lh2o_nrc_spec* S, const float* grid, const float* mlp, const float* queries, long long n, double* out3) {
+    if (!S || !grid || !mlp || !queries || !out3 || n < 0) return 1;
+    float enc[64], act[5][64];
+    for (long long i = 0; i < n; i++) {
+        nrc_encode(*S, grid, queries + 16 * i, enc, false);
+        nrc_forward1(mlp, enc, act, out3 + 3 * i, false);
+    }
+    return 0;
+}
+
+int lh2o_nrc_gradients(const lh2o_nrc_spec* S, const float* grid, const float* mlp, const float* queries, const float* targets, long long n,
+                       int emulate, double* gMlp, double* gGrid, double* loss) {
+    if (!S || !grid || !mlp || !queries || !targets || !gMlp || n <= 0) return 1;
+    const double inv = 1.0 / (3.0 * (double)n);
+    double L = 0.0;
+    float enc[64], act[5][64];
+    double y[3];
+    for (long long i = 0; i < n; i++) {
+        const float* q = queries + 16 * i;
+        nrc_encode(*S, grid, q, enc, emulate != 0);
+        nrc_forward1(mlp, enc, act, y, emulate != 0);
+        /* relative L2: (y - t)^2 / (y^2 + 0.01), y constant in the denominator */
+        double delta[64] = {0};
+        for (int c = 0; c < 3; c++) {
+            const float yf = (float)y[c];
+            const double den = emulate ? (double)(yf * yf + 0.01f) : y[c] * y[c] + 0.01;
+            const double e = y[c] - (double)targets[4 * i + c];
+            L += e * e / den * inv;
+            const double d = 2.0 * e / den * inv;
+            delta[c] = emulate ? (double)bf16r((float)d) : d;
+        }
+        for (int j = 4; j >= 0; j--) {
+            const int rows = j < 4 ? NRC_HID : 3;
+            const float* W = mlp + (size_t)j * NRC_HID * NRC_IN;
+            double* gW = gMlp + (size_t)j * NRC_HID * NRC_IN;
+            for (int nn = 0; nn < rows; nn++)
+                for (int k = 0; k < NRC_IN; k++) gW[nn * NRC_IN + k] += delta[nn] * (double)act[j][k];
+            double g[64];
+            for (int k = 0; k < NRC_IN; k++) {
+                double sum = 0.0;
+                for (int nn = 0; nn < rows; nn++) sum += delta[nn] * (double)(emulate ? bf16r(W[nn * NRC_IN + k]) : W[nn * NRC_IN + k]);
+                g[k] = sum;
+            }
+            if (j > 0) {
+                for (int k = 0; k < NRC_IN; k++) {
+                    const double m = act[j][k] > 0.0f ? g[k] : 0.0;
+                    delta[k] = emulate ? (double)bf16r((float)m) : m;
+                }
+            } else if (gGrid) {
+                const f3 p = nrc_unit(*S, q);
+                for (int l = 0; l < NRC_LEVELS; l++) {
+                    const NrcCell c = nrc_cell(*S, l, p);
+                    for (int corner = 0; corner < 8; corner++) {
+                        const uint idx = nrc_index(*S, l, c.i + (corner & 1), c.j + ((corner >> 1) & 1), c.k + (corner >> 2));
+                        const double w = nrc_weight(c, corner);
+                        gGrid[((size_t)l * NRC_T + idx) * 2] += w * g[2 * l];
+                        gGrid[((size_t)l * NRC_T + idx) * 2 + 1] += w * g[2 * l + 1];
+                    }
+                }
+            }
+        }
+    }
+    if (loss) *loss = L;
+    return 0;
+}
+
+void lh2o_nrc_adam(float* p, float* m, float* v, const float* g, long long n, float lr, long long step) {
+    const float b1 = 0.9f, b2 = 0.99f, eps = 1e-15f;
+    const float c1 = (float)(1.0 / (1.0 - std::pow(0.9, (double)step))), c2 = (float)(1.0 / (1.0 - std::pow(0.99, (double)step)));
+    for (long long i = 0; i < n; i++) {
+        const float mi = b1 * m[i] + (1.0f - b1) * g[i];
+        const float vi = b2 * v[i] + (1.0f - b2) * (g[i] * g[i]);
+        p[i] = p[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+        m[i] = mi, v[i] = vi;
+    }
 }
 
 /* pure functions for the pinning tests */

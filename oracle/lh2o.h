@@ -93,6 +93,20 @@ typedef struct lh2o_svgf {
  * (RenderCore_Optix7Filter/rendercore.cpp:904-935). accum: 2*W*H float4 of the frame. */
 int lh2o_svgf_frame(lh2o_svgf* f, const float* accum, const lh2g_filter_params* fp, int nthreads);
 
+/* Radiance cache (no reference counterpart): the encoding, the network's outputs and the gradients of the mean
+ * relative L2 loss, with the GPU kernels' rounding points when emulate != 0 (fp16 grid features, bf16 weights,
+ * activations and loss gradients; sums in double), and one Adam step (beta1 0.9, beta2 0.99, eps 1e-15). Grid
+ * and weight layouts are those of lh2g_nrc_set_params; gMlp / gGrid are added to (double, same layouts). */
+typedef struct lh2o_nrc_spec { int res[12]; int dense[12]; float bmin[3], inv[3]; } lh2o_nrc_spec;
+void lh2o_nrc_encode(const lh2o_nrc_spec* spec, const float* grid, const float* query16, float* e64);
+int lh2o_nrc_forward(const lh2o_nrc_spec* spec, const float* grid, const float* mlp, const float* queries, long long n, float* out4,
+                     int emulate, int nthreads);
+/* outputs in double, without the GPU's rounding (finite-difference checks) */
+int lh2o_nrc_forward64(const lh2o_nrc_spec* spec, const float* grid, const float* mlp, const float* queries, long long n, double* out3);
+int lh2o_nrc_gradients(const lh2o_nrc_spec* spec, const float* grid, const float* mlp, const float* queries, const float* targets,
+                       long long n, int emulate, double* gMlp, double* gGrid, double* loss);
+void lh2o_nrc_adam(float* p, float* m, float* v, const float* g, long long n, float lr, long long step);
+
 /* Small pure functions exported for the pinning tests against the reference's own headers. */
 uint32_t lh2o_wanghash(uint32_t s);
 float lh2o_random_float(uint32_t* seed);
