@@ -199,6 +199,13 @@ LH2G_API int lh2g_nrc_train(lh2g_nrc* cache, const float* queries, const float* 
                             void* stream);
 /* one Adam step with the gradients accumulated by train calls with update = 0 (then cleared) */
 LH2G_API int lh2g_nrc_apply_update(lh2g_nrc* cache, void* stream);
+/* One frame with the radiance cache (like lh2g_render_ex with accumulate): paths reaching their second vertex
+ * through a diffuse bounce end there and add throughput x cache(query); one in sixteen of them trace on and
+ * their radiance from that vertex on, divided by the throughput into it, trains the cache after the frame
+ * (train != 0, at most 65536 samples, one Adam step). The plain estimator is unchanged everywhere else. */
+typedef struct lh2g_nrc_frame_stats { uint32_t queries, trainSamples; float loss; } lh2g_nrc_frame_stats;
+LH2G_API int lh2g_render_nrc(lh2g_context* ctx, lh2g_nrc* cache, const lh2g_view* view, const lh2g_render_params* params, int accumulate,
+                             int train, lh2g_nrc_frame_stats* stats);
 /* host buffers, synchronous */
 LH2G_API int lh2g_nrc_infer_host(lh2g_nrc* cache, const float* queries, long long n, float* out);
 LH2G_API int lh2g_nrc_train_host(lh2g_nrc* cache, const float* queries, const float* targets, long long n, int update, float* lossOut);

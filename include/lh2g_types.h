@@ -140,6 +140,9 @@ typedef struct lh2g_render_params {
  * indirect half (accumulator[W*H, 2*W*H)) at the first diffuse bounce, and a per-frame shading seed
  * (rendercore.cpp:834: RandomUInt(camRNGseed) + pathLength * 91771). */
 #define LH2G_RP_FILTER     4
+/* Radiance-cache frame (lh2g_render_nrc): a path that reaches its second vertex through a diffuse bounce records
+ * a cache query there; 15 of 16 such paths end and receive throughput x cache, the others trace on and train it. */
+#define LH2G_RP_NRC        8
 
 /* One SVGF pass over the accumulator of a LH2G_RP_FILTER frame (lib/RenderCore_Optix7Filter/rendercore.cpp:
  * 897-935 with the kernels of lib/CUDA/shared_kernel_code/finalize_shared.h:169-600). */

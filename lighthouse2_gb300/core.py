@@ -48,7 +48,7 @@ C_API = ["lh2g_create", "lh2g_destroy", "lh2g_last_error", "lh2g_set_geometry", 
          "lh2g_server_create", "lh2g_server_destroy", "lh2g_server_last_error", "lh2g_server_add_scene", "lh2g_server_submit_render",
          "lh2g_server_submit_trace", "lh2g_server_wait", "lh2g_server_release", "lh2g_server_get_stats",
          "lh2g_nrc_create", "lh2g_nrc_destroy", "lh2g_nrc_last_error", "lh2g_nrc_get_spec", "lh2g_nrc_set_params", "lh2g_nrc_get_params",
-         "lh2g_nrc_get_grads", "lh2g_nrc_infer", "lh2g_nrc_train", "lh2g_nrc_apply_update", "lh2g_nrc_infer_host", "lh2g_nrc_train_host"]
+         "lh2g_nrc_get_grads", "lh2g_nrc_infer", "lh2g_nrc_train", "lh2g_nrc_apply_update", "lh2g_render_nrc", "lh2g_nrc_infer_host", "lh2g_nrc_train_host"]
 
 _lib = None
 
@@ -99,6 +99,7 @@ def load_library(path: str | None = None):
     lib.lh2g_filter.argtypes = [vp, vp]
     lib.lh2g_read_filter_buffer.argtypes = [vp, i, vp]
     lib.lh2g_get_last_filter_frame.argtypes = [vp, vp, vp, vp]
+    lib.lh2g_render_nrc.argtypes = [vp, vp, vp, vp, i, i, vp]
     if path is None:
         _lib = lib
     return lib
@@ -287,6 +288,14 @@ class RenderCore:
         out = np.zeros(4, np.uint64)
         self._check(self.lib.lh2g_get_traversal_stats(self.ctx, _p(out)), "get_traversal_stats")
         return out
+
+    # --- radiance cache ---------------------------------------------------------------------------------
+    def render_nrc(self, cache, view, params, accumulate=False, train=True):
+        """One frame with the radiance cache (lh2g_render_nrc); returns (queries, training samples, loss)."""
+        st = np.zeros(3, np.uint32)
+        self._check(self.lib.lh2g_render_nrc(self.ctx, cache.h, _p(np.ascontiguousarray(view)), _p(np.ascontiguousarray(params)),
+                                             int(accumulate), int(train), _p(st)), "render_nrc")
+        return int(st[0]), int(st[1]), float(st[2:3].view(np.float32)[0])
 
     # --- SVGF (filter core) ----------------------------------------------------------------------------
     def filter(self, fparams):

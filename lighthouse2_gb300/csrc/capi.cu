@@ -20,6 +20,7 @@
 #include <chrono>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -132,6 +133,19 @@ uint32_t xorshift(uint32_t& s) { s ^= s << 13; s ^= s >> 17; s ^= s << 5; return
 
 }  // namespace
 
+constexpr uint32_t NRC_TRAIN_CAP = 65536;   /* training samples per radiance-cache frame */
+struct NrcBuffers {
+    float4* rec = nullptr;       /* 6 float4 per path (stride = path capacity) */
+    float4* queries = nullptr;   /* 4 float4 per query */
+    uint32_t* qPath = nullptr;
+    float4* pred = nullptr;
+    float4* trainQ = nullptr;
+    float4* trainT = nullptr;
+    uint32_t* counts = nullptr;
+    uint32_t* hostCounts = nullptr;
+    int64_t cap = 0;
+};
+
 struct lh2g_context {
     int device = 0;
     cudaStream_t st = nullptr;
@@ -199,6 +213,7 @@ struct lh2g_context {
     cudaEvent_t fev[2] = {nullptr, nullptr};   /* around the filter passes: coreStats.filterTime */
     bool filterPending = false;
     lh2g_filter_params lastFilter;
+    NrcBuffers nrcBuf;
     lh2g_view lastJittered;
     lh2g_render_params lastParams;
 };
@@ -243,6 +258,9 @@ void free_target(lh2g_context* ctx) {
     for (int k = 0; k < 2; k++) dfree(B.O[k]), dfree(B.D[k]), dfree(B.T[k]);
     dfree(B.hits), dfree(B.shO), dfree(B.shD), dfree(B.shE), dfree(B.pathAcc), dfree(B.accum), dfree(B.frame), dfree(B.counters);
     free_filter(ctx);
+    NrcBuffers& n = ctx->nrcBuf;
+    dfree(n.rec), dfree(n.queries), dfree(n.qPath), dfree(n.pred), dfree(n.trainQ), dfree(n.trainT), dfree(n.counts);
+    n.cap = 0;
     ctx->cap = 0, ctx->pathAccCap = 0;
 }
 
@@ -366,6 +384,7 @@ int lh2g_destroy(lh2g_context* ctx) {
     dfree(ctx->B.capHits), dfree(ctx->B.capSeeds);
     free_target(ctx);
     if (ctx->hostCounters) cudaFreeHost(ctx->hostCounters);
+    if (ctx->nrcBuf.hostCounts) cudaFreeHost(ctx->nrcBuf.hostCounts);
     cudaEventDestroy(ctx->ev[0]), cudaEventDestroy(ctx->ev[1]);
     if (ctx->fev[0]) cudaEventDestroy(ctx->fev[0]);
     if (ctx->fev[1]) cudaEventDestroy(ctx->fev[1]);
@@ -648,8 +667,32 @@ int lh2g_set_probe(lh2g_context* ctx, int x, int y) {
     return LH2G_OK;
 }
 
-int lh2g_render_ex(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* p, int accumulate, lh2g_hit* capHits, uint32_t* capSeeds,
-                   uint32_t* countersOut) {
+}  // extern "C"
+
+namespace {
+/* work between a frame's last wave and its finalize (radiance-cache frames) */
+using FinalizeHook = std::function<int(const FrameGPU&, const WaveBuffers&)>;
+
+int ensure_nrc(lh2g_context* ctx) {
+    NrcBuffers& n = ctx->nrcBuf;
+    if (n.cap >= ctx->cap) return LH2G_OK;
+    CK(cudaStreamSynchronize(ctx->st));
+    const size_t cap = (size_t)ctx->cap;
+    cudaError_t e = dalloc(n.rec, 6 * cap);
+    if (!e) e = dalloc(n.queries, 4 * cap);
+    if (!e) e = dalloc(n.qPath, cap);
+    if (!e) e = dalloc(n.pred, cap);
+    if (!e) e = dalloc(n.trainQ, 4 * (size_t)NRC_TRAIN_CAP);
+    if (!e) e = dalloc(n.trainT, (size_t)NRC_TRAIN_CAP);
+    if (!e) e = dalloc(n.counts, 4);
+    if (!e && !n.hostCounts) e = cudaMallocHost((void**)&n.hostCounts, 16);
+    if (e) return cuda_check(ctx, e, "radiance-cache buffers");
+    n.cap = ctx->cap;
+    return LH2G_OK;
+}
+
+int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* p, int accumulate, lh2g_hit* capHits, uint32_t* capSeeds,
+                 uint32_t* countersOut, const FinalizeHook* hook) {
     if (!ctx || !view || !p) return LH2G_ERR_INVALID;
     if (!ctx->finalized) return fail(ctx, LH2G_ERR_STATE, "render: scene not finalized (call lh2g_finalize_instances)");
     if (!ctx->cap) return fail(ctx, LH2G_ERR_STATE, "render: no target (call lh2g_set_target)");
@@ -657,9 +700,14 @@ int lh2g_render_ex(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_p
         return fail(ctx, LH2G_ERR_INVALID, "render: parameters do not match the target");
     if (!ctx->mats) return fail(ctx, LH2G_ERR_STATE, "render: no materials");
     cudaSetDevice(ctx->device);
-    const bool filt = (p->flags & LH2G_RP_FILTER) != 0;
+    const bool filt = (p->flags & LH2G_RP_FILTER) != 0, nrcFrame = (p->flags & LH2G_RP_NRC) != 0;
+    if (filt && nrcFrame) return fail(ctx, LH2G_ERR_INVALID, "render: filter and radiance-cache frames do not combine");
     if (filt) {
         const int r = ensure_filter(ctx);
+        if (r != LH2G_OK) return r;
+    }
+    if (nrcFrame) {
+        const int r = ensure_nrc(ctx);
         if (r != LH2G_OK) return r;
     }
     FrameGPU F = frame_of(view, p);
@@ -669,6 +717,7 @@ int lh2g_render_ex(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_p
     B.features = filt ? ctx->sv.features : nullptr;
     B.worldPos = filt ? ctx->sv.worldPos : nullptr;
     B.deltaDepth = filt ? ctx->sv.deltaDepth : nullptr;
+    B.nrcRec = nrcFrame ? ctx->nrcBuf.rec : nullptr;
     const size_t capN = (size_t)F.maxDepth * F.P;
     if (capHits || capSeeds) {
         CK(dalloc(ctx->B.capHits, capN));
@@ -701,6 +750,10 @@ int lh2g_render_ex(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_p
         mark(), launch_connect(S, F, B, d, ctx->blocksConnect, ctx->st), mark();
     }
     if (tail) mark(), launch_tail(S, F, B, waves + 1, ctx->blocksTail, ctx->st), mark();
+    if (hook) {
+        const int r = (*hook)(F, B);
+        if (r != LH2G_OK) return r;
+    }
     const int after = p->samplesTaken + F.spp;
     mark(), launch_finalize(F, B, 1.0f / (float)after, ctx->st), mark();
     ctx->lastLaunches = timing ? launches : 0;
@@ -716,6 +769,46 @@ int lh2g_render_ex(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_p
             for (int d = 0; d < F.maxDepth; d++) countersOut[2 * d] = ctx->hostCounters->extension[d], countersOut[2 * d + 1] = ctx->hostCounters->shadow[d];
         if (ctx->hostCounters->status) return fail(ctx, LH2G_ERR_OVERFLOW, "render: traversal stack overflow or step limit");
     }
+    return LH2G_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lh2g_render_ex(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* p, int accumulate, lh2g_hit* capHits, uint32_t* capSeeds,
+                   uint32_t* countersOut) {
+    return render_frame(ctx, view, p, accumulate, capHits, capSeeds, countersOut, nullptr);
+}
+
+int lh2g_render_nrc(lh2g_context* ctx, lh2g_nrc* cache, const lh2g_view* view, const lh2g_render_params* params, int accumulate, int train,
+                    lh2g_nrc_frame_stats* stats) {
+    if (!ctx || !cache || !view || !params) return LH2G_ERR_INVALID;
+    lh2g_render_params p = *params;
+    p.flags |= LH2G_RP_NRC;
+    uint32_t nq = 0, nt = 0;
+    const FinalizeHook hook = [&](const FrameGPU& F, const WaveBuffers& B) -> int {
+        NrcBuffers& n = ctx->nrcBuf;
+        CK(cudaMemsetAsync(n.counts, 0, 16, ctx->st));
+        launch_nrc_collect(F, B, n.queries, n.qPath, n.trainQ, n.trainT, n.counts, NRC_TRAIN_CAP, ctx->st);
+        CK(cudaMemcpyAsync(n.hostCounts, n.counts, 8, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        nq = n.hostCounts[0], nt = std::min<uint32_t>(n.hostCounts[1], NRC_TRAIN_CAP);
+        if (nq) {
+            const int r = lh2g_nrc_infer(cache, (const float*)n.queries, nq, (float*)n.pred, ctx->st);
+            if (r != LH2G_OK) return fail(ctx, r, std::string("radiance-cache inference: ") + lh2g_nrc_last_error(cache));
+            launch_nrc_apply(F, B, n.pred, n.qPath, n.counts, ctx->st);
+        }
+        return LH2G_OK;
+    };
+    int r = render_frame(ctx, view, &p, accumulate, nullptr, nullptr, nullptr, &hook);
+    if (r != LH2G_OK) return r;
+    float loss = 0.0f;
+    if (train && nt > 0) {
+        r = lh2g_nrc_train(cache, (const float*)ctx->nrcBuf.trainQ, (const float*)ctx->nrcBuf.trainT, nt, 1, &loss, ctx->st);
+        if (r != LH2G_OK) return fail(ctx, r, std::string("radiance-cache training: ") + lh2g_nrc_last_error(cache));
+    }
+    if (stats) stats->queries = nq, stats->trainSamples = nt, stats->loss = loss;
     return LH2G_OK;
 }
 

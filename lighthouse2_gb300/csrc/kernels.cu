@@ -32,6 +32,7 @@ __global__ void __launch_bounds__(256) k_generate(const FrameGPU F, const WaveBu
     B.T[0][i] = make_float4(1.0f, 1.0f, 1.0f, F.eps);
     B.pathAcc[i] = make_float4(0, 0, 0, 0);
     if (F.flags & LH2G_RP_FILTER) B.pathAcc[i + F.P] = make_float4(0, 0, 0, 0);
+    if (F.flags & LH2G_RP_NRC) B.nrcRec[i + 4 * F.P] = make_float4(0, 0, 0, 0);   /* no cache query yet */
 }
 __device__ __forceinline__ uint32_t queue_count(const FrameGPU& F, const Counters* C, int depth) {
     return depth == 1 ? (uint32_t)F.P : C->extension[depth - 2];
@@ -195,6 +196,50 @@ __global__ void __launch_bounds__(128) k_connect(const SceneGPU S, const FrameGP
 }
 
 /* -------------------------------------------------------------------------------------------------- */
+/* radiance cache: the queries of the paths that ended at their cache vertex (state 1) and the training samples of
+ * the paths that went on (state 2: target = radiance gathered from the vertex on / throughput into it) */
+__global__ void k_nrc_collect(const FrameGPU F, const WaveBuffers B, float4* __restrict__ queries, uint32_t* __restrict__ qPath,
+                              float4* __restrict__ trainQ, float4* __restrict__ trainT, uint32_t* counts, const uint32_t trainCap) {
+    const int64_t P = F.P;
+    const uint32_t lane = threadIdx.x & 31u;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < P; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t p = base + threadIdx.x;
+        const float state = p < P ? B.nrcRec[4 * P + p].w : 0.0f;
+        const uint32_t qm = __ballot_sync(0xffffffffu, state == 1.0f), tm = __ballot_sync(0xffffffffu, state == 2.0f);
+        uint32_t qb = 0, tb = 0;
+        if (lane == 0) {
+            if (qm) qb = atomicAdd(&counts[0], (uint32_t)__popc(qm));
+            if (tm) tb = atomicAdd(&counts[1], (uint32_t)__popc(tm));
+        }
+        qb = __shfl_sync(0xffffffffu, qb, 0) + __popc(qm & lanemask_lt());
+        tb = __shfl_sync(0xffffffffu, tb, 0) + __popc(tm & lanemask_lt());
+        if (state == 1.0f) {
+            for (int k = 0; k < 4; k++) queries[4 * (size_t)qb + k] = B.nrcRec[k * P + p];
+            qPath[qb] = (uint32_t)p;
+        } else if (state == 2.0f && tb < trainCap) {
+            const float4 T = B.nrcRec[4 * P + p], pre = B.nrcRec[5 * P + p], L = B.pathAcc[p];
+            const float tx = T.x > 1e-8f ? (L.x - pre.x) / T.x : 0.0f, ty = T.y > 1e-8f ? (L.y - pre.y) / T.y : 0.0f;
+            const float tz = T.z > 1e-8f ? (L.z - pre.z) / T.z : 0.0f;
+            for (int k = 0; k < 4; k++) trainQ[4 * (size_t)tb + k] = B.nrcRec[k * P + p];
+            trainT[tb] = make_float4(tx, ty, tz, 0.0f);
+        }
+    }
+}
+
+/* the cache's prediction, times the throughput into the vertex, completes each path that ended there */
+__global__ void k_nrc_apply(const FrameGPU F, const WaveBuffers B, const float4* __restrict__ pred, const uint32_t* __restrict__ qPath,
+                            const uint32_t* counts) {
+    const uint32_t n = counts[0];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t p = qPath[i];
+        const float4 T = B.nrcRec[4 * F.P + p], y = pred[i];
+        float4 acc = B.pathAcc[p];
+        acc.x += T.x * fmaxf(y.x, 0.0f), acc.y += T.y * fmaxf(y.y, 0.0f), acc.z += T.z * fmaxf(y.z, 0.0f);
+        B.pathAcc[p] = acc;
+    }
+}
+
+/* -------------------------------------------------------------------------------------------------- */
 __global__ void k_finalize(const FrameGPU F, const WaveBuffers B, const float scale) {
     const int64_t px = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t WH = (int64_t)F.W * F.H;
@@ -313,6 +358,13 @@ void launch_connect(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, 
 }
 void launch_tail(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int startDepth, int blocks, cudaStream_t st) {
     k_tail<<<blocks, WAVE_BLOCK, 0, st>>>(S, F, B, startDepth);
+}
+void launch_nrc_collect(const FrameGPU& F, const WaveBuffers& B, float4* queries, uint32_t* qPath, float4* trainQ, float4* trainT, uint32_t* counts,
+                        uint32_t trainCap, cudaStream_t st) {
+    k_nrc_collect<<<sm_count() * 8, 256, 0, st>>>(F, B, queries, qPath, trainQ, trainT, counts, trainCap);
+}
+void launch_nrc_apply(const FrameGPU& F, const WaveBuffers& B, const float4* pred, const uint32_t* qPath, const uint32_t* counts, cudaStream_t st) {
+    k_nrc_apply<<<sm_count() * 8, 256, 0, st>>>(F, B, pred, qPath, counts);
 }
 void launch_finalize(const FrameGPU& F, const WaveBuffers& B, float scale, cudaStream_t st) {
     const int64_t WH = (int64_t)F.W * F.H;

@@ -18,6 +18,7 @@ struct WaveBuffers {
     float4* accum;         /* per-pixel accumulator across frames */
     float4* frame;         /* finalized output: accum / samplesTaken */
     Counters* counters;
+    float4* nrcRec;        /* LH2G_RP_NRC: per path 6 float4 with stride P: query (4), throughput + state, radiance so far */
     uint4* features;       /* LH2G_RP_FILTER: SVGF features, world position and depth derivatives of sample 0 (W*H) */
     float4* worldPos;
     float4* deltaDepth;
@@ -32,6 +33,10 @@ void launch_connect(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, 
 /* path lengths startDepth..maxDepth of the frame's remaining paths, one persistent launch */
 void launch_tail(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int startDepth, int persistentBlocks, cudaStream_t st);
 void launch_finalize(const FrameGPU& F, const WaveBuffers& B, float scale, cudaStream_t st);
+/* radiance-cache frames: gather queries / training samples (counts[0], counts[1]), then add the predictions */
+void launch_nrc_collect(const FrameGPU& F, const WaveBuffers& B, float4* queries, uint32_t* qPath, float4* trainQ, float4* trainT, uint32_t* counts,
+                        uint32_t trainCap, cudaStream_t st);
+void launch_nrc_apply(const FrameGPU& F, const WaveBuffers& B, const float4* pred, const uint32_t* qPath, const uint32_t* counts, cudaStream_t st);
 void launch_trace(const SceneGPU& S, const lh2g_ray* rays, void* out, long long n, int mode, uint32_t* fetch, uint32_t* status,
                   int persistentBlocks, cudaStream_t st);
 

@@ -42,7 +42,7 @@ extern "C" LH2G_API int lh2g_render_noalloc(lh2g_context* ctx, const lh2g_view* 
     using namespace lh2g;
     if (!ctx || !view || !p || !accumDevice) return LH2G_ERR_INVALID;
     if (p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->maxDepth < 1 || p->maxDepth > 64) return LH2G_ERR_INVALID;
-    if (p->flags & LH2G_RP_FILTER) return LH2G_ERR_INVALID;   /* filter frames need the context's feature buffers */
+    if (p->flags & (LH2G_RP_FILTER | LH2G_RP_NRC)) return LH2G_ERR_INVALID;   /* these frames need the context's own buffers */
     const long long P = (long long)p->width * p->height * p->spp;
     if (P > LH2G_NOALLOC_MAX_PATHS) return LH2G_ERR_OVERFLOW;   /* width * height * spp above the static capacity */
     SceneGPU S;
@@ -78,7 +78,7 @@ extern "C" LH2G_API int lh2g_render_noalloc(lh2g_context* ctx, const lh2g_view* 
     B.counters = (Counters*)(f + 12 * n);
     B.accum = (float4*)accumDevice;
     B.capHits = nullptr, B.capSeeds = nullptr;
-    B.features = nullptr, B.worldPos = nullptr, B.deltaDepth = nullptr;
+    B.features = nullptr, B.worldPos = nullptr, B.deltaDepth = nullptr, B.nrcRec = nullptr;
     FrameGPU F;
     F.W = p->width, F.H = p->height, F.spp = p->spp, F.maxDepth = p->maxDepth, F.rrStart = p->rrStartDepth, F.samplesTaken = p->samplesTaken;
     F.cameraR0 = p->cameraR0, F.frameSeed = p->frameSeed, F.eps = p->geometryEpsilon, F.flags = p->flags;

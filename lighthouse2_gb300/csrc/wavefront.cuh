@@ -10,6 +10,7 @@ namespace lh2g {
 namespace {
 
 constexpr int WAVE_BLOCK = 128;
+constexpr int NRC_DEPTH = 2;   /* path length at which radiance-cache frames query the cache */
 
 __device__ __forceinline__ uint32_t lanemask_lt() { uint32_t m; asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m)); return m; }
 
@@ -124,6 +125,24 @@ __device__ __forceinline__ void shade_core(const SceneGPU& S, const FrameGPU& F,
         return;
     }
     *accP = acc;
+    if ((F.flags & LH2G_RP_NRC) && depth == NRC_DEPTH && (FLAGS & S_SPECULAR) == 0) {
+        /* radiance cache: the query of this vertex (looking back along the ray), the throughput that reaches it and
+         * the radiance gathered before it; a training path (1 in 16) traces on, the others end here */
+        const bool train = (WangHash(pathIdx * 3u + F.cameraR0) & 15u) == 0u;
+        const float side = dot(D, N) > 0 ? -1.0f : 1.0f;
+        float4* rec = B.nrcRec + pathIdx;
+        const int64_t P = F.P;
+        rec[0] = make_float4(I.x, I.y, I.z, ROUGHNESS(sd));
+        rec[P] = make_float4(-D.x, -D.y, -D.z, 0.0f);
+        rec[2 * P] = make_float4(fN.x * side, fN.y * side, fN.z * side, 0.0f);
+        rec[3 * P] = make_float4(sd.color.x, sd.color.y, sd.color.z, 0.0f);
+        rec[4 * P] = make_float4(throughput.x, throughput.y, throughput.z, train ? 2.0f : 1.0f);
+        rec[5 * P] = make_float4(acc.x, acc.y, acc.z, 0.0f);
+        if (!train) {
+            if (B.capSeeds) B.capSeeds[capIdx] = 0;
+            return;
+        }
+    }
     if (ROUGHNESS(sd) <= 0.001f || TRANSMISSION(sd) > 0.999f) FLAGS |= S_SPECULAR; else FLAGS &= ~S_SPECULAR;
     uint32_t seed = WangHash(pathIdx * 17u + R0);
     if (firstHitToBeStored) {
