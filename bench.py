@@ -15,8 +15,10 @@ depth 3, next-event estimation; frames follow a seeded 8-pose camera path. Seede
   cpu_baseline  the CPU oracle (a restatement of the reference's path tracer) on all host cores.
   svgf      filter-core frames of the same scene and camera path with SVGF + TAA: device time of the six filter
             launches per frame against the measured HBM bandwidth.
-  serving   the serving loop on a seeded job list over 4 resident scenes against sequential plain-core renders of
-            the same jobs: saturated throughput, and p50 / p99 latency under Poisson arrivals.
+  serving   the serving loop on seeded job lists over 4 resident scenes against sequential plain-core renders of
+            the same jobs: saturated throughput, and p50 / p99 latency under Poisson arrivals swept over rates.
+  radiance_cache  the cache estimator against the plain one on the same scene and frame size, RMSE and relative MSE
+            against a 4096-spp FP64-accumulated plain render, at equal device time and at equal sample count.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 Under torchrun each rank renders its own frames on its own GPU (replicas, weak scaling); rank 0 prints.
@@ -54,7 +56,7 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms during the timed region."""
     Q = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
 
@@ -66,7 +68,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
-                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                                          "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except Exception:
@@ -213,24 +215,34 @@ def svgf_leg(core, W, H, steps, warmup):
             "peak_GBps": peak, "frac": achieved / peak, "peak_source": peak_kind}
 
 
-def serving_jobs(n, n_scenes, seed=11):
-    """Seeded job list: scene, resolution in {256^2, 512^2, 1024^2, 1920x1080}, spp in {1, 4, 16}, depth 4..8,
-    a camera pose per job."""
+SERVING_MIXES = {
+    # the survey's job distribution: resolution in {256^2, 512^2, 1024^2, 1920x1080}, spp in {1, 4, 16}
+    "full": {"res": [(256, 256), (512, 512), (1024, 1024), (1920, 1080)], "spp": [1, 4, 16], "rates": [10, 25, 50, 100, 200, 500]},
+    # small interactive requests only, where one job alone leaves most of the GPU idle
+    "small": {"res": [(256, 256), (512, 512)], "spp": [1, 4], "rates": [100, 200, 500, 1000, 2000]},
+}
+
+
+def serving_jobs(n, n_scenes, mix, seed=11):
+    """Seeded job list: scene, resolution and spp drawn from the mix, depth 4..8, a camera pose per job."""
     import numpy as np
     rng = np.random.default_rng(seed)
-    res = [(256, 256), (512, 512), (1024, 1024), (1920, 1080)]
+    res, spp = SERVING_MIXES[mix]["res"], SERVING_MIXES[mix]["spp"]
     jobs = []
     for k in range(n):
-        W, H = res[int(rng.integers(0, 4))]
-        jobs.append({"scene": int(rng.integers(0, n_scenes)), "W": W, "H": H, "spp": int(rng.choice([1, 4, 16])),
+        W, H = res[int(rng.integers(0, len(res)))]
+        jobs.append({"scene": int(rng.integers(0, n_scenes)), "W": W, "H": H, "spp": int(rng.choice(spp)),
                      "depth": int(rng.integers(4, 9)), "frame": int(rng.integers(0, 64))})
     return jobs
 
 
 def serving_leg(args):
-    """The serving loop against sequential plain-core renders of the same job list: saturated throughput (all jobs
-    submitted at once) and latency under Poisson arrivals at a fraction of the sequential capacity."""
+    """The serving loop against sequential plain-core renders of the same job lists (one per mix): saturated
+    throughput (every job submitted at once), then latency under Poisson arrivals swept over rates. The sequential
+    arm's latencies at each rate come from its measured per-job service times (first come, first served). For each
+    arm, the highest tested rate whose p99 latency stays within 2x the p99 of the jobs' standalone latencies."""
     import numpy as np
+    import torch
     from lighthouse2_gb300 import scenes as S
     from lighthouse2_gb300.core import RenderCore, make_params, camera_r0, RP_NEE, RP_DEPTH_W
     from lighthouse2_gb300.server import RenderServer
@@ -239,18 +251,13 @@ def serving_leg(args):
                   ("spheres 16 (512k)", lambda: S.spheres_2m(seed=3, n_spheres=16)),
                   ("spheres 64 (2M)", lambda: S.spheres_2m(seed=7)),
                   ("spheres 128 (4M)", lambda: S.spheres_2m(seed=9, n_spheres=128))]
-    scenes, cores = [], []
+    cores = []
     for name, make in scene_defs:
-        sc = make()
         core = RenderCore(0)
-        core.set_scene(sc)
-        scenes.append(sc)
+        core.set_scene(make())
         cores.append(core)
     setup_s = time.time() - t0
-    jobs = serving_jobs(args.serving_jobs, len(cores))
-    import torch
-    # pinned host images for both arms (copies back are part of each job's latency)
-    pinned = [torch.empty((j["W"] * j["H"], 4), dtype=torch.float32, pin_memory=True).numpy() for j in jobs]
+    pct = lambda a, q: float(np.percentile(a, q) * 1e3)
 
     def inputs(j):
         view = S.cornell_view(j["W"], j["H"], frame=j["frame"] % 4) if j["scene"] == 0 else S.spheres_view(j["W"], j["H"], frame=j["frame"])
@@ -258,89 +265,172 @@ def serving_leg(args):
                         flags=RP_NEE | RP_DEPTH_W)
         return view, p
 
-    # sequential plain-core renders: service time of every job alone (render + image read back)
-    for c in cores:
-        c.SetTarget(64, 64, 1)
-    for j in jobs[:4]:   # warm-up
-        view, p = inputs(j)
-        cores[j["scene"]].SetTarget(j["W"], j["H"], j["spp"])
-        cores[j["scene"]].render_ex(view, p, counters=False)
-        cores[j["scene"]].read_accumulator()
-    # (SetTarget, which reallocates when the resolution changes, stays outside the service time: a plain-core
-    # deployment would keep a target per resolution)
-    service, seq_rays = [], 0
-    for j in jobs:
-        view, p = inputs(j)
-        c = cores[j["scene"]]
-        c.SetTarget(j["W"], j["H"], j["spp"])
-        c.WaitForRender()
+    def run_mix(mix, n_jobs):
+        jobs = serving_jobs(n_jobs, len(cores), mix)
+        # pinned host images for both arms (copies back are part of each job's latency)
+        pinned = [torch.empty((j["W"] * j["H"], 4), dtype=torch.float32, pin_memory=True).numpy() for j in jobs]
+        for j in jobs[:4]:   # warm-up
+            view, p = inputs(j)
+            cores[j["scene"]].SetTarget(j["W"], j["H"], j["spp"])
+            cores[j["scene"]].render_ex(view, p, counters=False)
+            cores[j["scene"]].read_accumulator()
+        # sequential plain-core renders: service time of every job alone (render + image read back). SetTarget,
+        # which reallocates when the resolution changes, stays outside: a plain-core deployment would keep a
+        # target per resolution.
+        service, seq_rays = [], 0
+        for k, j in enumerate(jobs):
+            view, p = inputs(j)
+            c = cores[j["scene"]]
+            c.SetTarget(j["W"], j["H"], j["spp"])
+            c.WaitForRender()
+            t = time.perf_counter()
+            out = c.render_ex(view, p, counters=True)
+            c.read_accumulator_into(pinned[k])
+            service.append(time.perf_counter() - t)
+            cnt = out["counters"]
+            seq_rays += j["W"] * j["H"] * j["spp"] + int(cnt[:, 0].sum()) + int(cnt[:, 1].sum())
+        service = np.array(service)
+        t_seq = float(service.sum())
+        cap = max(j["W"] * j["H"] * j["spp"] for j in jobs) * 2
+        srv = RenderServer(path_capacity=cap)
+        sids = [srv.add_scene(c) for c in cores]
+        for j in jobs[:4]:   # warm-up
+            view, p = inputs(j)
+            jid = srv.submit_render(sids[j["scene"]], view, p)
+            srv.wait(jid)
+            srv.release(jid)
+        r0 = srv.stats()["raysTraced"]
         t = time.perf_counter()
-        out = c.render_ex(view, p, counters=True)
-        c.read_accumulator_into(pinned[len(service)])
-        service.append(time.perf_counter() - t)
-        cnt = out["counters"]
-        seq_rays += j["W"] * j["H"] * j["spp"] + int(cnt[:, 0].sum()) + int(cnt[:, 1].sum())
-    t_seq = float(sum(service))
-    cap = max(j["W"] * j["H"] * j["spp"] for j in jobs) * 2
-    srv = RenderServer(path_capacity=cap)
-    sids = [srv.add_scene(c) for c in cores]
-    for j in jobs[:4]:   # warm-up
-        view, p = inputs(j)
-        srv.wait(srv.submit_render(sids[j["scene"]], view, p))
-    # saturated: every job at once
-    r0 = srv.stats()["raysTraced"]
-    t = time.perf_counter()
-    ids = []
-    for k, j in enumerate(jobs):
-        view, p = inputs(j)
-        ids.append(srv.submit_render(sids[j["scene"]], view, p, out=pinned[k]))
-    for i in ids:
-        srv.wait(i)
-    t_sat = time.perf_counter() - t
-    sat_rays = srv.stats()["raysTraced"] - r0
-    for i in ids:
-        srv.release(i)
-    # Poisson arrivals at a fraction of the sequential capacity
-    rate = args.serving_load * len(jobs) / t_seq
-    rng = np.random.default_rng(5)
-    arrivals = np.cumsum(rng.exponential(1.0 / rate, len(jobs)))
-    t_start = time.perf_counter()
-    ids = []
-    for k, j in enumerate(jobs):
-        delay = arrivals[k] - (time.perf_counter() - t_start)
-        if delay > 0:
-            time.sleep(delay)
-        view, p = inputs(j)
-        ids.append(srv.submit_render(sids[j["scene"]], view, p, out=pinned[k]))
-    lat = []
-    for i in ids:
-        ts, ta, td = srv.wait(i)
-        lat.append(td - ts)
-        srv.release(i)
-    srv.close()
+        ids = []
+        for k, j in enumerate(jobs):
+            view, p = inputs(j)
+            ids.append(srv.submit_render(sids[j["scene"]], view, p, out=pinned[k]))
+        for i in ids:
+            srv.wait(i)
+        t_sat = time.perf_counter() - t
+        sat_rays = srv.stats()["raysTraced"] - r0
+        for i in ids:
+            srv.release(i)
+        bound = 2.0 * np.percentile(service, 99)
+        sweep = []
+        for rate in SERVING_MIXES[mix]["rates"]:
+            arrivals = np.cumsum(np.random.default_rng(5).exponential(1.0 / rate, len(jobs)))
+            t_start = time.perf_counter()
+            ids = []
+            for k, j in enumerate(jobs):
+                delay = arrivals[k] - (time.perf_counter() - t_start)
+                if delay > 0:
+                    time.sleep(delay)
+                view, p = inputs(j)
+                ids.append(srv.submit_render(sids[j["scene"]], view, p, out=pinned[k]))
+            lat, last = [], 0.0
+            for i in ids:
+                ts, ta, td = srv.wait(i)
+                lat.append(td - ts)
+                last = max(last, td)
+                srv.release(i)
+            lat = np.array(lat)
+            seq_lat, free_at = [], 0.0
+            for k in range(len(jobs)):
+                start = max(arrivals[k], free_at)
+                free_at = start + service[k]
+                seq_lat.append(free_at - arrivals[k])
+            seq_lat = np.array(seq_lat)
+            sweep.append({"rate_jobs_per_s": rate, "server_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
+                          "sequential_fifo_ms": {"p50": pct(seq_lat, 50), "p99": pct(seq_lat, 99)},
+                          "server_p99_within_bound": bool(np.percentile(lat, 99) <= bound),
+                          "sequential_p99_within_bound": bool(np.percentile(seq_lat, 99) <= bound),
+                          "slowdown_vs_standalone": {"p50": float(np.percentile(lat / service, 50)), "p99": float(np.percentile(lat / service, 99))}})
+        srv.close()
+        ok_srv = [r["rate_jobs_per_s"] for r in sweep if r["server_p99_within_bound"]]
+        ok_seq = [r["rate_jobs_per_s"] for r in sweep if r["sequential_p99_within_bound"]]
+        return {"jobs": len(jobs), "resolutions": [f"{w}x{h}" for w, h in SERVING_MIXES[mix]["res"]], "spp": SERVING_MIXES[mix]["spp"],
+                "path_capacity": cap,
+                "standalone_ms": {"p50": pct(service, 50), "p99": pct(service, 99)},
+                "sequential": {"jobs_per_s": len(jobs) / t_seq, "Mrays_per_s": seq_rays / t_seq / 1e6, "seconds": t_seq},
+                "saturated": {"jobs_per_s": len(jobs) / t_sat, "Mrays_per_s": sat_rays / t_sat / 1e6, "seconds": t_sat,
+                              "throughput_vs_sequential": t_seq / t_sat},
+                "poisson_sweep": sweep,
+                "rate_at_p99_bound": {"bound_ms": bound * 1e3, "server": max(ok_srv) if ok_srv else None,
+                                      "sequential": max(ok_seq) if ok_seq else None}}
+
+    out = {"workload": f"seeded job lists over 4 resident scenes ({', '.join(n for n, _ in scene_defs)}), depth 4..8, one camera pose "
+                       f"per job; scenes built once ({setup_s:.0f} s); latency = submit to image in pinned host memory",
+           "full": run_mix("full", args.serving_jobs), "small": run_mix("small", 4 * args.serving_jobs)}
     for c in cores:
         c.close()
-    # the same arrivals served by the plain core one job at a time (first come, first served), from the measured
-    # service times
-    seq_lat, free_at = [], 0.0
-    for k in range(len(jobs)):
-        start = max(arrivals[k], free_at)
-        free_at = start + service[k]
-        seq_lat.append(free_at - arrivals[k])
-    lat, seq_lat, service = np.array(lat), np.array(seq_lat), np.array(service)
-    slow = lat / service
-    pct = lambda a, q: float(np.percentile(a, q) * 1e3)
-    return {"workload": f"{len(jobs)} seeded jobs over 4 resident scenes ({', '.join(n for n, _ in scene_defs)}); resolution in "
-                        "{256^2, 512^2, 1024^2, 1920x1080}, spp in {1, 4, 16}, depth 4..8; scenes built once (" + f"{setup_s:.0f} s)",
-            "path_capacity": cap,
-            "sequential": {"jobs_per_s": len(jobs) / t_seq, "Mrays_per_s": seq_rays / t_seq / 1e6, "seconds": t_seq},
-            "saturated": {"jobs_per_s": len(jobs) / t_sat, "Mrays_per_s": sat_rays / t_sat / 1e6, "seconds": t_sat,
-                          "throughput_vs_sequential": t_seq / t_sat},
-            "poisson": {"rate_jobs_per_s": rate, "load_vs_sequential_capacity": args.serving_load,
-                        "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
-                        "sequential_fifo_latency_ms": {"p50": pct(seq_lat, 50), "p99": pct(seq_lat, 99)},
-                        "standalone_latency_ms": {"p50": pct(service, 50), "p99": pct(service, 99)},
-                        "slowdown_vs_standalone": {"p50": float(np.percentile(slow, 50)), "p99": float(np.percentile(slow, 99))}}}
+    return out
+
+
+NRC_FIELD_BOUNDS = ((-100.0, -2.0, -100.0), (100.0, 48.0, 100.0))   # the sphere field and its lights, with margin
+
+
+def nrc_leg(args, core, name, view, bounds, W, H):
+    """Radiance cache against the plain estimator on the core's scene at W x H, judged by a plain render of
+    args.nrc_ref_spp samples per pixel accumulated in FP64: RMSE and relative MSE at equal device time (frame counts
+    from measured frame times) and at equal sample count, after the cache has trained online for some frames.
+    Both estimators run on the same core, scene and camera pose."""
+    import numpy as np
+    from lighthouse2_gb300.core import make_params, camera_r0, RP_NEE, RP_DEPTH_W
+    from lighthouse2_gb300.nrc import RadianceCache
+
+    def P(k, spp=1):
+        return make_params(W, H, spp, max_depth=MAX_DEPTH, rr_start=RR_START, samples_taken=k, camera_r0=camera_r0(k), flags=RP_NEE | RP_DEPTH_W)
+
+    t0 = time.time()
+    batch = 16
+    core.SetTarget(W, H, batch)
+    ref = np.zeros((W * H, 3), np.float64)
+    for k in range(args.nrc_ref_spp // batch):
+        p = P(batch * k, batch)
+        p["cameraR0"] = (0x9E3779B9 * (k + 7)) & 0xFFFFFFFF
+        core.render_ex(view, p, accumulate=False, counters=False)
+        ref += core.read_accumulator()[:, :3]
+    ref /= float(args.nrc_ref_spp // batch * batch)
+    ref_s = time.time() - t0
+    core.SetTarget(W, H, 1)
+    cache = RadianceCache(bounds[0], bounds[1], learning_rate=args.nrc_lr, seed=5)
+    stats = [core.render_nrc(cache, view, P(100000 + k)) for k in range(args.nrc_warmup)]
+
+    def timed(fn, n=16):
+        for k in range(3):
+            fn(k)
+        core.WaitForRender()
+        t = time.perf_counter()
+        for k in range(n):
+            fn(k)
+        core.WaitForRender()
+        return (time.perf_counter() - t) / n
+
+    plain = lambda k: core.render_ex(view, P(k), accumulate=k > 0, counters=False)
+    cached = lambda k: core.render_nrc(cache, view, P(k), accumulate=k > 0)
+    t_plain, t_cache = timed(plain), timed(cached)
+
+    def image(fn, n):
+        for k in range(n):
+            fn(k)
+        return core.read_accumulator()[:, :3].astype(np.float64) / n
+
+    def errors(img):
+        return {"rmse": float(np.sqrt(np.mean((img - ref) ** 2))), "relmse": float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))}
+
+    box = [[round(float(x), 3) for x in b] for b in bounds]
+    out = {"workload": f"{name}, {W}x{H}, depth {MAX_DEPTH}, RR after depth {RR_START - 1}, NEE; reference {args.nrc_ref_spp} spp plain, "
+                       f"FP64 sums ({ref_s:.0f} s); cache box {box}, Adam lr {args.nrc_lr}; trained over {args.nrc_warmup} frames "
+                       f"first, then online (1/16 of the paths, at most 65,536 per frame); relmse = mean of err^2 / (ref^2 + 0.01)",
+           "plain_ms_per_frame": t_plain * 1e3, "cache_ms_per_frame": t_cache * 1e3,
+           "cache_queries_per_frame": stats[-1][0], "train_samples_per_frame": stats[-1][1],
+           "loss_first": float(np.mean([x[2] for x in stats[:5]])), "loss_last": float(np.mean([x[2] for x in stats[-5:]])), "equal_time": {}}
+    for n_plain in (4, 16, 64):
+        n_cache = max(1, int(round(n_plain * t_plain / t_cache)))
+        e_p, e_c = errors(image(plain, n_plain)), errors(image(cached, n_cache))
+        out["equal_time"][f"{n_plain}_plain_frames"] = {"cache_frames": n_cache, "plain": e_p, "cache": e_c,
+                                                        "rmse_reduction": 1.0 - e_c["rmse"] / e_p["rmse"],
+                                                        "relmse_reduction": 1.0 - e_c["relmse"] / e_p["relmse"]}
+    e_p, e_c = errors(image(plain, 16)), errors(image(cached, 16))
+    out["equal_spp_16"] = {"plain": e_p, "cache": e_c, "rmse_reduction": 1.0 - e_c["rmse"] / e_p["rmse"]}
+    cache.close()
+    return out
 
 
 def run_gb300(args):
@@ -369,8 +459,14 @@ def run_gb300(args):
     frames = [frame_params(k, W, H) for k in range(8)]
     for k in range(args.warmup):
         core.render_ex(*frames[k % 8], counters=False)
+    # per-pose queue sizes and traversal work: a frame is a deterministic function of its view and parameters, so
+    # the timed frames below have exactly these (checked again after the timed region)
+    counts, trav_pose = [], []
+    for k in range(8):
+        counts.append(core.render_ex(*frames[k], counters=True)["counters"].copy())
+        trav_pose.append(np.asarray(core.traversal_stats(), np.float64))
     core.WaitForRender()
-    # ---- device-timed region: K frames, scene and path state resident ----
+    # ---- device-timed region: K frames back to back, scene and path state resident, no host synchronisation ----
     core.enable_launch_timing(True)
     clocks = ClockSampler(local)
     clocks.start()
@@ -381,22 +477,32 @@ def run_gb300(args):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with torch.cuda.stream(stream):
         e0.record()
+    for k in range(args.steps):
+        core.render_ex(*frames[k % 8], counters=False)
+    with torch.cuda.stream(stream):
+        e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    lt_all = [float(x) for x in core.launch_times()]
+    core.enable_launch_timing(False)
+    assert np.array_equal(core.render_ex(*frames[0], counters=True)["counters"], counts[0]), "frame counters are not deterministic"
+    per_frame = 2 + 3 * waves + (1 if waves < MAX_DEPTH else 0)
+    assert len(lt_all) == per_frame * args.steps, (len(lt_all), per_frame, args.steps)
     rays = 0
     per_kind = {"extend": [0.0, 0, 0], "shade": [0.0, 0, 0], "connect": [0.0, 0, 0], "tail": [0.0, 0, 0], "generate": [0.0, 0, 0],
                 "finalize": [0.0, 0, 0]}
-    launches = 0
+    launches = len(lt_all)
     trav = np.zeros(4, np.float64)
     ext_rays = shadow_rays = 0
     for k in range(args.steps):
-        out = core.render_ex(*frames[k % 8], counters=True)   # counters: the per-depth queue sizes of this frame
-        c = out["counters"]
+        c = counts[k % 8]
+        lt = lt_all[k * per_frame:(k + 1) * per_frame]
         n_in = [W * H] + [int(x) for x in c[:-1, 0]]
         rays += W * H + int(c[:, 0].sum()) + int(c[:, 1].sum())
-        lt = [float(x) for x in core.launch_times()]
-        trav += core.traversal_stats()
+        trav += trav_pose[k % 8]
         ext_rays += W * H + int(c[:-1, 0].sum())
         shadow_rays += int(c[:, 1].sum())
-        launches += len(lt)
         per_kind["generate"][0] += lt[0]
         per_kind["finalize"][0] += lt[-1]
         for d in range(waves):
@@ -413,12 +519,6 @@ def run_gb300(args):
             per_kind["tail"][0] += lt[1 + 3 * waves]
             per_kind["tail"][1] += b
             per_kind["tail"][2] += 1
-    with torch.cuda.stream(stream):
-        e1.record()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    clk = clocks.stop()
-    core.enable_launch_timing(False)
     if dist:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -432,14 +532,25 @@ def run_gb300(args):
     e2e_rays, t_e2e = 0, 0.0
     for k in range(args.steps):
         t = time.perf_counter()
-        out = core.render_ex(*frames[k % 8], counters=True)
+        core.render_ex(*frames[k % 8], counters=False)
         core.read_framebuffer_into(host.data_ptr())
         t_e2e += time.perf_counter() - t
-        c = out["counters"]
+        c = counts[k % 8]
         e2e_rays += W * H + int(c[:, 0].sum()) + int(c[:, 1].sum())
     e2e_value = e2e_rays * world / t_e2e / 1e6
     svgf = svgf_leg(core, W, H, max(args.steps, 8), args.warmup) if not args.no_svgf else None
     serving = serving_leg(args) if (not args.no_serving and rank == 0) else None
+    nrc = None
+    if not args.no_nrc and rank == 0:
+        # the large scene at the bench's frame size; paths there are short (most bounces leave the sphere field for
+        # the sky), so the cache also runs on the closed Cornell room, where every path is long
+        nrc = {"spheres_2m": nrc_leg(args, core, "spheres_2m", S.spheres_view(W, H, frame=0), NRC_FIELD_BOUNDS, W, H)}
+        cb = S.cornell_sphere(subdiv=6)
+        core_c = RenderCore(local)
+        core_c.set_scene(cb)
+        core_c.Setting("waveTail", args.wave_tail)
+        nrc["cornell"] = nrc_leg(args, core_c, "cornell 82k", S.cornell_view(1024, 1024), cb.bounds, 1024, 1024)
+        core_c.close()
     if rank != 0:
         return 0
     frame_ms = sum(v[0] for v in per_kind.values())
@@ -478,6 +589,8 @@ def run_gb300(args):
         line["svgf"] = svgf
     if serving is not None:
         line["serving"] = serving
+    if nrc is not None:
+        line["radiance_cache"] = nrc
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(sc, W, H, args.cpu_seconds, os.cpu_count() or 1)
     print(json.dumps(line, default=float), flush=True)
@@ -488,8 +601,8 @@ def run_gb300(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--width", type=int, default=W_DEFAULT)
     ap.add_argument("--height", type=int, default=H_DEFAULT)
@@ -497,8 +610,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-svgf", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-nrc", action="store_true")
+    ap.add_argument("--nrc-lr", type=float, default=1e-3)
+    ap.add_argument("--nrc-ref-spp", type=int, default=4096)
+    ap.add_argument("--nrc-warmup", type=int, default=200)
     ap.add_argument("--serving-jobs", type=int, default=120)
-    ap.add_argument("--serving-load", type=float, default=0.8, help="Poisson arrival rate as a fraction of the sequential capacity")
     ap.add_argument("--wave-tail", type=int, default=WAVE_TAIL, help="first path length of the persistent tail kernel (0: off)")
     args = ap.parse_args()
     if args.warmup < 3:

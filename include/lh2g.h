@@ -105,9 +105,11 @@ LH2G_API int lh2g_read_accumulator(lh2g_context* ctx, float* host);
 
 /* The context's CUDA stream (cudaStream_t), for callers that bracket frames with their own events. */
 LH2G_API int lh2g_get_stream(lh2g_context* ctx, void** stream);
-/* Per-launch device timing of the next frames (enable != 0): lh2g_get_launch_times fills ms[k] with the
- * duration of launch k of the last frame, in launch order [generate, (extend, shade, connect) x maxDepth,
- * finalize], and *count with the number of launches. Timing adds one event pair per launch. */
+/* Per-launch device timing of the next frames (enable != 0): lh2g_get_launch_times waits for the core's stream,
+ * fills ms[k] with the duration of launch k of every frame rendered since timing was enabled or since its previous
+ * call (frames in order; per frame [generate, (extend, shade, connect) x waves, tail if used, finalize]), sets
+ * *count to the number of those launches (up to 16384; older ones are dropped) and starts over. Timing adds one
+ * event pair per launch and no host synchronisation. */
 LH2G_API int lh2g_enable_launch_timing(lh2g_context* ctx, int enable);
 LH2G_API int lh2g_get_launch_times(lh2g_context* ctx, float* ms, int capacity, int* count);
 

@@ -279,7 +279,8 @@ class RenderCore:
         self._check(self.lib.lh2g_enable_launch_timing(self.ctx, int(on)), "enable_launch_timing")
 
     def launch_times(self):
-        buf = np.zeros(256, np.float32)
+        """Durations (ms) of every launch timed since the previous call, frames in order."""
+        buf = np.zeros(16384, np.float32)
         n = C.c_int(0)
         self._check(self.lib.lh2g_get_launch_times(self.ctx, _p(buf), len(buf), C.byref(n)), "get_launch_times")
         return buf[:n.value].copy()

@@ -193,7 +193,8 @@ struct lh2g_context {
     cudaEvent_t ev[2];
     bool launchTiming = false;
     std::vector<cudaEvent_t> lev;   /* 2 per launch */
-    int lastLaunches = 0;
+    int timedLaunches = 0;             /* launches timed since the last lh2g_get_launch_times */
+    static constexpr int MAX_TIMED_LAUNCHES = 1 << 14;
     int blocksExtend = 0, blocksConnect = 0, blocksShade = 0, blocksTail = 0;
     /* path length from which the remaining paths run to their end in one persistent kernel (0: wave loop
      * to the end); a scheduling choice only, results are the same */
@@ -734,13 +735,14 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
     const bool tail = waves < F.maxDepth;
     const int launches = 2 + 3 * waves + (tail ? 1 : 0);
     const bool timing = ctx->launchTiming;
+    if (timing && ctx->timedLaunches + launches > lh2g_context::MAX_TIMED_LAUNCHES) ctx->timedLaunches = 0;   /* never read: start over */
     if (timing)
-        while ((int)ctx->lev.size() < 2 * launches) {
+        while ((int)ctx->lev.size() < 2 * (ctx->timedLaunches + launches)) {
             cudaEvent_t e;
             CK(cudaEventCreate(&e));
             ctx->lev.push_back(e);
         }
-    int li = 0;
+    int li = 2 * ctx->timedLaunches;
     auto mark = [&]() { if (timing) cudaEventRecord(ctx->lev[li++], ctx->st); };
     CK(cudaEventRecord(ctx->ev[0], ctx->st));
     mark(), launch_generate(F, B, ctx->st), mark();
@@ -756,7 +758,7 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
     }
     const int after = p->samplesTaken + F.spp;
     mark(), launch_finalize(F, B, 1.0f / (float)after, ctx->st), mark();
-    ctx->lastLaunches = timing ? launches : 0;
+    if (timing) ctx->timedLaunches += launches;
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev[1], ctx->st));
     CK(cudaMemcpyAsync(ctx->hostCounters, B.counters, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->st));
@@ -1023,18 +1025,20 @@ int lh2g_get_stream(lh2g_context* ctx, void** stream) {
 int lh2g_enable_launch_timing(lh2g_context* ctx, int enable) {
     if (!ctx) return LH2G_ERR_INVALID;
     ctx->launchTiming = enable != 0;
+    ctx->timedLaunches = 0;
     return LH2G_OK;
 }
 
 int lh2g_get_launch_times(lh2g_context* ctx, float* ms, int capacity, int* count) {
     if (!ctx || !count || (capacity > 0 && !ms)) return LH2G_ERR_INVALID;
     CK(cudaStreamSynchronize(ctx->st));
-    *count = ctx->lastLaunches;
-    for (int k = 0; k < ctx->lastLaunches && k < capacity; k++) {
+    *count = ctx->timedLaunches;
+    for (int k = 0; k < ctx->timedLaunches && k < capacity; k++) {
         float t = 0;
         CK(cudaEventElapsedTime(&t, ctx->lev[2 * k], ctx->lev[2 * k + 1]));
         ms[k] = t;
     }
+    ctx->timedLaunches = 0;
     return LH2G_OK;
 }
 
