@@ -39,7 +39,8 @@ sys.path.insert(0, ROOT)
 
 W_DEFAULT, H_DEFAULT = 1920, 1080
 MAX_DEPTH, RR_START = 8, 4
-WAVE_TAIL = 4          # path lengths >= 4 run in the persistent tail kernel (setting "waveTail")
+WAVE_TAIL = 5          # path lengths >= 5 run in the persistent tail kernel (setting "waveTail")
+LANES = 3              # frames in flight (setting "pipelineFrames")
 WORKLOAD = "spheres_2m: 64 x 32k-tri displaced spheres + ground (2,048,002 tris, 66 instances), 16 quad + 4 point lights, " \
            "20 materials (4 textured), sky; 1920x1080 1spp, max depth 8, RR after depth 3, NEE"
 METRIC = "Mrays/s @1080p 1spp"
@@ -454,6 +455,7 @@ def run_gb300(args):
     build_ms = core.GetCoreStats()["bvhBuildTime"]
     core.SetTarget(W, H, 1)
     core.Setting("waveTail", args.wave_tail)
+    core.Setting("pipelineFrames", args.lanes)
     waves = min(MAX_DEPTH, args.wave_tail - 1) if args.wave_tail > 0 else MAX_DEPTH
     stream = torch.cuda.ExternalStream(core.stream_ptr())
     frames = [frame_params(k, W, H) for k in range(8)]
@@ -479,6 +481,7 @@ def run_gb300(args):
         e0.record()
     for k in range(args.steps):
         core.render_ex(*frames[k % 8], counters=False)
+    core.stream_ptr()   # orders the core's stream after the frames (consecutive frames overlap on two internal lanes)
     with torch.cuda.stream(stream):
         e1.record()
     torch.cuda.synchronize()
@@ -527,16 +530,20 @@ def run_gb300(args):
         dist.all_reduce(r)
         rays = int(r.item())
     value = rays / (ms / 1e3) / 1e6
-    # ---- end-to-end through the C ABI: camera in, frame read back to pinned host memory ----
-    host = torch.empty((W * H, 4), dtype=torch.float32, pin_memory=True)
-    e2e_rays, t_e2e = 0, 0.0
+    # ---- end-to-end through the C ABI: camera and parameters in from host memory, every frame copied back into
+    # pinned host memory (lh2g_render_to_host; consecutive frames and their copies overlap), timed on the host ----
+    hosts = [torch.empty((W * H, 4), dtype=torch.float32, pin_memory=True) for _ in range(2)]
+    core.WaitForRender()
+    e2e_rays = 0
+    t = time.perf_counter()
     for k in range(args.steps):
-        t = time.perf_counter()
-        core.render_ex(*frames[k % 8], counters=False)
-        core.read_framebuffer_into(host.data_ptr())
-        t_e2e += time.perf_counter() - t
+        core.render_to_host(*frames[k % 8], hosts[k % 2].data_ptr())
         c = counts[k % 8]
         e2e_rays += W * H + int(c[:, 0].sum()) + int(c[:, 1].sum())
+    core.WaitForRender()
+    t_e2e = time.perf_counter() - t
+    last = core.read_framebuffer()
+    assert np.array_equal(hosts[(args.steps - 1) % 2].numpy(), last), "the last copied frame differs from the device frame"
     e2e_value = e2e_rays * world / t_e2e / 1e6
     svgf = svgf_leg(core, W, H, max(args.steps, 8), args.warmup) if not args.no_svgf else None
     serving = serving_leg(args) if (not args.no_serving and rank == 0) else None
@@ -569,7 +576,7 @@ def run_gb300(args):
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": 1, "max_depth": MAX_DEPTH, "rr_start_depth": RR_START,
-                       "wave_tail": args.wave_tail,
+                       "wave_tail": args.wave_tail, "frames_in_flight": args.lanes,
                        "l2": "inputs larger than L2 (scene ~0.6 GB + path state ~0.36 GB resident), no flush",
                        "bvh_build_ms": round(build_ms, 2), "scene_generation_s": round(gen_s, 1),
                        "rays_per_frame": rays / args.steps / world,
@@ -615,6 +622,7 @@ def main():
     ap.add_argument("--nrc-ref-spp", type=int, default=4096)
     ap.add_argument("--nrc-warmup", type=int, default=200)
     ap.add_argument("--serving-jobs", type=int, default=120)
+    ap.add_argument("--lanes", type=int, default=LANES, help="frames in flight (0 or 1: one at a time)")
     ap.add_argument("--wave-tail", type=int, default=WAVE_TAIL, help="first path length of the persistent tail kernel (0: off)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -68,7 +68,10 @@ LH2G_API int lh2g_set_sky(lh2g_context* ctx, const float* rgb, int width, int he
 /* Setting (core_api_base.h:95): "epsilon", "clampValue", "maxDepth", "rrStartDepth", "nee", and the filter
  * core's "filter" (0/1, default 0), "TAA" (0/1, default 1), "clampDirect" (2.5), "clampIndirect" (15)
  * (lib/RenderCore_Optix7Filter/rendercore.cpp:674-677, rendercore.h:32-35). With "filter" on, lh2g_render
- * renders filter-core frames (LH2G_RP_FILTER, Halton-jittered when TAA is on) and denoises them with SVGF. */
+ * renders filter-core frames (LH2G_RP_FILTER, Halton-jittered when TAA is on) and denoises them with SVGF.
+ * Scheduling settings of this core (results do not change): "waveTail" (default 5; path lengths from this one on
+ * run to their end in one persistent kernel; 0: one launch per stage and wave throughout) and "pipelineFrames"
+ * (frames in flight, 0..3, default 3; 0 and 1 render one frame at a time; see lh2g_get_stream). */
 LH2G_API int lh2g_setting(lh2g_context* ctx, const char* name, float value);
 /* SetTarget (core_api_base.h:93), headless: the output is a device float4 buffer of width*height pixels. */
 LH2G_API int lh2g_set_target(lh2g_context* ctx, int width, int height, int spp);
@@ -82,6 +85,12 @@ LH2G_API int lh2g_render(lh2g_context* ctx, const lh2g_view* view, int converge)
  * receive per path length the extension and connection counts. */
 LH2G_API int lh2g_render_ex(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* params, int accumulate,
                    lh2g_hit* captureHits, uint32_t* captureSeeds, uint32_t* counters);
+/* lh2g_render_ex without captures, followed by an asynchronous copy of the finalized frame (W*H float4) into
+ * hostFrame: returns once the work is queued; hostFrame holds the frame after lh2g_wait (or any call that waits for
+ * the context). Consecutive calls overlap like other plain frames; the copy of one frame completes before the next
+ * frame's finalize overwrites the device frame. Pinned host memory makes the copy overlap rendering. */
+LH2G_API int lh2g_render_to_host(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* params, int accumulate,
+                                 float* hostFrame);
 /* SVGF on the accumulator of the last LH2G_RP_FILTER frame (lib/RenderCore_Optix7Filter/rendercore.cpp:904-935):
  * prepareFilter (demodulation, reprojection, luminance moments), applyFilter phases 1-3 (temporal blend,
  * a-trous at steps 1, 2, 4, remodulation), then TAA + unsharpen or finalizeNoTAA into the frame buffer, whose
@@ -94,7 +103,7 @@ LH2G_API int lh2g_read_filter_buffer(lh2g_context* ctx, int slot, void* host);
  * parameters of that frame (either pointer may be NULL). */
 LH2G_API int lh2g_get_last_filter_frame(lh2g_context* ctx, lh2g_filter_params* filter, lh2g_view* jitteredView,
                                         lh2g_render_params* params);
-/* WaitForRender (core_api_base.h:99): blocks until the context's stream is idle. */
+/* WaitForRender (core_api_base.h:99): blocks until every frame and operation submitted on the context is done. */
 LH2G_API int lh2g_wait(lh2g_context* ctx);
 /* GetCoreStats (core_api_base.h:87). */
 LH2G_API int lh2g_get_stats(lh2g_context* ctx, lh2g_stats* out);
@@ -103,7 +112,12 @@ LH2G_API int lh2g_get_framebuffer(lh2g_context* ctx, void** devicePtr);
 LH2G_API int lh2g_read_framebuffer(lh2g_context* ctx, float* host);
 LH2G_API int lh2g_read_accumulator(lh2g_context* ctx, float* host);
 
-/* The context's CUDA stream (cudaStream_t), for callers that bracket frames with their own events. */
+/* The context's CUDA stream (cudaStream_t), for callers that bracket frames with their own events. Plain frames
+ * (lh2g_render / lh2g_render_ex without read-backs, lh2g_render_to_host; targets up to 8M paths) run on internal
+ * streams in turn (setting "pipelineFrames"), so that one frame's last waves overlap the next frame's first ones; they
+ * wait for work enqueued on the context stream before them, and this call orders the context stream after every
+ * frame submitted so far, so an event recorded on the returned stream afterwards completes after those frames.
+ * Every call that reads results or changes the scene or target does the same. */
 LH2G_API int lh2g_get_stream(lh2g_context* ctx, void** stream);
 /* Per-launch device timing of the next frames (enable != 0): lh2g_get_launch_times waits for the core's stream,
  * fills ms[k] with the duration of launch k of every frame rendered since timing was enabled or since its previous

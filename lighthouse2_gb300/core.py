@@ -41,7 +41,7 @@ FILTER_SLOTS = {"features": (0, np.uint32, 4), "worldPos": (1, np.float32, 4), "
                 "filteredOUT": (9, np.float32, 4), "prevPixels": (10, np.float32, 4), "accum": (11, np.float32, 4)}
 C_API = ["lh2g_create", "lh2g_destroy", "lh2g_last_error", "lh2g_set_geometry", "lh2g_set_instance", "lh2g_finalize_instances",
          "lh2g_set_materials", "lh2g_pack_materials", "lh2g_set_textures", "lh2g_set_lights", "lh2g_set_sky", "lh2g_setting",
-         "lh2g_set_target", "lh2g_set_probe", "lh2g_render", "lh2g_render_ex", "lh2g_wait", "lh2g_get_stats",
+         "lh2g_set_target", "lh2g_set_probe", "lh2g_render", "lh2g_render_ex", "lh2g_render_to_host", "lh2g_wait", "lh2g_get_stats",
          "lh2g_get_framebuffer", "lh2g_read_framebuffer", "lh2g_read_accumulator", "lh2g_trace", "lh2g_trace_host",
          "lh2g_get_stream", "lh2g_enable_launch_timing", "lh2g_get_launch_times", "lh2g_get_traversal_stats",
          "lh2g_render_noalloc", "lh2g_filter", "lh2g_read_filter_buffer", "lh2g_get_last_filter_frame",
@@ -84,6 +84,7 @@ def load_library(path: str | None = None):
     lib.lh2g_set_probe.argtypes = [vp, i, i]
     lib.lh2g_render.argtypes = [vp, vp, i]
     lib.lh2g_render_ex.argtypes = [vp, vp, vp, i, vp, vp, vp]
+    lib.lh2g_render_to_host.argtypes = [vp, vp, vp, i, vp]
     lib.lh2g_wait.argtypes = [vp]
     lib.lh2g_get_stats.argtypes = [vp, vp]
     lib.lh2g_get_framebuffer.argtypes = [vp, C.POINTER(vp)]
@@ -249,6 +250,12 @@ class RenderCore:
         if counters:
             out["counters"] = cnt
         return out
+
+    def render_to_host(self, view, params, host_ptr, accumulate=False):
+        """Queues a frame and the copy of its finalized image (W*H float4) into host memory at host_ptr (pinned for
+        overlap); the image is there after WaitForRender or any call that reads results."""
+        self._check(self.lib.lh2g_render_to_host(self.ctx, _p(np.ascontiguousarray(view)), _p(np.ascontiguousarray(params)), int(accumulate),
+                                                 C.c_void_p(host_ptr)), "render_to_host")
 
     def read_framebuffer(self):
         out = np.zeros((self.W * self.H, 4), np.float32)

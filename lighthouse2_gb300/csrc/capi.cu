@@ -198,7 +198,7 @@ struct lh2g_context {
     int blocksExtend = 0, blocksConnect = 0, blocksShade = 0, blocksTail = 0;
     /* path length from which the remaining paths run to their end in one persistent kernel (0: wave loop
      * to the end); a scheduling choice only, results are the same */
-    int tailDepth = 4;
+    int tailDepth = 5;
     /* SVGF (filter core) state: settings of lib/RenderCore_Optix7Filter/rendercore.h:32-35 (this core renders
      * the unfiltered PrimeRef estimator unless "filter" is set) */
     int filterEnabled = 0, taaEnabled = 1;
@@ -217,6 +217,28 @@ struct lh2g_context {
     NrcBuffers nrcBuf;
     lh2g_view lastJittered;
     lh2g_render_params lastParams;
+    /* Frame pipelining (setting "pipelineFrames" = frames in flight, default 3): plain frames rotate over lanes,
+     * each with its own stream and path-state buffers (lane 0 uses B's, the others their own), so that the sparse
+     * last waves of one frame overlap the first waves of the next. The accumulator and the frame are shared: finalizes run
+     * in submission order (finEv). A lane frame waits for everything enqueued on the context stream before it
+     * (forkEv); every other operation first orders the context stream after the lanes' frames (join_frames). */
+    struct Lane {
+        cudaStream_t st = nullptr;
+        WaveBuffers B;
+        Counters* hostCounters = nullptr;
+        cudaEvent_t ev[2] = {nullptr, nullptr};
+        cudaEvent_t done = nullptr;
+        bool pending = false;
+        bool ready = false;
+    };
+    static constexpr int MAX_LANES = 3;
+    Lane lanes[MAX_LANES];
+    int pipelineFrames = 3;            /* lanes in use; 0 or 1: one frame at a time */
+    int nextLane = 0;
+    int lastSlot = -1;                 /* lane of the last frame, -1: the context stream */
+    cudaEvent_t forkEv = nullptr, finEv = nullptr;
+    bool finValid = false;
+    static constexpr int64_t PIPE_MAX_PATHS = 8ll << 20;   /* larger targets render one frame at a time */
 };
 
 namespace {
@@ -237,6 +259,21 @@ int cuda_check(lh2g_context* c, cudaError_t e, const char* what) {
         if (_r != LH2G_OK) return _r;                                 \
     } while (0)
 
+/* orders the context stream after every lane frame submitted so far (no host wait) */
+int join_frames(lh2g_context* ctx) {
+    for (auto& L : ctx->lanes)
+        if (L.pending) {
+            CK(cudaStreamWaitEvent(ctx->st, L.done, 0));
+            L.pending = false;
+        }
+    return LH2G_OK;
+}
+#define JOIN()                                  \
+    do {                                        \
+        const int _j = join_frames(ctx);        \
+        if (_j != LH2G_OK) return _j;           \
+    } while (0)
+
 template <typename T>
 void dfree(T*& p) { if (p) cudaFree((void*)p); p = nullptr; }
 
@@ -254,7 +291,18 @@ void free_filter(lh2g_context* ctx) {
     ctx->havePrevView = false;
 }
 
+void free_lane_buffers(lh2g_context* ctx) {
+    for (int l = 1; l < lh2g_context::MAX_LANES; l++) {
+        WaveBuffers& B = ctx->lanes[l].B;
+        if (!ctx->lanes[l].ready) continue;
+        for (int k = 0; k < 2; k++) dfree(B.O[k]), dfree(B.D[k]), dfree(B.T[k]);
+        dfree(B.hits), dfree(B.shO), dfree(B.shD), dfree(B.shE), dfree(B.pathAcc), dfree(B.counters);
+        ctx->lanes[l].ready = false;
+    }
+}
+
 void free_target(lh2g_context* ctx) {
+    free_lane_buffers(ctx);
     WaveBuffers& B = ctx->B;
     for (int k = 0; k < 2; k++) dfree(B.O[k]), dfree(B.D[k]), dfree(B.T[k]);
     dfree(B.hits), dfree(B.shO), dfree(B.shD), dfree(B.shE), dfree(B.pathAcc), dfree(B.accum), dfree(B.frame), dfree(B.counters);
@@ -355,6 +403,8 @@ int lh2g_create(int device, lh2g_context** out) {
     if (r == LH2G_OK) r = cuda_check(ctx, cudaEventCreate(&ctx->ev[1]), "cudaEventCreate");
     if (r == LH2G_OK) r = cuda_check(ctx, cudaEventCreate(&ctx->fev[0]), "cudaEventCreate");
     if (r == LH2G_OK) r = cuda_check(ctx, cudaEventCreate(&ctx->fev[1]), "cudaEventCreate");
+    if (r == LH2G_OK) r = cuda_check(ctx, cudaEventCreateWithFlags(&ctx->forkEv, cudaEventDisableTiming), "cudaEventCreate");
+    if (r == LH2G_OK) r = cuda_check(ctx, cudaEventCreateWithFlags(&ctx->finEv, cudaEventDisableTiming), "cudaEventCreate");
     if (r != LH2G_OK) {
         fprintf(stderr, "lh2g_create: %s\n", ctx->err.c_str());
         delete ctx;
@@ -378,6 +428,8 @@ int lh2g_destroy(lh2g_context* ctx) {
     if (!ctx) return LH2G_ERR_INVALID;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->st);
+    for (auto& L : ctx->lanes)
+        if (L.st) cudaStreamSynchronize(L.st);
     for (MeshDev& m : ctx->meshes) dfree(m.verts), dfree(m.tris);
     dfree(ctx->mats), dfree(ctx->texels), dfree(ctx->triL), dfree(ctx->ptL), dfree(ctx->spL), dfree(ctx->dirL), dfree(ctx->sky);
     dfree(ctx->pool), dfree(ctx->triData), dfree(ctx->instGPU), dfree(ctx->tlasPrims), dfree(ctx->instTris), dfree(ctx->instInvRows);
@@ -390,6 +442,14 @@ int lh2g_destroy(lh2g_context* ctx) {
     if (ctx->fev[0]) cudaEventDestroy(ctx->fev[0]);
     if (ctx->fev[1]) cudaEventDestroy(ctx->fev[1]);
     for (cudaEvent_t e : ctx->lev) cudaEventDestroy(e);
+    for (auto& L : ctx->lanes) {
+        if (!L.st) continue;
+        cudaEventDestroy(L.ev[0]), cudaEventDestroy(L.ev[1]), cudaEventDestroy(L.done);
+        if (L.hostCounters) cudaFreeHost(L.hostCounters);
+        cudaStreamDestroy(L.st);
+    }
+    if (ctx->forkEv) cudaEventDestroy(ctx->forkEv);
+    if (ctx->finEv) cudaEventDestroy(ctx->finEv);
     cudaStreamDestroy(ctx->st);
     delete ctx;
     return LH2G_OK;
@@ -402,6 +462,7 @@ int lh2g_set_geometry(lh2g_context* ctx, int meshIdx, const float* v4, int verte
     if (meshIdx < 0 || meshIdx > (int)ctx->meshes.size() || triangleCount < 0 || vertexCount != 3 * triangleCount || (triangleCount && (!v4 || !tris)))
         return fail(ctx, LH2G_ERR_INVALID, "set_geometry: meshes must arrive in index order with 3 vertices per triangle");
     if (triangleCount >= (1 << 28)) return fail(ctx, LH2G_ERR_INVALID, "set_geometry: at most 2^28 triangles per mesh");
+    JOIN();   /* frames in flight read the scene */
     cudaSetDevice(ctx->device);
     if (meshIdx == (int)ctx->meshes.size()) ctx->meshes.emplace_back();
     MeshDev& m = ctx->meshes[meshIdx];
@@ -438,6 +499,7 @@ int lh2g_set_instance(lh2g_context* ctx, int instIdx, int meshIdx, const float* 
 int lh2g_finalize_instances(lh2g_context* ctx) {
     if (!ctx) return LH2G_ERR_INVALID;
     cudaSetDevice(ctx->device);
+    JOIN();
     for (const InstHost& in : ctx->inst)
         if (in.mesh >= (int)ctx->meshes.size()) return fail(ctx, LH2G_ERR_INVALID, "finalize: instance of a mesh that was never set");
     const auto t0 = std::chrono::high_resolution_clock::now();
@@ -540,6 +602,7 @@ int lh2g_pack_materials(const lh2g_material* mats, int count, const lh2g_texture
 int lh2g_set_textures(lh2g_context* ctx, const lh2g_texture* tex, int count) {
     if (!ctx || count < 0 || (count && !tex)) return LH2G_ERR_INVALID;
     cudaSetDevice(ctx->device);
+    JOIN();
     ctx->texFirst.clear(), ctx->texWH.clear();
     size_t total = 0, slack = 64;
     for (int i = 0; i < count; i++) {
@@ -559,6 +622,7 @@ int lh2g_set_textures(lh2g_context* ctx, const lh2g_texture* tex, int count) {
 int lh2g_set_materials(lh2g_context* ctx, const lh2g_material* mats, int count) {
     if (!ctx || count < 0 || (count && !mats)) return LH2G_ERR_INVALID;
     cudaSetDevice(ctx->device);
+    JOIN();
     std::vector<lh2g_gpu_material> packed(std::max(count, 1));
     for (int i = 0; i < count; i++) {
         const lh2g_map_ref* refs[6] = {&mats[i].color_map, &mats[i].detail_color_map, &mats[i].normal_map, &mats[i].detail_normal_map, &mats[i].specular_map, &mats[i].roughness_map};
@@ -578,6 +642,7 @@ int lh2g_set_lights(lh2g_context* ctx, const lh2g_light_tri* tri, int ntri, cons
     if (!ctx || ntri < 0 || npt < 0 || nspot < 0 || ndir < 0) return LH2G_ERR_INVALID;
     if (ntri + npt + nspot + ndir > 64) return fail(ctx, LH2G_ERR_INVALID, "set_lights: at most 64 lights (MAXISLIGHTS)");
     cudaSetDevice(ctx->device);
+    JOIN();
     CK(dalloc(ctx->triL, (size_t)6 * std::max(ntri, 1)));
     CK(dalloc(ctx->ptL, (size_t)2 * std::max(npt, 1)));
     CK(dalloc(ctx->spL, (size_t)3 * std::max(nspot, 1)));
@@ -594,6 +659,7 @@ int lh2g_set_lights(lh2g_context* ctx, const lh2g_light_tri* tri, int ntri, cons
 int lh2g_set_sky(lh2g_context* ctx, const float* rgb, int w, int h, const float* m16) {
     if (!ctx || w < 0 || h < 0 || ((size_t)w * h && !rgb)) return LH2G_ERR_INVALID;
     cudaSetDevice(ctx->device);
+    JOIN();
     std::vector<float4> px((size_t)std::max(1, w * h));
     for (size_t i = 0; i < (size_t)w * h; i++) px[i] = make_float4(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2], 0.0f);
     CK(dalloc(ctx->sky, px.size()));
@@ -622,6 +688,12 @@ int lh2g_setting(lh2g_context* ctx, const char* name, float value) {
     else if (!strcmp(name, "clampIndirect")) ctx->clampIndirect = value;
     else if (!strcmp(name, "filter")) ctx->filterEnabled = value == 0 ? 0 : 1;
     else if (!strcmp(name, "TAA")) ctx->taaEnabled = value == 0 ? 0 : 1;
+    else if (!strcmp(name, "pipelineFrames")) {
+        if (value < 0 || value > lh2g_context::MAX_LANES) return fail(ctx, LH2G_ERR_INVALID, "setting pipelineFrames: 0..3 frames in flight");
+        JOIN();
+        ctx->pipelineFrames = (int)value;
+        ctx->nextLane = 0;
+    }
     /* other names are accepted and ignored, as the reference cores ignore settings they do not know
      * (rendercore.cpp:484-502) */
     return LH2G_OK;
@@ -632,6 +704,7 @@ int lh2g_set_target(lh2g_context* ctx, int w, int h, int spp) {
     const int64_t P = (int64_t)w * h * spp;
     if (P >= (1ll << 31)) return fail(ctx, LH2G_ERR_INVALID, "set_target: more than 2^31 paths");
     cudaSetDevice(ctx->device);
+    JOIN();
     CK(cudaStreamSynchronize(ctx->st));
     if (P > ctx->cap || (int64_t)w * h != (int64_t)ctx->W * ctx->H) {
         free_target(ctx);
@@ -692,8 +765,40 @@ int ensure_nrc(lh2g_context* ctx) {
     return LH2G_OK;
 }
 
+/* the stream, events and pinned counters of lane l; lanes above 0 also get their own path-state buffers */
+int ensure_lane(lh2g_context* ctx, int l) {
+    auto& L = ctx->lanes[l];
+    if (!L.st) {
+        CK(cudaStreamCreateWithFlags(&L.st, cudaStreamNonBlocking));
+        CK(cudaEventCreate(&L.ev[0]));
+        CK(cudaEventCreate(&L.ev[1]));
+        CK(cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming));
+        CK(cudaMallocHost((void**)&L.hostCounters, sizeof(Counters)));
+    }
+    if (l > 0 && !L.ready) {
+        memset(&L.B, 0, sizeof(L.B));
+        const size_t P = (size_t)ctx->cap;
+        WaveBuffers& B = L.B;
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < 2 && e == cudaSuccess; k++) {
+            if ((e = dalloc(B.O[k], P))) break;
+            if ((e = dalloc(B.D[k], P))) break;
+            e = dalloc(B.T[k], P);
+        }
+        if (!e) e = dalloc(B.hits, P);
+        if (!e) e = dalloc(B.shO, P);
+        if (!e) e = dalloc(B.shD, P);
+        if (!e) e = dalloc(B.shE, P);
+        if (!e) e = dalloc(B.pathAcc, P);
+        if (!e) e = dalloc(B.counters, 1);
+        if (e) { free_lane_buffers(ctx); return cuda_check(ctx, e, "frame lane buffers"); }
+        L.ready = true;
+    }
+    return LH2G_OK;
+}
+
 int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* p, int accumulate, lh2g_hit* capHits, uint32_t* capSeeds,
-                 uint32_t* countersOut, const FinalizeHook* hook) {
+                 uint32_t* countersOut, const FinalizeHook* hook, float* hostFrame = nullptr) {
     if (!ctx || !view || !p) return LH2G_ERR_INVALID;
     if (!ctx->finalized) return fail(ctx, LH2G_ERR_STATE, "render: scene not finalized (call lh2g_finalize_instances)");
     if (!ctx->cap) return fail(ctx, LH2G_ERR_STATE, "render: no target (call lh2g_set_target)");
@@ -703,6 +808,11 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
     cudaSetDevice(ctx->device);
     const bool filt = (p->flags & LH2G_RP_FILTER) != 0, nrcFrame = (p->flags & LH2G_RP_NRC) != 0;
     if (filt && nrcFrame) return fail(ctx, LH2G_ERR_INVALID, "render: filter and radiance-cache frames do not combine");
+    /* plain frames without host read-backs go to the next lane; everything else runs on the context stream after
+     * the lanes' frames */
+    const bool pipe = ctx->pipelineFrames > 1 && !filt && !nrcFrame && !capHits && !capSeeds && !countersOut && !hook &&
+                      ctx->cap <= lh2g_context::PIPE_MAX_PATHS;
+    if (!pipe) JOIN();
     if (filt) {
         const int r = ensure_filter(ctx);
         if (r != LH2G_OK) return r;
@@ -711,9 +821,27 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
         const int r = ensure_nrc(ctx);
         if (r != LH2G_OK) return r;
     }
+    cudaStream_t st = ctx->st;
+    Counters* hostCounters = ctx->hostCounters;
+    cudaEvent_t* fev = ctx->ev;
+    WaveBuffers B = ctx->B;
+    int slot = -1;
+    if (pipe) {
+        slot = ctx->nextLane;
+        const int r = ensure_lane(ctx, slot);
+        if (r != LH2G_OK) return r;
+        auto& L = ctx->lanes[slot];
+        st = L.st, hostCounters = L.hostCounters, fev = L.ev;
+        if (slot > 0) {
+            for (int k = 0; k < 2; k++) B.O[k] = L.B.O[k], B.D[k] = L.B.D[k], B.T[k] = L.B.T[k];
+            B.hits = L.B.hits, B.shO = L.B.shO, B.shD = L.B.shD, B.shE = L.B.shE, B.pathAcc = L.B.pathAcc, B.counters = L.B.counters;
+        }
+        CK(cudaEventRecord(ctx->forkEv, ctx->st));
+        CK(cudaStreamWaitEvent(st, ctx->forkEv, 0));
+        ctx->nextLane = (ctx->nextLane + 1) % ctx->pipelineFrames;
+    }
     FrameGPU F = frame_of(view, p);
     F.stride = ctx->cap;
-    WaveBuffers B = ctx->B;
     B.capHits = nullptr, B.capSeeds = nullptr;
     B.features = filt ? ctx->sv.features : nullptr;
     B.worldPos = filt ? ctx->sv.worldPos : nullptr;
@@ -729,8 +857,10 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
         B.capHits = ctx->B.capHits, B.capSeeds = ctx->B.capSeeds;
     }
     const SceneGPU S = scene_of(ctx);
-    if (!accumulate) CK(cudaMemsetAsync(B.accum, 0, sizeof(float4) * (size_t)F.W * F.H * (filt ? 2 : 1), ctx->st));
-    CK(cudaMemsetAsync(B.counters, 0, sizeof(Counters), ctx->st));
+    /* a frame that does not accumulate overwrites the accumulator in its finalize (filter frames clear both halves
+     * here, on the context stream) */
+    if (!accumulate && filt) CK(cudaMemsetAsync(B.accum, 0, sizeof(float4) * (size_t)F.W * F.H * 2, st));
+    CK(cudaMemsetAsync(B.counters, 0, sizeof(Counters), st));
     const int waves = ctx->tailDepth > 0 ? std::min(F.maxDepth, ctx->tailDepth - 1) : F.maxDepth;
     const bool tail = waves < F.maxDepth;
     const int launches = 2 + 3 * waves + (tail ? 1 : 0);
@@ -743,33 +873,42 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
             ctx->lev.push_back(e);
         }
     int li = 2 * ctx->timedLaunches;
-    auto mark = [&]() { if (timing) cudaEventRecord(ctx->lev[li++], ctx->st); };
-    CK(cudaEventRecord(ctx->ev[0], ctx->st));
-    mark(), launch_generate(F, B, ctx->st), mark();
+    auto mark = [&]() { if (timing) cudaEventRecord(ctx->lev[li++], st); };
+    CK(cudaEventRecord(fev[0], st));
+    mark(), launch_generate(F, B, st), mark();
     for (int d = 1; d <= waves; d++) {
-        mark(), launch_extend(S, F, B, d, ctx->blocksExtend, ctx->st), mark();
-        mark(), launch_shade(S, F, B, d, ctx->blocksShade, ctx->st), mark();
-        mark(), launch_connect(S, F, B, d, ctx->blocksConnect, ctx->st), mark();
+        mark(), launch_extend(S, F, B, d, ctx->blocksExtend, st), mark();
+        mark(), launch_shade(S, F, B, d, ctx->blocksShade, st), mark();
+        mark(), launch_connect(S, F, B, d, ctx->blocksConnect, st), mark();
     }
-    if (tail) mark(), launch_tail(S, F, B, waves + 1, ctx->blocksTail, ctx->st), mark();
+    if (tail) mark(), launch_tail(S, F, B, waves + 1, ctx->blocksTail, st), mark();
     if (hook) {
         const int r = (*hook)(F, B);
         if (r != LH2G_OK) return r;
     }
     const int after = p->samplesTaken + F.spp;
-    mark(), launch_finalize(F, B, 1.0f / (float)after, ctx->st), mark();
+    if (pipe && ctx->finValid) CK(cudaStreamWaitEvent(st, ctx->finEv, 0));   /* the previous frame's finalize first */
+    mark(), launch_finalize(F, B, 1.0f / (float)after, !accumulate && !filt, st), mark();
+    /* the frame to the caller's host buffer, before the next frame's finalize overwrites it */
+    if (hostFrame) CK(cudaMemcpyAsync(hostFrame, B.frame, sizeof(float4) * (size_t)F.W * F.H, cudaMemcpyDeviceToHost, st));
+    CK(cudaEventRecord(ctx->finEv, st));
+    ctx->finValid = true;
     if (timing) ctx->timedLaunches += launches;
     CK(cudaGetLastError());
-    CK(cudaEventRecord(ctx->ev[1], ctx->st));
-    CK(cudaMemcpyAsync(ctx->hostCounters, B.counters, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->st));
-    ctx->statsPending = true, ctx->lastDepth = F.maxDepth, ctx->lastP = F.P;
+    CK(cudaEventRecord(fev[1], st));
+    CK(cudaMemcpyAsync(hostCounters, B.counters, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+    ctx->statsPending = true, ctx->lastDepth = F.maxDepth, ctx->lastP = F.P, ctx->lastSlot = slot;
+    if (pipe) {
+        CK(cudaEventRecord(ctx->lanes[slot].done, st));
+        ctx->lanes[slot].pending = true;
+    }
     if (capHits || capSeeds || countersOut) {
-        CK(cudaStreamSynchronize(ctx->st));
+        CK(cudaStreamSynchronize(st));
         if (capHits) CK(cudaMemcpy(capHits, ctx->B.capHits, sizeof(lh2g_hit) * capN, cudaMemcpyDeviceToHost));
         if (capSeeds) CK(cudaMemcpy(capSeeds, ctx->B.capSeeds, sizeof(uint32_t) * capN, cudaMemcpyDeviceToHost));
         if (countersOut)
-            for (int d = 0; d < F.maxDepth; d++) countersOut[2 * d] = ctx->hostCounters->extension[d], countersOut[2 * d + 1] = ctx->hostCounters->shadow[d];
-        if (ctx->hostCounters->status) return fail(ctx, LH2G_ERR_OVERFLOW, "render: traversal stack overflow or step limit");
+            for (int d = 0; d < F.maxDepth; d++) countersOut[2 * d] = hostCounters->extension[d], countersOut[2 * d + 1] = hostCounters->shadow[d];
+        if (hostCounters->status) return fail(ctx, LH2G_ERR_OVERFLOW, "render: traversal stack overflow or step limit");
     }
     return LH2G_OK;
 }
@@ -781,6 +920,12 @@ extern "C" {
 int lh2g_render_ex(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* p, int accumulate, lh2g_hit* capHits, uint32_t* capSeeds,
                    uint32_t* countersOut) {
     return render_frame(ctx, view, p, accumulate, capHits, capSeeds, countersOut, nullptr);
+}
+
+int lh2g_render_to_host(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* p, int accumulate, float* hostFrame) {
+    if (!hostFrame) return LH2G_ERR_INVALID;
+    if (p && (p->flags & LH2G_RP_FILTER)) return fail(ctx, LH2G_ERR_INVALID, "render_to_host: filter frames are presented by lh2g_filter");
+    return render_frame(ctx, view, p, accumulate, nullptr, nullptr, nullptr, nullptr, hostFrame);
 }
 
 int lh2g_render_nrc(lh2g_context* ctx, lh2g_nrc* cache, const lh2g_view* view, const lh2g_render_params* params, int accumulate, int train,
@@ -868,6 +1013,7 @@ int lh2g_filter(lh2g_context* ctx, const lh2g_filter_params* fp) {
     if (!ctx->svAlloc) return fail(ctx, LH2G_ERR_STATE, "filter: no filter-core frame rendered on this target");
     if (fp->samplesTaken <= 0) return fail(ctx, LH2G_ERR_INVALID, "filter: samplesTaken must be positive");
     cudaSetDevice(ctx->device);
+    JOIN();
     SvgfBuffers b = ctx->sv;
     b.accum = ctx->B.accum, b.target = ctx->B.frame;
     SvgfArgs a;
@@ -894,6 +1040,7 @@ int lh2g_filter(lh2g_context* ctx, const lh2g_filter_params* fp) {
 int lh2g_read_filter_buffer(lh2g_context* ctx, int slot, void* host) {
     if (!ctx || !host || slot < 0 || slot >= LH2G_FB_COUNT) return LH2G_ERR_INVALID;
     if (!ctx->svAlloc) return fail(ctx, LH2G_ERR_STATE, "read_filter_buffer: no filter buffers");
+    JOIN();
     const size_t WH = (size_t)ctx->W * ctx->H;
     const SvgfBuffers& v = ctx->sv;
     const void* src = nullptr;
@@ -951,15 +1098,18 @@ int lh2g_render(lh2g_context* ctx, const lh2g_view* view, int converge) {
 
 int lh2g_wait(lh2g_context* ctx) {
     if (!ctx) return LH2G_ERR_INVALID;
+    JOIN();
     CK(cudaStreamSynchronize(ctx->st));
     return LH2G_OK;
 }
 
 int lh2g_get_stats(lh2g_context* ctx, lh2g_stats* out) {
     if (!ctx || !out) return LH2G_ERR_INVALID;
+    JOIN();
     if (ctx->statsPending) {
         CK(cudaStreamSynchronize(ctx->st));
-        const Counters& C = *ctx->hostCounters;
+        const bool lane = ctx->lastSlot >= 0;
+        const Counters& C = lane ? *ctx->lanes[ctx->lastSlot].hostCounters : *ctx->hostCounters;
         uint32_t ext = (uint32_t)ctx->lastP, sh = 0;
         for (int d = 0; d < ctx->lastDepth; d++) ext += C.extension[d], sh += C.shadow[d];
         ctx->stats.totalExtensionRays = ext, ctx->stats.totalShadowRays = sh, ctx->stats.totalRays = ext + sh;
@@ -969,7 +1119,8 @@ int lh2g_get_stats(lh2g_context* ctx, lh2g_stats* out) {
         for (int d = 1; d < ctx->lastDepth - 1; d++) deep += C.extension[d];
         ctx->stats.deepRayCount = deep;
         float ms = 0;
-        cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+        cudaEvent_t* fev = lane ? ctx->lanes[ctx->lastSlot].ev : ctx->ev;
+        cudaEventElapsedTime(&ms, fev[0], fev[1]);
         ctx->stats.renderTime = ms;
         ctx->stats.deviceStatus = C.status;
         ctx->statsPending = false;
@@ -988,6 +1139,7 @@ int lh2g_get_stats(lh2g_context* ctx, lh2g_stats* out) {
 int lh2g_get_framebuffer(lh2g_context* ctx, void** dev) {
     if (!ctx || !dev) return LH2G_ERR_INVALID;
     if (!ctx->cap) return fail(ctx, LH2G_ERR_STATE, "no target");
+    JOIN();
     *dev = ctx->B.frame;
     return LH2G_OK;
 }
@@ -995,6 +1147,7 @@ int lh2g_get_framebuffer(lh2g_context* ctx, void** dev) {
 int lh2g_read_framebuffer(lh2g_context* ctx, float* host) {
     if (!ctx || !host) return LH2G_ERR_INVALID;
     if (!ctx->cap) return fail(ctx, LH2G_ERR_STATE, "no target");
+    JOIN();
     CK(cudaMemcpyAsync(host, ctx->B.frame, sizeof(float4) * (size_t)ctx->W * ctx->H, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     return LH2G_OK;
@@ -1004,6 +1157,7 @@ int lh2g_read_accumulator(lh2g_context* ctx, float* host) {
     if (!ctx || !host) return LH2G_ERR_INVALID;
     if (!ctx->cap) return fail(ctx, LH2G_ERR_STATE, "no target");
     /* the direct half only when filter frames split it (LH2G_FB_ACCUM reads both) */
+    JOIN();
     CK(cudaMemcpyAsync(host, ctx->B.accum, sizeof(float4) * (size_t)ctx->W * ctx->H, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     return LH2G_OK;
@@ -1011,13 +1165,16 @@ int lh2g_read_accumulator(lh2g_context* ctx, float* host) {
 
 int lh2g_get_traversal_stats(lh2g_context* ctx, unsigned long long* out4) {
     if (!ctx || !out4) return LH2G_ERR_INVALID;
+    JOIN();
     CK(cudaStreamSynchronize(ctx->st));
-    for (int k = 0; k < 4; k++) out4[k] = ctx->hostCounters->travStats[k];
+    const Counters* C = ctx->lastSlot >= 0 ? ctx->lanes[ctx->lastSlot].hostCounters : ctx->hostCounters;
+    for (int k = 0; k < 4; k++) out4[k] = C->travStats[k];
     return LH2G_OK;
 }
 
 int lh2g_get_stream(lh2g_context* ctx, void** stream) {
     if (!ctx || !stream) return LH2G_ERR_INVALID;
+    JOIN();
     *stream = (void*)ctx->st;
     return LH2G_OK;
 }
@@ -1031,6 +1188,7 @@ int lh2g_enable_launch_timing(lh2g_context* ctx, int enable) {
 
 int lh2g_get_launch_times(lh2g_context* ctx, float* ms, int capacity, int* count) {
     if (!ctx || !count || (capacity > 0 && !ms)) return LH2G_ERR_INVALID;
+    JOIN();
     CK(cudaStreamSynchronize(ctx->st));
     *count = ctx->timedLaunches;
     for (int k = 0; k < ctx->timedLaunches && k < capacity; k++) {

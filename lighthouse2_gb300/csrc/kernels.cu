@@ -240,13 +240,14 @@ __global__ void k_nrc_apply(const FrameGPU F, const WaveBuffers B, const float4*
 }
 
 /* -------------------------------------------------------------------------------------------------- */
-__global__ void k_finalize(const FrameGPU F, const WaveBuffers B, const float scale) {
+/* overwrite: the accumulator starts from zero (a frame that does not accumulate) instead of its stored sum */
+__global__ void k_finalize(const FrameGPU F, const WaveBuffers B, const float scale, const int overwrite) {
     const int64_t px = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t WH = (int64_t)F.W * F.H;
     if (px >= WH) return;
     const bool filt = (F.flags & LH2G_RP_FILTER) != 0;
     for (int half = 0; half < (filt ? 2 : 1); half++) {
-        float4 acc = B.accum[half * WH + px];
+        float4 acc = overwrite ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : B.accum[half * WH + px];
         for (int s = 0; s < F.spp; s++) {
             const float4 v = B.pathAcc[half * F.P + s * WH + px];
             acc.x += v.x, acc.y += v.y, acc.z += v.z, acc.w += v.w;
@@ -366,9 +367,9 @@ void launch_nrc_collect(const FrameGPU& F, const WaveBuffers& B, float4* queries
 void launch_nrc_apply(const FrameGPU& F, const WaveBuffers& B, const float4* pred, const uint32_t* qPath, const uint32_t* counts, cudaStream_t st) {
     k_nrc_apply<<<sm_count() * 8, 256, 0, st>>>(F, B, pred, qPath, counts);
 }
-void launch_finalize(const FrameGPU& F, const WaveBuffers& B, float scale, cudaStream_t st) {
+void launch_finalize(const FrameGPU& F, const WaveBuffers& B, float scale, int overwrite, cudaStream_t st) {
     const int64_t WH = (int64_t)F.W * F.H;
-    k_finalize<<<(unsigned)((WH + 255) / 256), 256, 0, st>>>(F, B, scale);
+    k_finalize<<<(unsigned)((WH + 255) / 256), 256, 0, st>>>(F, B, scale, overwrite);
 }
 void launch_trace(const SceneGPU& S, const lh2g_ray* rays, void* out, long long n, int mode, uint32_t* fetch, uint32_t* status, int blocks, cudaStream_t st) {
     if (mode == 1) k_trace<1><<<blocks, 128, 0, st>>>(S, rays, out, n, fetch, status);

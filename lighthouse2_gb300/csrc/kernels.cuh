@@ -32,7 +32,8 @@ void launch_shade(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, in
 void launch_connect(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int persistentBlocks, cudaStream_t st);
 /* path lengths startDepth..maxDepth of the frame's remaining paths, one persistent launch */
 void launch_tail(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int startDepth, int persistentBlocks, cudaStream_t st);
-void launch_finalize(const FrameGPU& F, const WaveBuffers& B, float scale, cudaStream_t st);
+/* per-pixel sums of the frame's paths into the accumulator (from zero when overwrite != 0), then the frame */
+void launch_finalize(const FrameGPU& F, const WaveBuffers& B, float scale, int overwrite, cudaStream_t st);
 /* radiance-cache frames: gather queries / training samples (counts[0], counts[1]), then add the predictions */
 void launch_nrc_collect(const FrameGPU& F, const WaveBuffers& B, float4* queries, uint32_t* qPath, float4* trainQ, float4* trainT, uint32_t* counts,
                         uint32_t trainCap, cudaStream_t st);

@@ -101,7 +101,7 @@ extern "C" LH2G_API int lh2g_render_noalloc(lh2g_context* ctx, const lh2g_view* 
         launch_connect(S, F, B, d, blocks[1], st);
     }
     if (waves < F.maxDepth) launch_tail(S, F, B, waves + 1, blocks[3], st);
-    launch_finalize(F, B, 1.0f / (float)(p->samplesTaken + F.spp), st);
+    launch_finalize(F, B, 1.0f / (float)(p->samplesTaken + F.spp), 0, st);
     const cudaError_t e = cudaGetLastError();
     if (current != device) cudaSetDevice(current);
     return e == cudaSuccess ? LH2G_OK : LH2G_ERR_CUDA;

@@ -33,6 +33,10 @@ namespace lh2g {
 #ifndef LH2G_REFILL
 #define LH2G_REFILL 0
 #endif
+/* with LH2G_REFILL: idle lanes of a warp take new rays once at least this many are idle (or all are) */
+#ifndef LH2G_REFILL_MIN
+#define LH2G_REFILL_MIN 1
+#endif
 constexpr float BOX_MARGIN = 1.52587890625e-05f;
 constexpr uint32_t ENTRY_MARKER = 0xffffffffu;
 constexpr uint32_t MAX_STEPS = 1u << 20;   /* far beyond any traversal of a well-formed tree */
@@ -155,17 +159,27 @@ struct Traversal {
             cx(key[2], key[4]), cx(key[3], key[5]);
             cx(key[1], key[2]), cx(key[3], key[4]), cx(key[5], key[6]);
         }
+        /* leaf code = kind | (count - 1) << 28 | first slot; the fields do not overlap, so it is a sum */
+        const uint32_t leafBase = (curInst < 0 ? 0x80000000u : 0x40000000u) - (1u << 28) + n1.y;
+        if (sp + 8 <= LH2G_STACK) {
 #pragma unroll
-        for (int k = 7; k >= 0; k--) {
-            const uint32_t kk = key[k];
-            if (kk == 0xffffffffu) continue;
-            const uint32_t slot = kk & 7u;
-            const uint32_t meta = ((slot < 4 ? metaLo : metaHi) >> ((slot & 3u) * 8u)) & 255u;
-            uint32_t code;
-            if (meta & 0x80u) code = n1.x + (meta & 7u);
-            else code = (curInst < 0 ? 0x80000000u : 0x40000000u) | (((meta >> 5) - 1u) << 28) | (n1.y + (meta & 31u));
-            if (sp < LH2G_STACK) stack[sp++] = make_uint2(code, kk & ~7u);
-            else status |= LH2G_STATUS_STACK_OVERFLOW;
+            for (int k = 7; k >= 0; k--) {
+                const uint32_t kk = key[k];
+                if (kk == 0xffffffffu) continue;
+                const uint32_t meta = __byte_perm(metaLo, metaHi, kk & 7u) & 255u;   /* byte (slot) of the 8 meta bytes */
+                const uint32_t code = (meta & 0x80u) ? n1.x + (meta & 7u) : leafBase + ((meta >> 5) << 28) + (meta & 31u);
+                stack[sp++] = make_uint2(code, kk & ~7u);
+            }
+        } else {
+#pragma unroll
+            for (int k = 7; k >= 0; k--) {
+                const uint32_t kk = key[k];
+                if (kk == 0xffffffffu) continue;
+                const uint32_t meta = __byte_perm(metaLo, metaHi, kk & 7u) & 255u;
+                const uint32_t code = (meta & 0x80u) ? n1.x + (meta & 7u) : leafBase + ((meta >> 5) << 28) + (meta & 31u);
+                if (sp < LH2G_STACK) stack[sp++] = make_uint2(code, kk & ~7u);
+                else status |= LH2G_STATUS_STACK_OVERFLOW;
+            }
         }
         nodes++;
     }
@@ -482,7 +496,7 @@ LH2G_DEV void trace_queue(const SceneGPU& S, uint32_t* fetch, const uint32_t cou
     for (;;) {
         if (!exhausted) {
             const uint32_t need = __ballot_sync(0xffffffffu, !active);
-            if (need) {
+            if (need && (__popc(need) >= LH2G_REFILL_MIN || need == 0xffffffffu)) {
                 const int leader = __ffs(need) - 1;
                 uint32_t base = 0;
                 if ((int)lane == leader) base = atomicAdd(fetch, (uint32_t)__popc(need));

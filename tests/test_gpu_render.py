@@ -119,4 +119,44 @@ def test_wave_tail_split_changes_nothing(cornell, tail):
         acc = _check_frame(core, o, view, p)
         assert np.array_equal(acc, o.render(view, p)["accum"])
     finally:
-        core.Setting("waveTail", 4)
+        core.Setting("waveTail", 5)
+
+
+def test_pipelined_frames_match_one_at_a_time(core_lib):
+    """Consecutive plain frames overlap on two or three lanes (setting "pipelineFrames"); the accumulator, the frame and the
+    statistics must equal those of the same frames rendered one at a time, whether frames accumulate, restart or
+    converge through Render, and whatever is read between them."""
+    sc = S.spheres_2m(seed=5, n_spheres=6, slices=40, stacks=26, tex_size=64)
+    W, H = 160, 96
+    results = {}
+    for pipe in (0, 2, 3):
+        core = RenderCore()
+        core.set_scene(sc)
+        core.SetTarget(W, H, 1)
+        core.Setting("pipelineFrames", pipe)
+        core.Setting("maxDepth", 6)
+        out = []
+        for k in range(7):
+            view = S.spheres_view(W, H, frame=k % 3)
+            p = make_params(W, H, 1, max_depth=6, rr_start=3, samples_taken=k, camera_r0=camera_r0(k), flags=RP_NEE | RP_DEPTH_W)
+            core.render_ex(view, p, accumulate=k % 3 != 0, counters=False)
+            if k % 2 == 1:
+                out.append(core.read_accumulator().copy())
+        stats = core.GetCoreStats()
+        out.append(core.read_framebuffer().copy())
+        for k in range(4):   # Render: restart, then converge
+            core.Render(S.spheres_view(W, H, frame=1), converge=1 if k == 0 else 0)
+        out.append(core.read_framebuffer().copy())
+        out.append(np.array([stats["totalRays"], stats["totalShadowRays"]], np.float32))
+        # frames copied to host memory as they finish (lh2g_render_to_host), several in flight
+        hosts = [np.full((W * H, 4), np.nan, np.float32) for _ in range(3)]
+        for k in range(3):
+            p = make_params(W, H, 1, max_depth=6, rr_start=3, samples_taken=k, camera_r0=camera_r0(k), flags=RP_NEE | RP_DEPTH_W)
+            core.render_to_host(S.spheres_view(W, H, frame=k), p, hosts[k].ctypes.data, accumulate=k > 0)
+        core.WaitForRender()
+        out += hosts
+        results[pipe] = out
+        core.close()
+    for lanes in (2, 3):
+        for a, b in zip(results[0], results[lanes]):
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
