@@ -41,6 +41,9 @@ W_DEFAULT, H_DEFAULT = 1920, 1080
 MAX_DEPTH, RR_START = 8, 4
 WAVE_TAIL = 5          # path lengths >= 5 run in the persistent tail kernel (setting "waveTail")
 LANES = 3              # frames in flight (setting "pipelineFrames")
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of two k_extend launches of this workload (waves 2 and 3 of
+# camera pose 1): 190.11 MB + 72.66 MB (profiles/k_extend_spheres_2m_1080p.md)
+EXTEND_CAPTURE = {"pose": 1, "waves": (2, 3), "dram_bytes": 190.109184e6 + 72.664832e6}
 WORKLOAD = "spheres_2m: 64 x 32k-tri displaced spheres + ground (2,048,002 tris, 66 instances), 16 quad + 4 point lights, " \
            "20 materials (4 textured), sky; 1920x1080 1spp, max depth 8, RR after depth 3, NEE"
 METRIC = "Mrays/s @1080p 1spp"
@@ -189,6 +192,35 @@ def algorithmic_bytes(kind, n_in, n_ext, n_shadow):
 SVGF_BYTES_PER_PIXEL = (96 + 56) + (64 + 56 + 16) + 2 * (64 + 16) + (40 + 16) + (16 + 16)
 
 
+def decode_launches(lt_all, frames, counts, waves, W, H):
+    """Per stage kind: [summed launch ms, algorithmic bytes, launches] over `frames` frames whose per-launch device
+    times are lt_all (per frame: generate, (extend, shade, connect) x waves, tail if used, finalize) and whose
+    per-depth queue sizes are counts[frame % 8]."""
+    per_frame = 2 + 3 * waves + (1 if waves < MAX_DEPTH else 0)
+    per_kind = {k: [0.0, 0, 0] for k in ("extend", "shade", "connect", "tail", "generate", "finalize")}
+    for k in range(frames):
+        c = counts[k % 8]
+        lt = lt_all[k * per_frame:(k + 1) * per_frame]
+        n_in = [W * H] + [int(x) for x in c[:-1, 0]]
+        per_kind["generate"][0] += lt[0]
+        per_kind["finalize"][0] += lt[-1]
+        for d in range(waves):
+            te, ts, tc = lt[1 + 3 * d], lt[2 + 3 * d], lt[3 + 3 * d]
+            for kind, t, b in (("extend", te, algorithmic_bytes("extend", n_in[d], 0, 0)),
+                               ("shade", ts, algorithmic_bytes("shade", n_in[d], int(c[d, 0]), int(c[d, 1]))),
+                               ("connect", tc, algorithmic_bytes("connect", int(c[d, 1]), 0, 0))):
+                per_kind[kind][0] += t
+                per_kind[kind][1] += b
+                per_kind[kind][2] += 1
+        if waves < MAX_DEPTH:   # the tail kernel: every remaining path vertex is traced, shaded and connected
+            b = sum(algorithmic_bytes("extend", n_in[d], 0, 0) + algorithmic_bytes("shade", n_in[d], int(c[d, 0]), int(c[d, 1])) +
+                    algorithmic_bytes("connect", int(c[d, 1]), 0, 0) for d in range(waves, MAX_DEPTH))
+            per_kind["tail"][0] += lt[1 + 3 * waves]
+            per_kind["tail"][1] += b
+            per_kind["tail"][2] += 1
+    return per_kind
+
+
 def svgf_leg(core, W, H, steps, warmup):
     """Filter-core frames with SVGF + TAA over the 8-pose camera path (Restart every frame, as a moving camera
     does); the filter passes are timed by the core's own events (coreStats.filterTime)."""
@@ -218,9 +250,9 @@ def svgf_leg(core, W, H, steps, warmup):
 
 SERVING_MIXES = {
     # the survey's job distribution: resolution in {256^2, 512^2, 1024^2, 1920x1080}, spp in {1, 4, 16}
-    "full": {"res": [(256, 256), (512, 512), (1024, 1024), (1920, 1080)], "spp": [1, 4, 16], "rates": [10, 25, 50, 100, 200, 500]},
+    "full": {"res": [(256, 256), (512, 512), (1024, 1024), (1920, 1080)], "spp": [1, 4, 16], "rates": [10, 20, 30, 40, 50, 60, 100, 200]},
     # small interactive requests only, where one job alone leaves most of the GPU idle
-    "small": {"res": [(256, 256), (512, 512)], "spp": [1, 4], "rates": [100, 200, 500, 1000, 2000]},
+    "small": {"res": [(256, 256), (512, 512)], "spp": [1, 4], "rates": [100, 200, 300, 400, 500, 700, 1000, 2000]},
 }
 
 
@@ -404,7 +436,7 @@ def nrc_leg(args, core, name, view, bounds, W, H):
         return (time.perf_counter() - t) / n
 
     plain = lambda k: core.render_ex(view, P(k), accumulate=k > 0, counters=False)
-    cached = lambda k: core.render_nrc(cache, view, P(k), accumulate=k > 0)
+    cached = lambda k: core.render_nrc(cache, view, P(k), accumulate=k > 0, stats=False)
     t_plain, t_cache = timed(plain), timed(cached)
 
     def image(fn, n):
@@ -464,12 +496,14 @@ def run_gb300(args):
     # per-pose queue sizes and traversal work: a frame is a deterministic function of its view and parameters, so
     # the timed frames below have exactly these (checked again after the timed region)
     counts, trav_pose = [], []
+    core.enable_launch_timing(True)
     for k in range(8):
         counts.append(core.render_ex(*frames[k], counters=True)["counters"].copy())
         trav_pose.append(np.asarray(core.traversal_stats(), np.float64))
+    lt_iso = [float(x) for x in core.launch_times()]   # the counting frames run one at a time: isolated kernels
     core.WaitForRender()
+    per_frame = 2 + 3 * waves + (1 if waves < MAX_DEPTH else 0)
     # ---- device-timed region: K frames back to back, scene and path state resident, no host synchronisation ----
-    core.enable_launch_timing(True)
     clocks = ClockSampler(local)
     clocks.start()
     if dist:
@@ -481,7 +515,7 @@ def run_gb300(args):
         e0.record()
     for k in range(args.steps):
         core.render_ex(*frames[k % 8], counters=False)
-    core.stream_ptr()   # orders the core's stream after the frames (consecutive frames overlap on two internal lanes)
+    core.stream_ptr()   # orders the core's stream after the frames (consecutive frames overlap on internal lanes)
     with torch.cuda.stream(stream):
         e1.record()
     torch.cuda.synchronize()
@@ -490,38 +524,18 @@ def run_gb300(args):
     lt_all = [float(x) for x in core.launch_times()]
     core.enable_launch_timing(False)
     assert np.array_equal(core.render_ex(*frames[0], counters=True)["counters"], counts[0]), "frame counters are not deterministic"
-    per_frame = 2 + 3 * waves + (1 if waves < MAX_DEPTH else 0)
     assert len(lt_all) == per_frame * args.steps, (len(lt_all), per_frame, args.steps)
-    rays = 0
-    per_kind = {"extend": [0.0, 0, 0], "shade": [0.0, 0, 0], "connect": [0.0, 0, 0], "tail": [0.0, 0, 0], "generate": [0.0, 0, 0],
-                "finalize": [0.0, 0, 0]}
+    assert len(lt_iso) == per_frame * 8, (len(lt_iso), per_frame)
+    per_kind = decode_launches(lt_all, args.steps, counts, waves, W, H)
+    per_kind_iso = decode_launches(lt_iso, 8, counts, waves, W, H)
     launches = len(lt_all)
-    trav = np.zeros(4, np.float64)
-    ext_rays = shadow_rays = 0
+    rays, trav, ext_rays, shadow_rays = 0, np.zeros(4, np.float64), 0, 0
     for k in range(args.steps):
         c = counts[k % 8]
-        lt = lt_all[k * per_frame:(k + 1) * per_frame]
-        n_in = [W * H] + [int(x) for x in c[:-1, 0]]
         rays += W * H + int(c[:, 0].sum()) + int(c[:, 1].sum())
         trav += trav_pose[k % 8]
         ext_rays += W * H + int(c[:-1, 0].sum())
         shadow_rays += int(c[:, 1].sum())
-        per_kind["generate"][0] += lt[0]
-        per_kind["finalize"][0] += lt[-1]
-        for d in range(waves):
-            te, ts, tc = lt[1 + 3 * d], lt[2 + 3 * d], lt[3 + 3 * d]
-            for kind, t, b in (("extend", te, algorithmic_bytes("extend", n_in[d], 0, 0)),
-                               ("shade", ts, algorithmic_bytes("shade", n_in[d], int(c[d, 0]), int(c[d, 1]))),
-                               ("connect", tc, algorithmic_bytes("connect", int(c[d, 1]), 0, 0))):
-                per_kind[kind][0] += t
-                per_kind[kind][1] += b
-                per_kind[kind][2] += 1
-        if waves < MAX_DEPTH:   # the tail kernel: every remaining path vertex is traced, shaded and connected
-            b = sum(algorithmic_bytes("extend", n_in[d], 0, 0) + algorithmic_bytes("shade", n_in[d], int(c[d, 0]), int(c[d, 1])) +
-                    algorithmic_bytes("connect", int(c[d, 1]), 0, 0) for d in range(waves, MAX_DEPTH))
-            per_kind["tail"][0] += lt[1 + 3 * waves]
-            per_kind["tail"][1] += b
-            per_kind["tail"][2] += 1
     if dist:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -551,27 +565,34 @@ def run_gb300(args):
     if not args.no_nrc and rank == 0:
         # the large scene at the bench's frame size; paths there are short (most bounces leave the sphere field for
         # the sky), so the cache also runs on the closed Cornell room, where every path is long
-        nrc = {"spheres_2m": nrc_leg(args, core, "spheres_2m", S.spheres_view(W, H, frame=0), NRC_FIELD_BOUNDS, W, H)}
-        cb = S.cornell_sphere(subdiv=6)
-        core_c = RenderCore(local)
-        core_c.set_scene(cb)
-        core_c.Setting("waveTail", args.wave_tail)
-        nrc["cornell"] = nrc_leg(args, core_c, "cornell 82k", S.cornell_view(1024, 1024), cb.bounds, 1024, 1024)
-        core_c.close()
+        nrc = {}
+        scenes_nrc = args.nrc_scenes.split(",")
+        if "spheres_2m" in scenes_nrc:
+            nrc["spheres_2m"] = nrc_leg(args, core, "spheres_2m", S.spheres_view(W, H, frame=0), NRC_FIELD_BOUNDS, W, H)
+        if "cornell" in scenes_nrc:
+            cb = S.cornell_sphere(subdiv=6)
+            core_c = RenderCore(local)
+            core_c.set_scene(cb)
+            core_c.Setting("waveTail", args.wave_tail)
+            nrc["cornell"] = nrc_leg(args, core_c, "cornell 82k", S.cornell_view(1024, 1024), cb.bounds, 1024, 1024)
+            core_c.close()
     if rank != 0:
         return 0
     frame_ms = sum(v[0] for v in per_kind.values())
-    dom = max(("extend", "shade", "connect", "tail"), key=lambda k: per_kind[k][0])
+    frame_ms_iso = sum(v[0] for v in per_kind_iso.values())
+    # the dominant kernel by isolated device time (in the timed region consecutive frames overlap, so launch
+    # durations there include time shared with the other frames' kernels)
+    dom = max(("extend", "shade", "connect", "tail"), key=lambda k: per_kind_iso[k][0])
     t_dom, b_dom, n_dom = per_kind[dom]
     peak, peak_kind = peaks()
     achieved = (b_dom / n_dom) / ((t_dom / n_dom) / 1e3) / 1e9 if t_dom > 0 else 0.0
+    ti, bi, ni = per_kind_iso[dom]
+    achieved_iso = (bi / ni) / ((ti / ni) / 1e3) / 1e9 if ti > 0 else 0.0
     traffic = None
-    tp = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tp):
-        with open(tp) as f:
-            tj = json.load(f)
-        if dom in tj:
-            traffic = tj[dom].get("bytes_per_unit", 0) * (b_dom / n_dom) / tj[dom].get("algorithmic_bytes_per_unit", 1)
+    if dom == "extend":
+        # DRAM bytes per ray from the ncu capture of the same workload, scaled to this run's mean launch
+        rays_captured = sum(int(counts[EXTEND_CAPTURE["pose"]][w - 2, 0]) for w in EXTEND_CAPTURE["waves"])
+        traffic = EXTEND_CAPTURE["dram_bytes"] / rays_captured * (b_dom / n_dom) / algorithmic_bytes("extend", 1, 0, 0)
     line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
@@ -582,13 +603,19 @@ def run_gb300(args):
                        "rays_per_frame": rays / args.steps / world,
                        "kernel_ms_per_frame": {k: round(v[0] / args.steps, 4) for k, v in per_kind.items()},
                        "kernel_share": {k: round(v[0] / frame_ms, 4) for k, v in per_kind.items()},
+                       "kernel_ms_per_frame_isolated": {k: round(v[0] / 8, 4) for k, v in per_kind_iso.items()},
+                       "kernel_share_isolated": {k: round(v[0] / frame_ms_iso, 4) for k, v in per_kind_iso.items()},
+                       "queue_sizes_pose1": counts[1].tolist(),
                        "traversal": {"closest_nodes_per_ray": trav[0] / max(ext_rays, 1), "closest_tris_per_ray": trav[1] / max(ext_rays, 1),
                                      "any_nodes_per_ray": trav[2] / max(shadow_rays, 1), "any_tris_per_ray": trav[3] / max(shadow_rays, 1),
                                      "traversal_bytes_per_closest_ray": (trav[0] * 80 + trav[1] * 48) / max(ext_rays, 1),
                                      "extend_traversal_GBps": (trav[0] * 80 + trav[1] * 48) / max(per_kind["extend"][0], 1e-9) / 1e6}},
             "roofline": {"kernel": "k_" + dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
-                         "note": "traversal/shading are latency and issue bound; algorithmic bytes count queue traffic only"},
+                         "achieved_isolated": achieved_iso, "frac_isolated": achieved_iso / peak,
+                         "note": "traversal/shading are ALU-issue bound; algorithmic bytes count queue traffic only (48 B per ray); "
+                                 "achieved from launches in the timed region, where frames overlap; achieved_isolated from the same "
+                                 "kernels of frames rendered one at a time; traffic = ncu DRAM bytes per ray x rays per launch"},
             "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": VIEW_BYTES + PARAMS_BYTES, "d2h_bytes_per_step": W * H * 16},
             "gpu_launches": launches * world,
             "clocks": clk}
@@ -619,6 +646,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-nrc", action="store_true")
     ap.add_argument("--nrc-lr", type=float, default=1e-3)
+    ap.add_argument("--nrc-scenes", default="spheres_2m,cornell", help="comma list of spheres_2m, cornell")
     ap.add_argument("--nrc-ref-spp", type=int, default=4096)
     ap.add_argument("--nrc-warmup", type=int, default=200)
     ap.add_argument("--serving-jobs", type=int, default=120)

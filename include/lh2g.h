@@ -156,10 +156,12 @@ LH2G_API int lh2g_render_noalloc(lh2g_context* ctx, const lh2g_view* view, const
                                  void* stream);
 
 /* ---- serving loop (no counterpart in the reference, whose cores render one frame at a time) ----
- * Render and ray-query jobs of several resident scenes, continuously batched: jobs are admitted in arrival order
- * while their paths fit in the server's path capacity (the admission unit, 48 B x 2 + 64 B of queue memory per
- * path plus 16 B of per-path radiance), and the paths of every admitted job share one set of wavefront queues;
- * one CUDA graph per tick advances every in-flight path by one vertex. A job's image is the per-pixel sum of its
+ * Render and ray-query jobs of several resident scenes, continuously batched: jobs are admitted smallest first
+ * (oldest first once one has waited 0.2 s) while their paths fit in the server's path capacity (the admission
+ * unit, 48 B x 2 + 64 B of queue memory per path plus 16 B of per-path radiance), and the paths of every admitted
+ * job share one set of wavefront queues; one CUDA graph per tick advances every in-flight path by one vertex.
+ * Express jobs (at most "expressMaxPaths" paths) skip the queues: each of their paths is traced to its end within
+ * one tick, beside the waves, so a small job finishes in one tick instead of one tick per bounce. A job's image is the per-pixel sum of its
  * samples (what lh2g_render_ex with accumulate = 0 leaves in the accumulator), bit for bit the same whatever else
  * is in flight. Ray queries run concurrently on a second stream. Scenes are finalized contexts, added by
  * reference: they must outlive the server and stay unchanged while it runs. Host buffers passed to submit must
@@ -173,6 +175,10 @@ typedef struct lh2g_server_stats {
 } lh2g_server_stats;
 LH2G_API int lh2g_server_create(int device, long long pathCapacity, lh2g_server** out);
 LH2G_API int lh2g_server_destroy(lh2g_server* server);   /* finishes the jobs it holds first */
+/* Scheduling settings, applied to jobs admitted afterwards: "expressMaxPaths" (default 262144; 0: no express
+ * jobs), "expressBudget" (express paths per tick, default 1048576), "tickBudget" (new queue paths per tick,
+ * default clamp(capacity, 2^20, 2^22)), "maxWaitSeconds" (0.2). Results do not depend on them. */
+LH2G_API int lh2g_server_setting(lh2g_server* server, const char* name, double value);
 LH2G_API const char* lh2g_server_last_error(lh2g_server* server);
 LH2G_API int lh2g_server_add_scene(lh2g_server* server, lh2g_context* scene, int* sceneId);
 /* hostOut: width * height float4. Filter frames (LH2G_RP_FILTER) are not served. */
@@ -215,10 +221,22 @@ LH2G_API int lh2g_nrc_train(lh2g_nrc* cache, const float* queries, const float* 
                             void* stream);
 /* one Adam step with the gradients accumulated by train calls with update = 0 (then cleared) */
 LH2G_API int lh2g_nrc_apply_update(lh2g_nrc* cache, void* stream);
+/* as lh2g_nrc_infer / lh2g_nrc_train (update = 1) for a count that earlier device work leaves at countDevice
+ * (a uint32, at most maxCount are used): no host round trip. An empty training batch leaves the parameters
+ * unchanged (the Adam step count still advances). */
+LH2G_API int lh2g_nrc_infer_counted(lh2g_nrc* cache, const float* queries, const uint32_t* countDevice, long long maxCount, float* out,
+                                    void* stream);
+LH2G_API int lh2g_nrc_train_counted(lh2g_nrc* cache, const float* queries, const float* targets, const uint32_t* countDevice,
+                                    long long maxCount, void* stream);
+/* the mean loss of the last training batch (waits for the device) */
+LH2G_API int lh2g_nrc_last_loss(lh2g_nrc* cache, float* loss);
 /* One frame with the radiance cache (like lh2g_render_ex with accumulate): paths reaching their second vertex
  * through a diffuse bounce end there and add throughput x cache(query); one in sixteen of them trace on and
  * their radiance from that vertex on, divided by the throughput into it, trains the cache after the frame
- * (train != 0, at most 65536 samples, one Adam step). The plain estimator is unchanged everywhere else. */
+ * (train != 0, at most 65536 samples, one Adam step). The plain estimator is unchanged everywhere else.
+ * With stats == NULL the call returns once the frame is queued, and consecutive frames overlap like plain frames
+ * (their cache work stays in submission order: each frame's inference sees the previous frame's update);
+ * with stats it waits for the frame and reports its query and training-sample counts and training loss. */
 typedef struct lh2g_nrc_frame_stats { uint32_t queries, trainSamples; float loss; } lh2g_nrc_frame_stats;
 LH2G_API int lh2g_render_nrc(lh2g_context* ctx, lh2g_nrc* cache, const lh2g_view* view, const lh2g_render_params* params, int accumulate,
                              int train, lh2g_nrc_frame_stats* stats);

@@ -46,9 +46,10 @@ C_API = ["lh2g_create", "lh2g_destroy", "lh2g_last_error", "lh2g_set_geometry", 
          "lh2g_get_stream", "lh2g_enable_launch_timing", "lh2g_get_launch_times", "lh2g_get_traversal_stats",
          "lh2g_render_noalloc", "lh2g_filter", "lh2g_read_filter_buffer", "lh2g_get_last_filter_frame",
          "lh2g_server_create", "lh2g_server_destroy", "lh2g_server_last_error", "lh2g_server_add_scene", "lh2g_server_submit_render",
-         "lh2g_server_submit_trace", "lh2g_server_wait", "lh2g_server_release", "lh2g_server_get_stats",
+         "lh2g_server_submit_trace", "lh2g_server_wait", "lh2g_server_release", "lh2g_server_get_stats", "lh2g_server_setting",
          "lh2g_nrc_create", "lh2g_nrc_destroy", "lh2g_nrc_last_error", "lh2g_nrc_get_spec", "lh2g_nrc_set_params", "lh2g_nrc_get_params",
-         "lh2g_nrc_get_grads", "lh2g_nrc_infer", "lh2g_nrc_train", "lh2g_nrc_apply_update", "lh2g_render_nrc", "lh2g_nrc_infer_host", "lh2g_nrc_train_host"]
+         "lh2g_nrc_get_grads", "lh2g_nrc_infer", "lh2g_nrc_train", "lh2g_nrc_apply_update", "lh2g_nrc_infer_counted", "lh2g_nrc_train_counted",
+         "lh2g_nrc_last_loss", "lh2g_render_nrc", "lh2g_nrc_infer_host", "lh2g_nrc_train_host"]
 
 _lib = None
 
@@ -298,12 +299,13 @@ class RenderCore:
         return out
 
     # --- radiance cache ---------------------------------------------------------------------------------
-    def render_nrc(self, cache, view, params, accumulate=False, train=True):
-        """One frame with the radiance cache (lh2g_render_nrc); returns (queries, training samples, loss)."""
+    def render_nrc(self, cache, view, params, accumulate=False, train=True, stats=True):
+        """One frame with the radiance cache (lh2g_render_nrc). stats: wait for the frame and return (queries,
+        training samples, loss); else queue it (consecutive frames overlap) and return None."""
         st = np.zeros(3, np.uint32)
         self._check(self.lib.lh2g_render_nrc(self.ctx, cache.h, _p(np.ascontiguousarray(view)), _p(np.ascontiguousarray(params)),
-                                             int(accumulate), int(train), _p(st)), "render_nrc")
-        return int(st[0]), int(st[1]), float(st[2:3].view(np.float32)[0])
+                                             int(accumulate), int(train), _p(st) if stats else None), "render_nrc")
+        return (int(st[0]), int(st[1]), float(st[2:3].view(np.float32)[0])) if stats else None
 
     # --- SVGF (filter core) ----------------------------------------------------------------------------
     def filter(self, fparams):

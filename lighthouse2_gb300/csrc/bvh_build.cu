@@ -15,6 +15,7 @@
  *      child boxes quantised outward to 8 bits per plane relative to the parent box;
  *   6. leaf primitives stored contiguously per wide node (leafPrim gives the original primitive index).
  */
+#include <climits>
 #include "bvh_build.cuh"
 
 #include <algorithm>
@@ -107,14 +108,34 @@ __device__ __forceinline__ uint32_t expand_bits10(uint32_t v) {
 __device__ __forceinline__ int f2ord(float f) { const int i = __float_as_int(f); return i >= 0 ? i : i ^ 0x7fffffff; }
 __device__ __forceinline__ float ord2f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
 
+/* Segment boxes by atomics on order-preserving integers. Segments are runs of consecutive primitives, so a warp
+ * almost always lies in one segment: it then reduces its 32 boxes with shuffles and one lane does the 6 atomics
+ * (per-primitive atomics on a few dozen addresses serialise). Min and max do not depend on the order. */
 __global__ void k_seg_bounds(const float4* __restrict__ lo, const float4* __restrict__ hi, const uint32_t* __restrict__ seg, uint32_t n,
                              int* __restrict__ segBox /* 6 ints per segment: min xyz, max xyz (ordered ints) */) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t s = seg[i];
-    const float4 a = lo[i], b = hi[i];
-    atomicMin(&segBox[6 * s + 0], f2ord(a.x)), atomicMin(&segBox[6 * s + 1], f2ord(a.y)), atomicMin(&segBox[6 * s + 2], f2ord(a.z));
-    atomicMax(&segBox[6 * s + 3], f2ord(b.x)), atomicMax(&segBox[6 * s + 4], f2ord(b.y)), atomicMax(&segBox[6 * s + 5], f2ord(b.z));
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;   /* blockDim is a multiple of 32: whole warps */
+    const bool ok = i < n;
+    const uint32_t s = ok ? seg[i] : 0xffffffffu;
+    int v[6] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN};
+    if (ok) {
+        const float4 a = lo[i], b = hi[i];
+        v[0] = f2ord(a.x), v[1] = f2ord(a.y), v[2] = f2ord(a.z), v[3] = f2ord(b.x), v[4] = f2ord(b.y), v[5] = f2ord(b.z);
+    }
+    const uint32_t s0 = __shfl_sync(0xffffffffu, s, 0);
+    if (__all_sync(0xffffffffu, s == s0 || s == 0xffffffffu)) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) v[k] = min(v[k], __shfl_xor_sync(0xffffffffu, v[k], off));
+#pragma unroll
+            for (int k = 3; k < 6; k++) v[k] = max(v[k], __shfl_xor_sync(0xffffffffu, v[k], off));
+        }
+        if ((threadIdx.x & 31u) != 0u || s0 == 0xffffffffu) return;
+    } else if (!ok) {
+        return;
+    }
+    atomicMin(&segBox[6 * s + 0], v[0]), atomicMin(&segBox[6 * s + 1], v[1]), atomicMin(&segBox[6 * s + 2], v[2]);
+    atomicMax(&segBox[6 * s + 3], v[3]), atomicMax(&segBox[6 * s + 4], v[4]), atomicMax(&segBox[6 * s + 5], v[5]);
 }
 
 __global__ void k_morton(const float4* __restrict__ lo, const float4* __restrict__ hi, const uint32_t* __restrict__ seg, uint32_t n,

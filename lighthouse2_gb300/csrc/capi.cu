@@ -214,7 +214,9 @@ struct lh2g_context {
     cudaEvent_t fev[2] = {nullptr, nullptr};   /* around the filter passes: coreStats.filterTime */
     bool filterPending = false;
     lh2g_filter_params lastFilter;
-    NrcBuffers nrcBuf;
+    NrcBuffers nrcBuf[3];              /* radiance-cache frame buffers per lane (lane 0 also for frames on the context stream) */
+    cudaEvent_t cacheEv = nullptr;     /* the last queued radiance-cache work: the next frame's cache work waits for it */
+    bool cacheEvValid = false;
     lh2g_view lastJittered;
     lh2g_render_params lastParams;
     /* Frame pipelining (setting "pipelineFrames" = frames in flight, default 3): plain frames rotate over lanes,
@@ -307,9 +309,10 @@ void free_target(lh2g_context* ctx) {
     for (int k = 0; k < 2; k++) dfree(B.O[k]), dfree(B.D[k]), dfree(B.T[k]);
     dfree(B.hits), dfree(B.shO), dfree(B.shD), dfree(B.shE), dfree(B.pathAcc), dfree(B.accum), dfree(B.frame), dfree(B.counters);
     free_filter(ctx);
-    NrcBuffers& n = ctx->nrcBuf;
-    dfree(n.rec), dfree(n.queries), dfree(n.qPath), dfree(n.pred), dfree(n.trainQ), dfree(n.trainT), dfree(n.counts);
-    n.cap = 0;
+    for (NrcBuffers& n : ctx->nrcBuf) {
+        dfree(n.rec), dfree(n.queries), dfree(n.qPath), dfree(n.pred), dfree(n.trainQ), dfree(n.trainT), dfree(n.counts);
+        n.cap = 0;
+    }
     ctx->cap = 0, ctx->pathAccCap = 0;
 }
 
@@ -437,7 +440,9 @@ int lh2g_destroy(lh2g_context* ctx) {
     dfree(ctx->B.capHits), dfree(ctx->B.capSeeds);
     free_target(ctx);
     if (ctx->hostCounters) cudaFreeHost(ctx->hostCounters);
-    if (ctx->nrcBuf.hostCounts) cudaFreeHost(ctx->nrcBuf.hostCounts);
+    for (NrcBuffers& n : ctx->nrcBuf)
+        if (n.hostCounts) cudaFreeHost(n.hostCounts);
+    if (ctx->cacheEv) cudaEventDestroy(ctx->cacheEv);
     cudaEventDestroy(ctx->ev[0]), cudaEventDestroy(ctx->ev[1]);
     if (ctx->fev[0]) cudaEventDestroy(ctx->fev[0]);
     if (ctx->fev[1]) cudaEventDestroy(ctx->fev[1]);
@@ -744,13 +749,20 @@ int lh2g_set_probe(lh2g_context* ctx, int x, int y) {
 }  // extern "C"
 
 namespace {
-/* work between a frame's last wave and its finalize (radiance-cache frames) */
-using FinalizeHook = std::function<int(const FrameGPU&, const WaveBuffers&)>;
+/* Work a frame adds around its finalize (radiance-cache frames), enqueued on the frame's stream: before runs between
+ * the last wave and the finalize, after follows the finalize. async: the hooks never wait for the device, so the
+ * frame may run on a lane. */
+struct FrameHooks {
+    std::function<int(const FrameGPU&, const WaveBuffers&, cudaStream_t, int lane)> before, after;
+    bool async = false;
+};
 
-int ensure_nrc(lh2g_context* ctx) {
-    NrcBuffers& n = ctx->nrcBuf;
+int ensure_nrc(lh2g_context* ctx, int lane) {
+    NrcBuffers& n = ctx->nrcBuf[lane];
     if (n.cap >= ctx->cap) return LH2G_OK;
+    JOIN();
     CK(cudaStreamSynchronize(ctx->st));
+    dfree(n.rec), dfree(n.queries), dfree(n.qPath), dfree(n.pred), dfree(n.trainQ), dfree(n.trainT), dfree(n.counts);
     const size_t cap = (size_t)ctx->cap;
     cudaError_t e = dalloc(n.rec, 6 * cap);
     if (!e) e = dalloc(n.queries, 4 * cap);
@@ -798,7 +810,7 @@ int ensure_lane(lh2g_context* ctx, int l) {
 }
 
 int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* p, int accumulate, lh2g_hit* capHits, uint32_t* capSeeds,
-                 uint32_t* countersOut, const FinalizeHook* hook, float* hostFrame = nullptr) {
+                 uint32_t* countersOut, const FrameHooks* hook, float* hostFrame = nullptr) {
     if (!ctx || !view || !p) return LH2G_ERR_INVALID;
     if (!ctx->finalized) return fail(ctx, LH2G_ERR_STATE, "render: scene not finalized (call lh2g_finalize_instances)");
     if (!ctx->cap) return fail(ctx, LH2G_ERR_STATE, "render: no target (call lh2g_set_target)");
@@ -810,15 +822,16 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
     if (filt && nrcFrame) return fail(ctx, LH2G_ERR_INVALID, "render: filter and radiance-cache frames do not combine");
     /* plain frames without host read-backs go to the next lane; everything else runs on the context stream after
      * the lanes' frames */
-    const bool pipe = ctx->pipelineFrames > 1 && !filt && !nrcFrame && !capHits && !capSeeds && !countersOut && !hook &&
+    const bool pipe = ctx->pipelineFrames > 1 && !filt && !capHits && !capSeeds && !countersOut && (!hook || hook->async) &&
                       ctx->cap <= lh2g_context::PIPE_MAX_PATHS;
     if (!pipe) JOIN();
     if (filt) {
         const int r = ensure_filter(ctx);
         if (r != LH2G_OK) return r;
     }
+    const int nrcLane = pipe ? ctx->nextLane : 0;
     if (nrcFrame) {
-        const int r = ensure_nrc(ctx);
+        const int r = ensure_nrc(ctx, nrcLane);
         if (r != LH2G_OK) return r;
     }
     cudaStream_t st = ctx->st;
@@ -846,7 +859,7 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
     B.features = filt ? ctx->sv.features : nullptr;
     B.worldPos = filt ? ctx->sv.worldPos : nullptr;
     B.deltaDepth = filt ? ctx->sv.deltaDepth : nullptr;
-    B.nrcRec = nrcFrame ? ctx->nrcBuf.rec : nullptr;
+    B.nrcRec = nrcFrame ? ctx->nrcBuf[nrcLane].rec : nullptr;
     const size_t capN = (size_t)F.maxDepth * F.P;
     if (capHits || capSeeds) {
         CK(dalloc(ctx->B.capHits, capN));
@@ -882,8 +895,8 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
         mark(), launch_connect(S, F, B, d, ctx->blocksConnect, st), mark();
     }
     if (tail) mark(), launch_tail(S, F, B, waves + 1, ctx->blocksTail, st), mark();
-    if (hook) {
-        const int r = (*hook)(F, B);
+    if (hook && hook->before) {
+        const int r = hook->before(F, B, st, nrcLane);
         if (r != LH2G_OK) return r;
     }
     const int after = p->samplesTaken + F.spp;
@@ -893,6 +906,10 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
     if (hostFrame) CK(cudaMemcpyAsync(hostFrame, B.frame, sizeof(float4) * (size_t)F.W * F.H, cudaMemcpyDeviceToHost, st));
     CK(cudaEventRecord(ctx->finEv, st));
     ctx->finValid = true;
+    if (hook && hook->after) {
+        const int r = hook->after(F, B, st, nrcLane);
+        if (r != LH2G_OK) return r;
+    }
     if (timing) ctx->timedLaunches += launches;
     CK(cudaGetLastError());
     CK(cudaEventRecord(fev[1], st));
@@ -931,31 +948,52 @@ int lh2g_render_to_host(lh2g_context* ctx, const lh2g_view* view, const lh2g_ren
 int lh2g_render_nrc(lh2g_context* ctx, lh2g_nrc* cache, const lh2g_view* view, const lh2g_render_params* params, int accumulate, int train,
                     lh2g_nrc_frame_stats* stats) {
     if (!ctx || !cache || !view || !params) return LH2G_ERR_INVALID;
+    if (params->flags & LH2G_RP_FILTER) return fail(ctx, LH2G_ERR_INVALID, "render_nrc: filter frames do not combine with the cache");
     lh2g_render_params p = *params;
     p.flags |= LH2G_RP_NRC;
-    uint32_t nq = 0, nt = 0;
-    const FinalizeHook hook = [&](const FrameGPU& F, const WaveBuffers& B) -> int {
-        NrcBuffers& n = ctx->nrcBuf;
-        CK(cudaMemsetAsync(n.counts, 0, 16, ctx->st));
-        launch_nrc_collect(F, B, n.queries, n.qPath, n.trainQ, n.trainT, n.counts, NRC_TRAIN_CAP, ctx->st);
-        CK(cudaMemcpyAsync(n.hostCounts, n.counts, 8, cudaMemcpyDeviceToHost, ctx->st));
-        CK(cudaStreamSynchronize(ctx->st));
-        nq = n.hostCounts[0], nt = std::min<uint32_t>(n.hostCounts[1], NRC_TRAIN_CAP);
-        if (nq) {
-            const int r = lh2g_nrc_infer(cache, (const float*)n.queries, nq, (float*)n.pred, ctx->st);
-            if (r != LH2G_OK) return fail(ctx, r, std::string("radiance-cache inference: ") + lh2g_nrc_last_error(cache));
-            launch_nrc_apply(F, B, n.pred, n.qPath, n.counts, ctx->st);
+    if (!ctx->cacheEv) CK(cudaEventCreateWithFlags(&ctx->cacheEv, cudaEventDisableTiming));
+    FrameHooks hooks;
+    hooks.async = stats == nullptr;   /* nothing waits for the device: the frame may overlap others */
+    /* after the waves: gather the queries and training samples, infer, add throughput x prediction. The cache
+     * work waits for the previous frame's (its update), all counts stay on the device. */
+    hooks.before = [&](const FrameGPU& F, const WaveBuffers& B, cudaStream_t st, int lane) -> int {
+        NrcBuffers& n = ctx->nrcBuf[lane];
+        CK(cudaMemsetAsync(n.counts, 0, 16, st));
+        launch_nrc_collect(F, B, n.queries, n.qPath, n.trainQ, n.trainT, n.counts, NRC_TRAIN_CAP, st);
+        if (ctx->cacheEvValid) CK(cudaStreamWaitEvent(st, ctx->cacheEv, 0));
+        const int r = lh2g_nrc_infer_counted(cache, (const float*)n.queries, n.counts, F.P, (float*)n.pred, st);
+        if (r != LH2G_OK) return fail(ctx, r, std::string("radiance-cache inference: ") + lh2g_nrc_last_error(cache));
+        launch_nrc_apply(F, B, n.pred, n.qPath, n.counts, st);
+        if (!train) {
+            CK(cudaEventRecord(ctx->cacheEv, st));
+            ctx->cacheEvValid = true;
         }
         return LH2G_OK;
     };
-    int r = render_frame(ctx, view, &p, accumulate, nullptr, nullptr, nullptr, &hook);
+    /* after the finalize: one training step on the frame's samples */
+    if (train)
+        hooks.after = [&](const FrameGPU&, const WaveBuffers&, cudaStream_t st, int lane) -> int {
+            NrcBuffers& n = ctx->nrcBuf[lane];
+            const int r = lh2g_nrc_train_counted(cache, (const float*)n.trainQ, (const float*)n.trainT, n.counts + 1, NRC_TRAIN_CAP, st);
+            if (r != LH2G_OK) return fail(ctx, r, std::string("radiance-cache training: ") + lh2g_nrc_last_error(cache));
+            CK(cudaEventRecord(ctx->cacheEv, st));
+            ctx->cacheEvValid = true;
+            return LH2G_OK;
+        };
+    int r = render_frame(ctx, view, &p, accumulate, nullptr, nullptr, nullptr, &hooks);
     if (r != LH2G_OK) return r;
-    float loss = 0.0f;
-    if (train && nt > 0) {
-        r = lh2g_nrc_train(cache, (const float*)ctx->nrcBuf.trainQ, (const float*)ctx->nrcBuf.trainT, nt, 1, &loss, ctx->st);
-        if (r != LH2G_OK) return fail(ctx, r, std::string("radiance-cache training: ") + lh2g_nrc_last_error(cache));
+    if (stats) {   /* the frame ran on the context stream with lane 0's buffers */
+        NrcBuffers& n = ctx->nrcBuf[0];
+        CK(cudaMemcpyAsync(n.hostCounts, n.counts, 8, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        stats->queries = n.hostCounts[0];
+        stats->trainSamples = std::min<uint32_t>(n.hostCounts[1], NRC_TRAIN_CAP);
+        stats->loss = 0.0f;
+        if (train && stats->trainSamples > 0) {
+            r = lh2g_nrc_last_loss(cache, &stats->loss);
+            if (r != LH2G_OK) return fail(ctx, r, std::string("radiance-cache training: ") + lh2g_nrc_last_error(cache));
+        }
     }
-    if (stats) stats->queries = nq, stats->trainSamples = nt, stats->loss = loss;
     return LH2G_OK;
 }
 

@@ -106,8 +106,10 @@ constexpr uint32_t SMEM_SLACK = 1024 + 64;
 constexpr uint32_t INFER_SMEM = WEIGHT_BYTES + ACT_BYTES + SMEM_SLACK;
 
 __global__ void __launch_bounds__(TILE) k_infer(const GridSpec G, const __half2* __restrict__ grid, const __nv_bfloat16* __restrict__ W,
-                                                const float4* __restrict__ queries, const long long n, float4* __restrict__ out,
-                                                uint32_t* errors) {
+                                                const float4* __restrict__ queries, const long long nMax, const uint32_t* __restrict__ nDev,
+                                                float4* __restrict__ out, uint32_t* errors) {
+    /* query count: nMax, or the count a previous kernel left in device memory (at most nMax) */
+    const long long n = nDev ? min((long long)*nDev, nMax) : nMax;
     extern __shared__ unsigned char dyn[];
     Shared& sh = *reinterpret_cast<Shared*>(dyn);
     unsigned char* Ws = tiles_base(dyn);
@@ -184,8 +186,10 @@ __device__ __forceinline__ void load_row8(const unsigned char* tile, uint32_t r,
 }
 
 __global__ void __launch_bounds__(TILE, 1) k_train(const GridSpec G, const __half2* __restrict__ grid, const __nv_bfloat16* __restrict__ W,
-                                                   const float4* __restrict__ queries, const float4* __restrict__ targets, const long long n,
-                                                   float* __restrict__ gW, float* __restrict__ gGrid, float* __restrict__ loss, uint32_t* errors) {
+                                                   const float4* __restrict__ queries, const float4* __restrict__ targets, const long long nMax,
+                                                   const uint32_t* __restrict__ nDev, float* __restrict__ gW, float* __restrict__ gGrid,
+                                                   float* __restrict__ loss, uint32_t* errors) {
+    const long long n = nDev ? min((long long)*nDev, nMax) : nMax;
     extern __shared__ unsigned char dyn[];
     Shared& sh = *reinterpret_cast<Shared*>(dyn);
     unsigned char* Ws = tiles_base(dyn);
@@ -356,7 +360,9 @@ __global__ void __launch_bounds__(TILE, 1) k_train(const GridSpec G, const __hal
  * Adam on fp32 master parameters (gradients cleared), writing the copy the kernels read
  * ------------------------------------------------------------------------------------------------------- */
 __global__ void k_adam(float* __restrict__ p, float* __restrict__ m, float* __restrict__ v, float* __restrict__ g, const long long n, const float lr,
-                       const float c1, const float c2, __nv_bfloat16* __restrict__ outBf16, __half* __restrict__ outHalf) {
+                       const float c1, const float c2, __nv_bfloat16* __restrict__ outBf16, __half* __restrict__ outHalf,
+                       const uint32_t* __restrict__ batchDev) {
+    if (batchDev && *batchDev == 0u) return;   /* an empty training batch (counted on the device) changes nothing */
     const float b1 = 0.9f, b2 = 0.99f, eps = 1e-15f;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float gi = g[i];
@@ -480,11 +486,18 @@ int lh2g_nrc_create(int device, const lh2g_nrc_config* cfg, lh2g_nrc** out) {
     ok = ok && cudaMemset(c->Wdev, 0, sizeof(__nv_bfloat16) * WDEV) == cudaSuccess && cudaMemset(c->dErr, 0, 16) == cudaSuccess;
     ok = ok && cudaFuncSetAttribute(k_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)INFER_SMEM) == cudaSuccess;
     ok = ok && cudaFuncSetAttribute(k_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TRAIN_SMEM) == cudaSuccess;
+    /* all of the unified L1 / shared storage as shared memory, so that several inference CTAs share an SM: the
+     * hash-grid gathers of the encoding are latency bound and want warps to hide it */
+    ok = ok && cudaFuncSetAttribute(k_infer, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared) == cudaSuccess;
     if (!ok) return fail(LH2G_ERR_CUDA);
-    int sms = 1, per = 0;
+    int sms = 1, per = 0, smemSM = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_infer, TILE, INFER_SMEM);
-    c->blocksInfer = sms * std::max(1, std::min(per, 4));   /* 4 x 64 TMEM columns per SM at most */
+    cudaDeviceGetAttribute(&smemSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_infer, TILE, INFER_SMEM) != cudaSuccess) per = 0;
+    /* resident CTAs per SM: the occupancy calculator's answer, else what shared memory allows (1 KB reserved per
+     * CTA); at most 4 (4 x 64 of the SM's 512 TMEM columns) */
+    if (per < 1) per = smemSM / (int)(INFER_SMEM + 1024);
+    c->blocksInfer = sms * std::max(1, std::min(per, 4));
     c->blocksTrain = sms;
     if (launch_copies(c) != LH2G_OK || cudaStreamSynchronize(c->st) != cudaSuccess) return fail(LH2G_ERR_CUDA);
     *out = c;
@@ -544,15 +557,35 @@ int lh2g_nrc_get_grads(lh2g_nrc* c, float* mlp, float* grid) {
     return LH2G_OK;
 }
 
+static int infer_launch(lh2g_nrc* c, const float* queries, long long nMax, const uint32_t* nDev, float* out, void* stream) {
+    cudaSetDevice(c->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->st;
+    const long long tiles = (nMax + TILE - 1) / TILE;
+    const int blocks = (int)std::min<long long>(tiles, c->blocksInfer);
+    k_infer<<<blocks, TILE, INFER_SMEM, st>>>(c->G, reinterpret_cast<const __half2*>(c->grid16), c->Wdev, reinterpret_cast<const float4*>(queries), nMax,
+                                             nDev, reinterpret_cast<float4*>(out), c->dErr);
+    NCK(cudaGetLastError());
+    return LH2G_OK;
+}
+
 int lh2g_nrc_infer(lh2g_nrc* c, const float* queries, long long n, float* out, void* stream) {
     if (!c || (n > 0 && (!queries || !out)) || n < 0) return LH2G_ERR_INVALID;
     if (n == 0) return LH2G_OK;
-    cudaSetDevice(c->device);
-    cudaStream_t st = stream ? (cudaStream_t)stream : c->st;
-    const long long tiles = (n + TILE - 1) / TILE;
-    const int blocks = (int)std::min<long long>(tiles, c->blocksInfer);
-    k_infer<<<blocks, TILE, INFER_SMEM, st>>>(c->G, reinterpret_cast<const __half2*>(c->grid16), c->Wdev, reinterpret_cast<const float4*>(queries), n,
-                                             reinterpret_cast<float4*>(out), c->dErr);
+    return infer_launch(c, queries, n, nullptr, out, stream);
+}
+
+int lh2g_nrc_infer_counted(lh2g_nrc* c, const float* queries, const uint32_t* countDevice, long long maxCount, float* out, void* stream) {
+    if (!c || !countDevice || maxCount < 0 || (maxCount > 0 && (!queries || !out))) return LH2G_ERR_INVALID;
+    if (maxCount == 0) return LH2G_OK;
+    return infer_launch(c, queries, maxCount, countDevice, out, stream);
+}
+
+static int adam_launch(lh2g_nrc* c, cudaStream_t st, const uint32_t* batchDev) {
+    c->step++;
+    const float c1 = (float)(1.0 / (1.0 - std::pow(0.9, (double)c->step)));
+    const float c2 = (float)(1.0 / (1.0 - std::pow(0.99, (double)c->step)));
+    k_adam<<<64, 256, 0, st>>>(c->pW, c->mW, c->vW, c->gW, WMASTER, c->lr, c1, c2, c->Wdev, nullptr, batchDev);
+    k_adam<<<2048, 256, 0, st>>>(c->pG, c->mG, c->vG, c->gG, GRID_PARAMS, c->lr, c1, c2, nullptr, c->grid16, batchDev);
     NCK(cudaGetLastError());
     return LH2G_OK;
 }
@@ -560,13 +593,34 @@ int lh2g_nrc_infer(lh2g_nrc* c, const float* queries, long long n, float* out, v
 int lh2g_nrc_apply_update(lh2g_nrc* c, void* stream) {
     if (!c) return LH2G_ERR_INVALID;
     cudaSetDevice(c->device);
-    cudaStream_t st = stream ? (cudaStream_t)stream : c->st;
-    c->step++;
-    const float c1 = (float)(1.0 / (1.0 - std::pow(0.9, (double)c->step)));
-    const float c2 = (float)(1.0 / (1.0 - std::pow(0.99, (double)c->step)));
-    k_adam<<<64, 256, 0, st>>>(c->pW, c->mW, c->vW, c->gW, WMASTER, c->lr, c1, c2, c->Wdev, nullptr);
-    k_adam<<<2048, 256, 0, st>>>(c->pG, c->mG, c->vG, c->gG, GRID_PARAMS, c->lr, c1, c2, nullptr, c->grid16);
+    return adam_launch(c, stream ? (cudaStream_t)stream : c->st, nullptr);
+}
+
+static int train_launch(lh2g_nrc* c, const float* queries, const float* targets, long long nMax, const uint32_t* nDev, cudaStream_t st) {
+    NCK(cudaMemsetAsync(c->dLoss, 0, 4, st));
+    const long long tiles = (nMax + TILE - 1) / TILE;
+    const int blocks = (int)std::min<long long>(tiles, c->blocksTrain);
+    k_train<<<blocks, TILE, TRAIN_SMEM, st>>>(c->G, reinterpret_cast<const __half2*>(c->grid16), c->Wdev, reinterpret_cast<const float4*>(queries),
+                                             reinterpret_cast<const float4*>(targets), nMax, nDev, c->gW, c->gG, c->dLoss, c->dErr);
     NCK(cudaGetLastError());
+    return LH2G_OK;
+}
+
+int lh2g_nrc_train_counted(lh2g_nrc* c, const float* queries, const float* targets, const uint32_t* countDevice, long long maxCount, void* stream) {
+    if (!c || !countDevice || maxCount <= 0 || !queries || !targets) return LH2G_ERR_INVALID;
+    cudaSetDevice(c->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->st;
+    const int r = train_launch(c, queries, targets, maxCount, countDevice, st);
+    return r != LH2G_OK ? r : adam_launch(c, st, countDevice);
+}
+
+int lh2g_nrc_last_loss(lh2g_nrc* c, float* loss) {
+    if (!c || !loss) return LH2G_ERR_INVALID;
+    cudaSetDevice(c->device);
+    NCK(cudaMemcpy(loss, c->dLoss, 4, cudaMemcpyDeviceToHost));
+    uint32_t e = 0;
+    NCK(cudaMemcpy(&e, c->dErr, 4, cudaMemcpyDeviceToHost));
+    if (e) return nfail(c, LH2G_ERR_CUDA, "radiance cache: a tensor-core completion wait ran out");
     return LH2G_OK;
 }
 
@@ -574,14 +628,10 @@ int lh2g_nrc_train(lh2g_nrc* c, const float* queries, const float* targets, long
     if (!c || n <= 0 || !queries || !targets) return LH2G_ERR_INVALID;
     cudaSetDevice(c->device);
     cudaStream_t st = stream ? (cudaStream_t)stream : c->st;
-    NCK(cudaMemsetAsync(c->dLoss, 0, 4, st));
-    const long long tiles = (n + TILE - 1) / TILE;
-    const int blocks = (int)std::min<long long>(tiles, c->blocksTrain);
-    k_train<<<blocks, TILE, TRAIN_SMEM, st>>>(c->G, reinterpret_cast<const __half2*>(c->grid16), c->Wdev, reinterpret_cast<const float4*>(queries),
-                                             reinterpret_cast<const float4*>(targets), n, c->gW, c->gG, c->dLoss, c->dErr);
-    NCK(cudaGetLastError());
+    int r0 = train_launch(c, queries, targets, n, nullptr, st);
+    if (r0 != LH2G_OK) return r0;
     if (update) {
-        const int r = lh2g_nrc_apply_update(c, st);
+        const int r = adam_launch(c, st, nullptr);
         if (r != LH2G_OK) return r;
     }
     if (lossOut) {

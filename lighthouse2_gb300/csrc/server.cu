@@ -53,6 +53,7 @@ namespace srv {
 constexpr int MAX_SLOTS = 256;         /* job slots: 8 bits of the flag word */
 constexpr int MAX_NEW = 64;            /* path ranges admitted per tick */
 constexpr int MAX_SCENES = 16;         /* scene records travel as a kernel parameter */
+constexpr int MAX_EXPRESS = 64;        /* express jobs admitted per tick */
 constexpr uint32_t SLOT_SHIFT = 8, DEPTH_SHIFT = 16;
 
 struct JobGPU {
@@ -72,6 +73,9 @@ struct ServerState {
     uint32_t newSlot[MAX_NEW];
     uint32_t newStart[MAX_NEW];        /* first path (index within its job) of each range */
     uint32_t newPrefix[MAX_NEW + 1];
+    uint32_t expCount, expTotal;       /* express jobs of this tick (whole jobs) and their paths */
+    uint32_t expSlot[MAX_EXPRESS];
+    uint32_t expPrefix[MAX_EXPRESS + 1];
     unsigned long long rays;           /* rays traced over all ticks */
     unsigned long long ticks;
 };
@@ -160,9 +164,13 @@ __global__ void __launch_bounds__(WAVE_BLOCK) k_srv_shade(const __grid_constant_
             B.pathAcc = J.pathAcc;
             shade_core(scenes.s[J.scene], J.F, B, depth, o4, d4, t4, hit, out, potential + threadIdx.x);
             if (out.ext) out.eD.w = __uint_as_float(__float_as_uint(out.eD.w) + (1u << DEPTH_SHIFT));
-            else atomicSub(&alive[slot], 1);
             if (out.shadow) out.sE.w = __uint_as_float(__float_as_uint(out.sE.w) | (slot << SLOT_SHIFT));
         }
+        /* paths that end here leave their job's live count: one atomic per job and warp (one per path would
+         * serialise on the few counters of the jobs in flight) */
+        const uint32_t endSlot = (i < count && !out.ext) ? slot : 0xffffffffu;
+        const uint32_t peers = __match_any_sync(0xffffffffu, endSlot);
+        if (endSlot != 0xffffffffu && lane == (uint32_t)(__ffs(peers) - 1)) atomicSub(&alive[endSlot], __popc(peers));
         const uint32_t em = __ballot_sync(0xffffffffu, out.ext);
         if (em) {
             const int leader = __ffs(em) - 1;
@@ -218,6 +226,77 @@ __global__ void __launch_bounds__(128) k_srv_connect(const __grid_constant__ Sce
     if (status) atomicOr(&st->status, status);
 }
 
+/* Express jobs: every path of the small jobs admitted this tick, from its primary ray to its end, one thread per
+ * path (the loop of the plain core's tail kernel), beside the tick's wave kernels. A small job so finishes within
+ * one tick instead of one tick per bounce. Per-path work is the plain core's, as in the waves. */
+__global__ void __launch_bounds__(WAVE_BLOCK) k_srv_express(const __grid_constant__ SceneTable scenes, const JobGPU* __restrict__ jobs,
+                                                           ServerState* st, int* alive) {
+    const uint32_t total = st->expTotal, n = st->expCount;
+    if (total == 0) return;
+    __shared__ float potential[64 * WAVE_BLOCK];
+    float* pot = potential + threadIdx.x;
+    uint32_t status = 0;
+    unsigned long long rays = 0;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    /* whole warps go round the loop together, so that the warp-aggregated live-count update sees all lanes */
+    for (uint32_t g0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); g0 < total; g0 += stride) {
+        const uint32_t g = g0 + (threadIdx.x & 31u);
+        uint32_t slot = 0xffffffffu;
+        if (g < total) {
+            uint32_t j = 0;
+            while (j + 1 < n && st->expPrefix[j + 1] <= g) j++;
+            slot = st->expSlot[j];
+            const uint32_t i = g - st->expPrefix[j];
+            const JobGPU& J = jobs[slot];
+            const SceneGPU& S = scenes.s[J.scene];
+            WaveBuffers B;
+            memset(&B, 0, sizeof(B));
+            B.pathAcc = J.pathAcc;
+            float3 O, D;
+            primary_ray(J.F, i, O, D);
+            float4 o4 = make_float4(O.x, O.y, O.z, __uint_as_float(i));
+            float4 d4 = make_float4(D.x, D.y, D.z, __uint_as_float(S_SPECULAR | (slot << SLOT_SHIFT) | (1u << DEPTH_SHIFT)));
+            float4 t4 = make_float4(1.0f, 1.0f, 1.0f, J.F.eps);
+            J.pathAcc[i] = make_float4(0, 0, 0, 0);
+            for (int depth = 1; depth <= J.F.maxDepth; depth++) {
+                Traversal tr;
+                tr.begin(S, xyz(o4), xyz(d4), t4.w, 1e34f);
+                bool any = false;
+                if (S.tlasRoot != 0xffffffffu)
+                    while (tr.step<false>(S, status, any)) {}
+                rays++;
+                ShadeOut out;
+                out.ext = out.shadow = false;
+                shade_core(S, J.F, B, depth, o4, d4, t4, hit_record(tr.found, tr.best), out, pot);
+                if (out.shadow) {
+                    rays++;
+                    Traversal sh;
+                    sh.begin(S, xyz(out.sO), xyz(out.sD), 0.0f, out.sD.w);
+                    bool occluded = false;
+                    if (S.tlasRoot != 0xffffffffu)
+                        while (sh.step<true>(S, status, occluded)) {}
+                    if (!occluded) {
+                        float4* accP = J.pathAcc + ((__float_as_uint(out.sE.w) & 1u) ? J.F.P : 0) + __float_as_uint(out.sO.w);
+                        float4 acc = *accP;
+                        acc.x += out.sE.x, acc.y += out.sE.y, acc.z += out.sE.z;
+                        *accP = acc;
+                    }
+                }
+                if (!out.ext) break;
+                o4 = out.eO, d4 = out.eD, t4 = out.eT;
+                d4.w = __uint_as_float(__float_as_uint(d4.w) + (1u << DEPTH_SHIFT));
+            }
+        }
+        /* the finished paths leave their job's live count: one atomic per job and warp */
+        const uint32_t peers = __match_any_sync(0xffffffffu, slot);
+        if (slot != 0xffffffffu && (threadIdx.x & 31u) == (uint32_t)(__ffs(peers) - 1)) atomicSub(&alive[slot], __popc(peers));
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) rays += __shfl_xor_sync(0xffffffffu, rays, off);
+    if ((threadIdx.x & 31u) == 0 && rays) atomicAdd(&st->rays, rays);
+    if (status) atomicOr(&st->status, status);
+}
+
 /* closes a tick: swap the queues, count the rays, clear the per-tick state */
 __global__ void k_srv_end(ServerState* st) {
     const uint32_t cur = st->cur;
@@ -228,6 +307,7 @@ __global__ void k_srv_end(ServerState* st) {
     st->shadowCount = 0;
     st->fetch[0] = st->fetch[1] = 0;
     st->newCount = st->newTotal = 0;
+    st->expCount = st->expTotal = 0;
 }
 
 /* per-pixel sums of a finished job's paths in sample order (as the plain core's finalize) */
@@ -263,6 +343,7 @@ struct Job {
     int slot = -1;
     long long admitTick = -1;
     int state = 0;                     /* 0 pending, 1 running, 2 finishing, 3 done, 4 failed */
+    bool express = false;              /* traced whole in one tick beside the waves (no queue memory) */
     double tSubmit = 0, tAdmit = 0, tDone = 0;
     JobGPU gpu;
 };
@@ -276,6 +357,8 @@ struct lh2g_server {
     int device = 0;
     cudaStream_t st = nullptr;         /* render ticks */
     cudaStream_t io = nullptr;         /* worker: result copies, ray queries */
+    cudaStream_t side = nullptr;       /* second branch of the tick graph (express jobs) */
+    cudaEvent_t evFork = nullptr, evJoin = nullptr;
     std::string err;
     std::vector<SceneGPU> scenes;
     int graphScenes = -1;              /* scene count the tick graph was captured with */
@@ -287,12 +370,14 @@ struct lh2g_server {
     Queues Q;
     long long capacity = 0;
     long long tickBudget = 0;          /* new paths per tick */
+    long long expressMax = 1ll << 18;  /* jobs of at most this many paths are express jobs */
+    long long expressBudget = 1ll << 20;   /* express paths per tick */
     double maxWaitS = 0.2;             /* a job waiting longer than this is admitted before smaller ones */
     cudaGraphExec_t tickExec = nullptr;
     cudaGraph_t tickGraph = nullptr;
     std::vector<cudaEvent_t> tickEv;   /* ring of tick-completion events */
     long long ticksLaunched = 0, ticksDone = 0;
-    int blocksGen = 0, blocksExtend = 0, blocksShade = 0, blocksConnect = 0, blocksTrace0 = 0, blocksTrace1 = 0;
+    int blocksGen = 0, blocksExtend = 0, blocksShade = 0, blocksConnect = 0, blocksTrace0 = 0, blocksTrace1 = 0, blocksExpress = 0;
     /* jobs */
     std::mutex mu;
     std::condition_variable cvWork, cvDone;
@@ -384,7 +469,7 @@ void run_query(lh2g_server* s, Job* j) {
 }
 
 /* A path range of a job entering the queues at the next tick. */
-struct Range { Job* job; long long start, count; bool first; };
+struct Range { Job* job; long long start, count; bool first, express; };
 
 /* Admission for the next tick. Ray queries go to the worker. Render jobs are admitted when their paths fit in the
  * capacity (reserved whole) and a slot is free: the smallest pending job first, unless one has waited longer than
@@ -393,22 +478,24 @@ struct Range { Job* job; long long start, count; bool first; };
  * stretch the ticks that every small job needs. */
 void admit(lh2g_server* s, std::vector<Range>& ranges) {
     std::lock_guard<std::mutex> g(s->mu);
-    long long budget = s->tickBudget;
+    long long budget = s->tickBudget, expBudget = s->expressBudget;
+    int nNew = 0, nExp = 0;
     auto take = [&](Job* j, bool first) {
         const long long n = std::min(j->paths - j->admittedPaths, std::max(budget, 1ll));
-        ranges.push_back({j, j->admittedPaths, n, first});
+        ranges.push_back({j, j->admittedPaths, n, first, false});
         j->admittedPaths += n;
         budget -= n;
+        nNew++;
     };
     /* ranges of jobs admitted earlier, in admission order */
-    for (size_t k = 0; k < s->partial.size() && budget > 0 && (int)ranges.size() < MAX_NEW;) {
+    for (size_t k = 0; k < s->partial.size() && budget > 0 && nNew < MAX_NEW;) {
         Job* j = s->partial[k];
         take(j, false);
         if (j->admittedPaths == j->paths) s->partial.erase(s->partial.begin() + (long)k);
         else k++;
     }
     const double now = now_s();
-    while (!s->pending.empty() && budget > 0 && (int)ranges.size() < MAX_NEW) {
+    while (!s->pending.empty()) {
         size_t pick = 0;
         if (now - s->pending.front()->tSubmit <= s->maxWaitS)
             for (size_t k = 1; k < s->pending.size(); k++)
@@ -421,6 +508,26 @@ void admit(lh2g_server* s, std::vector<Range>& ranges) {
             continue;
         }
         if (j->scene >= s->graphScenes) break;                  /* its scene is not in the tick graph yet */
+        const bool express = j->paths <= s->expressMax;
+        if (express) {
+            /* a small job runs whole, beside the waves, in the next tick: no queue memory, its own budget */
+            if (j->paths > expBudget || nExp >= MAX_EXPRESS) break;
+            int slot = -1;
+            for (int k = 0; k < MAX_SLOTS; k++)
+                if (!s->slots[k]) { slot = k; break; }
+            if (slot < 0) break;
+            s->pending.erase(s->pending.begin() + (long)pick);
+            j->slot = slot;
+            j->express = true;
+            s->slots[slot] = j;
+            j->state = 1, j->tAdmit = now;
+            ranges.push_back({j, 0, j->paths, true, true});
+            j->admittedPaths = j->paths;
+            expBudget -= j->paths;
+            nExp++;
+            continue;
+        }
+        if (budget <= 0 || nNew >= MAX_NEW) break;
         if (s->pathsInFlight + j->paths > s->capacity) break;   /* wait for path memory */
         int slot = -1;
         for (int k = 0; k < MAX_SLOTS; k++)
@@ -479,49 +586,50 @@ void tick_loop_body(lh2g_server* s) {
             }
         }
         /* new jobs: device records, live counts, per-job memory (stream-ordered), tick parameters */
-        uint32_t total = 0;
+        uint32_t total = 0, expTotal = 0, nNew = 0, nExp = 0;
         /* staging entry of this tick: its previous user (ticksLaunched - ring) has completed, since at most two
          * ticks are in flight */
         ServerState& tp = s->hTick[s->ticksLaunched % ring];
-        tp.newCount = (uint32_t)admitted.size();
         for (size_t k = 0; k < admitted.size(); k++) {
             Job* j = admitted[k].job;
-            if (!admitted[k].first) {   /* a further range of a job already on the device */
-                tp.newSlot[k] = (uint32_t)j->slot;
-                tp.newStart[k] = (uint32_t)admitted[k].start;
-                tp.newPrefix[k] = total;
-                total += (uint32_t)admitted[k].count;
-                continue;
-            }
-            JobGPU& G = j->gpu;
-            G.F = frame_of(&j->view, &j->params);
-            G.scene = j->scene;
-            G.pathAcc = nullptr, G.out = nullptr;
-            if (cudaMallocAsync((void**)&G.pathAcc, sizeof(float4) * (size_t)j->paths, s->st) != cudaSuccess ||
-                cudaMallocAsync((void**)&G.out, sizeof(float4) * (size_t)G.F.W * G.F.H, s->st) != cudaSuccess) {
-                /* no device memory for this job: it fails, the others go on */
-                if (G.pathAcc) cudaFreeAsync(G.pathAcc, s->st);
-                {
-                    std::lock_guard<std::mutex> g(s->mu);
-                    s->slots[j->slot] = nullptr;
-                    s->pathsInFlight -= j->paths;
-                    s->partial.erase(std::remove(s->partial.begin(), s->partial.end(), j), s->partial.end());
+            if (admitted[k].first) {
+                JobGPU& G = j->gpu;
+                G.F = frame_of(&j->view, &j->params);
+                G.scene = j->scene;
+                G.pathAcc = nullptr, G.out = nullptr;
+                if (cudaMallocAsync((void**)&G.pathAcc, sizeof(float4) * (size_t)j->paths, s->st) != cudaSuccess ||
+                    cudaMallocAsync((void**)&G.out, sizeof(float4) * (size_t)G.F.W * G.F.H, s->st) != cudaSuccess) {
+                    /* no device memory for this job: it fails, the others go on */
+                    if (G.pathAcc) cudaFreeAsync(G.pathAcc, s->st);
+                    {
+                        std::lock_guard<std::mutex> g(s->mu);
+                        s->slots[j->slot] = nullptr;
+                        if (!j->express) s->pathsInFlight -= j->paths;
+                        s->partial.erase(std::remove(s->partial.begin(), s->partial.end(), j), s->partial.end());
+                    }
+                    finish(s, j, 4);
+                    continue;
                 }
-                finish(s, j, 4);
-                admitted.erase(admitted.begin() + (long)k--);
-                continue;
+                cudaMemcpyAsync(s->dJobs + j->slot, &G, sizeof(JobGPU), cudaMemcpyHostToDevice, s->st);
+                const int live = (int)j->paths;
+                cudaMemcpyAsync(s->dAlive + j->slot, &live, sizeof(int), cudaMemcpyHostToDevice, s->st);
+                j->admitTick = s->ticksLaunched;
             }
-            cudaMemcpyAsync(s->dJobs + j->slot, &G, sizeof(JobGPU), cudaMemcpyHostToDevice, s->st);
-            const int live = (int)j->paths;
-            cudaMemcpyAsync(s->dAlive + j->slot, &live, sizeof(int), cudaMemcpyHostToDevice, s->st);
-            tp.newSlot[k] = (uint32_t)j->slot;
-            tp.newStart[k] = (uint32_t)admitted[k].start;
-            tp.newPrefix[k] = total;
-            total += (uint32_t)admitted[k].count;
-            j->admitTick = s->ticksLaunched;
+            if (admitted[k].express) {
+                tp.expSlot[nExp] = (uint32_t)j->slot;
+                tp.expPrefix[nExp] = expTotal;
+                expTotal += (uint32_t)admitted[k].count;
+                nExp++;
+            } else {
+                tp.newSlot[nNew] = (uint32_t)j->slot;
+                tp.newStart[nNew] = (uint32_t)admitted[k].start;
+                tp.newPrefix[nNew] = total;
+                total += (uint32_t)admitted[k].count;
+                nNew++;
+            }
         }
-        tp.newPrefix[admitted.size()] = total;
-        tp.newTotal = total;
+        tp.newCount = nNew, tp.newPrefix[nNew] = total, tp.newTotal = total;
+        tp.expCount = nExp, tp.expPrefix[nExp] = expTotal, tp.expTotal = expTotal;
         cudaMemcpyAsync(&s->dState->newCount, &tp.newCount, offsetof(ServerState, rays) - offsetof(ServerState, newCount), cudaMemcpyHostToDevice,
                         s->st);
         /* the tick */
@@ -554,7 +662,7 @@ void tick_loop_body(lh2g_server* s) {
             {
                 std::lock_guard<std::mutex> g(s->mu);
                 s->slots[j->slot] = nullptr;
-                s->pathsInFlight -= j->paths;
+                if (!j->express) s->pathsInFlight -= j->paths;
                 j->state = 2;
             }
             post(s, [s, j, ev] {
@@ -585,9 +693,15 @@ int build_tick_graph(lh2g_server* s) {
     if (s->tickGraph) cudaGraphDestroy(s->tickGraph), s->tickGraph = nullptr;
     if (cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return LH2G_ERR_CUDA;
     k_srv_generate<<<s->blocksGen, 256, 0, s->st>>>(s->dJobs, s->dState, s->Q);
+    /* express jobs on a second branch, beside the waves; the tick ends when both are done */
+    cudaEventRecord(s->evFork, s->st);
+    cudaStreamWaitEvent(s->side, s->evFork, 0);
+    k_srv_express<<<s->blocksExpress, WAVE_BLOCK, 0, s->side>>>(T, s->dJobs, s->dState, s->dAlive);
+    cudaEventRecord(s->evJoin, s->side);
     k_srv_extend<<<s->blocksExtend, 128, 0, s->st>>>(T, s->dJobs, s->dState, s->Q);
     k_srv_shade<<<s->blocksShade, WAVE_BLOCK, 0, s->st>>>(T, s->dJobs, s->dState, s->Q, s->dAlive);
     k_srv_connect<<<s->blocksConnect, 128, 0, s->st>>>(T, s->dJobs, s->dState, s->Q);
+    cudaStreamWaitEvent(s->st, s->evJoin, 0);
     k_srv_end<<<1, 1, 0, s->st>>>(s->dState);
     cudaMemcpyAsync(s->hAlive, s->dAlive, sizeof(int) * MAX_SLOTS, cudaMemcpyDeviceToHost, s->st);
     if (cudaStreamEndCapture(s->st, &s->tickGraph) != cudaSuccess) return LH2G_ERR_CUDA;
@@ -621,6 +735,9 @@ int lh2g_server_create(int device, long long pathCapacity, lh2g_server** out) {
     bool ok = cudaSetDevice(device) == cudaSuccess;
     ok = ok && cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) == cudaSuccess;
     ok = ok && cudaStreamCreateWithFlags(&s->io, cudaStreamNonBlocking) == cudaSuccess;
+    ok = ok && cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) == cudaSuccess;
+    ok = ok && cudaEventCreateWithFlags(&s->evFork, cudaEventDisableTiming) == cudaSuccess;
+    ok = ok && cudaEventCreateWithFlags(&s->evJoin, cudaEventDisableTiming) == cudaSuccess;
     const size_t cap = (size_t)pathCapacity;
     for (int k = 0; k < 2 && ok; k++)
         ok = cudaMalloc((void**)&s->Q.O[k], 16 * cap) == cudaSuccess && cudaMalloc((void**)&s->Q.D[k], 16 * cap) == cudaSuccess &&
@@ -647,6 +764,10 @@ int lh2g_server_create(int device, long long pathCapacity, lh2g_server** out) {
         s->blocksExtend = occupancy_blocks(k_srv_extend, 128);
         s->blocksShade = occupancy_blocks(k_srv_shade, WAVE_BLOCK);
         s->blocksConnect = occupancy_blocks(k_srv_connect, 128);
+        /* a modest share of the SMs (two CTAs each): the express branch runs beside the waves */
+        int sms = 1;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        s->blocksExpress = 2 * sms;
         s->blocksTrace0 = persistent_blocks_trace(0);
         s->blocksTrace1 = persistent_blocks_trace(1);
         s->tickEv.resize(4);
@@ -682,6 +803,7 @@ int lh2g_server_destroy(lh2g_server* s) {
     cudaSetDevice(s->device);
     if (s->st) cudaStreamSynchronize(s->st);
     if (s->io) cudaStreamSynchronize(s->io);
+    if (s->side) cudaStreamSynchronize(s->side);
     if (s->tickExec) cudaGraphExecDestroy(s->tickExec);
     if (s->tickGraph) cudaGraphDestroy(s->tickGraph);
     for (auto& e : s->tickEv) if (e) cudaEventDestroy(e);
@@ -693,11 +815,29 @@ int lh2g_server_destroy(lh2g_server* s) {
     for (auto& kv : s->jobs) delete kv.second;
     if (s->st) cudaStreamDestroy(s->st);
     if (s->io) cudaStreamDestroy(s->io);
+    if (s->side) cudaStreamDestroy(s->side);
+    if (s->evFork) cudaEventDestroy(s->evFork);
+    if (s->evJoin) cudaEventDestroy(s->evJoin);
     delete s;
     return LH2G_OK;
 }
 
 const char* lh2g_server_last_error(lh2g_server* s) { return s ? s->err.c_str() : "null server"; }
+
+int lh2g_server_setting(lh2g_server* s, const char* name, double value) {
+    if (!s || !name || !(value >= 0.0)) return LH2G_ERR_INVALID;
+    std::lock_guard<std::mutex> g(s->mu);
+    if (!strcmp(name, "expressMaxPaths")) s->expressMax = (long long)value;
+    else if (!strcmp(name, "expressBudget")) s->expressBudget = (long long)value;
+    else if (!strcmp(name, "tickBudget")) s->tickBudget = std::max(1ll, (long long)value);
+    else if (!strcmp(name, "maxWaitSeconds")) s->maxWaitS = value;
+    else {
+        s->err = std::string("unknown server setting ") + name;
+        return LH2G_ERR_INVALID;
+    }
+    if (s->expressMax > s->expressBudget) s->expressBudget = s->expressMax;   /* every express job fits a tick */
+    return LH2G_OK;
+}
 
 int lh2g_server_add_scene(lh2g_server* s, lh2g_context* ctx, int* sceneId) {
     if (!s || !ctx || !sceneId) return LH2G_ERR_INVALID;

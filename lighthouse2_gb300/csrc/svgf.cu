@@ -163,6 +163,9 @@ __global__ void __launch_bounds__(BX* BY) k_prepare(const SvgfBuffers b, const S
 }
 
 /* ---- applyFilterKernel ---- */
+#ifndef LH2G_SVGF_UNROLL
+#define LH2G_SVGF_UNROLL 0   /* tuning switch: 0 rolled tap loops, 1 inner loop unrolled, 2 both unrolled */
+#endif
 template <int PHASE>
 __global__ void __launch_bounds__(BX* BY) k_apply(const SvgfBuffers b, const SvgfArgs a, const float4* __restrict__ A, const float4* __restrict__ B,
                                                   float4* __restrict__ C) {
@@ -188,12 +191,22 @@ __global__ void __launch_bounds__(BX* BY) k_apply(const SvgfBuffers b, const Svg
     const float rdir = -1.0f / (sigma * factor * sqrtf(var_dir + 0.00001f) + 0.00001f);
     const float rind = -1.0f / (sigma * factor * sqrtf(var_ind + 0.00001f) + 0.00001f);
     constexpr int step = 1 << (PHASE - 1);
+    /* the tap loops stay rolled (LH2G_SVGF_UNROLL 0): unrolled, the 20 tap bodies overflow the instruction cache
+     * and warps stall on instruction fetch */
+#if LH2G_SVGF_UNROLL >= 2
 #pragma unroll
+#else
+#pragma unroll 1
+#endif
     for (int vv = -2; vv <= 2; vv++) {
         const int v = vv * step + y;
         const int r = (vv == 2 || vv == -2) ? 1 : 2;
         if (v < 0 || v >= h) continue;
+#if LH2G_SVGF_UNROLL >= 1
 #pragma unroll
+#else
+#pragma unroll 1
+#endif
         for (int uu = -2; uu <= 2; uu++) {
             if (uu < -r || uu > r || (uu == 0 && vv == 0)) continue;
             const int u = min(max(uu * step + x, 0), w - 1);

@@ -31,13 +31,15 @@ def _bind(lib):
     lib.lh2g_server_wait.argtypes = [vp, ll, i, C.POINTER(JobTimes)]
     lib.lh2g_server_release.argtypes = [vp, ll]
     lib.lh2g_server_get_stats.argtypes = [vp, C.POINTER(ServerStats)]
+    lib.lh2g_server_setting.argtypes = [vp, C.c_char_p, C.c_double]
 
 
 class RenderServer:
     """One serving loop on one GPU. Scenes are RenderCore objects whose scene is finalized; they must outlive the
     server. Results land in numpy arrays owned by the job handles returned by submit_*."""
 
-    def __init__(self, path_capacity: int, device: int = 0):
+    def __init__(self, path_capacity: int, device: int = 0, **settings):
+        """settings: expressMaxPaths, expressBudget, tickBudget, maxWaitSeconds (lh2g_server_setting)."""
         self.lib = load_library()
         _bind(self.lib)
         self.srv = C.c_void_p()
@@ -46,6 +48,11 @@ class RenderServer:
             raise CoreError(f"lh2g_server_create failed with status {rc}")
         self._scenes = []
         self._keep = {}
+        for k, v in settings.items():
+            self.setting(k, v)
+
+    def setting(self, name: str, value: float):
+        self._check(self.lib.lh2g_server_setting(self.srv, name.encode(), float(value)), f"setting {name}")
 
     def _check(self, rc, what):
         if rc != 0:

@@ -85,3 +85,25 @@ def test_cache_frames_beat_plain_at_equal_time(setup):
     rmse_cache = np.sqrt(np.mean((img_cache - ref) ** 2))
     assert rmse_cache < 0.85 * rmse_plain, (rmse_plain, rmse_cache, t_plain, t_cache, n_cache)
     cache.close()
+
+
+def test_queued_cache_frames_match_waiting_ones(setup):
+    """Cache frames queued without waiting (stats=None: they overlap on the core's lanes, their cache work chained
+    in submission order) give what frames that wait for the device give: the first frame (initial weights) bit for
+    bit, later ones within the run-to-run noise of the gradient atomics."""
+    sc, core, view, ref = setup
+    out = []
+    for stats in (True, False):
+        cache = RadianceCache(sc.bounds[0], sc.bounds[1], learning_rate=1e-2, seed=9)
+        core.render_nrc(cache, view, params(300), stats=stats)
+        core.WaitForRender()
+        first = core.read_accumulator().copy()
+        for k in range(1, 8):
+            core.render_nrc(cache, view, params(300 + k), accumulate=True, stats=stats)
+        core.WaitForRender()
+        out.append((first, core.read_accumulator().copy(), cache.params()[0].copy()))
+        cache.close()
+    (f0, a0, w0), (f1, a1, w1) = out
+    assert np.array_equal(f0.view(np.uint32), f1.view(np.uint32))
+    assert np.sqrt(np.mean((a0 - a1) ** 2)) <= 1e-3 * np.sqrt(np.mean(a0 ** 2))
+    assert np.linalg.norm(w0 - w1) <= 1e-3 * np.linalg.norm(w0)

@@ -3,7 +3,8 @@
 Jobs of two resident scenes with different resolutions, sample counts and depths, submitted all at once so that
 they share the wavefront queues, must each produce exactly the image the plain core renders for the same job
 alone (lh2g_render_ex, accumulator after one frame), and the same image when the job runs alone through the
-server. A capacity smaller than the sum of the jobs makes them wait for path memory and still complete exactly;
+server, whether the jobs go through the shared queues, run as express jobs (each path traced whole within a tick)
+or both. A capacity smaller than the sum of the jobs makes them wait for path memory and still complete exactly;
 a job larger than the capacity is refused at submission. Ray queries run beside the render jobs and return what
 lh2g_trace_host returns. One job is checked against the CPU oracle as well.
 """
@@ -45,7 +46,8 @@ def plain_core_image(core, view, p):
     return core.read_accumulator()
 
 
-def test_jobs_in_the_mix_equal_plain_core_and_alone(two_scenes):
+@pytest.mark.parametrize("express_max", [0, 5000, None])   # all through the queues, mixed, all express
+def test_jobs_in_the_mix_equal_plain_core_and_alone(two_scenes, express_max):
     from lighthouse2_gb300.server import RenderServer
     (sa, ca), (sb, cb) = two_scenes
     cores = [ca, cb]
@@ -53,7 +55,7 @@ def test_jobs_in_the_mix_equal_plain_core_and_alone(two_scenes):
     for j in JOBS:
         view, p = job_inputs(*j)
         expect.append(plain_core_image(cores[j[0]], view, p))
-    srv = RenderServer(path_capacity=1 << 20)
+    srv = RenderServer(path_capacity=1 << 20, **({} if express_max is None else {"expressMaxPaths": express_max}))
     sid = [srv.add_scene(ca), srv.add_scene(cb)]
     # all at once: the jobs share ticks
     ids = []
@@ -81,7 +83,7 @@ def test_admission_by_path_memory_and_queries(two_scenes, oracle_lib):
     from lighthouse2_gb300.server import RenderServer
     (sa, ca), (sb, cb) = two_scenes
     cap = 20000                                  # smaller than the sum of the jobs below: they queue for memory
-    srv = RenderServer(path_capacity=cap)
+    srv = RenderServer(path_capacity=cap, expressMaxPaths=0)   # (express jobs would not use queue memory)
     sid = [srv.add_scene(ca), srv.add_scene(cb)]
     jobs = [(0, 96, 96, 2, 5, 2, 0), (1, 100, 100, 1, 6, 3, 1), (0, 64, 64, 4, 4, 1, 2), (1, 128, 64, 2, 5, 2, 3)]
     assert all(j[1] * j[2] * j[3] <= cap for j in jobs) and sum(j[1] * j[2] * j[3] for j in jobs) > cap
