@@ -192,6 +192,17 @@ def algorithmic_bytes(kind, n_in, n_ext, n_shadow):
 SVGF_BYTES_PER_PIXEL = (96 + 56) + (64 + 56 + 16) + 2 * (64 + 16) + (40 + 16) + (16 + 16)
 
 
+def reduce_replicas(dist, ms, units, device):
+    """Replicas (one process per GPU, no collective on the data path): the job's time is the slowest rank's, its
+    work the sum over ranks. Returns (max ms, total units)."""
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    dist.all_reduce(u)
+    return float(t.item()), int(u.item())
+
+
 def decode_launches(lt_all, frames, counts, waves, W, H):
     """Per stage kind: [summed launch ms, algorithmic bytes, launches] over `frames` frames whose per-launch device
     times are lt_all (per frame: generate, (extend, shade, connect) x waves, tail if used, finalize) and whose
@@ -537,12 +548,7 @@ def run_gb300(args):
         ext_rays += W * H + int(c[:-1, 0].sum())
         shadow_rays += int(c[:, 1].sum())
     if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        r = torch.tensor([float(rays)], device="cuda")
-        dist.all_reduce(r)
-        rays = int(r.item())
+        ms, rays = reduce_replicas(dist, ms, rays, "cuda")
     value = rays / (ms / 1e3) / 1e6
     # ---- end-to-end through the C ABI: camera and parameters in from host memory, every frame copied back into
     # pinned host memory (lh2g_render_to_host; consecutive frames and their copies overlap), timed on the host ----

@@ -160,8 +160,9 @@ LH2G_API int lh2g_render_noalloc(lh2g_context* ctx, const lh2g_view* view, const
  * (oldest first once one has waited 0.2 s) while their paths fit in the server's path capacity (the admission
  * unit, 48 B x 2 + 64 B of queue memory per path plus 16 B of per-path radiance), and the paths of every admitted
  * job share one set of wavefront queues; one CUDA graph per tick advances every in-flight path by one vertex.
- * Express jobs (at most "expressMaxPaths" paths) skip the queues: each of their paths is traced to its end within
- * one tick, beside the waves, so a small job finishes in one tick instead of one tick per bounce. A job's image is the per-pixel sum of its
+ * Express jobs (at most "expressMaxPaths" paths, off by default) skip the queues: each of their paths is traced to
+ * its end within one tick by one thread, beside the waves, so a small job finishes in one tick instead of one tick
+ * per bounce. A job's image is the per-pixel sum of its
  * samples (what lh2g_render_ex with accumulate = 0 leaves in the accumulator), bit for bit the same whatever else
  * is in flight. Ray queries run concurrently on a second stream. Scenes are finalized contexts, added by
  * reference: they must outlive the server and stay unchanged while it runs. Host buffers passed to submit must
@@ -175,8 +176,9 @@ typedef struct lh2g_server_stats {
 } lh2g_server_stats;
 LH2G_API int lh2g_server_create(int device, long long pathCapacity, lh2g_server** out);
 LH2G_API int lh2g_server_destroy(lh2g_server* server);   /* finishes the jobs it holds first */
-/* Scheduling settings, applied to jobs admitted afterwards: "expressMaxPaths" (default 262144; 0: no express
- * jobs), "expressBudget" (express paths per tick, default 1048576), "tickBudget" (new queue paths per tick,
+/* Scheduling settings, applied to jobs admitted afterwards: "expressMaxPaths" (default 0: no express jobs; a
+ * path traced whole by one thread is slower than the waves, so express jobs only pay when the GPU is otherwise
+ * idle), "expressBudget" (express paths per tick, default 1048576), "tickBudget" (new queue paths per tick,
  * default clamp(capacity, 2^20, 2^22)), "maxWaitSeconds" (0.2). Results do not depend on them. */
 LH2G_API int lh2g_server_setting(lh2g_server* server, const char* name, double value);
 LH2G_API const char* lh2g_server_last_error(lh2g_server* server);

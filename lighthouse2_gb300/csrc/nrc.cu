@@ -481,9 +481,11 @@ int lh2g_nrc_create(int device, const lh2g_nrc_config* cfg, lh2g_nrc** out) {
     for (auto& x : g) x = rng_uniform(seed, 1e-4f);
     ok = cudaMemcpy(c->pW, w.data(), sizeof(float) * WMASTER, cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemcpy(c->pG, g.data(), sizeof(float) * GRID_PARAMS, cudaMemcpyHostToDevice) == cudaSuccess;
-    for (float* q : {c->mW, c->vW, c->gW}) ok = ok && cudaMemset(q, 0, sizeof(float) * WMASTER) == cudaSuccess;
-    for (float* q : {c->mG, c->vG, c->gG}) ok = ok && cudaMemset(q, 0, sizeof(float) * GRID_PARAMS) == cudaSuccess;
-    ok = ok && cudaMemset(c->Wdev, 0, sizeof(__nv_bfloat16) * WDEV) == cudaSuccess && cudaMemset(c->dErr, 0, 16) == cudaSuccess;
+    /* on the cache's own (non-blocking) stream, ordered before the copies below: a legacy-stream memset would not be */
+    for (float* q : {c->mW, c->vW, c->gW}) ok = ok && cudaMemsetAsync(q, 0, sizeof(float) * WMASTER, c->st) == cudaSuccess;
+    for (float* q : {c->mG, c->vG, c->gG}) ok = ok && cudaMemsetAsync(q, 0, sizeof(float) * GRID_PARAMS, c->st) == cudaSuccess;
+    ok = ok && cudaMemsetAsync(c->Wdev, 0, sizeof(__nv_bfloat16) * WDEV, c->st) == cudaSuccess &&
+         cudaMemsetAsync(c->dErr, 0, 16, c->st) == cudaSuccess && cudaMemsetAsync(c->dLoss, 0, 16, c->st) == cudaSuccess;
     ok = ok && cudaFuncSetAttribute(k_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)INFER_SMEM) == cudaSuccess;
     ok = ok && cudaFuncSetAttribute(k_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TRAIN_SMEM) == cudaSuccess;
     /* all of the unified L1 / shared storage as shared memory, so that several inference CTAs share an SM: the
@@ -494,9 +496,10 @@ int lh2g_nrc_create(int device, const lh2g_nrc_config* cfg, lh2g_nrc** out) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     cudaDeviceGetAttribute(&smemSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_infer, TILE, INFER_SMEM) != cudaSuccess) per = 0;
-    /* resident CTAs per SM: the occupancy calculator's answer, else what shared memory allows (1 KB reserved per
-     * CTA); at most 4 (4 x 64 of the SM's 512 TMEM columns) */
-    if (per < 1) per = smemSM / (int)(INFER_SMEM + 1024);
+    /* resident CTAs per SM: what shared memory allows with the carveout above (1 KB reserved per CTA; the
+     * calculator may assume a smaller carveout), at most 4 (4 x 64 of the SM's 512 TMEM columns). Surplus CTAs
+     * would only wait: the kernel strides over its tiles. */
+    per = std::max(per, smemSM / (int)(INFER_SMEM + 1024));
     c->blocksInfer = sms * std::max(1, std::min(per, 4));
     c->blocksTrain = sms;
     if (launch_copies(c) != LH2G_OK || cudaStreamSynchronize(c->st) != cudaSuccess) return fail(LH2G_ERR_CUDA);
@@ -617,6 +620,7 @@ int lh2g_nrc_train_counted(lh2g_nrc* c, const float* queries, const float* targe
 int lh2g_nrc_last_loss(lh2g_nrc* c, float* loss) {
     if (!c || !loss) return LH2G_ERR_INVALID;
     cudaSetDevice(c->device);
+    NCK(cudaDeviceSynchronize());   /* training may have run on any stream */
     NCK(cudaMemcpy(loss, c->dLoss, 4, cudaMemcpyDeviceToHost));
     uint32_t e = 0;
     NCK(cudaMemcpy(&e, c->dErr, 4, cudaMemcpyDeviceToHost));

@@ -370,7 +370,7 @@ struct lh2g_server {
     Queues Q;
     long long capacity = 0;
     long long tickBudget = 0;          /* new paths per tick */
-    long long expressMax = 1ll << 18;  /* jobs of at most this many paths are express jobs */
+    long long expressMax = 0;          /* jobs of at most this many paths are express jobs (0: none) */
     long long expressBudget = 1ll << 20;   /* express paths per tick */
     double maxWaitS = 0.2;             /* a job waiting longer than this is admitted before smaller ones */
     cudaGraphExec_t tickExec = nullptr;

@@ -46,7 +46,7 @@ def plain_core_image(core, view, p):
     return core.read_accumulator()
 
 
-@pytest.mark.parametrize("express_max", [0, 5000, None])   # all through the queues, mixed, all express
+@pytest.mark.parametrize("express_max", [None, 5000, 1 << 20])   # all through the queues (default), mixed, all express
 def test_jobs_in_the_mix_equal_plain_core_and_alone(two_scenes, express_max):
     from lighthouse2_gb300.server import RenderServer
     (sa, ca), (sb, cb) = two_scenes
