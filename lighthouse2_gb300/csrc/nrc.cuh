@@ -32,6 +32,10 @@ constexpr int LEVELS = 12, LOG2T = 19, TABLE = 1 << LOG2T, FEAT = 2;
 constexpr int WMASTER = 4 * HID * IN + OUT * HID;   /* fp32 master weights, row-major [out][in] per layer */
 constexpr int WDEV = 4 * HID * IN + OUTP * HID;     /* bf16 device weights, output layer padded to 16 rows */
 constexpr long long GRID_PARAMS = (long long)LEVELS * TABLE * FEAT;
+#ifndef LH2G_NRC_LEVEL_UNROLL
+#define LH2G_NRC_LEVEL_UNROLL 12  /* tuning switch: hash-grid levels encoded per loop iteration (12: all) */
+#endif
+constexpr int LEVEL_UNROLL = LH2G_NRC_LEVEL_UNROLL;
 
 /* encoding parameters computed on the host */
 struct GridSpec {
@@ -86,7 +90,9 @@ __device__ __forceinline__ void sph01(const float3 d, float& th, float& ph) {
 /* the 64 network inputs of a query (fp32; the kernels round them to bf16) */
 __device__ __forceinline__ void encode(const GridSpec& G, const __half2* __restrict__ grid, const float4* q, float* e) {
     const float3 p = unit_position(G, q[0]);
-#pragma unroll 1
+    /* levels in groups of LEVEL_UNROLL so that several levels' gathers are in flight at once (the encoding is
+     * bound by the latency of these L2 reads) */
+#pragma unroll LEVEL_UNROLL
     for (int l = 0; l < LEVELS; l++) {
         const Cell c = grid_cell(G, l, p);
         float f0 = 0.0f, f1 = 0.0f;

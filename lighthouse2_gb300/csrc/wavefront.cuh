@@ -10,7 +10,8 @@ namespace lh2g {
 namespace {
 
 constexpr int WAVE_BLOCK = 128;
-constexpr int NRC_DEPTH = 2;   /* path length at which radiance-cache frames query the cache */
+constexpr int NRC_DEPTH = 2;   /* first path length at which radiance-cache frames query the cache */
+constexpr uint32_t S_CACHED = 8;   /* radiance-cache frames: the path has recorded its cache vertex */
 
 __device__ __forceinline__ uint32_t lanemask_lt() { uint32_t m; asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m)); return m; }
 
@@ -125,9 +126,11 @@ __device__ __forceinline__ void shade_core(const SceneGPU& S, const FrameGPU& F,
         return;
     }
     *accP = acc;
-    if ((F.flags & LH2G_RP_NRC) && depth == NRC_DEPTH && (FLAGS & S_SPECULAR) == 0) {
-        /* radiance cache: the query of this vertex (looking back along the ray), the throughput that reaches it and
-         * the radiance gathered before it; a training path (1 in 16) traces on, the others end here */
+    if ((F.flags & LH2G_RP_NRC) && depth >= NRC_DEPTH && (FLAGS & (S_SPECULAR | S_CACHED)) == 0) {
+        /* radiance cache, at the first vertex from path length 2 on that a diffuse bounce leads to (after a specular
+         * bounce the path footprint is still small: it traces on): the query of this vertex (looking back along the
+         * ray), the throughput that reaches it and the radiance gathered before it; a training path (1 in 16)
+         * traces on, the others end here */
         const bool train = (WangHash(pathIdx * 3u + F.cameraR0) & 15u) == 0u;
         const float side = dot(D, N) > 0 ? -1.0f : 1.0f;
         float4* rec = B.nrcRec + pathIdx;
@@ -142,6 +145,7 @@ __device__ __forceinline__ void shade_core(const SceneGPU& S, const FrameGPU& F,
             if (B.capSeeds) B.capSeeds[capIdx] = 0;
             return;
         }
+        FLAGS |= S_CACHED;
     }
     if (ROUGHNESS(sd) <= 0.001f || TRANSMISSION(sd) > 0.999f) FLAGS |= S_SPECULAR; else FLAGS &= ~S_SPECULAR;
     uint32_t seed = WangHash(pathIdx * 17u + R0);
