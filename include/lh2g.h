@@ -232,9 +232,9 @@ LH2G_API int lh2g_nrc_train_counted(lh2g_nrc* cache, const float* queries, const
                                     long long maxCount, void* stream);
 /* the mean loss of the last training batch (waits for the device) */
 LH2G_API int lh2g_nrc_last_loss(lh2g_nrc* cache, float* loss);
-/* One frame with the radiance cache (like lh2g_render_ex with accumulate): paths reaching their second vertex
- * through a diffuse bounce end there and add throughput x cache(query); one in sixteen of them trace on and
- * their radiance from that vertex on, divided by the throughput into it, trains the cache after the frame
+/* One frame with the radiance cache (like lh2g_render_ex with accumulate): a path ends at its first vertex from
+ * path length 2 on that a diffuse bounce leads to and adds throughput x cache(query) there; one in sixteen of
+ * them trace on and their radiance from that vertex on, divided by the throughput into it, trains the cache after the frame
  * (train != 0, at most 65536 samples, one Adam step). The plain estimator is unchanged everywhere else.
  * With stats == NULL the call returns once the frame is queued, and consecutive frames overlap like plain frames
  * (their cache work stays in submission order: each frame's inference sees the previous frame's update);
