@@ -166,9 +166,36 @@ __global__ void __launch_bounds__(BX* BY) k_prepare(const SvgfBuffers b, const S
 #ifndef LH2G_SVGF_UNROLL
 #define LH2G_SVGF_UNROLL 0   /* tuning switch: 0 rolled tap loops, 1 inner loop unrolled, 2 both unrolled */
 #endif
+/* The neighbours of a block's pixels (the block and a halo of 2 steps) are unpacked once per block into shared
+ * memory, four float4 per pixel: normal + depth, albedo + material id, direct light + its luminance, indirect light
+ * + its luminance; the taps read them there (unpacked per tap, the 20 taps of a pixel repeat the work of their
+ * neighbours). Columns are clamped to the image as the taps clamp them; rows outside the image are loaded clamped
+ * and never read. */
+template <int PHASE>
+struct ApplyTile {
+    static constexpr int STEP = 1 << (PHASE - 1), TW = BX + 4 * STEP, TH = BY + 4 * STEP, N = TW * TH;
+    static constexpr size_t BYTES = 4 * sizeof(float4) * N;
+};
+
 template <int PHASE>
 __global__ void __launch_bounds__(BX* BY) k_apply(const SvgfBuffers b, const SvgfArgs a, const float4* __restrict__ A, const float4* __restrict__ B,
                                                   float4* __restrict__ C) {
+    using T = ApplyTile<PHASE>;
+    extern __shared__ float4 tile[];
+    float4 *tN = tile, *tA = tile + T::N, *tD = tile + 2 * T::N, *tI = tile + 3 * T::N;
+    const int x0 = (int)(blockIdx.x * BX) - 2 * T::STEP, y0 = (int)(blockIdx.y * BY) - 2 * T::STEP;
+    for (int t = threadIdx.y * BX + threadIdx.x; t < T::N; t += BX * BY) {
+        const int u = min(max(x0 + t % T::TW, 0), a.W - 1), v = min(max(y0 + t / T::TW, 0), a.H - 1);
+        const size_t q = (size_t)u + (size_t)v * a.W;
+        const uint4 nf = __ldg(b.features + q);
+        const float4 nc = __ldg(A + q);
+        const float3 n = UnpackNormal2(nf.y), al = RGB32toHDR(nf.x), di = GetDirect(nc), in = GetIndirect(nc);
+        tN[t] = make_float4(n.x, n.y, n.z, __uint_as_float(nf.z));
+        tA[t] = make_float4(al.x, al.y, al.z, __uint_as_float(nf.w >> 4));
+        tD[t] = make_float4(di.x, di.y, di.z, Luminance(di));
+        tI[t] = make_float4(in.x, in.y, in.z, Luminance(in));
+    }
+    __syncthreads();
     Px p;
     if (!pixel(a.W, a.H, p)) return;
     const int w = a.W, h = a.H, x = p.x, y = p.y;
@@ -209,23 +236,22 @@ __global__ void __launch_bounds__(BX* BY) k_apply(const SvgfBuffers b, const Svg
 #endif
         for (int uu = -2; uu <= 2; uu++) {
             if (uu < -r || uu > r || (uu == 0 && vv == 0)) continue;
-            const int u = min(max(uu * step + x, 0), w - 1);
-            const size_t q = (size_t)u + (size_t)v * w;
-            const uint4 nf = __ldg(b.features + q);
-            const float4 nc = __ldg(A + q);
+            /* the tap's column, clamped to the image, is tile column x - x0 + uu * step (the tile holds clamped columns) */
+            const int t = (x - x0 + uu * step) + (v - y0) * T::TW;
+            const float4 tn = tN[t], ta = tA[t], td = tD[t], ti = tI[t];
             const float w_dist = (float)(uu * uu + vv * vv) * (-1.0f / 7.5f);
-            const float3 nDirect = GetDirect(nc), nIndirect = GetIndirect(nc);
-            float w_normal = pow128(fmaxf(0.0f, dot(UnpackNormal2(nf.y), localNormal)));
+            const float3 nDirect = make_float3(td.x, td.y, td.z), nIndirect = make_float3(ti.x, ti.y, ti.z);
+            float w_normal = pow128(fmaxf(0.0f, dot(make_float3(tn.x, tn.y, tn.z), localNormal)));
             const float expected = localDepth + localDdx * (float)(uu * step) + localDdy * (float)(vv * step);
-            const float depthError = fabsf(expected - __uint_as_float(nf.z));
+            const float depthError = fabsf(expected - tn.w);
             const float expectedDifference = fabsf(expected - localDepth);
             const float w_depth = depthError / fmaxf(0.00001f, (0.5f + (float)PHASE * 0.5f) * expectedDifference);
             /* material stop: the reference multiplies by the double literal 0.0001 here, i.e. in double; the same
              * float comes from exact integer arithmetic (no FP64 instruction) */
-            if ((nf.w >> 4) != localMatID) w_normal = material_stop(w_normal);
-            else w_normal = w_normal * dot(localColor, RGB32toHDR(nf.x));
-            float w_dir = w_normal * exp_cw(fabsf(localDirect - Luminance(nDirect)) * rdir + w_dist - w_depth);
-            float w_ind = w_normal * exp_cw(fabsf(localIndirect - Luminance(nIndirect)) * rind + w_dist - w_depth);
+            if (__float_as_uint(ta.w) != localMatID) w_normal = material_stop(w_normal);
+            else w_normal = w_normal * dot(localColor, make_float3(ta.x, ta.y, ta.z));
+            float w_dir = w_normal * exp_cw(fabsf(localDirect - td.w) * rdir + w_dist - w_depth);
+            float w_ind = w_normal * exp_cw(fabsf(localIndirect - ti.w) * rind + w_dist - w_depth);
             if (!isfinite(w_dir)) w_dir = 0;
             if (!isfinite(w_ind)) w_ind = 0;
             directSum = directSum + nDirect * w_dir, directWeightSum += w_dir;
@@ -365,9 +391,16 @@ __global__ void __launch_bounds__(BX* BY) k_finalize_no_taa(const SvgfArgs a, co
 void launch_svgf(const SvgfBuffers& b, const SvgfArgs& a, bool taa, cudaStream_t st) {
     const dim3 block(BX, BY), grid((a.W + BX - 1) / BX, (a.H + BY - 1) / BY);
     k_prepare<<<grid, block, 0, st>>>(b, a);
-    k_apply<1><<<grid, block, 0, st>>>(b, a, b.shading, b.filteredIN, b.filteredOUT);
-    k_apply<2><<<grid, block, 0, st>>>(b, a, b.filteredOUT, nullptr, b.filteredIN);
-    k_apply<3><<<grid, block, 0, st>>>(b, a, b.filteredIN, nullptr, b.shading);
+    static const bool attrs = [] {   /* the phase-3 tile (48 x 24 pixels, 72 KB) exceeds the 48 KB default */
+        cudaFuncSetAttribute(k_apply<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ApplyTile<1>::BYTES);
+        cudaFuncSetAttribute(k_apply<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ApplyTile<2>::BYTES);
+        cudaFuncSetAttribute(k_apply<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ApplyTile<3>::BYTES);
+        return true;
+    }();
+    (void)attrs;
+    k_apply<1><<<grid, block, ApplyTile<1>::BYTES, st>>>(b, a, b.shading, b.filteredIN, b.filteredOUT);
+    k_apply<2><<<grid, block, ApplyTile<2>::BYTES, st>>>(b, a, b.filteredOUT, nullptr, b.filteredIN);
+    k_apply<3><<<grid, block, ApplyTile<3>::BYTES, st>>>(b, a, b.filteredIN, nullptr, b.shading);
     if (taa) {
         k_taa<<<grid, block, 0, st>>>(b, a, b.shading, b.prevPixels, b.taaPixels);
         k_unsharpen<<<grid, block, 0, st>>>(a, b.taaPixels, b.target);
