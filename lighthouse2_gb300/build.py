@@ -76,5 +76,25 @@ def build(verbose=False, force=False):
     return LIB
 
 
+HARNESS = os.path.join(OUT, "headless_app")
+
+
+def build_harness(force=False):
+    """The headless Lighthouse 2 application (harness/headless_app.cpp): host C++ only, loads a core by name."""
+    os.makedirs(OUT, exist_ok=True)
+    src = os.path.join(HERE, "harness", "headless_app.cpp")
+    deps = [src] + [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
+    if force or _stale(HARNESS, deps):
+        cuda_inc = os.path.join(os.path.dirname(os.path.dirname(nvcc())), "include")
+        cmd = ["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), "-I", cuda_inc, src, "-o", HARNESS + ".tmp", "-ldl"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode:
+            sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+            raise RuntimeError("headless application build failed")
+        os.replace(HARNESS + ".tmp", HARNESS)
+    return HARNESS
+
+
 if __name__ == "__main__":
     print(build(verbose="-v" in sys.argv, force="-f" in sys.argv))
+    print(build_harness(force="-f" in sys.argv))
