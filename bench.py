@@ -260,7 +260,7 @@ def svgf_leg(core, W, H, steps, warmup):
 
 
 SERVING_MIXES = {
-    # the survey's job distribution: resolution in {256^2, 512^2, 1024^2, 1920x1080}, spp in {1, 4, 16}
+    # the serving workload's job distribution: resolution in {256^2, 512^2, 1024^2, 1920x1080}, spp in {1, 4, 16}
     "full": {"res": [(256, 256), (512, 512), (1024, 1024), (1920, 1080)], "spp": [1, 4, 16], "rates": [10, 20, 30, 40, 50, 60, 100, 200]},
     # small interactive requests only, where one job alone leaves most of the GPU idle
     "small": {"res": [(256, 256), (512, 512)], "spp": [1, 4], "rates": [100, 200, 300, 400, 500, 700, 1000, 2000]},

@@ -33,6 +33,11 @@ namespace lh2g {
 #ifndef LH2G_REFILL
 #define LH2G_REFILL 0
 #endif
+/* LH2G_SORT_CHILDREN 1: a node's hit children go on the stack sorted by entry distance; 0: the nearest is visited
+ * next, the others are pushed unsorted */
+#ifndef LH2G_SORT_CHILDREN
+#define LH2G_SORT_CHILDREN 1
+#endif
 /* with LH2G_REFILL: idle lanes of a warp take new rays once at least this many are idle (or all are) */
 #ifndef LH2G_REFILL_MIN
 #define LH2G_REFILL_MIN 1
@@ -111,9 +116,11 @@ struct Traversal {
         }
     }
 
-    /* tests the 8 children of interior node `entry` and pushes the hit ones, nearest on top */
+    /* tests the 8 children of interior node `entry`. LH2G_SORT_CHILDREN 1: pushes the hit ones, nearest on top,
+     * and returns false (the caller pops); 0: makes the nearest hit child the current entry, pushes the others
+     * unsorted and returns true (false when nothing was hit). Either order visits every box the ray may hit. */
     template <bool ANYHIT>
-    __device__ __forceinline__ void visit_node(const SceneGPU& S, uint32_t& status) {
+    __device__ __forceinline__ bool visit_node(const SceneGPU& S, uint32_t& status) {
         const uint4* np = S.nodes + (size_t)entry * 5;
         const uint4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3), n4 = __ldg(np + 4);
         /* slab distances in the form t(q) = q * a + b, a = 2^e * invD (exact), b = (p - O) * invD */
@@ -151,6 +158,27 @@ struct Traversal {
             /* key: distance with the low 3 bits replaced by the slot (rounded down: culling stays conservative) */
             key[i] = hit ? ((__float_as_uint(fmaxf(tn, 0.0f)) & ~7u) | (uint32_t)i) : 0xffffffffu;
         }
+        /* leaf code = kind | (count - 1) << 28 | first slot; the fields do not overlap, so it is a sum */
+        const uint32_t leafBase = (curInst < 0 ? 0x80000000u : 0x40000000u) - (1u << 28) + n1.y;
+#if !LH2G_SORT_CHILDREN
+        const uint32_t best = min(min(min(key[0], key[1]), min(key[2], key[3])), min(min(key[4], key[5]), min(key[6], key[7])));
+        nodes++;
+        if (best == 0xffffffffu) return false;
+        {
+            const uint32_t meta = __byte_perm(metaLo, metaHi, best & 7u) & 255u;
+            entry = (meta & 0x80u) ? n1.x + (meta & 7u) : leafBase + ((meta >> 5) << 28) + (meta & 31u);
+        }
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const uint32_t kk = key[k];
+            if (kk == 0xffffffffu || kk == best) continue;
+            const uint32_t meta = __byte_perm(metaLo, metaHi, kk & 7u) & 255u;
+            const uint32_t code = (meta & 0x80u) ? n1.x + (meta & 7u) : leafBase + ((meta >> 5) << 28) + (meta & 31u);
+            if (sp < LH2G_STACK) stack[sp++] = make_uint2(code, kk & ~7u);
+            else status |= LH2G_STATUS_STACK_OVERFLOW;
+        }
+        return true;
+#else
         if (!ANYHIT) {
             cx(key[0], key[1]), cx(key[2], key[3]), cx(key[4], key[5]), cx(key[6], key[7]);
             cx(key[0], key[2]), cx(key[1], key[3]), cx(key[4], key[6]), cx(key[5], key[7]);
@@ -159,8 +187,6 @@ struct Traversal {
             cx(key[2], key[4]), cx(key[3], key[5]);
             cx(key[1], key[2]), cx(key[3], key[4]), cx(key[5], key[6]);
         }
-        /* leaf code = kind | (count - 1) << 28 | first slot; the fields do not overlap, so it is a sum */
-        const uint32_t leafBase = (curInst < 0 ? 0x80000000u : 0x40000000u) - (1u << 28) + n1.y;
         if (sp + 8 <= LH2G_STACK) {
 #pragma unroll
             for (int k = 7; k >= 0; k--) {
@@ -182,6 +208,8 @@ struct Traversal {
             }
         }
         nodes++;
+        return false;
+#endif
     }
 
     /* returns true while the ray has work left; anyHitDone is set when an any-hit query found an occluder */
@@ -191,14 +219,12 @@ struct Traversal {
         /* node phase: descend until the current entry is a leaf, an instance or a marker */
         while ((entry >> 30) == 0u) {
             if (++steps > MAX_STEPS) { status |= LH2G_STATUS_TRAVERSAL_LIMIT; return false; }
-            visit_node<ANYHIT>(S, status);
-            if (!pop<ANYHIT>()) return false;
+            if (!visit_node<ANYHIT>(S, status) && !pop<ANYHIT>()) return false;
         }
 #else
         if ((entry >> 30) == 0u) {
             if (++steps > MAX_STEPS) { status |= LH2G_STATUS_TRAVERSAL_LIMIT; return false; }
-            visit_node<ANYHIT>(S, status);
-            return pop<ANYHIT>();
+            return visit_node<ANYHIT>(S, status) || pop<ANYHIT>();
         }
 #endif
         if (++steps > MAX_STEPS) { status |= LH2G_STATUS_TRAVERSAL_LIMIT; return false; }

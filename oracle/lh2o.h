@@ -43,7 +43,7 @@ int lh2o_set_sky(lh2o_scene* s, const float* rgb, int width, int height, const f
 int lh2o_finalize(lh2o_scene* s);
 
 /* Ray queries. mode 0: closest hit into hits (prim = -1 on miss); mode 1: any hit, occluded[i] = 0/1.
- * brute != 0 tests every triangle of every instance (the judge of the BVH). */
+ * brute != 0 tests every triangle of every instance (the check of the BVH). */
 int lh2o_trace(lh2o_scene* s, const lh2g_ray* rays, long long n, int mode, int brute, lh2g_hit* hits,
                uint32_t* occluded, int nthreads);
 
