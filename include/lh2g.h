@@ -242,6 +242,10 @@ LH2G_API int lh2g_nrc_last_loss(lh2g_nrc* cache, float* loss);
 typedef struct lh2g_nrc_frame_stats { uint32_t queries, trainSamples; float loss; } lh2g_nrc_frame_stats;
 LH2G_API int lh2g_render_nrc(lh2g_context* ctx, lh2g_nrc* cache, const lh2g_view* view, const lh2g_render_params* params, int accumulate,
                              int train, lh2g_nrc_frame_stats* stats);
+/* Self-test of the bounded tensor-core waits: a kernel waits on an mbarrier that nothing arrives on, gives up
+ * after `limit` polls and sets *status to 1 (the error word every timed-out wait of the cache kernels raises);
+ * the device stays usable. */
+LH2G_API int lh2g_nrc_wait_selftest(int device, uint32_t limit, uint32_t* status);
 /* host buffers, synchronous */
 LH2G_API int lh2g_nrc_infer_host(lh2g_nrc* cache, const float* queries, long long n, float* out);
 LH2G_API int lh2g_nrc_train_host(lh2g_nrc* cache, const float* queries, const float* targets, long long n, int update, float* lossOut);

@@ -375,6 +375,19 @@ __global__ void k_adam(float* __restrict__ p, float* __restrict__ m, float* __re
     }
 }
 
+/* Self-test of the bounded waits: an mbarrier that nothing arrives on. The wait gives up after `limit` polls and
+ * the kernel reports it, the failure path every tensor-core wait of this file takes. */
+__global__ void k_wait_probe(const uint32_t limit, uint32_t* status) {
+    __shared__ uint64_t mbar;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&mbar, 1);
+        tc::mbar_fence_init();
+    }
+    __syncthreads();
+    const bool done = tc::mbar_wait(&mbar, 0, limit);
+    if (!__syncthreads_and(done) && threadIdx.x == 0) atomicOr(status, ERR_TIMEOUT);
+}
+
 __global__ void k_to_copies(const float* __restrict__ p, const long long n, __nv_bfloat16* __restrict__ outBf16, __half* __restrict__ outHalf) {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         if (outBf16) outBf16[i] = __float2bfloat16_rn(p[i]);
@@ -646,6 +659,21 @@ int lh2g_nrc_train(lh2g_nrc* c, const float* queries, const float* targets, long
         if (e) return nfail(c, LH2G_ERR_CUDA, "radiance cache: a tensor-core completion wait ran out");
     }
     return LH2G_OK;
+}
+
+int lh2g_nrc_wait_selftest(int device, uint32_t limit, uint32_t* status) {
+    if (!status || limit == 0) return LH2G_ERR_INVALID;
+    if (cudaSetDevice(device) != cudaSuccess) return LH2G_ERR_CUDA;
+    uint32_t* d = nullptr;
+    if (cudaMalloc((void**)&d, 4) != cudaSuccess) return LH2G_ERR_OOM;
+    bool ok = cudaMemset(d, 0, 4) == cudaSuccess;
+    if (ok) {
+        k_wait_probe<<<1, 32>>>(limit, d);
+        ok = cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess;
+    }
+    ok = ok && cudaMemcpy(status, d, 4, cudaMemcpyDeviceToHost) == cudaSuccess;
+    cudaFree(d);
+    return ok ? LH2G_OK : LH2G_ERR_CUDA;
 }
 
 /* host-memory forms (tests, small batches): copy in, run on the cache's stream, copy out */

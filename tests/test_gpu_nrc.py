@@ -94,3 +94,21 @@ def test_training_reduces_error(pair):
     assert np.mean(losses[-20:]) < 0.2 * np.mean(losses[:5]), (losses[:5], losses[-5:])
     assert err1 < 0.3 * err0, (err0, err1)
     cache2.close()
+
+
+def test_bounded_wait_reports_timeout_and_device_stays_usable(pair):
+    """A tensor-core completion wait that never completes gives up after its poll limit and raises the error word
+    (no hang, no trap); the cache keeps working afterwards."""
+    import ctypes as C
+    cache, o = pair
+    lib = cache.lib
+    lib.lh2g_nrc_wait_selftest.argtypes = [C.c_int, C.c_uint32, C.POINTER(C.c_uint32)]
+    status = C.c_uint32(0)
+    assert lib.lh2g_nrc_wait_selftest(0, 64, C.byref(status)) == 0
+    assert status.value == 1
+    mlp, grid = random_params(21)
+    cache.set_params(mlp, grid)
+    q = random_queries(256, 22)
+    got = cache.infer(q)
+    exp = o.forward(grid, mlp, q, emulate=True)
+    assert rel(got[:, :3], exp[:, :3]) <= 1e-2
