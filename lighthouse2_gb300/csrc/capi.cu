@@ -196,6 +196,7 @@ struct lh2g_context {
     int timedLaunches = 0;             /* launches timed since the last lh2g_get_launch_times */
     static constexpr int MAX_TIMED_LAUNCHES = 1 << 14;
     int blocksExtend = 0, blocksConnect = 0, blocksShade = 0, blocksTail = 0;
+    int fullBlocks[3] = {0, 0, 0};     /* extend, connect, shade grids at full occupancy (setting "waveOccupancy" scales them) */
     /* path length from which the remaining paths run to their end in one persistent kernel (0: wave loop
      * to the end); a scheduling choice only, results are the same */
     int tailDepth = 5;
@@ -419,9 +420,9 @@ int lh2g_create(int device, lh2g_context** out) {
     ctx->stats.ccMajor = (uint32_t)prop.major, ctx->stats.ccMinor = (uint32_t)prop.minor;
     ctx->stats.VRAM = (uint32_t)(prop.totalGlobalMem >> 20);
     ctx->stats.probedTriid = -1;
-    ctx->blocksExtend = persistent_blocks_wave(0);
-    ctx->blocksConnect = persistent_blocks_wave(1);
-    ctx->blocksShade = persistent_blocks_wave(2);
+    ctx->blocksExtend = ctx->fullBlocks[0] = persistent_blocks_wave(0);
+    ctx->blocksConnect = ctx->fullBlocks[1] = persistent_blocks_wave(1);
+    ctx->blocksShade = ctx->fullBlocks[2] = persistent_blocks_wave(2);
     ctx->blocksTail = persistent_blocks_wave(3);
     *out = ctx;
     return LH2G_OK;
@@ -693,7 +694,13 @@ int lh2g_setting(lh2g_context* ctx, const char* name, float value) {
     else if (!strcmp(name, "clampIndirect")) ctx->clampIndirect = value;
     else if (!strcmp(name, "filter")) ctx->filterEnabled = value == 0 ? 0 : 1;
     else if (!strcmp(name, "TAA")) ctx->taaEnabled = value == 0 ? 0 : 1;
-    else if (!strcmp(name, "pipelineFrames")) {
+    else if (!strcmp(name, "waveOccupancy")) {
+        /* fraction of a full GPU the persistent wave kernels of one frame take (frames in flight share the rest) */
+        if (!(value > 0.0f && value <= 1.0f)) return fail(ctx, LH2G_ERR_INVALID, "setting waveOccupancy: (0, 1]");
+        JOIN();
+        int* blocks[3] = {&ctx->blocksExtend, &ctx->blocksConnect, &ctx->blocksShade};
+        for (int k = 0; k < 3; k++) *blocks[k] = std::max(1, (int)((float)ctx->fullBlocks[k] * value + 0.5f));
+    } else if (!strcmp(name, "pipelineFrames")) {
         if (value < 0 || value > lh2g_context::MAX_LANES) return fail(ctx, LH2G_ERR_INVALID, "setting pipelineFrames: 0..3 frames in flight");
         JOIN();
         ctx->pipelineFrames = (int)value;

@@ -78,7 +78,15 @@ __device__ __forceinline__ void shade_path(const SceneGPU& S, const FrameGPU& F,
     shade_core(S, F, B, depth, B.O[q][i], B.D[q][i], B.T[q][i], B.hits[i], out, pot);
 }
 
+/* tuning switch: resident CTAs per SM the shading kernel is compiled for (register cap); 0 leaves it to the compiler */
+#ifndef LH2G_SHADE_MINBLOCKS
+#define LH2G_SHADE_MINBLOCKS 0
+#endif
+#if LH2G_SHADE_MINBLOCKS > 0
+__global__ void __launch_bounds__(WAVE_BLOCK, LH2G_SHADE_MINBLOCKS) k_shade(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int depth) {
+#else
 __global__ void __launch_bounds__(WAVE_BLOCK) k_shade(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int depth) {
+#endif
     Counters* C = B.counters;
     const uint32_t count = queue_count(F, C, depth);
     const int nq = depth & 1;
