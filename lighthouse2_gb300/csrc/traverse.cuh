@@ -33,6 +33,12 @@ namespace lh2g {
 #ifndef LH2G_REFILL
 #define LH2G_REFILL 0
 #endif
+/* LH2G_SPECULATIVE 1: a lane that reaches a triangle leaf while other lanes of its warp still visit interior
+ * nodes sets the leaf aside and visits nodes too; it tests the leaf with the next one it reaches, before it leaves
+ * the instance, or at the end of the ray (Aila and Laine's speculative traversal). 0: one entry per step. */
+#ifndef LH2G_SPECULATIVE
+#define LH2G_SPECULATIVE 0
+#endif
 /* LH2G_SORT_CHILDREN 1: a node's hit children go on the stack sorted by entry distance; 0: the nearest is visited
  * next, the others are pushed unsorted */
 #ifndef LH2G_SORT_CHILDREN
@@ -93,6 +99,7 @@ struct Traversal {
     float tmin, tmax;
     int sp, curInst;
     uint32_t entry, steps, nodes, tris;
+    uint32_t postponed;   /* LH2G_SPECULATIVE: a triangle leaf set aside (0: none) */
     bool found;
     HitRec best;
 
@@ -102,6 +109,37 @@ struct Traversal {
         best.t = t1, best.u = best.v = 0.0f, best.inst = -1, best.prim = NOHIT;
         found = false, sp = 0, curInst = -1, steps = 0, nodes = 0, tris = 0;
         entry = S.tlasRoot;
+        postponed = 0u;
+    }
+
+    /* the triangles of a leaf entry; false when an any-hit query found an occluder */
+    template <bool ANYHIT>
+    __device__ __forceinline__ bool leaf(const SceneGPU& S, const uint32_t code, bool& anyHitDone) {
+        const uint32_t first = code & 0x0fffffffu, cnt = ((code >> 28) & 3u) + 1u;
+        for (uint32_t k = 0; k < cnt; k++) {
+            const float4* td = S.triData + (size_t)(first + k) * 3;
+            const float4 a = __ldg(td), b = __ldg(td + 1), c = __ldg(td + 2);
+            float t, u, v;
+            tris++;
+            if (!isect_tri(O, D, a, b, c, t, u, v)) continue;
+            if (!(t > tmin && t < tmax)) continue;
+            if (ANYHIT) { anyHitDone = true; return false; }
+            const int prim = __float_as_int(a.w);
+            if (!found || t < best.t || (t == best.t && (curInst < best.inst || (curInst == best.inst && prim < best.prim)))) {
+                best.t = t, best.u = u, best.v = v, best.inst = curInst, best.prim = prim;
+                found = true;
+            }
+        }
+        return true;
+    }
+
+    /* tests a set-aside leaf; false when an any-hit query found an occluder */
+    template <bool ANYHIT>
+    __device__ __forceinline__ bool flush(const SceneGPU& S, bool& anyHitDone) {
+        if (!postponed) return true;
+        const uint32_t p = postponed;
+        postponed = 0u;
+        return leaf<ANYHIT>(S, p, anyHitDone);
     }
 
     /* pops the next entry that can still hold a closer hit; false when the stack is empty */
@@ -221,6 +259,28 @@ struct Traversal {
             if (++steps > MAX_STEPS) { status |= LH2G_STATUS_TRAVERSAL_LIMIT; return false; }
             if (!visit_node<ANYHIT>(S, status) && !pop<ANYHIT>()) return false;
         }
+#elif LH2G_SPECULATIVE
+        /* lanes of the warp that are at interior nodes now (a lane at a leaf joins them instead of idling) */
+        const uint32_t atNode = __ballot_sync(__activemask(), (entry >> 30) == 0u);
+        if ((entry >> 30) == 0u) {
+            if (++steps > MAX_STEPS) { status |= LH2G_STATUS_TRAVERSAL_LIMIT; return false; }
+            if (visit_node<ANYHIT>(S, status) || pop<ANYHIT>()) return true;
+            flush<ANYHIT>(S, anyHitDone);   /* the stack is empty: the set-aside leaf ends the ray */
+            return false;
+        }
+        if ((entry >> 30) == 1u) {
+            if (++steps > MAX_STEPS) { status |= LH2G_STATUS_TRAVERSAL_LIMIT; return false; }
+            if (!postponed && atNode) {
+                postponed = entry;
+            } else if (!leaf<ANYHIT>(S, entry, anyHitDone) || !flush<ANYHIT>(S, anyHitDone)) {
+                return false;
+            }
+            if (pop<ANYHIT>()) return true;
+            flush<ANYHIT>(S, anyHitDone);
+            return false;
+        }
+        /* a marker or an instance changes the ray's space: the set-aside leaf (of the current space) goes first */
+        if (!flush<ANYHIT>(S, anyHitDone)) return false;
 #else
         if ((entry >> 30) == 0u) {
             if (++steps > MAX_STEPS) { status |= LH2G_STATUS_TRAVERSAL_LIMIT; return false; }
@@ -234,21 +294,7 @@ struct Traversal {
             invD = make_float3(safe_rcp(Dw.x), safe_rcp(Dw.y), safe_rcp(Dw.z));
             curInst = -1;
         } else if (kind == 1u) {
-            const uint32_t first = entry & 0x0fffffffu, cnt = ((entry >> 28) & 3u) + 1u;
-            for (uint32_t k = 0; k < cnt; k++) {
-                const float4* td = S.triData + (size_t)(first + k) * 3;
-                const float4 a = __ldg(td), b = __ldg(td + 1), c = __ldg(td + 2);
-                float t, u, v;
-                tris++;
-                if (!isect_tri(O, D, a, b, c, t, u, v)) continue;
-                if (!(t > tmin && t < tmax)) continue;
-                if (ANYHIT) { anyHitDone = true; return false; }
-                const int prim = __float_as_int(a.w);
-                if (!found || t < best.t || (t == best.t && (curInst < best.inst || (curInst == best.inst && prim < best.prim)))) {
-                    best.t = t, best.u = u, best.v = v, best.inst = curInst, best.prim = prim;
-                    found = true;
-                }
-            }
+            if (!leaf<ANYHIT>(S, entry, anyHitDone)) return false;
         } else {
             const uint32_t first = entry & 0x0fffffffu, cnt = ((entry >> 28) & 3u) + 1u;
             if (cnt > 1u && sp < LH2G_STACK) stack[sp++] = make_uint2(0x80000000u | ((cnt - 2u) << 28) | (first + 1u), 0u);
