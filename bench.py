@@ -40,7 +40,7 @@ sys.path.insert(0, ROOT)
 W_DEFAULT, H_DEFAULT = 1920, 1080
 MAX_DEPTH, RR_START = 8, 4
 WAVE_TAIL = 5          # path lengths >= 5 run in the persistent tail kernel (setting "waveTail")
-LANES = 3              # frames in flight (setting "pipelineFrames")
+LANES = 4              # frames in flight (setting "pipelineFrames")
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of two k_extend launches of this workload (waves 2 and 3 of
 # camera pose 1): 190.11 MB + 72.66 MB (profiles/k_extend_spheres_2m_1080p.md)
 EXTEND_CAPTURE = {"pose": 1, "waves": (2, 3), "dram_bytes": 190.109184e6 + 72.664832e6}

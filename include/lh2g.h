@@ -71,7 +71,7 @@ LH2G_API int lh2g_set_sky(lh2g_context* ctx, const float* rgb, int width, int he
  * renders filter-core frames (LH2G_RP_FILTER, Halton-jittered when TAA is on) and denoises them with SVGF.
  * Scheduling settings of this core (results do not change): "waveTail" (default 5; path lengths from this one on
  * run to their end in one persistent kernel; 0: one launch per stage and wave throughout) and "pipelineFrames"
- * (frames in flight, 0..3, default 3; 0 and 1 render one frame at a time; see lh2g_get_stream) and "waveOccupancy"
+ * (frames in flight, 0..4, default 4; 0 and 1 render one frame at a time; see lh2g_get_stream) and "waveOccupancy"
  * (fraction of the GPU the persistent wave kernels of one frame launch, (0, 1], default 1). */
 LH2G_API int lh2g_setting(lh2g_context* ctx, const char* name, float value);
 /* SetTarget (core_api_base.h:93), headless: the output is a device float4 buffer of width*height pixels. */

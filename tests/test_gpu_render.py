@@ -123,13 +123,13 @@ def test_wave_tail_split_changes_nothing(cornell, tail):
 
 
 def test_pipelined_frames_match_one_at_a_time(core_lib):
-    """Consecutive plain frames overlap on two or three lanes (setting "pipelineFrames"); the accumulator, the frame and the
+    """Consecutive plain frames overlap on two or four lanes (setting "pipelineFrames"); the accumulator, the frame and the
     statistics must equal those of the same frames rendered one at a time, whether frames accumulate, restart or
     converge through Render, and whatever is read between them."""
     sc = S.spheres_2m(seed=5, n_spheres=6, slices=40, stacks=26, tex_size=64)
     W, H = 160, 96
     results = {}
-    for pipe in (0, 2, 3):
+    for pipe in (0, 2, 4):
         core = RenderCore()
         core.set_scene(sc)
         core.SetTarget(W, H, 1)
@@ -157,6 +157,6 @@ def test_pipelined_frames_match_one_at_a_time(core_lib):
         out += hosts
         results[pipe] = out
         core.close()
-    for lanes in (2, 3):
+    for lanes in (2, 4):
         for a, b in zip(results[0], results[lanes]):
             assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
