@@ -17,6 +17,7 @@ depth 3, next-event estimation; frames follow a seeded 8-pose camera path. Seede
             launches per frame against the measured HBM bandwidth.
   serving   the serving loop on seeded job lists over 4 resident scenes against sequential plain-core renders of
             the same jobs: saturated throughput, and p50 / p99 latency under Poisson arrivals swept over rates.
+  ray_queries  closest-hit and any-hit queries of 16M incoherent and 16M secondary-like rays on the same BVH.
   radiance_cache  the cache estimator against the plain one on the same scene and frame size, RMSE and relative MSE
             against a 4096-spp FP64-accumulated plain render, at equal device time and at equal sample count.
 
@@ -201,6 +202,55 @@ def reduce_replicas(dist, ms, units, device):
     u = torch.tensor([float(units)], dtype=torch.float64, device=device)
     dist.all_reduce(u)
     return float(t.item()), int(u.item())
+
+
+def ray_query_leg(core, sc, n, cpu):
+    """The ray-query microbenchmark on the large scene's BVH: n incoherent rays (origins uniform in the scene box,
+    directions uniform on the sphere) and n secondary-like rays (origins on area-weighted surface points,
+    cosine-weighted directions), tmax ~ U[0.1, scene diagonal], closest hit and any hit. Rays and results stay in
+    device memory (lh2g_trace); CUDA events on the core's stream. The CPU oracle traces 2^20 of the same rays."""
+    import numpy as np
+    import torch
+    from lighthouse2_gb300 import scenes as S
+    from oracle import bind
+    peak, _ = peaks()
+    out = {"workload": f"spheres_2m BVH (2,048,034 triangles, 66 instances), {n} rays per kind, rays and hits resident on the device"}
+    o = None
+    if cpu:
+        o = bind.Oracle()
+        o.set_scene(sc)
+    stream = torch.cuda.ExternalStream(core.stream_ptr())
+    for kind, seed in (("incoherent", 21), ("secondary", 22)):
+        rays = S.random_rays(sc, n, seed=seed, kind=kind)
+        d_rays = torch.from_numpy(rays.view(np.uint8).reshape(-1)).cuda()
+        for mode, name, bytes_per_ray in ((0, "closest", 48), (1, "any", 36)):
+            d_out = torch.empty(n * (16 if mode == 0 else 4), dtype=torch.uint8, device="cuda")
+            for _ in range(2):
+                core.trace(d_rays.data_ptr(), d_out.data_ptr(), n, mode, core.stream_ptr())
+            core.stream_ptr()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            reps = 5
+            with torch.cuda.stream(stream):
+                e0.record()
+            for _ in range(reps):
+                core.trace(d_rays.data_ptr(), d_out.data_ptr(), n, mode, core.stream_ptr())
+            with torch.cuda.stream(stream):
+                e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            res = d_out.cpu().numpy()
+            hits = float((res.view(S.HIT_DTYPE)["prim"] >= 0).mean()) if mode == 0 else float((res.view(np.uint32) != 0).mean())
+            gbps = n * bytes_per_ray / (ms / 1e3) / 1e9
+            row = {"Mrays_per_s": n / (ms / 1e3) / 1e6, "ms": ms, "hit_fraction": hits, "algorithmic_GBps": gbps, "frac_of_hbm": gbps / peak}
+            if o is not None:
+                m = 1 << 20
+                t = time.time()
+                o.trace(rays[:m], mode=mode, nthreads=os.cpu_count() or 1)
+                row["cpu_Mrays_per_s"] = m / (time.time() - t) / 1e6
+                row["cpu_cores"] = os.cpu_count() or 1
+            out[f"{kind}_{name}"] = row
+        del d_rays
+    return out
 
 
 def decode_launches(lt_all, frames, counts, waves, W, H):
@@ -565,6 +615,7 @@ def run_gb300(args):
     last = core.read_framebuffer()
     assert np.array_equal(hosts[(args.steps - 1) % 2].numpy(), last), "the last copied frame differs from the device frame"
     e2e_value = e2e_rays * world / t_e2e / 1e6
+    rq = ray_query_leg(core, sc, args.rays, world == 1 and not args.no_cpu_baseline) if (not args.no_rays and rank == 0) else None
     svgf = svgf_leg(core, W, H, max(args.steps, 8), args.warmup) if not args.no_svgf else None
     serving = serving_leg(args) if (not args.no_serving and rank == 0) else None
     nrc = None
@@ -625,6 +676,8 @@ def run_gb300(args):
             "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": VIEW_BYTES + PARAMS_BYTES, "d2h_bytes_per_step": W * H * 16},
             "gpu_launches": launches * world,
             "clocks": clk}
+    if rq is not None:
+        line["ray_queries"] = rq
     if svgf is not None:
         line["svgf"] = svgf
     if serving is not None:
@@ -651,6 +704,8 @@ def main():
     ap.add_argument("--no-svgf", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-nrc", action="store_true")
+    ap.add_argument("--no-rays", action="store_true")
+    ap.add_argument("--rays", type=int, default=1 << 24, help="rays per kind of the ray-query leg")
     ap.add_argument("--nrc-lr", type=float, default=1e-3)
     ap.add_argument("--nrc-scenes", default="spheres_2m,cornell", help="comma list of spheres_2m, cornell")
     ap.add_argument("--nrc-ref-spp", type=int, default=4096)
