@@ -84,13 +84,19 @@ bool load_scene(const char* path, Scene& s) {
     char magic[8];
     r.read(magic, 8);
     if (memcmp(magic, "LH2GSCN1", 8) != 0) { fclose(r.f); return false; }
-    uint c[10];
+    uint c[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     r.read(c, 10);
+    /* a truncated or foreign file must fail here, not allocate from garbage counts */
+    const uint limit = 1u << 28;
+    bool sane = r.ok && c[8] < (1u << 16) && c[9] < (1u << 16);
+    for (int k = 0; k < 8; k++) sane = sane && c[k] < limit;
+    if (!sane) { fclose(r.f); return false; }
     s.meshes.resize(c[0]), s.instances.resize(c[1]), s.materials.resize(c[2]), s.textures.resize(c[3]);
     s.triLights.resize(c[4]), s.pointLights.resize(c[5]), s.spotLights.resize(c[6]), s.dirLights.resize(c[7]);
     s.skyW = c[8], s.skyH = c[9];
     for (Mesh& m : s.meshes) {
         const uint n = r.get<uint>();
+        if (!r.ok || n >= limit) { fclose(r.f); return false; }
         m.verts.resize(3 * (size_t)n), m.tris.resize(n);
         r.read(m.verts.data(), m.verts.size());
         r.read(m.tris.data(), n);
@@ -102,7 +108,9 @@ bool load_scene(const char* path, Scene& s) {
     r.read(s.materials.data(), s.materials.size());
     for (Texture& t : s.textures) {
         t.width = r.get<uint>(), t.height = r.get<uint>();
-        t.texels.resize(r.get<uint>());
+        const uint n = r.get<uint>();
+        if (!r.ok || n >= limit) { fclose(r.f); return false; }
+        t.texels.resize(n);
         r.read(t.texels.data(), t.texels.size());
     }
     r.read(s.triLights.data(), s.triLights.size());
@@ -122,7 +130,9 @@ bool load_frames(const char* path, std::vector<Frame>& frames) {
     char magic[8];
     r.read(magic, 8);
     if (memcmp(magic, "LH2GFRM1", 8) != 0) { fclose(r.f); return false; }
-    frames.resize(r.get<uint>());
+    const uint n = r.get<uint>();
+    if (!r.ok || n >= (1u << 20)) { fclose(r.f); return false; }
+    frames.resize(n);
     for (Frame& f : frames) {
         r.read(&f.view, 1);
         f.converge = r.get<int>();
