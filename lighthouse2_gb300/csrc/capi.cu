@@ -41,6 +41,7 @@ struct MeshDev {
     float4* verts = nullptr;   /* 3 per triangle */
     float4* tris = nullptr;    /* CoreTri4, 13 float4 per triangle */
     uint32_t n = 0;
+    uint32_t maxMaterial = 0;  /* largest material index of its triangles (checked against the materials at render) */
     float bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0};
 };
 
@@ -271,6 +272,15 @@ int join_frames(lh2g_context* ctx) {
         }
     return LH2G_OK;
 }
+/* every instanced triangle's material index must name a material: shading reads the material array with it */
+bool materials_cover_meshes(const lh2g_context* ctx) {
+    for (const InstHost& in : ctx->inst)
+        if (in.mesh >= 0 && in.mesh < (int)ctx->meshes.size() && ctx->meshes[in.mesh].n &&
+            ctx->meshes[in.mesh].maxMaterial >= ctx->hostMats.size())
+            return false;
+    return true;
+}
+
 #define JOIN()                                  \
     do {                                        \
         const int _j = join_frames(ctx);        \
@@ -477,6 +487,8 @@ int lh2g_set_geometry(lh2g_context* ctx, int meshIdx, const float* v4, int verte
     CK(dalloc(m.tris, (size_t)13 * triangleCount));
     CK(cudaMemcpyAsync(m.verts, v4, sizeof(float4) * 3 * (size_t)triangleCount, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemcpyAsync(m.tris, tris, sizeof(lh2g_core_tri) * (size_t)triangleCount, cudaMemcpyHostToDevice, ctx->st));
+    m.maxMaterial = 0;
+    for (int i = 0; i < triangleCount; i++) m.maxMaterial = std::max(m.maxMaterial, tris[i].material);
     for (int k = 0; k < 3; k++) m.bmin[k] = 1e30f, m.bmax[k] = -1e30f;
     for (size_t i = 0; i < (size_t)vertexCount; i++)
         for (int k = 0; k < 3; k++) m.bmin[k] = std::min(m.bmin[k], v4[4 * i + k]), m.bmax[k] = std::max(m.bmax[k], v4[4 * i + k]);
@@ -824,6 +836,7 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
     if (p->width != ctx->W || p->height != ctx->H || p->spp != ctx->spp || p->maxDepth < 1 || p->maxDepth > 64)
         return fail(ctx, LH2G_ERR_INVALID, "render: parameters do not match the target");
     if (!ctx->mats) return fail(ctx, LH2G_ERR_STATE, "render: no materials");
+    if (!materials_cover_meshes(ctx)) return fail(ctx, LH2G_ERR_INVALID, "render: a triangle's material index exceeds the material count");
     cudaSetDevice(ctx->device);
     const bool filt = (p->flags & LH2G_RP_FILTER) != 0, nrcFrame = (p->flags & LH2G_RP_NRC) != 0;
     if (filt && nrcFrame) return fail(ctx, LH2G_ERR_INVALID, "render: filter and radiance-cache frames do not combine");
@@ -1309,6 +1322,7 @@ int context_scene(lh2g_context* ctx, SceneGPU* scene, int* device, int* blocks4,
     if (!ctx || !scene || !device || !blocks4 || !tailDepth) return LH2G_ERR_INVALID;
     if (!ctx->finalized) return fail(ctx, LH2G_ERR_STATE, "render: scene not finalized (call lh2g_finalize_instances)");
     if (!ctx->mats) return fail(ctx, LH2G_ERR_STATE, "render: no materials");
+    if (!materials_cover_meshes(ctx)) return fail(ctx, LH2G_ERR_INVALID, "render: a triangle's material index exceeds the material count");
     *scene = scene_of(ctx);
     *device = ctx->device;
     blocks4[0] = ctx->blocksExtend, blocks4[1] = ctx->blocksConnect, blocks4[2] = ctx->blocksShade, blocks4[3] = ctx->blocksTail;

@@ -160,3 +160,25 @@ def test_pipelined_frames_match_one_at_a_time(core_lib):
     for lanes in (2, 4):
         for a, b in zip(results[0], results[lanes]):
             assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_material_index_out_of_range_is_refused(core_lib):
+    """A triangle naming a material that was never set is refused at render time (the shading kernel would read
+    past the material array); the context stays usable once the materials cover the index."""
+    from lighthouse2_gb300.core import CoreError
+    sc = S.cornell_sphere(subdiv=2)
+    core = RenderCore()
+    core.set_scene(sc)
+    n = len(sc.materials)
+    core.SetMaterials(sc.materials[:1])
+    W, H = 32, 24
+    core.SetTarget(W, H, 1)
+    view = S.cornell_view(W, H)
+    p = make_params(W, H, 1, max_depth=3, camera_r0=camera_r0(0), flags=RP_NEE | RP_DEPTH_W)
+    with pytest.raises(CoreError):
+        core.render_ex(view, p)
+    core.SetMaterials(sc.materials)
+    assert n > 1
+    core.render_ex(view, p)
+    assert core.read_accumulator()[:, :3].sum() > 0
+    core.close()
