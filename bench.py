@@ -549,6 +549,7 @@ def run_gb300(args):
     core.SetTarget(W, H, 1)
     core.Setting("waveTail", args.wave_tail)
     core.Setting("pipelineFrames", args.lanes)
+    core.Setting("sortConnections", args.sort_connections)
     waves = min(MAX_DEPTH, args.wave_tail - 1) if args.wave_tail > 0 else MAX_DEPTH
     stream = torch.cuda.ExternalStream(core.stream_ptr())
     frames = [frame_params(k, W, H) for k in range(8)]
@@ -712,6 +713,7 @@ def main():
     ap.add_argument("--nrc-warmup", type=int, default=200)
     ap.add_argument("--serving-jobs", type=int, default=120)
     ap.add_argument("--lanes", type=int, default=LANES, help="frames in flight (0 or 1: one at a time)")
+    ap.add_argument("--sort-connections", type=int, default=0, help="group connections by light before the any-hit queries")
     ap.add_argument("--wave-tail", type=int, default=WAVE_TAIL, help="first path length of the persistent tail kernel (0: off)")
     args = ap.parse_args()
     if args.warmup < 3:

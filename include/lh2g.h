@@ -72,7 +72,8 @@ LH2G_API int lh2g_set_sky(lh2g_context* ctx, const float* rgb, int width, int he
  * Scheduling settings of this core (results do not change): "waveTail" (default 5; path lengths from this one on
  * run to their end in one persistent kernel; 0: one launch per stage and wave throughout) and "pipelineFrames"
  * (frames in flight, 0..4, default 4; 0 and 1 render one frame at a time; see lh2g_get_stream) and "waveOccupancy"
- * (fraction of the GPU the persistent wave kernels of one frame launch, (0, 1], default 1). */
+ * (fraction of the GPU the persistent wave kernels of one frame launch, (0, 1], default 1) and "sortConnections"
+ * (1: group each wave's light connections by the light they sample before the any-hit queries; default 0). */
 LH2G_API int lh2g_setting(lh2g_context* ctx, const char* name, float value);
 /* SetTarget (core_api_base.h:93), headless: the output is a device float4 buffer of width*height pixels. */
 LH2G_API int lh2g_set_target(lh2g_context* ctx, int width, int height, int spp);

@@ -238,6 +238,7 @@ struct lh2g_context {
     static constexpr int MAX_LANES = 4;
     Lane lanes[MAX_LANES];
     int pipelineFrames = 4;            /* lanes in use; 0 or 1: one frame at a time */
+    int sortConnections = 0;           /* group each wave's connections by light before the any-hit queries */
     int nextLane = 0;
     int lastSlot = -1;                 /* lane of the last frame, -1: the context stream */
     cudaEvent_t forkEv = nullptr, finEv = nullptr;
@@ -310,6 +311,7 @@ void free_lane_buffers(lh2g_context* ctx) {
         if (!ctx->lanes[l].ready) continue;
         for (int k = 0; k < 2; k++) dfree(B.O[k]), dfree(B.D[k]), dfree(B.T[k]);
         dfree(B.hits), dfree(B.shO), dfree(B.shD), dfree(B.shE), dfree(B.pathAcc), dfree(B.counters);
+        dfree(B.sortO), dfree(B.sortD), dfree(B.sortE), dfree(B.connBins);
         ctx->lanes[l].ready = false;
     }
 }
@@ -319,6 +321,7 @@ void free_target(lh2g_context* ctx) {
     WaveBuffers& B = ctx->B;
     for (int k = 0; k < 2; k++) dfree(B.O[k]), dfree(B.D[k]), dfree(B.T[k]);
     dfree(B.hits), dfree(B.shO), dfree(B.shD), dfree(B.shE), dfree(B.pathAcc), dfree(B.accum), dfree(B.frame), dfree(B.counters);
+    dfree(B.sortO), dfree(B.sortD), dfree(B.sortE), dfree(B.connBins);
     free_filter(ctx);
     for (NrcBuffers& n : ctx->nrcBuf) {
         dfree(n.rec), dfree(n.queries), dfree(n.qPath), dfree(n.pred), dfree(n.trainQ), dfree(n.trainT), dfree(n.counts);
@@ -706,6 +709,7 @@ int lh2g_setting(lh2g_context* ctx, const char* name, float value) {
     else if (!strcmp(name, "clampIndirect")) ctx->clampIndirect = value;
     else if (!strcmp(name, "filter")) ctx->filterEnabled = value == 0 ? 0 : 1;
     else if (!strcmp(name, "TAA")) ctx->taaEnabled = value == 0 ? 0 : 1;
+    else if (!strcmp(name, "sortConnections")) ctx->sortConnections = value == 0 ? 0 : 1;
     else if (!strcmp(name, "waveOccupancy")) {
         /* fraction of a full GPU the persistent wave kernels of one frame take (frames in flight share the rest) */
         if (!(value > 0.0f && value <= 1.0f)) return fail(ctx, LH2G_ERR_INVALID, "setting waveOccupancy: (0, 1]");
@@ -747,6 +751,11 @@ int lh2g_set_target(lh2g_context* ctx, int w, int h, int spp) {
         if (!e) e = dalloc(B.accum, (size_t)w * h);
         if (!e) e = dalloc(B.frame, (size_t)w * h);
         if (!e) e = dalloc(B.counters, 1);
+        if (!e) e = dalloc(B.sortO, P);
+        if (!e) e = dalloc(B.sortD, P);
+        if (!e) e = dalloc(B.sortE, P);
+        if (!e) e = dalloc(B.connBins, 128);
+        if (!e) e = cudaMemset(B.connBins, 0, 128 * sizeof(uint32_t));
         if (e) { free_target(ctx); return cuda_check(ctx, e, "set_target allocation"); }
         ctx->cap = P, ctx->pathAccCap = P;
         CK(cudaMemsetAsync(B.accum, 0, sizeof(float4) * (size_t)w * h, ctx->st));
@@ -822,6 +831,11 @@ int ensure_lane(lh2g_context* ctx, int l) {
         if (!e) e = dalloc(B.shE, P);
         if (!e) e = dalloc(B.pathAcc, P);
         if (!e) e = dalloc(B.counters, 1);
+        if (!e) e = dalloc(B.sortO, P);
+        if (!e) e = dalloc(B.sortD, P);
+        if (!e) e = dalloc(B.sortE, P);
+        if (!e) e = dalloc(B.connBins, 128);
+        if (!e) e = cudaMemset(B.connBins, 0, 128 * sizeof(uint32_t));
         if (e) { free_lane_buffers(ctx); return cuda_check(ctx, e, "frame lane buffers"); }
         L.ready = true;
     }
@@ -868,6 +882,7 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
         if (slot > 0) {
             for (int k = 0; k < 2; k++) B.O[k] = L.B.O[k], B.D[k] = L.B.D[k], B.T[k] = L.B.T[k];
             B.hits = L.B.hits, B.shO = L.B.shO, B.shD = L.B.shD, B.shE = L.B.shE, B.pathAcc = L.B.pathAcc, B.counters = L.B.counters;
+            B.sortO = L.B.sortO, B.sortD = L.B.sortD, B.sortE = L.B.sortE, B.connBins = L.B.connBins;
         }
         CK(cudaEventRecord(ctx->forkEv, ctx->st));
         CK(cudaStreamWaitEvent(st, ctx->forkEv, 0));
@@ -912,7 +927,13 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
     for (int d = 1; d <= waves; d++) {
         mark(), launch_extend(S, F, B, d, ctx->blocksExtend, st), mark();
         mark(), launch_shade(S, F, B, d, ctx->blocksShade, st), mark();
-        mark(), launch_connect(S, F, B, d, ctx->blocksConnect, st), mark();
+        if (ctx->sortConnections) {   /* one timed slot: the regrouping and the any-hit queries */
+            WaveBuffers Bs = B;
+            Bs.shO = B.sortO, Bs.shD = B.sortD, Bs.shE = B.sortE;
+            mark(), launch_sort_connections(B, d, st), launch_connect(S, F, Bs, d, ctx->blocksConnect, st), mark();
+        } else {
+            mark(), launch_connect(S, F, B, d, ctx->blocksConnect, st), mark();
+        }
     }
     if (tail) mark(), launch_tail(S, F, B, waves + 1, ctx->blocksTail, st), mark();
     if (hook && hook->before) {

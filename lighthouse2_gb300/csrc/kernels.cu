@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(WAVE_BLOCK) k_tail(const SceneGPU S, const Fra
                     while (sh.step<true>(S, status, occluded)) {}
                 an += sh.nodes, at += sh.tris;
                 if (!occluded) {
-                    float4* accP = B.pathAcc + (__float_as_uint(out.sE.w) ? F.P : 0) + __float_as_uint(out.sO.w);
+                    float4* accP = B.pathAcc + ((__float_as_uint(out.sE.w) & 1u) ? F.P : 0) + __float_as_uint(out.sO.w);
                     float4 acc = *accP;
                     acc.x += out.sE.x, acc.y += out.sE.y, acc.z += out.sE.z;
                     *accP = acc;
@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(128) k_connect(const SceneGPU S, const FrameGP
     auto add = [&](uint32_t i) {
         const float4 e = B.shE[i];
         const uint32_t pathIdx = __float_as_uint(B.shO[i].w);
-        float4* accP = B.pathAcc + (__float_as_uint(e.w) ? F.P : 0) + pathIdx;   /* e.w: indirect half */
+        float4* accP = B.pathAcc + ((__float_as_uint(e.w) & 1u) ? F.P : 0) + pathIdx;   /* e.w bit 0: indirect half */
         float4 acc = *accP;
         acc.x += e.x, acc.y += e.y, acc.z += e.z;
         *accP = acc;
@@ -201,6 +201,58 @@ __global__ void __launch_bounds__(128) k_connect(const SceneGPU S, const FrameGP
         [&](uint32_t i, const CoopRay&, bool occluded) { if (!occluded && (threadIdx.x & (COOP - 1)) == 0) add(i); },
         C->travStats + 2);
     if (status) atomicOr(&C->status, status);
+}
+
+/* --------------------------------------------------------------------------------------------------
+ * Connections grouped by light: a counting sort over the light index the shading stage keeps in E.w bits 1..6.
+ * Shadow rays towards one light from neighbouring points visit much of the same tree, so a warp of them
+ * diverges less. The order within a light follows the original order (warp by warp). */
+__global__ void k_conn_count(const WaveBuffers B, const int depth) {
+    __shared__ uint32_t h[64];
+    if (threadIdx.x < 64) h[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t n = B.counters->shadow[depth - 1];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        atomicAdd(&h[(__float_as_uint(B.shE[i].w) >> 1) & 63u], 1u);
+    __syncthreads();
+    if (threadIdx.x < 64 && h[threadIdx.x]) atomicAdd(&B.connBins[threadIdx.x], h[threadIdx.x]);
+}
+/* one block of 64 threads: running offsets of the bins, counts cleared for the next wave */
+__global__ void k_conn_scan(const WaveBuffers B) {
+    __shared__ uint32_t v[64];
+    const uint32_t t = threadIdx.x;
+    v[t] = B.connBins[t];
+    __syncthreads();
+    if (t == 0) {
+        uint32_t run = 0;
+        for (int k = 0; k < 64; k++) {
+            const uint32_t c = v[k];
+            v[k] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    B.connBins[64 + t] = v[t];
+    B.connBins[t] = 0;
+}
+__global__ void k_conn_scatter(const WaveBuffers B, const int depth) {
+    const uint32_t n = B.counters->shadow[depth - 1];
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t w0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); w0 < n; w0 += gridDim.x * blockDim.x) {
+        const uint32_t i = w0 + lane;
+        const bool valid = i < n;
+        const float4 e = valid ? B.shE[i] : make_float4(0, 0, 0, 0);
+        const uint32_t bin = valid ? (__float_as_uint(e.w) >> 1) & 63u : 64u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, bin);
+        const uint32_t leader = (uint32_t)__ffs(peers) - 1u;
+        uint32_t base = 0;
+        if (valid && lane == leader) base = atomicAdd(&B.connBins[64 + bin], (uint32_t)__popc(peers));
+        base = __shfl_sync(0xffffffffu, base, (int)leader);
+        if (valid) {
+            const uint32_t pos = base + (uint32_t)__popc(peers & lanemask_lt());
+            B.sortO[pos] = B.shO[i], B.sortD[pos] = B.shD[i], B.sortE[pos] = e;
+        }
+    }
 }
 
 /* -------------------------------------------------------------------------------------------------- */
@@ -374,6 +426,11 @@ void launch_nrc_collect(const FrameGPU& F, const WaveBuffers& B, float4* queries
 }
 void launch_nrc_apply(const FrameGPU& F, const WaveBuffers& B, const float4* pred, const uint32_t* qPath, const uint32_t* counts, cudaStream_t st) {
     k_nrc_apply<<<sm_count() * 8, 256, 0, st>>>(F, B, pred, qPath, counts);
+}
+void launch_sort_connections(const WaveBuffers& B, int depth, cudaStream_t st) {
+    k_conn_count<<<sm_count() * 4, 256, 0, st>>>(B, depth);
+    k_conn_scan<<<1, 64, 0, st>>>(B);
+    k_conn_scatter<<<sm_count() * 8, 256, 0, st>>>(B, depth);
 }
 void launch_finalize(const FrameGPU& F, const WaveBuffers& B, float scale, int overwrite, cudaStream_t st) {
     const int64_t WH = (int64_t)F.W * F.H;

@@ -24,6 +24,10 @@ struct WaveBuffers {
     float4* deltaDepth;
     lh2g_hit* capHits;     /* optional per-(depth, path) capture */
     uint32_t* capSeeds;
+    float4* sortO;         /* connections grouped by light (setting "sortConnections"): a second O, D, E set */
+    float4* sortD;
+    float4* sortE;
+    uint32_t* connBins;    /* 64 per-light counts, then their running offsets */
 };
 
 void launch_generate(const FrameGPU& F, const WaveBuffers& B, cudaStream_t st);
@@ -32,6 +36,8 @@ void launch_shade(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, in
 void launch_connect(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int persistentBlocks, cudaStream_t st);
 /* path lengths startDepth..maxDepth of the frame's remaining paths, one persistent launch */
 void launch_tail(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int startDepth, int persistentBlocks, cudaStream_t st);
+/* the connections of wave `depth` regrouped by light into sortO/D/E (counting sort over 64 bins) */
+void launch_sort_connections(const WaveBuffers& B, int depth, cudaStream_t st);
 /* per-pixel sums of the frame's paths into the accumulator (from zero when overwrite != 0), then the frame */
 void launch_finalize(const FrameGPU& F, const WaveBuffers& B, float scale, int overwrite, cudaStream_t st);
 /* radiance-cache frames: gather queries / training samples (counts[0], counts[1]), then add the predictions */

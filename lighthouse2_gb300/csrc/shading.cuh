@@ -290,7 +290,7 @@ LH2G_DEV float Potential(const SceneGPU& S, int i, const float3& I, const float3
 /* pot: this thread's slice of a potential array (entry i at pot[i * stride]), as the reference's local
  * potential[MAXISLIGHTS] array (lights_shared.h:232); it lives in shared memory. */
 LH2G_DEV float3 RandomPointOnLight(const SceneGPU& S, float r0, float r1, const float3& I, const float3& N, float& pickProb, float& lightPdf, float3& lightColor,
-                                   float* pot, const int stride) {
+                                   float* pot, const int stride, int& picked) {
     const int lights = S.nTri + S.nPoint + S.nSpot + S.nDir;
     const float lightCount = (float)lights;
     const float3 bary = RandomBarycentrics(r0);
@@ -309,6 +309,7 @@ LH2G_DEV float3 RandomPointOnLight(const SceneGPU& S, float r0, float r1, const 
     }
     pickProb = pot[lightIdx * stride] / sum;
     lightIdx = max(0, min(lightIdx, f2i(lightCount) - 1));
+    picked = lightIdx;
     if (lightIdx < S.nTri) {
         const float4* l = S.triLights + (size_t)lightIdx * 6;
         const float4 n4 = __ldg(l + 1), r4 = __ldg(l + 2), v0 = __ldg(l + 3), v1 = __ldg(l + 4), v2 = __ldg(l + 5);

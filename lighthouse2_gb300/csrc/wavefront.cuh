@@ -168,7 +168,8 @@ __device__ __forceinline__ void shade_core(const SceneGPU& S, const FrameGPU& F,
         const float q0 = RandomFloat(seed), q1 = RandomFloat(seed);
         float pickProb = 0, lightPdf = 0;
         float3 lightColor = mk3(0);
-        float3 L = RandomPointOnLight(S, q0, q1, I, fN * faceDir, pickProb, lightPdf, lightColor, pot, WAVE_BLOCK) - I;
+        int picked = 0;
+        float3 L = RandomPointOnLight(S, q0, q1, I, fN * faceDir, pickProb, lightPdf, lightColor, pot, WAVE_BLOCK, picked) - I;
         const float dist = length(L);
         L = L * (1.0f / dist);
         const float NdotL = dot(L, fN * faceDir);
@@ -180,7 +181,8 @@ __device__ __forceinline__ void shade_core(const SceneGPU& S, const FrameGPU& F,
             out.shadow = true;
             out.sO = make_float4(SO.x, SO.y, SO.z, __uint_as_float(pathIdx));
             out.sD = make_float4(L.x, L.y, L.z, dist - 2 * F.eps);
-            out.sE = make_float4(contribution.x, contribution.y, contribution.z, __uint_as_float(half));
+            /* w: bit 0 the radiance half (filter frames), bits 1..6 the light (connections may be grouped by it) */
+            out.sE = make_float4(contribution.x, contribution.y, contribution.z, __uint_as_float(half | ((uint32_t)picked << 1)));
         }
     }
     if (depth == F.maxDepth && firstHitToBeStored) {

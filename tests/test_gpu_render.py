@@ -182,3 +182,30 @@ def test_material_index_out_of_range_is_refused(core_lib):
     core.render_ex(view, p)
     assert core.read_accumulator()[:, :3].sum() > 0
     core.close()
+
+
+@pytest.mark.parametrize("tail", [0, 5])
+def test_connections_grouped_by_light_change_nothing(core_lib, tail):
+    """Grouping each wave's connections by light before the any-hit queries (setting "sortConnections") reorders
+    work only: accumulator and queue counts equal those of the ungrouped frame, bit for bit, also in filter frames."""
+    sc = S.spheres_2m(seed=5, n_spheres=6, slices=40, stacks=26, tex_size=64)
+    W, H = 160, 96
+    view = S.spheres_view(W, H, frame=1)
+    p = make_params(W, H, 2, max_depth=6, rr_start=3, camera_r0=camera_r0(0), flags=RP_NEE | RP_DEPTH_W)
+    out = []
+    for on in (0, 1):
+        core = RenderCore()     # a core per setting: the filter's temporal history must start empty in both
+        core.set_scene(sc)
+        core.SetTarget(W, H, 2)
+        core.Setting("waveTail", tail)
+        core.Setting("sortConnections", on)
+        c = core.render_ex(view, p, counters=True)["counters"].copy()
+        acc = core.read_accumulator().copy()
+        core.Setting("filter", 1)
+        core.Render(view, converge=1)
+        core.Render(S.spheres_view(W, H, frame=2), converge=1)
+        out.append((c, acc, core.read_framebuffer().copy()))
+        core.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1].view(np.uint32), out[1][1].view(np.uint32))
+    assert np.array_equal(out[0][2].view(np.uint32), out[1][2].view(np.uint32))
