@@ -49,6 +49,7 @@ namespace lh2g {
 #define LH2G_REFILL_MIN 1
 #endif
 constexpr float BOX_MARGIN = 1.52587890625e-05f;
+constexpr float SLAB_MARGIN = 1.71661376953125e-05f;   /* 2^-16 + 2^-19 */
 constexpr uint32_t ENTRY_MARKER = 0xffffffffu;
 constexpr uint32_t MAX_STEPS = 1u << 20;   /* far beyond any traversal of a well-formed tree */
 
@@ -166,8 +167,15 @@ struct Traversal {
                     az = __uint_as_float(((n0.w >> 16) & 255u) << 23) * invD.z;
         const float bx = (__uint_as_float(n0.x) - O.x) * invD.x, by = (__uint_as_float(n0.y) - O.y) * invD.y,
                     bz = (__uint_as_float(n0.z) - O.z) * invD.z;
-        /* absolute rounding bound of the three distances (a few ulp of the operands, taken with margin 2^-20) */
-        const float err = (fmaxf(fmaxf(fabsf(bx), fabsf(by)), fabsf(bz)) + 255.0f * fmaxf(fmaxf(fabsf(ax), fabsf(ay)), fabsf(az))) * 9.5367431640625e-07f;
+        /* Widening folded into b, per axis: M = |b| + 255 |a| bounds |t| of every plane of the axis, the rounding of
+         * its distances is below 2^-20 M (a few ulp of the operands) and the margin wanted is 2^-16 |t|; m = (2^-16 +
+         * 2^-19) M covers both and the two roundings the folded form adds (b - m and the FMA, each below 2^-24 (M + m)).
+         * t - 2^-16 |t| is increasing in t, so the margin taken per axis before the max (min) is the margin of the
+         * entry (exit) distance. A bound per axis, not the largest of the three, keeps rays almost parallel to a
+         * plane (one huge |b|) from widening their other two slabs. */
+        const float mx = fmaf(255.0f, fabsf(ax), fabsf(bx)) * SLAB_MARGIN, my = fmaf(255.0f, fabsf(ay), fabsf(by)) * SLAB_MARGIN,
+                    mz = fmaf(255.0f, fabsf(az), fabsf(bz)) * SLAB_MARGIN;
+        const float bxl = bx - mx, bxh = bx + mx, byl = by - my, byh = by + my, bzl = bz - mz, bzh = bz + mz;
         /* near / far plane words per axis, swapped for negative directions */
         const bool nx = invD.x < 0.0f, ny = invD.y < 0.0f, nz = invD.z < 0.0f;
         const uint32_t nlx0 = nx ? n3.z : n2.x, nlx1 = nx ? n3.w : n2.y, nhx0 = nx ? n2.x : n3.z, nhx1 = nx ? n2.y : n3.w;
@@ -180,18 +188,14 @@ struct Traversal {
         for (int i = 0; i < 8; i++) {
             const uint32_t sel = 0x4440u | (uint32_t)(i & 3);
             const uint32_t meta = __byte_perm(i < 4 ? metaLo : metaHi, 0u, sel);
-            const float txn = fmaf(plane_byte(i < 4 ? nlx0 : nlx1, i), ax, bx);
-            const float txf = fmaf(plane_byte(i < 4 ? nhx0 : nhx1, i), ax, bx);
-            const float tyn = fmaf(plane_byte(i < 4 ? nly0 : nly1, i), ay, by);
-            const float tyf = fmaf(plane_byte(i < 4 ? nhy0 : nhy1, i), ay, by);
-            const float tzn = fmaf(plane_byte(i < 4 ? nlz0 : nlz1, i), az, bz);
-            const float tzf = fmaf(plane_byte(i < 4 ? nhz0 : nhz1, i), az, bz);
-            float tn = fmax3f(txn, tyn, tzn);
-            float tf = fmin3f(txf, tyf, tzf);
-            tn = fmaf(-fabsf(tn), BOX_MARGIN, tn) - err;
-            tf = fmaf(fabsf(tf), BOX_MARGIN, tf) + err;
-            tn = fmaxf(tn, tmin);
-            tf = fminf(tf, limit);
+            const float txn = fmaf(plane_byte(i < 4 ? nlx0 : nlx1, i), ax, bxl);
+            const float txf = fmaf(plane_byte(i < 4 ? nhx0 : nhx1, i), ax, bxh);
+            const float tyn = fmaf(plane_byte(i < 4 ? nly0 : nly1, i), ay, byl);
+            const float tyf = fmaf(plane_byte(i < 4 ? nhy0 : nhy1, i), ay, byh);
+            const float tzn = fmaf(plane_byte(i < 4 ? nlz0 : nlz1, i), az, bzl);
+            const float tzf = fmaf(plane_byte(i < 4 ? nhz0 : nhz1, i), az, bzh);
+            const float tn = fmaxf(fmax3f(txn, tyn, tzn), tmin);
+            const float tf = fminf(fmin3f(txf, tyf, tzf), limit);
             const bool hit = meta != 0u && tn <= tf;
             /* key: distance with the low 3 bits replaced by the slot (rounded down: culling stays conservative) */
             key[i] = hit ? ((__float_as_uint(fmaxf(tn, 0.0f)) & ~7u) | (uint32_t)i) : 0xffffffffu;
