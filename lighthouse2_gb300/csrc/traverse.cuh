@@ -86,6 +86,8 @@ LH2G_DEV uint32_t byte_of(uint32_t w0, uint32_t w1, int i) { return ((i < 4 ? w0
 /* byte i & 3 of w as a float, exactly: one byte permute builds the bits of 2^23 + byte (0x4B0000bb), one FADD
  * removes 2^23 (an integer-to-float conversion would run on the quarter-rate conversion pipe, 48 times per node) */
 LH2G_DEV float plane_byte(uint32_t w, int i) { return __uint_as_float(__byte_perm(w, 0x4Bu, 0x4550u | (uint32_t)(i & 3))) - 8388608.0f; }
+/* 1 + (byte i & 3 of w) * 2^-15, exactly: one byte permute builds the bits 0x3F80bb00 */
+LH2G_DEV float plane_unit(uint32_t w, int i) { return __uint_as_float(__byte_perm(w, 0x3F80u, 0x5406u | ((uint32_t)(i & 3) << 4))); }
 
 /* Compare-exchange for the sorting network. */
 LH2G_DEV void cx(uint32_t& a, uint32_t& b) { const uint32_t lo = min(a, b), hi = max(a, b); a = lo, b = hi; }
@@ -167,15 +169,20 @@ struct Traversal {
                     az = __uint_as_float(((n0.w >> 16) & 255u) << 23) * invD.z;
         const float bx = (__uint_as_float(n0.x) - O.x) * invD.x, by = (__uint_as_float(n0.y) - O.y) * invD.y,
                     bz = (__uint_as_float(n0.z) - O.z) * invD.z;
-        /* Widening folded into b, per axis: M = |b| + 255 |a| bounds |t| of every plane of the axis, the rounding of
-         * its distances is below 2^-20 M (a few ulp of the operands) and the margin wanted is 2^-16 |t|; m = (2^-16 +
-         * 2^-19) M covers both and the two roundings the folded form adds (b - m and the FMA, each below 2^-24 (M + m)).
-         * t - 2^-16 |t| is increasing in t, so the margin taken per axis before the max (min) is the margin of the
-         * entry (exit) distance. A bound per axis, not the largest of the three, keeps rays almost parallel to a
-         * plane (one huge |b|) from widening their other two slabs. */
-        const float mx = fmaf(255.0f, fabsf(ax), fabsf(bx)) * SLAB_MARGIN, my = fmaf(255.0f, fabsf(ay), fabsf(by)) * SLAB_MARGIN,
-                    mz = fmaf(255.0f, fabsf(az), fabsf(bz)) * SLAB_MARGIN;
-        const float bxl = bx - mx, bxh = bx + mx, byl = by - my, byh = by + my, bzl = bz - mz, bzh = bz + mz;
+        /* A plane byte q enters as v = 1 + q 2^-15, so t = q a + b = v A + (b - A) with A = 2^15 a (exact): one FMA
+         * per plane. Widening folded into the offset, per axis: M = |b| + 255 |a| bounds |t| of every plane of the
+         * axis; the rounding of the distances is below 2^-21 M + 2^-8 |a| (a few ulp of the operands, the roundings
+         * of b - A - m (below 2^-23 (|b| + |A| + m)) and of the FMA); the margin wanted is 2^-16 |t|.
+         * m = (2^-16 + 2^-19) M + 2^-7 |a| covers all of it. t - 2^-16 |t| is increasing in t, so the margin taken per
+         * axis before the max (min) is the margin of the entry (exit) distance; a bound per axis, not the largest of
+         * the three, keeps rays almost parallel to a plane (one huge |b|) from widening their other two slabs. An
+         * overflowing A makes both distances of its axis NaN, which the min / max ignore: the box is kept. */
+        const float Ax = ax * 32768.0f, Ay = ay * 32768.0f, Az = az * 32768.0f;
+        const float mx = fmaf(fabsf(ax), 0.0078125f, fmaf(255.0f, fabsf(ax), fabsf(bx)) * SLAB_MARGIN),
+                    my = fmaf(fabsf(ay), 0.0078125f, fmaf(255.0f, fabsf(ay), fabsf(by)) * SLAB_MARGIN),
+                    mz = fmaf(fabsf(az), 0.0078125f, fmaf(255.0f, fabsf(az), fabsf(bz)) * SLAB_MARGIN);
+        const float cx0 = bx - Ax, cy0 = by - Ay, cz0 = bz - Az;
+        const float bxl = cx0 - mx, bxh = cx0 + mx, byl = cy0 - my, byh = cy0 + my, bzl = cz0 - mz, bzh = cz0 + mz;
         /* near / far plane words per axis, swapped for negative directions */
         const bool nx = invD.x < 0.0f, ny = invD.y < 0.0f, nz = invD.z < 0.0f;
         const uint32_t nlx0 = nx ? n3.z : n2.x, nlx1 = nx ? n3.w : n2.y, nhx0 = nx ? n2.x : n3.z, nhx1 = nx ? n2.y : n3.w;
@@ -188,12 +195,12 @@ struct Traversal {
         for (int i = 0; i < 8; i++) {
             const uint32_t sel = 0x4440u | (uint32_t)(i & 3);
             const uint32_t meta = __byte_perm(i < 4 ? metaLo : metaHi, 0u, sel);
-            const float txn = fmaf(plane_byte(i < 4 ? nlx0 : nlx1, i), ax, bxl);
-            const float txf = fmaf(plane_byte(i < 4 ? nhx0 : nhx1, i), ax, bxh);
-            const float tyn = fmaf(plane_byte(i < 4 ? nly0 : nly1, i), ay, byl);
-            const float tyf = fmaf(plane_byte(i < 4 ? nhy0 : nhy1, i), ay, byh);
-            const float tzn = fmaf(plane_byte(i < 4 ? nlz0 : nlz1, i), az, bzl);
-            const float tzf = fmaf(plane_byte(i < 4 ? nhz0 : nhz1, i), az, bzh);
+            const float txn = fmaf(plane_unit(i < 4 ? nlx0 : nlx1, i), Ax, bxl);
+            const float txf = fmaf(plane_unit(i < 4 ? nhx0 : nhx1, i), Ax, bxh);
+            const float tyn = fmaf(plane_unit(i < 4 ? nly0 : nly1, i), Ay, byl);
+            const float tyf = fmaf(plane_unit(i < 4 ? nhy0 : nhy1, i), Ay, byh);
+            const float tzn = fmaf(plane_unit(i < 4 ? nlz0 : nlz1, i), Az, bzl);
+            const float tzf = fmaf(plane_unit(i < 4 ? nhz0 : nhz1, i), Az, bzh);
             const float tn = fmaxf(fmax3f(txn, tyn, tzn), tmin);
             const float tf = fminf(fmin3f(txf, tyf, tzf), limit);
             const bool hit = meta != 0u && tn <= tf;
