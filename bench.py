@@ -255,8 +255,9 @@ def ray_query_leg(core, sc, n, cpu):
 
 def decode_launches(lt_all, frames, counts, waves, W, H):
     """Per stage kind: [summed launch ms, algorithmic bytes, launches] over `frames` frames whose per-launch device
-    times are lt_all (per frame: generate, (extend, shade, connect) x waves, tail if used, finalize) and whose
-    per-depth queue sizes are counts[frame % 8]."""
+    times are lt_all (per frame: generate, (extend, shade, connect) x waves, tail if used, finalize; a shade slot
+    spans the partition of the queue into hits and misses and the shading) and whose per-depth queue sizes are
+    counts[frame % 8]."""
     per_frame = 2 + 3 * waves + (1 if waves < MAX_DEPTH else 0)
     per_kind = {k: [0.0, 0, 0] for k in ("extend", "shade", "connect", "tail", "generate", "finalize")}
     for k in range(frames):
@@ -590,7 +591,7 @@ def run_gb300(args):
     assert len(lt_iso) == per_frame * 8, (len(lt_iso), per_frame)
     per_kind = decode_launches(lt_all, args.steps, counts, waves, W, H)
     per_kind_iso = decode_launches(lt_iso, 8, counts, waves, W, H)
-    launches = len(lt_all)
+    launches = len(lt_all) + args.steps * waves   # each shading slot launches k_partition and k_shade
     rays, trav, ext_rays, shadow_rays = 0, np.zeros(4, np.float64), 0, 0
     for k in range(args.steps):
         c = counts[k % 8]

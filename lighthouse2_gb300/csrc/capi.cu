@@ -311,7 +311,7 @@ void free_lane_buffers(lh2g_context* ctx) {
         if (!ctx->lanes[l].ready) continue;
         for (int k = 0; k < 2; k++) dfree(B.O[k]), dfree(B.D[k]), dfree(B.T[k]);
         dfree(B.hits), dfree(B.shO), dfree(B.shD), dfree(B.shE), dfree(B.pathAcc), dfree(B.counters);
-        dfree(B.sortO), dfree(B.sortD), dfree(B.sortE), dfree(B.connBins);
+        dfree(B.sortO), dfree(B.sortD), dfree(B.sortE), dfree(B.connBins), dfree(B.order);
         ctx->lanes[l].ready = false;
     }
 }
@@ -321,7 +321,7 @@ void free_target(lh2g_context* ctx) {
     WaveBuffers& B = ctx->B;
     for (int k = 0; k < 2; k++) dfree(B.O[k]), dfree(B.D[k]), dfree(B.T[k]);
     dfree(B.hits), dfree(B.shO), dfree(B.shD), dfree(B.shE), dfree(B.pathAcc), dfree(B.accum), dfree(B.frame), dfree(B.counters);
-    dfree(B.sortO), dfree(B.sortD), dfree(B.sortE), dfree(B.connBins);
+    dfree(B.sortO), dfree(B.sortD), dfree(B.sortE), dfree(B.connBins), dfree(B.order);
     free_filter(ctx);
     for (NrcBuffers& n : ctx->nrcBuf) {
         dfree(n.rec), dfree(n.queries), dfree(n.qPath), dfree(n.pred), dfree(n.trainQ), dfree(n.trainT), dfree(n.counts);
@@ -756,6 +756,7 @@ int lh2g_set_target(lh2g_context* ctx, int w, int h, int spp) {
         if (!e) e = dalloc(B.sortE, P);
         if (!e) e = dalloc(B.connBins, 128);
         if (!e) e = cudaMemset(B.connBins, 0, 128 * sizeof(uint32_t));
+        if (!e) e = dalloc(B.order, P);
         if (e) { free_target(ctx); return cuda_check(ctx, e, "set_target allocation"); }
         ctx->cap = P, ctx->pathAccCap = P;
         CK(cudaMemsetAsync(B.accum, 0, sizeof(float4) * (size_t)w * h, ctx->st));
@@ -836,6 +837,7 @@ int ensure_lane(lh2g_context* ctx, int l) {
         if (!e) e = dalloc(B.sortE, P);
         if (!e) e = dalloc(B.connBins, 128);
         if (!e) e = cudaMemset(B.connBins, 0, 128 * sizeof(uint32_t));
+        if (!e) e = dalloc(B.order, P);
         if (e) { free_lane_buffers(ctx); return cuda_check(ctx, e, "frame lane buffers"); }
         L.ready = true;
     }
@@ -882,7 +884,7 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
         if (slot > 0) {
             for (int k = 0; k < 2; k++) B.O[k] = L.B.O[k], B.D[k] = L.B.D[k], B.T[k] = L.B.T[k];
             B.hits = L.B.hits, B.shO = L.B.shO, B.shD = L.B.shD, B.shE = L.B.shE, B.pathAcc = L.B.pathAcc, B.counters = L.B.counters;
-            B.sortO = L.B.sortO, B.sortD = L.B.sortD, B.sortE = L.B.sortE, B.connBins = L.B.connBins;
+            B.sortO = L.B.sortO, B.sortD = L.B.sortD, B.sortE = L.B.sortE, B.connBins = L.B.connBins, B.order = L.B.order;
         }
         CK(cudaEventRecord(ctx->forkEv, ctx->st));
         CK(cudaStreamWaitEvent(st, ctx->forkEv, 0));

@@ -85,6 +85,7 @@ struct Counters {
     uint32_t probeInst, probePrim;
     float probeDist;
     unsigned long long travStats[4];   /* extend: nodes, triangles; connect: nodes, triangles */
+    uint32_t hitCount[64], missCount[64];   /* per path length: queue slots placed in the shading order so far */
 };
 
 #define LH2G_STATUS_STACK_OVERFLOW 1u

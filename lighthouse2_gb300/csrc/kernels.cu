@@ -78,6 +78,50 @@ __device__ __forceinline__ void shade_path(const SceneGPU& S, const FrameGPU& F,
     shade_core(S, F, B, depth, B.O[q][i], B.D[q][i], B.T[q][i], B.hits[i], out, pot);
 }
 
+/* The shading order of the extension queue of path length `depth`. A ray that hit nothing shades in a few
+ * instructions (sky, no connection, no extension), one that hit a surface in thousands; shaded in queue order, a
+ * warp of a bounce wave runs the long path with the few lanes whose ray hit. Here each tile of PART_TILE
+ * consecutive slots puts its hit slots, in queue order, at one place of the front of B.order and its missed ones
+ * at one place of the back, so that the shading warps run one kind of path: with the tiles' hits kept together,
+ * consecutive connections and extension rays still come from nearby slots. */
+constexpr uint32_t PART_TILE = 512;
+__global__ void __launch_bounds__(PART_TILE) k_partition(const FrameGPU F, const WaveBuffers B, const int depth) {
+    Counters* C = B.counters;
+    const uint32_t count = queue_count(F, C, depth);
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    __shared__ uint32_t hitsBefore[PART_TILE / 32], validBefore[PART_TILE / 32], base[2];
+    for (uint32_t t0 = blockIdx.x * PART_TILE; t0 < count; t0 += gridDim.x * PART_TILE) {   /* uniform in the block */
+        const uint32_t s = t0 + threadIdx.x;
+        const bool valid = s < count;
+        const bool hit = valid && __float_as_int(__ldg(&B.hits[s].z)) != NOHIT;
+        const uint32_t hm = __ballot_sync(0xffffffffu, hit), vm = __ballot_sync(0xffffffffu, valid);
+        if (lane == 0) hitsBefore[warp] = __popc(hm), validBefore[warp] = __popc(vm);
+        __syncthreads();
+        if (warp == 0) {   /* exclusive prefix over the 16 warps, the tile's bases in the order */
+            const uint32_t h0 = lane < PART_TILE / 32 ? hitsBefore[lane] : 0u, v0 = lane < PART_TILE / 32 ? validBefore[lane] : 0u;
+            uint32_t h = h0, v = v0;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const uint32_t h2 = __shfl_up_sync(0xffffffffu, h, off), v2 = __shfl_up_sync(0xffffffffu, v, off);
+                if ((int)lane >= off) h += h2, v += v2;
+            }
+            if (lane < PART_TILE / 32) hitsBefore[lane] = h - h0, validBefore[lane] = v - v0;
+            if (lane == PART_TILE / 32 - 1) {
+                base[0] = h ? atomicAdd(&C->hitCount[depth - 1], h) : 0u;
+                base[1] = v - h ? atomicAdd(&C->missCount[depth - 1], v - h) : 0u;
+            }
+        }
+        __syncthreads();
+        if (valid) {
+            const uint32_t lt = lanemask_lt();
+            const uint32_t pos = hit ? base[0] + hitsBefore[warp] + __popc(hm & lt)
+                                     : count - 1u - (base[1] + (validBefore[warp] - hitsBefore[warp]) + __popc(vm & ~hm & lt));
+            B.order[pos] = s;
+        }
+        __syncthreads();   /* the next tile rewrites the prefixes */
+    }
+}
+
 /* tuning switch: resident CTAs per SM the shading kernel is compiled for (register cap); 0 leaves it to the compiler */
 #ifndef LH2G_SHADE_MINBLOCKS
 #define LH2G_SHADE_MINBLOCKS 0
@@ -97,7 +141,7 @@ __global__ void __launch_bounds__(WAVE_BLOCK) k_shade(const SceneGPU S, const Fr
         const uint32_t i = base + threadIdx.x;
         ShadeOut out;
         out.ext = out.shadow = false;
-        if (i < count) shade_path(S, F, B, depth, i, out, potential + threadIdx.x);
+        if (i < count) shade_path(S, F, B, depth, B.order ? __ldg(B.order + i) : i, out, potential + threadIdx.x);
         const uint32_t em = __ballot_sync(0xffffffffu, out.ext);
         if (em) {
             const int leader = __ffs(em) - 1;
@@ -412,6 +456,7 @@ void launch_extend(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, i
     k_extend<<<blocks, 128, 0, st>>>(S, F, B, depth);
 }
 void launch_shade(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int blocks, cudaStream_t st) {
+    if (B.order) k_partition<<<sm_count() * 2, PART_TILE, 0, st>>>(F, B, depth);
     k_shade<<<blocks, WAVE_BLOCK, 0, st>>>(S, F, B, depth);
 }
 void launch_connect(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int blocks, cudaStream_t st) {

@@ -28,10 +28,13 @@ struct WaveBuffers {
     float4* sortD;
     float4* sortE;
     uint32_t* connBins;    /* 64 per-light counts, then their running offsets */
+    uint32_t* order = nullptr;   /* shading order of the extension queue: the slots whose ray hit something first,
+                                  * those that missed after them (null: queue order) */
 };
 
 void launch_generate(const FrameGPU& F, const WaveBuffers& B, cudaStream_t st);
 void launch_extend(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int persistentBlocks, cudaStream_t st);
+/* with B.order: the partition of the queue into hits and misses (k_partition), then the shading */
 void launch_shade(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int blocks, cudaStream_t st);
 void launch_connect(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int persistentBlocks, cudaStream_t st);
 /* path lengths startDepth..maxDepth of the frame's remaining paths, one persistent launch */
