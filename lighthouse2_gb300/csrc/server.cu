@@ -78,6 +78,7 @@ struct ServerState {
     uint32_t expPrefix[MAX_EXPRESS + 1];
     unsigned long long rays;           /* rays traced over all ticks */
     unsigned long long ticks;
+    uint32_t hitCount, missCount;      /* slots placed in this tick's shading order */
 };
 
 struct SceneTable { SceneGPU s[MAX_SCENES]; };
@@ -90,6 +91,7 @@ struct Queues {
     float4* shO;
     float4* shD;
     float4* shE;
+    uint32_t* order;                   /* shading order of the current queue (partition_queue) */
 };
 
 __device__ __forceinline__ uint32_t slot_of(const float4& d4) { return (__float_as_uint(d4.w) >> SLOT_SHIFT) & 255u; }
@@ -150,11 +152,12 @@ __global__ void __launch_bounds__(WAVE_BLOCK) k_srv_shade(const __grid_constant_
     const uint32_t lane = threadIdx.x & 31u;
     __shared__ float potential[64 * WAVE_BLOCK];
     for (uint32_t b0 = blockIdx.x * blockDim.x; b0 < count; b0 += gridDim.x * blockDim.x) {
-        const uint32_t i = b0 + threadIdx.x;
+        const uint32_t j = b0 + threadIdx.x;
         ShadeOut out;
         out.ext = out.shadow = false;
         uint32_t slot = 0;
-        if (i < count) {
+        if (j < count) {
+            const uint32_t i = __ldg(Q.order + j);
             const float4 o4 = Q.O[cur][i], d4 = Q.D[cur][i], t4 = Q.T[cur][i], hit = Q.hits[i];
             slot = slot_of(d4);
             const int depth = (int)((__float_as_uint(d4.w) >> DEPTH_SHIFT) & 127u);
@@ -168,7 +171,7 @@ __global__ void __launch_bounds__(WAVE_BLOCK) k_srv_shade(const __grid_constant_
         }
         /* paths that end here leave their job's live count: one atomic per job and warp (one per path would
          * serialise on the few counters of the jobs in flight) */
-        const uint32_t endSlot = (i < count && !out.ext) ? slot : 0xffffffffu;
+        const uint32_t endSlot = (j < count && !out.ext) ? slot : 0xffffffffu;
         const uint32_t peers = __match_any_sync(0xffffffffu, endSlot);
         if (endSlot != 0xffffffffu && lane == (uint32_t)(__ffs(peers) - 1)) atomicSub(&alive[endSlot], __popc(peers));
         const uint32_t em = __ballot_sync(0xffffffffu, out.ext);
@@ -188,6 +191,11 @@ __global__ void __launch_bounds__(WAVE_BLOCK) k_srv_shade(const __grid_constant_
             if (out.shadow) Q.shO[s] = out.sO, Q.shD[s] = out.sD, Q.shE[s] = out.sE;
         }
     }
+}
+
+/* the shading order of this tick's queue: hits first, misses last */
+__global__ void __launch_bounds__(PART_TILE) k_srv_partition(ServerState* st, const Queues Q) {
+    partition_queue(Q.hits, st->qCount[st->cur] + st->newTotal, Q.order, &st->hitCount, &st->missCount);
 }
 
 /* any hit of every connection; unoccluded ones add their contribution to their path */
@@ -308,6 +316,7 @@ __global__ void k_srv_end(ServerState* st) {
     st->fetch[0] = st->fetch[1] = 0;
     st->newCount = st->newTotal = 0;
     st->expCount = st->expTotal = 0;
+    st->hitCount = st->missCount = 0;
 }
 
 /* per-pixel sums of a finished job's paths in sample order (as the plain core's finalize) */
@@ -377,7 +386,7 @@ struct lh2g_server {
     cudaGraph_t tickGraph = nullptr;
     std::vector<cudaEvent_t> tickEv;   /* ring of tick-completion events */
     long long ticksLaunched = 0, ticksDone = 0;
-    int blocksGen = 0, blocksExtend = 0, blocksShade = 0, blocksConnect = 0, blocksTrace0 = 0, blocksTrace1 = 0, blocksExpress = 0;
+    int blocksGen = 0, blocksExtend = 0, blocksShade = 0, blocksConnect = 0, blocksTrace0 = 0, blocksTrace1 = 0, blocksExpress = 0, blocksPart = 0;
     /* jobs */
     std::mutex mu;
     std::condition_variable cvWork, cvDone;
@@ -699,6 +708,7 @@ int build_tick_graph(lh2g_server* s) {
     k_srv_express<<<s->blocksExpress, WAVE_BLOCK, 0, s->side>>>(T, s->dJobs, s->dState, s->dAlive);
     cudaEventRecord(s->evJoin, s->side);
     k_srv_extend<<<s->blocksExtend, 128, 0, s->st>>>(T, s->dJobs, s->dState, s->Q);
+    k_srv_partition<<<s->blocksPart, PART_TILE, 0, s->st>>>(s->dState, s->Q);
     k_srv_shade<<<s->blocksShade, WAVE_BLOCK, 0, s->st>>>(T, s->dJobs, s->dState, s->Q, s->dAlive);
     k_srv_connect<<<s->blocksConnect, 128, 0, s->st>>>(T, s->dJobs, s->dState, s->Q);
     cudaStreamWaitEvent(s->st, s->evJoin, 0);
@@ -743,7 +753,8 @@ int lh2g_server_create(int device, long long pathCapacity, lh2g_server** out) {
         ok = cudaMalloc((void**)&s->Q.O[k], 16 * cap) == cudaSuccess && cudaMalloc((void**)&s->Q.D[k], 16 * cap) == cudaSuccess &&
              cudaMalloc((void**)&s->Q.T[k], 16 * cap) == cudaSuccess;
     ok = ok && cudaMalloc((void**)&s->Q.hits, 16 * cap) == cudaSuccess && cudaMalloc((void**)&s->Q.shO, 16 * cap) == cudaSuccess &&
-         cudaMalloc((void**)&s->Q.shD, 16 * cap) == cudaSuccess && cudaMalloc((void**)&s->Q.shE, 16 * cap) == cudaSuccess;
+         cudaMalloc((void**)&s->Q.shD, 16 * cap) == cudaSuccess && cudaMalloc((void**)&s->Q.shE, 16 * cap) == cudaSuccess &&
+         cudaMalloc((void**)&s->Q.order, 4 * cap) == cudaSuccess;
     ok = ok && cudaMalloc((void**)&s->dJobs, sizeof(JobGPU) * MAX_SLOTS) == cudaSuccess;
     ok = ok && cudaMalloc((void**)&s->dAlive, sizeof(int) * MAX_SLOTS) == cudaSuccess;
     ok = ok && cudaMalloc((void**)&s->dState, sizeof(ServerState)) == cudaSuccess;
@@ -768,6 +779,7 @@ int lh2g_server_create(int device, long long pathCapacity, lh2g_server** out) {
         int sms = 1;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
         s->blocksExpress = 2 * sms;
+        s->blocksPart = 2 * sms;
         s->blocksTrace0 = persistent_blocks_trace(0);
         s->blocksTrace1 = persistent_blocks_trace(1);
         s->tickEv.resize(4);
@@ -808,7 +820,7 @@ int lh2g_server_destroy(lh2g_server* s) {
     if (s->tickGraph) cudaGraphDestroy(s->tickGraph);
     for (auto& e : s->tickEv) if (e) cudaEventDestroy(e);
     for (int k = 0; k < 2; k++) cudaFree(s->Q.O[k]), cudaFree(s->Q.D[k]), cudaFree(s->Q.T[k]);
-    cudaFree(s->Q.hits), cudaFree(s->Q.shO), cudaFree(s->Q.shD), cudaFree(s->Q.shE);
+    cudaFree(s->Q.hits), cudaFree(s->Q.shO), cudaFree(s->Q.shD), cudaFree(s->Q.shE), cudaFree(s->Q.order);
     cudaFree(s->dJobs), cudaFree(s->dAlive), cudaFree(s->dState);
     if (s->hAlive) cudaFreeHost(s->hAlive);
     if (s->hTick) cudaFreeHost(s->hTick);

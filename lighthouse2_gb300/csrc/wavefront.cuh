@@ -52,6 +52,50 @@ struct ShadeOut {
     float4 sO, sD, sE;
 };
 
+/* The shading order of a queue of `count` rays with their hit records. A ray that hit nothing shades in a few
+ * instructions (sky, no connection, no extension), one that hit a surface in thousands; shaded in queue order, a
+ * warp of a bounce wave runs the long path with the few lanes whose ray hit. Each tile of PART_TILE consecutive
+ * slots puts its hit slots, in queue order, at one place of the front of `order` (counter *hitCount) and its
+ * missed ones at one place of the back (*missCount), so that the shading warps run one kind of path; with the
+ * tiles' hits kept together, consecutive connections and extension rays still come from nearby slots. Launched
+ * with PART_TILE threads per block; both counters start at zero. */
+constexpr uint32_t PART_TILE = 512;
+__device__ __forceinline__ void partition_queue(const float4* __restrict__ hits, const uint32_t count, uint32_t* __restrict__ order,
+                                                uint32_t* hitCount, uint32_t* missCount) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    __shared__ uint32_t hitsBefore[PART_TILE / 32], validBefore[PART_TILE / 32], base[2];
+    for (uint32_t t0 = blockIdx.x * PART_TILE; t0 < count; t0 += gridDim.x * PART_TILE) {   /* uniform in the block */
+        const uint32_t s = t0 + threadIdx.x;
+        const bool valid = s < count;
+        const bool hit = valid && __float_as_int(__ldg(&hits[s].z)) != NOHIT;
+        const uint32_t hm = __ballot_sync(0xffffffffu, hit), vm = __ballot_sync(0xffffffffu, valid);
+        if (lane == 0) hitsBefore[warp] = __popc(hm), validBefore[warp] = __popc(vm);
+        __syncthreads();
+        if (warp == 0) {   /* exclusive prefix over the 16 warps, the tile's bases in the order */
+            const uint32_t h0 = lane < PART_TILE / 32 ? hitsBefore[lane] : 0u, v0 = lane < PART_TILE / 32 ? validBefore[lane] : 0u;
+            uint32_t h = h0, v = v0;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const uint32_t h2 = __shfl_up_sync(0xffffffffu, h, off), v2 = __shfl_up_sync(0xffffffffu, v, off);
+                if ((int)lane >= off) h += h2, v += v2;
+            }
+            if (lane < PART_TILE / 32) hitsBefore[lane] = h - h0, validBefore[lane] = v - v0;
+            if (lane == PART_TILE / 32 - 1) {
+                base[0] = h ? atomicAdd(hitCount, h) : 0u;
+                base[1] = v - h ? atomicAdd(missCount, v - h) : 0u;
+            }
+        }
+        __syncthreads();
+        if (valid) {
+            const uint32_t lt = lanemask_lt();
+            const uint32_t pos = hit ? base[0] + hitsBefore[warp] + __popc(hm & lt)
+                                     : count - 1u - (base[1] + (validBefore[warp] - hitsBefore[warp]) + __popc(vm & ~hm & lt));
+            order[pos] = s;
+        }
+        __syncthreads();   /* the next tile rewrites the prefixes */
+    }
+}
+
 /* Shading of one path vertex (lib/RenderCore_PrimeRef/kernels/pathtracer.h:45-168, with the filter core's
  * feature gathering for LH2G_RP_FILTER): o4, d4, t4 = the path's ray state, hit = its closest hit. Radiance goes
  * to the path's own accumulator; a connection and an extension ray are returned in out. */
