@@ -418,7 +418,7 @@ void launch_extend(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, i
     k_extend<<<blocks, 128, 0, st>>>(S, F, B, depth);
 }
 void launch_shade(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int blocks, cudaStream_t st) {
-    if (B.order) k_partition<<<sm_count() * 2, PART_TILE, 0, st>>>(F, B, depth);
+    if (B.order) k_partition<<<sm_count() * 4, PART_TILE, 0, st>>>(F, B, depth);
     k_shade<<<blocks, WAVE_BLOCK, 0, st>>>(S, F, B, depth);
 }
 void launch_connect(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int blocks, cudaStream_t st) {

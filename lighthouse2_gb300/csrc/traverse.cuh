@@ -55,7 +55,13 @@ constexpr uint32_t MAX_STEPS = 1u << 20;   /* far beyond any traversal of a well
 
 struct HitRec { float t, u, v; int inst, prim; };
 
-LH2G_DEV float safe_rcp(float d) { return fabsf(d) < 1e-30f ? (d < 0.0f ? -1e30f : 1e30f) : 1.0f / d; }
+/* 1 / d for the box tests, which only cull: the hardware reciprocal (at most 1 ulp off, which the slab margins
+ * cover); |d| below 1e-30 (no denormal reaches rcp) gives +-1e30 */
+LH2G_DEV float safe_rcp(float d) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(d));
+    return fabsf(d) < 1e-30f ? (d < 0.0f ? -1e30f : 1e30f) : r;
+}
 
 LH2G_DEV float3 xform_point(const float* m, float3 p) {
     return make_float3(m[0] * p.x + m[1] * p.y + m[2] * p.z + m[3], m[4] * p.x + m[5] * p.y + m[6] * p.z + m[7],
