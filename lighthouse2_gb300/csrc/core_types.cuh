@@ -31,12 +31,13 @@ struct BVH8Node {
 static_assert(sizeof(BVH8Node) == 80, "BVH8 node must be 80 bytes");
 
 /* Instance record for traversal (64 B): inverse transform rows (object <- world), BLAS root, mesh. */
-struct InstanceGPU {
+struct alignas(16) InstanceGPU {   /* read as four float4 by the traversal */
     float inv[12];
     uint32_t blasRoot;       /* 0xffffffff: empty mesh */
     uint32_t mesh;
     uint32_t pad0, pad1;
 };
+static_assert(sizeof(InstanceGPU) == 64, "InstanceGPU must be four float4");
 
 /* Everything the kernels read about the scene. Passed by value. */
 struct SceneGPU {

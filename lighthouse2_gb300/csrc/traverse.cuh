@@ -316,12 +316,12 @@ struct Traversal {
             const uint32_t first = entry & 0x0fffffffu, cnt = ((entry >> 28) & 3u) + 1u;
             if (cnt > 1u && sp < LH2G_STACK) stack[sp++] = make_uint2(0x80000000u | ((cnt - 2u) << 28) | (first + 1u), 0u);
             const int ii = (int)__ldg(S.tlasPrims + first);
-            const InstanceGPU* in = S.inst + ii;
-            const uint32_t root = __ldg(&in->blasRoot);
+            /* an InstanceGPU is four aligned float4: the three rows of the inverse transform, then blasRoot */
+            const float4* in = reinterpret_cast<const float4*>(S.inst + ii);
+            const uint32_t root = __float_as_uint(__ldg(in + 3).x);
             if (root != 0xffffffffu && sp < LH2G_STACK) {
-                float m[12];
-#pragma unroll
-                for (int k = 0; k < 12; k++) m[k] = __ldg(&in->inv[k]);
+                const float4 r0 = __ldg(in), r1 = __ldg(in + 1), r2 = __ldg(in + 2);
+                const float m[12] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w};
                 O = xform_point(m, Ow), D = xform_vector(m, Dw);
                 invD = make_float3(safe_rcp(D.x), safe_rcp(D.y), safe_rcp(D.z));
                 curInst = ii;
