@@ -43,8 +43,8 @@ MAX_DEPTH, RR_START = 8, 4
 WAVE_TAIL = 5          # path lengths >= 5 run in the persistent tail kernel (setting "waveTail")
 LANES = 4              # frames in flight (setting "pipelineFrames")
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of two k_extend launches of this workload (waves 2 and 3 of
-# camera pose 1): 192.95 MB + 73.18 MB (profiles/k_extend_spheres_2m_1080p.md)
-EXTEND_CAPTURE = {"pose": 1, "waves": (2, 3), "dram_bytes": 192.948736e6 + 73.179648e6}
+# camera pose 1): 196.85 MB + 74.09 MB (profiles/k_extend_spheres_2m_1080p.md)
+EXTEND_CAPTURE = {"pose": 1, "waves": (2, 3), "dram_bytes": 196.84736e6 + 74.086912e6}
 WORKLOAD = "spheres_2m: 64 x 32k-tri displaced spheres + ground (2,048,002 tris, 66 instances), 16 quad + 4 point lights, " \
            "20 materials (4 textured), sky; 1920x1080 1spp, max depth 8, RR after depth 3, NEE"
 METRIC = "Mrays/s @1080p 1spp"
