@@ -406,7 +406,13 @@ int persistent_blocks_wave(int which) {
     int per = 0;
     if (which == 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_extend, 128, 0);
     else if (which == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_connect, 128, 0);
-    else if (which == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_shade, WAVE_BLOCK, 0);
+    else if (which == 2) {
+#if LH2G_SHADE_MINBLOCKS > 4
+        /* more than four CTAs of 32 KB need a shared-memory configuration above 132 KB */
+        cudaFuncSetAttribute(k_shade, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+#endif
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_shade, WAVE_BLOCK, 0);
+    }
     else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_tail, WAVE_BLOCK, 0);
     return sm_count() * (per > 0 ? per : 1);
 }
