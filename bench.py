@@ -512,7 +512,7 @@ def nrc_leg(args, core, name, view, bounds, W, H):
     box = [[round(float(x), 3) for x in b] for b in bounds]
     out = {"workload": f"{name}, {W}x{H}, depth {MAX_DEPTH}, RR after depth {RR_START - 1}, NEE; reference {args.nrc_ref_spp} spp plain, "
                        f"FP64 sums ({ref_s:.0f} s); cache box {box}, Adam lr {args.nrc_lr}; trained over {args.nrc_warmup} frames "
-                       f"first, then online (1/16 of the paths, at most 65,536 per frame); relmse = mean of err^2 / (ref^2 + 0.01)",
+                       f"first, then online (1/32 of the cached paths, at most 65,536 per frame); relmse = mean of err^2 / (ref^2 + 0.01)",
            "plain_ms_per_frame": t_plain * 1e3, "cache_ms_per_frame": t_cache * 1e3,
            "cache_queries_per_frame": stats[-1][0], "train_samples_per_frame": stats[-1][1],
            "loss_first": float(np.mean([x[2] for x in stats[:5]])), "loss_last": float(np.mean([x[2] for x in stats[-5:]])), "equal_time": {}}

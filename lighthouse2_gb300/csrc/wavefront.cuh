@@ -11,6 +11,11 @@ namespace {
 
 constexpr int WAVE_BLOCK = 128;
 constexpr int NRC_DEPTH = 2;   /* first path length at which radiance-cache frames query the cache */
+#ifndef LH2G_NRC_TRAIN_SHIFT
+#define LH2G_NRC_TRAIN_SHIFT 5
+#endif
+/* 1 in 2^LH2G_NRC_TRAIN_SHIFT cached paths trace on and train the cache (about 3 %) */
+constexpr uint32_t NRC_TRAIN_MASK = (1u << LH2G_NRC_TRAIN_SHIFT) - 1u;
 constexpr uint32_t S_CACHED = 8;   /* radiance-cache frames: the path has recorded its cache vertex */
 
 __device__ __forceinline__ uint32_t lanemask_lt() { uint32_t m; asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m)); return m; }
@@ -173,9 +178,9 @@ __device__ __forceinline__ void shade_core(const SceneGPU& S, const FrameGPU& F,
     if ((F.flags & LH2G_RP_NRC) && depth >= NRC_DEPTH && (FLAGS & (S_SPECULAR | S_CACHED)) == 0) {
         /* radiance cache, at the first vertex from path length 2 on that a diffuse bounce leads to (after a specular
          * bounce the path footprint is still small: it traces on): the query of this vertex (looking back along the
-         * ray), the throughput that reaches it and the radiance gathered before it; a training path (1 in 16)
-         * traces on, the others end here */
-        const bool train = (WangHash(pathIdx * 3u + F.cameraR0) & 15u) == 0u;
+         * ray), the throughput that reaches it and the radiance gathered before it; a training path
+         * (NRC_TRAIN_MASK) traces on, the others end here */
+        const bool train = (WangHash(pathIdx * 3u + F.cameraR0) & NRC_TRAIN_MASK) == 0u;
         const float side = dot(D, N) > 0 ? -1.0f : 1.0f;
         float4* rec = B.nrcRec + pathIdx;
         const int64_t P = F.P;
