@@ -44,6 +44,10 @@ namespace lh2g {
 #ifndef LH2G_SORT_CHILDREN
 #define LH2G_SORT_CHILDREN 1
 #endif
+/* LH2G_SORT_ANYHIT 1: any-hit queries push their hit children sorted too (nearest first); 0: in slot order */
+#ifndef LH2G_SORT_ANYHIT
+#define LH2G_SORT_ANYHIT 0
+#endif
 /* with LH2G_REFILL: idle lanes of a warp take new rays once at least this many are idle (or all are) */
 #ifndef LH2G_REFILL_MIN
 #define LH2G_REFILL_MIN 1
@@ -234,7 +238,7 @@ struct Traversal {
         }
         return true;
 #else
-        if (!ANYHIT) {
+        if (!ANYHIT || LH2G_SORT_ANYHIT) {
             cx(key[0], key[1]), cx(key[2], key[3]), cx(key[4], key[5]), cx(key[6], key[7]);
             cx(key[0], key[2]), cx(key[1], key[3]), cx(key[4], key[6]), cx(key[5], key[7]);
             cx(key[1], key[2]), cx(key[5], key[6]);
