@@ -212,7 +212,8 @@ __global__ void __launch_bounds__(128) k_connect(const SceneGPU S, const FrameGP
 /* --------------------------------------------------------------------------------------------------
  * Connections grouped by light: a counting sort over the light index the shading stage keeps in E.w bits 1..6.
  * Shadow rays towards one light from neighbouring points visit much of the same tree, so a warp of them
- * diverges less. The order within a light follows the original order (warp by warp). */
+ * diverges less. Within a light, each warp's connections stay together and in their order; the warps' runs follow
+ * one another in the order their atomics arrive. */
 __global__ void k_conn_count(const WaveBuffers B, const int depth) {
     __shared__ uint32_t h[64];
     if (threadIdx.x < 64) h[threadIdx.x] = 0;
