@@ -91,5 +91,6 @@ struct Counters {
 
 #define LH2G_STATUS_STACK_OVERFLOW 1u
 #define LH2G_STATUS_TRAVERSAL_LIMIT 2u
+#define LH2G_STATUS_QUEUE_OVERFLOW 4u   /* serving loop: new paths would not have fit the queue (skipped) */
 
 }  // namespace lh2g

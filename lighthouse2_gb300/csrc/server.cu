@@ -10,7 +10,8 @@
  *             connect (any hit); swap the queues; copy the per-job counts of live paths to the host.
  *             A path carries its job slot (bits 8..15) and its own path length (bits 16..22) in its flag word,
  *             so paths of jobs admitted at different ticks, and at different depths, are processed together.
- *   admission a job is admitted when its paths fit in the queue capacity (path memory, reserved whole) and a
+ *   admission a job is admitted when its paths fit in the queue capacity (path memory, counted from the live
+ *             paths of the jobs in flight) and a
  *             slot is free: the smallest pending job first, the oldest one once it has waited longer than a bound.
  *             Its paths enter the queues in ranges, at most a tick budget of new paths per tick, so that a large
  *             job does not stretch the ticks every small job needs. A job whose live-path count reached zero is
@@ -92,6 +93,7 @@ struct Queues {
     float4* shD;
     float4* shE;
     uint32_t* order;                   /* shading order of the current queue (partition_queue) */
+    uint32_t cap;                      /* slots of each queue */
 };
 
 __device__ __forceinline__ uint32_t slot_of(const float4& d4) { return (__float_as_uint(d4.w) >> SLOT_SHIFT) & 255u; }
@@ -101,7 +103,10 @@ __global__ void __launch_bounds__(256) k_srv_generate(const JobGPU* __restrict__
     const uint32_t total = st->newTotal, n = st->newCount;
     if (total == 0) return;
     const uint32_t cur = st->cur, base = st->qCount[cur];
-    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+    /* admission keeps base + total within the queue; should it not, the paths that do not fit are left out and
+     * the tick reports it instead of writing past the queue */
+    if (base + total > Q.cap && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&st->status, LH2G_STATUS_QUEUE_OVERFLOW);
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total && base + g < Q.cap; g += gridDim.x * blockDim.x) {
         uint32_t j = 0;
         while (j + 1 < n && st->newPrefix[j + 1] <= g) j++;
         const uint32_t slot = st->newSlot[j], i = st->newStart[j] + (g - st->newPrefix[j]);
@@ -481,13 +486,23 @@ void run_query(lh2g_server* s, Job* j) {
 struct Range { Job* job; long long start, count; bool first, express; };
 
 /* Admission for the next tick. Ray queries go to the worker. Render jobs are admitted when their paths fit in the
- * capacity (reserved whole) and a slot is free: the smallest pending job first, unless one has waited longer than
+ * capacity beside the live paths of the jobs in flight and a slot is free: the smallest pending job first, unless one has waited longer than
  * maxWaitS (then the oldest); a job that does not fit stops admission, so no job waits forever. The paths of
  * admitted jobs enter the queues in ranges, at most tickBudget new paths per tick, so that one large job does not
  * stretch the ticks that every small job needs. */
 void admit(lh2g_server* s, std::vector<Range>& ranges) {
     std::lock_guard<std::mutex> g(s->mu);
     long long budget = s->tickBudget, expBudget = s->expressBudget;
+    /* Queue slots the next tick can need for the jobs in flight. A job's live count (its paths not yet ended,
+     * including those not yet in the queue) only falls, and the host's copy of it is at most one tick old, so it
+     * bounds the job's share of the next queue from above; a job whose first tick has not completed yet counts
+     * all its paths. Capacity is thus released as paths end, not when the job's last path ends. */
+    long long inUse = 0;
+    for (int k = 0; k < MAX_SLOTS; k++) {
+        const Job* j = s->slots[k];
+        if (!j || j->express) continue;
+        inUse += (j->admitTick >= 0 && j->admitTick < s->ticksDone) ? std::min<long long>(std::max(s->hAlive[k], 0), j->paths) : j->paths;
+    }
     int nNew = 0, nExp = 0;
     auto take = [&](Job* j, bool first) {
         const long long n = std::min(j->paths - j->admittedPaths, std::max(budget, 1ll));
@@ -537,7 +552,7 @@ void admit(lh2g_server* s, std::vector<Range>& ranges) {
             continue;
         }
         if (budget <= 0 || nNew >= MAX_NEW) break;
-        if (s->pathsInFlight + j->paths > s->capacity) break;   /* wait for path memory */
+        if (inUse + j->paths > s->capacity) break;   /* wait for path memory */
         int slot = -1;
         for (int k = 0; k < MAX_SLOTS; k++)
             if (!s->slots[k]) { slot = k; break; }
@@ -546,6 +561,7 @@ void admit(lh2g_server* s, std::vector<Range>& ranges) {
         j->slot = slot;
         s->slots[slot] = j;
         s->pathsInFlight += j->paths;
+        inUse += j->paths;
         j->state = 1, j->tAdmit = now;
         take(j, true);
         if (j->admittedPaths < j->paths) s->partial.push_back(j);
@@ -755,6 +771,7 @@ int lh2g_server_create(int device, long long pathCapacity, lh2g_server** out) {
     ok = ok && cudaMalloc((void**)&s->Q.hits, 16 * cap) == cudaSuccess && cudaMalloc((void**)&s->Q.shO, 16 * cap) == cudaSuccess &&
          cudaMalloc((void**)&s->Q.shD, 16 * cap) == cudaSuccess && cudaMalloc((void**)&s->Q.shE, 16 * cap) == cudaSuccess &&
          cudaMalloc((void**)&s->Q.order, 4 * cap) == cudaSuccess;
+    s->Q.cap = (uint32_t)cap;
     ok = ok && cudaMalloc((void**)&s->dJobs, sizeof(JobGPU) * MAX_SLOTS) == cudaSuccess;
     ok = ok && cudaMalloc((void**)&s->dAlive, sizeof(int) * MAX_SLOTS) == cudaSuccess;
     ok = ok && cudaMalloc((void**)&s->dState, sizeof(ServerState)) == cudaSuccess;

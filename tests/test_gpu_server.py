@@ -100,6 +100,8 @@ def test_admission_by_path_memory_and_queries(two_scenes, oracle_lib):
         view, p = job_inputs(*jobs[k])
         exp = plain_core_image([ca, cb][jobs[k][0]], view, p)
         assert np.array_equal(srv.result(jid).view(np.uint32), exp.view(np.uint32)), f"job {k} under admission limits differs"
+    # admission counts the live paths of the jobs in flight: the queue never had to drop new paths
+    assert srv.stats()["deviceStatus"] == 0
     srv.wait(q0), srv.wait(q1)
     assert np.array_equal(srv.result(q0), cb.trace_host(rays, 0))
     assert np.array_equal(srv.result(q1), cb.trace_host(rays, 1))
