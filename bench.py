@@ -310,6 +310,9 @@ def svgf_leg(core, W, H, steps, warmup):
             "peak_GBps": peak, "frac": achieved / peak, "peak_source": peak_kind}
 
 
+# serving loop queue capacity in paths when the mix's largest job needs less: 8M paths hold about 1.2 GB of queues
+# (well inside a 40 GB path-memory budget at 64 B per path) and let ticks carry several small jobs at once
+SERVING_CAPACITY = 1 << 23
 SERVING_MIXES = {
     # the serving workload's job distribution: resolution in {256^2, 512^2, 1024^2, 1920x1080}, spp in {1, 4, 16}
     "full": {"res": [(256, 256), (512, 512), (1024, 1024), (1920, 1080)], "spp": [1, 4, 16], "rates": [10, 20, 30, 40, 50, 60, 100, 200]},
@@ -386,7 +389,7 @@ def serving_leg(args):
             seq_rays += j["W"] * j["H"] * j["spp"] + int(cnt[:, 0].sum()) + int(cnt[:, 1].sum())
         service = np.array(service)
         t_seq = float(service.sum())
-        cap = max(j["W"] * j["H"] * j["spp"] for j in jobs) * 2
+        cap = max(max(j["W"] * j["H"] * j["spp"] for j in jobs) * 2, args.serving_capacity)
         srv = RenderServer(path_capacity=cap)
         sids = [srv.add_scene(c) for c in cores]
         for j in jobs[:4]:   # warm-up
@@ -713,6 +716,8 @@ def main():
     ap.add_argument("--nrc-ref-spp", type=int, default=4096)
     ap.add_argument("--nrc-warmup", type=int, default=200)
     ap.add_argument("--serving-jobs", type=int, default=120)
+    ap.add_argument("--serving-capacity", type=int, default=SERVING_CAPACITY,
+                    help="queue capacity of the serving loop in paths (at least twice the largest job)")
     ap.add_argument("--lanes", type=int, default=LANES, help="frames in flight (0 or 1: one at a time)")
     ap.add_argument("--sort-connections", type=int, default=0, help="group connections by light before the any-hit queries")
     ap.add_argument("--wave-tail", type=int, default=WAVE_TAIL, help="first path length of the persistent tail kernel (0: off)")
