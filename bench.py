@@ -390,7 +390,7 @@ def serving_leg(args):
         service = np.array(service)
         t_seq = float(service.sum())
         cap = max(max(j["W"] * j["H"] * j["spp"] for j in jobs) * 2, args.serving_capacity)
-        srv = RenderServer(path_capacity=cap)
+        srv = RenderServer(path_capacity=cap, **({"tickBudget": args.serving_tick_budget} if args.serving_tick_budget else {}))
         sids = [srv.add_scene(c) for c in cores]
         for j in jobs[:4]:   # warm-up
             view, p = inputs(j)
@@ -718,6 +718,7 @@ def main():
     ap.add_argument("--serving-jobs", type=int, default=120)
     ap.add_argument("--serving-capacity", type=int, default=SERVING_CAPACITY,
                     help="queue capacity of the serving loop in paths (at least twice the largest job)")
+    ap.add_argument("--serving-tick-budget", type=int, default=0, help="new paths per tick of the serving loop (0: the loop's default)")
     ap.add_argument("--lanes", type=int, default=LANES, help="frames in flight (0 or 1: one at a time)")
     ap.add_argument("--sort-connections", type=int, default=0, help="group connections by light before the any-hit queries")
     ap.add_argument("--wave-tail", type=int, default=WAVE_TAIL, help="first path length of the persistent tail kernel (0: off)")
