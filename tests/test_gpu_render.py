@@ -209,3 +209,37 @@ def test_connections_grouped_by_light_change_nothing(core_lib, tail):
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1].view(np.uint32), out[1][1].view(np.uint32))
     assert np.array_equal(out[0][2].view(np.uint32), out[1][2].view(np.uint32))
+
+
+@pytest.fixture(scope="module")
+def spheres_small(core_lib, oracle_lib):
+    sc = S.spheres_2m(n_spheres=6, slices=32, stacks=20, tex_size=64)
+    core = RenderCore()
+    core.set_scene(sc)
+    o = oracle_lib.Oracle()
+    o.set_scene(sc)
+    return sc, core, o
+
+
+@pytest.mark.parametrize("W,H,spp", [(1, 1, 1), (7, 5, 3), (33, 31, 1)])
+def test_ragged_path_counts(spheres_small, W, H, spp):
+    """Path counts that fill no whole tile of the shading partition (512 queue slots) nor a whole warp."""
+    sc, core, o = spheres_small
+    core.SetTarget(W, H, spp)
+    view = S.spheres_view(W, H, frame=3)
+    p = make_params(W, H, spp, max_depth=8, rr_start=4, camera_r0=camera_r0(2), flags=RP_NEE | RP_DEPTH_W)
+    _check_frame(core, o, view, p)
+
+
+def test_all_rays_miss(spheres_small):
+    """A camera above the lights looking up: every primary ray misses, the waves after the first are empty and the
+    frame is the sky alone."""
+    sc, core, o = spheres_small
+    W, H, spp = 37, 23, 3
+    core.SetTarget(W, H, spp)
+    view = S.make_view((0.0, 60.0, 0.0), (0.0, 200.0, 0.0), 40.0, W, H, up=(1.0, 0.0, 0.0))
+    p = make_params(W, H, spp, max_depth=8, rr_start=4, camera_r0=camera_r0(0), flags=RP_NEE | RP_DEPTH_W)
+    img = _check_frame(core, o, view, p)
+    c = core.render_ex(view, p, counters=True)["counters"]
+    assert c.sum() == 0, c.tolist()
+    assert np.isfinite(img).all() and img[:, :3].min() > 0
