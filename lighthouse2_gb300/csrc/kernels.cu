@@ -84,9 +84,10 @@ __global__ void __launch_bounds__(PART_TILE) k_partition(const FrameGPU F, const
     partition_queue(B.hits, queue_count(F, C, depth), B.order, &C->hitCount[depth - 1], &C->missCount[depth - 1]);
 }
 
-/* tuning switch: resident CTAs per SM the shading kernel is compiled for (register cap); 0 leaves it to the compiler */
+/* tuning switch: resident CTAs per SM the shading kernel is compiled for (register cap; 6: 80 registers and a
+ * few spills, 24 warps per SM where the compiler's 128 registers allowed 16); 0 leaves it to the compiler */
 #ifndef LH2G_SHADE_MINBLOCKS
-#define LH2G_SHADE_MINBLOCKS 0
+#define LH2G_SHADE_MINBLOCKS 6
 #endif
 #if LH2G_SHADE_MINBLOCKS > 0
 __global__ void __launch_bounds__(WAVE_BLOCK, LH2G_SHADE_MINBLOCKS) k_shade(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int depth) {
@@ -98,7 +99,7 @@ __global__ void __launch_bounds__(WAVE_BLOCK) k_shade(const SceneGPU S, const Fr
     const int nq = depth & 1;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t stride = gridDim.x * blockDim.x;
-    __shared__ float potential[64 * WAVE_BLOCK];   /* light-selection potentials, 64 lights x 128 threads */
+    extern __shared__ float potential[];   /* light-selection potentials, (lights) x 128 threads, sized at launch */
     for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += stride) {
         const uint32_t i = base + threadIdx.x;
         ShadeOut out;
@@ -408,11 +409,9 @@ int persistent_blocks_wave(int which) {
     if (which == 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_extend, 128, 0);
     else if (which == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_connect, 128, 0);
     else if (which == 2) {
-#if LH2G_SHADE_MINBLOCKS > 4
-        /* more than four CTAs of 32 KB need a shared-memory configuration above 132 KB */
-        cudaFuncSetAttribute(k_shade, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-#endif
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_shade, WAVE_BLOCK, 0);
+        /* the grid the registers allow; the potentials' shared memory grows with the scene's lights, and as the
+         * shading loop is grid-stride, blocks beyond what shared memory lets reside simply start later */
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_shade, WAVE_BLOCK, WAVE_BLOCK * sizeof(float));
     }
     else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_tail, WAVE_BLOCK, 0);
     return sm_count() * (per > 0 ? per : 1);
@@ -426,7 +425,8 @@ void launch_extend(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, i
 }
 void launch_shade(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int blocks, cudaStream_t st) {
     if (B.order) k_partition<<<sm_count() * 4, PART_TILE, 0, st>>>(F, B, depth);
-    k_shade<<<blocks, WAVE_BLOCK, 0, st>>>(S, F, B, depth);
+    const int lights = std::max(1, S.nTri + S.nPoint + S.nSpot + S.nDir);   /* at most 64 (lh2g_set_lights) */
+    k_shade<<<blocks, WAVE_BLOCK, (size_t)lights * WAVE_BLOCK * sizeof(float), st>>>(S, F, B, depth);
 }
 void launch_connect(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int blocks, cudaStream_t st) {
     k_connect<<<blocks, 128, 0, st>>>(S, F, B, depth);
