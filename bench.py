@@ -464,7 +464,7 @@ NRC_FIELD_BOUNDS = ((-100.0, -2.0, -100.0), (100.0, 48.0, 100.0))   # the sphere
 
 
 def nrc_leg(args, core, name, view, bounds, W, H):
-    """Radiance cache against the plain estimator on the core's scene at W x H, judged by a plain render of
+    """Radiance cache against the plain estimator on the core's scene at W x H, measured against a plain render of
     args.nrc_ref_spp samples per pixel accumulated in FP64: RMSE and relative MSE at equal device time (frame counts
     from measured frame times) and at equal sample count, after the cache has trained online for some frames.
     Both estimators run on the same core, scene and camera pose."""

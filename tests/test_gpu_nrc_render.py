@@ -1,4 +1,4 @@
-"""Radiance-cache frames (lh2g_render_nrc) against the plain estimator, both judged by a converged plain render.
+"""Radiance-cache frames (lh2g_render_nrc) against the plain estimator, both measured against a converged plain render.
 
 The plain estimator (1 spp per frame, accumulated) and the cache estimator (paths end into the cache at their first
 diffuse-led vertex from path length 2 on, 1 in 32 trace on and train it online) render the Cornell scene at
