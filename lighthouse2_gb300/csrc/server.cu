@@ -151,11 +151,13 @@ __global__ void __launch_bounds__(128) k_srv_extend(const __grid_constant__ Scen
 
 /* one vertex of every path in the current queue: extension rays to the other queue, connections to the shadow
  * queue (warp ballot + popc, one atomic per warp), finished paths leave their job's live count */
-__global__ void __launch_bounds__(WAVE_BLOCK) k_srv_shade(const __grid_constant__ SceneTable scenes, const JobGPU* __restrict__ jobs,
+/* register cap as the plain core's shading kernel: 6 CTAs per SM, with the light potentials in dynamic shared
+ * memory sized to the largest light count of the resident scenes */
+__global__ void __launch_bounds__(WAVE_BLOCK, 6) k_srv_shade(const __grid_constant__ SceneTable scenes, const JobGPU* __restrict__ jobs,
                                                          ServerState* st, const Queues Q, int* alive) {
     const uint32_t cur = st->cur, nq = cur ^ 1u, count = st->qCount[cur] + st->newTotal;
     const uint32_t lane = threadIdx.x & 31u;
-    __shared__ float potential[64 * WAVE_BLOCK];
+    extern __shared__ float potential[];   /* (largest light count of the scenes) x 128 threads */
     for (uint32_t b0 = blockIdx.x * blockDim.x; b0 < count; b0 += gridDim.x * blockDim.x) {
         const uint32_t j = b0 + threadIdx.x;
         ShadeOut out;
@@ -725,7 +727,9 @@ int build_tick_graph(lh2g_server* s) {
     cudaEventRecord(s->evJoin, s->side);
     k_srv_extend<<<s->blocksExtend, 128, 0, s->st>>>(T, s->dJobs, s->dState, s->Q);
     k_srv_partition<<<s->blocksPart, PART_TILE, 0, s->st>>>(s->dState, s->Q);
-    k_srv_shade<<<s->blocksShade, WAVE_BLOCK, 0, s->st>>>(T, s->dJobs, s->dState, s->Q, s->dAlive);
+    int lights = 1;   /* at most 64 per scene (lh2g_set_lights) */
+    for (int k = 0; k < n; k++) lights = std::max(lights, T.s[k].nTri + T.s[k].nPoint + T.s[k].nSpot + T.s[k].nDir);
+    k_srv_shade<<<s->blocksShade, WAVE_BLOCK, (size_t)lights * WAVE_BLOCK * sizeof(float), s->st>>>(T, s->dJobs, s->dState, s->Q, s->dAlive);
     k_srv_connect<<<s->blocksConnect, 128, 0, s->st>>>(T, s->dJobs, s->dState, s->Q);
     cudaStreamWaitEvent(s->st, s->evJoin, 0);
     k_srv_end<<<1, 1, 0, s->st>>>(s->dState);
