@@ -176,12 +176,13 @@ def run_reference(args):
 
 def algorithmic_bytes(kind, n_in, n_ext, n_shadow):
     """Bytes a stage must move per launch (path-state and queue traffic; scene data counted per access):
-    extend: ray 32 B in + hit 16 B out; shade: path state 48 B + hit 16 B + 5 triangle float4 (80 B) + 2 material
-    float4 (32 B) per path, 48 B per extension ray and per connection written; connect: ray 32 B + contribution 16 B."""
+    extend: ray 32 B in + hit 16 B out; shade: the partition's hit record read (16 B) and order written (4 B), then
+    the order read back (4 B), path state 48 B + hit 16 B + 5 triangle float4 (80 B) + 2 material float4 (32 B) per
+    path, 48 B per extension ray and per connection written; connect: ray 32 B + contribution 16 B."""
     if kind == "extend":
         return n_in * 48
     if kind == "shade":
-        return n_in * (48 + 16 + 80 + 32) + 48 * n_ext + 48 * n_shadow
+        return n_in * (16 + 4 + 4 + 48 + 16 + 80 + 32) + 48 * n_ext + 48 * n_shadow
     return n_in * 48
 
 
