@@ -311,7 +311,7 @@ def svgf_leg(core, W, H, steps, warmup):
             "peak_GBps": peak, "frac": achieved / peak, "peak_source": peak_kind}
 
 
-# serving loop queue capacity in paths when the mix's largest job needs less: 8M paths hold about 1.2 GB of queues
+# serving loop queue capacity in paths when the mix's largest job needs less: 8M paths hold about 1.4 GB of queues (164 B per path)
 # (well inside a 40 GB path-memory budget at 64 B per path) and let ticks carry several small jobs at once
 SERVING_CAPACITY = 1 << 23
 SERVING_MIXES = {
