@@ -39,7 +39,17 @@ __device__ __forceinline__ uint32_t queue_count(const FrameGPU& F, const Counter
 }
 
 /* -------------------------------------------------------------------------------------------------- */
-__global__ void __launch_bounds__(128) k_extend(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int depth) {
+/* tuning switch: resident CTAs per SM the traversal kernels (k_extend, k_connect) are compiled for (register cap);
+ * 0 leaves it to the compiler */
+#ifndef LH2G_TRAV_MINBLOCKS
+#define LH2G_TRAV_MINBLOCKS 0
+#endif
+#if LH2G_TRAV_MINBLOCKS > 0
+#define LH2G_TRAV_BOUNDS __launch_bounds__(128, LH2G_TRAV_MINBLOCKS)
+#else
+#define LH2G_TRAV_BOUNDS __launch_bounds__(128)
+#endif
+__global__ void LH2G_TRAV_BOUNDS k_extend(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int depth) {
     Counters* C = B.counters;
     const uint32_t count = queue_count(F, C, depth);
     const int q = (depth - 1) & 1;
@@ -186,7 +196,7 @@ __global__ void __launch_bounds__(WAVE_BLOCK) k_tail(const SceneGPU S, const Fra
 }
 
 /* -------------------------------------------------------------------------------------------------- */
-__global__ void __launch_bounds__(128) k_connect(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int depth) {
+__global__ void LH2G_TRAV_BOUNDS k_connect(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int depth) {
     Counters* C = B.counters;
     const uint32_t count = C->shadow[depth - 1];
     uint32_t status = 0;
