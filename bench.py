@@ -119,14 +119,18 @@ def frame_params(k, W, H):
     return view, p
 
 
-def cpu_baseline(sc, W, H, seconds, threads):
-    """The oracle on the host cores; one full frame at a time until `seconds` have elapsed."""
+def cpu_baseline(sc, W, H, seconds, threads, core=None, compare=3):
+    """The oracle on the host cores; one full frame at a time until `seconds` have elapsed. With `core`, the first
+    `compare` oracle frames are checked against the GPU core's frames of the same poses (outside any timed region):
+    per path length the extension and connection counts exactly, per-pixel radiance within 1e-4 relative."""
+    import numpy as np
     from oracle import bind
     o = bind.Oracle()
     t0 = time.time()
     o.set_scene(sc)
     build_s = time.time() - t0
     rays, elapsed, frames = 0, 0.0, 0
+    parity = {"frames_compared": 0, "counters_equal": True, "max_rel_radiance": 0.0}
     while frames == 0 or elapsed < seconds:
         view, p = frame_params(frames, W, H)
         t = time.time()
@@ -134,10 +138,28 @@ def cpu_baseline(sc, W, H, seconds, threads):
         elapsed += time.time() - t
         c = r["counters"]
         rays += W * H + int(c[:, 0].sum()) + int(c[:, 1].sum())
+        if core is not None and frames < compare:
+            g = core.render_ex(view, p, counters=True)["counters"]
+            acc = core.read_accumulator()
+            rel = np.abs(acc - r["accum"]) / np.maximum(np.abs(r["accum"]), 1e-6)
+            parity["frames_compared"] += 1
+            parity["counters_equal"] &= bool(np.array_equal(g, c))
+            parity["max_rel_radiance"] = max(parity["max_rel_radiance"], float(rel.max()))
         frames += 1
-    return {"value": rays / elapsed / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
-            "sample": f"{frames} full 1920x1080 1spp frame(s) of the same scene and estimator ({elapsed:.1f} s; oracle BVH build "
-                      f"{build_s:.1f} s not timed)", "ms_per_frame": elapsed / frames * 1e3}
+    out = {"value": rays / elapsed / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+           "sample": f"{frames} full 1920x1080 1spp frame(s) of the same scene and estimator ({elapsed:.1f} s; oracle BVH build "
+                     f"{build_s:.1f} s not timed)", "ms_per_frame": elapsed / frames * 1e3}
+    if core is not None:
+        parity["ok"] = parity["counters_equal"] and parity["max_rel_radiance"] <= 1e-4
+        out["parity_vs_gpu"] = parity
+    return out
+
+
+def bench_config(W, H):
+    """The workload both arms run (the same keys in both lines)."""
+    return {"workload": WORKLOAD, "width": W, "height": H, "spp": 1, "max_depth": MAX_DEPTH, "rr_start_depth": RR_START,
+            "nee": True, "scene_seed": 7, "camera_path": "8 seeded poses, frame k uses pose k % 8",
+            "l2": "inputs larger than L2 (scene ~0.6 GB + path state ~0.36 GB resident), no flush"}
 
 
 def run_reference(args):
@@ -166,7 +188,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": 1, "max_depth": MAX_DEPTH},
+            "config": bench_config(W, H),
             "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
                              "sample": f"{args.steps} full frames after {args.warmup} warm-up frames"},
             "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -205,8 +227,8 @@ def reduce_replicas(dist, ms, units, device):
     return float(t.item()), int(u.item())
 
 
-def ray_query_leg(core, sc, n, cpu):
-    """The ray-query microbenchmark on the large scene's BVH: n incoherent rays (origins uniform in the scene box,
+def ray_query_leg(core, sc, n, cpu, name):
+    """The ray-query microbenchmark on a scene's BVH: n incoherent rays (origins uniform in the scene box,
     directions uniform on the sphere) and n secondary-like rays (origins on area-weighted surface points,
     cosine-weighted directions), tmax ~ U[0.1, scene diagonal], closest hit and any hit. Rays and results stay in
     device memory (lh2g_trace); CUDA events on the core's stream. The CPU oracle traces 2^20 of the same rays."""
@@ -215,7 +237,8 @@ def ray_query_leg(core, sc, n, cpu):
     from lighthouse2_gb300 import scenes as S
     from oracle import bind
     peak, _ = peaks()
-    out = {"workload": f"spheres_2m BVH (2,048,034 triangles, 66 instances), {n} rays per kind, rays and hits resident on the device"}
+    out = {"workload": f"{name} BVH ({sc.triangle_count:,} triangles, {len(sc.instances)} instances), {n} rays per kind, rays and hits "
+                       f"resident on the device"}
     o = None
     if cpu:
         o = bind.Oracle()
@@ -621,7 +644,16 @@ def run_gb300(args):
     last = core.read_framebuffer()
     assert np.array_equal(hosts[(args.steps - 1) % 2].numpy(), last), "the last copied frame differs from the device frame"
     e2e_value = e2e_rays * world / t_e2e / 1e6
-    rq = ray_query_leg(core, sc, args.rays, world == 1 and not args.no_cpu_baseline) if (not args.no_rays and rank == 0) else None
+    rq = None
+    if not args.no_rays and rank == 0:
+        # the large scene's BVH (most incoherent and secondary-like rays leave the open sphere field) and the small
+        # scene's (a room: most rays hit)
+        rq = {"spheres_2m": ray_query_leg(core, sc, args.rays, world == 1 and not args.no_cpu_baseline, "spheres_2m")}
+        cb = S.cornell_sphere(subdiv=6)
+        core_c = RenderCore(local)
+        core_c.set_scene(cb)
+        rq["cornell"] = ray_query_leg(core_c, cb, args.rays, world == 1 and not args.no_cpu_baseline, "cornell 82k")
+        core_c.close()
     svgf = svgf_leg(core, W, H, max(args.steps, 8), args.warmup) if not args.no_svgf else None
     serving = serving_leg(args) if (not args.no_serving and rank == 0) else None
     nrc = None
@@ -659,9 +691,8 @@ def run_gb300(args):
     line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": 1, "max_depth": MAX_DEPTH, "rr_start_depth": RR_START,
-                       "wave_tail": args.wave_tail, "frames_in_flight": args.lanes,
-                       "l2": "inputs larger than L2 (scene ~0.6 GB + path state ~0.36 GB resident), no flush",
+            "config": bench_config(W, H),
+            "details": {"wave_tail": args.wave_tail, "frames_in_flight": args.lanes,
                        "bvh_build_ms": round(build_ms, 2), "scene_generation_s": round(gen_s, 1),
                        "rays_per_frame": rays / args.steps / world,
                        "kernel_ms_per_frame": {k: round(v[0] / args.steps, 4) for k, v in per_kind.items()},
@@ -691,7 +722,7 @@ def run_gb300(args):
     if nrc is not None:
         line["radiance_cache"] = nrc
     if world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(sc, W, H, args.cpu_seconds, os.cpu_count() or 1)
+        line["cpu_baseline"] = cpu_baseline(sc, W, H, args.cpu_seconds, os.cpu_count() or 1, core=core)
     print(json.dumps(line, default=float), flush=True)
     core.close()
     return 0

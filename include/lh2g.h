@@ -150,12 +150,15 @@ LH2G_API int lh2g_trace_host(lh2g_context* ctx, const lh2g_ray* rays, void* out,
  * the frame's per-pixel sums to accumDevice (caller-owned device memory, width*height float4).
  * Limit: width * height * spp <= LH2G_NOALLOC_MAX_PATHS, else LH2G_ERR_OVERFLOW. The scene comes from ctx,
  * which must be finalized; no render target is needed. stream may be NULL (legacy default stream). The first
- * call on a device looks up the array's device address (cudaGetSymbolAddress); make that first call before
- * any stream capture. All calls share the array and it keeps the last call's contents: calls whose GPU work
- * overlaps (other streams, threads or contexts on the same device) race. */
+ * call on a device (and the first in any other CUDA context on it, e.g. after cudaDeviceReset) looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call before any stream capture. All calls share
+ * the array and it keeps the last call's contents: calls whose GPU work overlaps (other streams, threads or
+ * contexts on the same device) race. statusHost (may be NULL) receives the frame's LH2G_STATUS_* word (traversal
+ * stack overflow or step limit: the frame is then incomplete), copied on the stream: read it after the stream has
+ * completed (pinned memory) or on return (pageable memory, which makes the copy synchronous). */
 #define LH2G_NOALLOC_MAX_PATHS 32768
 LH2G_API int lh2g_render_noalloc(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* params, float* accumDevice,
-                                 void* stream);
+                                 void* stream, uint32_t* statusHost);
 
 /* ---- serving loop (no counterpart in the reference, whose cores render one frame at a time) ----
  * Render and ray-query jobs of several resident scenes, continuously batched: jobs are admitted smallest first

@@ -33,9 +33,9 @@ def nvcc():
     raise FileNotFoundError("nvcc not found")
 
 
-def _flags():
+def _flags(defines=()):
     extra = os.environ.get("LH2G_NVCC_FLAGS", "").split()   # e.g. traversal strategy: -DLH2G_COOP=1 -DLH2G_REFILL=1
-    return ARCH + extra + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
+    return ARCH + extra + list(defines) + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
                    "-Xcompiler", "-fPIC,-O2,-fvisibility=hidden,-ffp-contract=off", "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 
 
@@ -46,8 +46,12 @@ def _stale(obj, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose=False, force=False):
-    os.makedirs(OUT, exist_ok=True)
+def build(verbose=False, force=False, out_dir=None, defines=()):
+    """Compiles the library into out_dir (default lighthouse2_gb300/_build); `defines` are extra nvcc flags of a
+    variant build (e.g. ["-DLH2G_STACK=12"] into its own directory), whose objects never mix with the default's."""
+    out = out_dir or OUT
+    lib = os.path.join(out, LIB_NAME)
+    os.makedirs(out, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers += [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
     cc = nvcc()
@@ -55,10 +59,10 @@ def build(verbose=False, force=False):
     objs = []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(OUT, src + ".o")
+        o = os.path.join(out, src + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([cc] + _flags() + ["-c", s, "-o", o])
+            jobs.append([cc] + _flags(defines) + ["-c", s, "-o", o])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         results = list(ex.map(lambda cmd: subprocess.run(cmd, capture_output=True, text=True), jobs))
     for cmd, r in zip(jobs, results):
@@ -66,14 +70,14 @@ def build(verbose=False, force=False):
             sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
         if r.returncode:
             raise RuntimeError("nvcc failed for " + cmd[-3])
-    if force or jobs or not os.path.exists(LIB):
-        link = [cc] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-Xlinker", "--exclude-libs,ALL"]
+    if force or jobs or not os.path.exists(lib):
+        link = [cc] + ARCH + ["-shared", "-o", lib + ".tmp"] + objs + ["-Xlinker", "--exclude-libs,ALL"]
         r = subprocess.run(link, capture_output=True, text=True)
         if r.returncode:
             sys.stderr.write(" ".join(link) + "\n" + r.stdout + r.stderr)
             raise RuntimeError("link failed")
-        os.replace(LIB + ".tmp", LIB)
-    return LIB
+        os.replace(lib + ".tmp", lib)
+    return lib
 
 
 HARNESS = os.path.join(OUT, "headless_app")

@@ -97,7 +97,7 @@ def load_library(path: str | None = None):
     lib.lh2g_enable_launch_timing.argtypes = [vp, i]
     lib.lh2g_get_launch_times.argtypes = [vp, vp, i, C.POINTER(i)]
     lib.lh2g_get_traversal_stats.argtypes = [vp, vp]
-    lib.lh2g_render_noalloc.argtypes = [vp, vp, vp, vp, vp]
+    lib.lh2g_render_noalloc.argtypes = [vp, vp, vp, vp, vp, vp]
     lib.lh2g_filter.argtypes = [vp, vp]
     lib.lh2g_read_filter_buffer.argtypes = [vp, i, vp]
     lib.lh2g_get_last_filter_frame.argtypes = [vp, vp, vp, vp]

@@ -12,9 +12,16 @@
  * process exits. All calls share it and it keeps the last call's contents; the queue counters are cleared at the
  * start of every call and every other buffer is written before it is read. Calls whose work overlaps on the GPU
  * (two streams, two threads, two contexts on one device) race on the array.
+ *
+ * The array's device address belongs to the CUDA context that loaded the module: it is looked up per device
+ * and cached together with the unique id of the context current at the time (cuCtxGetId). A call from another
+ * context on the device, or after cudaDeviceReset ended the old one, sees a different id and looks the address up
+ * again instead of using a stale one.
  */
 #include <algorithm>
 #include <mutex>
+
+#include <cuda.h>
 
 #include "kernels.cuh"
 #include "lh2g.h"
@@ -29,6 +36,31 @@ __device__ __align__(256) unsigned char g_noalloc_scratch[(size_t)LH2G_NOALLOC_M
 
 std::mutex g_setup_mutex;
 unsigned char* g_scratch_addr[MAX_DEVICES] = {nullptr};
+unsigned long long g_scratch_ctx[MAX_DEVICES] = {0};   /* cuCtxGetId of the context the address belongs to */
+
+/* unique id of the current context (0 when it cannot be had), through the runtime's driver entry points so that
+ * the library needs no link against the driver library */
+unsigned long long current_context_id() {
+    typedef CUresult (*GetCurrent)(CUcontext*);
+    typedef CUresult (*GetId)(CUcontext, unsigned long long*);
+    static GetCurrent getCurrent = nullptr;
+    static GetId getId = nullptr;
+    static bool looked = false;
+    if (!looked) {
+        void* a = nullptr;
+        void* b = nullptr;
+        cudaDriverEntryPointQueryResult qa, qb;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) == cudaSuccess && qa == cudaDriverEntryPointSuccess)
+            getCurrent = (GetCurrent)a;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) == cudaSuccess && qb == cudaDriverEntryPointSuccess)
+            getId = (GetId)b;
+        looked = true;
+    }
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (!getCurrent || !getId || getCurrent(&c) != CUDA_SUCCESS || !c || getId(c, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
 
 }  // namespace
 
@@ -38,7 +70,7 @@ int context_scene(lh2g_context* ctx, SceneGPU* scene, int* device, int* blocks4,
 }
 
 extern "C" LH2G_API int lh2g_render_noalloc(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* p, float* accumDevice,
-                                             void* stream) {
+                                             void* stream, uint32_t* statusHost) {
     using namespace lh2g;
     if (!ctx || !view || !p || !accumDevice) return LH2G_ERR_INVALID;
     if (p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->maxDepth < 1 || p->maxDepth > 64) return LH2G_ERR_INVALID;
@@ -58,18 +90,20 @@ extern "C" LH2G_API int lh2g_render_noalloc(lh2g_context* ctx, const lh2g_view* 
         /* once per device, with that device current: the device address of the array (in host code its name
          * only stands for it) */
         std::lock_guard<std::mutex> lock(g_setup_mutex);
-        if (!g_scratch_addr[device]) {
+        const unsigned long long cid = current_context_id();
+        if (!g_scratch_addr[device] || cid == 0 || cid != g_scratch_ctx[device]) {
             void* a = nullptr;
             if (cudaGetSymbolAddress(&a, g_noalloc_scratch) != cudaSuccess || !a) {
                 if (current != device) cudaSetDevice(current);
                 return LH2G_ERR_CUDA;
             }
             g_scratch_addr[device] = (unsigned char*)a;
+            g_scratch_ctx[device] = cid;
         }
         base = g_scratch_addr[device];
     }
     cudaStream_t st = (cudaStream_t)stream;
-    WaveBuffers B;
+    WaveBuffers B{};   /* every buffer not set below is null */
     float4* f = (float4*)base;
     const size_t n = (size_t)LH2G_NOALLOC_MAX_PATHS;
     B.O[0] = f, B.D[0] = f + n, B.T[0] = f + 2 * n, B.O[1] = f + 3 * n, B.D[1] = f + 4 * n, B.T[1] = f + 5 * n;
@@ -102,7 +136,10 @@ extern "C" LH2G_API int lh2g_render_noalloc(lh2g_context* ctx, const lh2g_view* 
     }
     if (waves < F.maxDepth) launch_tail(S, F, B, waves + 1, blocks[3], st);
     launch_finalize(F, B, 1.0f / (float)(p->samplesTaken + F.spp), 0, st);
-    const cudaError_t e = cudaGetLastError();
+    /* the status word (LH2G_STATUS_* bits: traversal stack overflow, step limit) to the caller, on the stream */
+    cudaError_t e = statusHost ? cudaMemcpyAsync(statusHost, &B.counters->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st) : cudaSuccess;
+    const cudaError_t le = cudaGetLastError();
+    if (e == cudaSuccess) e = le;
     if (current != device) cudaSetDevice(current);
     return e == cudaSuccess ? LH2G_OK : LH2G_ERR_CUDA;
 }

@@ -318,11 +318,16 @@ struct Traversal {
             if (!leaf<ANYHIT>(S, entry, anyHitDone)) return false;
         } else {
             const uint32_t first = entry & 0x0fffffffu, cnt = ((entry >> 28) & 3u) + 1u;
-            if (cnt > 1u && sp < LH2G_STACK) stack[sp++] = make_uint2(0x80000000u | ((cnt - 2u) << 28) | (first + 1u), 0u);
+            /* a full stack drops work: the status word says so (the hit record may then be wrong) */
+            if (cnt > 1u) {
+                if (sp < LH2G_STACK) stack[sp++] = make_uint2(0x80000000u | ((cnt - 2u) << 28) | (first + 1u), 0u);
+                else status |= LH2G_STATUS_STACK_OVERFLOW;
+            }
             const int ii = (int)__ldg(S.tlasPrims + first);
             /* an InstanceGPU is four aligned float4: the three rows of the inverse transform, then blasRoot */
             const float4* in = reinterpret_cast<const float4*>(S.inst + ii);
             const uint32_t root = __float_as_uint(__ldg(in + 3).x);
+            if (root != 0xffffffffu && sp >= LH2G_STACK) status |= LH2G_STATUS_STACK_OVERFLOW;
             if (root != 0xffffffffu && sp < LH2G_STACK) {
                 const float4 r0 = __ldg(in), r1 = __ldg(in + 1), r2 = __ldg(in + 2);
                 const float m[12] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w};
@@ -456,10 +461,13 @@ LH2G_DEV bool coop_step(const SceneGPU& S, CoopRay& r, uint2* stk, const int g, 
             if (g == 0) stk[r.sp] = make_uint2(0x80000000u | ((cnt - 2u) << 28) | (first + 1u), 0u);
             __syncwarp(gmask);
             r.sp++;
+        } else if (cnt > 1u) {
+            status |= LH2G_STATUS_STACK_OVERFLOW;
         }
         const int ii = (int)__ldg(S.tlasPrims + first);
         const InstanceGPU* in = S.inst + ii;
         const uint32_t root = __ldg(&in->blasRoot);
+        if (root != 0xffffffffu && r.sp >= COOP_STACK) status |= LH2G_STATUS_STACK_OVERFLOW;
         if (root != 0xffffffffu && r.sp < COOP_STACK) {
             float m[12];
 #pragma unroll

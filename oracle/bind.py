@@ -15,7 +15,9 @@ from lighthouse2_gb300 import scenes as S
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liblh2o.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref.so")
-REFERENCE_TREE = os.environ.get("LH2_REFERENCE", "/root/reference")
+# the Lighthouse 2 source tree, named by the caller (environment variable LH2_REFERENCE); without it the
+# reference-kernel harness is not built and the tests that need it are skipped
+REFERENCE_TREE = os.environ.get("LH2_REFERENCE", "")
 
 PARAMS_DTYPE = np.dtype([("width", "<i4"), ("height", "<i4"), ("spp", "<i4"), ("maxDepth", "<i4"),
                          ("rrStartDepth", "<i4"), ("samplesTaken", "<i4"), ("cameraR0", "<u4"),
@@ -33,7 +35,7 @@ def build_oracle():
 
 def build_ref():
     """Compile the reference's own kernels for the host (only where the reference tree exists)."""
-    if not os.path.isdir(os.path.join(REFERENCE_TREE, "lib", "RenderCore_PrimeRef")):
+    if not REFERENCE_TREE or not os.path.isdir(os.path.join(REFERENCE_TREE, "lib", "RenderCore_PrimeRef")):
         return None
     build_oracle()
     subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), "REF=" + REFERENCE_TREE], check=True)

@@ -7,8 +7,9 @@ import pytest
 
 from lighthouse2_gb300 import scenes as S
 
-REF = os.environ.get("LH2_REFERENCE", "/root/reference")
-pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "lib", "RenderCore_PrimeRef")), reason="reference tree not mounted")
+REF = os.environ.get("LH2_REFERENCE", "")   # the Lighthouse 2 source tree, named by the caller
+pytestmark = pytest.mark.skipif(not REF or not os.path.isdir(os.path.join(REF, "lib", "RenderCore_PrimeRef")),
+                                reason="reference tree not given (LH2_REFERENCE)")
 
 
 @pytest.fixture(scope="module")

@@ -33,20 +33,22 @@ def test_render_noalloc_matches_render_ex(core_lib):
     assert expected[:, :3].sum() > 0
 
     fn = core.lib.lh2g_render_noalloc
-    fn.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    fn.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     fn.restype = C.c_int
     acc = torch.zeros((W * H, 4), dtype=torch.float32, device="cuda:0")
+    status = np.full(1, 0xDEAD, np.uint32)
     for call in range(2):                        # two calls in a row share (and must reset) the static scratch
         acc.zero_()
         torch.cuda.synchronize()
-        rc = fn(core.ctx, view.ctypes.data, p.ctypes.data, acc.data_ptr(), None)
+        rc = fn(core.ctx, view.ctypes.data, p.ctypes.data, acc.data_ptr(), None, status.ctypes.data)
         assert rc == 0, f"call {call}: status {rc}"
         torch.cuda.synchronize()
+        assert status[0] == 0, f"call {call}: device status {status[0]}"
         got = acc.cpu().numpy()
         rel = np.abs(got - expected) / np.maximum(np.abs(expected), 1e-6)
         assert rel.max() <= 1e-4, f"call {call}: max relative difference {rel.max()}"
 
     big = make_params(256, 256, 1, max_depth=3, camera_r0=camera_r0(0), flags=RP_NEE)
-    assert fn(core.ctx, view.ctypes.data, big.ctypes.data, acc.data_ptr(), None) == LH2G_ERR_OVERFLOW
-    assert fn(core.ctx, view.ctypes.data, p.ctypes.data, None, None) == LH2G_ERR_INVALID
+    assert fn(core.ctx, view.ctypes.data, big.ctypes.data, acc.data_ptr(), None, None) == LH2G_ERR_OVERFLOW
+    assert fn(core.ctx, view.ctypes.data, p.ctypes.data, None, None, None) == LH2G_ERR_INVALID
     core.close()
