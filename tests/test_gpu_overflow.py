@@ -1,7 +1,8 @@
 """Traversal that runs out of stack reports it.
 
-A variant of the core built with a 12-entry traversal stack (-DLH2G_STACK=12, in its own build directory) cannot
-hold the pending children of a two-level traversal through 66 instances, so it drops work; every place where a
+A variant of the core built with a 3-entry traversal stack (-DLH2G_STACK=3, in its own build directory) cannot
+hold the pending children of a two-level traversal through 66 instances (a node a ray crosses often has four or more
+hit children, and entering an instance takes a slot for the return marker), so it drops work; every place where a
 push is refused (sorted children, an instance leaf's remaining instances, the entry into an instance) sets the
 stack-overflow bit of the status word, and the C ABI turns the word into LH2G_ERR_OVERFLOW. No call may return
 a truncated traversal as a success. The default build traces the same rays without an error."""
@@ -18,7 +19,7 @@ pytestmark = pytest.mark.gpu
 @pytest.fixture(scope="module")
 def small_stack_lib(core_lib):
     from lighthouse2_gb300 import build
-    return build.build(out_dir=os.path.join(build.OUT, "stack12"), defines=["-DLH2G_STACK=12"])
+    return build.build(out_dir=os.path.join(build.OUT, "stack3"), defines=["-DLH2G_STACK=3"])
 
 
 @pytest.fixture(scope="module")
@@ -30,16 +31,16 @@ def test_small_stack_reports_overflow(small_stack_lib, scene):
     from lighthouse2_gb300.core import RenderCore, CoreError, make_params, camera_r0, RP_NEE
     core = RenderCore(0, lib_path=small_stack_lib)
     core.set_scene(scene)
-    rays = S.random_rays(scene, 100_000, seed=3, kind="incoherent")
-    for mode in (0, 1):
-        with pytest.raises(CoreError, match="overflow"):
-            core.trace_host(rays, mode=mode)
     W, H = 64, 48
     core.SetTarget(W, H, 1)
     p = make_params(W, H, 1, max_depth=4, camera_r0=camera_r0(0), flags=RP_NEE)
     with pytest.raises(CoreError, match="overflow"):
         core.render_ex(S.spheres_view(W, H), p, counters=True)
     assert core.GetCoreStats()["deviceStatus"] & 1
+    rays = S.random_rays(scene, 100_000, seed=3, kind="secondary")
+    for mode in (0, 1):
+        with pytest.raises(CoreError, match="overflow"):
+            core.trace_host(rays, mode=mode)
     core.close()
 
 
@@ -47,7 +48,7 @@ def test_default_stack_traces_the_same_rays(core_lib, scene, oracle_lib):
     from lighthouse2_gb300.core import RenderCore
     core = RenderCore(0)
     core.set_scene(scene)
-    rays = S.random_rays(scene, 100_000, seed=3, kind="incoherent")
+    rays = S.random_rays(scene, 100_000, seed=3, kind="secondary")
     g = core.trace_host(rays, mode=0)
     o = oracle_lib.Oracle()
     o.set_scene(scene)
