@@ -22,6 +22,19 @@ def small_stack_lib(core_lib):
     return build.build(out_dir=os.path.join(build.OUT, "stack3"), defines=["-DLH2G_STACK=3"])
 
 
+def _field_rays(scene, n, seed=3):
+    """Rays from the camera position towards random points among the spheres: every one crosses the field."""
+    rng = np.random.default_rng(seed)
+    view = S.spheres_view(64, 48)
+    rays = np.zeros(n, S.RAY_DTYPE)
+    rays["o"] = view["pos"]
+    target = rng.uniform((-40.0, 0.0, -40.0), (40.0, 8.0, 40.0), (n, 3))
+    d = target - view["pos"].astype(np.float64)
+    rays["d"] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    rays["tmin"], rays["tmax"] = 0.0, 1e30
+    return rays
+
+
 @pytest.fixture(scope="module")
 def scene():
     return S.spheres_2m(slices=24, stacks=16, tex_size=32)
@@ -37,7 +50,7 @@ def test_small_stack_reports_overflow(small_stack_lib, scene):
     with pytest.raises(CoreError, match="overflow"):
         core.render_ex(S.spheres_view(W, H), p, counters=True)
     assert core.GetCoreStats()["deviceStatus"] & 1
-    rays = S.random_rays(scene, 100_000, seed=3, kind="secondary")
+    rays = _field_rays(scene, 100_000)
     for mode in (0, 1):
         with pytest.raises(CoreError, match="overflow"):
             core.trace_host(rays, mode=mode)
@@ -48,7 +61,7 @@ def test_default_stack_traces_the_same_rays(core_lib, scene, oracle_lib):
     from lighthouse2_gb300.core import RenderCore
     core = RenderCore(0)
     core.set_scene(scene)
-    rays = S.random_rays(scene, 100_000, seed=3, kind="secondary")
+    rays = _field_rays(scene, 100_000)
     g = core.trace_host(rays, mode=0)
     o = oracle_lib.Oracle()
     o.set_scene(scene)
