@@ -48,7 +48,7 @@ EXTEND_CAPTURE = {"pose": 1, "waves": (2, 3), "dram_bytes": 196.84736e6 + 74.086
 WORKLOAD = "spheres_2m: 64 x 32k-tri displaced spheres + ground (2,048,002 tris, 66 instances), 16 quad + 4 point lights, " \
            "20 materials (4 textured), sky; 1920x1080 1spp, max depth 8, RR after depth 3, NEE"
 METRIC = "Mrays/s @1080p 1spp"
-VIEW_BYTES, PARAMS_BYTES = 68, 44     # lh2g_view and lh2g_render_params copied host -> device per frame
+VIEW_BYTES, PARAMS_BYTES = 68, 48     # lh2g_view and lh2g_render_params copied host -> device per frame
 
 
 def peaks():

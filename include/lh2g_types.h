@@ -129,7 +129,9 @@ typedef struct lh2g_render_params {
     float geometryEpsilon;                  /* ray offset / tmin, 'epsilon' setting (rendersystem.h:67) */
     float clampValue;                       /* 'clampValue' setting (kept for the settings interface) */
     int32_t flags;                          /* LH2G_RP_* */
-    uint32_t frameSeed;                     /* LH2G_RP_FILTER only: shading R0 = frameSeed + pathLength * 91771 */
+    uint32_t frameSeed;                     /* LH2G_RP_FILTER: shading R0 = frameSeed + pathLength * 91771;
+                                             * adaptive frames: R0 of the second wave's primary rays */
+    uint32_t shift;                         /* LH2G_RP_OPTIX7 / adaptive frames: blue-noise tile shift (shiftSeed) */
 } lh2g_render_params;
 
 #define LH2G_RP_NEE        1                /* next-event estimation (connections buffer present) */
@@ -143,6 +145,18 @@ typedef struct lh2g_render_params {
 /* Radiance-cache frame (lh2g_render_nrc): a path that reaches its second vertex through a diffuse bounce records
  * a cache query there; 15 of 16 such paths end and receive throughput x cache, the others trace on and train it. */
 #define LH2G_RP_NRC        8
+/* The OptiX 7 core's estimator (lib/rendercore_optix7/kernels/pathtracer.h:54-238 with the ray generation of
+ * optix/.optix.cu:85-129): primary rays seeded WangHash(pathIdx * 16789 + pass * 1791) through RayTarget, blue-noise
+ * samples (blueNoiseSampler4, tools_shared.h:324-337) for sample indices below 64 when tables are set
+ * (lh2g_set_blue_noise), MIS weights on emissive hits and on light connections (lights_shared.h:111-190), path
+ * regularisation after the first diffuse bounce, paths capped at their second diffuse vertex, intensity clamp
+ * ('clampValue'), NaN suppression, the small sky after a bounce, connections traced with tmin = epsilon and counted
+ * in accumulator.w. cameraR0 is the frame's first draw of RandomUInt(camRNGseed): wave d shades with the d-th draw
+ * + d * 91771 (rendercore.cpp:900). Radiance per path: the terminal sky or emitter term, then the connections. */
+#define LH2G_RP_OPTIX7     16
+/* Set by lh2g_render_adaptive (not by callers): the PrimeAdaptive core's shading (the OptiX 7 estimator with
+ * per-sample accumulators, a sample count in w and albedo/normal features for the variance estimate). */
+#define LH2G_RP_ADAPTIVE   32
 
 /* One SVGF pass over the accumulator of a LH2G_RP_FILTER frame (lib/RenderCore_Optix7Filter/rendercore.cpp:
  * 897-935 with the kernels of lib/CUDA/shared_kernel_code/finalize_shared.h:169-600). */

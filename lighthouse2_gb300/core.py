@@ -19,7 +19,8 @@ LIB_PATH = os.path.join(HERE, "_build", "libRenderCore_GB300.so")
 
 PARAMS_DTYPE = np.dtype([("width", "<i4"), ("height", "<i4"), ("spp", "<i4"), ("maxDepth", "<i4"),
                          ("rrStartDepth", "<i4"), ("samplesTaken", "<i4"), ("cameraR0", "<u4"),
-                         ("geometryEpsilon", "<f4"), ("clampValue", "<f4"), ("flags", "<i4"), ("frameSeed", "<u4")])
+                         ("geometryEpsilon", "<f4"), ("clampValue", "<f4"), ("flags", "<i4"), ("frameSeed", "<u4"),
+                         ("shift", "<u4")])
 FILTER_PARAMS_DTYPE = np.dtype([("prevView", S.VIEW_DTYPE), ("j0", "<f4"), ("j1", "<f4"), ("prevj0", "<f4"), ("prevj1", "<f4"),
                                 ("clampDirect", "<f4"), ("clampIndirect", "<f4"), ("samplesTaken", "<i4"),
                                 ("camIsStationary", "<i4"), ("taa", "<i4")])
@@ -33,7 +34,7 @@ STATS_FIELDS = ["totalRays", "totalExtensionRays", "totalShadowRays", "primaryRa
 STATS_DTYPE = np.dtype([(f, "<u4") for f in STATS_FIELDS[:6]] + [(f, "<f4") for f in STATS_FIELDS[6:14]] +
                        [(f, "<u4") for f in STATS_FIELDS[14:18]] + [("probedInstid", "<i4"), ("probedTriid", "<i4"),
                                                                     ("probedDist", "<f4"), ("deviceStatus", "<u4")])
-RP_NEE, RP_DEPTH_W, RP_FILTER = 1, 2, 4
+RP_NEE, RP_DEPTH_W, RP_FILTER, RP_OPTIX7, RP_ADAPTIVE = 1, 2, 4, 16, 32
 # filter buffer slots (LH2G_FB_*): name -> (index, element dtype, components per pixel)
 FILTER_SLOTS = {"features": (0, np.uint32, 4), "worldPos": (1, np.float32, 4), "prevWorldPos": (2, np.float32, 4),
                 "deltaDepth": (3, np.float32, 4), "motion": (4, np.float32, 2), "moments": (5, np.float32, 4),
@@ -125,11 +126,12 @@ def texture_descs(textures):
 
 
 def make_params(width, height, spp=1, max_depth=3, rr_start=1, samples_taken=0, camera_r0=0, eps=1e-3, clamp=10.0, flags=RP_NEE,
-                frame_seed=0):
+                frame_seed=0, shift=0):
     p = np.zeros((), PARAMS_DTYPE)
     p["width"], p["height"], p["spp"], p["maxDepth"] = width, height, spp, max_depth
     p["rrStartDepth"], p["samplesTaken"], p["cameraR0"] = rr_start, samples_taken, camera_r0
     p["geometryEpsilon"], p["clampValue"], p["flags"], p["frameSeed"] = eps, clamp, flags, frame_seed
+    p["shift"] = shift
     return p
 
 

@@ -93,6 +93,7 @@ class Scene:
     dir_lights: np.ndarray = None
     sky: tuple | None = None                           # (rgb float32 (h*w*3), w, h)
     bounds: tuple = None                               # (min3, max3) world bounds
+    blue_noise: tuple | None = None                    # (sobol 65536, scrambling 131072, ranking 131072) uint8 tables
 
     @property
     def triangle_count(self):
@@ -520,3 +521,12 @@ def random_rays(scene, n, seed, kind="incoherent"):
     rays["tmin"] = 0.0
     rays["tmax"] = rng.uniform(0.1, diag, n)
     return rays
+
+
+def synthetic_blue_noise(seed=5):
+    """Blue-noise tables in the layout of the OptiX 7 core's (a 256 x 256 Sobol table of 8-bit values and two
+    128 x 128 x 8 tiles of scrambling and ranking keys), filled with seeded uniform bytes. The sampler maps any such
+    bytes to numbers in (0, 1); the reference's published tables are the user's to upload."""
+    rng = np.random.default_rng(seed)
+    return (rng.integers(0, 256, 65536, dtype=np.uint8), rng.integers(0, 256, 131072, dtype=np.uint8),
+            rng.integers(0, 256, 131072, dtype=np.uint8))

@@ -21,11 +21,12 @@ REFERENCE_TREE = os.environ.get("LH2_REFERENCE", "")
 
 PARAMS_DTYPE = np.dtype([("width", "<i4"), ("height", "<i4"), ("spp", "<i4"), ("maxDepth", "<i4"),
                          ("rrStartDepth", "<i4"), ("samplesTaken", "<i4"), ("cameraR0", "<u4"),
-                         ("geometryEpsilon", "<f4"), ("clampValue", "<f4"), ("flags", "<i4"), ("frameSeed", "<u4")])
+                         ("geometryEpsilon", "<f4"), ("clampValue", "<f4"), ("flags", "<i4"), ("frameSeed", "<u4"),
+                         ("shift", "<u4")])
 FILTER_PARAMS_DTYPE = np.dtype([("prevView", S.VIEW_DTYPE), ("j0", "<f4"), ("j1", "<f4"), ("prevj0", "<f4"), ("prevj1", "<f4"),
                                 ("clampDirect", "<f4"), ("clampIndirect", "<f4"), ("samplesTaken", "<i4"),
                                 ("camIsStationary", "<i4"), ("taa", "<i4")])
-RP_NEE, RP_DEPTH_W, RP_FILTER = 1, 2, 4
+RP_NEE, RP_DEPTH_W, RP_FILTER, RP_OPTIX7, RP_ADAPTIVE = 1, 2, 4, 16, 32
 
 
 def build_oracle():
@@ -43,11 +44,12 @@ def build_ref():
 
 
 def make_params(width, height, spp=1, max_depth=3, rr_start=1, samples_taken=0, camera_r0=0, eps=1e-3,
-                clamp=10.0, flags=RP_NEE, frame_seed=0):
+                clamp=10.0, flags=RP_NEE, frame_seed=0, shift=0):
     p = np.zeros((), PARAMS_DTYPE)
     p["width"], p["height"], p["spp"], p["maxDepth"] = width, height, spp, max_depth
     p["rrStartDepth"], p["samplesTaken"], p["cameraR0"] = rr_start, samples_taken, camera_r0
     p["geometryEpsilon"], p["clampValue"], p["flags"], p["frameSeed"] = eps, clamp, flags, frame_seed
+    p["shift"] = shift
     return p
 
 
@@ -89,6 +91,8 @@ class Oracle:
         L.lh2o_render.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         L.lh2o_render_ex.argtypes = [C.c_void_p] * 8 + [C.c_int]
         L.lh2o_svgf_frame.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        L.lh2o_set_blue_noise.argtypes = [C.c_void_p] * 4
+        L.lh2o_render_adaptive.argtypes = [C.c_void_p] * 12 + [C.c_int]
         self.s = L.lh2o_create()
         self._keep = []
 
@@ -115,7 +119,41 @@ class Oracle:
             rgb, w, h = sc.sky
             rgb = np.ascontiguousarray(rgb, np.float32)
             assert L.lh2o_set_sky(s, _p(rgb), w, h, None) == 0
+        self.set_blue_noise(sc.blue_noise)
         assert L.lh2o_finalize(s) == 0
+
+    def set_blue_noise(self, tables):
+        if tables is None:
+            assert self.lib.lh2o_set_blue_noise(self.s, None, None, None) == 0
+            return
+        t = [np.ascontiguousarray(x, np.uint8) for x in tables]
+        assert [len(x) for x in t] == [65536, 131072, 131072]
+        assert self.lib.lh2o_set_blue_noise(self.s, _p(t[0]), _p(t[1]), _p(t[2])) == 0
+
+    def render_adaptive(self, view, params, accum, dev_scale, capture=False, nthreads=0):
+        """One PrimeAdaptive frame; accum (W*H float4) is updated in place. Returns the new devScale, the frame,
+        per-wave counters, the second wave's path count and the intermediate buffers."""
+        W, H, spp, D = int(params["width"]), int(params["height"]), int(params["spp"]), int(params["maxDepth"])
+        P = W * H * spp
+        frame = np.zeros((W * H, 4), np.float32)
+        ds = np.array([dev_scale], np.float32)
+        counters = np.zeros((2 * D, 2), np.uint32)
+        n2 = np.zeros(1, np.uint32)
+        facc = np.zeros((P, 4), np.float32)
+        feat = np.zeros((P, 4), np.float32)
+        dev = np.zeros(W * H, np.float32)
+        cap = hits = seeds = None
+        if capture:
+            hits = np.zeros(D * P, S.HIT_DTYPE)
+            seeds = np.zeros(D * P, np.uint32)
+            cap = _Capture(hits.ctypes.data, seeds.ctypes.data)
+        assert self.lib.lh2o_render_adaptive(self.s, _p(view), _p(params), _p(accum), _p(frame), _p(ds), _p(counters), _p(n2), _p(facc),
+                                             _p(feat), _p(dev), C.byref(cap) if cap is not None else None, nthreads) == 0
+        out = {"dev_scale": float(ds[0]), "frame": frame, "counters": counters, "adaptive_paths": int(n2[0]), "frame_acc": facc,
+               "features": feat, "deviation": dev}
+        if capture:
+            out["hits"], out["seeds"] = hits.reshape(D, -1), seeds.reshape(D, -1)
+        return out
 
     def trace(self, rays, mode=0, brute=False, nthreads=0):
         n = len(rays)
@@ -373,6 +411,285 @@ class RefKernels:
             if count == 0:
                 break
         return {"accum": acc, "counters": counters}
+
+
+def _xorshift(x):
+    x ^= (x << 13) & 0xFFFFFFFF
+    x ^= x >> 17
+    x ^= (x << 5) & 0xFFFFFFFF
+    return x
+
+
+def _sky_with_small(sc):
+    """sky float4 pixels followed by the 64x scaled-down copy (RenderCore::SetSkyData, rendercore_optix7/
+    rendercore.cpp:726-737): each tile summed in float32, row by row, then scaled by 1/4096"""
+    if sc.sky is None:
+        return None, 0, 0
+    rgb, w, h = sc.sky
+    px = np.asarray(rgb, np.float32).reshape(h, w, 3)
+    sw, sh = w >> 6, h >> 6
+    small = np.zeros((sh * sw, 4), np.float32)
+    for y in range(sh):
+        for x in range(sw):
+            tile = px[y * 64:(y + 1) * 64, x * 64:(x + 1) * 64].reshape(-1, 3)
+            small[x + y * sw, :3] = np.add.accumulate(tile, axis=0, dtype=np.float32)[-1] * np.float32(1.0 / 4096)
+    sky4 = np.zeros((w * h + sw * sh, 4), np.float32)
+    sky4[:w * h, :3] = px.reshape(-1, 3)
+    sky4[w * h:] = small
+    return sky4, w, h
+
+
+def _ref_scene(lib, oracle, sc):
+    inst = np.zeros((len(sc.instances), 20), np.float32)
+    for i, (mi, T) in enumerate(sc.instances):
+        inv = np.zeros(16, np.float32)
+        lib.ref_invert4x4(_p(np.ascontiguousarray(T, np.float32).reshape(-1)), _p(inv))
+        inst[i].view(np.uint64)[0] = sc.meshes[mi].tris.ctypes.data
+        inst[i, 4:] = inv
+    packed = pack_materials(oracle, sc)
+    texels = np.concatenate([t.texels for t in sc.textures]).astype(np.uint32) if sc.textures else np.zeros(16, np.uint32)
+    sky4, sw, sh = _sky_with_small(sc)
+    return inst, packed, texels, sky4, sw, sh
+
+
+def expand_blue_noise(tables):
+    """the blue-noise tables as the OptiX 7 core expands them (rendercore.cpp:247-256), plus 64 zero entries"""
+    bn = np.zeros(65536 * 5 + 64, np.uint32)
+    bn[:65536] = tables[0]
+    bn[65536:65536 + 131072] = tables[1]
+    bn[3 * 65536:3 * 65536 + 131072] = tables[2]
+    return bn
+
+
+def reference_blue_noise():
+    """the reference's own tables (common_bluenoise.h, compiled by path into the harness), as three byte arrays"""
+    lib = C.CDLL(REF_LIB)
+    out = []
+    for name, n in (("ref_bluenoise_sobol", 65536), ("ref_bluenoise_scrambling", 131072), ("ref_bluenoise_ranking", 131072)):
+        fn = getattr(lib, name)
+        fn.restype = C.POINTER(C.c_uint8)
+        out.append(np.ctypeslib.as_array(fn(), shape=(n,)).copy())
+    return tuple(out)
+
+
+class RefOptix7(RefKernels):
+    """The OptiX 7 core's shading kernel and ray generation compiled for the host (oracle/ref/ref_optix7.cpp), driven
+    through the core's wave loop (lib/rendercore_optix7/rendercore.cpp:874-922) with the oracle answering the ray
+    queries. The connection buffer is made large enough that the loop's early flush (rendercore.cpp:906-913) never
+    triggers."""
+
+    def __init__(self):
+        super().__init__()
+        L = self.lib
+        vp, i, f, u = C.c_void_p, C.c_int, C.c_float, C.c_uint32
+        L.ref_o7_set_scene.argtypes = [vp] * 2 + [vp, i] * 4 + [vp, f, f, i, vp, i, i, vp]
+        L.ref_o7_init_counters.argtypes = [i]
+        L.ref_o7_counters.argtypes = [vp]
+        L.ref_o7_generate.argtypes = [vp, i, i, i, i, i, vp, f, vp, vp, vp, f]
+        L.ref_o7_shade.argtypes = [i, vp, vp, vp, vp, u, u, i, i, i, i, i, f, i]
+        L.ref_o7_finalize_connections.argtypes = [i, vp, vp, vp, i]
+        L.ref_o7_bluenoise4.argtypes = [vp, i, i, i, i, vp]
+        L.ref_o7_set_shadow_count.argtypes = [u]
+
+    def render(self, oracle: Oracle, sc: S.Scene, view, params, accum=None):
+        """One frame; returns the accumulator, per path length the extension and connection counts, and whether the
+        loop flushed its connection buffer early (pathCount + shadowRays >= 2 P: connections then reach the
+        accumulator before later path lengths' terms)."""
+        L = self.lib
+        W, H, spp, D = int(params["width"]), int(params["height"]), int(params["spp"]), int(params["maxDepth"])
+        P = W * H * spp
+        eps = float(params["geometryEpsilon"])
+        nee = int(params["flags"]) & RP_NEE
+        inst, packed, texels, sky4, sw, sh = _ref_scene(L, oracle, sc)
+        bn = expand_blue_noise(sc.blue_noise)
+        self._keep = [inst, packed, texels, sky4, bn]
+        L.ref_o7_set_scene(_p(inst), _p(packed), _p(sc.tri_lights), len(sc.tri_lights), _p(sc.point_lights), len(sc.point_lights),
+                           _p(sc.spot_lights), len(sc.spot_lights), _p(sc.dir_lights), len(sc.dir_lights), _p(texels), eps,
+                           float(params["clampValue"]), D, _p(sky4), sw, sh, _p(bn))
+        ps = np.zeros((3 * P, 4), np.float32)
+        hits = np.zeros((P, 4), np.float32)
+        conn = np.zeros((6 * P, 4), np.float32)           # O4, D4, E4 at 0, 2 P, 4 P (rendercore.cpp:312)
+        acc = np.zeros((W * H, 4), np.float32) if accum is None else accum
+        v = view
+        right = (v["p2"] - v["p1"]).astype(np.float32)
+        up = (v["p3"] - v["p1"]).astype(np.float32)
+        shift = int(params["shift"])
+        L.ref_o7_generate(_p(ps), W, H, spp, int(params["samplesTaken"]), shift - (1 << 32) if shift >= 1 << 31 else shift,
+                          _p(v["pos"].copy()), float(v["aperture"]), _p(right), _p(up), _p(v["p1"].copy()), float(v["distortion"]))
+        L.ref_o7_init_counters(P)
+        counters = np.zeros((D, 2), np.uint32)
+        draw, count, seen, flushed = int(params["cameraR0"]), P, 0, False
+        c2 = np.zeros(2, np.uint32)
+
+        def connect(n):
+            rays = np.zeros(n, S.RAY_DTYPE)
+            rays["o"], rays["d"] = conn[:n, :3], conn[2 * P:2 * P + n, :3]
+            rays["tmin"], rays["tmax"] = eps, conn[2 * P:2 * P + n, 3]
+            occ = oracle.trace(rays, mode=1).astype(np.uint32)
+            L.ref_o7_finalize_connections(n, _p(acc), _p(conn), _p(occ), P)
+
+        for pl in range(1, D + 1):
+            if pl > 1:
+                L.ref_o7_next_counters()
+                draw = _xorshift(draw)
+            rays = np.zeros(count, S.RAY_DTYPE)
+            rays["o"], rays["d"] = ps[:count, :3], ps[P:P + count, :3]
+            rays["tmin"], rays["tmax"] = eps, 1e34
+            h = oracle.trace(rays, mode=0)
+            hits[:count, 0] = h["bary"].view(np.float32)
+            hits[:count, 1] = h["inst"].view(np.float32)
+            hits[:count, 2] = h["prim"].view(np.float32)
+            hits[:count, 3] = h["t"]
+            L.ref_o7_shade(count, _p(acc), _p(ps), _p(hits), _p(conn), (draw + pl * 91771) & 0xFFFFFFFF, shift,
+                           int(params["samplesTaken"]), pl, W, H, spp, float(v["spreadAngle"]), nee)
+            L.ref_o7_counters(_p(c2))
+            counters[pl - 1] = (c2[0], c2[1] - seen)
+            seen, count = int(c2[1]), int(c2[0])
+            if count == 0:
+                break
+            if count + seen >= 2 * P and seen > 0:   # rendercore.cpp:906-913
+                connect(seen)
+                flushed = True
+                L.ref_o7_set_shadow_count(0)
+                seen = 0
+        if seen:
+            connect(seen)
+        return {"accum": acc, "counters": counters, "flushed": flushed}
+
+    def bluenoise4(self, bn, x, y, sample, dim):
+        out = np.zeros(4, np.float32)
+        self.lib.ref_o7_bluenoise4(_p(bn), x, y, sample, dim, _p(out))
+        return out
+
+
+class RefAdaptive(RefKernels):
+    """The PrimeAdaptive core's kernels compiled for the host (oracle/ref/ref_adaptive.cpp), driven through the
+    core's RenderImpl and FinalizeRender (lib/RenderCore_PrimeAdaptive/rendercore.cpp:600-755) with the oracle
+    answering the ray queries. Launches run their threads in index order, so the adaptive ray generation's
+    compaction gives slots in thread order."""
+
+    ISECT = np.dtype([("t", "<f4"), ("triid", "<i4"), ("instid", "<i4"), ("u", "<f4"), ("v", "<f4")])
+
+    def __init__(self):
+        super().__init__()
+        L = self.lib
+        vp, i, f, u = C.c_void_p, C.c_int, C.c_float, C.c_uint32
+        L.ref_ad_set_scene.argtypes = [vp] * 2 + [vp, i] * 4 + [vp, f, f, i, vp, i, i]
+        L.ref_ad_init_extend.argtypes = [i]
+        L.ref_ad_counters.argtypes = [vp]
+        L.ref_ad_set_active.argtypes = [u]
+        L.ref_ad_set_shadow.argtypes = [u]
+        L.ref_ad_generate.argtypes = [vp, vp, u, vp, i, vp, f, vp, vp, vp, f, i, i, i]
+        L.ref_ad_generate_adaptive.argtypes = [vp, vp, vp, u, i, vp, vp, f, vp, vp, vp, f, i, i, i]
+        L.ref_ad_shade.argtypes = [i, vp, vp, vp, vp, vp, vp, vp, vp, vp, u, u, vp, i, i, i, i, f, i]
+        L.ref_ad_finalize_connections.argtypes = [i, vp, vp, vp]
+        L.ref_ad_estimate_variance.argtypes = [vp, vp, vp, f, i, i, i]
+        L.ref_ad_finalize.argtypes = [vp, vp, vp, i, i, i, i]
+
+    def render(self, oracle: Oracle, sc: S.Scene, view, params, accum, dev_scale):
+        """One frame: accum (W*H float4) is updated in place. Returns the new devScale, the frame, the per-wave
+        counters, the second wave's path count, the intermediate buffers and whether a wave loop flushed its
+        connection buffer early (rendercore.cpp:636-645)."""
+        L, O = self.lib, oracle.lib
+        W, H, spp, D = int(params["width"]), int(params["height"]), int(params["spp"]), int(params["maxDepth"])
+        P = W * H * spp
+        eps = float(params["geometryEpsilon"])
+        nee = int(params["flags"]) & RP_NEE
+        st = int(params["samplesTaken"])
+        shift = int(params["shift"])
+        inst, packed, texels, sky4, sw, sh = _ref_scene(L, oracle, sc)
+        bn = expand_blue_noise(sc.blue_noise)
+        L.ref_ad_set_scene(_p(inst), _p(packed), _p(sc.tri_lights), len(sc.tri_lights), _p(sc.point_lights), len(sc.point_lights),
+                           _p(sc.spot_lights), len(sc.spot_lights), _p(sc.dir_lights), len(sc.dir_lights), _p(texels), eps,
+                           float(params["clampValue"]), D, _p(sky4), sw, sh)
+        rays = [np.zeros((P, 8), np.float32), np.zeros((P, 8), np.float32)]
+        ps = [np.zeros((2 * P, 4), np.float32), np.zeros((2 * P, 4), np.float32)]
+        conn = np.zeros((2 * P, 8), np.float32)
+        pot = np.zeros((2 * P, 4), np.float32)
+        isect = np.zeros(P, self.ISECT)
+        facc = np.zeros((P, 4), np.float32)
+        feat = np.zeros((P, 4), np.float32)
+        self._keep = [inst, packed, texels, sky4, bn, rays, ps, conn, pot, isect, facc, feat]
+        v = view
+        right = (v["p2"] - v["p1"]).astype(np.float32)
+        up = (v["p3"] - v["p1"]).astype(np.float32)
+        pos, p1 = v["pos"].copy(), v["p1"].copy()
+        counters = np.zeros((2 * D, 2), np.uint32)
+        c3 = np.zeros(3, np.uint32)
+        tt = np.zeros(P, np.float32); ii = np.zeros(P, np.int32); pp = np.zeros(P, np.int32)
+        uu = np.zeros(P, np.float32); vv = np.zeros(P, np.float32)
+        flushed = [False]
+
+        def connect():
+            L.ref_ad_counters(_p(c3))
+            n = int(c3[2])
+            if n == 0:
+                return
+            occ = oracle.trace(np.ascontiguousarray(conn[:n]).view(S.RAY_DTYPE).reshape(-1), mode=1)
+            bits = np.zeros((n + 31) // 32, np.uint32)
+            idx = np.nonzero(occ)[0]
+            np.bitwise_or.at(bits, idx >> 5, (np.uint32(1) << (idx & 31).astype(np.uint32)))
+            L.ref_ad_finalize_connections(n, _p(facc), _p(bits), _p(pot))
+
+        def wave_loop(count, cin, R0of, passv, row):
+            seen = 0
+            for pl in range(1, D + 1):
+                r = np.ascontiguousarray(rays[cin][:count])
+                O.lh2o_trace_raw(oracle.s, _p(r), count, _p(tt), _p(ii), _p(pp), _p(uu), _p(vv), 0)
+                isect["t"][:count], isect["triid"][:count], isect["instid"][:count] = tt[:count], pp[:count], ii[:count]
+                isect["u"][:count], isect["v"][:count] = uu[:count], vv[:count]
+                L.ref_ad_shade(count, _p(facc), _p(feat), _p(rays[cin]), _p(ps[cin]), _p(isect), _p(rays[1 - cin]), _p(ps[1 - cin]),
+                               _p(conn), _p(pot), R0of(pl) & 0xFFFFFFFF, shift, _p(bn), passv, pl, W, H, float(v["spreadAngle"]), nee)
+                L.ref_ad_counters(_p(c3))
+                counters[row + pl - 1] = (c3[1], int(c3[2]) - seen)
+                seen = int(c3[2])
+                if pl >= D:
+                    break
+                count, cin = int(c3[1]), 1 - cin
+                if int(c3[2]) + count >= 2 * P:
+                    connect()
+                    L.ref_ad_set_shadow(0)
+                    seen = 0
+                    flushed[0] = True
+                L.ref_ad_next()
+            connect()
+            return cin
+
+        # first wave (rendercore.cpp:606-658)
+        L.ref_ad_init_extend(P)
+        L.ref_ad_generate(_p(rays[0]), _p(ps[0]), int(params["cameraR0"]), _p(bn), st, _p(pos), float(v["aperture"]), _p(right), _p(up), _p(p1),
+                          float(v["distortion"]), W, H, spp)
+        cin = wave_loop(P, 0, lambda pl: st * 7907 + pl * 91771, st, 0)
+        # variance estimate and adaptive rays (rendercore.cpp:663-680)
+        dev = np.zeros(W * H, np.float32)
+        L.ref_ad_estimate_variance(_p(facc), _p(feat), _p(dev), float(np.float32(dev_scale)), W, H, spp)
+        feat_wave1, facc_wave1 = feat.copy(), facc.copy()
+        L.ref_ad_init_stage2()
+        L.ref_ad_generate_adaptive(_p(dev), _p(rays[cin]), _p(ps[cin]), int(params["frameSeed"]), st, _p(bn), _p(pos), float(v["aperture"]),
+                                   _p(right), _p(up), _p(p1), float(v["distortion"]), W, H, spp)
+        L.ref_ad_counters(_p(c3))
+        count = int(c3[0])
+        budget = np.float32(W * H * spp)
+        if np.float32(count) > budget:
+            count = int(budget)
+            L.ref_ad_set_active(count)
+        ds = np.float32(dev_scale)
+        fc = np.float32(count)
+        if fc > np.float32(0.98) * budget:
+            ds = np.float32(ds * np.float32(0.92))
+        elif fc > np.float32(0.96) * budget:
+            ds = np.float32(ds * np.float32(0.98))
+        elif fc < np.float32(0.91) * budget:
+            ds = np.float32(ds * np.float32(1.08))
+        elif fc < np.float32(0.94) * budget:
+            ds = np.float32(ds * np.float32(1.02))
+        # second wave (rendercore.cpp:682-713)
+        wave_loop(count, cin, lambda pl: st * 59071 + pl * 31771, st + spp, D)
+        # FinalizeRender (rendercore.cpp:749-755)
+        frame = np.zeros((W * H, 4), np.float32)
+        L.ref_ad_finalize(_p(facc), _p(accum), _p(frame), W, H, st + spp, spp)
+        return {"dev_scale": float(ds), "frame": frame, "counters": counters, "adaptive_paths": count, "frame_acc": facc,
+                "frame_acc_wave1": facc_wave1, "features": feat_wave1, "deviation": dev, "flushed": flushed[0]}
 
 
 def pack_materials(oracle: Oracle, sc: S.Scene):

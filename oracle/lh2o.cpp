@@ -301,7 +301,9 @@ struct Instance {
     float wmin[3], wmax[3];
 };
 
-struct Sky { std::vector<f3> px; int w = 0, h = 0; float m[16]; };
+/* the sky and its 64x scaled-down copy (the average of each 64 x 64 tile, RenderCore::SetSkyData,
+ * lib/rendercore_optix7/rendercore.cpp:716-740), which the OptiX 7 estimator samples after a diffuse bounce */
+struct Sky { std::vector<f3> px; int w = 0, h = 0; float m[16]; std::vector<f3> small; };
 
 }  // namespace
 
@@ -319,6 +321,11 @@ struct lh2o_scene {
     Sky sky;
     BVH2 top;
     bool finalized = false;
+    /* blue-noise tables expanded to one uint per entry as rendercore_optix7/rendercore.cpp:247-256 does: Sobol
+     * 256 x 256 at 0, scrambling 128 x 128 x 8 at 65536, ranking 128 x 128 x 8 at 3 * 65536; then 64 zero entries,
+     * which the ranking reads of deep path lengths at the last tile pixel reach (the reference reads past its
+     * buffer there). Empty: no tables, every sample uses xorshift numbers. */
+    std::vector<uint> blueNoise;
 };
 
 namespace {
@@ -1629,6 +1636,335 @@ void nrc_forward1(const float* mlp, const float* e, float act[5][64], double* y,
     }
 }
 
+
+/* ------------------------------------------------------------------------------------------------------
+ * The OptiX 7 core's estimator (lib/rendercore_optix7/kernels/pathtracer.h:54-238, ray generation of
+ * optix/.optix.cu:71-129) and the PrimeAdaptive core's variant of it (lib/RenderCore_PrimeAdaptive/kernels/
+ * pathtracer.h:52-238, camera.h:39-139), both with the Lambert BSDF of lib/sharedBSDFs/lambert.h (the alternative
+ * their kernels/bsdf.h offers). Run per path depth first: every random number depends on (path, depth) only.
+ * ---------------------------------------------------------------------------------------------------- */
+constexpr uint S_BOUNCEDTWICE = 8;                   /* rendercore_optix7/kernels/pathtracer.h:31 */
+constexpr int MIS_OPTIX7 = 1, MIS_ADAPTIVE = 2;
+
+/* RayTarget, lib/RenderSystem/common_functions.h:29-50 (atan2f, sinf, cosf by the oracle's own functions) */
+inline f3 RayTarget(const int sx, const int sy, const float r0, const float r1, const int W, const int H, const float distortion,
+                    const f3 p1, const f3 right, const f3 up) {
+    if (distortion == 0) {
+        const float u = ((float)sx + r0) * (1.0f / W);
+        const float v = ((float)sy + r1) * (1.0f / H);
+        return p1 + u * right + v * up;
+    }
+    const float tx = sx / (float)W - 0.5f, ty = sy / (float)H - 0.5f;
+    const float rr = tx * tx + ty * ty;
+    const float rq = sqrtf(rr) * (1.0f + distortion * rr + distortion * rr * rr);
+    const float theta = lm_atan2f(tx, ty);
+    float st, ct;
+    lm_sincos(theta, &st, &ct);
+    const float bx = (st * rq + 0.5f) * W;
+    const float by = (ct * rq + 0.5f) * H;
+    return p1 + (bx + r0) * (right / (float)W) + (by + r1) * (up / (float)H);
+}
+
+/* RandomPointOnLens, optix/.optix.cu:71-83 and RenderCore_PrimeAdaptive/kernels/camera.h:22-33 */
+inline f3 RandomPointOnLens(const float r0, float r1, const f3 pos, const float aperture, const f3 right, const f3 up) {
+    const float blade = (float)f2i(r0 * 9);
+    float r2 = (r0 - blade * (1.0f / 9.0f)) * 9.0f;
+    float x1, y1, x2, y2;
+    lm_sincos(blade * PI / 4.5f, &x1, &y1);
+    lm_sincos((blade + 1.0f) * PI / 4.5f, &x2, &y2);
+    if ((r1 + r2) > 1) r1 = 1.0f - r1, r2 = 1.0f - r2;
+    const float xr = x1 * r1 + x2 * r2;
+    const float yr = y1 * r1 + y2 * r2;
+    return pos + aperture * (right * xr + up * yr);
+}
+
+/* blueNoiseSampler4, lib/CUDA/shared_kernel_code/tools_shared.h:324-337 */
+inline f4 blueNoiseSampler4(const uint* bn, int x, int y, int sampleIndex, int sampleDimension) {
+    const uint* r = bn + sampleDimension + (x + y * 128) * 8 + 65536 * 3;
+    const int rsi1 = (sampleIndex ^ (int)r[0]) & 255, rsi2 = (sampleIndex ^ (int)r[1]) & 255;
+    const int rsi3 = (sampleIndex ^ (int)r[2]) & 255, rsi4 = (sampleIndex ^ (int)r[3]) & 255;
+    const int v1 = (int)bn[sampleDimension + 0 + rsi1 * 256];
+    const int v2 = (int)bn[sampleDimension + 1 + rsi2 * 256];
+    const int v3 = (int)bn[sampleDimension + 2 + rsi3 * 256];
+    const int v4 = (int)bn[sampleDimension + 3 + rsi4 * 256];
+    const uint* b = bn + (sampleDimension & 7) + (x + y * 128) * 8 + 65536;
+    return mk4((0.5f + (float)(v1 ^ (int)b[0])) * (1.0f / 256.0f), (0.5f + (float)(v2 ^ (int)b[1])) * (1.0f / 256.0f),
+               (0.5f + (float)(v3 ^ (int)b[2])) * (1.0f / 256.0f), (0.5f + (float)(v4 ^ (int)b[3])) * (1.0f / 256.0f));
+}
+
+/* SampleSmallSkydome, tools_shared.h:204-211, on the 64x scaled-down sky */
+f3 SampleSmallSkydome(const lh2o_scene* s, const f3& Dw) {
+    const uint w = (uint)s->sky.w >> 6, h = (uint)s->sky.h >> 6;
+    if (w == 0 || h == 0) return mk3(0);
+    const float* m = s->sky.m;
+    const f3 D = -mk3(m[0] * Dw.x + m[1] * Dw.y + m[2] * Dw.z, m[4] * Dw.x + m[5] * Dw.y + m[6] * Dw.z, m[8] * Dw.x + m[9] * Dw.y + m[10] * Dw.z);
+    float p = lm_atan2f(D.y, D.x);
+    p = (p < 0) ? (p + 2 * PI) : p;
+    const float theta = lm_acosf(D.z < -1.f ? -1.f : (D.z > 1.f ? 1.f : D.z));
+    const uint u = f2u((float)w * p * INV2PI - 0.5f);
+    const uint v = f2u((float)h * theta * INVPI - 0.5f);
+    const uint idx = u + v * w;
+    return idx < w * h ? s->sky.small[idx] : mk3(0);
+}
+
+/* CalculateLightPDF and LightPickProb, lights_shared.h:111-117, 158-177 */
+inline float CalculateLightPDF(const f3& D, const float t, const float lightArea, const f3 lightNormal) {
+    return (t * t) / (fabsf(dot(D, lightNormal)) * lightArea);
+}
+float LightPickProb(const lh2o_scene* s, int idx, const f3& O, const f3& N, const f3& I) {
+    float potential[64];
+    float sum = 0;
+    int lights = 0;
+    for (size_t i = 0; i < s->triLights.size(); i++) { const float c = PotentialTriLightContribution(s, (int)i, O, N, I, mk3(-1)); potential[lights++] = c; sum += c; }
+    for (size_t i = 0; i < s->pointLights.size(); i++) { const float c = PotentialPointLightContribution(s, (int)i, O, N); potential[lights++] = c; sum += c; }
+    for (size_t i = 0; i < s->spotLights.size(); i++) { const float c = PotentialSpotLightContribution(s, (int)i, O, N); potential[lights++] = c; sum += c; }
+    for (size_t i = 0; i < s->dirLights.size(); i++) { const float c = PotentialDirectionalLightContribution(s, (int)i, O, N); potential[lights++] = c; sum += c; }
+    if (sum <= 0) return 0;
+    return (idx >= 0 && idx < lights) ? potential[idx] / sum : 0.0f;
+}
+
+inline void add4(float* a, const f4& v) { a[0] += v.x, a[1] += v.y, a[2] += v.z, a[3] += v.w; }
+
+/* CLAMPINTENSITY (core_settings.h:191-194) and FIXNAN_FLOAT3 (common_settings.h:66) */
+inline void clamp_intensity(f3& c, const float clampValue) {
+    const float v = fmaxr(c.x, fmaxr(c.y, c.z));
+    if (v > clampValue) { const float m = clampValue / v; c.x *= m, c.y *= m, c.z *= m; }
+}
+inline void fix_nan(f3& a) { if (!std::isfinite(a.x + a.y + a.z)) a = mk3(0); }
+
+/* Radiance of one path of these estimators, summed in the order the path produces it: per path length its sky or
+ * emitter term, then the contribution of its light connection when that is unoccluded. (The reference adds the
+ * connections to the pixel after the wave loop, and the paths of a pixel race on it; the order here is fixed, and
+ * the sums agree with the reference's within float rounding.) w: the connections' count (OptiX 7) or the sample
+ * count (PrimeAdaptive). */
+struct MisPath { f4 acc; };
+
+/* pathIdx: the path as the shading sees it (pixel + layer * W*H); pass: the 'pass' of the shading kernel;
+ * R0(d) is the shading seed of path length d; O, D, tmin: the primary ray. feat (PrimeAdaptive, may be null):
+ * this path's float4 feature (albedo, packed normal). capIdx: the path's slot in capture arrays (-1: none). */
+template <typename R0Fn>
+void trace_path_mis(const Frame& F, const int flavor, const uint pathIdx, const uint pass, const R0Fn& R0, f3 O, f3 D, float tmin,
+                    MisPath& out, std::vector<uint>& ext, std::vector<uint>& shad, lh2g_capture* cap, long long capIdx, float* feat) {
+    const lh2o_scene* s = F.s;
+    const lh2g_render_params& p = F.p;
+    const int W = p.width, H = p.height;
+    const float eps = p.geometryEpsilon;
+    const bool nee = (p.flags & LH2G_RP_NEE) != 0;
+    const uint* bn = s->blueNoise.empty() ? nullptr : s->blueNoise.data();
+    out.acc = mk4(0, 0, 0, flavor == MIS_ADAPTIVE ? 1.0f : 0.0f);   /* accumulator[pathIdx].w += 1 at path length 1 */
+    f3 throughput = mk3(1);
+    float bsdfPdf = 1;
+    uint FLAGS = S_SPECULAR, packedNormal = 0;
+    const uint sampleIdx = pathIdx / ((uint)W * (uint)H) + pass;
+    for (int pathLength = 1; pathLength <= p.maxDepth; pathLength++) {
+        HitRec h;
+        trace_scene(s, O, D, tmin, 1e34f, false, false, h);
+        const lh2g_hit hit = make_hit(h);
+        const long long ci = capIdx < 0 ? -1 : (long long)(pathLength - 1) * F.P + capIdx;
+        if (cap && cap->hits && ci >= 0) cap->hits[ci] = hit;
+        auto capSeed = [&](uint v) { if (cap && cap->seeds && ci >= 0) cap->seeds[ci] = v; };
+        const bool firstHitToBeStored = feat && (FLAGS & S_BOUNCED) == 0;
+        if (hit.prim == NOHIT) {
+            const f3 skyPixel = (FLAGS & S_BOUNCED) ? SampleSmallSkydome(s, D) : SampleSkydome(s, D);
+            f3 contribution = throughput * skyPixel * (1.0f / bsdfPdf);
+            clamp_intensity(contribution, p.clampValue);
+            fix_nan(contribution);
+            out.acc.x += contribution.x, out.acc.y += contribution.y, out.acc.z += contribution.z;
+            if (firstHitToBeStored) store4(feat, contribution.x, contribution.y, contribution.z, bitsf(PackNormal2(D * -1.0f)));
+            capSeed(0);
+            return;
+        }
+        const float HIT_U = (float)(hit.bary & 65535u) * (1.0f / 65535.0f);
+        const float HIT_V = (float)(hit.bary >> 16) * (1.0f / 65535.0f);
+        const float HIT_T = hit.t;
+        const lh2g_core_tri& tri = s->meshes[s->inst[hit.inst].mesh].tris[hit.prim];
+        ShadingData sd;
+        f3 N, iN, fN, T;
+        const f3 I = O + HIT_T * D;
+        GetShadingData(s, D, HIT_U, HIT_V, F.view.spreadAngle * HIT_T, tri, hit.inst, sd, N, iN, fN, T);
+        if (firstHitToBeStored) store4(feat, sd.color.x, sd.color.y, sd.color.z, bitsf(PackNormal2(iN)));
+        if (sd.flags & 1) {   /* alpha: the ray continues behind the surface */
+            capSeed(0);
+            if (pathLength >= p.maxDepth) return;
+            ext[pathLength - 1]++;
+            fix_nan(throughput);
+            if (flavor == MIS_OPTIX7) {
+                O = I + D * eps;   /* flags, direction, packed normal and pdf carry over */
+                tmin = eps;
+            } else {
+                O = I;
+                tmin = EPSILON;
+                packedNormal = 0;
+            }
+            continue;
+        }
+        if (IsEmissive(sd)) {
+            const float DdotNL = -dot(D, N);
+            if (DdotNL > 0) {
+                f3 contribution = mk3(0);
+                if (pathLength == 1 || (FLAGS & S_SPECULAR) || !nee) {
+                    contribution = sd.color;   /* the reference leaves the throughput out here */
+                } else {
+                    const f3 lastN = UnpackNormal(packedNormal);
+                    const float lightPdf = CalculateLightPDF(D, HIT_T, tri.area, N);
+                    const float pickProb = LightPickProb(s, tri.ltriIdx, O, lastN, I);
+                    if ((bsdfPdf + lightPdf * pickProb) > 0) contribution = throughput * sd.color * (1.0f / (bsdfPdf + lightPdf * pickProb));
+                }
+                clamp_intensity(contribution, p.clampValue);
+                fix_nan(contribution);
+                out.acc.x += contribution.x, out.acc.y += contribution.y, out.acc.z += contribution.z;
+            }
+            capSeed(0);
+            return;
+        }
+        if (FLAGS & S_BOUNCED) sd.params[0] |= 255u << 24;   /* path regularisation: roughness 1 after a bounce */
+        if (ROUGHNESS(sd) <= 0.001f || TRANSMISSION(sd) > 0.5f) FLAGS |= S_SPECULAR; else FLAGS &= ~S_SPECULAR;
+        const float faceDir = (dot(D, N) > 0) ? -1.0f : 1.0f;
+        if (faceDir == 1) sd.transmittance = mk3(0);
+        throughput = throughput * (1.0f / bsdfPdf);
+        uint seed = WangHash(pathIdx * 17u + R0(pathLength));
+        f4 r4;
+        if (sampleIdx < 64 && bn) {
+            const uint x = ((pathIdx % (uint)W) + (p.shift & 127u)) & 127u;
+            const uint y = ((pathIdx / (uint)W) + (p.shift >> 24)) & 127u;
+            r4 = blueNoiseSampler4(bn, (int)x, (int)y, (int)sampleIdx, 4 * pathLength - 4);
+        } else {
+            r4.x = RandomFloat(seed), r4.y = RandomFloat(seed);
+            r4.z = RandomFloat(seed), r4.w = RandomFloat(seed);
+        }
+        if ((FLAGS & S_SPECULAR) == 0 && nee) {
+            float pickProb = 0, lightPdf = 0;
+            f3 lightColor = mk3(0);
+            f3 L = RandomPointOnLight(s, r4.x, r4.y, I, fN * faceDir, pickProb, lightPdf, lightColor) - I;
+            const float dist = length(L);
+            L = L * (1.0f / dist);
+            const float NdotL = dot(L, fN * faceDir);
+            if (NdotL > 0 && lightPdf > 0) {
+                float lbsdfPdf;
+                const f3 sampledBSDF = EvaluateBSDF(sd, fN, L, lbsdfPdf) * ROUGHNESS(sd);
+                if (lbsdfPdf > 0) {
+                    f3 contribution = throughput * sampledBSDF * lightColor * (NdotL / (pickProb * lightPdf + lbsdfPdf));
+                    fix_nan(contribution);
+                    clamp_intensity(contribution, p.clampValue);
+                    shad[pathLength - 1]++;
+                    HitRec sh;
+                    const f3 SO = SafeOrigin(I, L, N, eps);
+                    const bool occluded = trace_scene(s, SO, L, flavor == MIS_OPTIX7 ? eps : 0.0f, dist - 2 * eps, true, false, sh);
+                    if (!occluded) {
+                        out.acc.x += contribution.x, out.acc.y += contribution.y, out.acc.z += contribution.z;
+                        if (flavor == MIS_OPTIX7) out.acc.w += 1.0f;
+                    }
+                }
+            }
+        }
+        /* one diffuse bounce at most (ENOUGH_BOUNCES = S_BOUNCED), or the maximum path length */
+        if ((FLAGS & S_BOUNCED) || pathLength == p.maxDepth) { capSeed(seed); return; }
+        f3 R;
+        float newBsdfPdf;
+        bool specular = false;
+        const float r5 = RandomFloat(seed);   /* the r5 argument of lambert.h's SampleBSDF: drawn, not used */
+        (void)r5;
+        const f3 bsdf = SampleBSDF(sd, fN, N, D * -1.0f, HIT_T, r4.z, r4.w, R, newBsdfPdf, specular);
+        if (newBsdfPdf < EPSILON || std::isnan(newBsdfPdf)) { capSeed(seed); return; }
+        if (specular) FLAGS |= S_SPECULAR;
+        const float pr = ((FLAGS & S_SPECULAR) || (FLAGS & S_BOUNCED) == 0) ? 1.0f : SurvivalProbability(bsdf);
+        if (pr < RandomFloat(seed)) { capSeed(seed); return; }
+        throughput = throughput * (1 / pr);
+        capSeed(seed);
+        ext[pathLength - 1]++;
+        packedNormal = PackNormal(fN * faceDir);
+        if (!(FLAGS & S_SPECULAR)) FLAGS |= (FLAGS & S_BOUNCED) ? S_BOUNCEDTWICE : S_BOUNCED; else FLAGS |= S_VIASPECULAR;
+        O = SafeOrigin(I, R, N, eps);
+        D = R;
+        fix_nan(throughput);
+        throughput = throughput * bsdf * fabsf(dot(fN, R));
+        bsdfPdf = newBsdfPdf;
+        tmin = flavor == MIS_OPTIX7 ? eps : 0.0f;
+    }
+}
+
+/* the primary ray of the OptiX 7 core, optix/.optix.cu:85-129 (setupPrimaryRay, generateEyeRay) */
+inline void primary_optix7(const Frame& F, const uint pathIdx, f3& O, f3& D) {
+    const lh2g_render_params& p = F.p;
+    const uint W = (uint)p.width, H = (uint)p.height;
+    const uint pixelIdx = pathIdx % (W * H);
+    const uint sampleIdx = pathIdx / (W * H) + (uint)p.samplesTaken;
+    uint seed = WangHash(pathIdx * 16789u + (uint)p.samplesTaken * 1791u);
+    const int sx = (int)(pixelIdx % W), sy = (int)(pixelIdx / W);
+    f4 r4;
+    if (sampleIdx < 64 && !F.s->blueNoise.empty()) {
+        r4 = blueNoiseSampler4(F.s->blueNoise.data(), (sx + (int)(p.shift & 127u)) & 127, (sy + (int)(p.shift >> 24)) & 127, (int)sampleIdx, 0);
+    } else {
+        r4.x = RandomFloat(seed), r4.y = RandomFloat(seed);
+        r4.z = RandomFloat(seed), r4.w = RandomFloat(seed);
+    }
+    O = RandomPointOnLens(r4.x, r4.z, ld3(F.view.pos), F.view.aperture, F.right, F.up);
+    const f3 posOnPixel = RayTarget(sx, sy, r4.y, r4.w, (int)W, (int)H, F.view.distortion, ld3(F.view.p1), F.right, F.up);
+    D = normalize(posOnPixel - O);
+}
+
+/* the primary ray of the PrimeAdaptive core for pixel (sx, sy) and sample index sampleIdx: blue noise (no tile
+ * shift) below 64, else xorshift numbers from WangHash(thread + R0) (camera.h:39-80, 96-139) */
+inline void primary_adaptive(const Frame& F, const int sx, const int sy, const uint sampleIdx, const uint thread, const uint R0, f3& O, f3& D) {
+    f4 r4;
+    if (sampleIdx < 64 && !F.s->blueNoise.empty()) {
+        r4 = blueNoiseSampler4(F.s->blueNoise.data(), sx & 127, sy & 127, (int)sampleIdx, 0);
+    } else {
+        uint seed = WangHash(thread + R0);
+        r4.x = RandomFloat(seed), r4.y = RandomFloat(seed);
+        r4.z = RandomFloat(seed), r4.w = RandomFloat(seed);
+    }
+    O = RandomPointOnLens(r4.x, r4.z, ld3(F.view.pos), F.view.aperture, F.right, F.up);
+    const f3 posOnPixel = RayTarget(sx, sy, r4.y, r4.w, F.p.width, F.p.height, F.view.distortion, ld3(F.view.p1), F.right, F.up);
+    D = normalize(posOnPixel - O);
+}
+
+/* estimateVarianceKernel, lib/CUDA/shared_kernel_code/finalize_shared.h:97-151 (powf(x, 2) as x * x) */
+float estimate_variance(const float* frameAcc, const float* features, const int x, const int y, const int W, const int H, const int spp) {
+    const long long WH = (long long)W * H;
+    const float x1 = (float)imax(0, x - 4), y1 = (float)imax(0, y - 4), x2 = (float)imin(W - 1, x + 4), y2 = (float)imin(H - 1, y + 4);
+    f3 total = mk3(0);
+    float weightSum = 0;
+    for (int i = 0; i < spp; i++) {
+        const f3 Nlocal = UnpackNormal2(fbits(features[4 * (x + (long long)y * W + i * WH) + 3]));
+        for (int v = (int)y1; v <= y2; v++)
+            for (int u = (int)x1; u <= x2; u++) {
+                const long long a = u + (long long)v * W + i * WH;
+                const float* feature = features + 4 * a;
+                const f3 normal = UnpackNormal2(fbits(feature[3]));
+                const f3 albedo = ld3(feature);
+                const f3 smp = ld3(frameAcc + 4 * a);
+                const f3 lighting = mk3(smp.x / fmaxr(albedo.x, 0.001f), smp.y / fmaxr(albedo.y, 0.001f), smp.z / fmaxr(albedo.z, 0.001f));
+                const uint dx = (uint)std::abs(x - u), dy = (uint)std::abs(y - v);
+                const float xweight = dx == 1 ? 0.9f : (dx == 2 ? 0.75f : (dx == 3 ? 0.55f : (dx == 4 ? 0.35f : 1.0f)));
+                const float yweight = dy == 1 ? 0.9f : (dy == 2 ? 0.75f : (dy == 3 ? 0.55f : (dy == 4 ? 0.35f : 1.0f)));
+                const float c = fmaxr(0.0001f, dot(normal, Nlocal));
+                const float weight = xweight * yweight * (c * c);
+                weightSum += weight;
+                total = total + lighting * weight;
+            }
+    }
+    const f3 average = total * (1.0f / weightSum);
+    float variance = 0;
+    for (int i = 0; i < spp; i++) {
+        const long long a = x + (long long)y * W + i * WH;
+        const f3 albedo = ld3(features + 4 * a);
+        const f3 smp = ld3(frameAcc + 4 * a);
+        const f3 lighting = mk3(smp.x / fmaxr(albedo.x, 0.001f), smp.y / fmaxr(albedo.y, 0.001f), smp.z / fmaxr(albedo.z, 0.001f));
+        const float d = Luminance(lighting) - Luminance(average);
+        variance += d * d;
+    }
+    variance /= 3.0f * spp;
+    return (variance + EPSILON) / (Luminance(average) + EPSILON);
+}
+
+/* samples S = 1..24 a pixel asks for (generateEyeRaysKernelAdaptive: sample S when !(S > deviation)) */
+inline int adaptive_wanted(const float d) {
+    int c = 0;
+    for (int S = 1; S <= 24; S++) if (!((float)S > d)) c = S;
+    return c;
+}
+
 }  // namespace
 
 /* ==========================================================================================================
@@ -1712,6 +2048,24 @@ int lh2o_set_sky(lh2o_scene* s, const float* rgb, int w, int h, const float* m16
     s->sky.px.resize((size_t)w * h);
     for (size_t i = 0; i < (size_t)w * h; i++) s->sky.px[i] = mk3(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]);
     for (int i = 0; i < 16; i++) s->sky.m[i] = m16 ? m16[i] : ((i % 5 == 0) ? 1.0f : 0.0f);
+    const int sw = w >> 6, sh = h >> 6;
+    s->sky.small.assign((size_t)sw * sh, mk3(0));
+    for (int y = 0; y < sh; y++)
+        for (int x = 0; x < sw; x++) {
+            f3 total = mk3(0);
+            for (int v = 0; v < 64; v++)
+                for (int u = 0; u < 64; u++) total = total + s->sky.px[(size_t)(x * 64 + u) + (size_t)(y * 64 + v) * w];
+            s->sky.small[(size_t)x + (size_t)y * sw] = total * (1.0f / (64 * 64));
+        }
+    return 0;
+}
+
+int lh2o_set_blue_noise(lh2o_scene* s, const uint8_t* sobol, const uint8_t* scrambling, const uint8_t* ranking) {
+    if (!s) return 1;
+    if (!sobol || !scrambling || !ranking) { s->blueNoise.clear(); return 0; }
+    s->blueNoise.assign(65536 * 5 + 64, 0u);
+    for (int i = 0; i < 65536; i++) s->blueNoise[i] = sobol[i];
+    for (int i = 0; i < 128 * 128 * 8; i++) s->blueNoise[i + 65536] = scrambling[i], s->blueNoise[i + 3 * 65536] = ranking[i];
     return 0;
 }
 
@@ -1790,9 +2144,59 @@ int lh2o_trace_raw(lh2o_scene* s, const lh2g_ray* rays, long long n, float* t, i
     return 0;
 }
 
+/* A frame of the OptiX 7 core's estimator: per path its terminal term and connections; per pixel the terms of the
+ * frame's samples in sample order, then their connections (first, then second) in sample order. */
+static int render_optix7(lh2o_scene* s, const lh2g_view* view, const lh2g_render_params* p, float* pixelAccum, double* pixelAccum64,
+                         uint32_t* counters, lh2g_capture* capture, int nthreads) {
+    Frame F;
+    F.s = s, F.view = *view, F.p = *p;
+    F.right = ld3(view->p2) - ld3(view->p1);
+    F.up = ld3(view->p3) - ld3(view->p1);
+    memset(&F.feat, 0, sizeof(F.feat));
+    const long long WH = (long long)p->width * p->height;
+    F.P = WH * p->spp;
+    const int D = p->maxDepth;
+    if (capture && capture->hits)
+        for (long long i = 0; i < F.P * D; i++) capture->hits[i] = lh2g_hit{0, -1, -2, 0.0f};
+    if (capture && capture->seeds) memset(capture->seeds, 0, sizeof(uint32_t) * F.P * D);
+    /* shading seed of wave d: the d-th RandomUInt(camRNGseed) of the frame (cameraR0 is the first) + d * 91771 */
+    uint draws[65];
+    draws[1] = p->cameraR0;
+    for (int d = 2; d <= D; d++) { uint x = draws[d - 1]; draws[d] = RandomInt(x); }
+    auto R0 = [&](int d) { return draws[d] + (uint)d * 91771u; };
+    std::vector<MisPath> paths(F.P);
+    std::mutex mtx;
+    std::vector<uint> extTot(D, 0), shadTot(D, 0);
+    parallel_for(F.P, nthreads, 256, [&](long long b, long long e) {
+        std::vector<uint> ext(D, 0), shad(D, 0);
+        for (long long i = b; i < e; i++) {
+            f3 O, Dd;
+            primary_optix7(F, (uint)i, O, Dd);
+            trace_path_mis(F, MIS_OPTIX7, (uint)i, (uint)p->samplesTaken, R0, O, Dd, p->geometryEpsilon, paths[i], ext, shad, capture, i, nullptr);
+        }
+        std::lock_guard<std::mutex> g(mtx);
+        for (int d = 0; d < D; d++) extTot[d] += ext[d], shadTot[d] += shad[d];
+    });
+    for (long long px = 0; px < WH; px++)
+        for (int smp = 0; smp < p->spp; smp++) {
+            const f4& v = paths[smp * WH + px].acc;
+            if (pixelAccum) add4(pixelAccum + 4 * px, v);
+            if (pixelAccum64) {
+                double* a64 = pixelAccum64 + 4 * px;
+                a64[0] += v.x, a64[1] += v.y, a64[2] += v.z, a64[3] += v.w;
+            }
+        }
+    if (counters) for (int d = 0; d < D; d++) counters[2 * d] = extTot[d], counters[2 * d + 1] = shadTot[d];
+    return 0;
+}
+
 int lh2o_render_ex(lh2o_scene* s, const lh2g_view* view, const lh2g_render_params* p, float* pixelAccum, double* pixelAccum64,
                    uint32_t* counters, lh2g_capture* capture, const lh2o_features* feat, int nthreads) {
     if (!s || !s->finalized || !view || !p || p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->maxDepth <= 0 || p->maxDepth > 64) return 1;
+    if (p->flags & LH2G_RP_OPTIX7) {
+        if (p->flags & (LH2G_RP_FILTER | LH2G_RP_NRC | LH2G_RP_ADAPTIVE)) return 1;
+        return render_optix7(s, view, p, pixelAccum, pixelAccum64, counters, capture, nthreads);
+    }
     const bool filt = (p->flags & LH2G_RP_FILTER) != 0;
     Frame F;
     F.s = s, F.view = *view, F.p = *p;
@@ -1838,6 +2242,115 @@ int lh2o_render_ex(lh2o_scene* s, const lh2g_view* view, const lh2g_render_param
 int lh2o_render(lh2o_scene* s, const lh2g_view* view, const lh2g_render_params* p, float* pixelAccum, double* pixelAccum64,
                 uint32_t* counters, lh2g_capture* capture, int nthreads) {
     return lh2o_render_ex(s, view, p, pixelAccum, pixelAccum64, counters, capture, nullptr, nthreads);
+}
+
+int lh2o_render_adaptive(lh2o_scene* s, const lh2g_view* view, const lh2g_render_params* p, float* accum, float* frame, float* devScale,
+                         uint32_t* counters, uint32_t* adaptivePaths, float* frameAccOut, float* featuresOut, float* deviationOut,
+                         lh2g_capture* capture, int nthreads) {
+    if (!s || !s->finalized || !view || !p || !accum || !devScale || p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->maxDepth <= 0 ||
+        p->maxDepth > 32 || (p->flags & (LH2G_RP_FILTER | LH2G_RP_NRC | LH2G_RP_OPTIX7)))
+        return 1;
+    Frame F;
+    F.s = s, F.view = *view, F.p = *p;
+    F.right = ld3(view->p2) - ld3(view->p1);
+    F.up = ld3(view->p3) - ld3(view->p1);
+    memset(&F.feat, 0, sizeof(F.feat));
+    const int W = p->width, H = p->height, spp = p->spp, D = p->maxDepth;
+    const long long WH = (long long)W * H, P = WH * spp;
+    F.P = P;
+    const uint pass = (uint)p->samplesTaken;
+    if (capture && capture->hits)
+        for (long long i = 0; i < P * D; i++) capture->hits[i] = lh2g_hit{0, -1, -2, 0.0f};
+    if (capture && capture->seeds) memset(capture->seeds, 0, sizeof(uint32_t) * P * D);
+    std::vector<float> frameAcc(4 * P, 0.0f), feat(4 * P, 0.0f);
+    std::vector<MisPath> paths(P);
+    std::mutex mtx;
+    std::vector<uint> extTot(2 * D, 0), shadTot(2 * D, 0);
+    /* first wave: spp samples per pixel (RenderCore_PrimeAdaptive/rendercore.cpp:606-658) */
+    auto R0a = [&](int d) { return pass * 7907u + (uint)d * 91771u; };
+    parallel_for(P, nthreads, 256, [&](long long b, long long e) {
+        std::vector<uint> ext(D, 0), shad(D, 0);
+        for (long long j = b; j < e; j++) {
+            const int sx = (int)(j % W);
+            const uint row = (uint)(j / W);
+            const uint sampleIdx = pass + row / (uint)H;
+            f3 O, Dd;
+            primary_adaptive(F, sx, (int)(row % (uint)H), sampleIdx, (uint)j, p->cameraR0, O, Dd);
+            trace_path_mis(F, MIS_ADAPTIVE, (uint)j, pass, R0a, O, Dd, p->geometryEpsilon, paths[j], ext, shad, capture, j, &feat[4 * j]);
+        }
+        std::lock_guard<std::mutex> g(mtx);
+        for (int d = 0; d < D; d++) extTot[d] += ext[d], shadTot[d] += shad[d];
+    });
+    for (long long j = 0; j < P; j++) add4(&frameAcc[4 * j], paths[j].acc);
+    /* variance estimate, the samples each pixel asks for, the budget (rendercore.cpp:663-680) */
+    std::vector<float> dev(WH);
+    std::vector<int> want(WH);
+    const float scale = *devScale;
+    parallel_for(WH, nthreads, 1024, [&](long long b, long long e) {
+        for (long long px = b; px < e; px++) {
+            dev[px] = estimate_variance(frameAcc.data(), feat.data(), (int)(px % W), (int)(px / W), W, H, spp) * scale;
+            want[px] = adaptive_wanted(dev[px]);
+        }
+    });
+    unsigned long long total = 0;
+    for (long long px = 0; px < WH; px++) total += (unsigned long long)want[px];
+    const float budget = (float)(W * H * spp);
+    uint pathCount = (uint)total;
+    if ((float)pathCount > budget) pathCount = (uint)budget;
+    if ((float)pathCount > 0.98f * budget) *devScale *= 0.92f;
+    else if ((float)pathCount > 0.96f * budget) *devScale *= 0.98f;
+    else if ((float)pathCount < 0.91f * budget) *devScale *= 1.08f;
+    else if ((float)pathCount < 0.94f * budget) *devScale *= 1.02f;
+    /* the samples kept: the first `budget` in the order of the generating threads (thread = pixel + (S - 1) * W*H),
+     * i.e. all with S below S*, and those with S = S* of the first r pixels that ask for S* */
+    std::vector<int> kept(WH);
+    {
+        long long room = (long long)pathCount;
+        for (long long px = 0; px < WH; px++) kept[px] = 0;
+        for (int S = 1; S <= 24 && room > 0; S++)
+            for (long long px = 0; px < WH && room > 0; px++)
+                if (want[px] >= S) kept[px] = S, room--;
+    }
+    if (adaptivePaths) *adaptivePaths = pathCount;
+    /* second wave (rendercore.cpp:682-713): slots in pixel order, S ascending within a pixel */
+    std::vector<long long> first(WH + 1, 0);
+    for (long long px = 0; px < WH; px++) first[px + 1] = first[px] + kept[px];
+    const long long n2 = first[WH];
+    std::vector<MisPath> extra(n2);
+    auto R0b = [&](int d) { return pass * 59071u + (uint)d * 31771u; };
+    parallel_for(WH, nthreads, 64, [&](long long b, long long e) {
+        std::vector<uint> ext(D, 0), shad(D, 0);
+        for (long long px = b; px < e; px++)
+            for (int S = 1; S <= kept[px]; S++) {
+                const uint thread = (uint)(px + (long long)(S - 1) * WH);
+                const uint pathIdx = (uint)(px + (long long)(S % spp) * WH);
+                f3 O, Dd;
+                primary_adaptive(F, (int)(px % W), (int)(px / W), (uint)S + (uint)spp + pass, thread, p->frameSeed, O, Dd);
+                trace_path_mis(F, MIS_ADAPTIVE, pathIdx, pass + (uint)spp, R0b, O, Dd, p->geometryEpsilon, extra[first[px] + S - 1], ext, shad,
+                               nullptr, -1, nullptr);
+            }
+        std::lock_guard<std::mutex> g(mtx);
+        for (int d = 0; d < D; d++) extTot[D + d] += ext[d], shadTot[D + d] += shad[d];
+    });
+    /* into the layers: the second-wave paths of layer i are those with S % spp == i, added in S order */
+    for (long long px = 0; px < WH; px++)
+        for (int S = 1; S <= kept[px]; S++) add4(&frameAcc[4 * (px + (S % spp) * WH)], extra[first[px] + S - 1].acc);
+    /* finalizeASRenderKernel (finalize_shared.h:71-93) after samplesTaken += spp */
+    const int frames = (p->samplesTaken + spp) / spp;
+    const float pixelValueScale = 1.0f / (float)frames;
+    for (long long px = 0; px < WH; px++) {
+        f4 q = mk4(0, 0, 0, 0);
+        for (int i = 0; i < spp; i++) q = q + ld4(&frameAcc[4 * (px + i * WH)]);
+        const f4 add = q * (1.0f / q.w);
+        float* a = accum + 4 * px;
+        add4(a, add);
+        if (frame) for (int k = 0; k < 4; k++) frame[4 * px + k] = a[k] * pixelValueScale;
+    }
+    if (counters) for (int d = 0; d < 2 * D; d++) counters[2 * d] = extTot[d], counters[2 * d + 1] = shadTot[d];
+    if (frameAccOut) memcpy(frameAccOut, frameAcc.data(), sizeof(float) * 4 * P);
+    if (featuresOut) memcpy(featuresOut, feat.data(), sizeof(float) * 4 * P);
+    if (deviationOut) memcpy(deviationOut, dev.data(), sizeof(float) * WH);
+    return 0;
 }
 
 int lh2o_svgf_frame(lh2o_svgf* f, const float* accum, const lh2g_filter_params* fp, int nthreads) {
@@ -1984,6 +2497,10 @@ void lh2o_svgf_view(const lh2g_view* v, int h, float* out16) {
     for (int k = 0; k < 4; k++) out16[4 * k] = q[k].x, out16[4 * k + 1] = q[k].y, out16[4 * k + 2] = q[k].z, out16[4 * k + 3] = q[k].w;
 }
 uint32_t lh2o_wanghash(uint32_t v) { return WangHash(v); }
+void lh2o_bluenoise4(const uint32_t* bn, int x, int y, int sampleIndex, int sampleDimension, float* out4) {
+    const f4 r = blueNoiseSampler4(bn, x, y, sampleIndex, sampleDimension);
+    out4[0] = r.x, out4[1] = r.y, out4[2] = r.z, out4[3] = r.w;
+}
 float lh2o_random_float(uint32_t* seed) { return RandomFloat(*seed); }
 void lh2o_random_barycentrics(float r0, float* o) { const f3 b = RandomBarycentrics(r0); o[0] = b.x, o[1] = b.y, o[2] = b.z; }
 uint32_t lh2o_pack_normal(const float* n) { return PackNormal(ld3(n)); }

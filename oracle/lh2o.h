@@ -12,6 +12,10 @@
  *   - shadow connections  lib/RenderCore_PrimeRef/kernels/connections.h:22-34
  *   - the wave loop       lib/RenderCore_PrimeRef/rendercore.cpp:535-632, run per path depth-first, which is
  *                         equivalent because every random number depends only on (path, depth).
+ * and, as other estimators, the OptiX 7 core's (lib/rendercore_optix7/kernels/pathtracer.h:54-238 with
+ * optix/.optix.cu:71-129: MIS, blue noise, path regularisation, one diffuse bounce) and the PrimeAdaptive core's
+ * adaptive frames (lib/RenderCore_PrimeAdaptive/rendercore.cpp:600-755, kernels/camera.h, kernels/pathtracer.h,
+ * lib/CUDA/shared_kernel_code/finalize_shared.h:71-151).
  * Ray traversal in the reference is closed NVIDIA code (OptiX / OptiX Prime), so the oracle brings its own
  * scalar binned-SAH BVH2 and a brute-force intersector; both return the closest hit with ties broken by the
  * lowest (instance, primitive).
@@ -58,6 +62,22 @@ int lh2o_trace_raw(lh2o_scene* s, const lh2g_ray* rays, long long n, float* t, i
  * per-depth hits and RNG states (maxDepth * W*H*spp entries each). Returns 0 on success. */
 int lh2o_render(lh2o_scene* s, const lh2g_view* view, const lh2g_render_params* p, float* pixelAccum,
                 double* pixelAccum64, uint32_t* counters, lh2g_capture* capture, int nthreads);
+
+/* Blue-noise tables of the OptiX 7 estimator (lib/RenderSystem/common_bluenoise.h layout, 8 bits per entry):
+ * sobol 256 x 256, scrambling and ranking 128 x 128 x 8 each. NULL pointers remove them. */
+int lh2o_set_blue_noise(lh2o_scene* s, const uint8_t* sobol, const uint8_t* scrambling, const uint8_t* ranking);
+
+/* One frame of the PrimeAdaptive core (lib/RenderCore_PrimeAdaptive/rendercore.cpp:600-755): spp samples per pixel
+ * with the OptiX 7 estimator, a per-pixel variance estimate scaled by *devScale, up to 24 more samples per pixel
+ * where it asks for them (at most W*H*spp in all; *devScale is then steered towards 91-98 % of that budget), and
+ * finalizeASRender: accum (W*H float4) += each pixel's samples divided by their count; frame (optional) =
+ * accum / frames. p->cameraR0 and p->frameSeed are the frame's two draws of RandomUInt(camRNGseed), p->shift the
+ * blue-noise shift. counters (optional, 4 * maxDepth): per path length the extension and connection counts of the
+ * first wave, then of the second. adaptivePaths: the second wave's path count. frameAccOut, featuresOut (W*H*spp
+ * float4) and deviationOut (W*H) are optional copies of the intermediate buffers; capture covers the first wave. */
+int lh2o_render_adaptive(lh2o_scene* s, const lh2g_view* view, const lh2g_render_params* p, float* accum, float* frame, float* devScale,
+                         uint32_t* counters, uint32_t* adaptivePaths, float* frameAccOut, float* featuresOut, float* deviationOut,
+                         lh2g_capture* capture, int nthreads);
 
 /* SVGF feature buffers of a LH2G_RP_FILTER frame, W*H entries each, written for the paths of sample 0 of a
  * frame with samplesTaken == 0 (RenderCore_Optix7Filter/kernels/pathtracer.h:95-232). features: uint4;
@@ -109,6 +129,8 @@ void lh2o_nrc_adam(float* p, float* m, float* v, const float* g, long long n, fl
 
 /* Small pure functions exported for the pinning tests against the reference's own headers. */
 uint32_t lh2o_wanghash(uint32_t s);
+/* blueNoiseSampler4 over an expanded table (5 * 65536 + 64 entries) */
+void lh2o_bluenoise4(const uint32_t* bn, int x, int y, int sampleIndex, int sampleDimension, float* out4);
 float lh2o_random_float(uint32_t* seed);
 void lh2o_random_barycentrics(float r0, float* out3);
 uint32_t lh2o_pack_normal(const float* n3);
