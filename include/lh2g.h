@@ -65,6 +65,12 @@ LH2G_API int lh2g_set_lights(lh2g_context* ctx, const lh2g_light_tri* tri, int n
                     const lh2g_spot_light* spot, int nspot, const lh2g_dir_light* dir, int ndir);
 /* SetSkyData (core_api_base.h:112): width*height RGB floats; worldToSky16 may be NULL (identity). */
 LH2G_API int lh2g_set_sky(lh2g_context* ctx, const float* rgb, int width, int height, const float* worldToSky16);
+/* Blue-noise tables of the OptiX 7 estimator (LH2G_RP_OPTIX7 and adaptive frames), in the layout of the Lighthouse 2
+ * RenderSystem's lib/RenderSystem/common_bluenoise.h read as bytes: sobol 256 x 256 (65536 bytes), scrambling and
+ * ranking 128 x 128 x 8 (131072 bytes each). The reference's OptiX 7 core compiles them in and expands them at Init
+ * (lib/rendercore_optix7/rendercore.cpp:247-256); this core takes them from its host. Without tables (or after a
+ * call with NULL pointers) every sample uses xorshift numbers, as the reference does for sample indices from 64 on. */
+LH2G_API int lh2g_set_blue_noise(lh2g_context* ctx, const uint8_t* sobol, const uint8_t* scrambling, const uint8_t* ranking);
 /* Setting (core_api_base.h:95): "epsilon", "clampValue", "maxDepth", "rrStartDepth", "nee", and the filter
  * core's "filter" (0/1, default 0), "TAA" (0/1, default 1), "clampDirect" (2.5), "clampIndirect" (15)
  * (lib/RenderCore_Optix7Filter/rendercore.cpp:674-677, rendercore.h:32-35). With "filter" on, lh2g_render
@@ -73,7 +79,10 @@ LH2G_API int lh2g_set_sky(lh2g_context* ctx, const float* rgb, int width, int he
  * run to their end in one persistent kernel; 0: one launch per stage and wave throughout) and "pipelineFrames"
  * (frames in flight, 0..4, default 4; 0 and 1 render one frame at a time; see lh2g_get_stream) and "waveOccupancy"
  * (fraction of the GPU the persistent wave kernels of one frame launch, (0, 1], default 1) and "sortConnections"
- * (1: group each wave's light connections by the light they sample before the any-hit queries; default 0). */
+ * (1: group each wave's light connections by the light they sample before the any-hit queries; default 0).
+ * Estimator of lh2g_render: "estimator" 0 (PrimeRef, default) or 1 (the OptiX 7 core's, LH2G_RP_OPTIX7; one camera
+ * seed drawn per wave of maxDepth, where the reference draws only for the waves its loop runs), "adaptive" 1
+ * (PrimeAdaptive frames, lh2g_render_adaptive). Both draw a blue-noise shift per frame from seed 0x11331445. */
 LH2G_API int lh2g_setting(lh2g_context* ctx, const char* name, float value);
 /* SetTarget (core_api_base.h:93), headless: the output is a device float4 buffer of width*height pixels. */
 LH2G_API int lh2g_set_target(lh2g_context* ctx, int width, int height, int spp);
@@ -87,6 +96,22 @@ LH2G_API int lh2g_render(lh2g_context* ctx, const lh2g_view* view, int converge)
  * receive per path length the extension and connection counts. */
 LH2G_API int lh2g_render_ex(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* params, int accumulate,
                    lh2g_hit* captureHits, uint32_t* captureSeeds, uint32_t* counters);
+/* One frame of the PrimeAdaptive core (lib/RenderCore_PrimeAdaptive/rendercore.cpp:600-755): the OptiX 7 estimator
+ * (LH2G_RP_OPTIX7's shading, with per-sample accumulators) over W*H*spp paths, each pixel's variance estimate
+ * (finalize_shared.h:97-151) scaled by devScale, up to 24 more samples per pixel where the estimate asks for them (at
+ * most W*H*spp in all; beyond that the requests of lower sample numbers, then of lower pixels, are kept), a second
+ * wave of those paths, and finalizeASRender: the accumulator gets each pixel's samples divided by their count
+ * (cleared first unless accumulate), the frame the accumulator divided by (samplesTaken + spp) / spp. devScale stays
+ * on the device and steers the next frame towards 91-98 % of the budget (initially 10, lh2g_set_adaptive_scale).
+ * params: flags LH2G_RP_NEE or 0; cameraR0 / frameSeed = the frame's two draws of RandomUInt(camRNGseed); shift =
+ * the shift draw; maxDepth <= 32. captureHits / captureSeeds cover the first wave (maxDepth * W*H*spp entries);
+ * counters (host, 4 * maxDepth) the first wave's then the second's per path length; stats (may be NULL): devScale for
+ * the next frame, the second wave's paths and the samples requested. With any of them the call waits. */
+typedef struct lh2g_adaptive_stats { float devScale; uint32_t adaptivePaths, requested; } lh2g_adaptive_stats;
+LH2G_API int lh2g_render_adaptive(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* params, int accumulate,
+                                  lh2g_hit* captureHits, uint32_t* captureSeeds, uint32_t* counters, lh2g_adaptive_stats* stats);
+/* devScale the next adaptive frame starts from (RenderCore_PrimeAdaptive/rendercore.h: 10) */
+LH2G_API int lh2g_set_adaptive_scale(lh2g_context* ctx, float devScale);
 /* lh2g_render_ex without captures, followed by an asynchronous copy of the finalized frame (W*H float4) into
  * hostFrame: returns once the work is queued; hostFrame holds the frame after lh2g_wait (or any call that waits for
  * the context). Consecutive calls overlap like other plain frames; the copy of one frame completes before the next

@@ -50,7 +50,8 @@ C_API = ["lh2g_create", "lh2g_destroy", "lh2g_last_error", "lh2g_set_geometry", 
          "lh2g_server_submit_trace", "lh2g_server_wait", "lh2g_server_release", "lh2g_server_get_stats", "lh2g_server_setting",
          "lh2g_nrc_create", "lh2g_nrc_destroy", "lh2g_nrc_last_error", "lh2g_nrc_get_spec", "lh2g_nrc_set_params", "lh2g_nrc_get_params",
          "lh2g_nrc_get_grads", "lh2g_nrc_infer", "lh2g_nrc_train", "lh2g_nrc_apply_update", "lh2g_nrc_infer_counted", "lh2g_nrc_train_counted",
-         "lh2g_nrc_last_loss", "lh2g_nrc_wait_selftest", "lh2g_render_nrc", "lh2g_nrc_infer_host", "lh2g_nrc_train_host"]
+         "lh2g_nrc_last_loss", "lh2g_nrc_wait_selftest", "lh2g_render_nrc", "lh2g_nrc_infer_host", "lh2g_nrc_train_host",
+         "lh2g_set_blue_noise", "lh2g_render_adaptive", "lh2g_set_adaptive_scale"]
 
 _lib = None
 
@@ -103,6 +104,9 @@ def load_library(path: str | None = None):
     lib.lh2g_read_filter_buffer.argtypes = [vp, i, vp]
     lib.lh2g_get_last_filter_frame.argtypes = [vp, vp, vp, vp]
     lib.lh2g_render_nrc.argtypes = [vp, vp, vp, vp, i, i, vp]
+    lib.lh2g_set_blue_noise.argtypes = [vp, vp, vp, vp]
+    lib.lh2g_render_adaptive.argtypes = [vp, vp, vp, i, vp, vp, vp, vp]
+    lib.lh2g_set_adaptive_scale.argtypes = [vp, f]
     if path is None:
         _lib = lib
     return lib
@@ -238,7 +242,36 @@ class RenderCore:
         if sc.sky is not None:
             rgb, w, h = sc.sky
             self.SetSkyData(rgb, w, h)
+        if sc.blue_noise is not None:
+            self.set_blue_noise(sc.blue_noise)
         self.FinalizeInstances()
+
+    def set_blue_noise(self, tables):
+        """Blue-noise tables (sobol 65536, scrambling 131072, ranking 131072 bytes) or None to remove them."""
+        if tables is None:
+            self._check(self.lib.lh2g_set_blue_noise(self.ctx, None, None, None), "set_blue_noise")
+            return
+        t = [np.ascontiguousarray(x, np.uint8) for x in tables]
+        assert [len(x) for x in t] == [65536, 131072, 131072]
+        self._check(self.lib.lh2g_set_blue_noise(self.ctx, _p(t[0]), _p(t[1]), _p(t[2])), "set_blue_noise")
+
+    def render_adaptive(self, view, params, accumulate=False, capture=False):
+        """One PrimeAdaptive frame (lh2g_render_adaptive); waits and returns the per-wave counters, the devScale for
+        the next frame, the second wave's path count and the samples requested (and first-wave captures)."""
+        D, P = int(params["maxDepth"]), int(params["width"]) * int(params["height"]) * int(params["spp"])
+        hits = np.zeros(D * P, S.HIT_DTYPE) if capture else None
+        seeds = np.zeros(D * P, np.uint32) if capture else None
+        cnt = np.zeros((2 * D, 2), np.uint32)
+        st = np.zeros(3, np.uint32)
+        self._check(self.lib.lh2g_render_adaptive(self.ctx, _p(np.ascontiguousarray(view)), _p(np.ascontiguousarray(params)), int(accumulate),
+                                                  _p(hits), _p(seeds), _p(cnt), _p(st)), "render_adaptive")
+        out = {"counters": cnt, "dev_scale": float(st[0:1].view(np.float32)[0]), "adaptive_paths": int(st[1]), "requested": int(st[2])}
+        if capture:
+            out["hits"], out["seeds"] = hits.reshape(D, P), seeds.reshape(D, P)
+        return out
+
+    def set_adaptive_scale(self, dev_scale):
+        self._check(self.lib.lh2g_set_adaptive_scale(self.ctx, float(dev_scale)), "set_adaptive_scale")
 
     def render_ex(self, view, params, accumulate=False, capture=False, counters=True):
         D, P = int(params["maxDepth"]), int(params["width"]) * int(params["height"]) * int(params["spp"])

@@ -160,6 +160,8 @@ struct lh2g_context {
     float4 *triL = nullptr, *ptL = nullptr, *spL = nullptr, *dirL = nullptr;
     int nTri = 0, nPt = 0, nSpot = 0, nDir = 0;
     float4* sky = nullptr;
+    float4* skySmall = nullptr;       /* the sky's 64x scaled-down copy (OptiX 7 estimator after a bounce) */
+    uint32_t* blueNoise = nullptr;    /* expanded blue-noise tables (lh2g_set_blue_noise) */
     int skyW = 0, skyH = 0;
     float w2s[16];
     /* acceleration structure */
@@ -244,6 +246,27 @@ struct lh2g_context {
     cudaEvent_t forkEv = nullptr, finEv = nullptr;
     bool finValid = false;
     static constexpr int64_t PIPE_MAX_PATHS = 8ll << 20;   /* larger targets render one frame at a time */
+    /* estimator of lh2g_render (setting "estimator": 0 PrimeRef, 1 OptiX 7; "adaptive" 1: PrimeAdaptive frames) and
+     * the OptiX 7 cores' blue-noise shift seed (rendercore.h: shiftSeed = 0x11331445, never reset) */
+    int estimator = 0, adaptive = 0;
+    uint32_t shiftSeed = 0x11331445u;
+    /* PrimeAdaptive frames: the second wave's per-slot radiance and layer, the first wave's features, per-pixel
+     * deviation / requested / kept counts and slots, scan scratch, the device state and the second wave's counters */
+    struct Adaptive {
+        float4* pathAcc2 = nullptr;
+        uint32_t* slotLayer = nullptr;
+        float4* features = nullptr;
+        float* deviation = nullptr;
+        uint32_t *want = nullptr, *tmp = nullptr, *rank = nullptr, *kept = nullptr, *first = nullptr, *sums = nullptr;
+        AdaptiveState* state = nullptr;
+        Counters* counters2 = nullptr;
+        AdaptiveState* hostState = nullptr;
+        Counters* hostCounters2 = nullptr;
+        int64_t cap = 0, pixels = 0;
+        float pendingScale = 10.0f;     /* devScale to start the next adaptive frame from (rendercore.h: 10) */
+        bool scaleDirty = true;
+        bool last = false;              /* the last frame was adaptive: its statistics include the second wave */
+    } ad;
 };
 
 namespace {
@@ -327,6 +350,19 @@ void free_target(lh2g_context* ctx) {
         dfree(n.rec), dfree(n.queries), dfree(n.qPath), dfree(n.pred), dfree(n.trainQ), dfree(n.trainT), dfree(n.counts);
         n.cap = 0;
     }
+    {
+        auto& a = ctx->ad;
+        dfree(a.pathAcc2), dfree(a.slotLayer), dfree(a.features), dfree(a.deviation), dfree(a.want), dfree(a.tmp), dfree(a.rank);
+        dfree(a.kept), dfree(a.first), dfree(a.sums), dfree(a.counters2);
+        if (a.state) {   /* keep devScale across a new target, as the reference's core does */
+            if (!a.scaleDirty && a.hostState) {
+                cudaMemcpy(a.hostState, a.state, sizeof(AdaptiveState), cudaMemcpyDeviceToHost);
+                a.pendingScale = a.hostState->devScale, a.scaleDirty = true;
+            }
+            dfree(a.state);
+        }
+        a.cap = 0, a.pixels = 0;
+    }
     ctx->cap = 0, ctx->pathAccCap = 0;
 }
 
@@ -391,6 +427,7 @@ SceneGPU scene_of(const lh2g_context* c) {
     S.triLights = c->triL, S.pointLights = c->ptL, S.spotLights = c->spL, S.dirLights = c->dirL;
     S.nTri = c->nTri, S.nPoint = c->nPt, S.nSpot = c->nSpot, S.nDir = c->nDir;
     S.skyPixels = c->sky, S.skyW = c->skyW, S.skyH = c->skyH;
+    S.skySmall = c->skySmall, S.blueNoise = c->blueNoise;
     for (int r = 0; r < 3; r++) S.worldToSky[r] = make_float4(c->w2s[4 * r], c->w2s[4 * r + 1], c->w2s[4 * r + 2], c->w2s[4 * r + 3]);
     return S;
 }
@@ -449,11 +486,14 @@ int lh2g_destroy(lh2g_context* ctx) {
         if (L.st) cudaStreamSynchronize(L.st);
     for (MeshDev& m : ctx->meshes) dfree(m.verts), dfree(m.tris);
     dfree(ctx->mats), dfree(ctx->texels), dfree(ctx->triL), dfree(ctx->ptL), dfree(ctx->spL), dfree(ctx->dirL), dfree(ctx->sky);
+    dfree(ctx->skySmall), dfree(ctx->blueNoise);
     dfree(ctx->pool), dfree(ctx->triData), dfree(ctx->instGPU), dfree(ctx->tlasPrims), dfree(ctx->instTris), dfree(ctx->instInvRows);
     dfree(ctx->traceFetch), dfree(ctx->hostRaysDev), dfree(ctx->hostOutDev);
     dfree(ctx->B.capHits), dfree(ctx->B.capSeeds);
     free_target(ctx);
     if (ctx->hostCounters) cudaFreeHost(ctx->hostCounters);
+    if (ctx->ad.hostState) cudaFreeHost(ctx->ad.hostState);
+    if (ctx->ad.hostCounters2) cudaFreeHost(ctx->ad.hostCounters2);
     for (NrcBuffers& n : ctx->nrcBuf)
         if (n.hostCounts) cudaFreeHost(n.hostCounts);
     if (ctx->cacheEv) cudaEventDestroy(ctx->cacheEv);
@@ -685,9 +725,44 @@ int lh2g_set_sky(lh2g_context* ctx, const float* rgb, int w, int h, const float*
     for (size_t i = 0; i < (size_t)w * h; i++) px[i] = make_float4(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2], 0.0f);
     CK(dalloc(ctx->sky, px.size()));
     CK(cudaMemcpyAsync(ctx->sky, px.data(), sizeof(float4) * px.size(), cudaMemcpyHostToDevice, ctx->st));
+    /* the average of every 64 x 64 tile, summed row by row (RenderCore::SetSkyData, rendercore_optix7/rendercore.cpp:726-737) */
+    const int sw = w >> 6, sh = h >> 6;
+    std::vector<float4> small((size_t)std::max(1, sw * sh), make_float4(0, 0, 0, 0));
+    for (int y = 0; y < sh; y++)
+        for (int x = 0; x < sw; x++) {
+            float tx = 0, ty = 0, tz = 0;
+            for (int v = 0; v < 64; v++)
+                for (int u = 0; u < 64; u++) {
+                    const float4& q = px[(size_t)(x * 64 + u) + (size_t)(y * 64 + v) * w];
+                    tx += q.x, ty += q.y, tz += q.z;
+                }
+            const float k = 1.0f / (64 * 64);
+            small[(size_t)x + (size_t)y * sw] = make_float4(tx * k, ty * k, tz * k, 0.0f);
+        }
+    CK(dalloc(ctx->skySmall, small.size()));
+    CK(cudaMemcpyAsync(ctx->skySmall, small.data(), sizeof(float4) * small.size(), cudaMemcpyHostToDevice, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     ctx->skyW = w, ctx->skyH = h;
     for (int i = 0; i < 16; i++) ctx->w2s[i] = m16 ? m16[i] : ((i % 5 == 0) ? 1.0f : 0.0f);
+    return LH2G_OK;
+}
+
+int lh2g_set_blue_noise(lh2g_context* ctx, const uint8_t* sobol, const uint8_t* scrambling, const uint8_t* ranking) {
+    if (!ctx) return LH2G_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    JOIN();
+    CK(cudaStreamSynchronize(ctx->st));
+    if (!sobol || !scrambling || !ranking) {
+        dfree(ctx->blueNoise);
+        return LH2G_OK;
+    }
+    /* one uint per entry as rendercore_optix7/rendercore.cpp:247-256 expands them, then 64 zeros: the ranking
+     * reads of deep path lengths at the last tile pixel reach past the tables (the reference reads past its buffer) */
+    std::vector<uint32_t> bn(65536 * 5 + 64, 0u);
+    for (int i = 0; i < 65536; i++) bn[i] = sobol[i];
+    for (int i = 0; i < 128 * 128 * 8; i++) bn[i + 65536] = scrambling[i], bn[i + 3 * 65536] = ranking[i];
+    CK(dalloc(ctx->blueNoise, bn.size()));
+    CK(cudaMemcpy(ctx->blueNoise, bn.data(), sizeof(uint32_t) * bn.size(), cudaMemcpyHostToDevice));
     return LH2G_OK;
 }
 
@@ -700,6 +775,10 @@ int lh2g_setting(lh2g_context* ctx, const char* name, float value) {
         ctx->maxDepth = (int)value;
     } else if (!strcmp(name, "rrStartDepth")) ctx->rrStart = (int)value;
     else if (!strcmp(name, "nee")) ctx->nee = value != 0.0f;
+    else if (!strcmp(name, "estimator")) {
+        if (value != 0.0f && value != 1.0f) return fail(ctx, LH2G_ERR_INVALID, "setting estimator: 0 (PrimeRef) or 1 (OptiX 7)");
+        ctx->estimator = (int)value;
+    } else if (!strcmp(name, "adaptive")) ctx->adaptive = value != 0.0f;
     else if (!strcmp(name, "waveTail")) {
         if (value < 0 || value > 65) return fail(ctx, LH2G_ERR_INVALID, "setting waveTail: 0 (off) or 1..65");
         ctx->tailDepth = (int)value;
@@ -856,6 +935,11 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
     cudaSetDevice(ctx->device);
     const bool filt = (p->flags & LH2G_RP_FILTER) != 0, nrcFrame = (p->flags & LH2G_RP_NRC) != 0;
     if (filt && nrcFrame) return fail(ctx, LH2G_ERR_INVALID, "render: filter and radiance-cache frames do not combine");
+    if (p->flags & LH2G_RP_ADAPTIVE) return fail(ctx, LH2G_ERR_INVALID, "render: adaptive frames go through lh2g_render_adaptive");
+    if ((p->flags & LH2G_RP_OPTIX7) && (filt || nrcFrame || (p->flags & LH2G_RP_DEPTH_W)))
+        return fail(ctx, LH2G_ERR_INVALID, "render: the OptiX 7 estimator combines with none of filter, radiance-cache or depth frames");
+    if ((p->flags & LH2G_RP_OPTIX7) && ctx->cap >= (1ll << MIS_SLOT_BITS))
+        return fail(ctx, LH2G_ERR_INVALID, "render: the OptiX 7 estimator takes at most 2^26 paths per frame");
     /* plain frames without host read-backs go to the next lane; everything else runs on the context stream after
      * the lanes' frames */
     const bool pipe = ctx->pipelineFrames > 1 && !filt && !capHits && !capSeeds && !countersOut && (!hook || hook->async) &&
@@ -925,7 +1009,10 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
     int li = 2 * ctx->timedLaunches;
     auto mark = [&]() { if (timing) cudaEventRecord(ctx->lev[li++], st); };
     CK(cudaEventRecord(fev[0], st));
-    mark(), launch_generate(F, B, st), mark();
+    mark();
+    if (p->flags & LH2G_RP_OPTIX7) launch_generate_mis(S, F, B, st);
+    else launch_generate(F, B, st);
+    mark();
     for (int d = 1; d <= waves; d++) {
         mark(), launch_extend(S, F, B, d, ctx->blocksExtend, st), mark();
         mark(), launch_shade(S, F, B, d, ctx->blocksShade, st), mark();
@@ -973,13 +1060,162 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
     return LH2G_OK;
 }
 
+/* buffers of PrimeAdaptive frames for the current target */
+int ensure_adaptive(lh2g_context* ctx) {
+    auto& a = ctx->ad;
+    const int64_t WH = (int64_t)ctx->W * ctx->H;
+    if (!a.hostState) {
+        CK(cudaMallocHost((void**)&a.hostState, sizeof(AdaptiveState)));
+        CK(cudaMallocHost((void**)&a.hostCounters2, sizeof(Counters)));
+    }
+    if (a.cap < ctx->cap || a.pixels < WH) {
+        dfree(a.pathAcc2), dfree(a.slotLayer), dfree(a.features), dfree(a.deviation), dfree(a.want), dfree(a.tmp), dfree(a.rank);
+        dfree(a.kept), dfree(a.first), dfree(a.sums), dfree(a.counters2);
+        const size_t P = (size_t)ctx->cap, n = (size_t)WH;
+        cudaError_t e = dalloc(a.pathAcc2, P);
+        if (!e) e = dalloc(a.slotLayer, P);
+        if (!e) e = dalloc(a.features, P);
+        if (!e) e = dalloc(a.deviation, n);
+        if (!e) e = dalloc(a.want, n);
+        if (!e) e = dalloc(a.tmp, n);
+        if (!e) e = dalloc(a.rank, n);
+        if (!e) e = dalloc(a.kept, n);
+        if (!e) e = dalloc(a.first, n);
+        if (!e) e = dalloc(a.sums, n / 4096 + 2);
+        if (!e) e = dalloc(a.counters2, 1);
+        if (!e && !a.state) e = dalloc(a.state, 1);
+        if (e) return cuda_check(ctx, e, "adaptive frame buffers");
+        a.cap = ctx->cap, a.pixels = WH;
+    }
+    if (a.scaleDirty) {
+        AdaptiveState init;
+        memset(&init, 0, sizeof(init));
+        init.devScale = a.pendingScale;
+        CK(cudaMemcpyAsync(a.state, &init, sizeof(init), cudaMemcpyHostToDevice, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        a.scaleDirty = false;
+    }
+    return LH2G_OK;
+}
+
+/* One PrimeAdaptive frame (lib/RenderCore_PrimeAdaptive/rendercore.cpp:600-713 and FinalizeRender :749-755) on the
+ * context stream: the first wave over the target's sample layers, the variance estimate, the second wave of
+ * adaptively placed samples, finalizeASRender. */
+int render_adaptive(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* p, int accumulate, lh2g_hit* capHits, uint32_t* capSeeds,
+                    uint32_t* countersOut, lh2g_adaptive_stats* statsOut) {
+    if (!ctx || !view || !p) return LH2G_ERR_INVALID;
+    if (!ctx->finalized) return fail(ctx, LH2G_ERR_STATE, "render: scene not finalized (call lh2g_finalize_instances)");
+    if (!ctx->cap) return fail(ctx, LH2G_ERR_STATE, "render: no target (call lh2g_set_target)");
+    if (p->width != ctx->W || p->height != ctx->H || p->spp != ctx->spp || p->maxDepth < 1 || p->maxDepth > 32)
+        return fail(ctx, LH2G_ERR_INVALID, "render_adaptive: parameters do not match the target (or maxDepth beyond 32)");
+    if (p->flags & ~LH2G_RP_NEE) return fail(ctx, LH2G_ERR_INVALID, "render_adaptive: only LH2G_RP_NEE combines with adaptive frames");
+    if (ctx->cap >= (1ll << MIS_SLOT_BITS)) return fail(ctx, LH2G_ERR_INVALID, "render_adaptive: at most 2^26 paths per frame");
+    if (!ctx->mats) return fail(ctx, LH2G_ERR_STATE, "render: no materials");
+    if (!materials_cover_meshes(ctx)) return fail(ctx, LH2G_ERR_INVALID, "render: a triangle's material index exceeds the material count");
+    cudaSetDevice(ctx->device);
+    JOIN();
+    {
+        const int r = ensure_adaptive(ctx);
+        if (r != LH2G_OK) return r;
+    }
+    auto& a = ctx->ad;
+    cudaStream_t st = ctx->st;
+    const SceneGPU S = scene_of(ctx);
+    FrameGPU F = frame_of(view, p);
+    F.stride = ctx->cap;
+    F.flags |= LH2G_RP_ADAPTIVE;
+    F.pass = (uint32_t)p->samplesTaken;
+    F.r0Base = (uint32_t)p->samplesTaken * 7907u, F.r0Depth = 91771u;
+    WaveBuffers B = ctx->B;
+    B.capHits = nullptr, B.capSeeds = nullptr;
+    B.features = nullptr, B.worldPos = nullptr, B.deltaDepth = nullptr, B.nrcRec = nullptr;
+    B.misFeatures = a.features, B.slotLayer = nullptr, B.firstCount = nullptr;
+    const size_t capN = (size_t)F.maxDepth * F.P;
+    if (capHits || capSeeds) {
+        CK(dalloc(ctx->B.capHits, capN));
+        CK(dalloc(ctx->B.capSeeds, capN));
+        std::vector<lh2g_hit> init(capN, lh2g_hit{0u, -1, -2, 0.0f});
+        CK(cudaMemcpyAsync(ctx->B.capHits, init.data(), sizeof(lh2g_hit) * capN, cudaMemcpyHostToDevice, st));
+        CK(cudaMemsetAsync(ctx->B.capSeeds, 0, sizeof(uint32_t) * capN, st));
+        B.capHits = ctx->B.capHits, B.capSeeds = ctx->B.capSeeds;
+    }
+    const int waves = ctx->tailDepth > 0 ? std::min(F.maxDepth, ctx->tailDepth - 1) : F.maxDepth;
+    auto run_waves = [&](const FrameGPU& Fw, const WaveBuffers& Bw) {
+        for (int d = 1; d <= waves; d++) {
+            launch_extend(S, Fw, Bw, d, ctx->blocksExtend, st);
+            launch_shade(S, Fw, Bw, d, ctx->blocksShade, st);
+            launch_connect(S, Fw, Bw, d, ctx->blocksConnect, st);
+        }
+        if (waves < Fw.maxDepth) launch_tail(S, Fw, Bw, waves + 1, ctx->blocksTail, st);
+    };
+    CK(cudaEventRecord(ctx->ev[0], st));
+    /* first wave */
+    CK(cudaMemsetAsync(B.counters, 0, sizeof(Counters), st));
+    launch_generate_mis(S, F, B, st);
+    run_waves(F, B);
+    /* variance estimate, budget, kept samples and their slots */
+    CK(cudaMemsetAsync(a.state->hist, 0, sizeof(a.state->hist), st));
+    launch_adaptive_estimate(F, B, a.deviation, a.want, a.state, st);
+    launch_adaptive_keep(F, a.want, a.tmp, a.rank, a.kept, a.first, a.sums, a.state, st);
+    /* second wave: pass samplesTaken + spp, shading seeds samplesTaken * 59071 + depth * 31771 (rendercore.cpp:689-691) */
+    FrameGPU F2 = F;
+    F2.pass = (uint32_t)(p->samplesTaken + p->spp);
+    F2.r0Base = (uint32_t)p->samplesTaken * 59071u, F2.r0Depth = 31771u;
+    WaveBuffers B2 = B;
+    B2.pathAcc = a.pathAcc2, B2.slotLayer = a.slotLayer, B2.misFeatures = nullptr, B2.firstCount = &a.state->pathCount;
+    B2.counters = a.counters2, B2.capHits = nullptr, B2.capSeeds = nullptr;
+    CK(cudaMemsetAsync(B2.counters, 0, sizeof(Counters), st));
+    launch_adaptive_generate(S, F2, B2, a.kept, a.first, a.slotLayer, p->frameSeed, st);
+    run_waves(F2, B2);
+    /* finalizeASRender after samplesTaken += spp */
+    const int frames = (p->samplesTaken + p->spp) / p->spp;
+    launch_adaptive_finalize(F, B.pathAcc, a.pathAcc2, a.kept, a.first, B.accum, B.frame, 1.0f / (float)frames, accumulate ? 0 : 1, st);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev[1], st));
+    CK(cudaMemcpyAsync(ctx->hostCounters, B.counters, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(a.hostCounters2, a.counters2, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(a.hostState, a.state, sizeof(AdaptiveState), cudaMemcpyDeviceToHost, st));
+    ctx->statsPending = true, ctx->lastDepth = F.maxDepth, ctx->lastP = F.P, ctx->lastSlot = -1;
+    a.last = true;
+    if (capHits || capSeeds || countersOut || statsOut) {
+        CK(cudaStreamSynchronize(st));
+        if (capHits) CK(cudaMemcpy(capHits, ctx->B.capHits, sizeof(lh2g_hit) * capN, cudaMemcpyDeviceToHost));
+        if (capSeeds) CK(cudaMemcpy(capSeeds, ctx->B.capSeeds, sizeof(uint32_t) * capN, cudaMemcpyDeviceToHost));
+        if (countersOut)
+            for (int d = 0; d < F.maxDepth; d++) {
+                countersOut[2 * d] = ctx->hostCounters->extension[d], countersOut[2 * d + 1] = ctx->hostCounters->shadow[d];
+                countersOut[2 * (F.maxDepth + d)] = a.hostCounters2->extension[d];
+                countersOut[2 * (F.maxDepth + d) + 1] = a.hostCounters2->shadow[d];
+            }
+        if (statsOut) {
+            statsOut->devScale = a.hostState->devScale;
+            statsOut->adaptivePaths = a.hostState->pathCount;
+            statsOut->requested = a.hostState->requested;
+        }
+        if (ctx->hostCounters->status | a.hostCounters2->status) return fail(ctx, LH2G_ERR_OVERFLOW, "render: traversal stack overflow or step limit");
+    }
+    return LH2G_OK;
+}
+
 }  // namespace
 
 extern "C" {
 
 int lh2g_render_ex(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* p, int accumulate, lh2g_hit* capHits, uint32_t* capSeeds,
                    uint32_t* countersOut) {
+    if (ctx) ctx->ad.last = false;
     return render_frame(ctx, view, p, accumulate, capHits, capSeeds, countersOut, nullptr);
+}
+
+int lh2g_render_adaptive(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* p, int accumulate, lh2g_hit* capHits,
+                         uint32_t* capSeeds, uint32_t* counters, lh2g_adaptive_stats* stats) {
+    return render_adaptive(ctx, view, p, accumulate, capHits, capSeeds, counters, stats);
+}
+
+int lh2g_set_adaptive_scale(lh2g_context* ctx, float devScale) {
+    if (!ctx || !(devScale > 0.0f)) return LH2G_ERR_INVALID;
+    ctx->ad.pendingScale = devScale, ctx->ad.scaleDirty = true;
+    return LH2G_OK;
 }
 
 int lh2g_render_to_host(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* p, int accumulate, float* hostFrame) {
@@ -1169,10 +1405,29 @@ int lh2g_render(lh2g_context* ctx, const lh2g_view* view, int converge) {
     memset(&p, 0, sizeof(p));
     p.width = ctx->W, p.height = ctx->H, p.spp = ctx->spp, p.maxDepth = ctx->maxDepth, p.rrStartDepth = ctx->rrStart;
     p.samplesTaken = ctx->samplesTaken;
-    p.cameraR0 = xorshift(ctx->camSeed);
     p.geometryEpsilon = ctx->eps, p.clampValue = ctx->clampValue;
-    p.flags = (ctx->nee ? LH2G_RP_NEE : 0) | LH2G_RP_DEPTH_W;
-    const int r = lh2g_render_ex(ctx, view, &p, ctx->samplesTaken > 0 ? 1 : 0, nullptr, nullptr, nullptr);
+    int r;
+    if (ctx->adaptive) {
+        /* RenderCore_PrimeAdaptive/rendercore.cpp:606-609: one shift draw, then two camera draws per frame */
+        p.shift = xorshift(ctx->shiftSeed);
+        p.cameraR0 = xorshift(ctx->camSeed);
+        p.frameSeed = xorshift(ctx->camSeed);
+        p.maxDepth = std::min(ctx->maxDepth, 32);
+        p.flags = ctx->nee ? LH2G_RP_NEE : 0;
+        r = lh2g_render_adaptive(ctx, view, &p, ctx->samplesTaken > 0 ? 1 : 0, nullptr, nullptr, nullptr, nullptr);
+    } else if (ctx->estimator == 1) {
+        /* rendercore_optix7/rendercore.cpp:855,900: one shift draw per frame, one camera draw per wave (here every
+         * wave of maxDepth is drawn for, also where the reference's loop ends early) */
+        p.shift = xorshift(ctx->shiftSeed);
+        p.cameraR0 = xorshift(ctx->camSeed);
+        for (int d = 1; d < p.maxDepth; d++) xorshift(ctx->camSeed);
+        p.flags = (ctx->nee ? LH2G_RP_NEE : 0) | LH2G_RP_OPTIX7;
+        r = lh2g_render_ex(ctx, view, &p, ctx->samplesTaken > 0 ? 1 : 0, nullptr, nullptr, nullptr);
+    } else {
+        p.cameraR0 = xorshift(ctx->camSeed);
+        p.flags = (ctx->nee ? LH2G_RP_NEE : 0) | LH2G_RP_DEPTH_W;
+        r = lh2g_render_ex(ctx, view, &p, ctx->samplesTaken > 0 ? 1 : 0, nullptr, nullptr, nullptr);
+    }
     if (r == LH2G_OK) ctx->samplesTaken += ctx->spp;
     return r;
 }
@@ -1193,8 +1448,15 @@ int lh2g_get_stats(lh2g_context* ctx, lh2g_stats* out) {
         const Counters& C = lane ? *ctx->lanes[ctx->lastSlot].hostCounters : *ctx->hostCounters;
         uint32_t ext = (uint32_t)ctx->lastP, sh = 0;
         for (int d = 0; d < ctx->lastDepth; d++) ext += C.extension[d], sh += C.shadow[d];
+        uint32_t primary = (uint32_t)ctx->lastP;
+        if (ctx->ad.last) {   /* an adaptive frame: its second wave's rays too */
+            const Counters& C2 = *ctx->ad.hostCounters2;
+            const uint32_t n2 = ctx->ad.hostState->pathCount;
+            ext += n2, primary += n2;
+            for (int d = 0; d < ctx->lastDepth; d++) ext += C2.extension[d], sh += C2.shadow[d];
+        }
         ctx->stats.totalExtensionRays = ext, ctx->stats.totalShadowRays = sh, ctx->stats.totalRays = ext + sh;
-        ctx->stats.primaryRayCount = (uint32_t)ctx->lastP;
+        ctx->stats.primaryRayCount = primary;
         ctx->stats.bounce1RayCount = ctx->lastDepth > 1 ? C.extension[0] : 0;
         uint32_t deep = 0;
         for (int d = 1; d < ctx->lastDepth - 1; d++) deep += C.extension[d];
@@ -1337,6 +1599,7 @@ FrameGPU frame_of(const lh2g_view* view, const lh2g_render_params* p) {
     F.up = make_float3(view->p3[0] - view->p1[0], view->p3[1] - view->p1[1], view->p3[2] - view->p1[2]);
     F.P = (int64_t)F.W * F.H * F.spp;
     F.stride = F.P;
+    F.distortion = view->distortion, F.shift = p->shift, F.pass = (uint32_t)p->samplesTaken, F.clampValue = p->clampValue;
     return F;
 }
 

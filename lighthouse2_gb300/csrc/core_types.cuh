@@ -61,6 +61,8 @@ struct SceneGPU {
     const float4* skyPixels;
     int skyW, skyH;
     float4 worldToSky[3];            /* rows of the 3x3 part */
+    const float4* skySmall;          /* (skyW >> 6) x (skyH >> 6) tile averages, read by the OptiX 7 estimator after a bounce */
+    const uint32_t* blueNoise;       /* expanded blue-noise tables (5 * 65536 + 64 entries); null: xorshift numbers only */
 };
 
 /* Per-frame parameters. */
@@ -74,6 +76,12 @@ struct FrameGPU {
     float3 pos, p1, right, up;
     int64_t P;                       /* paths in the frame */
     int64_t stride;                  /* capacity of the SoA buffers */
+    /* the OptiX 7 / PrimeAdaptive estimators (LH2G_RP_OPTIX7, LH2G_RP_ADAPTIVE) */
+    uint32_t shift;                  /* blue-noise tile shift */
+    uint32_t pass;                   /* the shading kernel's 'pass' (sample index of layer 0) */
+    uint32_t r0Base, r0Depth;        /* PrimeAdaptive shading seed: r0Base + depth * r0Depth */
+    float clampValue;
+    float distortion;
 };
 
 /* Device counters of one frame. extension[d] counts extension rays written while shading path length
@@ -88,6 +96,12 @@ struct Counters {
     unsigned long long travStats[4];   /* extend: nodes, triangles; connect: nodes, triangles */
     uint32_t hitCount[64], missCount[64];   /* per path length: queue slots placed in the shading order so far */
 };
+
+/* Path flags. The OptiX 7 / PrimeAdaptive estimators keep them in the low 6 bits of O4.w, above them the path's
+ * slot: bits 0-3 the reference's S_* flags, bits 4-5 the ray's tmin (0: 0, 1: the geometry epsilon, 2: EPSILON) */
+constexpr uint32_t S_BOUNCEDTWICE = 8;   /* (S_SPECULAR 1, S_BOUNCED 2 and S_VIASPECULAR 4 as in the other estimators) */
+constexpr uint32_t MIS_TMIN_SHIFT = 4, MIS_TMIN_EPS = 1u << 4, MIS_TMIN_EPSILON = 2u << 4;
+constexpr int MIS_SLOT_BITS = 26;   /* slots below 2^26 (67M paths) */
 
 #define LH2G_STATUS_STACK_OVERFLOW 1u
 #define LH2G_STATUS_TRAVERSAL_LIMIT 2u

@@ -139,6 +139,11 @@ LH2G_DEV float acos_at(float x) {
 /* ---- random numbers (the reference's WangHash seeding and Marsaglia xorshift32) ---- */
 LH2G_DEV uint32_t WangHash(uint32_t s) { s = (s ^ 61u) ^ (s >> 16), s *= 9u, s = s ^ (s >> 4), s *= 0x27d4eb2du, s = s ^ (s >> 15); return s; }
 LH2G_DEV uint32_t RandomInt(uint32_t& s) { s ^= s << 13, s ^= s >> 17, s ^= s << 5; return s; }
+/* the n-th xorshift32 successor of x (RandomUInt applied n times) */
+LH2G_DEV uint32_t xorshift_n(uint32_t x, const int n) {
+    for (int i = 0; i < n; i++) x ^= x << 13, x ^= x >> 17, x ^= x << 5;
+    return x;
+}
 LH2G_DEV float RandomFloat(uint32_t& s) { return __uint2float_rn(RandomInt(s)) * 2.3283064365387e-10f; }
 
 LH2G_DEV float half2float(uint32_t h) { return __half2float(__ushort_as_half((unsigned short)h)); }

@@ -34,8 +34,25 @@ __global__ void __launch_bounds__(256) k_generate(const FrameGPU F, const WaveBu
     if (F.flags & LH2G_RP_FILTER) B.pathAcc[i + F.P] = make_float4(0, 0, 0, 0);
     if (F.flags & LH2G_RP_NRC) B.nrcRec[i + 4 * F.P] = make_float4(0, 0, 0, 0);   /* no cache query yet */
 }
-__device__ __forceinline__ uint32_t queue_count(const FrameGPU& F, const Counters* C, int depth) {
-    return depth == 1 ? (uint32_t)F.P : C->extension[depth - 2];
+/* primary rays of the OptiX 7 estimator, or the first wave of a PrimeAdaptive frame (sample layers of W*H paths) */
+__global__ void __launch_bounds__(256) k_generate_mis(const SceneGPU S, const FrameGPU F, const WaveBuffers B) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= F.P) return;
+    float3 O, D;
+    const bool adaptive = (F.flags & LH2G_RP_ADAPTIVE) != 0;
+    if (adaptive) {
+        const uint32_t row = (uint32_t)i / (uint32_t)F.W;
+        primary_adaptive(S, F, (int)((uint32_t)i % (uint32_t)F.W), (int)(row % (uint32_t)F.H), F.pass + row / (uint32_t)F.H, (uint32_t)i, F.cameraR0, O, D);
+    } else {
+        primary_optix7(S, F, (uint32_t)i, O, D);
+    }
+    B.O[0][i] = make_float4(O.x, O.y, O.z, __uint_as_float(((uint32_t)i << 6) | S_SPECULAR | MIS_TMIN_EPS));
+    B.D[0][i] = make_float4(D.x, D.y, D.z, __uint_as_float(0u));
+    B.T[0][i] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+    B.pathAcc[i] = make_float4(0.0f, 0.0f, 0.0f, adaptive ? 1.0f : 0.0f);   /* PrimeAdaptive: w counts the pixel's samples */
+}
+__device__ __forceinline__ uint32_t queue_count(const FrameGPU& F, const WaveBuffers& B, const Counters* C, int depth) {
+    return depth == 1 ? (B.firstCount ? *B.firstCount : (uint32_t)F.P) : C->extension[depth - 2];
 }
 
 /* -------------------------------------------------------------------------------------------------- */
@@ -49,9 +66,10 @@ __device__ __forceinline__ uint32_t queue_count(const FrameGPU& F, const Counter
 #else
 #define LH2G_TRAV_BOUNDS __launch_bounds__(128)
 #endif
+template <bool MIS>
 __global__ void LH2G_TRAV_BOUNDS k_extend(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int depth) {
     Counters* C = B.counters;
-    const uint32_t count = queue_count(F, C, depth);
+    const uint32_t count = queue_count(F, B, C, depth);
     const int q = (depth - 1) & 1;
     const float4* __restrict__ O4 = B.O[q];
     const float4* __restrict__ D4 = B.D[q];
@@ -65,7 +83,7 @@ __global__ void LH2G_TRAV_BOUNDS k_extend(const SceneGPU S, const FrameGPU F, co
         else rec = make_float4(__uint_as_float(0u), __int_as_float(0), __int_as_float(NOHIT), 1e34f);
         B.hits[i] = rec;
         if (B.capHits) {
-            const uint32_t pathIdx = __float_as_uint(O4[i].w);
+            const uint32_t pathIdx = MIS ? __float_as_uint(O4[i].w) >> 6 : __float_as_uint(O4[i].w);
             lh2g_hit c;
             c.bary = __float_as_uint(rec.x), c.inst = __float_as_int(rec.y), c.prim = __float_as_int(rec.z), c.t = rec.w;
             B.capHits[(size_t)(depth - 1) * F.P + pathIdx] = c;
@@ -73,7 +91,12 @@ __global__ void LH2G_TRAV_BOUNDS k_extend(const SceneGPU S, const FrameGPU F, co
     };
     trace_queue_any<false>(S, &C->fetch[depth - 1], count, status, stackBase,
         [&](uint32_t i, float3& o, float3& d, float& t0, float& t1) {
-            o = xyz(O4[i]), d = xyz(D4[i]), t0 = T4[i].w, t1 = 1e34f;
+            if (MIS) {
+                const float4 a = O4[i];
+                o = xyz(a), d = xyz(D4[i]), t0 = mis_tmin(__float_as_uint(a.w), F.eps), t1 = 1e34f;
+            } else {
+                o = xyz(O4[i]), d = xyz(D4[i]), t0 = T4[i].w, t1 = 1e34f;
+            }
         },
         [&](uint32_t i, const Traversal& tr, bool) { write(i, tr.found, tr.best); },
         [&](uint32_t i, const CoopRay& tr, bool) { if ((threadIdx.x & (COOP - 1)) == 0) write(i, tr.found, tr.best); },
@@ -82,16 +105,18 @@ __global__ void LH2G_TRAV_BOUNDS k_extend(const SceneGPU S, const FrameGPU F, co
 }
 
 /* -------------------------------------------------------------------------------------------------- */
+template <bool MIS>
 __device__ __forceinline__ void shade_path(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, const int depth, const uint32_t i, ShadeOut& out,
                                            float* pot) {
     const int q = (depth - 1) & 1;
-    shade_core(S, F, B, depth, B.O[q][i], B.D[q][i], B.T[q][i], B.hits[i], out, pot);
+    if (MIS) shade_mis(S, F, B, depth, B.O[q][i], B.D[q][i], B.T[q][i], B.hits[i], out, pot);
+    else shade_core(S, F, B, depth, B.O[q][i], B.D[q][i], B.T[q][i], B.hits[i], out, pot);
 }
 
 /* the shading order of the extension queue of path length `depth` (partition_queue) */
 __global__ void __launch_bounds__(PART_TILE) k_partition(const FrameGPU F, const WaveBuffers B, const int depth) {
     Counters* C = B.counters;
-    partition_queue(B.hits, queue_count(F, C, depth), B.order, &C->hitCount[depth - 1], &C->missCount[depth - 1]);
+    partition_queue(B.hits, queue_count(F, B, C, depth), B.order, &C->hitCount[depth - 1], &C->missCount[depth - 1]);
 }
 
 /* tuning switch: resident CTAs per SM the shading kernel is compiled for (register cap; 6: 80 registers and a
@@ -100,12 +125,14 @@ __global__ void __launch_bounds__(PART_TILE) k_partition(const FrameGPU F, const
 #define LH2G_SHADE_MINBLOCKS 6
 #endif
 #if LH2G_SHADE_MINBLOCKS > 0
+template <bool MIS>
 __global__ void __launch_bounds__(WAVE_BLOCK, LH2G_SHADE_MINBLOCKS) k_shade(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int depth) {
 #else
+template <bool MIS>
 __global__ void __launch_bounds__(WAVE_BLOCK) k_shade(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int depth) {
 #endif
     Counters* C = B.counters;
-    const uint32_t count = queue_count(F, C, depth);
+    const uint32_t count = queue_count(F, B, C, depth);
     const int nq = depth & 1;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -114,7 +141,7 @@ __global__ void __launch_bounds__(WAVE_BLOCK) k_shade(const SceneGPU S, const Fr
         const uint32_t i = base + threadIdx.x;
         ShadeOut out;
         out.ext = out.shadow = false;
-        if (i < count) shade_path(S, F, B, depth, B.order ? __ldg(B.order + i) : i, out, potential + threadIdx.x);
+        if (i < count) shade_path<MIS>(S, F, B, depth, B.order ? __ldg(B.order + i) : i, out, potential + threadIdx.x);
         const uint32_t em = __ballot_sync(0xffffffffu, out.ext);
         if (em) {
             const int leader = __ffs(em) - 1;
@@ -141,9 +168,10 @@ __global__ void __launch_bounds__(WAVE_BLOCK) k_shade(const SceneGPU S, const Fr
  * the connection's any-hit query and its contribution, the next segment. Every per-path quantity (RNG states,
  * hit records, radiance and its order of accumulation, queue counts per path length) is the one the wave loop
  * produces. */
+template <bool MIS>
 __global__ void __launch_bounds__(WAVE_BLOCK) k_tail(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int startDepth) {
     Counters* C = B.counters;
-    const uint32_t count = queue_count(F, C, startDepth);
+    const uint32_t count = queue_count(F, B, C, startDepth);
     const int q = (startDepth - 1) & 1;
     __shared__ float potential[64 * WAVE_BLOCK];
     float* pot = potential + threadIdx.x;
@@ -156,7 +184,7 @@ __global__ void __launch_bounds__(WAVE_BLOCK) k_tail(const SceneGPU S, const Fra
         float4 o4 = B.O[q][i], d4 = B.D[q][i], t4 = B.T[q][i];
         for (int depth = startDepth; depth <= F.maxDepth; depth++) {
             Traversal tr;
-            tr.begin(S, xyz(o4), xyz(d4), t4.w, 1e34f);
+            tr.begin(S, xyz(o4), xyz(d4), MIS ? mis_tmin(__float_as_uint(o4.w), F.eps) : t4.w, 1e34f);
             bool any = false;
             if (S.tlasRoot != 0xffffffffu)
                 while (tr.step<false>(S, status, any)) {}
@@ -165,15 +193,16 @@ __global__ void __launch_bounds__(WAVE_BLOCK) k_tail(const SceneGPU S, const Fra
             if (B.capHits) {
                 lh2g_hit c;
                 c.bary = __float_as_uint(hit.x), c.inst = __float_as_int(hit.y), c.prim = __float_as_int(hit.z), c.t = hit.w;
-                B.capHits[(size_t)(depth - 1) * F.P + __float_as_uint(o4.w)] = c;
+                B.capHits[(size_t)(depth - 1) * F.P + (MIS ? __float_as_uint(o4.w) >> 6 : __float_as_uint(o4.w))] = c;
             }
             ShadeOut out;
             out.ext = out.shadow = false;
-            shade_core(S, F, B, depth, o4, d4, t4, hit, out, pot);
+            if (MIS) shade_mis(S, F, B, depth, o4, d4, t4, hit, out, pot);
+            else shade_core(S, F, B, depth, o4, d4, t4, hit, out, pot);
             if (out.shadow) {
                 atomicAdd(&C->shadow[depth - 1], 1u);
                 Traversal sh;
-                sh.begin(S, xyz(out.sO), xyz(out.sD), 0.0f, out.sD.w);
+                sh.begin(S, xyz(out.sO), xyz(out.sD), (MIS && (F.flags & LH2G_RP_OPTIX7)) ? F.eps : 0.0f, out.sD.w);
                 bool occluded = false;
                 if (S.tlasRoot != 0xffffffffu)
                     while (sh.step<true>(S, status, occluded)) {}
@@ -182,6 +211,7 @@ __global__ void __launch_bounds__(WAVE_BLOCK) k_tail(const SceneGPU S, const Fra
                     float4* accP = B.pathAcc + ((__float_as_uint(out.sE.w) & 1u) ? F.P : 0) + __float_as_uint(out.sO.w);
                     float4 acc = *accP;
                     acc.x += out.sE.x, acc.y += out.sE.y, acc.z += out.sE.z;
+                    if (MIS && (F.flags & LH2G_RP_OPTIX7)) acc.w += 1.0f;   /* the OptiX 7 core counts connections in w */
                     *accP = acc;
                 }
             }
@@ -201,18 +231,20 @@ __global__ void LH2G_TRAV_BOUNDS k_connect(const SceneGPU S, const FrameGPU F, c
     const uint32_t count = C->shadow[depth - 1];
     uint32_t status = 0;
     __shared__ uint2 stackBase[LH2G_COOP ? 128 / COOP * COOP_STACK : 1];
+    const bool optix7 = (F.flags & LH2G_RP_OPTIX7) != 0;   /* tmin epsilon, and a count of the connections in w */
     auto add = [&](uint32_t i) {
         const float4 e = B.shE[i];
         const uint32_t pathIdx = __float_as_uint(B.shO[i].w);
         float4* accP = B.pathAcc + ((__float_as_uint(e.w) & 1u) ? F.P : 0) + pathIdx;   /* e.w bit 0: indirect half */
         float4 acc = *accP;
         acc.x += e.x, acc.y += e.y, acc.z += e.z;
+        if (optix7) acc.w += 1.0f;
         *accP = acc;
     };
     trace_queue_any<true>(S, &C->fetch[64 + depth - 1], count, status, stackBase,
         [&](uint32_t i, float3& o, float3& d, float& t0, float& t1) {
             const float4 d4 = B.shD[i];
-            o = xyz(B.shO[i]), d = xyz(d4), t0 = 0.0f, t1 = d4.w;
+            o = xyz(B.shO[i]), d = xyz(d4), t0 = optix7 ? F.eps : 0.0f, t1 = d4.w;
         },
         [&](uint32_t i, const Traversal&, bool occluded) { if (!occluded) add(i); },
         [&](uint32_t i, const CoopRay&, bool occluded) { if (!occluded && (threadIdx.x & (COOP - 1)) == 0) add(i); },
@@ -416,33 +448,40 @@ int persistent_blocks_trace(int mode) {
 
 int persistent_blocks_wave(int which) {
     int per = 0;
-    if (which == 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_extend, 128, 0);
+    if (which == 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_extend<false>, 128, 0);
     else if (which == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_connect, 128, 0);
     else if (which == 2) {
         /* the grid the registers allow; the potentials' shared memory grows with the scene's lights, and as the
          * shading loop is grid-stride, blocks beyond what shared memory lets reside simply start later */
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_shade, WAVE_BLOCK, WAVE_BLOCK * sizeof(float));
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_shade<false>, WAVE_BLOCK, WAVE_BLOCK * sizeof(float));
     }
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_tail, WAVE_BLOCK, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_tail<false>, WAVE_BLOCK, 0);
     return sm_count() * (per > 0 ? per : 1);
 }
 
+constexpr int MIS_FLAGS = LH2G_RP_OPTIX7 | LH2G_RP_ADAPTIVE;
 void launch_generate(const FrameGPU& F, const WaveBuffers& B, cudaStream_t st) {
     k_generate<<<(unsigned)((F.P + 255) / 256), 256, 0, st>>>(F, B);
 }
+void launch_generate_mis(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, cudaStream_t st) {
+    k_generate_mis<<<(unsigned)((F.P + 255) / 256), 256, 0, st>>>(S, F, B);
+}
 void launch_extend(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int blocks, cudaStream_t st) {
-    k_extend<<<blocks, 128, 0, st>>>(S, F, B, depth);
+    if (F.flags & MIS_FLAGS) k_extend<true><<<blocks, 128, 0, st>>>(S, F, B, depth);
+    else k_extend<false><<<blocks, 128, 0, st>>>(S, F, B, depth);
 }
 void launch_shade(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int blocks, cudaStream_t st) {
     if (B.order) k_partition<<<sm_count() * 4, PART_TILE, 0, st>>>(F, B, depth);
     const int lights = std::max(1, S.nTri + S.nPoint + S.nSpot + S.nDir);   /* at most 64 (lh2g_set_lights) */
-    k_shade<<<blocks, WAVE_BLOCK, (size_t)lights * WAVE_BLOCK * sizeof(float), st>>>(S, F, B, depth);
+    if (F.flags & MIS_FLAGS) k_shade<true><<<blocks, WAVE_BLOCK, (size_t)lights * WAVE_BLOCK * sizeof(float), st>>>(S, F, B, depth);
+    else k_shade<false><<<blocks, WAVE_BLOCK, (size_t)lights * WAVE_BLOCK * sizeof(float), st>>>(S, F, B, depth);
 }
 void launch_connect(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int blocks, cudaStream_t st) {
     k_connect<<<blocks, 128, 0, st>>>(S, F, B, depth);
 }
 void launch_tail(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int startDepth, int blocks, cudaStream_t st) {
-    k_tail<<<blocks, WAVE_BLOCK, 0, st>>>(S, F, B, startDepth);
+    if (F.flags & MIS_FLAGS) k_tail<true><<<blocks, WAVE_BLOCK, 0, st>>>(S, F, B, startDepth);
+    else k_tail<false><<<blocks, WAVE_BLOCK, 0, st>>>(S, F, B, startDepth);
 }
 void launch_nrc_collect(const FrameGPU& F, const WaveBuffers& B, float4* queries, uint32_t* qPath, float4* trainQ, float4* trainT, uint32_t* counts,
                         uint32_t trainCap, cudaStream_t st) {

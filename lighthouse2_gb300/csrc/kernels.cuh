@@ -30,9 +30,16 @@ struct WaveBuffers {
     uint32_t* connBins;    /* 64 per-light counts, then their running offsets */
     uint32_t* order = nullptr;   /* shading order of the extension queue: the slots whose ray hit something first,
                                   * those that missed after them (null: queue order) */
+    /* the OptiX 7 / PrimeAdaptive estimators */
+    const uint32_t* slotLayer = nullptr;   /* adaptive second wave: the sample layer (pathIdx) each slot shades as */
+    float4* misFeatures = nullptr;         /* adaptive first wave: albedo + packed normal per sample (variance estimate) */
+    const uint32_t* firstCount = nullptr;  /* paths in the first queue when a device count gives it (else F.P) */
 };
 
 void launch_generate(const FrameGPU& F, const WaveBuffers& B, cudaStream_t st);
+/* primary rays of the OptiX 7 estimator (LH2G_RP_OPTIX7) or of a PrimeAdaptive frame's first wave (LH2G_RP_ADAPTIVE);
+ * the other stages choose their estimator by the same flags */
+void launch_generate_mis(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, cudaStream_t st);
 void launch_extend(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int persistentBlocks, cudaStream_t st);
 /* with B.order: the partition of the queue into hits and misses (k_partition), then the shading */
 void launch_shade(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int blocks, cudaStream_t st);
@@ -53,6 +60,24 @@ void launch_trace(const SceneGPU& S, const lh2g_ray* rays, void* out, long long 
 /* scene preparation */
 void launch_tri_prep(const float4* verts, uint32_t n, uint32_t seg, float4* triData, float4* lo, float4* hi, uint32_t* segOf, cudaStream_t st);
 void launch_gather_tris(const float4* triIn, const uint32_t* leafPrim, uint32_t n, float4* triOut, cudaStream_t st);
+
+/* PrimeAdaptive frames (adaptive.cu): device state between the two waves. devScale carries over to the next frame;
+ * hist must be zero before launch_adaptive_estimate. */
+struct AdaptiveState {
+    float devScale;
+    uint32_t requested;   /* samples the pixels asked for */
+    uint32_t pathCount;   /* second-wave paths: requested, capped at W*H*spp */
+    uint32_t sStar, room; /* the cap keeps requests with S < sStar, and S = sStar for the first `room` pixels asking for it */
+    uint32_t hist[25];    /* pixels per requested sample count 0..24 */
+};
+void launch_adaptive_estimate(const FrameGPU& F, const WaveBuffers& B, float* deviation, uint32_t* want, AdaptiveState* state, cudaStream_t st);
+/* per pixel its kept sample count and first second-wave slot (tmp, rank, kept, first: W*H; sums: W*H / 4096 + 1) */
+void launch_adaptive_keep(const FrameGPU& F, const uint32_t* want, uint32_t* tmp, uint32_t* rank, uint32_t* kept, uint32_t* first, uint32_t* sums,
+                          const AdaptiveState* state, cudaStream_t st);
+void launch_adaptive_generate(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, const uint32_t* kept, const uint32_t* first,
+                              uint32_t* slotLayer, uint32_t R1, cudaStream_t st);
+void launch_adaptive_finalize(const FrameGPU& F, const float4* layers, const float4* extra, const uint32_t* kept, const uint32_t* first, float4* accum,
+                              float4* frame, float scale, int overwrite, cudaStream_t st);
 
 int persistent_blocks_trace(int mode);
 int persistent_blocks_wave(int which);   /* 0 extend, 1 connect, 2 shade, 3 tail */

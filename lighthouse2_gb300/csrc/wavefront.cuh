@@ -259,6 +259,304 @@ __device__ __forceinline__ void shade_core(const SceneGPU& S, const FrameGPU& F,
     out.eT = make_float4(throughput.x, throughput.y, throughput.z, 0.0f);
 }
 
+/* ======================================================================================================
+ * The OptiX 7 core's estimator (lib/rendercore_optix7/kernels/pathtracer.h:54-238, ray generation of
+ * optix/.optix.cu:71-129) and the PrimeAdaptive core's variant (lib/RenderCore_PrimeAdaptive/kernels/pathtracer.h,
+ * camera.h), with the Lambert BSDF. Path state: O4.w = slot << 6 | flags (S_* bits 0-3, tmin class bits 4-5),
+ * D4.w = the packed normal of the previous vertex, T4 = throughput (bsdf * cos, the pdf not yet divided out) and
+ * w = the pdf of the bounce that led here. Radiance goes to pathAcc[slot]; a slot's RNG identity is slotLayer[slot]
+ * in the adaptive second wave, else the slot itself.
+ * ==================================================================================================== */
+constexpr uint32_t MIS_FLAG_MASK = 63u;
+
+LH2G_DEV uint32_t PackNormal(const float3 N) {   /* tools_shared.h:101-107 */
+    const float f = 65535.0f / fmaxf(sqrtf(8.0f * N.z + 8.0f), 0.0001f);
+    return f2u(N.x * f + 32767.0f) + (f2u(N.y * f + 32767.0f) << 16);
+}
+LH2G_DEV float3 UnpackNormal(const uint32_t p) {   /* tools_shared.h:108-120 */
+    float4 nn = make_float4(u2f23(p & 65535u) * (2.0f / 65535.0f), u2f23(p >> 16) * (2.0f / 65535.0f), 0.0f, 0.0f);
+    nn = nn + make_float4(-1.0f, -1.0f, 1.0f, -1.0f);
+    float l = dot(make_float3(nn.x, nn.y, nn.z), make_float3(-nn.x, -nn.y, -nn.w));
+    nn.z = l, l = sqrtf(l), nn.x *= l, nn.y *= l;
+    return make_float3(nn.x, nn.y, nn.z) * 2.0f + mk3(0.0f, 0.0f, -1.0f);
+}
+
+/* blueNoiseSampler4 (tools_shared.h:324-337) over the expanded tables */
+LH2G_DEV float4 blue_noise4(const uint32_t* __restrict__ bn, const int x, const int y, const int sampleIndex, const int sampleDimension) {
+    const uint4 r = __ldg(reinterpret_cast<const uint4*>(bn + sampleDimension + (x + y * 128) * 8 + 65536 * 3));
+    const int rsi1 = (sampleIndex ^ (int)r.x) & 255, rsi2 = (sampleIndex ^ (int)r.y) & 255;
+    const int rsi3 = (sampleIndex ^ (int)r.z) & 255, rsi4 = (sampleIndex ^ (int)r.w) & 255;
+    const int v1 = (int)__ldg(bn + sampleDimension + 0 + rsi1 * 256), v2 = (int)__ldg(bn + sampleDimension + 1 + rsi2 * 256);
+    const int v3 = (int)__ldg(bn + sampleDimension + 2 + rsi3 * 256), v4 = (int)__ldg(bn + sampleDimension + 3 + rsi4 * 256);
+    const uint4 b = __ldg(reinterpret_cast<const uint4*>(bn + (sampleDimension & 7) + (x + y * 128) * 8 + 65536));
+    return make_float4((0.5f + (float)(v1 ^ (int)b.x)) * (1.0f / 256.0f), (0.5f + (float)(v2 ^ (int)b.y)) * (1.0f / 256.0f),
+                       (0.5f + (float)(v3 ^ (int)b.z)) * (1.0f / 256.0f), (0.5f + (float)(v4 ^ (int)b.w)) * (1.0f / 256.0f));
+}
+
+/* RayTarget (lib/RenderSystem/common_functions.h:29-50) */
+LH2G_DEV float3 ray_target(const int sx, const int sy, const float r0, const float r1, const int W, const int H, const float distortion,
+                           const float3 p1, const float3 right, const float3 up) {
+    if (distortion == 0) {
+        const float u = ((float)sx + r0) * (1.0f / W);
+        const float v = ((float)sy + r1) * (1.0f / H);
+        return p1 + u * right + v * up;
+    }
+    const float tx = sx / (float)W - 0.5f, ty = sy / (float)H - 0.5f;
+    const float rr = tx * tx + ty * ty;
+    const float rq = sqrtf(rr) * (1.0f + distortion * rr + distortion * rr * rr);
+    const float theta = atan2_at(tx, ty);
+    float st, ct;
+    sincos_cw(theta, &st, &ct);
+    const float bx = (st * rq + 0.5f) * W;
+    const float by = (ct * rq + 0.5f) * H;
+    return p1 + (bx + r0) * (right / (float)W) + (by + r1) * (up / (float)H);
+}
+
+/* RandomPointOnLens (optix/.optix.cu:71-83; RenderCore_PrimeAdaptive/kernels/camera.h:22-33) */
+LH2G_DEV float3 lens_point(const float r0, float r1, const float3 pos, const float aperture, const float3 right, const float3 up) {
+    const float blade = (float)f2i(r0 * 9);
+    float r2 = (r0 - blade * (1.0f / 9.0f)) * 9.0f;
+    float x1, y1, x2, y2;
+    sincos_cw(blade * PI / 4.5f, &x1, &y1);
+    sincos_cw((blade + 1.0f) * PI / 4.5f, &x2, &y2);
+    if ((r1 + r2) > 1) r1 = 1.0f - r1, r2 = 1.0f - r2;
+    const float xr = x1 * r1 + x2 * r2;
+    const float yr = y1 * r1 + y2 * r2;
+    return pos + aperture * (right * xr + up * yr);
+}
+
+/* the primary ray of path pathIdx of an OptiX 7 frame (optix/.optix.cu:85-121) */
+__device__ __forceinline__ void primary_optix7(const SceneGPU& S, const FrameGPU& F, const uint32_t pathIdx, float3& O, float3& D) {
+    const uint32_t WH = (uint32_t)F.W * (uint32_t)F.H;
+    const uint32_t pixelIdx = pathIdx % WH;
+    const uint32_t sampleIdx = pathIdx / WH + (uint32_t)F.samplesTaken;
+    uint32_t seed = WangHash(pathIdx * 16789u + (uint32_t)F.samplesTaken * 1791u);
+    const int sx = (int)(pixelIdx % (uint32_t)F.W), sy = (int)(pixelIdx / (uint32_t)F.W);
+    float4 r4;
+    if (sampleIdx < 64 && S.blueNoise) {
+        r4 = blue_noise4(S.blueNoise, (sx + (int)(F.shift & 127u)) & 127, (sy + (int)(F.shift >> 24)) & 127, (int)sampleIdx, 0);
+    } else {
+        r4.x = RandomFloat(seed), r4.y = RandomFloat(seed);
+        r4.z = RandomFloat(seed), r4.w = RandomFloat(seed);
+    }
+    O = lens_point(r4.x, r4.z, F.pos, F.aperture, F.right, F.up);
+    D = normalize(ray_target(sx, sy, r4.y, r4.w, F.W, F.H, F.distortion, F.p1, F.right, F.up) - O);
+}
+
+/* the primary ray of pixel (sx, sy) with sample index sampleIdx in a PrimeAdaptive frame (camera.h:39-80, 96-139) */
+__device__ __forceinline__ void primary_adaptive(const SceneGPU& S, const FrameGPU& F, const int sx, const int sy, const uint32_t sampleIdx,
+                                                 const uint32_t thread, const uint32_t R0, float3& O, float3& D) {
+    float4 r4;
+    if (sampleIdx < 64 && S.blueNoise) {
+        r4 = blue_noise4(S.blueNoise, sx & 127, sy & 127, (int)sampleIdx, 0);
+    } else {
+        uint32_t seed = WangHash(thread + R0);
+        r4.x = RandomFloat(seed), r4.y = RandomFloat(seed);
+        r4.z = RandomFloat(seed), r4.w = RandomFloat(seed);
+    }
+    O = lens_point(r4.x, r4.z, F.pos, F.aperture, F.right, F.up);
+    D = normalize(ray_target(sx, sy, r4.y, r4.w, F.W, F.H, F.distortion, F.p1, F.right, F.up) - O);
+}
+
+/* SampleSmallSkydome (tools_shared.h:204-211) */
+LH2G_DEV float3 sample_small_sky(const SceneGPU& S, const float3& Dw) {
+    const uint32_t w = (uint32_t)S.skyW >> 6, h = (uint32_t)S.skyH >> 6;
+    if (w == 0 || h == 0 || !S.skySmall) return mk3(0);
+    const float4 m0 = S.worldToSky[0], m1 = S.worldToSky[1], m2 = S.worldToSky[2];
+    const float3 D = -make_float3(m0.x * Dw.x + m0.y * Dw.y + m0.z * Dw.z, m1.x * Dw.x + m1.y * Dw.y + m1.z * Dw.z, m2.x * Dw.x + m2.y * Dw.y + m2.z * Dw.z);
+    float p = atan2_at(D.y, D.x);
+    p = (p < 0) ? (p + 2 * PI) : p;
+    const float theta = acos_at(D.z < -1.f ? -1.f : (D.z > 1.f ? 1.f : D.z));
+    const uint32_t u = f2u((float)w * p * INV2PI - 0.5f);
+    const uint32_t v = f2u((float)h * theta * INVPI - 0.5f);
+    const uint32_t idx = u + v * w;
+    return idx < w * h ? xyz(__ldg(S.skySmall + idx)) : mk3(0);
+}
+
+/* LightPickProb (lights_shared.h:158-177): the chance that light idx would have been picked from O with normal N,
+ * the tri lights' potential taken at the light point I */
+LH2G_DEV float light_pick_prob(const SceneGPU& S, const int idx, const float3& O, const float3& N, const float3& I) {
+    const int lights = S.nTri + S.nPoint + S.nSpot + S.nDir;
+    float sum = 0, mine = 0;
+    for (int i = 0; i < lights; i++) {
+        float c;
+        if (i < S.nTri) {
+            const float4* l = S.triLights + (size_t)i * 6;
+            const float4 c4 = __ldg(l), n4 = __ldg(l + 1);
+            float3 L = I - O;
+            const float att = 1.0f / dot(L, L);
+            L = normalize(L);
+            const float LNdotL = fmaxf(0.0f, -dot(xyz(n4), L));
+            const float NdotL = fmaxf(0.0f, dot(N, L));
+            c = c4.w * LNdotL * NdotL * att;
+        } else if (i < S.nTri + S.nPoint) {
+            c = PotentialPoint(S, i - S.nTri, O, N);
+        } else if (i < S.nTri + S.nPoint + S.nSpot) {
+            c = PotentialSpot(S, i - S.nTri - S.nPoint, O, N);
+        } else {
+            c = PotentialDir(S, i - S.nTri - S.nPoint - S.nSpot, N);
+        }
+        if (i == idx) mine = c;
+        sum += c;
+    }
+    if (sum <= 0) return 0.0f;
+    return (idx >= 0 && idx < lights) ? mine / sum : 0.0f;
+}
+
+/* CLAMPINTENSITY (rendercore_optix7/core_settings.h:191-194) and FIXNAN_FLOAT3 (common_settings.h:66) */
+LH2G_DEV void clamp_intensity(float3& c, const float clampValue) {
+    const float v = fmaxf(c.x, fmaxf(c.y, c.z));
+    if (v > clampValue) { const float m = clampValue / v; c.x *= m, c.y *= m, c.z *= m; }
+}
+LH2G_DEV void fix_nan(float3& a) { if (!isfinite(a.x + a.y + a.z)) a = mk3(0); }
+
+/* the ray's tmin from its flags */
+LH2G_DEV float mis_tmin(const uint32_t flags, const float eps) {
+    const uint32_t c = (flags >> MIS_TMIN_SHIFT) & 3u;
+    return c == 1u ? eps : (c == 2u ? EPSILON : 0.0f);
+}
+
+/* Shading of one path vertex of the OptiX 7 / PrimeAdaptive estimators. */
+__device__ __forceinline__ void shade_mis(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, const int depth, const float4 o4,
+                                          const float4 d4, const float4 t4, const float4 hit, ShadeOut& out, float* pot) {
+    const bool optix7 = (F.flags & LH2G_RP_OPTIX7) != 0;
+    const uint32_t word = __float_as_uint(o4.w);
+    const uint32_t slot = word >> 6;
+    uint32_t FLAGS = word & 15u;
+    const uint32_t pathIdx = B.slotLayer ? __ldg(B.slotLayer + slot) : slot;
+    const float3 O = xyz(o4), D = xyz(d4);
+    float3 throughput = xyz(t4);
+    const float bsdfPdf = t4.w;
+    const int PRIM = __float_as_int(hit.z), INST = __float_as_int(hit.y);
+    const float HIT_T = hit.w;
+    const size_t capIdx = (size_t)(depth - 1) * F.P + slot;
+    const uint32_t WH = (uint32_t)F.W * (uint32_t)F.H;
+    const uint32_t sampleIdx = pathIdx / WH + F.pass;
+    float4* accP = B.pathAcc + slot;
+    /* PrimeAdaptive: albedo and normal of the first diffuse-led vertex, for the variance estimate (first wave only) */
+    float4* feat = (B.misFeatures && (FLAGS & S_BOUNCED) == 0) ? B.misFeatures + pathIdx : nullptr;
+    if (PRIM == NOHIT) {
+        const float3 skyPixel = (FLAGS & S_BOUNCED) ? sample_small_sky(S, D) : SampleSkydome(S, D);
+        float3 contribution = throughput * skyPixel * (1.0f / bsdfPdf);
+        clamp_intensity(contribution, F.clampValue);
+        fix_nan(contribution);
+        float4 acc = *accP;
+        acc.x += contribution.x, acc.y += contribution.y, acc.z += contribution.z;
+        *accP = acc;
+        if (feat) *feat = make_float4(contribution.x, contribution.y, contribution.z, __uint_as_float(PackNormal2(D * -1.0f)));
+        if (B.capSeeds) B.capSeeds[capIdx] = 0;
+        return;
+    }
+    const float HIT_U = (float)(__float_as_uint(hit.x) & 65535u) * (1.0f / 65535.0f);
+    const float HIT_V = (float)(__float_as_uint(hit.x) >> 16) * (1.0f / 65535.0f);
+    Shading sd;
+    float3 N, iN, fN, T;
+    const float3 I = O + HIT_T * D;
+    GetShadingData(S, D, HIT_U, HIT_V, F.spreadAngle * HIT_T, INST, PRIM, sd, N, iN, fN, T);
+    if (feat) *feat = make_float4(sd.color.x, sd.color.y, sd.color.z, __uint_as_float(PackNormal2(iN)));
+    const uint32_t tminBits = optix7 ? MIS_TMIN_EPS : 0u;
+    if (sd.flags & 1) {   /* alpha: the ray continues behind the surface */
+        if (B.capSeeds) B.capSeeds[capIdx] = 0;
+        if (depth >= F.maxDepth) return;
+        fix_nan(throughput);
+        out.ext = true;
+        if (optix7) {
+            const float3 P = I + D * F.eps;
+            out.eO = make_float4(P.x, P.y, P.z, __uint_as_float((slot << 6) | FLAGS | MIS_TMIN_EPS));
+            out.eD = d4;
+        } else {
+            out.eO = make_float4(I.x, I.y, I.z, __uint_as_float((slot << 6) | FLAGS | MIS_TMIN_EPSILON));
+            out.eD = make_float4(D.x, D.y, D.z, __uint_as_float(0u));
+        }
+        out.eT = make_float4(throughput.x, throughput.y, throughput.z, bsdfPdf);
+        return;
+    }
+    if (IsEmissive(sd)) {
+        const float DdotNL = -dot(D, N);
+        if (DdotNL > 0) {
+            float3 contribution = mk3(0);
+            if (depth == 1 || (FLAGS & S_SPECULAR) || !(F.flags & LH2G_RP_NEE)) {
+                contribution = sd.color;   /* the reference leaves the throughput out here */
+            } else {
+                const float3 lastN = UnpackNormal(__float_as_uint(d4.w));
+                const float4 tv = __ldg(S.instTris[INST] + (size_t)PRIM * 13 + 5);   /* T, area */
+                const float lightPdf = (HIT_T * HIT_T) / (fabsf(dot(D, N)) * tv.w);
+                const int ltri = __float_as_int(__ldg(S.instTris[INST] + (size_t)PRIM * 13).w);
+                const float pickProb = light_pick_prob(S, ltri, O, lastN, I);
+                if ((bsdfPdf + lightPdf * pickProb) > 0) contribution = throughput * sd.color * (1.0f / (bsdfPdf + lightPdf * pickProb));
+            }
+            clamp_intensity(contribution, F.clampValue);
+            fix_nan(contribution);
+            float4 acc = *accP;
+            acc.x += contribution.x, acc.y += contribution.y, acc.z += contribution.z;
+            *accP = acc;
+        }
+        if (B.capSeeds) B.capSeeds[capIdx] = 0;
+        return;
+    }
+    if (FLAGS & S_BOUNCED) sd.params[0] |= 255u << 24;   /* path regularisation: roughness 1 after a bounce */
+    if (ROUGHNESS(sd) <= 0.001f || TRANSMISSION(sd) > 0.5f) FLAGS |= S_SPECULAR; else FLAGS &= ~S_SPECULAR;
+    const float faceDir = (dot(D, N) > 0) ? -1.0f : 1.0f;
+    if (faceDir == 1) sd.transmittance = mk3(0);
+    throughput = throughput * (1.0f / bsdfPdf);
+    const uint32_t R0 = optix7 ? xorshift_n(F.cameraR0, depth - 1) + (uint32_t)depth * 91771u : F.r0Base + (uint32_t)depth * F.r0Depth;
+    uint32_t seed = WangHash(pathIdx * 17u + R0);
+    float4 r4;
+    if (sampleIdx < 64 && S.blueNoise) {
+        const uint32_t x = ((pathIdx % (uint32_t)F.W) + (F.shift & 127u)) & 127u;
+        const uint32_t y = ((pathIdx / (uint32_t)F.W) + (F.shift >> 24)) & 127u;
+        r4 = blue_noise4(S.blueNoise, (int)x, (int)y, (int)sampleIdx, 4 * depth - 4);
+    } else {
+        r4.x = RandomFloat(seed), r4.y = RandomFloat(seed);
+        r4.z = RandomFloat(seed), r4.w = RandomFloat(seed);
+    }
+    if ((FLAGS & S_SPECULAR) == 0 && (F.flags & LH2G_RP_NEE)) {
+        float pickProb = 0, lightPdf = 0;
+        float3 lightColor = mk3(0);
+        int picked = 0;
+        float3 L = RandomPointOnLight(S, r4.x, r4.y, I, fN * faceDir, pickProb, lightPdf, lightColor, pot, WAVE_BLOCK, picked) - I;
+        const float dist = length(L);
+        L = L * (1.0f / dist);
+        const float NdotL = dot(L, fN * faceDir);
+        if (NdotL > 0 && lightPdf > 0) {
+            float lbsdfPdf;
+            const float3 sampledBSDF = EvaluateBSDF(sd, fN, L, lbsdfPdf) * ROUGHNESS(sd);
+            if (lbsdfPdf > 0) {
+                float3 contribution = throughput * sampledBSDF * lightColor * (NdotL / (pickProb * lightPdf + lbsdfPdf));
+                fix_nan(contribution);
+                clamp_intensity(contribution, F.clampValue);
+                const float3 SO = SafeOrigin(I, L, N, F.eps);
+                out.shadow = true;
+                out.sO = make_float4(SO.x, SO.y, SO.z, __uint_as_float(slot));
+                out.sD = make_float4(L.x, L.y, L.z, dist - 2 * F.eps);
+                out.sE = make_float4(contribution.x, contribution.y, contribution.z, __uint_as_float((uint32_t)picked << 1));
+            }
+        }
+    }
+    /* one diffuse bounce at most (ENOUGH_BOUNCES = S_BOUNCED), or the maximum path length */
+    if ((FLAGS & S_BOUNCED) || depth == F.maxDepth) { if (B.capSeeds) B.capSeeds[capIdx] = seed; return; }
+    float3 R;
+    float newBsdfPdf;
+    bool specular = false;
+    (void)RandomFloat(seed);   /* the r5 argument of lambert.h's SampleBSDF: drawn, not used */
+    const float3 bsdf = SampleBSDF(sd, fN, N, D * -1.0f, HIT_T, r4.z, r4.w, R, newBsdfPdf, specular);
+    if (newBsdfPdf < EPSILON || isnan(newBsdfPdf)) { if (B.capSeeds) B.capSeeds[capIdx] = seed; return; }
+    if (specular) FLAGS |= S_SPECULAR;
+    const float pr = ((FLAGS & S_SPECULAR) || (FLAGS & S_BOUNCED) == 0) ? 1.0f : SurvivalProbability(bsdf);
+    if (pr < RandomFloat(seed)) { if (B.capSeeds) B.capSeeds[capIdx] = seed; return; }
+    throughput = throughput * (1 / pr);
+    if (B.capSeeds) B.capSeeds[capIdx] = seed;
+    const uint32_t packedNormal = PackNormal(fN * faceDir);
+    if (!(FLAGS & S_SPECULAR)) FLAGS |= (FLAGS & S_BOUNCED) ? S_BOUNCEDTWICE : S_BOUNCED; else FLAGS |= S_VIASPECULAR;
+    const float3 EO = SafeOrigin(I, R, N, F.eps);
+    fix_nan(throughput);
+    const float3 tn = throughput * bsdf * fabsf(dot(fN, R));
+    out.ext = true;
+    out.eO = make_float4(EO.x, EO.y, EO.z, __uint_as_float((slot << 6) | FLAGS | tminBits));
+    out.eD = make_float4(R.x, R.y, R.z, __uint_as_float(packedNormal));
+    out.eT = make_float4(tn.x, tn.y, tn.z, newBsdfPdf);
+}
+
 __device__ __forceinline__ float4 hit_record(const bool found, const HitRec& best) {
     if (found) return make_float4(__uint_as_float(f2u(65535.0f * best.u) + (f2u(65535.0f * best.v) << 16)), __int_as_float(best.inst),
                                   __int_as_float(best.prim), best.t);
