@@ -48,7 +48,7 @@ EXTEND_CAPTURE = {"pose": 1, "waves": (2, 3), "dram_bytes": 196.84736e6 + 74.086
 WORKLOAD = "spheres_2m: 64 x 32k-tri displaced spheres + ground (2,048,002 tris, 66 instances), 16 quad + 4 point lights, " \
            "20 materials (4 textured), sky; 1920x1080 1spp, max depth 8, RR after depth 3, NEE"
 METRIC = "Mrays/s @1080p 1spp"
-VIEW_BYTES, PARAMS_BYTES = 68, 48     # lh2g_view and lh2g_render_params copied host -> device per frame
+VIEW_BYTES, PARAMS_BYTES = 68, 56     # lh2g_view and lh2g_render_params copied host -> device per frame
 
 
 def peaks():
@@ -305,6 +305,69 @@ def decode_launches(lt_all, frames, counts, waves, W, H):
             per_kind["tail"][1] += b
             per_kind["tail"][2] += 1
     return per_kind
+
+
+def estimators_leg(core, sc, W, H, steps):
+    """The OptiX 7 core's estimator (LH2G_RP_OPTIX7: MIS, blue noise for the first 64 samples, one diffuse bounce)
+    and PrimeAdaptive frames (variance-driven second wave) on the same scene and frame size, seeded synthetic
+    blue-noise tables; device time per frame from CUDA events on the core's stream, rays from the frames' counters."""
+    import numpy as np
+    import torch
+    from lighthouse2_gb300 import scenes as S
+    from lighthouse2_gb300.core import make_params, camera_r0, RP_NEE, RP_OPTIX7
+    core.set_blue_noise(S.synthetic_blue_noise(7))
+    stream = torch.cuda.ExternalStream(core.stream_ptr())
+    out = {"workload": f"the same scene and camera path, {W}x{H} 1 spp, max depth {MAX_DEPTH}; synthetic blue-noise tables"}
+
+    def timed(render, n):
+        core.WaitForRender()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record()
+        for k in range(n):
+            render(k)
+        core.stream_ptr()
+        with torch.cuda.stream(stream):
+            e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n
+
+    def o7(k, counters=False):
+        p = make_params(W, H, 1, max_depth=MAX_DEPTH, samples_taken=k, camera_r0=camera_r0(k), flags=RP_NEE | RP_OPTIX7,
+                        shift=(0x11331445 * (k + 1)) & 0xFFFFFFFF)
+        return core.render_ex(S.spheres_view(W, H, frame=k % 8), p, accumulate=k > 0, counters=counters)
+
+    rays = [W * H + int(c[:, 0].sum()) + int(c[:, 1].sum()) for c in (o7(k, True)["counters"] for k in range(8))]
+    ms = timed(o7, steps)
+    out["optix7"] = {"ms_per_frame": ms, "Mrays_per_s": float(np.mean(rays)) / (ms / 1e3) / 1e6, "rays_per_frame": float(np.mean(rays))}
+    core.set_adaptive_scale(10.0)
+
+    def ad(k):
+        p = make_params(W, H, 1, max_depth=MAX_DEPTH, samples_taken=k, camera_r0=camera_r0(2 * k), frame_seed=camera_r0(2 * k + 1), flags=RP_NEE,
+                        shift=(0x11331445 * (k + 1)) & 0xFFFFFFFF)
+        return core.render_adaptive(S.spheres_view(W, H, frame=0), p, accumulate=k > 0)
+
+    hist = [ad(k) for k in range(24)]   # devScale settles towards the 91-98 % budget band
+    t = []
+    for k in range(24, 24 + max(4, steps // 4)):
+        core.WaitForRender()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record()
+        r = ad(k)
+        with torch.cuda.stream(stream):
+            e1.record()
+        torch.cuda.synchronize()
+        t.append(e0.elapsed_time(e1))
+        hist.append(r)
+    last = hist[-1]
+    rays_ad = [W * H + r["adaptive_paths"] + int(r["counters"][:, 0].sum()) + int(r["counters"][:, 1].sum()) for r in hist[-len(t):]]
+    out["adaptive"] = {"ms_per_frame": float(np.median(t)), "Mrays_per_s": float(np.mean(rays_ad)) / (float(np.median(t)) / 1e3) / 1e6,
+                       "second_wave_paths": last["adaptive_paths"], "requested": last["requested"], "budget": W * H,
+                       "dev_scale": last["dev_scale"], "frames_before_timing": 24,
+                       "note": "one frame at a time (the frame waits for its statistics); rays: both waves' primary, extension and shadow rays"}
+    core.set_blue_noise(None)
+    return out
 
 
 def svgf_leg(core, W, H, steps, warmup):
@@ -655,6 +718,7 @@ def run_gb300(args):
         rq["cornell"] = ray_query_leg(core_c, cb, args.rays, world == 1 and not args.no_cpu_baseline, "cornell 82k")
         core_c.close()
     svgf = svgf_leg(core, W, H, max(args.steps, 8), args.warmup) if not args.no_svgf else None
+    estimators = estimators_leg(core, sc, W, H, max(args.steps, 8)) if not args.no_estimators and rank == 0 else None
     serving = serving_leg(args) if (not args.no_serving and rank == 0) else None
     nrc = None
     if not args.no_nrc and rank == 0:
@@ -717,6 +781,8 @@ def run_gb300(args):
         line["ray_queries"] = rq
     if svgf is not None:
         line["svgf"] = svgf
+    if estimators is not None:
+        line["estimators"] = estimators
     if serving is not None:
         line["serving"] = serving
     if nrc is not None:
@@ -739,6 +805,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-svgf", action="store_true")
+    ap.add_argument("--no-estimators", action="store_true", help="skip the OptiX 7 estimator and adaptive-frame leg")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-nrc", action="store_true")
     ap.add_argument("--no-rays", action="store_true")

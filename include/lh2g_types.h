@@ -132,6 +132,11 @@ typedef struct lh2g_render_params {
     uint32_t frameSeed;                     /* LH2G_RP_FILTER: shading R0 = frameSeed + pathLength * 91771;
                                              * adaptive frames: R0 of the second wave's primary rays */
     uint32_t shift;                         /* LH2G_RP_OPTIX7 / adaptive frames: blue-noise tile shift (shiftSeed) */
+    /* A band of the frame (rowCount > 0): only pixel rows [rowBegin, rowBegin + rowCount) of the width x height
+     * frame are rendered, each path with the seeds it has in the whole frame, so the bands of one frame rendered
+     * apart (one per GPU) and put together equal the frame bit for bit. The target is the band (width x rowCount x
+     * spp); the accumulator holds the band's rows. PrimeRef estimator only. rowCount 0: the whole frame. */
+    int32_t rowBegin, rowCount;
 } lh2g_render_params;
 
 #define LH2G_RP_NEE        1                /* next-event estimation (connections buffer present) */

@@ -20,7 +20,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libRenderCore_GB300.so")
 PARAMS_DTYPE = np.dtype([("width", "<i4"), ("height", "<i4"), ("spp", "<i4"), ("maxDepth", "<i4"),
                          ("rrStartDepth", "<i4"), ("samplesTaken", "<i4"), ("cameraR0", "<u4"),
                          ("geometryEpsilon", "<f4"), ("clampValue", "<f4"), ("flags", "<i4"), ("frameSeed", "<u4"),
-                         ("shift", "<u4")])
+                         ("shift", "<u4"), ("rowBegin", "<i4"), ("rowCount", "<i4")])
 FILTER_PARAMS_DTYPE = np.dtype([("prevView", S.VIEW_DTYPE), ("j0", "<f4"), ("j1", "<f4"), ("prevj0", "<f4"), ("prevj1", "<f4"),
                                 ("clampDirect", "<f4"), ("clampIndirect", "<f4"), ("samplesTaken", "<i4"),
                                 ("camIsStationary", "<i4"), ("taa", "<i4")])
@@ -274,7 +274,8 @@ class RenderCore:
         self._check(self.lib.lh2g_set_adaptive_scale(self.ctx, float(dev_scale)), "set_adaptive_scale")
 
     def render_ex(self, view, params, accumulate=False, capture=False, counters=True):
-        D, P = int(params["maxDepth"]), int(params["width"]) * int(params["height"]) * int(params["spp"])
+        rows = int(params["rowCount"]) if int(params["rowCount"]) > 0 else int(params["height"])
+        D, P = int(params["maxDepth"]), int(params["width"]) * rows * int(params["spp"])
         hits = np.zeros(D * P, S.HIT_DTYPE) if capture else None
         seeds = np.zeros(D * P, np.uint32) if capture else None
         cnt = np.zeros((D, 2), np.uint32) if counters else None

@@ -928,8 +928,12 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
     if (!ctx || !view || !p) return LH2G_ERR_INVALID;
     if (!ctx->finalized) return fail(ctx, LH2G_ERR_STATE, "render: scene not finalized (call lh2g_finalize_instances)");
     if (!ctx->cap) return fail(ctx, LH2G_ERR_STATE, "render: no target (call lh2g_set_target)");
-    if (p->width != ctx->W || p->height != ctx->H || p->spp != ctx->spp || p->maxDepth < 1 || p->maxDepth > 64)
+    const bool band = p->rowCount > 0;
+    if (p->width != ctx->W || (band ? p->rowCount : p->height) != ctx->H || p->spp != ctx->spp || p->maxDepth < 1 || p->maxDepth > 64)
         return fail(ctx, LH2G_ERR_INVALID, "render: parameters do not match the target");
+    if (band && (p->rowBegin < 0 || p->rowBegin + p->rowCount > p->height || (int64_t)p->width * p->height * p->spp >= (1ll << 32) ||
+                 (p->flags & (LH2G_RP_FILTER | LH2G_RP_NRC | LH2G_RP_OPTIX7 | LH2G_RP_ADAPTIVE))))
+        return fail(ctx, LH2G_ERR_INVALID, "render: a band must lie in the frame and render the PrimeRef estimator");
     if (!ctx->mats) return fail(ctx, LH2G_ERR_STATE, "render: no materials");
     if (!materials_cover_meshes(ctx)) return fail(ctx, LH2G_ERR_INVALID, "render: a triangle's material index exceeds the material count");
     cudaSetDevice(ctx->device);
@@ -1033,7 +1037,7 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
     if (pipe && ctx->finValid) CK(cudaStreamWaitEvent(st, ctx->finEv, 0));   /* the previous frame's finalize first */
     mark(), launch_finalize(F, B, 1.0f / (float)after, !accumulate && !filt, st), mark();
     /* the frame to the caller's host buffer, before the next frame's finalize overwrites it */
-    if (hostFrame) CK(cudaMemcpyAsync(hostFrame, B.frame, sizeof(float4) * (size_t)F.W * F.H, cudaMemcpyDeviceToHost, st));
+    if (hostFrame) CK(cudaMemcpyAsync(hostFrame, B.frame, sizeof(float4) * (size_t)F.W * F.rowCount, cudaMemcpyDeviceToHost, st));
     CK(cudaEventRecord(ctx->finEv, st));
     ctx->finValid = true;
     if (hook && hook->after) {
@@ -1108,7 +1112,8 @@ int render_adaptive(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_
     if (!ctx->cap) return fail(ctx, LH2G_ERR_STATE, "render: no target (call lh2g_set_target)");
     if (p->width != ctx->W || p->height != ctx->H || p->spp != ctx->spp || p->maxDepth < 1 || p->maxDepth > 32)
         return fail(ctx, LH2G_ERR_INVALID, "render_adaptive: parameters do not match the target (or maxDepth beyond 32)");
-    if (p->flags & ~LH2G_RP_NEE) return fail(ctx, LH2G_ERR_INVALID, "render_adaptive: only LH2G_RP_NEE combines with adaptive frames");
+    if ((p->flags & ~LH2G_RP_NEE) || p->rowCount != 0)
+        return fail(ctx, LH2G_ERR_INVALID, "render_adaptive: only LH2G_RP_NEE combines with adaptive frames (whole frames)");
     if (ctx->cap >= (1ll << MIS_SLOT_BITS)) return fail(ctx, LH2G_ERR_INVALID, "render_adaptive: at most 2^26 paths per frame");
     if (!ctx->mats) return fail(ctx, LH2G_ERR_STATE, "render: no materials");
     if (!materials_cover_meshes(ctx)) return fail(ctx, LH2G_ERR_INVALID, "render: a triangle's material index exceeds the material count");
@@ -1600,6 +1605,13 @@ FrameGPU frame_of(const lh2g_view* view, const lh2g_render_params* p) {
     F.P = (int64_t)F.W * F.H * F.spp;
     F.stride = F.P;
     F.distortion = view->distortion, F.shift = p->shift, F.pass = (uint32_t)p->samplesTaken, F.clampValue = p->clampValue;
+    F.rowBegin = 0, F.rowCount = F.H, F.bandPix = 0;
+    if (p->rowCount > 0) {   /* a band of rows: its paths, with their seeds of the whole frame */
+        F.rowBegin = p->rowBegin, F.rowCount = p->rowCount;
+        F.bandPix = (uint32_t)F.W * (uint32_t)p->rowCount;
+        F.P = (int64_t)F.bandPix * F.spp;
+        F.stride = F.P;
+    }
     return F;
 }
 

@@ -82,7 +82,17 @@ struct FrameGPU {
     uint32_t r0Base, r0Depth;        /* PrimeAdaptive shading seed: r0Base + depth * r0Depth */
     float clampValue;
     float distortion;
+    /* a band of rows [rowBegin, rowBegin + rowCount) of the W x H frame (bandPix = W * rowCount; 0: the whole frame);
+     * a path's local index l maps to its index in the whole frame, which seeds its random numbers */
+    int rowBegin, rowCount;
+    uint32_t bandPix;
 };
+
+/* the index in the whole frame of the band's path l */
+__device__ __forceinline__ uint32_t global_path(const FrameGPU& F, const uint32_t l) {
+    if (!F.bandPix) return l;
+    return (l / F.bandPix) * ((uint32_t)F.W * (uint32_t)F.H) + (uint32_t)F.rowBegin * (uint32_t)F.W + l % F.bandPix;
+}
 
 /* Device counters of one frame. extension[d] counts extension rays written while shading path length
  * d+1 (the queue of the next wave), shadow[d] the connections; status holds error bits. */

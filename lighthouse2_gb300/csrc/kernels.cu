@@ -353,7 +353,7 @@ __global__ void k_nrc_apply(const FrameGPU F, const WaveBuffers B, const float4*
 /* overwrite: the accumulator starts from zero (a frame that does not accumulate) instead of its stored sum */
 __global__ void k_finalize(const FrameGPU F, const WaveBuffers B, const float scale, const int overwrite) {
     const int64_t px = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t WH = (int64_t)F.W * F.H;
+    const int64_t WH = F.bandPix ? (int64_t)F.bandPix : (int64_t)F.W * F.H;   /* the pixels rendered (a band's) */
     if (px >= WH) return;
     const bool filt = (F.flags & LH2G_RP_FILTER) != 0;
     for (int half = 0; half < (filt ? 2 : 1); half++) {
@@ -496,7 +496,7 @@ void launch_sort_connections(const WaveBuffers& B, int depth, cudaStream_t st) {
     k_conn_scatter<<<sm_count() * 8, 256, 0, st>>>(B, depth);
 }
 void launch_finalize(const FrameGPU& F, const WaveBuffers& B, float scale, int overwrite, cudaStream_t st) {
-    const int64_t WH = (int64_t)F.W * F.H;
+    const int64_t WH = F.bandPix ? (int64_t)F.bandPix : (int64_t)F.W * F.H;
     k_finalize<<<(unsigned)((WH + 255) / 256), 256, 0, st>>>(F, B, scale, overwrite);
 }
 void launch_trace(const SceneGPU& S, const lh2g_ray* rays, void* out, long long n, int mode, uint32_t* fetch, uint32_t* status, int blocks, cudaStream_t st) {

@@ -75,7 +75,7 @@ extern "C" LH2G_API int lh2g_render_noalloc(lh2g_context* ctx, const lh2g_view* 
     if (!ctx || !view || !p || !accumDevice) return LH2G_ERR_INVALID;
     if (p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->maxDepth < 1 || p->maxDepth > 64) return LH2G_ERR_INVALID;
     /* filter, radiance-cache and adaptive frames need the context's own buffers; this path renders the plain estimator */
-    if (p->flags & (LH2G_RP_FILTER | LH2G_RP_NRC | LH2G_RP_OPTIX7 | LH2G_RP_ADAPTIVE)) return LH2G_ERR_INVALID;
+    if ((p->flags & (LH2G_RP_FILTER | LH2G_RP_NRC | LH2G_RP_OPTIX7 | LH2G_RP_ADAPTIVE)) || p->rowCount != 0) return LH2G_ERR_INVALID;
     const long long P = (long long)p->width * p->height * p->spp;
     if (P > LH2G_NOALLOC_MAX_PATHS) return LH2G_ERR_OVERFLOW;   /* width * height * spp above the static capacity */
     SceneGPU S;
@@ -114,7 +114,8 @@ extern "C" LH2G_API int lh2g_render_noalloc(lh2g_context* ctx, const lh2g_view* 
     B.accum = (float4*)accumDevice;
     B.capHits = nullptr, B.capSeeds = nullptr;
     B.features = nullptr, B.worldPos = nullptr, B.deltaDepth = nullptr, B.nrcRec = nullptr;
-    FrameGPU F;
+    FrameGPU F{};
+    F.rowCount = p->height;   /* the whole frame (bandPix 0) */
     F.W = p->width, F.H = p->height, F.spp = p->spp, F.maxDepth = p->maxDepth, F.rrStart = p->rrStartDepth, F.samplesTaken = p->samplesTaken;
     F.cameraR0 = p->cameraR0, F.frameSeed = p->frameSeed, F.eps = p->geometryEpsilon, F.flags = p->flags;
     F.spreadAngle = view->spreadAngle, F.aperture = view->aperture;

@@ -22,7 +22,8 @@ __device__ __forceinline__ uint32_t lanemask_lt() { uint32_t m; asm("mov.u32 %0,
 
 /* Primary ray of path jobIndex (lib/RenderCore_PrimeRef/kernels/camera.h:39-68; pixel corner without lens for
  * LH2G_RP_FILTER frames, RenderCore_Optix7Filter/optix/.optix.cu:66-100). */
-__device__ __forceinline__ void primary_ray(const FrameGPU& F, const uint32_t jobIndex, float3& O, float3& D) {
+__device__ __forceinline__ void primary_ray(const FrameGPU& F, const uint32_t local, float3& O, float3& D) {
+    const uint32_t jobIndex = global_path(F, local);   /* the path's index in the whole frame */
     const uint32_t x = jobIndex % (uint32_t)F.W;
     uint32_t y = jobIndex / (uint32_t)F.W;
     y %= (uint32_t)F.H;
@@ -197,7 +198,7 @@ __device__ __forceinline__ void shade_core(const SceneGPU& S, const FrameGPU& F,
         FLAGS |= S_CACHED;
     }
     if (ROUGHNESS(sd) <= 0.001f || TRANSMISSION(sd) > 0.999f) FLAGS |= S_SPECULAR; else FLAGS &= ~S_SPECULAR;
-    uint32_t seed = WangHash(pathIdx * 17u + R0);
+    uint32_t seed = WangHash(global_path(F, pathIdx) * 17u + R0);
     if (firstHitToBeStored) {
         if (FLAGS & S_SPECULAR) {
             B.features[pathIdx].x = HDRtoRGB32(sd.color);   /* modulated by the first diffuse vertex later */

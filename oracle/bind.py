@@ -22,7 +22,7 @@ REFERENCE_TREE = os.environ.get("LH2_REFERENCE", "")
 PARAMS_DTYPE = np.dtype([("width", "<i4"), ("height", "<i4"), ("spp", "<i4"), ("maxDepth", "<i4"),
                          ("rrStartDepth", "<i4"), ("samplesTaken", "<i4"), ("cameraR0", "<u4"),
                          ("geometryEpsilon", "<f4"), ("clampValue", "<f4"), ("flags", "<i4"), ("frameSeed", "<u4"),
-                         ("shift", "<u4")])
+                         ("shift", "<u4"), ("rowBegin", "<i4"), ("rowCount", "<i4")])
 FILTER_PARAMS_DTYPE = np.dtype([("prevView", S.VIEW_DTYPE), ("j0", "<f4"), ("j1", "<f4"), ("prevj0", "<f4"), ("prevj1", "<f4"),
                                 ("clampDirect", "<f4"), ("clampIndirect", "<f4"), ("samplesTaken", "<i4"),
                                 ("camIsStationary", "<i4"), ("taa", "<i4")])
@@ -169,6 +169,8 @@ class Oracle:
         """One frame. LH2G_RP_FILTER frames accumulate 2*W*H pixels (direct, then indirect) and write the SVGF
         features into `features` (an SvgfState, or None)."""
         W, H, spp, D = int(params["width"]), int(params["height"]), int(params["spp"]), int(params["maxDepth"])
+        if int(params["rowCount"]) > 0:   # a band of rows: its pixels only
+            H = int(params["rowCount"])
         halves = 2 if int(params["flags"]) & RP_FILTER else 1
         if accum is None:
             accum = np.zeros((halves * H * W, 4), np.float32)

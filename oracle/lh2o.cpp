@@ -955,6 +955,12 @@ struct Frame {
     f3 right, up;
     long long P;
     lh2o_features feat;        /* LH2G_RP_FILTER: SVGF feature buffers (W*H entries each) */
+    uint bandPix = 0;          /* a band of rows (lh2g_render_params rowBegin / rowCount): its pixels; 0: the whole frame */
+    /* the index in the whole frame of the band's path l */
+    uint global(uint l) const {
+        if (!bandPix) return l;
+        return (l / bandPix) * ((uint)p.width * (uint)p.height) + (uint)p.rowBegin * (uint)p.width + l % bandPix;
+    }
 };
 
 /* Radiance of one path: rgbw[0] = the direct half (and the primary distance in w), rgbw[1] = the indirect
@@ -1018,11 +1024,12 @@ void trace_path(const Frame& F, const uint jobIndex, PathOut& out, std::vector<u
     const bool nee = (p.flags & LH2G_RP_NEE) != 0;
     const bool filt = (p.flags & LH2G_RP_FILTER) != 0;
     const uint WH = (uint)W * (uint)H;
-    /* generateEyeRaysKernel */
-    const uint x = jobIndex % (uint)W;
-    uint y = jobIndex / (uint)W;
+    /* generateEyeRaysKernel (a band's paths take their index in the whole frame) */
+    const uint gIdx = F.global(jobIndex);
+    const uint x = gIdx % (uint)W;
+    uint y = gIdx / (uint)W;
     y %= (uint)H;
-    uint seed = WangHash(jobIndex + p.cameraR0);
+    uint seed = WangHash(gIdx + p.cameraR0);
     const float r0 = RandomFloat(seed), r1 = RandomFloat(seed);
     const float r2 = RandomFloat(seed), r3 = RandomFloat(seed);
     const f3 p1 = ld3(F.view.p1), pos = ld3(F.view.pos);
@@ -1116,7 +1123,7 @@ void trace_path(const Frame& F, const uint jobIndex, PathOut& out, std::vector<u
             return;
         }
         if (ROUGHNESS(sd) <= 0.001f || TRANSMISSION(sd) > 0.999f) FLAGS |= S_SPECULAR; else FLAGS &= ~S_SPECULAR;
-        seed = WangHash(pathIdx * 17u + R0);
+        seed = WangHash(gIdx * 17u + R0);
         if (firstHitToBeStored) {
             if (FLAGS & S_SPECULAR) {
                 feat[0] = HDRtoRGB32(sd.color);   /* modulated by the first diffuse vertex later */
@@ -2194,17 +2201,21 @@ int lh2o_render_ex(lh2o_scene* s, const lh2g_view* view, const lh2g_render_param
                    uint32_t* counters, lh2g_capture* capture, const lh2o_features* feat, int nthreads) {
     if (!s || !s->finalized || !view || !p || p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->maxDepth <= 0 || p->maxDepth > 64) return 1;
     if (p->flags & LH2G_RP_OPTIX7) {
-        if (p->flags & (LH2G_RP_FILTER | LH2G_RP_NRC | LH2G_RP_ADAPTIVE)) return 1;
+        if ((p->flags & (LH2G_RP_FILTER | LH2G_RP_NRC | LH2G_RP_ADAPTIVE)) || p->rowCount != 0) return 1;
         return render_optix7(s, view, p, pixelAccum, pixelAccum64, counters, capture, nthreads);
     }
     const bool filt = (p->flags & LH2G_RP_FILTER) != 0;
+    const bool band = p->rowCount > 0;
+    if (band && (filt || (p->flags & LH2G_RP_NRC) || p->rowBegin < 0 || p->rowBegin + p->rowCount > p->height)) return 1;
     Frame F;
     F.s = s, F.view = *view, F.p = *p;
     F.right = ld3(view->p2) - ld3(view->p1);
     F.up = ld3(view->p3) - ld3(view->p1);
     memset(&F.feat, 0, sizeof(F.feat));
     if (filt && feat) F.feat = *feat;
-    const long long WH = (long long)p->width * p->height;
+    /* WH: the pixels rendered (a band's rows, or the frame); the accumulator holds them */
+    const long long WH = (long long)p->width * (band ? p->rowCount : p->height);
+    if (band) F.bandPix = (uint)WH;
     F.P = WH * p->spp;
     const int D = p->maxDepth;
     if (capture && capture->hits)
@@ -2248,7 +2259,7 @@ int lh2o_render_adaptive(lh2o_scene* s, const lh2g_view* view, const lh2g_render
                          uint32_t* counters, uint32_t* adaptivePaths, float* frameAccOut, float* featuresOut, float* deviationOut,
                          lh2g_capture* capture, int nthreads) {
     if (!s || !s->finalized || !view || !p || !accum || !devScale || p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->maxDepth <= 0 ||
-        p->maxDepth > 32 || (p->flags & (LH2G_RP_FILTER | LH2G_RP_NRC | LH2G_RP_OPTIX7)))
+        p->maxDepth > 32 || (p->flags & (LH2G_RP_FILTER | LH2G_RP_NRC | LH2G_RP_OPTIX7)) || p->rowCount != 0)
         return 1;
     Frame F;
     F.s = s, F.view = *view, F.p = *p;

@@ -53,7 +53,7 @@ static_assert(sizeof(CoreTri) == 208, "CoreTri");
 static_assert(sizeof(CoreLightTri) == 96 && sizeof(CorePointLight) == 32 && sizeof(CoreSpotLight) == 48, "lights");
 static_assert(sizeof(CoreDirectionalLight) == 32 && sizeof(ViewPyramid) == 68 && sizeof(mat4) == 64, "view");
 static_assert(sizeof(CoreTexDesc) == 40 && sizeof(CoreMaterial::Vec3Value) == 48 && sizeof(CoreMaterial::ScalarValue) == 40, "material");
-static_assert(sizeof(lh2g_material) == 196 && sizeof(lh2g_gpu_material) == 128 && sizeof(lh2g_render_params) == 48 && sizeof(lh2g_filter_params) == 104, "abi");
+static_assert(sizeof(lh2g_material) == 196 && sizeof(lh2g_gpu_material) == 128 && sizeof(lh2g_render_params) == 56 && sizeof(lh2g_filter_params) == 104, "abi");
 int main(int argc, char** argv) {
     void* m = dlopen(argv[1], RTLD_NOW | RTLD_GLOBAL);
     if (!m) { printf("dlopen failed: %s\n", dlerror()); return 1; }
