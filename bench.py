@@ -637,13 +637,23 @@ def run_gb300(args):
     core = RenderCore(local)
     core.set_scene(sc)
     build_ms = core.GetCoreStats()["bvhBuildTime"]
-    core.SetTarget(W, H, 1)
+    split = world > 1 and args.partition == "rows"
+    band = None
+    if split:   # each rank renders its band of every frame's rows (lighthouse2_gb300.sharding)
+        from lighthouse2_gb300 import sharding
+        band = sharding.row_bands(H, world)[rank]
+        core.SetTarget(W, band[1], 1)
+    else:
+        core.SetTarget(W, H, 1)
     core.Setting("waveTail", args.wave_tail)
     core.Setting("pipelineFrames", args.lanes)
     core.Setting("sortConnections", args.sort_connections)
     waves = min(MAX_DEPTH, args.wave_tail - 1) if args.wave_tail > 0 else MAX_DEPTH
     stream = torch.cuda.ExternalStream(core.stream_ptr())
     frames = [frame_params(k, W, H) for k in range(8)]
+    if split:
+        frames = [(v, sharding.band_params(p, rank, world)) for v, p in frames]
+    pix = W * (band[1] if split else H)   # primary rays per frame on this rank
     for k in range(args.warmup):
         core.render_ex(*frames[k % 8], counters=False)
     # per-pose queue sizes and traversal work: a frame is a deterministic function of its view and parameters, so
@@ -685,23 +695,26 @@ def run_gb300(args):
     rays, trav, ext_rays, shadow_rays = 0, np.zeros(4, np.float64), 0, 0
     for k in range(args.steps):
         c = counts[k % 8]
-        rays += W * H + int(c[:, 0].sum()) + int(c[:, 1].sum())
+        rays += pix + int(c[:, 0].sum()) + int(c[:, 1].sum())
         trav += trav_pose[k % 8]
-        ext_rays += W * H + int(c[:-1, 0].sum())
+        ext_rays += pix + int(c[:-1, 0].sum())
         shadow_rays += int(c[:, 1].sum())
     if dist:
         ms, rays = reduce_replicas(dist, ms, rays, "cuda")
+        if split:   # the one gather of the partition, after the timed region: the last frame's bands into the whole frame
+            whole = sharding.gather_frame(dist, core.read_accumulator(), frames[(args.steps - 1) % 8][1], rank, world, device="cuda")
+            assert whole.shape == (W * H, 4)
     value = rays / (ms / 1e3) / 1e6
     # ---- end-to-end through the C ABI: camera and parameters in from host memory, every frame copied back into
     # pinned host memory (lh2g_render_to_host; consecutive frames and their copies overlap), timed on the host ----
-    hosts = [torch.empty((W * H, 4), dtype=torch.float32, pin_memory=True) for _ in range(2)]
+    hosts = [torch.empty((pix, 4), dtype=torch.float32, pin_memory=True) for _ in range(2)]
     core.WaitForRender()
     e2e_rays = 0
     t = time.perf_counter()
     for k in range(args.steps):
         core.render_to_host(*frames[k % 8], hosts[k % 2].data_ptr())
         c = counts[k % 8]
-        e2e_rays += W * H + int(c[:, 0].sum()) + int(c[:, 1].sum())
+        e2e_rays += pix + int(c[:, 0].sum()) + int(c[:, 1].sum())
     core.WaitForRender()
     t_e2e = time.perf_counter() - t
     last = core.read_framebuffer()
@@ -753,7 +766,7 @@ def run_gb300(args):
         rays_captured = sum(int(counts[EXTEND_CAPTURE["pose"]][w - 2, 0]) for w in EXTEND_CAPTURE["waves"])
         traffic = EXTEND_CAPTURE["dram_bytes"] / rays_captured * (b_dom / n_dom) / algorithmic_bytes("extend", 1, 0, 0)
     line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "strong" if split else "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": bench_config(W, H),
             "details": {"wave_tail": args.wave_tail, "frames_in_flight": args.lanes,
@@ -774,7 +787,7 @@ def run_gb300(args):
                          "note": "traversal/shading are ALU-issue bound; algorithmic bytes count queue traffic only (48 B per ray); "
                                  "achieved from launches in the timed region, where frames overlap; achieved_isolated from the same "
                                  "kernels of frames rendered one at a time; traffic = ncu DRAM bytes per ray x rays per launch"},
-            "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": VIEW_BYTES + PARAMS_BYTES, "d2h_bytes_per_step": W * H * 16},
+            "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": VIEW_BYTES + PARAMS_BYTES, "d2h_bytes_per_step": pix * 16},
             "gpu_launches": launches * world,
             "clocks": clk}
     if rq is not None:
@@ -819,6 +832,8 @@ def main():
                     help="queue capacity of the serving loop in paths (at least twice the largest job)")
     ap.add_argument("--serving-tick-budget", type=int, default=0, help="new paths per tick of the serving loop (0: the loop's default)")
     ap.add_argument("--lanes", type=int, default=LANES, help="frames in flight (0 or 1: one at a time)")
+    ap.add_argument("--partition", default="replicas", choices=["replicas", "rows"],
+                    help="under torchrun: replicas (every rank renders whole frames) or rows (every frame's rows split over the ranks)")
     ap.add_argument("--sort-connections", type=int, default=0, help="group connections by light before the any-hit queries")
     ap.add_argument("--wave-tail", type=int, default=WAVE_TAIL, help="first path length of the persistent tail kernel (0: off)")
     args = ap.parse_args()
