@@ -648,6 +648,7 @@ def run_gb300(args):
     core.Setting("waveTail", args.wave_tail)
     core.Setting("pipelineFrames", args.lanes)
     core.Setting("sortConnections", args.sort_connections)
+    core.Setting("sortRays", args.sort_rays)
     waves = min(MAX_DEPTH, args.wave_tail - 1) if args.wave_tail > 0 else MAX_DEPTH
     stream = torch.cuda.ExternalStream(core.stream_ptr())
     frames = [frame_params(k, W, H) for k in range(8)]
@@ -835,6 +836,7 @@ def main():
     ap.add_argument("--partition", default="replicas", choices=["replicas", "rows"],
                     help="under torchrun: replicas (every rank renders whole frames) or rows (every frame's rows split over the ranks)")
     ap.add_argument("--sort-connections", type=int, default=0, help="group connections by light before the any-hit queries")
+    ap.add_argument("--sort-rays", type=int, default=0, help="group bounce waves' extension rays by direction octant")
     ap.add_argument("--wave-tail", type=int, default=WAVE_TAIL, help="first path length of the persistent tail kernel (0: off)")
     args = ap.parse_args()
     if args.warmup < 3:

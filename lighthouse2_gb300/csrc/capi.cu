@@ -241,6 +241,7 @@ struct lh2g_context {
     Lane lanes[MAX_LANES];
     int pipelineFrames = 4;            /* lanes in use; 0 or 1: one frame at a time */
     int sortConnections = 0;           /* group each wave's connections by light before the any-hit queries */
+    int sortRays = 0;                  /* group each bounce wave's extension rays by direction octant before the closest-hit queries */
     int nextLane = 0;
     int lastSlot = -1;                 /* lane of the last frame, -1: the context stream */
     cudaEvent_t forkEv = nullptr, finEv = nullptr;
@@ -789,6 +790,7 @@ int lh2g_setting(lh2g_context* ctx, const char* name, float value) {
     else if (!strcmp(name, "filter")) ctx->filterEnabled = value == 0 ? 0 : 1;
     else if (!strcmp(name, "TAA")) ctx->taaEnabled = value == 0 ? 0 : 1;
     else if (!strcmp(name, "sortConnections")) ctx->sortConnections = value == 0 ? 0 : 1;
+    else if (!strcmp(name, "sortRays")) ctx->sortRays = value == 0 ? 0 : 1;
     else if (!strcmp(name, "waveOccupancy")) {
         /* fraction of a full GPU the persistent wave kernels of one frame take (frames in flight share the rest) */
         if (!(value > 0.0f && value <= 1.0f)) return fail(ctx, LH2G_ERR_INVALID, "setting waveOccupancy: (0, 1]");
@@ -1018,8 +1020,15 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
     else launch_generate(F, B, st);
     mark();
     for (int d = 1; d <= waves; d++) {
-        mark(), launch_extend(S, F, B, d, ctx->blocksExtend, st), mark();
-        mark(), launch_shade(S, F, B, d, ctx->blocksShade, st), mark();
+        WaveBuffers Bq = B;   /* with "sortRays": the queue of a bounce wave regrouped by direction octant */
+        if (ctx->sortRays && d >= 2) {
+            const int q = (d - 1) & 1;
+            Bq.O[q] = B.sortO, Bq.D[q] = B.sortD, Bq.T[q] = B.sortE;
+            mark(), launch_sort_rays(B, d, st), launch_extend(S, F, Bq, d, ctx->blocksExtend, st), mark();
+        } else {
+            mark(), launch_extend(S, F, Bq, d, ctx->blocksExtend, st), mark();
+        }
+        mark(), launch_shade(S, F, Bq, d, ctx->blocksShade, st), mark();
         if (ctx->sortConnections) {   /* one timed slot: the regrouping and the any-hit queries */
             WaveBuffers Bs = B;
             Bs.shO = B.sortO, Bs.shD = B.sortD, Bs.shE = B.sortE;

@@ -305,6 +305,45 @@ __global__ void k_conn_scatter(const WaveBuffers B, const int depth) {
     }
 }
 
+/* --------------------------------------------------------------------------------------------------
+ * Extension rays grouped by direction octant before a bounce wave's closest-hit queries (setting "sortRays"): a
+ * counting sort over 8 bins of the queue into sortO/D/E; within a bin, each warp's rays stay together and in order,
+ * so neighbouring pixels' rays stay neighbours. A warp of rays heading into one octant visits more of the same
+ * nodes. Results do not change (everything per path follows the path, not its queue slot). */
+__device__ __forceinline__ uint32_t ray_octant(const float4 d) {
+    return (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+}
+__global__ void k_ray_count(const WaveBuffers B, const int depth) {
+    __shared__ uint32_t h[8];
+    if (threadIdx.x < 8) h[threadIdx.x] = 0;
+    __syncthreads();
+    const int q = (depth - 1) & 1;
+    const uint32_t n = B.counters->extension[depth - 2];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) atomicAdd(&h[ray_octant(B.D[q][i])], 1u);
+    __syncthreads();
+    if (threadIdx.x < 8 && h[threadIdx.x]) atomicAdd(&B.connBins[threadIdx.x], h[threadIdx.x]);
+}
+__global__ void k_ray_scatter(const WaveBuffers B, const int depth) {
+    const int q = (depth - 1) & 1;
+    const uint32_t n = B.counters->extension[depth - 2];
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t w0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); w0 < n; w0 += gridDim.x * blockDim.x) {
+        const uint32_t i = w0 + lane;
+        const bool valid = i < n;
+        const float4 d = valid ? B.D[q][i] : make_float4(0, 0, 0, 0);
+        const uint32_t bin = valid ? ray_octant(d) : 64u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, bin);
+        const uint32_t leader = (uint32_t)__ffs(peers) - 1u;
+        uint32_t base = 0;
+        if (valid && lane == leader) base = atomicAdd(&B.connBins[64 + bin], (uint32_t)__popc(peers));
+        base = __shfl_sync(0xffffffffu, base, (int)leader);
+        if (valid) {
+            const uint32_t pos = base + (uint32_t)__popc(peers & lanemask_lt());
+            B.sortO[pos] = B.O[q][i], B.sortD[pos] = d, B.sortE[pos] = B.T[q][i];
+        }
+    }
+}
+
 /* -------------------------------------------------------------------------------------------------- */
 /* radiance cache: the queries of the paths that ended at their cache vertex (state 1) and the training samples of
  * the paths that went on (state 2: target = radiance gathered from the vertex on / throughput into it) */
@@ -494,6 +533,11 @@ void launch_sort_connections(const WaveBuffers& B, int depth, cudaStream_t st) {
     k_conn_count<<<sm_count() * 4, 256, 0, st>>>(B, depth);
     k_conn_scan<<<1, 64, 0, st>>>(B);
     k_conn_scatter<<<sm_count() * 8, 256, 0, st>>>(B, depth);
+}
+void launch_sort_rays(const WaveBuffers& B, int depth, cudaStream_t st) {
+    k_ray_count<<<sm_count() * 4, 256, 0, st>>>(B, depth);
+    k_conn_scan<<<1, 64, 0, st>>>(B);
+    k_ray_scatter<<<sm_count() * 8, 256, 0, st>>>(B, depth);
 }
 void launch_finalize(const FrameGPU& F, const WaveBuffers& B, float scale, int overwrite, cudaStream_t st) {
     const int64_t WH = F.bandPix ? (int64_t)F.bandPix : (int64_t)F.W * F.H;

@@ -46,6 +46,8 @@ void launch_shade(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, in
 void launch_connect(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int persistentBlocks, cudaStream_t st);
 /* path lengths startDepth..maxDepth of the frame's remaining paths, one persistent launch */
 void launch_tail(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int startDepth, int persistentBlocks, cudaStream_t st);
+/* the extension queue of wave `depth` (>= 2) regrouped by direction octant into sortO/D/E (O, D, T) */
+void launch_sort_rays(const WaveBuffers& B, int depth, cudaStream_t st);
 /* the connections of wave `depth` regrouped by light into sortO/D/E (counting sort over 64 bins) */
 void launch_sort_connections(const WaveBuffers& B, int depth, cudaStream_t st);
 /* per-pixel sums of the frame's paths into the accumulator (from zero when overwrite != 0), then the frame */

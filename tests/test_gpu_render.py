@@ -243,3 +243,24 @@ def test_all_rays_miss(spheres_small):
     c = core.render_ex(view, p, counters=True)["counters"]
     assert c.sum() == 0, c.tolist()
     assert np.isfinite(img).all() and img[:, :3].min() > 0
+
+
+@pytest.mark.parametrize("tail", [0, 5])
+def test_rays_grouped_by_octant_change_nothing(core_lib, oracle_lib, tail):
+    """Regrouping each bounce wave's extension rays by direction octant before the closest-hit queries (setting
+    "sortRays") reorders work only: hit records, RNG states, queue counts and radiance equal the oracle's."""
+    sc = S.spheres_2m(seed=5, n_spheres=6, slices=40, stacks=26, tex_size=64)
+    W, H = 160, 96
+    view = S.spheres_view(W, H, frame=1)
+    p = make_params(W, H, 2, max_depth=7, rr_start=3, camera_r0=camera_r0(0), flags=RP_NEE | RP_DEPTH_W)
+    core = RenderCore()
+    core.set_scene(sc)
+    core.SetTarget(W, H, 2)
+    core.Setting("waveTail", tail)
+    core.Setting("sortRays", 1)
+    o = oracle_lib.Oracle()
+    o.set_scene(sc)
+    _check_frame(core, o, view, p)
+    core.Setting("sortConnections", 1)   # both regroupings share the sort buffers
+    _check_frame(core, o, view, p)
+    core.close()
