@@ -48,6 +48,13 @@ namespace lh2g {
 #ifndef LH2G_SORT_ANYHIT
 #define LH2G_SORT_ANYHIT 0
 #endif
+/* LH2G_SHORT_STACK K (a power of two, 0: off): the top K entries of a lane's stack live in shared memory, a ring of
+ * K slots strided by the block size; older entries spill to the local-memory stack when the ring is full and are
+ * popped back from there. Every kernel that traverses with it runs LH2G_TRAV_BLOCK threads per block. */
+#ifndef LH2G_SHORT_STACK
+#define LH2G_SHORT_STACK 0
+#endif
+constexpr int LH2G_TRAV_BLOCK = 128;
 /* with LH2G_REFILL: idle lanes of a warp take new rays once at least this many are idle (or all are) */
 #ifndef LH2G_REFILL_MIN
 #define LH2G_REFILL_MIN 1
@@ -111,6 +118,41 @@ struct Traversal {
     float3 Ow, Dw, O, D, invD;
     float tmin, tmax;
     int sp, curInst;
+#if LH2G_SHORT_STACK
+    int base;   /* entries [0, base) are in the local stack, [base, sp) in the lane's shared ring */
+    /* the lane's ring: slot j at ring()[j * LH2G_TRAV_BLOCK] (one ring per lane, shared by the lane's traversals) */
+    static __device__ __forceinline__ uint2* ring() {
+        __shared__ uint2 shortStack[LH2G_SHORT_STACK * LH2G_TRAV_BLOCK];
+        return shortStack + threadIdx.x;
+    }
+#endif
+    /* pushes one entry; the caller has checked sp < LH2G_STACK */
+    __device__ __forceinline__ void push(const uint2 e) {
+#if LH2G_SHORT_STACK
+        uint2* r = ring();
+        if (sp - base == LH2G_SHORT_STACK) {
+            stack[base] = r[(base & (LH2G_SHORT_STACK - 1)) * LH2G_TRAV_BLOCK];
+            base++;
+        }
+        r[(sp & (LH2G_SHORT_STACK - 1)) * LH2G_TRAV_BLOCK] = e;
+        sp++;
+#else
+        stack[sp++] = e;
+#endif
+    }
+    /* removes and returns the top entry; the caller has checked sp > 0 */
+    __device__ __forceinline__ uint2 take() {
+#if LH2G_SHORT_STACK
+        if (sp == base) {
+            base = --sp;
+            return stack[sp];
+        }
+        --sp;
+        return ring()[(sp & (LH2G_SHORT_STACK - 1)) * LH2G_TRAV_BLOCK];
+#else
+        return stack[--sp];
+#endif
+    }
     uint32_t entry, steps, nodes, tris;
     uint32_t postponed;   /* LH2G_SPECULATIVE: a triangle leaf set aside (0: none) */
     bool found;
@@ -121,6 +163,9 @@ struct Traversal {
         invD = make_float3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
         best.t = t1, best.u = best.v = 0.0f, best.inst = -1, best.prim = NOHIT;
         found = false, sp = 0, curInst = -1, steps = 0, nodes = 0, tris = 0;
+#if LH2G_SHORT_STACK
+        base = 0;
+#endif
         entry = S.tlasRoot;
         postponed = 0u;
     }
@@ -160,7 +205,7 @@ struct Traversal {
     __device__ __forceinline__ bool pop() {
         for (;;) {
             if (sp == 0) return false;
-            const uint2 e = stack[--sp];
+            const uint2 e = take();
             entry = e.x;
             if (entry == ENTRY_MARKER || ANYHIT || (entry >> 30) == 2u) return true;
             if (!found || __uint_as_float(e.y) <= best.t) return true;
@@ -233,7 +278,7 @@ struct Traversal {
             if (kk == 0xffffffffu || kk == best) continue;
             const uint32_t meta = __byte_perm(metaLo, metaHi, kk & 7u) & 255u;
             const uint32_t code = (meta & 0x80u) ? n1.x + (meta & 7u) : leafBase + ((meta >> 5) << 28) + (meta & 31u);
-            if (sp < LH2G_STACK) stack[sp++] = make_uint2(code, kk & ~7u);
+            if (sp < LH2G_STACK) push(make_uint2(code, kk & ~7u));
             else status |= LH2G_STATUS_STACK_OVERFLOW;
         }
         return true;
@@ -253,7 +298,7 @@ struct Traversal {
                 if (kk == 0xffffffffu) continue;
                 const uint32_t meta = __byte_perm(metaLo, metaHi, kk & 7u) & 255u;   /* byte (slot) of the 8 meta bytes */
                 const uint32_t code = (meta & 0x80u) ? n1.x + (meta & 7u) : leafBase + ((meta >> 5) << 28) + (meta & 31u);
-                stack[sp++] = make_uint2(code, kk & ~7u);
+                push(make_uint2(code, kk & ~7u));
             }
         } else {
 #pragma unroll
@@ -262,7 +307,7 @@ struct Traversal {
                 if (kk == 0xffffffffu) continue;
                 const uint32_t meta = __byte_perm(metaLo, metaHi, kk & 7u) & 255u;
                 const uint32_t code = (meta & 0x80u) ? n1.x + (meta & 7u) : leafBase + ((meta >> 5) << 28) + (meta & 31u);
-                if (sp < LH2G_STACK) stack[sp++] = make_uint2(code, kk & ~7u);
+                if (sp < LH2G_STACK) push(make_uint2(code, kk & ~7u));
                 else status |= LH2G_STATUS_STACK_OVERFLOW;
             }
         }
@@ -320,7 +365,7 @@ struct Traversal {
             const uint32_t first = entry & 0x0fffffffu, cnt = ((entry >> 28) & 3u) + 1u;
             /* a full stack drops work: the status word says so (the hit record may then be wrong) */
             if (cnt > 1u) {
-                if (sp < LH2G_STACK) stack[sp++] = make_uint2(0x80000000u | ((cnt - 2u) << 28) | (first + 1u), 0u);
+                if (sp < LH2G_STACK) push(make_uint2(0x80000000u | ((cnt - 2u) << 28) | (first + 1u), 0u));
                 else status |= LH2G_STATUS_STACK_OVERFLOW;
             }
             const int ii = (int)__ldg(S.tlasPrims + first);
@@ -334,7 +379,7 @@ struct Traversal {
                 O = xform_point(m, Ow), D = xform_vector(m, Dw);
                 invD = make_float3(safe_rcp(D.x), safe_rcp(D.y), safe_rcp(D.z));
                 curInst = ii;
-                stack[sp++] = make_uint2(ENTRY_MARKER, 0u);
+                push(make_uint2(ENTRY_MARKER, 0u));
                 entry = root;
                 return true;
             }

@@ -10,6 +10,7 @@ namespace lh2g {
 namespace {
 
 constexpr int WAVE_BLOCK = 128;
+static_assert(WAVE_BLOCK == LH2G_TRAV_BLOCK, "traversal kernels run LH2G_TRAV_BLOCK threads per block");
 constexpr int NRC_DEPTH = 2;   /* first path length at which radiance-cache frames query the cache */
 #ifndef LH2G_NRC_TRAIN_SHIFT
 #define LH2G_NRC_TRAIN_SHIFT 5
