@@ -370,6 +370,75 @@ def estimators_leg(core, sc, W, H, steps):
     return out
 
 
+def raster_leg(core, sc, W, H, steps, cpu, device):
+    """The SoftRasterizer core (lh2g_raster_render) on the path tracer's scenes: the 2M-triangle sphere field at
+    W x H (8 camera poses; the core already holds the scene and the target) and the closed room at 512 x 512. Device
+    time per frame by CUDA events on the core's stream (no host copies); e2e with every frame's pixels copied to host
+    memory; parity: pixels and z-buffer of two poses equal the oracle's bit for bit (outside the timed regions); CPU
+    baseline: the oracle's single-threaded restatement (the reference rasterizer is single-threaded) on a few frames."""
+    import numpy as np
+    import torch
+    from lighthouse2_gb300 import scenes as S
+    from lighthouse2_gb300.core import RenderCore
+    peak, peak_kind = peaks()
+
+    def one(core, views, W, H, sc, label):
+        stream = torch.cuda.ExternalStream(core.stream_ptr())
+        for k in range(3):
+            core.raster(views[k % len(views)], pixels=False)
+        st = core.raster(views[0], pixels=False, stats=True)["stats"]
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record()
+        for k in range(steps):
+            core.raster(views[k % len(views)], pixels=False)
+        with torch.cuda.stream(stream):
+            e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        t = time.perf_counter()
+        for k in range(steps):
+            core.raster(views[k % len(views)])
+        ms_e2e = (time.perf_counter() - t) / steps * 1e3
+        out = {"workload": label, "ms_per_frame": ms, "frames_per_s": 1e3 / ms, "Mtriangles_per_s": st["triangles"] / (ms / 1e3) / 1e6,
+               "e2e": {"ms_per_frame": ms_e2e, "Mtriangles_per_s": st["triangles"] / (ms_e2e / 1e3) / 1e6, "d2h_bytes_per_frame": 4 * W * H},
+               "stats_pose0": st}
+        # bytes a frame must move: every kept triangle's vertices and face normal (60 B), the pixels written (4 B)
+        alg = st["triangles"] * 60 + 4 * W * H
+        out["roofline"] = {"bound": "hbm", "achieved": alg / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                           "frac": alg / (ms / 1e3) / 1e9 / peak, "peak_source": peak_kind, "algorithmic_bytes_per_frame": alg,
+                           "note": "two passes (depth keys, then colour) and per-triangle setup; issue- and latency-bound, not HBM-bound"}
+        if cpu:
+            from oracle.bind import Oracle
+            o = Oracle()
+            o.set_scene(sc)
+            same = True
+            for k in (0, len(views) // 2):
+                r = o.raster(views[k], W, H)
+                g = core.raster(views[k], depth=True)
+                same = same and np.array_equal(r["pixels"], g["pixels"]) and np.array_equal(r["zbuffer"].view(np.uint32), g["zbuffer"].view(np.uint32))
+            n = 3
+            t = time.perf_counter()
+            for k in range(n):
+                o.raster(views[k % len(views)], W, H)
+            cms = (time.perf_counter() - t) / n * 1e3
+            out["parity_vs_oracle"] = same
+            out["cpu_baseline"] = {"value": st["triangles"] / (cms / 1e3) / 1e6, "unit": "Mtriangles/s", "ms_per_frame": cms, "cores": 1,
+                                   "kind": "port", "sample": f"{n} frames of the same poses, single-threaded like the reference"}
+        return out
+
+    res = {"spheres_2m": one(core, [S.spheres_view(W, H, frame=k) for k in range(8)], W, H, sc,
+                             f"spheres_2m (2,048,002 triangles) {W}x{H}, 8 camera poses")}
+    cb = S.cornell_sphere(subdiv=6)
+    core_c = RenderCore(device)
+    core_c.set_scene(cb)
+    core_c.SetTarget(512, 512, 1)
+    res["cornell"] = one(core_c, [S.cornell_view(512, 512, frame=k) for k in range(8)], 512, 512, cb, "cornell_sphere subdiv 6 (81,932 triangles) 512x512")
+    core_c.close()
+    return res
+
+
 def svgf_leg(core, W, H, steps, warmup):
     """Filter-core frames with SVGF + TAA over the 8-pose camera path (Restart every frame, as a moving camera
     does); the filter passes are timed by the core's own events (coreStats.filterTime)."""
@@ -733,6 +802,7 @@ def run_gb300(args):
         core_c.close()
     svgf = svgf_leg(core, W, H, max(args.steps, 8), args.warmup) if not args.no_svgf else None
     estimators = estimators_leg(core, sc, W, H, max(args.steps, 8)) if not args.no_estimators and rank == 0 else None
+    raster = raster_leg(core, sc, W, H, max(args.steps, 8), world == 1 and not args.no_cpu_baseline, local) if not args.no_raster and rank == 0 else None
     serving = serving_leg(args) if (not args.no_serving and rank == 0) else None
     nrc = None
     if not args.no_nrc and rank == 0:
@@ -797,6 +867,8 @@ def run_gb300(args):
         line["svgf"] = svgf
     if estimators is not None:
         line["estimators"] = estimators
+    if raster is not None:
+        line["rasterizer"] = raster
     if serving is not None:
         line["serving"] = serving
     if nrc is not None:
@@ -837,6 +909,7 @@ def main():
                     help="under torchrun: replicas (every rank renders whole frames) or rows (every frame's rows split over the ranks)")
     ap.add_argument("--sort-connections", type=int, default=0, help="group connections by light before the any-hit queries")
     ap.add_argument("--sort-rays", type=int, default=0, help="group bounce waves' extension rays by direction octant")
+    ap.add_argument("--no-raster", action="store_true", help="skip the SoftRasterizer leg")
     ap.add_argument("--wave-tail", type=int, default=WAVE_TAIL, help="first path length of the persistent tail kernel (0: off)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -185,6 +185,30 @@ LH2G_API int lh2g_trace_host(lh2g_context* ctx, const lh2g_ray* rays, void* out,
 LH2G_API int lh2g_render_noalloc(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* params, float* accumDevice,
                                  void* stream, uint32_t* statusHost);
 
+/* ---- SoftRasterizer core ----
+ * Replaces RenderCore_SoftRasterizer's Render (lib/RenderCore_SoftRasterizer/rendercore.cpp:213-227 over
+ * rasterizer.cpp:66-171,225-240): z-buffered scanline rasterisation of the context's instances (meshes, instance
+ * transforms, materials' base colour or colour texture) into the target set by lh2g_set_target (3..8192 pixels per
+ * side; spp is ignored), with the reference core's fixed projection (focal length = target width), its near plane
+ * at z = -0.2, back-face culling by the triangles' face normals and flat shading by their object-space normal z.
+ * Pixels are RGBA8 words, 0 where nothing was drawn (the reference's memset) and for the one-pixel border it never
+ * draws; instances that share a mesh all take the transform set last for it (the reference's scene graph holds
+ * one transform per mesh). Results equal the reference core's pixel for pixel and its z-buffer bit for bit.
+ * The frame runs on the context stream; pixelsHost / depthHost (W*H words, may be NULL) receive the image and the
+ * z-buffer (interpolated 1/z of each drawn pixel, 0 elsewhere), and stats (may be NULL) the frame's counts; with
+ * any of them the call returns when the frame is done. lh2g_raster_pixels_device gives the device image of the
+ * last frame (valid until the next raster frame or lh2g_destroy; NULL before the first). */
+typedef struct lh2g_raster_stats {
+    uint32_t instancesDrawn;   /* instances the mesh culling kept */
+    uint32_t triangles;        /* their triangles */
+    uint32_t smallTriangles;   /* triangles rasterised one per thread that offered fragments */
+    uint32_t bigTriangles;     /* triangles rasterised one block per 128 rows */
+    uint32_t fragments;        /* fragments offered to the depth test (1/z < 0) */
+    uint32_t status;           /* nonzero: a triangle named a missing material (not drawn) */
+} lh2g_raster_stats;
+LH2G_API int lh2g_raster_render(lh2g_context* ctx, const lh2g_view* view, uint32_t* pixelsHost, float* depthHost, lh2g_raster_stats* stats);
+LH2G_API uint32_t* lh2g_raster_pixels_device(lh2g_context* ctx);
+
 /* ---- serving loop (no counterpart in the reference, whose cores render one frame at a time) ----
  * Render and ray-query jobs of several resident scenes, continuously batched: jobs are admitted smallest first
  * (oldest first once one has waited 0.2 s) while their paths fit in the server's path capacity (the admission

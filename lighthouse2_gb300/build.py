@@ -23,7 +23,7 @@ OUT = os.path.join(HERE, "_build")
 LIB_NAME = "libRenderCore_GB300.so"
 LIB = os.path.join(OUT, LIB_NAME)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["bvh_build.cu", "kernels.cu", "adaptive.cu", "svgf.cu", "capi.cu", "rendercore.cu", "noalloc.cu", "server.cu", "nrc.cu"]
+SOURCES = ["bvh_build.cu", "kernels.cu", "adaptive.cu", "svgf.cu", "capi.cu", "rendercore.cu", "noalloc.cu", "server.cu", "nrc.cu", "raster.cu"]
 
 
 def nvcc():

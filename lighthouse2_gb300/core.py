@@ -51,7 +51,7 @@ C_API = ["lh2g_create", "lh2g_destroy", "lh2g_last_error", "lh2g_set_geometry", 
          "lh2g_nrc_create", "lh2g_nrc_destroy", "lh2g_nrc_last_error", "lh2g_nrc_get_spec", "lh2g_nrc_set_params", "lh2g_nrc_get_params",
          "lh2g_nrc_get_grads", "lh2g_nrc_infer", "lh2g_nrc_train", "lh2g_nrc_apply_update", "lh2g_nrc_infer_counted", "lh2g_nrc_train_counted",
          "lh2g_nrc_last_loss", "lh2g_nrc_wait_selftest", "lh2g_render_nrc", "lh2g_nrc_infer_host", "lh2g_nrc_train_host",
-         "lh2g_set_blue_noise", "lh2g_render_adaptive", "lh2g_set_adaptive_scale"]
+         "lh2g_set_blue_noise", "lh2g_render_adaptive", "lh2g_set_adaptive_scale", "lh2g_raster_render", "lh2g_raster_pixels_device"]
 
 _lib = None
 
@@ -107,6 +107,9 @@ def load_library(path: str | None = None):
     lib.lh2g_set_blue_noise.argtypes = [vp, vp, vp, vp]
     lib.lh2g_render_adaptive.argtypes = [vp, vp, vp, i, vp, vp, vp, vp]
     lib.lh2g_set_adaptive_scale.argtypes = [vp, f]
+    lib.lh2g_raster_render.argtypes = [vp, vp, vp, vp, vp]
+    lib.lh2g_raster_pixels_device.argtypes = [vp]
+    lib.lh2g_raster_pixels_device.restype = vp
     if path is None:
         _lib = lib
     return lib
@@ -269,6 +272,25 @@ class RenderCore:
         if capture:
             out["hits"], out["seeds"] = hits.reshape(D, P), seeds.reshape(D, P)
         return out
+
+    def raster(self, view, pixels=True, depth=False, stats=False):
+        """One SoftRasterizer frame of the target's size (lh2g_raster_render): RGBA8 pixels (uint32, W*H), the
+        z-buffer (float32) and the frame's counts, as asked."""
+        px = np.zeros(self.W * self.H, np.uint32) if pixels else None
+        zb = np.zeros(self.W * self.H, np.float32) if depth else None
+        st = np.zeros(6, np.uint32) if stats else None
+        self._check(self.lib.lh2g_raster_render(self.ctx, _p(np.ascontiguousarray(view)), _p(px), _p(zb), _p(st)), "raster_render")
+        out = {}
+        if pixels:
+            out["pixels"] = px
+        if depth:
+            out["zbuffer"] = zb
+        if stats:
+            out["stats"] = dict(zip(["instancesDrawn", "triangles", "smallTriangles", "bigTriangles", "fragments", "status"], map(int, st)))
+        return out
+
+    def raster_pixels_device(self):
+        return self.lib.lh2g_raster_pixels_device(self.ctx)
 
     def set_adaptive_scale(self, dev_scale):
         self._check(self.lib.lh2g_set_adaptive_scale(self.ctx, float(dev_scale)), "set_adaptive_scale")

@@ -28,6 +28,7 @@
 #include "kernels.cuh"
 #include "lh2g.h"
 #include "svgf.cuh"
+#include "raster.cuh"
 
 using namespace lh2g;
 
@@ -268,6 +269,20 @@ struct lh2g_context {
         bool scaleDirty = true;
         bool last = false;              /* the last frame was adaptive: its statistics include the second wave */
     } ad;
+    /* SoftRasterizer frames (lh2g_raster_render): pixels, depth keys, the passes' triangle lists and counters, the
+     * kept instances and the materials as the rasterizer reads them */
+    struct Raster {
+        uint32_t* pixels = nullptr;
+        unsigned long long* keys = nullptr;
+        float* depth = nullptr;
+        uint32_t *list = nullptr, *big = nullptr, *counters = nullptr;
+        RasterInst* inst = nullptr;
+        RasterMat* mats = nullptr;
+        int64_t pixCap = 0, triCap = 0;
+        int instCap = 0, matCap = 0;
+        int W = 0, H = 0;               /* size of the last frame */
+        bool valid = false;
+    } rs;
 };
 
 namespace {
@@ -491,6 +506,8 @@ int lh2g_destroy(lh2g_context* ctx) {
     dfree(ctx->pool), dfree(ctx->triData), dfree(ctx->instGPU), dfree(ctx->tlasPrims), dfree(ctx->instTris), dfree(ctx->instInvRows);
     dfree(ctx->traceFetch), dfree(ctx->hostRaysDev), dfree(ctx->hostOutDev);
     dfree(ctx->B.capHits), dfree(ctx->B.capSeeds);
+    dfree(ctx->rs.pixels), dfree(ctx->rs.keys), dfree(ctx->rs.depth), dfree(ctx->rs.list), dfree(ctx->rs.big), dfree(ctx->rs.counters);
+    dfree(ctx->rs.inst), dfree(ctx->rs.mats);
     free_target(ctx);
     if (ctx->hostCounters) cudaFreeHost(ctx->hostCounters);
     if (ctx->ad.hostState) cudaFreeHost(ctx->ad.hostState);
@@ -1637,3 +1654,176 @@ int context_scene(lh2g_context* ctx, SceneGPU* scene, int* device, int* blocks4,
     return LH2G_OK;
 }
 }  // namespace lh2g
+
+/* ======================================================================================================
+ * SoftRasterizer core (lib/RenderCore_SoftRasterizer): the frame's host half. The camera transform
+ * (rendercore.cpp:215-222), its inverse (rasterizer.cpp:239), the per-mesh transforms (SGNode::Render,
+ * rasterizer.cpp:185-190), the frustum planes (Rasterizer::Reinit, :205-214) and the mesh culling (:69-75) are a
+ * few hundred flops per frame and run here, in the reference's operation order (host code is built without FMA
+ * contraction); the triangles run on the device (raster.cu).
+ * ==================================================================================================== */
+namespace {
+
+struct RsM { float m[16]; };
+struct RsV { float x, y, z; };
+RsV rs_sub(RsV a, RsV b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+float rs_dot(RsV a, RsV b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+RsV rs_cross(RsV a, RsV b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+RsV rs_normalize(RsV v) { const float inv = 1.0f / sqrtf(rs_dot(v, v)); return {v.x * inv, v.y * inv, v.z * inv}; }
+/* operator*(mat4, mat4), lib/platform/system.cpp:57-68 */
+RsM rs_mul(const float* a, const float* b) {
+    RsM r;
+    for (int i = 0; i < 16; i += 4)
+        for (int j = 0; j < 4; j++) r.m[i + j] = a[i] * b[j] + a[i + 1] * b[j + 4] + a[i + 2] * b[j + 8] + a[i + 3] * b[j + 12];
+    return r;
+}
+int rs_f2i(float x) {   /* truncation, saturating, NaN -> 0 (as the device's conversion) */
+    if (x != x) return 0;
+    if (x >= 2147483648.0f) return 2147483647;
+    if (x <= -2147483648.0f) return (int)0x80000000u;
+    return (int)x;
+}
+
+}  // namespace
+
+int lh2g_raster_render(lh2g_context* ctx, const lh2g_view* view, uint32_t* pixelsHost, float* depthHost, lh2g_raster_stats* stats) {
+    if (!ctx || !view) return LH2G_ERR_INVALID;
+    const int W = ctx->W, H = ctx->H;
+    if (W < 3 || H < 3 || W > 8192 || H > 8192) return fail(ctx, LH2G_ERR_INVALID, "raster_render: the target must be 3..8192 pixels on each side");
+    if (!materials_cover_meshes(ctx)) return fail(ctx, LH2G_ERR_INVALID, "raster_render: a triangle names a missing material");
+    cudaSetDevice(ctx->device);
+    JOIN();
+    auto& R0 = ctx->rs;
+    /* frustum planes (rasterizer.cpp:205-214) */
+    float4 fr[5];
+    {
+        const float w = (float)W, h = (float)H;
+        const float C = -1.0f, x1 = 0.5f, x2 = W - 1.5f, y1 = 0.5f, y2 = H - 1.5f;
+        const RsV p0 = {0.0f, 0.0f, 0.0f};
+        const RsV p1 = {((x1 - w * 0.5f) * C) / w, ((y1 - h * 0.5f) * C) / w, 1.0f};
+        const RsV p2 = {((x2 - w * 0.5f) * C) / w, ((y1 - h * 0.5f) * C) / w, 1.0f};
+        const RsV p3 = {((x2 - w * 0.5f) * C) / w, ((y2 - h * 0.5f) * C) / w, 1.0f};
+        const RsV p4 = {((x1 - w * 0.5f) * C) / w, ((y2 - h * 0.5f) * C) / w, 1.0f};
+        const RsV a = rs_normalize(rs_cross(rs_sub(p1, p0), rs_sub(p4, p1))), b = rs_normalize(rs_cross(rs_sub(p2, p0), rs_sub(p1, p2)));
+        const RsV c = rs_normalize(rs_cross(rs_sub(p3, p0), rs_sub(p2, p3))), d = rs_normalize(rs_cross(rs_sub(p4, p0), rs_sub(p3, p4)));
+        fr[0] = make_float4(0.0f, 0.0f, -1.0f, 0.2f);
+        fr[1] = make_float4(a.x, a.y, a.z, 0.0f), fr[2] = make_float4(b.x, b.y, b.z, 0.0f);
+        fr[3] = make_float4(c.x, c.y, c.z, 0.0f), fr[4] = make_float4(d.x, d.y, d.z, 0.0f);
+    }
+    /* camera transform, inverted, times the scene root's identity (rendercore.cpp:215-222, rasterizer.cpp:187,239) */
+    RsM root;
+    {
+        const RsV pos = {view->pos[0], view->pos[1], view->pos[2]}, p1 = {view->p1[0], view->p1[1], view->p1[2]};
+        const RsV p2 = {view->p2[0], view->p2[1], view->p2[2]}, p3 = {view->p3[0], view->p3[1], view->p3[2]};
+        const RsV X = rs_normalize(rs_sub(p2, p1)), Y = rs_normalize(rs_sub(p1, p3));
+        const RsV mid = {0.5f * (p2.x + p3.x), 0.5f * (p2.y + p3.y), 0.5f * (p2.z + p3.z)};
+        const RsV Z = rs_normalize(rs_sub(pos, mid));
+        float Rm[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+        Rm[0] = X.x, Rm[4] = X.y, Rm[8] = X.z;
+        Rm[1] = Y.x, Rm[5] = Y.y, Rm[9] = Y.z;
+        Rm[2] = Z.x, Rm[6] = Z.y, Rm[10] = Z.z;
+        const float Tr[16] = {1, 0, 0, pos.x, 0, 1, 0, pos.y, 0, 0, 1, pos.z, 0, 0, 0, 1};
+        const RsM cam = rs_mul(Tr, Rm);
+        float inv[16];
+        invert4x4(cam.m, inv);
+        const float I[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+        root = rs_mul(inv, I);
+    }
+    /* instances sharing a mesh share its scene-graph node and with it the transform set last (rendercore.cpp:118-131) */
+    std::vector<const float*> meshT(ctx->meshes.size(), nullptr);
+    for (const InstHost& in : ctx->inst) meshT[in.mesh] = in.T;
+    std::vector<RasterInst> kept;
+    uint32_t total = 0;
+    for (const InstHost& in : ctx->inst) {
+        const MeshDev& m = ctx->meshes[in.mesh];
+        if (!m.n) continue;
+        const RsM M = rs_mul(root.m, meshT[in.mesh]);
+        /* cull the mesh's bounding box (rasterizer.cpp:69-75): out when every corner is outside one plane */
+        bool culled = false;
+        for (int p = 0; p < 5 && !culled; p++) {
+            int i = 0;
+            for (; i < 8; i++) {
+                const float bx = (i & 1) ? m.bmax[0] : m.bmin[0], by = ((i >> 1) & 1) ? m.bmax[1] : m.bmin[1], bz = (i >> 2) ? m.bmax[2] : m.bmin[2];
+                const RsV c = {M.m[0] * bx + M.m[1] * by + M.m[2] * bz + M.m[3] * 1.0f, M.m[4] * bx + M.m[5] * by + M.m[6] * bz + M.m[7] * 1.0f,
+                               M.m[8] * bx + M.m[9] * by + M.m[10] * bz + M.m[11] * 1.0f};
+                if ((rs_dot({fr[p].x, fr[p].y, fr[p].z}, c) - fr[p].w) > 0) break;
+            }
+            culled = i == 8;
+        }
+        if (culled) continue;
+        if ((uint64_t)total + m.n >= (1ull << 32)) return fail(ctx, LH2G_ERR_INVALID, "raster_render: more than 2^32 triangles in view");
+        RasterInst r;
+        memcpy(r.M, M.m, sizeof(r.M));
+        r.verts = m.verts, r.tris = m.tris, r.first = total, r.count = m.n, r.pad[0] = r.pad[1] = 0;
+        kept.push_back(r);
+        total += m.n;
+    }
+    /* materials (rendercore.cpp:166-185) */
+    std::vector<RasterMat> mats(std::max<size_t>(1, ctx->hostMats.size()));
+    for (size_t i = 0; i < ctx->hostMats.size(); i++) {
+        const lh2g_material& hm = ctx->hostMats[i];
+        const int t = hm.color_map.texture;
+        RasterMat rm;
+        rm.diffuse = ((uint32_t)rs_f2i(hm.color[2] * 255.0f) << 16) + ((uint32_t)rs_f2i(hm.color[1] * 255.0f) << 8) + (uint32_t)rs_f2i(hm.color[0] * 255.0f);
+        if (t >= 0 && t < (int)ctx->texFirst.size()) rm.texFirst = ctx->texFirst[t], rm.width = ctx->texWH[2 * t], rm.height = ctx->texWH[2 * t + 1];
+        else rm.texFirst = 0, rm.width = 0, rm.height = 0;
+        mats[i] = rm;
+    }
+    /* buffers */
+    const int64_t WH = (int64_t)W * H;
+    if (WH > R0.pixCap) {
+        CK(dalloc(R0.pixels, WH));
+        CK(dalloc(R0.keys, WH));
+        dfree(R0.depth);
+        R0.pixCap = WH;
+    }
+    if ((int64_t)total > R0.triCap) {
+        CK(dalloc(R0.list, total));
+        CK(dalloc(R0.big, total));
+        R0.triCap = total;
+    }
+    if (!R0.counters) CK(dalloc(R0.counters, 4));
+    if ((int)kept.size() > R0.instCap) {
+        CK(dalloc(R0.inst, kept.size()));
+        R0.instCap = (int)kept.size();
+    }
+    if ((int)mats.size() > R0.matCap) {
+        CK(dalloc(R0.mats, mats.size()));
+        R0.matCap = (int)mats.size();
+    }
+    cudaStream_t st = ctx->st;
+    if (!kept.empty()) CK(cudaMemcpyAsync(R0.inst, kept.data(), sizeof(RasterInst) * kept.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(R0.mats, mats.data(), sizeof(RasterMat) * mats.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(R0.pixels, 0, sizeof(uint32_t) * WH, st));
+    CK(cudaMemsetAsync(R0.keys, 0xff, sizeof(unsigned long long) * WH, st));
+    CK(cudaMemsetAsync(R0.counters, 0, 4 * sizeof(uint32_t), st));
+    RasterFrame F;
+    F.W = W, F.H = H, F.nearPlane = fr[0], F.leftPlane = fr[1];
+    F.inst = R0.inst, F.nInst = (int)kept.size(), F.total = total;
+    F.mats = R0.mats, F.nMats = (uint32_t)ctx->hostMats.size(), F.texels = ctx->texels;
+    F.pixels = R0.pixels, F.keys = R0.keys, F.list = R0.list, F.big = R0.big, F.counters = R0.counters;
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    launch_raster(F, sms, st);
+    CK(cudaGetLastError());
+    if (depthHost) {
+        if (!R0.depth) CK(dalloc(R0.depth, R0.pixCap));
+        launch_raster_depth(F, R0.depth, st);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(depthHost, R0.depth, sizeof(float) * WH, cudaMemcpyDeviceToHost, st));
+    }
+    if (pixelsHost) CK(cudaMemcpyAsync(pixelsHost, R0.pixels, sizeof(uint32_t) * WH, cudaMemcpyDeviceToHost, st));
+    R0.W = W, R0.H = H, R0.valid = true;
+    if (stats) {
+        uint32_t c[4];
+        CK(cudaMemcpyAsync(c, R0.counters, sizeof(c), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        stats->instancesDrawn = (uint32_t)kept.size(), stats->triangles = total;
+        stats->smallTriangles = c[0], stats->bigTriangles = c[1], stats->fragments = c[2], stats->status = c[3];
+    } else if (pixelsHost || depthHost) {
+        CK(cudaStreamSynchronize(st));
+    }
+    return LH2G_OK;
+}
+
+uint32_t* lh2g_raster_pixels_device(lh2g_context* ctx) { return ctx && ctx->rs.valid ? ctx->rs.pixels : nullptr; }

@@ -93,6 +93,7 @@ class Oracle:
         L.lh2o_svgf_frame.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         L.lh2o_set_blue_noise.argtypes = [C.c_void_p] * 4
         L.lh2o_render_adaptive.argtypes = [C.c_void_p] * 12 + [C.c_int]
+        L.lh2o_raster.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         self.s = L.lh2o_create()
         self._keep = []
 
@@ -193,6 +194,15 @@ class Oracle:
             out["hits"] = hits.reshape(D, -1)
             out["seeds"] = seeds.reshape(D, -1)
         return out
+
+
+    def raster(self, view, W, H):
+        """One SoftRasterizer frame: W*H RGBA8 pixels (uint32), the z-buffer (float32) and the depth-test passes."""
+        px = np.zeros(W * H, np.uint32)
+        zb = np.zeros(W * H, np.float32)
+        frags = np.zeros(1, np.uint64)
+        assert self.lib.lh2o_raster(self.s, _p(view), W, H, _p(px), _p(zb), _p(frags)) == 0
+        return {"pixels": px, "zbuffer": zb, "fragments": int(frags[0])}
 
 
 class NrcSpec(C.Structure):
@@ -692,6 +702,35 @@ class RefAdaptive(RefKernels):
         L.ref_ad_finalize(_p(facc), _p(accum), _p(frame), W, H, st + spp, spp)
         return {"dev_scale": float(ds), "frame": frame, "counters": counters, "adaptive_paths": count, "frame_acc": facc,
                 "frame_acc_wave1": facc_wave1, "features": feat_wave1, "deviation": dev, "flushed": flushed[0]}
+
+
+class RefRaster:
+    """The reference's SoftRasterizer core compiled for the host (oracle/ref/ref_raster.cpp), driven through its own
+    RenderCore methods (lib/RenderCore_SoftRasterizer/rendercore.cpp)."""
+
+    def __init__(self):
+        if build_ref() is None:
+            raise FileNotFoundError("reference tree not available")
+        self.lib = C.CDLL(REF_LIB)
+        self.lib.ref_raster.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                        C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+
+    def raster(self, sc: S.Scene, view, W, H):
+        nm = len(sc.meshes)
+        tri_count = np.array([len(m.tris) for m in sc.meshes], np.int32)
+        verts = [np.ascontiguousarray(m.vertices, np.float32) for m in sc.meshes]
+        tris = [np.ascontiguousarray(m.tris) for m in sc.meshes]
+        vp = (C.c_void_p * max(1, nm))(*[v.ctypes.data for v in verts])
+        tp = (C.c_void_p * max(1, nm))(*[t.ctypes.data for t in tris])
+        inst_mesh = np.array([mi for mi, _ in sc.instances], np.int32)
+        inst_t = np.ascontiguousarray(np.array([np.asarray(T, np.float32).reshape(16) for _, T in sc.instances], np.float32).reshape(-1))
+        texdesc, keep = texture_descs(sc.textures)
+        px = np.zeros(W * H, np.uint32)
+        zb = np.zeros(W * H, np.float32)
+        rc = self.lib.ref_raster(W, H, nm, _p(tri_count), C.cast(vp, C.c_void_p), C.cast(tp, C.c_void_p), len(sc.instances), _p(inst_mesh),
+                                 _p(inst_t), len(sc.materials), _p(sc.materials), len(sc.textures), _p(texdesc), _p(view), _p(px), _p(zb))
+        assert rc == 0
+        return {"pixels": px, "zbuffer": zb}
 
 
 def pack_materials(oracle: Oracle, sc: S.Scene):

@@ -290,6 +290,7 @@ struct BVH2 {
 
 struct Mesh {
     std::vector<lh2g_core_tri> tris;
+    std::vector<f3> pos;          /* the vertex buffer, 3 per triangle (the rasteriser transforms it) */
     std::vector<f3> v0, e1, e2;   /* intersection data: v0, v1 - v0, v2 - v0 from the vertex buffer */
     BVH2 bvh;
     float bmin[3], bmax[3];
@@ -1977,6 +1978,194 @@ inline int adaptive_wanted(const float d) {
 /* ==========================================================================================================
  * C API
  * ======================================================================================================== */
+namespace {
+
+/* ======================================================================================================
+ * SoftRasterizer core (lib/RenderCore_SoftRasterizer): z-buffered scanline rasterisation of every instance,
+ * restated from rasterizer.cpp:66-171 (Mesh::Render), :201-215 (Rasterizer::Reinit), :225-240
+ * (Rasterizer::Render) and rendercore.cpp:55-185,213-222 (SetGeometry / SetInstance / SetMaterials / Render).
+ * Sequential, in the reference's order: instances, then triangles, then edges, then rows and spans; a fragment
+ * replaces the pixel when its interpolated 1/z is below the z-buffer's (which starts at 0).
+ *
+ * Conversions the C++ source leaves to the platform are fixed here, and the GPU core does the same:
+ * float -> int truncates and saturates (NaN -> 0), as Arm and the GPU do (x86 returns INT_MIN out of range);
+ * float -> unsigned (the texel coordinates and the shade) truncates to a 64-bit integer and keeps its low 32
+ * bits, as x86-64 compilers emit it (0 for NaN and beyond the 64-bit range).
+ * Two guards the reference lacks, both unreachable for finite input: a span whose left end lies at x <= -1 is dropped
+ * (the reference would write into the previous row; clipping against the left plane keeps spans at x >= 0.5 up to
+ * rounding), and a fragment whose 1/z is NaN is dropped (the reference's z-test lets it through).
+ * ==================================================================================================== */
+struct RsMesh4 { float m[16]; };
+
+inline int rs_f2i(float x) {
+    if (x != x) return 0;
+    if (x >= 2147483648.0f) return 2147483647;
+    if (x <= -2147483648.0f) return (int)0x80000000u;
+    return (int)x;
+}
+inline uint rs_f2u(float x) {
+    if (!(x > -9223372036854775808.0f && x < 9223372036854775808.0f)) return 0u;
+    return (uint)(uint64_t)(int64_t)x;
+}
+/* operator*(mat4, mat4), lib/platform/system.cpp:57-68 */
+inline RsMesh4 rs_mul(const float* a, const float* b) {
+    RsMesh4 r;
+    for (int i = 0; i < 16; i += 4)
+        for (int j = 0; j < 4; j++) r.m[i + j] = a[i] * b[j] + a[i + 1] * b[j + 4] + a[i + 2] * b[j + 8] + a[i + 3] * b[j + 12];
+    return r;
+}
+/* operator*(mat4, float4), system.cpp:90-96 (the xyz rows) */
+inline f3 rs_xform(const float* a, float x, float y, float z, float w) {
+    return mk3(a[0] * x + a[1] * y + a[2] * z + a[3] * w, a[4] * x + a[5] * y + a[6] * z + a[7] * w, a[8] * x + a[9] * y + a[10] * z + a[11] * w);
+}
+/* ScaleColor, rasterizer.cpp:20-25 */
+inline uint rs_scale_color(uint c, uint scale) {
+    const uint rb = (((c & 0xff00ffu) * scale) >> 8) & 0xff00ffu;
+    const uint g = (((c & 0xff00u) * scale) >> 8) & 0xff00u;
+    return rb + g;
+}
+
+/* Rasterizer::Reinit's frustum planes (rasterizer.cpp:205-214) for a w x h target */
+void rs_frustum(int w, int h, f4* fr) {
+    const float C = -1.0f, x1 = 0.5f, x2 = w - 1.5f, y1 = 0.5f, y2 = h - 1.5f;
+    const f3 p0 = mk3(0.0f, 0.0f, 0.0f);
+    const f3 p1 = mk3(((x1 - w * 0.5f) * C) / w, ((y1 - h * 0.5f) * C) / w, 1.0f);
+    const f3 p2 = mk3(((x2 - w * 0.5f) * C) / w, ((y1 - h * 0.5f) * C) / w, 1.0f);
+    const f3 p3 = mk3(((x2 - w * 0.5f) * C) / w, ((y2 - h * 0.5f) * C) / w, 1.0f);
+    const f3 p4 = mk3(((x1 - w * 0.5f) * C) / w, ((y2 - h * 0.5f) * C) / w, 1.0f);
+    fr[0] = {0.0f, 0.0f, -1.0f, 0.2f};
+    const f3 a = normalize(cross(p1 - p0, p4 - p1)), b = normalize(cross(p2 - p0, p1 - p2));
+    const f3 c = normalize(cross(p3 - p0, p2 - p3)), d = normalize(cross(p4 - p0, p3 - p4));
+    fr[1] = {a.x, a.y, a.z, 0.0f}, fr[2] = {b.x, b.y, b.z, 0.0f}, fr[3] = {c.x, c.y, c.z, 0.0f}, fr[4] = {d.x, d.y, d.z, 0.0f};
+}
+
+/* RenderCore::Render's camera transform (rendercore.cpp:215-222), inverted as Rasterizer::Render does
+ * (rasterizer.cpp:239), times the scene root's identity transform (SGNode::Render, rasterizer.cpp:187) */
+RsMesh4 rs_view(const lh2g_view* v) {
+    const f3 pos = ld3(v->pos), p1 = ld3(v->p1), p2 = ld3(v->p2), p3 = ld3(v->p3);
+    const f3 X = normalize(p2 - p1), Y = normalize(p1 - p3), Z = normalize(pos - 0.5f * (p2 + p3));
+    float R[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    R[0] = X.x, R[4] = X.y, R[8] = X.z;
+    R[1] = Y.x, R[5] = Y.y, R[9] = Y.z;
+    R[2] = Z.x, R[6] = Z.y, R[10] = Z.z;
+    const float Tr[16] = {1, 0, 0, pos.x, 0, 1, 0, pos.y, 0, 0, 1, pos.z, 0, 0, 0, 1};
+    const RsMesh4 cam = rs_mul(Tr, R);
+    float inv[16];
+    invert4x4(cam.m, inv);
+    const float I[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    return rs_mul(inv, I);
+}
+
+/* RenderCore::SetMaterials' colour (rendercore.cpp:175-181) */
+uint rs_diffuse(const lh2g_material& m) {
+    return ((uint)rs_f2i(m.color[2] * 255.0f) << 16) + ((uint)rs_f2i(m.color[1] * 255.0f) << 8) + (uint)rs_f2i(m.color[0] * 255.0f);
+}
+
+struct RsTables { std::vector<float> xl, xr, ul, ur, vl, vr, zl, zr; };
+
+/* Mesh::Render (rasterizer.cpp:66-171) for one instance; returns the fragments that passed the depth test */
+uint64_t rs_mesh(const lh2o_scene& s, const Mesh& mesh, const float* T, const f4* fr, int W, int H, RsTables& tb, uint* pixels, float* zbuffer) {
+    /* cull the mesh against the five planes (:69-75) */
+    f3 c[8];
+    for (int i = 0; i < 8; i++) c[i] = rs_xform(T, (i & 1) ? mesh.bmax[0] : mesh.bmin[0], ((i >> 1) & 1) ? mesh.bmax[1] : mesh.bmin[1], (i >> 2) ? mesh.bmax[2] : mesh.bmin[2], 1.0f);
+    for (int p = 0; p < 5; p++) {
+        int i = 0;
+        for (; i < 8; i++)
+            if ((dot(mk3(fr[p].x, fr[p].y, fr[p].z), c[i]) - fr[p].w) > 0) break;
+        if (i == 8) return 0;
+    }
+    uint64_t frags = 0;
+    const size_t nt = mesh.tris.size();
+    for (size_t i = 0; i < nt; i++) {
+        const lh2g_core_tri& ct = mesh.tris[i];
+        const lh2g_material& mat = s.hostMats[ct.material];
+        const int tex = mat.color_map.texture;
+        const uint diffuse = rs_diffuse(mat);
+        const uint* src = tex >= 0 ? s.texels.data() + s.texFirst[tex] : &diffuse;
+        const float tw = tex >= 0 ? (float)s.texWH[2 * tex] : 1.0f, th = tex >= 0 ? (float)s.texWH[2 * tex + 1] : 1.0f;
+        const int umask = (int)tw, vmask = (int)th;
+        f3 tpos[3];
+        for (int v = 0; v < 3; v++) tpos[v] = rs_xform(T, mesh.pos[3 * i + v].x, mesh.pos[3 * i + v].y, mesh.pos[3 * i + v].z, 1.0f);
+        /* back faces (:86-87) */
+        const f3 Nt = rs_xform(T, ct.Nx, ct.Ny, ct.Nz, 0.0f);
+        if (dot(tpos[0], Nt) > 0) continue;
+        /* clip against the near and left planes (:89-106) */
+        f3 cpos[2][8];
+        f2 cuv[2][8];
+        int nin = 3, nout = 0, from = 0, to = 1;
+        const float us[3] = {ct.u0, ct.u1, ct.u2}, vs[3] = {ct.v0, ct.v1, ct.v2};
+        for (int v = 0; v < 3; v++) cpos[0][v] = tpos[v], cuv[0][v] = {us[v], vs[v]};
+        for (int p = 0; p < 2; p++, from = 1 - from, to = 1 - to, nin = nout, nout = 0)
+            for (int v = 0; v < nin; v++) {
+                const f3 A = cpos[from][v], B = cpos[from][(v + 1) % nin];
+                const f2 Auv = cuv[from][v], Buv = cuv[from][(v + 1) % nin];
+                const f3 pn = mk3(fr[p].x, fr[p].y, fr[p].z);
+                const float t1 = dot(pn, A) - fr[p].w, t2 = dot(pn, B) - fr[p].w;
+                if (t1 < 0 && t2 >= 0) {
+                    const float f = t1 / (t1 - t2);
+                    cuv[to][nout] = {Auv.x + (Buv.x - Auv.x) * f, Auv.y + (Buv.y - Auv.y) * f}, cpos[to][nout++] = A + f * (B - A);
+                    cuv[to][nout] = Buv, cpos[to][nout++] = B;
+                } else if (t1 >= 0 && t2 >= 0) {
+                    cuv[to][nout] = Buv, cpos[to][nout++] = B;
+                } else if (t1 >= 0 && t2 < 0) {
+                    const float f = t1 / (t1 - t2);
+                    cuv[to][nout] = {Auv.x + (Buv.x - Auv.x) * f, Auv.y + (Buv.y - Auv.y) * f}, cpos[to][nout++] = A + f * (B - A);
+                }
+            }
+        if (nin == 0) continue;
+        /* project (:109-112) */
+        f3* pos = cpos[from];
+        const f2* tuv = cuv[from];
+        for (int v = 0; v < nin; v++)
+            pos[v].x = ((pos[v].x * W) / -pos[v].z) + (float)(W / 2), pos[v].y = ((pos[v].y * W) / pos[v].z) + (float)(H / 2);
+        /* edges into the outline tables (:114-137) */
+        const uint shade = rs_f2u((ct.Nz + 1) * 64.0f + 127.9f);
+        int miny = H - 1, maxy = 0;
+        for (int j = 0; j < nin; j++) {
+            int vert0 = j, vert1 = (j + 1) % nin;
+            if (pos[vert0].y > pos[vert1].y) std::swap(vert0, vert1);
+            const float y0 = pos[vert0].y, y1 = pos[vert1].y, rydiff = 1.0f / (y1 - y0);
+            if (y0 == y1 || y0 >= H || y1 < 1) continue;
+            const int iy0 = std::max(1, rs_f2i(y0) + 1), iy1 = std::min(H - 2, rs_f2i(y1));
+            float x0 = pos[vert0].x, dx = (pos[vert1].x - x0) * rydiff;
+            float z0 = 1.0f / pos[vert0].z, z1 = 1.0f / pos[vert1].z, dz = (z1 - z0) * rydiff;
+            float u0 = tuv[vert0].x * z0, du = (tuv[vert1].x * z1 - u0) * rydiff;
+            float v0 = tuv[vert0].y * z0, dv = (tuv[vert1].y * z1 - v0) * rydiff;
+            const float f = (float)iy0 - y0;
+            x0 += dx * f, u0 += du * f, v0 += dv * f, z0 += dz * f;
+            for (int y = iy0; y <= iy1; y++) {
+                if (x0 < tb.xl[y]) tb.xl[y] = x0, tb.ul[y] = u0, tb.vl[y] = v0, tb.zl[y] = z0;
+                if (x0 > tb.xr[y]) tb.xr[y] = x0, tb.ur[y] = u0, tb.vr[y] = v0, tb.zr[y] = z0;
+                x0 += dx, u0 += du, v0 += dv, z0 += dz;
+            }
+            miny = std::min(miny, iy0), maxy = std::max(maxy, iy1);
+        }
+        /* spans (:138-169), resetting the tables' rows behind them */
+        for (int y = miny; y <= maxy; tb.xl[y] = (float)(W - 1), tb.xr[y++] = 0.0f) {
+            const float x0 = tb.xl[y], x1 = tb.xr[y], rxdiff = 1.0f / (x1 - x0);
+            float u0 = tb.ul[y], du = (tb.ur[y] - u0) * rxdiff;
+            float v0 = tb.vl[y], dv = (tb.vr[y] - v0) * rxdiff;
+            float z0 = tb.zl[y], dz = (tb.zr[y] - z0) * rxdiff;
+            const int ix0 = rs_f2i(x0) + 1, ix1 = std::min(W - 2, rs_f2i(x1));
+            if (ix0 < 1) continue;
+            const float f = (float)ix0 - x0;
+            u0 += f * du, v0 += f * dv, z0 += f * dz;
+            uint* dest = pixels + (size_t)y * W;
+            float* zbuf = zbuffer + (size_t)y * W;
+            for (int x = ix0; x <= ix1; x++, u0 += du, v0 += dv, z0 += dz) {
+                if (!(z0 < zbuf[x])) continue;
+                const float z = 1.0f / z0;
+                const uint u = rs_f2u(u0 * z * tw) % (uint)umask, v = rs_f2u(v0 * z * th) % (uint)vmask;
+                dest[x] = rs_scale_color(src[u + v * (uint)umask], shade), zbuf[x] = z0;
+                frags++;
+            }
+        }
+    }
+    return frags;
+}
+
+}  // namespace
+
 extern "C" {
 
 lh2o_scene* lh2o_create(void) { return new lh2o_scene(); }
@@ -1987,12 +2176,13 @@ int lh2o_set_geometry(lh2o_scene* s, int meshIdx, const float* v4, int vertexCou
     if (meshIdx == (int)s->meshes.size()) s->meshes.emplace_back();
     Mesh& m = s->meshes[meshIdx];
     m.tris.assign(tris, tris + triangleCount);
-    m.v0.resize(triangleCount), m.e1.resize(triangleCount), m.e2.resize(triangleCount);
+    m.v0.resize(triangleCount), m.e1.resize(triangleCount), m.e2.resize(triangleCount), m.pos.resize((size_t)3 * triangleCount);
     for (int a = 0; a < 3; a++) m.bmin[a] = 1e30f, m.bmax[a] = -1e30f;
     for (int i = 0; i < triangleCount; i++) {
         const float* a = v4 + 12 * i;
         const f3 p0 = mk3(a[0], a[1], a[2]), p1 = mk3(a[4], a[5], a[6]), p2 = mk3(a[8], a[9], a[10]);
         m.v0[i] = p0, m.e1[i] = p1 - p0, m.e2[i] = p2 - p0;
+        m.pos[3 * i] = p0, m.pos[3 * i + 1] = p1, m.pos[3 * i + 2] = p2;
         const f3 ps[3] = {p0, p1, p2};
         for (const f3& q : ps) {
             m.bmin[0] = std::min(m.bmin[0], q.x), m.bmin[1] = std::min(m.bmin[1], q.y), m.bmin[2] = std::min(m.bmin[2], q.z);
@@ -2528,6 +2718,34 @@ uint16_t lh2o_float2half(float f) { return float2half(f); }
 float lh2o_half2float(uint16_t h) { return half2float(h); }
 void lh2o_pack_material(const lh2g_material* m, const uint32_t* first, const uint32_t* wh, lh2g_gpu_material* out) { pack_material(*m, first, wh, *out); }
 void lh2o_invert4x4(const float* m, float* o) { invert4x4(m, o); }
+
+int lh2o_raster(lh2o_scene* s, const lh2g_view* view, int W, int H, uint32_t* pixels, float* zbuffer, uint64_t* fragments) {
+    if (!s || !view || !pixels || W < 3 || H < 3 || W > 8192 || H > 8192) return 1;
+    for (const Instance& in : s->inst)
+        for (const lh2g_core_tri& t : s->meshes[in.mesh].tris)
+            if (t.material >= s->hostMats.size()) return 1;
+    std::vector<float> zb;
+    if (!zbuffer) zb.resize((size_t)W * H), zbuffer = zb.data();
+    memset(pixels, 0, sizeof(uint) * (size_t)W * H);
+    memset(zbuffer, 0, sizeof(float) * (size_t)W * H);
+    f4 fr[5];
+    rs_frustum(W, H, fr);
+    RsTables tb;
+    for (std::vector<float>* t : {&tb.xl, &tb.xr, &tb.ul, &tb.ur, &tb.vl, &tb.vr, &tb.zl, &tb.zr}) t->assign(H, 0.0f);
+    for (int y = 0; y < H; y++) tb.xl[y] = (float)(W - 1), tb.xr[y] = 0.0f;
+    const RsMesh4 root = rs_view(view);
+    /* instances that share a mesh share its scene-graph node, whose transform is the one set last
+     * (rendercore.cpp:118-131: the Mesh object is the child node and holds localTransform) */
+    std::vector<const float*> meshT(s->meshes.size(), nullptr);
+    for (const Instance& in : s->inst) meshT[in.mesh] = in.T;
+    uint64_t frags = 0;
+    for (const Instance& in : s->inst) {
+        const RsMesh4 M = rs_mul(root.m, meshT[in.mesh]);
+        frags += rs_mesh(*s, s->meshes[in.mesh], M.m, fr, W, H, tb, pixels, zbuffer);
+    }
+    if (fragments) *fragments = frags;
+    return 0;
+}
 
 }  // extern "C"
 

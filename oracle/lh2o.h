@@ -127,6 +127,11 @@ int lh2o_nrc_gradients(const lh2o_nrc_spec* spec, const float* grid, const float
                        long long n, int emulate, double* gMlp, double* gGrid, double* loss);
 void lh2o_nrc_adam(float* p, float* m, float* v, const float* g, long long n, float lr, long long step);
 
+/* SoftRasterizer core (lib/RenderCore_SoftRasterizer/rasterizer.cpp:66-171,201-240, rendercore.cpp:213-222):
+ * one frame of W x H RGBA8 pixels (0 where nothing was drawn) and the z-buffer of interpolated 1/z (0 where
+ * nothing was drawn; may be null); fragments = depth-test passes (may be null). W, H in 3..8192. */
+int lh2o_raster(lh2o_scene* s, const lh2g_view* view, int W, int H, uint32_t* pixels, float* zbuffer, uint64_t* fragments);
+
 /* Small pure functions exported for the pinning tests against the reference's own headers. */
 uint32_t lh2o_wanghash(uint32_t s);
 /* blueNoiseSampler4 over an expanded table (5 * 65536 + 64 entries) */
