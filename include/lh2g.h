@@ -202,7 +202,7 @@ typedef struct lh2g_raster_stats {
     uint32_t instancesDrawn;   /* instances the mesh culling kept */
     uint32_t triangles;        /* their triangles */
     uint32_t smallTriangles;   /* triangles rasterised one per thread that offered fragments */
-    uint32_t bigTriangles;     /* triangles rasterised one block per 128 rows */
+    uint32_t bigTriangles;     /* triangles rasterised by blocks of 8 rows x 512 columns, a warp per row */
     uint32_t fragments;        /* fragments offered to the depth test (1/z < 0) */
     uint32_t status;           /* nonzero: a triangle named a missing material (not drawn) */
 } lh2g_raster_stats;

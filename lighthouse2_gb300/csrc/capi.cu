@@ -41,6 +41,7 @@ namespace {
 struct MeshDev {
     float4* verts = nullptr;   /* 3 per triangle */
     float4* tris = nullptr;    /* CoreTri4, 13 float4 per triangle */
+    float4* rsNorms = nullptr; /* rasterizer: face normal + material per triangle, packed at its first raster frame */
     uint32_t n = 0;
     uint32_t maxMaterial = 0;  /* largest material index of its triangles (checked against the materials at render) */
     float bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0};
@@ -500,7 +501,7 @@ int lh2g_destroy(lh2g_context* ctx) {
     cudaStreamSynchronize(ctx->st);
     for (auto& L : ctx->lanes)
         if (L.st) cudaStreamSynchronize(L.st);
-    for (MeshDev& m : ctx->meshes) dfree(m.verts), dfree(m.tris);
+    for (MeshDev& m : ctx->meshes) dfree(m.verts), dfree(m.tris), dfree(m.rsNorms);
     dfree(ctx->mats), dfree(ctx->texels), dfree(ctx->triL), dfree(ctx->ptL), dfree(ctx->spL), dfree(ctx->dirL), dfree(ctx->sky);
     dfree(ctx->skySmall), dfree(ctx->blueNoise);
     dfree(ctx->pool), dfree(ctx->triData), dfree(ctx->instGPU), dfree(ctx->tlasPrims), dfree(ctx->instTris), dfree(ctx->instInvRows);
@@ -546,6 +547,7 @@ int lh2g_set_geometry(lh2g_context* ctx, int meshIdx, const float* v4, int verte
     m.n = (uint32_t)triangleCount;
     CK(dalloc(m.verts, (size_t)3 * triangleCount));
     CK(dalloc(m.tris, (size_t)13 * triangleCount));
+    dfree(m.rsNorms);
     CK(cudaMemcpyAsync(m.verts, v4, sizeof(float4) * 3 * (size_t)triangleCount, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemcpyAsync(m.tris, tris, sizeof(lh2g_core_tri) * (size_t)triangleCount, cudaMemcpyHostToDevice, ctx->st));
     m.maxMaterial = 0;
@@ -1733,6 +1735,7 @@ int lh2g_raster_render(lh2g_context* ctx, const lh2g_view* view, uint32_t* pixel
     std::vector<const float*> meshT(ctx->meshes.size(), nullptr);
     for (const InstHost& in : ctx->inst) meshT[in.mesh] = in.T;
     std::vector<RasterInst> kept;
+    std::vector<int> keptMesh;
     uint32_t total = 0;
     for (const InstHost& in : ctx->inst) {
         const MeshDev& m = ctx->meshes[in.mesh];
@@ -1754,7 +1757,8 @@ int lh2g_raster_render(lh2g_context* ctx, const lh2g_view* view, uint32_t* pixel
         if ((uint64_t)total + m.n >= (1ull << 32)) return fail(ctx, LH2G_ERR_INVALID, "raster_render: more than 2^32 triangles in view");
         RasterInst r;
         memcpy(r.M, M.m, sizeof(r.M));
-        r.verts = m.verts, r.tris = m.tris, r.first = total, r.count = m.n, r.pad[0] = r.pad[1] = 0;
+        r.verts = m.verts, r.tris = m.tris, r.norms = nullptr, r.first = total, r.count = m.n;
+        keptMesh.push_back(in.mesh);
         kept.push_back(r);
         total += m.n;
     }
@@ -1792,6 +1796,16 @@ int lh2g_raster_render(lh2g_context* ctx, const lh2g_view* view, uint32_t* pixel
         R0.matCap = (int)mats.size();
     }
     cudaStream_t st = ctx->st;
+    /* the first pass's compact per-triangle records, once per mesh geometry */
+    for (size_t k = 0; k < kept.size(); k++) {
+        MeshDev& m = ctx->meshes[keptMesh[k]];
+        if (!m.rsNorms) {
+            CK(dalloc(m.rsNorms, m.n));
+            launch_raster_pack(m.tris, m.n, m.rsNorms, st);
+            CK(cudaGetLastError());
+        }
+        kept[k].norms = m.rsNorms;
+    }
     if (!kept.empty()) CK(cudaMemcpyAsync(R0.inst, kept.data(), sizeof(RasterInst) * kept.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(R0.mats, mats.data(), sizeof(RasterMat) * mats.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(R0.pixels, 0, sizeof(uint32_t) * WH, st));

@@ -17,7 +17,7 @@ namespace lh2g {
 namespace {
 
 constexpr int RS_MAXV = 5;           /* a triangle clipped by two planes has at most 5 vertices */
-constexpr float RS_SMALL_WORK = 512.0f;   /* rows x columns above which a triangle takes the block path */
+constexpr float RS_SMALL_WORK = 64.0f;    /* rows x columns above which a triangle takes the block path */
 
 LH2G_DEV int rs_f2i(float x) { return __float2int_rz(x); }
 LH2G_DEV uint32_t rs_f2u(float x) {
@@ -104,7 +104,8 @@ LH2G_DEV bool setup(const RasterFrame& R, const uint32_t g, Setup& E) {
     const float4* vp = I.verts + 3 * (size_t)t;
     const float4* tp = I.tris + 13 * (size_t)t;
     const float4 p0 = __ldg(vp), p1 = __ldg(vp + 1), p2 = __ldg(vp + 2);
-    const float Nx = __ldg(tp + 2).w, Ny = __ldg(tp + 3).w, Nz = __ldg(tp + 4).w;
+    const float4 nm = __ldg(I.norms + t);
+    const float Nx = nm.x, Ny = nm.y, Nz = nm.z;
     /* make_float4(pos, 1) * T and make_float4(N, 0) * T (system.cpp:90-103: the matrix times the column) */
     auto tx = [&](int r, float x, float y, float z, float w) { return M[4 * r] * x + M[4 * r + 1] * y + M[4 * r + 2] * z + M[4 * r + 3] * w; };
     Poly A;
@@ -118,7 +119,7 @@ LH2G_DEV bool setup(const RasterFrame& R, const uint32_t g, Setup& E) {
     if (UV) {
         const float4 t0 = __ldg(tp), t1 = __ldg(tp + 1);
         A.u[0] = t0.x, A.u[1] = t0.y, A.u[2] = t0.z, A.v[0] = t1.x, A.v[1] = t1.y, A.v[2] = t1.z;
-        E.mat = __float_as_uint(t1.w);
+        E.mat = __float_as_uint(nm.w);
         E.shade = rs_f2u((Nz + 1.0f) * 64.0f + 127.9f);
     }
     Poly B, P;
@@ -189,18 +190,25 @@ struct Shader {
     const uint32_t* src;
     uint32_t diffuse, umask, vmask, shade;
     float tw, th;
+    bool pow2;   /* both sizes powers of two: the modulo is a mask */
     __device__ __forceinline__ void init(const RasterFrame& R, const Setup& E) {
         const RasterMat m = R.mats[E.mat];
         diffuse = m.diffuse, shade = E.shade;
         if (m.width) src = R.texels + m.texFirst, umask = m.width, vmask = m.height, tw = (float)m.width, th = (float)m.height;
         else src = nullptr, umask = vmask = 1u, tw = th = 1.0f;
+        pow2 = !(umask & (umask - 1u)) && !(vmask & (vmask - 1u));
     }
-    __device__ __forceinline__ uint32_t color(float u0, float v0, float z0) const {
+    /* the texel index of a fragment */
+    __device__ __forceinline__ uint32_t texel(float u0, float v0, float z0) const {
         const float z = 1.0f / z0;
-        const uint32_t u = rs_f2u(u0 * z * tw) % umask, v = rs_f2u(v0 * z * th) % vmask;
-        return rs_scale_color(src ? __ldg(src + u + v * umask) : diffuse, shade);
+        const uint32_t uu = rs_f2u(u0 * z * tw), vv = rs_f2u(v0 * z * th);
+        const uint32_t u = pow2 ? uu & (umask - 1u) : uu % umask, v = pow2 ? vv & (vmask - 1u) : vv % vmask;
+        return u + v * umask;
     }
+    __device__ __forceinline__ uint32_t fetch(uint32_t idx) const { return src ? __ldg(src + idx) : diffuse; }
 };
+
+constexpr int RS_BATCH = 8;   /* pass 2 handles a span's pixels in groups: their key and texel loads are independent */
 
 /* one row's span (rasterizer.cpp:140-168): pass 1 offers depth keys, pass 2 writes the colour where its key won */
 template <int PASS>
@@ -216,20 +224,38 @@ LH2G_DEV uint32_t span(const RasterFrame& R, const int y, const float xl, const 
     z0 += f * dz;
     uint32_t offered = 0;
     unsigned long long* keys = R.keys + (size_t)y * R.W;
-    for (int x = ix0; x <= ix1; x++) {
-        if (z0 < 0.0f) {
-            const unsigned long long key = rs_key(z0, g);
-            if (PASS == 1) {
-                if (key < keys[x]) atomicMin(keys + x, key);
-                offered++;
-            } else if (keys[x] == key) {
-                R.pixels[(size_t)y * R.W + x] = sh.color(u0, v0, z0);
+    if (PASS == 1) {
+        /* the minimum is all pass 1 needs: a reduction without a returned value does not wait for memory */
+        for (int x = ix0; x <= ix1; x++) {
+            if (z0 < 0.0f) atomicMin(keys + x, rs_key(z0, g)), offered++;
+            z0 += dz;
+        }
+        return offered;
+    }
+    uint32_t* out = R.pixels + (size_t)y * R.W;
+    for (int xb = ix0; xb <= ix1; xb += RS_BATCH) {
+        unsigned long long k[RS_BATCH];
+#pragma unroll
+        for (int i = 0; i < RS_BATCH; i++) k[i] = xb + i <= ix1 ? __ldg(keys + xb + i) : 0ull;
+        uint32_t idx[RS_BATCH];
+        bool win[RS_BATCH];
+#pragma unroll
+        for (int i = 0; i < RS_BATCH; i++) {
+            win[i] = false;
+            if (xb + i <= ix1) {
+                win[i] = z0 < 0.0f && k[i] == rs_key(z0, g);
+                idx[i] = win[i] ? sh.texel(u0, v0, z0) : 0u;
+                u0 += du, v0 += dv, z0 += dz;
             }
         }
-        if (PASS == 2) u0 += du, v0 += dv;
-        z0 += dz;
+        uint32_t c[RS_BATCH];
+#pragma unroll
+        for (int i = 0; i < RS_BATCH; i++) c[i] = win[i] ? sh.fetch(idx[i]) : 0u;
+#pragma unroll
+        for (int i = 0; i < RS_BATCH; i++)
+            if (win[i]) out[xb + i] = rs_scale_color(c[i], sh.shade);
     }
-    return offered;
+    return 0;
 }
 
 /* a whole small triangle in one thread: rows in order, each edge advanced on the rows it covers */
@@ -271,7 +297,7 @@ LH2G_DEV void append(uint32_t* list, uint32_t* count, bool take, uint32_t g) {
 }
 
 /* pass 1: every triangle of the kept instances */
-__global__ void __launch_bounds__(256) k_rs_cover(const RasterFrame R) {
+__global__ void __launch_bounds__(128) k_rs_cover(const RasterFrame R) {
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     Setup E;
     bool small = false, big = false;
@@ -293,7 +319,7 @@ __global__ void __launch_bounds__(256) k_rs_cover(const RasterFrame R) {
 }
 
 /* pass 2: the small triangles that offered fragments */
-__global__ void __launch_bounds__(256) k_rs_color(const RasterFrame R) {
+__global__ void __launch_bounds__(128) k_rs_color(const RasterFrame R) {
     const uint32_t n = R.counters[0];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t g = R.list[i];
@@ -306,26 +332,92 @@ __global__ void __launch_bounds__(256) k_rs_color(const RasterFrame R) {
     }
 }
 
-/* big triangles: one block per (triangle, chunk of RS_CHUNK rows). Threads 0..n-1 walk one edge each from its
- * first row to the chunk's end and leave the chunk's values in shared memory; then thread r fills row r. */
+/* one row's span by a whole warp (the block path): every lane runs the span's running sums (u0 += du, v0 += dv,
+ * z0 += dz, the reference's exact sequence) and lane i keeps the values of pixel i of each group of 32; then each lane
+ * handles its pixel. The serial part is a few adds per pixel; the key, texel and store work spreads over the lanes. */
+constexpr int RS_SEG = 512;   /* columns of a row one warp fills in the block path */
+
 template <int PASS>
-__global__ void __launch_bounds__(RS_CHUNK) k_rs_big(const RasterFrame R, const int chunksPerTri) {
+LH2G_DEV uint32_t warp_span(const RasterFrame& R, const int y, const float xl, const float xr, const float ul, const float ur, const float vl,
+                            const float vr, const float zl, const float zr, const uint32_t g, const Shader& sh, const int lane, const int seg) {
+    const float rxdiff = 1.0f / (xr - xl);
+    float u0 = ul, v0 = vl, z0 = zl;
+    const float du = (ur - u0) * rxdiff, dv = (vr - v0) * rxdiff, dz = (zr - z0) * rxdiff;
+    const int ix0 = rs_f2i(xl) + 1, ix1 = min(R.W - 2, rs_f2i(xr));
+    if (ix0 < 1) return 0;
+    const float f = (float)ix0 - xl;
+    if (PASS == 2) u0 += f * du, v0 += f * dv;
+    z0 += f * dz;
+    /* this warp's columns: segment seg of the row; the running sums first advance to its first pixel */
+    const int xs = max(ix0, 1 + seg * RS_SEG), xe = min(ix1, seg * RS_SEG + RS_SEG);
+    if (xs > xe) return 0;
+    for (int x = ix0; x < xs; x++) {
+        z0 += dz;
+        if (PASS == 2) u0 += du, v0 += dv;
+    }
+    uint32_t offered = 0;
+    unsigned long long* keys = R.keys + (size_t)y * R.W;
+    uint32_t* out = R.pixels + (size_t)y * R.W;
+    for (int xb = xs; xb <= xe; xb += 32) {
+        const int cnt = min(32, xe - xb + 1);
+        float mu = 0.0f, mv = 0.0f, mz = 0.0f;
+        if (cnt == 32) {
+#pragma unroll
+            for (int i = 0; i < 32; i++) {
+                if (lane == i) {
+                    mz = z0;
+                    if (PASS == 2) mu = u0, mv = v0;
+                }
+                z0 += dz;
+                if (PASS == 2) u0 += du, v0 += dv;
+            }
+        } else {
+            for (int i = 0; i < cnt; i++) {
+                if (lane == i) {
+                    mz = z0;
+                    if (PASS == 2) mu = u0, mv = v0;
+                }
+                z0 += dz;
+                if (PASS == 2) u0 += du, v0 += dv;
+            }
+        }
+        if (lane < cnt && mz < 0.0f) {
+            const int x = xb + lane;
+            const unsigned long long key = rs_key(mz, g);
+            if (PASS == 1) {
+                atomicMin(keys + x, key);
+                offered++;
+            } else if (__ldg(keys + x) == key) {
+                out[x] = rs_scale_color(sh.fetch(sh.texel(mu, mv, mz)), sh.shade);
+            }
+        }
+    }
+    return offered;
+}
+
+/* Triangles past the one-thread size: one block per (triangle, chunk of RS_CHUNK rows, segment of RS_SEG columns).
+ * Threads 0..n-1 walk one edge each from its first row to the chunk's end and leave the chunk's values in shared
+ * memory; then warp w fills the segment of row w of the chunk (warp_span). */
+constexpr int RS_BIG_WARPS = RS_CHUNK;
+template <int PASS>
+__global__ void __launch_bounds__(32 * RS_BIG_WARPS) k_rs_big(const RasterFrame R, const int chunksPerTri, const int segsPerRow) {
     __shared__ float4 rows[RS_MAXV][RS_CHUNK];   /* x, z, u, v of each edge on each row of the chunk */
-    const uint32_t items = R.counters[1] * (uint32_t)chunksPerTri;
+    const uint32_t perTri = (uint32_t)(chunksPerTri * segsPerRow);
+    const uint32_t items = R.counters[1] * perTri;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     uint32_t offered = 0;
     for (uint32_t item = blockIdx.x; item < items; item += gridDim.x) {
-        const uint32_t g = R.big[item / chunksPerTri];
-        const int chunk = (int)(item % chunksPerTri);
+        const uint32_t g = R.big[item / perTri];
+        const int chunk = (int)(item % perTri) / segsPerRow, seg = (int)(item % perTri) % segsPerRow;
         Setup E;
         if (!setup<PASS == 2>(R, g, E)) continue;   /* same outcome in every thread */
         const int c0 = E.miny + chunk * RS_CHUNK;
         if (c0 > E.maxy) continue;
         const int c1 = min(c0 + RS_CHUNK - 1, E.maxy);
         if (PASS == 2 && E.mat >= R.nMats) {
-            if (threadIdx.x == 0 && chunk == 0) atomicOr(R.counters + 3, 1u);
+            if (t == 0 && chunk == 0) atomicOr(R.counters + 3, 1u);
             continue;
         }
-        const int t = threadIdx.x;
 #pragma unroll
         for (int j = 0; j < RS_MAXV; j++) {
             if (t != j || E.iy0[j] > E.iy1[j]) continue;
@@ -339,23 +431,34 @@ __global__ void __launch_bounds__(RS_CHUNK) k_rs_big(const RasterFrame R, const 
             }
         }
         __syncthreads();
-        const int y = c0 + t;
-        if (y <= c1) {
+        Shader sh{};
+        if (PASS == 2) sh.init(R, E);
+        for (int r = warp; r <= c1 - c0; r += RS_BIG_WARPS) {
+            const int y = c0 + r;
             float xl = (float)(R.W - 1), xr = 0.0f, ul = 0.0f, ur = 0.0f, vl = 0.0f, vr = 0.0f, zl = 0.0f, zr = 0.0f;
 #pragma unroll
             for (int j = 0; j < RS_MAXV; j++) {
                 if (y < E.iy0[j] || y > E.iy1[j]) continue;
-                const float4 e = rows[j][t];
+                const float4 e = rows[j][r];
                 if (e.x < xl) xl = e.x, zl = e.y, ul = e.z, vl = e.w;
                 if (e.x > xr) xr = e.x, zr = e.y, ur = e.z, vr = e.w;
             }
-            Shader sh{};
-            if (PASS == 2) sh.init(R, E);
-            offered += span<PASS>(R, y, xl, xr, ul, ur, vl, vr, zl, zr, g, sh);
+            offered += warp_span<PASS>(R, y, xl, xr, ul, ur, vl, vr, zl, zr, g, sh, lane, seg);
         }
         __syncthreads();
     }
-    if (PASS == 1 && offered) atomicAdd(R.counters + 2, offered);
+    if (PASS == 1) {
+#pragma unroll
+        for (int s = 16; s > 0; s >>= 1) offered += __shfl_down_sync(0xffffffffu, offered, s);
+        if (lane == 0 && offered) atomicAdd(R.counters + 2, offered);
+    }
+}
+
+__global__ void k_rs_pack(const float4* __restrict__ tris, const uint32_t n, float4* __restrict__ norms) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const float4* r = tris + 13 * (size_t)t;
+    norms[t] = make_float4(r[2].w, r[3].w, r[4].w, r[1].w);
 }
 
 __global__ void k_rs_depth(const RasterFrame R, float* zbuffer) {
@@ -368,11 +471,15 @@ __global__ void k_rs_depth(const RasterFrame R, float* zbuffer) {
 }  // namespace
 
 void launch_raster(const RasterFrame& R, int smCount, cudaStream_t st) {
-    const int chunksPerTri = (R.H - 2 + RS_CHUNK - 1) / RS_CHUNK;
-    if (R.total) k_rs_cover<<<(R.total + 255) / 256, 256, 0, st>>>(R);
-    k_rs_big<1><<<smCount * 8, RS_CHUNK, 0, st>>>(R, chunksPerTri);
-    k_rs_color<<<smCount * 8, 256, 0, st>>>(R);
-    k_rs_big<2><<<smCount * 8, RS_CHUNK, 0, st>>>(R, chunksPerTri);
+    const int chunksPerTri = (R.H - 2 + RS_CHUNK - 1) / RS_CHUNK, segsPerRow = (R.W - 2 + RS_SEG - 1) / RS_SEG;
+    if (R.total) k_rs_cover<<<(R.total + 127) / 128, 128, 0, st>>>(R);
+    k_rs_big<1><<<smCount * 8, 32 * RS_BIG_WARPS, 0, st>>>(R, chunksPerTri, segsPerRow);
+    k_rs_color<<<smCount * 12, 128, 0, st>>>(R);
+    k_rs_big<2><<<smCount * 8, 32 * RS_BIG_WARPS, 0, st>>>(R, chunksPerTri, segsPerRow);
+}
+
+void launch_raster_pack(const float4* tris, uint32_t n, float4* norms, cudaStream_t st) {
+    if (n) k_rs_pack<<<(n + 255) / 256, 256, 0, st>>>(tris, n, norms);
 }
 
 void launch_raster_depth(const RasterFrame& R, float* zbuffer, cudaStream_t st) {

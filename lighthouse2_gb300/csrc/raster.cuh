@@ -11,8 +11,8 @@
  *          texel colour.
  * Every interpolant is the reference's running sum (x0 += dx per row, u0 += du per pixel, ...), recomputed the
  * same way in both passes, so the GPU's pixels and z-buffer equal the sequential result bit for bit. Triangles
- * covering more than a few hundred pixels are queued instead and run as one block per (triangle, 128-row chunk)
- * (k_rs_big), a thread per row. */
+ * covering more than a few dozen pixels are queued instead and run as one block per (triangle, 8-row chunk,
+ * 512-column segment) (k_rs_big), a warp per row. */
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -23,10 +23,10 @@ namespace lh2g {
 struct RasterInst {
     float M[12];               /* rows 0..2 of transform x localTransform (rasterizer.cpp:187) */
     const float4* verts;       /* 3 per triangle */
-    const float4* tris;        /* CoreTri4 records, 13 float4 per triangle */
+    const float4* tris;        /* CoreTri4 records, 13 float4 per triangle (texture coordinates) */
+    const float4* norms;       /* per triangle: face normal xyz, material index bits (launch_raster_pack) */
     uint32_t first;            /* draw order of its first triangle among the kept instances' triangles */
     uint32_t count;
-    uint32_t pad[2];
 };
 
 /* a material as the rasterizer reads it (rendercore.cpp:166-185): a packed colour, or a texture's level 0 */
@@ -48,8 +48,10 @@ struct RasterFrame {
     uint32_t* counters;              /* [0] list, [1] big, [2] fragments offered, [3] status (bad material) */
 };
 
-constexpr int RS_CHUNK = 128;        /* rows per block of the big-triangle path */
+constexpr int RS_CHUNK = 8;          /* rows per block of the big-triangle path (a warp per row) */
 
+/* a mesh's per-triangle face normal and material (16 B, from the CoreTri4 records) for the first pass */
+void launch_raster_pack(const float4* tris, uint32_t n, float4* norms, cudaStream_t st);
 /* the frame's two passes on `st` (keys and pixels must be cleared and counters zeroed before) */
 void launch_raster(const RasterFrame& R, int smCount, cudaStream_t st);
 /* the z-buffer of the reference (interpolated 1/z of the kept fragment, 0 where none) from the depth keys */
