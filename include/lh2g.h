@@ -208,6 +208,8 @@ typedef struct lh2g_raster_stats {
 } lh2g_raster_stats;
 LH2G_API int lh2g_raster_render(lh2g_context* ctx, const lh2g_view* view, uint32_t* pixelsHost, float* depthHost, lh2g_raster_stats* stats);
 LH2G_API uint32_t* lh2g_raster_pixels_device(lh2g_context* ctx);
+/* the last raster frame's pixels (its W*H words) to host memory; waits for the context stream */
+LH2G_API int lh2g_raster_read(lh2g_context* ctx, uint32_t* pixelsHost);
 
 /* ---- serving loop (no counterpart in the reference, whose cores render one frame at a time) ----
  * Render and ray-query jobs of several resident scenes, continuously batched: jobs are admitted smallest first

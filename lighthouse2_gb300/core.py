@@ -51,7 +51,7 @@ C_API = ["lh2g_create", "lh2g_destroy", "lh2g_last_error", "lh2g_set_geometry", 
          "lh2g_nrc_create", "lh2g_nrc_destroy", "lh2g_nrc_last_error", "lh2g_nrc_get_spec", "lh2g_nrc_set_params", "lh2g_nrc_get_params",
          "lh2g_nrc_get_grads", "lh2g_nrc_infer", "lh2g_nrc_train", "lh2g_nrc_apply_update", "lh2g_nrc_infer_counted", "lh2g_nrc_train_counted",
          "lh2g_nrc_last_loss", "lh2g_nrc_wait_selftest", "lh2g_render_nrc", "lh2g_nrc_infer_host", "lh2g_nrc_train_host",
-         "lh2g_set_blue_noise", "lh2g_render_adaptive", "lh2g_set_adaptive_scale", "lh2g_raster_render", "lh2g_raster_pixels_device"]
+         "lh2g_set_blue_noise", "lh2g_render_adaptive", "lh2g_set_adaptive_scale", "lh2g_raster_render", "lh2g_raster_pixels_device", "lh2g_raster_read"]
 
 _lib = None
 

@@ -1841,3 +1841,12 @@ int lh2g_raster_render(lh2g_context* ctx, const lh2g_view* view, uint32_t* pixel
 }
 
 uint32_t* lh2g_raster_pixels_device(lh2g_context* ctx) { return ctx && ctx->rs.valid ? ctx->rs.pixels : nullptr; }
+
+int lh2g_raster_read(lh2g_context* ctx, uint32_t* pixelsHost) {
+    if (!ctx || !pixelsHost) return LH2G_ERR_INVALID;
+    if (!ctx->rs.valid) return fail(ctx, LH2G_ERR_INVALID, "raster_read: no raster frame yet");
+    cudaSetDevice(ctx->device);
+    CK(cudaMemcpyAsync(pixelsHost, ctx->rs.pixels, sizeof(uint32_t) * (size_t)ctx->rs.W * ctx->rs.H, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return LH2G_OK;
+}

@@ -41,11 +41,18 @@ public:
     void Init() override { if (!ctx) lh2g_create(0, &ctx); }
     void SetProbePos(const int2 pos) override { lh2g_set_probe(ctx, pos.x, pos.y); }
     void SetTarget(GLTexture* target, const uint spp) override { if (target) lh2g_set_target(ctx, (int)target->width, (int)target->height, (int)spp); }
-    void Setting(const char* name, float value) override { lh2g_setting(ctx, name, value); }
+    /* "rasterizer" 1: Render draws the SoftRasterizer core's frame (RenderCore_SoftRasterizer/rendercore.cpp:213-227)
+     * instead of path tracing; read it with lh2g_raster_read / lh2g_raster_pixels_device */
+    bool raster = false;
+    void Setting(const char* name, float value) override {
+        if (!strcmp(name, "rasterizer")) raster = value != 0.0f;
+        else lh2g_setting(ctx, name, value);
+    }
     void Render(const ViewPyramid& view, const Convergence converge, bool async) override {
         lh2g_view v;
         memcpy(&v, &view, sizeof(v));
-        lh2g_render(ctx, &v, converge == Restart ? 1 : 0);
+        if (raster) lh2g_raster_render(ctx, &v, nullptr, nullptr, nullptr);
+        else lh2g_render(ctx, &v, converge == Restart ? 1 : 0);
         if (!async) lh2g_wait(ctx);
     }
     void WaitForRender() override { lh2g_wait(ctx); }

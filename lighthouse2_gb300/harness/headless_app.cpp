@@ -11,7 +11,8 @@
  *                 Restart | Converge, async = true), WaitForRender, GetCoreStats
  *   output        the headless target: the core's frame read through its C ABI (GB300_GetContext +
  *                 lh2g_read_framebuffer, found with dlsym) and appended to a file; one line of statistics per
- *                 frame on stdout
+ *                 frame on stdout. With the setting rasterizer=1 the core draws the SoftRasterizer core's frame
+ *                 and the file gets its RGBA8 words (lh2g_raster_read)
  *
  * usage: headless_app <core name or library path> <scene file> <frames file> <output file> <width> <height> <spp>
  *                     [setting=value ...]
@@ -205,7 +206,9 @@ int main(int argc, char** argv) {
     const contextFunction getContext = (contextFunction)dlsym(lib, "GB300_GetContext");
     typedef int (*readFunction)(lh2g_context*, float*);
     const readFunction readFrame = (readFunction)dlsym(lib, "lh2g_read_framebuffer");
-    if (!createCore || !getContext || !readFrame) { fprintf(stderr, "core %s lacks its entry points\n", name.c_str()); return 3; }
+    typedef int (*rasterReadFunction)(lh2g_context*, uint32_t*);
+    const rasterReadFunction readRaster = (rasterReadFunction)dlsym(lib, "lh2g_raster_read");
+    if (!createCore || !getContext || !readFrame || !readRaster) { fprintf(stderr, "core %s lacks its entry points\n", name.c_str()); return 3; }
     CoreAPI_Base* core = createCore();
     core->Init();
 
@@ -232,10 +235,13 @@ int main(int argc, char** argv) {
     core->SetInstance((int)scene.instances.size(), -1);
     core->FinalizeInstances();
 
+    bool raster = false;
     for (int a = 8; a < argc; a++) {
         const char* eq = strchr(argv[a], '=');
         if (!eq) continue;
-        core->Setting(std::string(argv[a], eq - argv[a]).c_str(), (float)atof(eq + 1));
+        const std::string key(argv[a], eq - argv[a]);
+        if (key == "rasterizer") raster = atof(eq + 1) != 0.0;
+        core->Setting(key.c_str(), (float)atof(eq + 1));
     }
     GLTexture target;
     target.width = W, target.height = H;
@@ -244,6 +250,7 @@ int main(int argc, char** argv) {
     FILE* out = fopen(argv[4], "wb");
     if (!out) { fprintf(stderr, "cannot write %s\n", argv[4]); return 2; }
     std::vector<float> pixels(4 * (size_t)W * H);
+    std::vector<uint32_t> words((size_t)W * H);
     int status = 0;
     for (size_t k = 0; k < frames.size(); k++) {
         const Frame& f = frames[k];
@@ -254,8 +261,13 @@ int main(int argc, char** argv) {
         core->Render(f.view, f.converge ? Restart : Converge, true);
         core->WaitForRender();
         const CoreStats st = core->GetCoreStats();
-        if (readFrame(getContext(core), pixels.data()) != 0) { status = 4; break; }
-        fwrite(pixels.data(), sizeof(float), pixels.size(), out);
+        if (raster) {
+            if (readRaster(getContext(core), words.data()) != 0) { status = 4; break; }
+            fwrite(words.data(), sizeof(uint32_t), words.size(), out);
+        } else {
+            if (readFrame(getContext(core), pixels.data()) != 0) { status = 4; break; }
+            fwrite(pixels.data(), sizeof(float), pixels.size(), out);
+        }
         printf("{\"frame\": %zu, \"totalRays\": %u, \"totalExtensionRays\": %u, \"totalShadowRays\": %u, \"primaryRayCount\": %u, "
                "\"renderTime_ms\": %.4f, \"bvhBuildTime_ms\": %.4f, \"SMcount\": %u}\n",
                k, st.totalRays, st.totalExtensionRays, st.totalShadowRays, st.primaryRayCount, st.renderTime, st.bvhBuildTime, st.SMcount);

@@ -62,3 +62,33 @@ def test_headless_application_matches_c_abi(core_lib, tmp_path):
     core.Render(frames[2][0], converge=1)
     assert not np.array_equal(core.read_framebuffer(), moved_img)
     core.close()
+
+
+def test_headless_application_rasterizer(core_lib, tmp_path):
+    """With the setting rasterizer=1 the plugin's Render draws the SoftRasterizer core's frame; every frame equals
+    lh2g_raster_render's through the C ABI, a moved instance included."""
+    from lighthouse2_gb300 import build as B
+    app = B.build_harness()
+    W2, H2 = 200, 120
+    sc = S.spheres_2m(seed=5, n_spheres=6, slices=40, stacks=26, tex_size=64)
+    moved = sc.instances[2][1].copy()
+    moved[0, 3] += 1.5
+    frames = [(S.spheres_view(W2, H2, frame=0), 1, None), (S.spheres_view(W2, H2, frame=1), 0, (2, sc.instances[2][0], moved))]
+    scenefile.write_scene(tmp_path / "scene.bin", sc)
+    scenefile.write_frames(tmp_path / "frames.bin", frames)
+    r = subprocess.run([app, core_lib, str(tmp_path / "scene.bin"), str(tmp_path / "frames.bin"), str(tmp_path / "out.bin"), str(W2), str(H2),
+                        "1", "rasterizer=1"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    got = np.fromfile(tmp_path / "out.bin", np.uint32).reshape(-1, W2 * H2)
+    assert len(got) == len(frames)
+    core = RenderCore()
+    core.set_scene(sc)
+    core.SetTarget(W2, H2, 1)
+    for k, (view, _, change) in enumerate(frames):
+        if change is not None:
+            core.SetInstance(change[0], change[1], change[2])
+            core.FinalizeInstances()
+        expect = core.raster(view)["pixels"]
+        assert np.array_equal(got[k], expect), f"frame {k}: {np.count_nonzero(got[k] != expect)} pixels differ"
+        assert np.count_nonzero(expect) > W2 * H2 // 10
+    core.close()
