@@ -162,6 +162,11 @@ typedef struct lh2g_render_params {
 /* Set by lh2g_render_adaptive (not by callers): the PrimeAdaptive core's shading (the OptiX 7 estimator with
  * per-sample accumulators, a sample count in w and albedo/normal features for the variance estimate). */
 #define LH2G_RP_ADAPTIVE   32
+/* With LH2G_RP_OPTIX7 or LH2G_RP_ADAPTIVE: the Disney principled BSDF (lib/sharedBSDFs/disney.h with ggxmdf.h and
+ * frosted.h, the default branch of those cores' kernels/bsdf.h) instead of lambert.h; light connections then take
+ * the BSDF value without lambert.h's ROUGHNESS factor (BSDF_HAS_PURE_SPECULARS is lambert.h's), and the sampler
+ * uses the third random number that lambert.h draws and ignores. */
+#define LH2G_RP_DISNEY     64
 
 /* One SVGF pass over the accumulator of a LH2G_RP_FILTER frame (lib/RenderCore_Optix7Filter/rendercore.cpp:
  * 897-935 with the kernels of lib/CUDA/shared_kernel_code/finalize_shared.h:169-600). */

@@ -34,7 +34,7 @@ STATS_FIELDS = ["totalRays", "totalExtensionRays", "totalShadowRays", "primaryRa
 STATS_DTYPE = np.dtype([(f, "<u4") for f in STATS_FIELDS[:6]] + [(f, "<f4") for f in STATS_FIELDS[6:14]] +
                        [(f, "<u4") for f in STATS_FIELDS[14:18]] + [("probedInstid", "<i4"), ("probedTriid", "<i4"),
                                                                     ("probedDist", "<f4"), ("deviceStatus", "<u4")])
-RP_NEE, RP_DEPTH_W, RP_FILTER, RP_OPTIX7, RP_ADAPTIVE = 1, 2, 4, 16, 32
+RP_NEE, RP_DEPTH_W, RP_FILTER, RP_OPTIX7, RP_ADAPTIVE, RP_DISNEY = 1, 2, 4, 16, 32, 64
 # filter buffer slots (LH2G_FB_*): name -> (index, element dtype, components per pixel)
 FILTER_SLOTS = {"features": (0, np.uint32, 4), "worldPos": (1, np.float32, 4), "prevWorldPos": (2, np.float32, 4),
                 "deltaDepth": (3, np.float32, 4), "motion": (4, np.float32, 2), "moments": (5, np.float32, 4),

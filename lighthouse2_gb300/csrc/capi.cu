@@ -252,6 +252,7 @@ struct lh2g_context {
     /* estimator of lh2g_render (setting "estimator": 0 PrimeRef, 1 OptiX 7; "adaptive" 1: PrimeAdaptive frames) and
      * the OptiX 7 cores' blue-noise shift seed (rendercore.h: shiftSeed = 0x11331445, never reset) */
     int estimator = 0, adaptive = 0;
+    int bsdf = 0;                      /* setting "bsdf" for those two estimators: 0 lambert.h, 1 disney.h (LH2G_RP_DISNEY) */
     uint32_t shiftSeed = 0x11331445u;
     /* PrimeAdaptive frames: the second wave's per-slot radiance and layer, the first wave's features, per-pixel
      * deviation / requested / kept counts and slots, scan scratch, the device state and the second wave's counters */
@@ -799,6 +800,10 @@ int lh2g_setting(lh2g_context* ctx, const char* name, float value) {
         if (value != 0.0f && value != 1.0f) return fail(ctx, LH2G_ERR_INVALID, "setting estimator: 0 (PrimeRef) or 1 (OptiX 7)");
         ctx->estimator = (int)value;
     } else if (!strcmp(name, "adaptive")) ctx->adaptive = value != 0.0f;
+    else if (!strcmp(name, "bsdf")) {
+        if (value != 0.0f && value != 1.0f) return fail(ctx, LH2G_ERR_INVALID, "setting bsdf: 0 (lambert.h) or 1 (disney.h)");
+        ctx->bsdf = (int)value;
+    }
     else if (!strcmp(name, "waveTail")) {
         if (value < 0 || value > 65) return fail(ctx, LH2G_ERR_INVALID, "setting waveTail: 0 (off) or 1..65");
         ctx->tailDepth = (int)value;
@@ -961,6 +966,8 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
     const bool filt = (p->flags & LH2G_RP_FILTER) != 0, nrcFrame = (p->flags & LH2G_RP_NRC) != 0;
     if (filt && nrcFrame) return fail(ctx, LH2G_ERR_INVALID, "render: filter and radiance-cache frames do not combine");
     if (p->flags & LH2G_RP_ADAPTIVE) return fail(ctx, LH2G_ERR_INVALID, "render: adaptive frames go through lh2g_render_adaptive");
+    if ((p->flags & LH2G_RP_DISNEY) && !(p->flags & LH2G_RP_OPTIX7))
+        return fail(ctx, LH2G_ERR_INVALID, "render: the Disney BSDF belongs to the OptiX 7 estimator and adaptive frames");
     if ((p->flags & LH2G_RP_OPTIX7) && (filt || nrcFrame || (p->flags & LH2G_RP_DEPTH_W)))
         return fail(ctx, LH2G_ERR_INVALID, "render: the OptiX 7 estimator combines with none of filter, radiance-cache or depth frames");
     if ((p->flags & LH2G_RP_OPTIX7) && ctx->cap >= (1ll << MIS_SLOT_BITS))
@@ -1140,8 +1147,8 @@ int render_adaptive(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_
     if (!ctx->cap) return fail(ctx, LH2G_ERR_STATE, "render: no target (call lh2g_set_target)");
     if (p->width != ctx->W || p->height != ctx->H || p->spp != ctx->spp || p->maxDepth < 1 || p->maxDepth > 32)
         return fail(ctx, LH2G_ERR_INVALID, "render_adaptive: parameters do not match the target (or maxDepth beyond 32)");
-    if ((p->flags & ~LH2G_RP_NEE) || p->rowCount != 0)
-        return fail(ctx, LH2G_ERR_INVALID, "render_adaptive: only LH2G_RP_NEE combines with adaptive frames (whole frames)");
+    if ((p->flags & ~(LH2G_RP_NEE | LH2G_RP_DISNEY)) || p->rowCount != 0)
+        return fail(ctx, LH2G_ERR_INVALID, "render_adaptive: only LH2G_RP_NEE and LH2G_RP_DISNEY combine with adaptive frames (whole frames)");
     if (ctx->cap >= (1ll << MIS_SLOT_BITS)) return fail(ctx, LH2G_ERR_INVALID, "render_adaptive: at most 2^26 paths per frame");
     if (!ctx->mats) return fail(ctx, LH2G_ERR_STATE, "render: no materials");
     if (!materials_cover_meshes(ctx)) return fail(ctx, LH2G_ERR_INVALID, "render: a triangle's material index exceeds the material count");
@@ -1446,7 +1453,7 @@ int lh2g_render(lh2g_context* ctx, const lh2g_view* view, int converge) {
         p.cameraR0 = xorshift(ctx->camSeed);
         p.frameSeed = xorshift(ctx->camSeed);
         p.maxDepth = std::min(ctx->maxDepth, 32);
-        p.flags = ctx->nee ? LH2G_RP_NEE : 0;
+        p.flags = (ctx->nee ? LH2G_RP_NEE : 0) | (ctx->bsdf ? LH2G_RP_DISNEY : 0);
         r = lh2g_render_adaptive(ctx, view, &p, ctx->samplesTaken > 0 ? 1 : 0, nullptr, nullptr, nullptr, nullptr);
     } else if (ctx->estimator == 1) {
         /* rendercore_optix7/rendercore.cpp:855,900: one shift draw per frame, one camera draw per wave (here every
@@ -1454,7 +1461,7 @@ int lh2g_render(lh2g_context* ctx, const lh2g_view* view, int converge) {
         p.shift = xorshift(ctx->shiftSeed);
         p.cameraR0 = xorshift(ctx->camSeed);
         for (int d = 1; d < p.maxDepth; d++) xorshift(ctx->camSeed);
-        p.flags = (ctx->nee ? LH2G_RP_NEE : 0) | LH2G_RP_OPTIX7;
+        p.flags = (ctx->nee ? LH2G_RP_NEE : 0) | LH2G_RP_OPTIX7 | (ctx->bsdf ? LH2G_RP_DISNEY : 0);
         r = lh2g_render_ex(ctx, view, &p, ctx->samplesTaken > 0 ? 1 : 0, nullptr, nullptr, nullptr);
     } else {
         p.cameraR0 = xorshift(ctx->camSeed);

@@ -24,6 +24,8 @@ LH2G_DEV float3 operator*(float3 a, float3 b) { return make_float3(a.x * b.x, a.
 LH2G_DEV float3 operator*(float3 a, float b) { return make_float3(a.x * b, a.y * b, a.z * b); }
 LH2G_DEV float3 operator*(float b, float3 a) { return make_float3(b * a.x, b * a.y, b * a.z); }
 LH2G_DEV float3 operator/(float3 a, float b) { return make_float3(a.x / b, a.y / b, a.z / b); }
+LH2G_DEV float3 operator+(float3 a, float b) { return make_float3(a.x + b, a.y + b, a.z + b); }
+LH2G_DEV float3 operator+(float b, float3 a) { return make_float3(b + a.x, b + a.y, b + a.z); }
 LH2G_DEV float2 operator+(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 LH2G_DEV float2 operator*(float2 a, float2 b) { return make_float2(a.x * b.x, a.y * b.y); }
 LH2G_DEV float2 operator*(float2 a, float b) { return make_float2(a.x * b, a.y * b); }
@@ -109,6 +111,35 @@ LH2G_DEV float log2_at(float x) {
     const float s2 = s * s;
     const float at = s + s * s2 * ((float)(1.0 / 3.0) + s2 * ((float)(1.0 / 5.0) + s2 * ((float)(1.0 / 7.0) + s2 * ((float)(1.0 / 9.0) + s2 * (float)(1.0 / 11.0)))));
     return (float)e + at * 2.885390043258667f;
+}
+
+/* natural logarithm: log2_at's reduction and atanh series, ln x = e ln 2 + 2 atanh(s) (ln 2 split in two so that
+ * e ln 2 is exact) */
+LH2G_DEV float log_at(float x) {
+    if (x != x) return x;
+    if (x < 0.0f) return __int_as_float(0x7fc00000);
+    if (x == 0.0f) return __int_as_float(0xff800000);
+    if (x == __int_as_float(0x7f800000)) return x;
+    uint32_t b = __float_as_uint(x);
+    int e = 0;
+    if (b < 0x00800000u) { x = x * 8388608.0f; b = __float_as_uint(x); e = -23; }
+    e += (int)((b >> 23) & 255u) - 127;
+    float m = __uint_as_float((b & 0x007fffffu) | 0x3f800000u);
+    if (m > 1.41421356f) { m = m * 0.5f; e += 1; }
+    const float s = (m - 1.0f) / (m + 1.0f);
+    const float s2 = s * s;
+    const float at = s + s * s2 * ((float)(1.0 / 3.0) + s2 * ((float)(1.0 / 5.0) + s2 * ((float)(1.0 / 7.0) + s2 * ((float)(1.0 / 9.0) + s2 * (float)(1.0 / 11.0)))));
+    return (float)e * LN2_HI + ((float)e * LN2_LO + at * 2.0f);
+}
+
+/* x^y as exp(y ln x) for x > 0; 0^y = 0 (y > 0) or 1 (y = 0); NaN for x < 0 (the BSDFs raise squared roughness in
+ * (0, 1) to a power in [0, 1]) */
+LH2G_DEV float pow_at(float x, float y) {
+    if (x != x || y != y) return x + y;
+    if (x < 0.0f) return __int_as_float(0x7fc00000);
+    if (y == 0.0f) return 1.0f;
+    if (x == 0.0f) return y > 0.0f ? 0.0f : __int_as_float(0x7f800000);
+    return exp_cw(y * log_at(x));
 }
 
 LH2G_DEV float atan_unit(float t) {

@@ -23,7 +23,20 @@ struct Shading {
     float3 transmittance;
     uint32_t params[4];
     int flags;
+    float4 tint;   /* the Disney BSDF's tint (xyz) and luminance (w) of the base colour; set when GetShadingData is asked */
 };
+
+/* material_shared.h:19-35: the CIE XYZ conversions of the base colour's tint */
+LH2G_DEV float4 tint_of(const float3 rgb) {
+    const float3 xyz = make_float3(fmaxf(0.0f, 0.412453f * rgb.x + 0.357580f * rgb.y + 0.180423f * rgb.z),
+                                   fmaxf(0.0f, 0.212671f * rgb.x + 0.715160f * rgb.y + 0.072169f * rgb.z),
+                                   fmaxf(0.0f, 0.019334f * rgb.x + 0.119193f * rgb.y + 0.950227f * rgb.z));
+    if (!(xyz.y > 0)) return make_float4(1.0f, 1.0f, 1.0f, xyz.y);
+    const float3 n = xyz * (1.0f / xyz.y);
+    return make_float4(fmaxf(0.0f, 3.240479f * n.x - 1.537150f * n.y - 0.498535f * n.z),
+                       fmaxf(0.0f, -0.969256f * n.x + 1.875992f * n.y + 0.041556f * n.z),
+                       fmaxf(0.0f, 0.055648f * n.x - 0.204043f * n.y + 1.057311f * n.z), xyz.y);
+}
 
 LH2G_DEV float char2flt(uint32_t a, int s) { return ((float)((a >> s) & 255u)) * (1.0f / 255.0f); }
 LH2G_DEV float ROUGHNESS(const Shading& sd) { return fmaxf(0.001f, char2flt(sd.params[0], 24)); }
@@ -78,7 +91,7 @@ LH2G_DEV float3 ConsistentNormal(const float3& D, const float3& iN, const float 
 
 /* GetShadingData + SetupFrame for triangle prim of instance inst. */
 LH2G_DEV void GetShadingData(const SceneGPU& S, const float3 D, const float u, const float v, const float coneWidth, const int inst,
-                             const int prim, Shading& sd, float3& N, float3& iN, float3& fN, float3& T) {
+                             const int prim, Shading& sd, float3& N, float3& iN, float3& fN, float3& T, const bool withTint = false) {
     const float4* tri = S.instTris[inst] + (size_t)prim * 13;
     const float4 t1 = __ldg(tri + 1), t2 = __ldg(tri + 2), t3 = __ldg(tri + 3), t4 = __ldg(tri + 4), t5 = __ldg(tri + 5), t7 = __ldg(tri + 7);
     const uint4* mat = S.materials + (size_t)min(__float_as_uint(t1.w), (uint32_t)(S.nMaterials - 1)) * 8;
@@ -88,6 +101,7 @@ LH2G_DEV void GetShadingData(const SceneGPU& S, const float3 D, const float u, c
     sd.transmittance = make_float3(half2float(base.y >> 16), half2float(base.z & 0xffffu), half2float(base.z >> 16));
     sd.params[0] = params.x, sd.params[1] = params.y, sd.params[2] = params.z, sd.params[3] = params.w;
     sd.flags = 0;
+    if (withTint) sd.tint = tint_of(sd.color);
     N = iN = fN = make_float3(t2.w, t3.w, t4.w);
     T = xyz(t5);
     const float w = 1 - (u + v);

@@ -3,6 +3,7 @@
 #pragma once
 #include "kernels.cuh"
 #include "shading.cuh"
+#include "disney.cuh"
 #include "svgf.cuh"
 #include "traverse.cuh"
 
@@ -454,7 +455,8 @@ __device__ __forceinline__ void shade_mis(const SceneGPU& S, const FrameGPU& F, 
     Shading sd;
     float3 N, iN, fN, T;
     const float3 I = O + HIT_T * D;
-    GetShadingData(S, D, HIT_U, HIT_V, F.spreadAngle * HIT_T, INST, PRIM, sd, N, iN, fN, T);
+    const bool disneyBsdf = (F.flags & LH2G_RP_DISNEY) != 0;   /* kernels/bsdf.h's default branch: disney.h */
+    GetShadingData(S, D, HIT_U, HIT_V, F.spreadAngle * HIT_T, INST, PRIM, sd, N, iN, fN, T, disneyBsdf);
     if (feat) *feat = make_float4(sd.color.x, sd.color.y, sd.color.z, __uint_as_float(PackNormal2(iN)));
     const uint32_t tminBits = optix7 ? MIS_TMIN_EPS : 0u;
     if (sd.flags & 1) {   /* alpha: the ray continues behind the surface */
@@ -522,7 +524,9 @@ __device__ __forceinline__ void shade_mis(const SceneGPU& S, const FrameGPU& F, 
         const float NdotL = dot(L, fN * faceDir);
         if (NdotL > 0 && lightPdf > 0) {
             float lbsdfPdf;
-            const float3 sampledBSDF = EvaluateBSDF(sd, fN, L, lbsdfPdf) * ROUGHNESS(sd);
+            /* lambert.h defines BSDF_HAS_PURE_SPECULARS: its value is scaled by ROUGHNESS (pathtracer.h:194-198) */
+            const float3 sampledBSDF = disneyBsdf ? disney::EvaluateBSDF(sd, fN, T, D * -1.0f, L, lbsdfPdf)
+                                                  : EvaluateBSDF(sd, fN, L, lbsdfPdf) * ROUGHNESS(sd);
             if (lbsdfPdf > 0) {
                 float3 contribution = throughput * sampledBSDF * lightColor * (NdotL / (pickProb * lightPdf + lbsdfPdf));
                 fix_nan(contribution);
@@ -537,11 +541,12 @@ __device__ __forceinline__ void shade_mis(const SceneGPU& S, const FrameGPU& F, 
     }
     /* one diffuse bounce at most (ENOUGH_BOUNCES = S_BOUNCED), or the maximum path length */
     if ((FLAGS & S_BOUNCED) || depth == F.maxDepth) { if (B.capSeeds) B.capSeeds[capIdx] = seed; return; }
-    float3 R;
-    float newBsdfPdf;
+    float3 R = mk3(0);
+    float newBsdfPdf = 0.0f;   /* the Disney sampler leaves it unset on its early exits: the path ends there */
     bool specular = false;
-    (void)RandomFloat(seed);   /* the r5 argument of lambert.h's SampleBSDF: drawn, not used */
-    const float3 bsdf = SampleBSDF(sd, fN, N, D * -1.0f, HIT_T, r4.z, r4.w, R, newBsdfPdf, specular);
+    const float r5 = RandomFloat(seed);   /* lambert.h's SampleBSDF draws it and does not use it */
+    const float3 bsdf = disneyBsdf ? disney::SampleBSDF(sd, fN, N, T, D * -1.0f, HIT_T, r4.z, r4.w, r5, R, newBsdfPdf, specular)
+                                   : SampleBSDF(sd, fN, N, D * -1.0f, HIT_T, r4.z, r4.w, R, newBsdfPdf, specular);
     if (newBsdfPdf < EPSILON || isnan(newBsdfPdf)) { if (B.capSeeds) B.capSeeds[capIdx] = seed; return; }
     if (specular) FLAGS |= S_SPECULAR;
     const float pr = ((FLAGS & S_SPECULAR) || (FLAGS & S_BOUNCED) == 0) ? 1.0f : SurvivalProbability(bsdf);

@@ -26,7 +26,7 @@ PARAMS_DTYPE = np.dtype([("width", "<i4"), ("height", "<i4"), ("spp", "<i4"), ("
 FILTER_PARAMS_DTYPE = np.dtype([("prevView", S.VIEW_DTYPE), ("j0", "<f4"), ("j1", "<f4"), ("prevj0", "<f4"), ("prevj1", "<f4"),
                                 ("clampDirect", "<f4"), ("clampIndirect", "<f4"), ("samplesTaken", "<i4"),
                                 ("camIsStationary", "<i4"), ("taa", "<i4")])
-RP_NEE, RP_DEPTH_W, RP_FILTER, RP_OPTIX7, RP_ADAPTIVE = 1, 2, 4, 16, 32
+RP_NEE, RP_DEPTH_W, RP_FILTER, RP_OPTIX7, RP_ADAPTIVE, RP_DISNEY = 1, 2, 4, 16, 32, 64
 
 
 def build_oracle():
@@ -490,32 +490,36 @@ class RefOptix7(RefKernels):
     queries. The connection buffer is made large enough that the loop's early flush (rendercore.cpp:906-913) never
     triggers."""
 
-    def __init__(self):
+    def __init__(self, disney=False):
+        """disney: the kernel built with the Disney BSDF (ref_o7d_*) instead of lambert.h (ref_o7_*)."""
         super().__init__()
-        L = self.lib
         vp, i, f, u = C.c_void_p, C.c_int, C.c_float, C.c_uint32
-        L.ref_o7_set_scene.argtypes = [vp] * 2 + [vp, i] * 4 + [vp, f, f, i, vp, i, i, vp]
-        L.ref_o7_init_counters.argtypes = [i]
-        L.ref_o7_counters.argtypes = [vp]
-        L.ref_o7_generate.argtypes = [vp, i, i, i, i, i, vp, f, vp, vp, vp, f]
-        L.ref_o7_shade.argtypes = [i, vp, vp, vp, vp, u, u, i, i, i, i, i, f, i]
-        L.ref_o7_finalize_connections.argtypes = [i, vp, vp, vp, i]
-        L.ref_o7_bluenoise4.argtypes = [vp, i, i, i, i, vp]
-        L.ref_o7_set_shadow_count.argtypes = [u]
+        pre = "ref_o7d_" if disney else "ref_o7_"
+        sig = {"set_scene": [vp] * 2 + [vp, i] * 4 + [vp, f, f, i, vp, i, i, vp], "init_counters": [i], "next_counters": [],
+               "counters": [vp], "generate": [vp, i, i, i, i, i, vp, f, vp, vp, vp, f], "shade": [i, vp, vp, vp, vp, u, u, i, i, i, i, i, f, i],
+               "finalize_connections": [i, vp, vp, vp, i], "bluenoise4": [vp, i, i, i, i, vp], "set_shadow_count": [u]}
+
+        class _Fns:
+            pass
+        self.fn = _Fns()
+        for name, args in sig.items():
+            fn = getattr(self.lib, pre + name)
+            fn.argtypes = args
+            setattr(self.fn, name, fn)
 
     def render(self, oracle: Oracle, sc: S.Scene, view, params, accum=None):
         """One frame; returns the accumulator, per path length the extension and connection counts, and whether the
         loop flushed its connection buffer early (pathCount + shadowRays >= 2 P: connections then reach the
         accumulator before later path lengths' terms)."""
-        L = self.lib
+        L = self.fn
         W, H, spp, D = int(params["width"]), int(params["height"]), int(params["spp"]), int(params["maxDepth"])
         P = W * H * spp
         eps = float(params["geometryEpsilon"])
         nee = int(params["flags"]) & RP_NEE
-        inst, packed, texels, sky4, sw, sh = _ref_scene(L, oracle, sc)
+        inst, packed, texels, sky4, sw, sh = _ref_scene(self.lib, oracle, sc)
         bn = expand_blue_noise(sc.blue_noise)
         self._keep = [inst, packed, texels, sky4, bn]
-        L.ref_o7_set_scene(_p(inst), _p(packed), _p(sc.tri_lights), len(sc.tri_lights), _p(sc.point_lights), len(sc.point_lights),
+        L.set_scene(_p(inst), _p(packed), _p(sc.tri_lights), len(sc.tri_lights), _p(sc.point_lights), len(sc.point_lights),
                            _p(sc.spot_lights), len(sc.spot_lights), _p(sc.dir_lights), len(sc.dir_lights), _p(texels), eps,
                            float(params["clampValue"]), D, _p(sky4), sw, sh, _p(bn))
         ps = np.zeros((3 * P, 4), np.float32)
@@ -526,9 +530,9 @@ class RefOptix7(RefKernels):
         right = (v["p2"] - v["p1"]).astype(np.float32)
         up = (v["p3"] - v["p1"]).astype(np.float32)
         shift = int(params["shift"])
-        L.ref_o7_generate(_p(ps), W, H, spp, int(params["samplesTaken"]), shift - (1 << 32) if shift >= 1 << 31 else shift,
+        L.generate(_p(ps), W, H, spp, int(params["samplesTaken"]), shift - (1 << 32) if shift >= 1 << 31 else shift,
                           _p(v["pos"].copy()), float(v["aperture"]), _p(right), _p(up), _p(v["p1"].copy()), float(v["distortion"]))
-        L.ref_o7_init_counters(P)
+        L.init_counters(P)
         counters = np.zeros((D, 2), np.uint32)
         draw, count, seen, flushed = int(params["cameraR0"]), P, 0, False
         c2 = np.zeros(2, np.uint32)
@@ -538,11 +542,11 @@ class RefOptix7(RefKernels):
             rays["o"], rays["d"] = conn[:n, :3], conn[2 * P:2 * P + n, :3]
             rays["tmin"], rays["tmax"] = eps, conn[2 * P:2 * P + n, 3]
             occ = oracle.trace(rays, mode=1).astype(np.uint32)
-            L.ref_o7_finalize_connections(n, _p(acc), _p(conn), _p(occ), P)
+            L.finalize_connections(n, _p(acc), _p(conn), _p(occ), P)
 
         for pl in range(1, D + 1):
             if pl > 1:
-                L.ref_o7_next_counters()
+                L.next_counters()
                 draw = _xorshift(draw)
             rays = np.zeros(count, S.RAY_DTYPE)
             rays["o"], rays["d"] = ps[:count, :3], ps[P:P + count, :3]
@@ -552,9 +556,9 @@ class RefOptix7(RefKernels):
             hits[:count, 1] = h["inst"].view(np.float32)
             hits[:count, 2] = h["prim"].view(np.float32)
             hits[:count, 3] = h["t"]
-            L.ref_o7_shade(count, _p(acc), _p(ps), _p(hits), _p(conn), (draw + pl * 91771) & 0xFFFFFFFF, shift,
+            L.shade(count, _p(acc), _p(ps), _p(hits), _p(conn), (draw + pl * 91771) & 0xFFFFFFFF, shift,
                            int(params["samplesTaken"]), pl, W, H, spp, float(v["spreadAngle"]), nee)
-            L.ref_o7_counters(_p(c2))
+            L.counters(_p(c2))
             counters[pl - 1] = (c2[0], c2[1] - seen)
             seen, count = int(c2[1]), int(c2[0])
             if count == 0:
@@ -562,7 +566,7 @@ class RefOptix7(RefKernels):
             if count + seen >= 2 * P and seen > 0:   # rendercore.cpp:906-913
                 connect(seen)
                 flushed = True
-                L.ref_o7_set_shadow_count(0)
+                L.set_shadow_count(0)
                 seen = 0
         if seen:
             connect(seen)
@@ -570,7 +574,7 @@ class RefOptix7(RefKernels):
 
     def bluenoise4(self, bn, x, y, sample, dim):
         out = np.zeros(4, np.float32)
-        self.lib.ref_o7_bluenoise4(_p(bn), x, y, sample, dim, _p(out))
+        self.fn.bluenoise4(_p(bn), x, y, sample, dim, _p(out))
         return out
 
 

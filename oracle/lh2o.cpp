@@ -43,6 +43,8 @@ inline f3 operator*(f3 a, f3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
 inline f3 operator*(f3 a, float b) { return {a.x * b, a.y * b, a.z * b}; }
 inline f3 operator*(float b, f3 a) { return {b * a.x, b * a.y, b * a.z}; }
 inline f3 operator/(f3 a, float b) { return {a.x / b, a.y / b, a.z / b}; }
+inline f3 operator+(f3 a, float b) { return {a.x + b, a.y + b, a.z + b}; }
+inline f3 operator+(float b, f3 a) { return {b + a.x, b + a.y, b + a.z}; }
 inline f2 operator+(f2 a, f2 b) { return {a.x + b.x, a.y + b.y}; }
 inline f2 operator*(f2 a, f2 b) { return {a.x * b.x, a.y * b.y}; }
 inline f2 operator*(f2 a, float b) { return {a.x * b, a.y * b}; }
@@ -147,6 +149,33 @@ inline float lm_log2f(float x) {
     const float s2 = s * s;
     const float at = s + s * s2 * ((float)(1.0 / 3.0) + s2 * ((float)(1.0 / 5.0) + s2 * ((float)(1.0 / 7.0) + s2 * ((float)(1.0 / 9.0) + s2 * (float)(1.0 / 11.0)))));
     return (float)e + at * 2.885390043258667f;
+}
+
+/* natural logarithm: lm_log2f's reduction and atanh series, ln x = e ln 2 + 2 atanh(s) (ln 2 split so e ln 2 is exact) */
+inline float lm_logf(float x) {
+    if (x != x) return x;
+    if (x < 0.0f) return bitsf(0x7fc00000u);
+    if (x == 0.0f) return bitsf(0xff800000u);
+    if (x == bitsf(0x7f800000u)) return x;
+    uint b = fbits(x);
+    int e = 0;
+    if (b < 0x00800000u) { x = x * 8388608.0f; b = fbits(x); e = -23; }
+    e += (int)((b >> 23) & 255u) - 127;
+    float m = bitsf((b & 0x007fffffu) | 0x3f800000u);
+    if (m > 1.41421356f) { m = m * 0.5f; e += 1; }
+    const float s = (m - 1.0f) / (m + 1.0f);
+    const float s2 = s * s;
+    const float at = s + s * s2 * ((float)(1.0 / 3.0) + s2 * ((float)(1.0 / 5.0) + s2 * ((float)(1.0 / 7.0) + s2 * ((float)(1.0 / 9.0) + s2 * (float)(1.0 / 11.0)))));
+    return (float)e * LN2_HI + ((float)e * LN2_LO + at * 2.0f);
+}
+
+/* x^y as exp(y ln x) for x > 0; 0^y = 0 (y > 0) or 1 (y = 0); NaN for x < 0 */
+inline float lm_powf(float x, float y) {
+    if (x != x || y != y) return x + y;
+    if (x < 0.0f) return bitsf(0x7fc00000u);
+    if (y == 0.0f) return 1.0f;
+    if (x == 0.0f) return y > 0.0f ? 0.0f : bitsf(0x7f800000u);
+    return lm_expf(y * lm_logf(x));
 }
 
 inline float lm_atan_unit(float t) { /* |t| <= 1 */
@@ -650,7 +679,18 @@ struct ShadingData {
     f3 color; int flags;
     f3 transmittance; int matID;
     uint params[4];
+    f4 tint;   /* the Disney BSDF's tint (xyz) and luminance (w) of the base colour, when GetShadingData is asked */
 };
+/* material_shared.h:19-35,118-119: the base colour's tint through CIE XYZ */
+inline f4 tint_of(const f3 rgb) {
+    const f3 xyz = mk3(fmaxf(0.0f, 0.412453f * rgb.x + 0.357580f * rgb.y + 0.180423f * rgb.z),
+                       fmaxf(0.0f, 0.212671f * rgb.x + 0.715160f * rgb.y + 0.072169f * rgb.z),
+                       fmaxf(0.0f, 0.019334f * rgb.x + 0.119193f * rgb.y + 0.950227f * rgb.z));
+    if (!(xyz.y > 0)) return {1.0f, 1.0f, 1.0f, xyz.y};
+    const f3 n = xyz * (1.0f / xyz.y);
+    return {fmaxf(0.0f, 3.240479f * n.x - 1.537150f * n.y - 0.498535f * n.z), fmaxf(0.0f, -0.969256f * n.x + 1.875992f * n.y + 0.041556f * n.z),
+            fmaxf(0.0f, 0.055648f * n.x - 0.204043f * n.y + 1.057311f * n.z), xyz.y};
+}
 inline float char2flt(uint a, int s) { return ((float)((a >> s) & 255u)) * (1.0f / 255.0f); }
 inline float ROUGHNESS(const ShadingData& sd) { return fmaxr(0.001f, char2flt(sd.params[0], 24)); }
 inline float TRANSMISSION(const ShadingData& sd) { return char2flt(sd.params[2], 16); }
@@ -699,7 +739,7 @@ inline f2 map_uvoffs(const uint* m) { return mk2(half2float(m[2] & 0xffffu), hal
 /* GetShadingData + SetupFrame, material_shared.h:42-206 (non-Prime barycentric convention: w V0 + u V1 + v V2,
  * CONSISTENTNORMALS on). Returns the three normals and the tangent. */
 void GetShadingData(const lh2o_scene* s, const f3 D, const float u, const float v, const float coneWidth,
-                    const lh2g_core_tri& tri, const int instIdx, ShadingData& sd, f3& N, f3& iN, f3& fN, f3& T) {
+                    const lh2g_core_tri& tri, const int instIdx, ShadingData& sd, f3& N, f3& iN, f3& fN, f3& T, const bool withTint = false) {
     const lh2g_gpu_material& mat = s->mats[tri.material];
     const uint part0 = mat.base[0], part1 = mat.base[1], part2 = mat.base[2], flags = mat.base[3];
     sd.color = mk3(half2float(part0 & 0xffffu), half2float(part0 >> 16), half2float(part1 & 0xffffu));
@@ -707,6 +747,7 @@ void GetShadingData(const lh2o_scene* s, const f3 D, const float u, const float 
     sd.transmittance = mk3(half2float(part1 >> 16), half2float(part2 & 0xffffu), half2float(part2 >> 16));
     sd.matID = 0;
     for (int i = 0; i < 4; i++) sd.params[i] = mat.params[i];
+    if (withTint) sd.tint = tint_of(sd.color);
     /* SetupFrame */
     N = iN = fN = mk3(tri.Nx, tri.Ny, tri.Nz);
     T = ld3(tri.T);
@@ -833,6 +874,341 @@ f3 SampleBSDF(const ShadingData& sd, f3 iN, const f3 N, const f3 wo, const float
     if (dot(N * flip, wi) <= 0) pdf = 0;
     return bsdf;
 }
+
+/* ------------------------------------------------------------------------------------------------------
+ * The Disney principled BSDF (the OptiX 7 / PrimeAdaptive cores' default kernels/bsdf.h branch):
+ * lib/sharedBSDFs/disney.h, ggxmdf.h (CUDA branches of the samplers) and frosted.h, restated in their operation
+ * order with this file's transcendentals (lm_sincos, lm_expf, lm_logf, lm_powf). Values the reference leaves unset
+ * on measure-zero paths (a direction exactly in the tangent plane) are zero here.
+ * ---------------------------------------------------------------------------------------------------- */
+namespace dis {
+inline float METALLIC(const ShadingData& s) { return char2flt(s.params[0], 0); }
+inline float SUBSURFACE(const ShadingData& s) { return char2flt(s.params[0], 8); }
+inline float SPECULAR(const ShadingData& s) { return char2flt(s.params[0], 16); }
+inline float SPECTINT(const ShadingData& s) { return char2flt(s.params[1], 0); }
+inline float ANISOTROPIC(const ShadingData& s) { return char2flt(s.params[1], 8); }
+inline float SHEEN(const ShadingData& s) { return char2flt(s.params[1], 16); }
+inline float SHEENTINT(const ShadingData& s) { return char2flt(s.params[1], 24); }
+inline float CLEARCOAT(const ShadingData& s) { return char2flt(s.params[2], 0); }
+inline float CLEARCOATGLOSS(const ShadingData& s) { return char2flt(s.params[2], 8); }
+inline f3 TINT(const ShadingData& s) { return mk3(s.tint.x, s.tint.y, s.tint.z); }
+inline float LUMINANCE(const ShadingData& s) { return s.tint.w; }
+inline float sqr(float x) { return x * x; }
+inline float saturate(float x) { return fmaxr(0.0f, fminr(1.0f, x)); }
+inline float lerp(float a, float b, float t) { return a + t * (b - a); }
+inline float mix(float a, float b, float x) { return x <= 0 ? a : x >= 1 ? b : lerp(a, b, x); }
+inline float clampv(float f, float a, float b) { return fmaxr(a, fminr(f, b)); }
+inline f3 w2t(const f3 V, const f3 N, const f3 T, const f3 B) { return mk3(dot(V, T), dot(V, B), dot(V, N)); }
+inline f3 t2w(const f3 V, const f3 N, const f3 T, const f3 B) { return V.x * T + V.y * B + V.z * N; }
+inline f3 cos_sample(const float r0, const float r1, const f3 N, const f3 T, const f3 B) {   /* common_functions.h:118-124 */
+    const float term1 = TWOPI * r0, term2 = sqrtf(1 - r1);
+    float sn, cs;
+    lm_sincos(term1, &sn, &cs);
+    return (cs * term2 * T) + (sn * term2) * B + sqrtf(r1) * N;
+}
+/* ggxmdf.h */
+inline float ggx_D(const f3 m, const float ax, const float ay) {
+    if (m.z == 0) return sqr(ax) * INVPI;
+    const float c2 = sqr(m.z), sinT = sqrtf(fmaxr(0.0f, 1 - c2)), tan2 = (1.0f - c2) / c2;
+    const float st = (ax == ay || sinT == 0.0f) ? 1.0f / sqr(ax) : sqr(m.x / (sinT * ax)) + sqr(m.y / (sinT * ay));
+    return 1.0f / (PI * ax * ay * sqr(c2) * sqr(1.0f + tan2 * st));
+}
+inline float ggx_lambda(const f3 v, const float ax, const float ay) {
+    if (v.z == 0) return 0;
+    const float c2 = v.z * v.z, sinT = sqrtf(fmaxr(0.0f, 1 - c2));
+    const float proj = (ax == ay || sinT == 0.0f) ? ax : sqrtf(sqr((v.x * ax) / sinT) + sqr((v.y * ay) / sinT));
+    const float tan2 = sqr(sinT) / c2, a2rcp = sqr(proj) * tan2;
+    return (-1.0f + sqrtf(1.0f + a2rcp)) * 0.5f;
+}
+inline float ggx_G(const f3 wi, const f3 wo, const float ax, const float ay) { return 1.0f / (1.0f + ggx_lambda(wo, ax, ay) + ggx_lambda(wi, ax, ay)); }
+inline float ggx_G1(const f3 v, const float ax, const float ay) { return 1.0f / (1.0f + ggx_lambda(v, ax, ay)); }
+inline f3 ggx_sample(const f3 v, const float r0, const float r1, const float ax, const float ay) {
+    const float sgn = v.z < 0.0f ? -1.0f : 1.0f;
+    const f3 st = normalize(mk3(sgn * v.x * ax, sgn * v.y * ay, sgn * v.z));
+    const f3 t1 = v.z < 0.9999f ? normalize(cross(st, mk3(0, 0, 1))) : mk3(1, 0, 0);
+    const f3 t2 = cross(t1, st);
+    const float a = 1.0f / (1.0f + st.z), r = sqrtf(r0);
+    const float phi = r1 < a ? (r1 / a * PI) : (PI + (r1 - a) / (1.0f - a) * PI);
+    float p1, p2;
+    lm_sincos(phi, &p2, &p1);
+    p1 *= r;
+    p2 *= r * (r1 < a ? 1.0f : st.z);
+    const f3 h = p1 * t1 + p2 * t2 + sqrtf(fmaxr(0.0f, 1.0f - p1 * p1 - p2 * p2)) * st;
+    return normalize(mk3(h.x * ax, h.y * ay, fmaxr(0.0f, h.z)));
+}
+inline float ggx_pdf(const f3 v, const f3 m, const float ax, const float ay) {
+    if (v.z == 0.0f) return 0;
+    return ggx_G1(v, ax, ay) * fabsf(dot(v, m)) * ggx_D(m, ax, ay) / fabsf(v.z);
+}
+inline float gtr1_D(const f3 m, const float ax) {
+    const float alpha = clampv(ax, 0.001f, 0.999f), a2 = sqr(alpha);
+    const float a = (a2 - 1.0f) / (PI * lm_logf(a2)), b = (1 / (1 + (a2 - 1) * sqr(m.z)));
+    return a * b;
+}
+inline float gtr1_lambda(const f3 v, const float ax) {
+    if (v.z == 0) return 0;
+    const float c2 = sqr(v.z), sinT = sqrtf(fmaxr(0.0f, 1.0f - c2));
+    if (sinT == 0) return 0;
+    const float cot2 = c2 / sqr(sinT), cot = sqrtf(cot2), alpha2 = sqr(clampv(ax, 0.001f, 0.999f));
+    const float a = sqrtf(cot2 + alpha2), b = sqrtf(cot2 + 1.0f), c = lm_logf(cot + b), d = lm_logf(cot + a);
+    return (a - b + cot * (c - d)) / (cot * lm_logf(alpha2));
+}
+inline float gtr1_G(const f3 wi, const f3 wo, const float ax) { return 1.0f / (1.0f + gtr1_lambda(wo, ax) + gtr1_lambda(wi, ax)); }
+inline f3 gtr1_sample(const float r0, const float r1, const float ax) {
+    const float alpha = clampv(ax, 0.001f, 0.999f), a2 = sqr(alpha);
+    const float c2 = (1.0f - lm_powf(a2, 1.0f - r0)) / (1.0f - a2), sinT = sqrtf(fmaxr(0.0f, 1.0f - c2));
+    float sp, cp;
+    lm_sincos(TWOPI * r1, &sp, &cp);
+    return mk3(cp * sinT, sp * sinT, sqrtf(c2));
+}
+inline float gtr1_pdf(const f3 m, const float ax) { return gtr1_D(m, ax) * fabsf(m.z); }
+inline void alpha_from_roughness(const float roughness, const float anisotropy, float& ax, float& ay) {
+    const float sq = roughness * roughness, aspect = sqrtf(1.0f + anisotropy * (anisotropy < 0 ? 0.9f : -0.9f));
+    ax = fmaxr(0.001f, sq / aspect), ay = fmaxr(0.001f, sq * aspect);
+}
+/* frosted.h */
+inline float fresnel_dielectric(const float eta, const float ci, const float ct) {
+    if (ci == 0 && ct == 0) return 1;
+    const float k0 = eta * ct, k1 = eta * ci;
+    return 0.5f * (sqr((ci - k0) / (ci + k0)) + sqr((ct - k1) / (ct + k1)));
+}
+inline float fresnel_reflectance(const float ci, const float eta, float& ct) {
+    const float st2 = (1 - sqr(ci)) * sqr(eta);
+    if (st2 > 1) { ct = 0; return 1; }
+    ct = fminr(sqrtf(fmaxr(1 - st2, 0.0f)), 1.0f);
+    return fresnel_dielectric(eta, fabsf(ci), ct);
+}
+inline f3 refracted_direction(const f3 wo, const f3 m, const float cwm, const float ct, const float rcpEta) {
+    const f3 wi = cwm > 0 ? (rcpEta * cwm - ct) * m - rcpEta * wo : (rcpEta * cwm + ct) * m - rcpEta * wo;
+    return wi * ((3 - dot(wi, wi)) * 0.5f);
+}
+inline float choose_reflection(const float F) { const float r = F * 1, t = (1 - F) * 1, sum = r + t; return sum != 0 ? r / sum : 1; }
+inline f3 half_reflection(const f3 wo, const f3 wi) { const f3 h = normalize(wi + wo); return h.z < 0 ? (h * -1) : h; }
+inline f3 half_refraction(const f3 wo, const f3 wi, const float eta) { const f3 h = normalize(wo + eta * wi); return h.z < 0 ? (h * -1) : h; }
+inline f3 eval_reflection(const f3 color, const f3 wo, const f3 wi, const f3 m, const float ax, const float ay, const float F) {
+    const float denom = fabsf(4 * wo.z * wi.z);
+    if (denom == 0) return mk3(0);
+    const float D = ggx_D(m, ax, ay), G = ggx_G(wi, wo, ax, ay);
+    return color * (F * D * G / denom);
+}
+inline f3 eval_refraction(const float eta, const f3 color, const f3 wo, const f3 wi, const f3 m, const float ax, const float ay, const float Tr) {
+    if (wo.z == 0 || wi.z == 0) return mk3(0);
+    const float cih = dot(m, wi), coh = dot(m, wo), dots = (cih * coh) / (wi.z * wo.z), sd = coh + eta * cih;
+    if (fabsf(sd) < 1.0e-6f) return mk3(0);
+    const float D = ggx_D(m, ax, ay), G = ggx_G(wi, wo, ax, ay);
+    float mult = fabsf(dots) * Tr * D * G / sqr(sd);
+    mult *= sqr(eta);
+    return color * mult;
+}
+inline float reflection_jacobian(const float coh) { return coh == 0 ? 0.0f : 1 / (4 * fabsf(coh)); }
+inline float refraction_jacobian(const f3 wo, const f3 wi, const f3 m, const float eta) {
+    const float cih = dot(m, wi), coh = dot(m, wo), sd = coh + eta * cih;
+    if (fabsf(sd) < 1.0e-6f) return 0;
+    return fabsf(cih) * sqr(eta / sd);
+}
+/* disney.h */
+inline float schlick(const float u) { const float m = saturate(1.0f - u), m2 = sqr(m), m4 = sqr(m2); return m4 * m; }
+inline float clearcoat_roughness(const ShadingData& s) { return mix(0.1f, 0.001f, CLEARCOATGLOSS(s)); }
+inline f3 specular_fresnel(const ShadingData& s, const f3 o, const f3 h) {
+    const float st = SPECTINT(s), M = METALLIC(s);
+    f3 v = (1.0f - st) + st * TINT(s);
+    v = v * (SPECULAR(s) * 0.08f);
+    v = (1.0f - M) * v + M * s.color;
+    const float f = schlick(fabsf(dot(o, h)));
+    return (1.0f - f) * v + f;
+}
+inline f3 clearcoat_fresnel(const ShadingData& s, const f3 o, const f3 h) { return mk3(mix(0.04f, 1.0f, schlick(fabsf(dot(o, h)))) * 0.25f * CLEARCOAT(s)); }
+template <bool GTR1>
+inline void sample_mf(const ShadingData& s, const float r0, const float r1, const float ax, const float ay, const f3 wol, f3& wil, float& pdf, f3& value) {
+    if (wol.z == 0) { value = mk3(0); pdf = 0; return; }
+    const f3 m = GTR1 ? gtr1_sample(r0, r1, ax) : ggx_sample(wol, r0, r1, ax, ay);
+    wil = reflect(wol * -1.0f, m);
+    if (wil.z == 0) return;
+    const float coh = dot(wol, m);
+    pdf = (GTR1 ? gtr1_pdf(m, ax) : ggx_pdf(wol, m, ax, ay)) / fabsf(4.0f * coh);
+    if (pdf < 1.0e-6f) return;
+    const float D = GTR1 ? gtr1_D(m, ax) : ggx_D(m, ax, ay);
+    const float G = GTR1 ? gtr1_G(wil, wol, ax) : ggx_G(wil, wol, ax, ay);
+    value = GTR1 ? clearcoat_fresnel(s, wol, m) : specular_fresnel(s, wol, m);
+    value = value * (D * G);
+}
+template <bool GTR1>
+inline float evaluate_mf(const ShadingData& s, const float ax, const float ay, const f3 wol, const f3 wil, const f3 m, f3& bsdf) {
+    if (wol.z == 0 || wil.z == 0) return 0;
+    const float coh = dot(wol, m);
+    if (coh == 0) return 0;
+    const float D = GTR1 ? gtr1_D(m, ax) : ggx_D(m, ax, ay);
+    const float G = GTR1 ? gtr1_G(wil, wol, ax) : ggx_G(wil, wol, ax, ay);
+    bsdf = GTR1 ? clearcoat_fresnel(s, wol, m) : specular_fresnel(s, wol, m);
+    bsdf = bsdf * (D * G / fabsf(4.0f * wol.z * wil.z));
+    return (GTR1 ? gtr1_pdf(m, ax) : ggx_pdf(wol, m, ax, ay)) / fabsf(4.0f * coh);
+}
+inline float evaluate_diffuse(const ShadingData& s, const f3 iN, const f3 wow, const f3 wiw, const f3 m, f3& value) {
+    const float con = dot(iN, wow), cin = dot(iN, wiw), cih = dot(wiw, m);
+    const float fl = schlick(cin), fv = schlick(con), R = ROUGHNESS(s), SS = SUBSURFACE(s);
+    float fd = 0;
+    if (SS != 1.0f) {
+        const float fd90 = 0.5f + 2.0f * sqr(cih) * R;
+        fd = mix(1.0f, fd90, fl) * mix(1.0f, fd90, fv);
+    }
+    if (SS > 0) {
+        const float fss90 = sqr(cih) * R, fss = mix(1.0f, fss90, fl) * mix(1.0f, fss90, fv);
+        const float ss = 1.25f * (fss * (1.0f / (fabsf(con) + fabsf(cin)) - 0.5f) + 0.5f);
+        fd = mix(fd, ss, SS);
+    }
+    value = s.color * fd * INVPI * (1.0f - METALLIC(s));
+    return fabsf(cin) * INVPI;
+}
+inline float evaluate_sheen(const ShadingData& s, const f3 wiw, const f3 m, f3& value) {
+    const float fh = schlick(dot(wiw, m)), st = SHEENTINT(s);
+    value = (1.0f - st) + st * TINT(s);
+    value = value * (fh * SHEEN(s) * (1.0f - METALLIC(s)));
+    return 1.0f / (2 * PI);
+}
+inline f4 weights_of(const ShadingData& s) {
+    const float M = METALLIC(s);
+    f4 w = {lerp(LUMINANCE(s), 0, M), lerp(SHEEN(s), 0, M), lerp(SPECULAR(s), 1, M), CLEARCOAT(s) * 0.25f};
+    return w * (1.0f / (w.x + w.y + w.z + w.w));
+}
+f3 SampleBSDF(const ShadingData& s, f3 iN, const f3 N, const f3 iT, const f3 wow, const float distance, const float r0, const float r1,
+              const float r2, f3& wiw, float& pdf, bool& specular) {
+    const float flip = (dot(wow, N) < 0) ? -1.0f : 1.0f;
+    iN = iN * flip;
+    const f3 B = normalize(cross(iN, iT)), T = normalize(cross(iN, B));
+    const float TR = TRANSMISSION(s);
+    if (r0 < TR) {
+        specular = true;
+        const float r3 = r0 / TR;
+        const f3 wol = w2t(wow, iN, T, B);
+        const float eta = flip < 0 ? (1 / ETA(s)) : ETA(s);
+        if (eta == 1) return mk3(0);
+        const f3 beer = mk3(lm_expf(-s.transmittance.x * distance * 2.0f), lm_expf(-s.transmittance.y * distance * 2.0f),
+                            lm_expf(-s.transmittance.z * distance * 2.0f));
+        float ax, ay;
+        alpha_from_roughness(ROUGHNESS(s), ANISOTROPIC(s), ax, ay);
+        const f3 m = ggx_sample(wol, r1, r3, ax, ay);
+        const float rcpEta = 1 / eta, cwm = clampv(dot(wol, m), -1.0f, 1.0f);
+        float ct, jac;
+        const float F = fresnel_reflectance(cwm, eta, ct);
+        f3 wil, ret;
+        if (r2 < F) {
+            wil = reflect(wol * -1.0f, m);
+            if (wil.z * wol.z <= 0) return mk3(0);
+            ret = eval_reflection(s.color, wol, wil, m, ax, ay, F);
+            pdf = F, jac = reflection_jacobian(cwm);
+        } else {
+            wil = refracted_direction(wol, m, cwm, ct, eta);
+            if (wil.z * wol.z > 0) return mk3(0);
+            ret = eval_refraction(rcpEta, s.color, wol, wil, m, ax, ay, 1 - F);
+            pdf = 1 - F, jac = refraction_jacobian(wol, wil, m, rcpEta);
+        }
+        pdf *= jac * ggx_pdf(wol, m, ax, ay);
+        if (pdf > 1.0e-6f) wiw = t2w(wil, iN, T, B);
+        return ret * beer;
+    }
+    const float r3 = (r0 - TR) / (1 - TR);
+    f4 w = weights_of(s);
+    const f4 cdf = {w.x, w.x + w.y, w.x + w.y + w.z, 0};
+    float probability, cpdf = 0;
+    f3 contrib = mk3(0), value = mk3(0);
+    if (r3 < cdf.y) {
+        const float r2b = r3 / cdf.y;
+        wiw = cos_sample(r2b, r1, iN, T, B);
+        const f3 m = normalize(wiw + wow);
+        if (r3 < cdf.x) cpdf = evaluate_diffuse(s, iN, wow, wiw, m, value), probability = w.x * cpdf, w.x = 0;
+        else cpdf = evaluate_sheen(s, wiw, m, value), probability = w.y * cpdf, w.y = 0;
+    } else {
+        const f3 wol = w2t(wow, iN, T, B);
+        f3 wil = mk3(0);
+        if (r3 < cdf.z) {
+            const float r2b = (r3 - cdf.y) / (cdf.z - cdf.y);
+            float ax, ay;
+            alpha_from_roughness(ROUGHNESS(s), ANISOTROPIC(s), ax, ay);
+            sample_mf<false>(s, r2b, r1, ax, ay, wol, wil, cpdf, value);
+            probability = w.z * cpdf, w.z = 0;
+        } else {
+            const float r2b = (r3 - cdf.z) / (1 - cdf.z), a = clearcoat_roughness(s);
+            sample_mf<true>(s, r2b, r1, a, a, wol, wil, cpdf, value);
+            probability = w.w * cpdf, w.w = 0;
+        }
+        value = value * (1.0f / fabsf(4.0f * wol.z * wil.z));
+        wiw = t2w(wil, iN, T, B);
+    }
+    if (w.x + w.y > 0) {
+        const f3 m = normalize(wiw + wow);
+        if (w.x > 0) probability += w.x * evaluate_diffuse(s, iN, wow, wiw, m, contrib), value = value + contrib;
+        if (w.y > 0) probability += w.y * evaluate_sheen(s, wiw, m, contrib), value = value + contrib;
+    }
+    if (w.z + w.w > 0) {
+        const f3 wol = w2t(wow, iN, T, B), wil = w2t(wiw, iN, T, B), m = normalize(wol + wil);
+        if (w.z > 0) {
+            float ax, ay;
+            alpha_from_roughness(ROUGHNESS(s), ANISOTROPIC(s), ax, ay);
+            probability += w.z * evaluate_mf<false>(s, ax, ay, wol, wil, m, contrib);
+            value = value + contrib;
+        }
+        if (w.w > 0) {
+            const float a = clearcoat_roughness(s);
+            probability += w.w * evaluate_mf<true>(s, a, a, wol, wil, m, contrib);
+            value = value + contrib;
+        }
+    }
+    pdf = probability > 1.0e-6f ? probability : 0;
+    return value;
+}
+f3 EvaluateBSDF(const ShadingData& s, const f3 iN, const f3 iT, const f3 wow, const f3 wiw, float& pdf) {
+    if (TRANSMISSION(s) > 0.5f) {
+        const f3 B = normalize(cross(iN, iT)), T = normalize(cross(iN, B));
+        const f3 wol = w2t(wow, iN, T, B), wil = w2t(wiw, iN, T, B);
+        const float eta = wol.z > 0 ? ETA(s) : (1.0f / ETA(s));
+        if (eta == 1) { pdf = 0; return mk3(0); }
+        float ax, ay, jac;
+        alpha_from_roughness(ROUGHNESS(s), ANISOTROPIC(s), ax, ay);
+        f3 ret, m;
+        float ct;
+        if (wil.z * wol.z >= 0) {
+            m = half_reflection(wol, wil);
+            const float cwm = dot(wol, m), F = fresnel_reflectance(cwm, 1 / eta, ct);
+            ret = eval_reflection(s.color, wol, wil, m, ax, ay, F);
+            pdf = choose_reflection(F), jac = reflection_jacobian(cwm);
+        } else {
+            m = half_refraction(wol, wil, eta);
+            const float cwm = dot(wol, m), F = fresnel_reflectance(cwm, 1 / eta, ct);
+            ret = eval_refraction(eta, s.color, wol, wil, m, ax, ay, 1 - F);
+            pdf = 1 - choose_reflection(F), jac = refraction_jacobian(wol, wil, m, eta);
+        }
+        pdf *= jac * ggx_pdf(wol, m, ax, ay);
+        return ret;
+    }
+    if (ROUGHNESS(s) <= 0.001f) { pdf = 0; return mk3(0); }
+    const f3 B = normalize(cross(iN, iT)), T = normalize(cross(iN, B));
+    const f4 w = weights_of(s);
+    pdf = 0;
+    f3 value = mk3(0);
+    if (w.x + w.y > 0) {
+        const f3 m = normalize(wiw + wow);
+        if (w.x > 0) pdf += w.x * evaluate_diffuse(s, iN, wow, wiw, m, value);
+        if (w.y > 0) pdf += w.y * evaluate_sheen(s, wiw, m, value);   /* overwrites the diffuse value, as disney.h does */
+    }
+    if (w.z + w.w > 0) {
+        const f3 wol = w2t(wow, iN, T, B), wil = w2t(wiw, iN, T, B), m = normalize(wol + wil);
+        if (w.z > 0) {
+            float ax, ay;
+            alpha_from_roughness(ROUGHNESS(s), ANISOTROPIC(s), ax, ay);
+            f3 c = mk3(0);
+            const float sp = evaluate_mf<false>(s, ax, ay, wol, wil, m, c);
+            if (sp > 0) pdf += w.z * sp, value = value + c;
+        }
+        if (w.w > 0) {
+            const float a = clearcoat_roughness(s);
+            f3 c = mk3(0);
+            const float cp = evaluate_mf<true>(s, a, a, wol, wil, m, c);
+            if (cp > 0) pdf += w.w * cp, value = value + c;
+        }
+    }
+    return value;
+}
+}  // namespace dis
 
 /* ------------------------------------------------------------------------------------------------------
  * lights: lights_shared.h:37-105, 225-313 (ISLIGHTS importance selection over at most 64 lights)
@@ -1211,7 +1587,6 @@ inline f3 fmin3(f3 a, float b) { return mk3(fminr(a.x, b), fminr(a.y, b), fminr(
 inline f3 fmax3(float a, f3 b) { return mk3(fmaxr(a, b.x), fmaxr(a, b.y), fmaxr(a, b.z)); }
 inline float clampf(float f, float a, float b) { return fmaxr(a, fminr(f, b)); }
 inline f3 clamp3(f3 v, f3 a, f3 b) { return mk3(clampf(v.x, a.x, b.x), clampf(v.y, a.y, b.y), clampf(v.z, a.z, b.z)); }
-inline f3 operator+(f3 a, float b) { return {a.x + b, a.y + b, a.z + b}; }
 
 inline float Luminance(const f3 rgb) { return 0.299f * fminr(rgb.x, 10.0f) + 0.587f * fminr(rgb.y, 10.0f) + 0.114f * fminr(rgb.z, 10.0f); }
 inline f3 RGBToYCoCg(const f3 RGB) {
@@ -1789,7 +2164,8 @@ void trace_path_mis(const Frame& F, const int flavor, const uint pathIdx, const 
         ShadingData sd;
         f3 N, iN, fN, T;
         const f3 I = O + HIT_T * D;
-        GetShadingData(s, D, HIT_U, HIT_V, F.view.spreadAngle * HIT_T, tri, hit.inst, sd, N, iN, fN, T);
+        const bool disney = (p.flags & LH2G_RP_DISNEY) != 0;   /* kernels/bsdf.h's default branch */
+        GetShadingData(s, D, HIT_U, HIT_V, F.view.spreadAngle * HIT_T, tri, hit.inst, sd, N, iN, fN, T, disney);
         if (firstHitToBeStored) store4(feat, sd.color.x, sd.color.y, sd.color.z, bitsf(PackNormal2(iN)));
         if (sd.flags & 1) {   /* alpha: the ray continues behind the surface */
             capSeed(0);
@@ -1849,7 +2225,8 @@ void trace_path_mis(const Frame& F, const int flavor, const uint pathIdx, const 
             const float NdotL = dot(L, fN * faceDir);
             if (NdotL > 0 && lightPdf > 0) {
                 float lbsdfPdf;
-                const f3 sampledBSDF = EvaluateBSDF(sd, fN, L, lbsdfPdf) * ROUGHNESS(sd);
+                /* lambert.h's BSDF_HAS_PURE_SPECULARS scales the value by ROUGHNESS (pathtracer.h:194-198) */
+                const f3 sampledBSDF = disney ? dis::EvaluateBSDF(sd, fN, T, D * -1.0f, L, lbsdfPdf) : EvaluateBSDF(sd, fN, L, lbsdfPdf) * ROUGHNESS(sd);
                 if (lbsdfPdf > 0) {
                     f3 contribution = throughput * sampledBSDF * lightColor * (NdotL / (pickProb * lightPdf + lbsdfPdf));
                     fix_nan(contribution);
@@ -1867,12 +2244,12 @@ void trace_path_mis(const Frame& F, const int flavor, const uint pathIdx, const 
         }
         /* one diffuse bounce at most (ENOUGH_BOUNCES = S_BOUNCED), or the maximum path length */
         if ((FLAGS & S_BOUNCED) || pathLength == p.maxDepth) { capSeed(seed); return; }
-        f3 R;
-        float newBsdfPdf;
+        f3 R = mk3(0);
+        float newBsdfPdf = 0.0f;   /* the Disney sampler leaves it unset on its early exits: the path ends there */
         bool specular = false;
-        const float r5 = RandomFloat(seed);   /* the r5 argument of lambert.h's SampleBSDF: drawn, not used */
-        (void)r5;
-        const f3 bsdf = SampleBSDF(sd, fN, N, D * -1.0f, HIT_T, r4.z, r4.w, R, newBsdfPdf, specular);
+        const float r5 = RandomFloat(seed);   /* lambert.h's SampleBSDF draws it and does not use it */
+        const f3 bsdf = disney ? dis::SampleBSDF(sd, fN, N, T, D * -1.0f, HIT_T, r4.z, r4.w, r5, R, newBsdfPdf, specular)
+                               : SampleBSDF(sd, fN, N, D * -1.0f, HIT_T, r4.z, r4.w, R, newBsdfPdf, specular);
         if (newBsdfPdf < EPSILON || std::isnan(newBsdfPdf)) { capSeed(seed); return; }
         if (specular) FLAGS |= S_SPECULAR;
         const float pr = ((FLAGS & S_SPECULAR) || (FLAGS & S_BOUNCED) == 0) ? 1.0f : SurvivalProbability(bsdf);
@@ -2710,6 +3087,8 @@ void lh2o_diffuse_cos(float r0, float r1, float* o) { const f3 v = DiffuseReflec
 void lh2o_tangent2world(const float* v, const float* n, float* o) { const f3 r = Tangent2World(ld3(v), ld3(n)); o[0] = r.x, o[1] = r.y, o[2] = r.z; }
 void lh2o_consistent_normal(const float* d, const float* in, float alpha, float* o) { const f3 r = ConsistentNormal(ld3(d), ld3(in), alpha); o[0] = r.x, o[1] = r.y, o[2] = r.z; }
 void lh2o_sincos(float x, float* s, float* c) { lm_sincos(x, s, c); }
+float lh2o_logf(float x) { return lm_logf(x); }
+float lh2o_powf(float x, float y) { return lm_powf(x, y); }
 float lh2o_expf(float x) { return lm_expf(x); }
 float lh2o_log2f(float x) { return lm_log2f(x); }
 float lh2o_atan2f(float y, float x) { return lm_atan2f(y, x); }

@@ -146,6 +146,8 @@ void lh2o_consistent_normal(const float* d3, const float* in3, float alpha, floa
 void lh2o_sincos(float x, float* s, float* c);
 float lh2o_expf(float x);
 float lh2o_log2f(float x);
+float lh2o_logf(float x);
+float lh2o_powf(float x, float y);
 float lh2o_atan2f(float y, float x);
 float lh2o_acosf(float x);
 uint16_t lh2o_float2half(float f);

@@ -15,7 +15,23 @@
 #include "common_classes.h"
 #include "common_functions.h"
 
-namespace refo7 {
+/* Built twice: as is with the Lambert BSDF (entry points ref_o7_*), and with -DREF_O7_DISNEY with the Disney BSDF
+ * (the default branch of the core's kernels/bsdf.h: lib/sharedBSDFs/ggxmdf.h, frosted.h, disney.h; entry points
+ * ref_o7d_*). The Disney build reads copies the Makefile makes in $(OUT)/inc_o7d: the three BSDF headers with their
+ * CUDA branches selected (the samplers' sincosf form and the adjoint parameter), and pathtracer.h with its unset
+ * newBsdfPdf (pathtracer.h:219) zero-initialised, so that a sampler exit that leaves it unset ends the path on the
+ * host as the restatement does. logf and powf go to the oracle's own functions, as the other transcendentals do. */
+#ifdef REF_O7_DISNEY
+#define REF_NS refo7d
+#define O7(name) ref_o7d_##name
+extern "C" float lh2o_logf(float x);
+extern "C" float lh2o_powf(float x, float y);
+#else
+#define REF_NS refo7
+#define O7(name) ref_o7_##name
+#endif
+
+namespace REF_NS {
 #include "ref_globals.h"
 /* CLAMPINTENSITY of the core's core_settings.h (CLAMPFIREFLIES on): scales a contribution whose largest channel
  * exceeds clampValue down to it, w untouched */
@@ -27,15 +43,25 @@ namespace refo7 {
             contribution.x *= m_, contribution.y *= m_, contribution.z *= m_;                                                  \
         }                                                                                                                      \
     }
+#ifdef REF_O7_DISNEY
+using std::abs;
+#define logf(x) lh2o_logf(x)
+#define powf(x, y) lh2o_powf(x, y)
+#include "inc_o7d/ggxmdf.h"
+#include "inc_o7d/frosted.h"
+#include "inc_o7d/disney.h"
+#include "inc_o7d/pathtracer.h"
+#else
 #include "lambert.h"
 #include "inc_o7/pathtracer.h"
+#endif
 /* the fields of Params (lib/rendercore_optix7/core_settings.h:113-133) that the ray-generation helpers read */
 struct RefParams { float4 posLensSize; float3 right, up, p1; float geometryEpsilon, distortion; int3 scrsize; int pass, phase, shift; uint* blueNoise; };
 static RefParams params;
 #include "inc_o7/optix_raygen.h"
-}  // namespace refo7
+}  // namespace REF_NS
 
-using namespace refo7;
+using namespace REF_NS;
 
 static void grid1(long long n, void (*body)(long long, void*), void* ctx) {
     blockDim.x = blockDim.y = blockDim.z = 1;
@@ -48,7 +74,7 @@ extern "C" {
 
 /* scene: all pointers stay owned by the caller; sky4 holds the sky and then its 64x scaled-down copy;
  * blueNoise: 5 * 65536 entries plus padding (the expanded tables of rendercore.cpp:247-256) */
-void ref_o7_set_scene(void* instDescs, void* mats, void* tri, int ntri, void* pt, int npt, void* spot, int nspot, void* dir, int ndir,
+void O7(set_scene)(void* instDescs, void* mats, void* tri, int ntri, void* pt, int npt, void* spot, int nspot, void* dir, int ndir,
                       uint32_t* texels, float geoEps, float clampVal, int maxPathLength, float* sky4, int skyW, int skyH, uint32_t* blueNoise) {
     instanceDescriptors = (CoreInstanceDesc*)instDescs;
     materials = (CUDAMaterial4*)mats;
@@ -63,18 +89,18 @@ void ref_o7_set_scene(void* instDescs, void* mats, void* tri, int ntri, void* pt
 }
 
 /* InitCountersForExtend / InitCountersSubsequent (lib/rendercore_optix7/kernels/.cuda.cu:191-212) */
-void ref_o7_init_counters(int pathCount) {
+void O7(init_counters)(int pathCount) {
     memset(counters, 0, sizeof(Counters));
     counters->activePaths = (uint)pathCount, counters->totalExtensionRays = (uint)pathCount;
 }
-void ref_o7_next_counters() {
+void O7(next_counters)() {
     counters->totalExtensionRays += counters->extensionRays;
     counters->activePaths = counters->extensionRays;
     counters->extended = counters->shaded = 0;
     counters->extensionRays = 0;
 }
-void ref_o7_counters(uint32_t* out2) { out2[0] = counters->extensionRays, out2[1] = counters->shadowRays; }
-void ref_o7_set_shadow_count(uint32_t n) { counters->shadowRays = n; }
+void O7(counters)(uint32_t* out2) { out2[0] = counters->extensionRays, out2[1] = counters->shadowRays; }
+void O7(set_shadow_count)(uint32_t n) { counters->shadowRays = n; }
 
 /* the first part of setupPrimaryRay (optix/.optix.cu:112-121): the eye ray of every path and its path state
  * (the optixTrace that follows it there is the caller's) */
@@ -90,7 +116,7 @@ static void gen_body(long long i, void* c) {
     a->ps[pathIdx] = make_float4(O, __uint_as_float((pathIdx << 6) + 1));
     a->ps[pathIdx + a->stride] = make_float4(D, 0);
 }
-void ref_o7_generate(float* pathStates, int w, int h, int spp, int pass, int shift, const float* pos, float aperture, const float* right,
+void O7(generate)(float* pathStates, int w, int h, int spp, int pass, int shift, const float* pos, float aperture, const float* right,
                      const float* up, const float* p1, float distortion) {
     params.posLensSize = make_float4(pos[0], pos[1], pos[2], aperture);
     params.right = make_float3(right[0], right[1], right[2]), params.up = make_float3(up[0], up[1], up[2]);
@@ -108,7 +134,7 @@ static void shade_body(long long, void* c) {
     ShadeArgs* a = (ShadeArgs*)c;
     shadeKernel(a->acc, a->stride, a->ps, a->hits, a->conn, a->R0, a->shift, params.blueNoise, a->pass, -1, a->pathLength, a->w, a->h, a->spread, a->n);
 }
-void ref_o7_shade(int pathCount, float* accumulator, float* pathStates, float* hits, float* connections, uint32_t R0, uint32_t shift, int pass,
+void O7(shade)(int pathCount, float* accumulator, float* pathStates, float* hits, float* connections, uint32_t R0, uint32_t shift, int pass,
                   int pathLength, int w, int h, int spp, float spreadAngle, int nee) {
     ShadeArgs a;
     a.acc = (float4*)accumulator, a.stride = (uint)(w * h * spp), a.ps = (float4*)pathStates, a.hits = (float4*)hits;
@@ -119,7 +145,7 @@ void ref_o7_shade(int pathCount, float* accumulator, float* pathStates, float* h
 
 /* the part of generateShadowRay (optix/.optix.cu:142-154) after optixTrace: unoccluded connections add their
  * contribution and 1 in w to the pixel */
-void ref_o7_finalize_connections(int count, float* accumulator, const float* connections, const uint32_t* occluded, int stride) {
+void O7(finalize_connections)(int count, float* accumulator, const float* connections, const uint32_t* occluded, int stride) {
     const float4* cd = (const float4*)connections;
     float4* acc = (float4*)accumulator;
     for (int i = 0; i < count; i++) {
@@ -131,7 +157,7 @@ void ref_o7_finalize_connections(int count, float* accumulator, const float* con
 }
 
 /* blueNoiseSampler4 of tools_shared.h:324-337 (the shading kernels' copy) */
-void ref_o7_bluenoise4(const uint32_t* bn, int x, int y, int sampleIndex, int sampleDimension, float* out4) {
+void O7(bluenoise4)(const uint32_t* bn, int x, int y, int sampleIndex, int sampleDimension, float* out4) {
     const float4 r = blueNoiseSampler4(bn, x, y, sampleIndex, sampleDimension);
     out4[0] = r.x, out4[1] = r.y, out4[2] = r.z, out4[3] = r.w;
 }

@@ -153,3 +153,76 @@ def test_render_api_estimators(core_lib, oracle_lib):
     stats = core.GetCoreStats()
     assert stats["primaryRayCount"] >= W * H
     core.close()
+
+
+# ---- the Disney BSDF (LH2G_RP_DISNEY), pinned in the oracle against the reference kernel built with disney.h ----
+@pytest.fixture(scope="module")
+def disney_pair(core_lib, oracle_lib):
+    from tests.golden.make_golden_disney import disney_scene
+    sc = disney_scene()
+    core = RenderCore()
+    core.set_scene(sc)
+    o = oracle_lib.Oracle()
+    o.set_scene(sc)
+    yield core, o
+    core.close()
+
+
+@pytest.mark.parametrize("W,H,spp,depth,st,tail", [(64, 48, 1, 5, 0, 5), (40, 32, 2, 6, 3, 0), (48, 40, 1, 8, 70, 2)])
+def test_disney_frames(disney_pair, W, H, spp, depth, st, tail):
+    from lighthouse2_gb300.core import RP_DISNEY
+    core, o = disney_pair
+    core.SetTarget(W, H, spp)
+    core.Setting("waveTail", tail)
+    try:
+        p = make_params(W, H, spp, max_depth=depth, samples_taken=st, camera_r0=camera_r0(st), flags=RP_NEE | RP_OPTIX7 | RP_DISNEY,
+                        shift=0x91331445 + st)
+        g = core.render_ex(S.cornell_view(W, H), p, capture=True)
+        c = o.render(S.cornell_view(W, H), p, capture=True)
+        _compare(g, c, core.read_accumulator(), c["accum"])
+    finally:
+        core.Setting("waveTail", 5)
+
+
+def test_disney_adaptive_and_render_api(disney_pair, oracle_lib):
+    """Adaptive frames with the Disney BSDF, and Render with the settings "adaptive" 1 / "estimator" 1 and "bsdf" 1."""
+    from lighthouse2_gb300.core import RP_DISNEY
+    from tests.golden.make_golden_mis import adaptive_params
+    core, o = disney_pair
+    W, H, spp, depth = 40, 32, 1, 5
+    core.SetTarget(W, H, spp)
+    core.set_adaptive_scale(30.0)
+    acc = np.zeros((W * H, 4), np.float32)
+    ds = 30.0
+    for k in range(2):
+        p = adaptive_params(W, H, spp, depth, k)
+        p["flags"] = int(p["flags"]) | RP_DISNEY
+        g = core.render_adaptive(S.cornell_view(W, H), p, accumulate=k > 0, capture=True)
+        c = o.render_adaptive(S.cornell_view(W, H), p, acc, ds, capture=True)
+        ds = c["dev_scale"]
+        assert g["dev_scale"] == np.float32(ds) and g["adaptive_paths"] == c["adaptive_paths"]
+        _compare(g, {"counters": c["counters"], "hits": c["hits"], "seeds": c["seeds"]}, core.read_accumulator(), acc)
+    # the plugin-level switch: estimator 1 + bsdf 1 renders the same frame as render_ex with the flags
+    core.Setting("maxDepth", depth)
+    core.Setting("estimator", 1)
+    core.Setting("bsdf", 1)
+    try:
+        core.Render(S.cornell_view(W, H), converge=1)
+        seeds = [0x12345678, 0x11331445]
+
+        def nxt(i):
+            x = seeds[i]
+            x ^= (x << 13) & 0xFFFFFFFF
+            x ^= x >> 17
+            x ^= (x << 5) & 0xFFFFFFFF
+            seeds[i] = x
+            return x
+        shift, r0 = nxt(1), nxt(0)
+        p = make_params(W, H, spp, max_depth=depth, samples_taken=0, camera_r0=r0, flags=RP_NEE | RP_OPTIX7 | RP_DISNEY, shift=shift)
+        ref = o.render(S.cornell_view(W, H), p)["accum"]
+        assert np.allclose(core.read_accumulator(), ref, rtol=1e-4, atol=1e-7)
+    finally:
+        core.Setting("estimator", 0)
+        core.Setting("bsdf", 0)
+    with pytest.raises(Exception):   # the Disney BSDF belongs to the OptiX 7 / adaptive estimators
+        core.render_ex(S.cornell_view(W, H), make_params(W, H, spp, max_depth=depth, flags=RP_NEE | RP_DISNEY))

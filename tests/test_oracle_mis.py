@@ -116,3 +116,64 @@ def test_live_adaptive_on_reference_tables(oracle_lib):
         assert np.array_equal(a["counters"], r["counters"]) and ds_o == ds_r and a["adaptive_paths"] == r["adaptive_paths"]
         assert np.array_equal(a["features"].view(np.uint32), r["features"].view(np.uint32))
         assert _close(acc_o, acc_r)
+
+
+# ---- the Disney BSDF (LH2G_RP_DISNEY): the OptiX 7 kernel built with lib/sharedBSDFs/disney.h ----
+DISNEY_GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "disney_vectors.npz")
+
+
+def test_disney_frames(oracle_lib):
+    """Frames of a room whose materials span the Disney parameters (metal with anisotropy, sheen, subsurface,
+    clearcoat, rough dielectric, tinted specular) against the reference kernel built with disney.h."""
+    from tests.golden import make_golden_disney as G
+    B = oracle_lib
+    gold = np.load(DISNEY_GOLD)
+    sc = G.disney_scene()
+    o = B.Oracle()
+    o.set_scene(sc)
+    for name, W, H, spp, D, st, shift in G.FRAMES:
+        p = B.make_params(W, H, spp, max_depth=D, samples_taken=st, camera_r0=B.camera_r0(st), flags=B.RP_NEE | B.RP_OPTIX7 | B.RP_DISNEY,
+                          shift=shift)
+        r = o.render(S.cornell_view(W, H), p)
+        assert np.array_equal(r["counters"], gold[name + "/counters"]), name
+        assert _close(r["accum"], gold[name + "/accum"]), name
+        lam = o.render(S.cornell_view(W, H), B.make_params(W, H, spp, max_depth=D, samples_taken=st, camera_r0=B.camera_r0(st),
+                                                            flags=B.RP_NEE | B.RP_OPTIX7, shift=shift))
+        assert not np.array_equal(lam["accum"], r["accum"])   # the BSDF matters on this scene
+
+
+def test_own_log_and_pow():
+    """The oracle's logf / powf (used by the GTR1 clearcoat distribution and sampler) against numpy in float64."""
+    import ctypes as Cc
+    from oracle import bind as B
+    L = Cc.CDLL(B.LIB)
+    L.lh2o_logf.restype, L.lh2o_logf.argtypes = Cc.c_float, [Cc.c_float]
+    L.lh2o_powf.restype, L.lh2o_powf.argtypes = Cc.c_float, [Cc.c_float, Cc.c_float]
+    rng = np.random.default_rng(4)
+    xs = np.concatenate([rng.uniform(1e-6, 1.0, 3000), 10.0 ** rng.uniform(-37, 37, 3000)]).astype(np.float32)
+    for x in xs:
+        ref = np.log(np.float64(x))
+        assert abs(L.lh2o_logf(float(x)) - ref) <= 2.5e-7 * max(abs(ref), 1e-3), x
+    a, b = rng.uniform(1e-6, 0.999, 3000).astype(np.float32), rng.uniform(0.0, 1.0, 3000).astype(np.float32)
+    for x, y in zip(a, b):
+        ref = np.float64(x) ** np.float64(y)
+        assert abs(L.lh2o_powf(float(x), float(y)) - ref) <= 1e-6 * ref, (x, y)
+    assert L.lh2o_powf(0.0, 0.5) == 0.0 and L.lh2o_powf(0.3, 0.0) == 1.0
+
+
+@live
+def test_live_disney_frames(oracle_lib):
+    B = oracle_lib
+    from tests.golden import make_golden_disney as G
+    ref = B.RefOptix7(disney=True)
+    sc = G.disney_scene()
+    o = B.Oracle()
+    o.set_scene(sc)
+    for W, H, spp, D, st in ((40, 32, 1, 5, 0), (32, 24, 2, 6, 66)):
+        p = B.make_params(W, H, spp, max_depth=D, samples_taken=st, camera_r0=B.camera_r0(st), flags=B.RP_NEE | B.RP_OPTIX7 | B.RP_DISNEY,
+                          shift=0x31337)
+        a = o.render(S.cornell_view(W, H), p)
+        r = ref.render(o, sc, S.cornell_view(W, H), p)
+        assert not r["flushed"]
+        assert np.array_equal(a["counters"], r["counters"])
+        assert _close(a["accum"], r["accum"])
