@@ -671,7 +671,7 @@ def nrc_leg(args, core, name, view, bounds, W, H):
     box = [[round(float(x), 3) for x in b] for b in bounds]
     out = {"workload": f"{name}, {W}x{H}, depth {MAX_DEPTH}, RR after depth {RR_START - 1}, NEE; reference {args.nrc_ref_spp} spp plain, "
                        f"FP64 sums ({ref_s:.0f} s); cache box {box}, Adam lr {args.nrc_lr}; trained over {args.nrc_warmup} frames "
-                       f"first, then online (1/32 of the cached paths, at most 65,536 per frame); relmse = mean of err^2 / (ref^2 + 0.01)",
+                       f"first, then online (1/16 of the cached paths, at most 65,536 per frame); relmse = mean of err^2 / (ref^2 + 0.01)",
            "plain_ms_per_frame": t_plain * 1e3, "cache_ms_per_frame": t_cache * 1e3,
            "cache_queries_per_frame": stats[-1][0], "train_samples_per_frame": stats[-1][1],
            "loss_first": float(np.mean([x[2] for x in stats[:5]])), "loss_last": float(np.mean([x[2] for x in stats[-5:]])), "equal_time": {}}
@@ -683,6 +683,25 @@ def nrc_leg(args, core, name, view, bounds, W, H):
                                                         "relmse_reduction": 1.0 - e_c["relmse"] / e_p["relmse"]}
     e_p, e_c = errors(image(plain, 16)), errors(image(cached, 16))
     out["equal_spp_16"] = {"plain": e_p, "cache": e_c, "rmse_reduction": 1.0 - e_c["rmse"] / e_p["rmse"]}
+    # where the plain estimator's error lives: the direct part (emission seen by the camera and light connected at the
+    # first vertex: the same estimator at depth 1), which the cache cannot touch (it replaces paths from their second
+    # diffuse-led vertex on), against the whole; both against references of args.nrc_ref_spp samples
+    def P1(k, spp=1):
+        return make_params(W, H, spp, max_depth=1, rr_start=RR_START, samples_taken=k, camera_r0=camera_r0(k), flags=RP_NEE | RP_DEPTH_W)
+    core.SetTarget(W, H, batch)
+    ref1 = np.zeros((W * H, 3), np.float64)
+    for k in range(args.nrc_ref_spp // batch):
+        p = P1(batch * k, batch)
+        p["cameraR0"] = (0x9E3779B9 * (k + 7)) & 0xFFFFFFFF
+        core.render_ex(view, p, accumulate=False, counters=False)
+        ref1 += core.read_accumulator()[:, :3]
+    ref1 /= float(args.nrc_ref_spp // batch * batch)
+    core.SetTarget(W, H, 1)
+    direct = lambda k: core.render_ex(view, P1(k), accumulate=k > 0, counters=False)
+    img1 = image(direct, 16)
+    mse_direct = float(np.mean((img1 - ref1) ** 2))
+    out["error_budget_16_frames"] = {"mse_all": e_p["rmse"] ** 2, "mse_direct": mse_direct, "direct_share": mse_direct / max(e_p["rmse"] ** 2, 1e-30),
+                                     "note": "direct = the depth-1 estimator (primary emission + one light connection); the cache acts on the rest"}
     cache.close()
     return out
 

@@ -71,14 +71,19 @@ __device__ void stage_weights(const __nv_bfloat16* __restrict__ W, unsigned char
     }
 }
 
-/* D[128 x N] = A[128 x K] * B[N x K]^T on the tensor core (thread 0 issues, then commits to mbar) */
-__device__ __forceinline__ void issue_gemm(uint32_t dTmem, uint32_t aAddr, uint32_t bAddr, int K, int N, uint64_t* mbar) {
+/* D[128 x N] (+)= A[128 x K] * B[N x K]^T on the tensor core, issued by the calling thread (no commit); with accumulate
+ * the first K step adds to D too */
+__device__ __forceinline__ void issue_mma(uint32_t dTmem, uint32_t aAddr, uint32_t bAddr, int K, int N, bool accumulate) {
     const uint32_t sbo = (uint32_t)K * 16u;
     const uint32_t idesc = tc::idesc_bf16_f32(TILE, N);
-    tc::fence_after_sync();
     for (int s = 0; s < K / 16; s++)
         tc::mma_bf16(dTmem, tc::smem_desc(aAddr + (uint32_t)s * 256u, 128u, sbo), tc::smem_desc(bAddr + (uint32_t)s * 256u, 128u, sbo), idesc,
-                     s > 0 ? 1u : 0u);
+                     (accumulate || s > 0) ? 1u : 0u);
+}
+/* D[128 x N] = A[128 x K] * B[N x K]^T on the tensor core (thread 0 issues, then commits to mbar) */
+__device__ __forceinline__ void issue_gemm(uint32_t dTmem, uint32_t aAddr, uint32_t bAddr, int K, int N, uint64_t* mbar) {
+    tc::fence_after_sync();
+    issue_mma(dTmem, aAddr, bAddr, K, N, false);
     tc::mma_commit(mbar);
 }
 
@@ -177,12 +182,38 @@ __global__ void __launch_bounds__(TILE) k_infer(const GridSpec G, const __half2*
  * layout) and gGrid, and the loss into *loss
  * ------------------------------------------------------------------------------------------------------- */
 constexpr uint32_t DELTA_BYTES = TILE * HID * 2;
-constexpr uint32_t TRAIN_SMEM = 2 * WEIGHT_BYTES + 5 * ACT_BYTES + DELTA_BYTES + SMEM_SLACK;
+constexpr uint32_t GRADT_BYTES = HID * TILE * 2;   /* a [64 x 128] bf16 tile: delta_j^T or act_j^T */
+constexpr uint32_t TRAIN_SMEM = 2 * WEIGHT_BYTES + 5 * ACT_BYTES + DELTA_BYTES + 2 * GRADT_BYTES + SMEM_SLACK;
+/* TMEM: columns 0..63 the forward / backward products, 64 (j + 1) .. 64 (j + 2) - 1 the sums of dW_j (j = 0..3) */
+constexpr uint32_t TRAIN_TMEM_COLS = 512;
 
 __device__ __forceinline__ void load_row8(const unsigned char* tile, uint32_t r, uint32_t col8, uint32_t K, float* v) {
     const uint4 u = *reinterpret_cast<const uint4*>(tile + tc::kmajor_offset(r, col8, K));
     v[0] = bf16_lo(u.x), v[1] = bf16_hi(u.x), v[2] = bf16_lo(u.y), v[3] = bf16_hi(u.y);
     v[4] = bf16_lo(u.z), v[5] = bf16_hi(u.z), v[6] = bf16_lo(u.w), v[7] = bf16_hi(u.w);
+}
+
+/* column b of a [64 x TILE] K-major tile (K = TILE): 64 bf16 values, element (n, b) */
+__device__ __forceinline__ void store_col64(unsigned char* tile, uint32_t b, const float* v) {
+#pragma unroll
+    for (int n = 0; n < 64; n += 2) {
+        const uint32_t u = pack_bf16(v[n], v[n + 1]);
+        *reinterpret_cast<uint16_t*>(tile + tc::kmajor_offset((uint32_t)n, b, TILE)) = (uint16_t)(u & 0xffffu);
+        *reinterpret_cast<uint16_t*>(tile + tc::kmajor_offset((uint32_t)n + 1u, b, TILE)) = (uint16_t)(u >> 16);
+    }
+}
+/* row r of a K = 64 tile, bit for bit, into column r of a [64 x TILE] K-major tile */
+__device__ __forceinline__ void transpose_row64(const unsigned char* src, unsigned char* dst, uint32_t r) {
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        const uint4 u = *reinterpret_cast<const uint4*>(src + tc::kmajor_offset(r, 8u * c, IN));
+        const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            *reinterpret_cast<uint16_t*>(dst + tc::kmajor_offset(8u * c + 2u * i, r, TILE)) = (uint16_t)(w[i] & 0xffffu);
+            *reinterpret_cast<uint16_t*>(dst + tc::kmajor_offset(8u * c + 2u * i + 1u, r, TILE)) = (uint16_t)(w[i] >> 16);
+        }
+    }
 }
 
 __global__ void __launch_bounds__(TILE, 1) k_train(const GridSpec G, const __half2* __restrict__ grid, const __nv_bfloat16* __restrict__ W,
@@ -196,8 +227,14 @@ __global__ void __launch_bounds__(TILE, 1) k_train(const GridSpec G, const __hal
     unsigned char* Wt = Ws + WEIGHT_BYTES;
     unsigned char* act = Wt + WEIGHT_BYTES;          /* act_0 (inputs) .. act_4, [128 x 64] each */
     unsigned char* delta = act + 5 * ACT_BYTES;      /* delta_j, [128 x rows_j] */
+    /* the weight-gradient product of hidden layer j, dW_j = delta_j^T act_j (sum over the tile's rows), on the tensor
+     * core: A = delta_j^T [64 x 128] (K = the tile's rows) in deltaT, B = act_j^T [64 x 128] in actT. The MMA is
+     * M = 128: its rows 64..127 read the 16 KB after deltaT (actT) and land in TMEM lanes 64..127, which are never
+     * read. dW_j accumulates over the CTA's tiles in TMEM columns 64 (j + 1) .. 64 (j + 2), lanes 0..63. */
+    unsigned char* deltaT = delta + DELTA_BYTES;
+    unsigned char* actT = deltaT + GRADT_BYTES;
     if (threadIdx.x < 32) {
-        tc::tmem_alloc(&sh.tmem, 64);
+        tc::tmem_alloc(&sh.tmem, TRAIN_TMEM_COLS);
         tc::tmem_relinquish();
     }
     if (threadIdx.x == 0) {
@@ -210,16 +247,14 @@ __global__ void __launch_bounds__(TILE, 1) k_train(const GridSpec G, const __hal
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = sh.tmem, wAddr = tc::smem_u32(Ws), wtAddr = tc::smem_u32(Wt), actAddr = tc::smem_u32(act), dAddr = tc::smem_u32(delta);
+    const uint32_t dtAddr = tc::smem_u32(deltaT), atAddr = tc::smem_u32(actT);
     const uint32_t r = threadIdx.x;
-    /* weight-gradient ownership: hidden layers rows n0 .. n0 + 3, columns k0 .. k0 + 7; output layer row n4 */
-    const uint32_t n0 = (r >> 3) * 4, k0 = (r & 7) * 8, n4 = r >> 3;
-    float gw[4][32], gw4[8];
-#pragma unroll
-    for (int l = 0; l < 4; l++)
-#pragma unroll
-        for (int i = 0; i < 32; i++) gw[l][i] = 0.0f;
+    /* the output layer's gradient (16 x 64) on the FP32 pipes: row n4, columns k0 .. k0 + 7 of this thread */
+    const uint32_t k0 = (r & 7) * 8, n4 = r >> 3;
+    float gw4[8];
 #pragma unroll
     for (int i = 0; i < 8; i++) gw4[i] = 0.0f;
+    bool anyTile = false;   /* the TMEM gradient columns hold sums once the first tile has run */
     float lossSum = 0.0f;
     const float invCount = 1.0f / (3.0f * (float)n);
     uint32_t phase = 0;
@@ -278,28 +313,27 @@ __global__ void __launch_bounds__(TILE, 1) k_train(const GridSpec G, const __hal
 #pragma unroll
         for (int j = LAYERS - 1; j >= 0; j--) {
             const int Nj = layer_rows(j);
+            const unsigned char* aj = act + (uint32_t)j * ACT_BYTES;
+            if (j < LAYERS - 1) transpose_row64(aj, actT, r);   /* act_j^T, the weight-gradient product's B */
             tc::fence_proxy_async();
             tc::fence_before_sync();
             __syncthreads();
-            /* dL/d act_j = delta_j * W_j on the tensor core ... */
-            if (r == 0) issue_gemm(tmem, dAddr, wtAddr + layer_offset(j), Nj, HID, &sh.mbar);
-            /* ... while every thread adds delta_j^T act_j over the tile's rows to its share of dW_j */
-            const unsigned char* aj = act + (uint32_t)j * ACT_BYTES;
+            /* dL/d act_j = delta_j * W_j and, for the hidden layers, dW_j += delta_j^T act_j, on the tensor core ... */
+            if (r == 0) {
+                tc::fence_after_sync();
+                issue_mma(tmem, dAddr, wtAddr + layer_offset(j), Nj, HID, false);
+                if (j < LAYERS - 1) issue_mma(tmem + 64u * (uint32_t)(j + 1), dtAddr, atAddr, TILE, HID, anyTile);
+                tc::mma_commit(&sh.mbar);
+            }
+            /* ... while the output layer's gradient (16 rows) accumulates on the FP32 pipes */
+            if (j == LAYERS - 1) {
 #pragma unroll 2
-            for (uint32_t b = 0; b < (uint32_t)TILE; b++) {
-                float a8[8];
-                load_row8(aj, b, k0, IN, a8);
-                if (j == LAYERS - 1) {
+                for (uint32_t b = 0; b < (uint32_t)TILE; b++) {
+                    float a8[8];
+                    load_row8(aj, b, k0, IN, a8);
                     const float d = __uint_as_float((uint32_t)*reinterpret_cast<const uint16_t*>(delta + tc::kmajor_offset(b, n4, OUTP)) << 16);
 #pragma unroll
                     for (int i = 0; i < 8; i++) gw4[i] += d * a8[i];
-                } else {
-                    const uint2 du = *reinterpret_cast<const uint2*>(delta + tc::kmajor_offset(b, n0, HID));
-                    const float d4[4] = {bf16_lo(du.x), bf16_hi(du.x), bf16_lo(du.y), bf16_hi(du.y)};
-#pragma unroll
-                    for (int a = 0; a < 4; a++)
-#pragma unroll
-                        for (int i = 0; i < 8; i++) gw[j < 4 ? j : 0][8 * a + i] += d4[a] * a8[i];
                 }
             }
             if (!tc::mbar_wait(&sh.mbar, phase, WAIT_LIMIT)) sh.failed = 1;
@@ -319,6 +353,7 @@ __global__ void __launch_bounds__(TILE, 1) k_train(const GridSpec G, const __hal
                     for (int i = 0; i < 8; i++) g[8 * c + i] = m[i] > 0.0f ? g[8 * c + i] : 0.0f;
                 }
                 store_row64(delta, r, g);
+                store_col64(deltaT, r, g);   /* delta_{j-1}^T, the next weight-gradient product's A */
             } else if (valid) {
                 /* dL/d inputs: the hash-grid features receive it through the trilinear weights */
                 const float3 p = unit_position(G, qq[0]);
@@ -335,15 +370,18 @@ __global__ void __launch_bounds__(TILE, 1) k_train(const GridSpec G, const __hal
                 }
             }
         }
+        anyTile = true;
         if (__syncthreads_or(sh.failed)) break;
     }
-    /* this CTA's gradient shares and loss */
+    /* this CTA's gradient sums and loss: the hidden layers' from TMEM (lanes 0..63 = rows of dW_j, warps 0 and 1) */
+    tc::fence_after_sync();
+    if (anyTile && r < (uint32_t)HID)
+        for (int l = 0; l < 4; l++) {
+            float g[HID];
+            read_row(tmem + 64u * (uint32_t)(l + 1), 4, g);
 #pragma unroll
-    for (int l = 0; l < 4; l++)
-#pragma unroll
-        for (int a = 0; a < 4; a++)
-#pragma unroll
-            for (int i = 0; i < 8; i++) atomicAdd(gW + l * HID * IN + (n0 + a) * IN + k0 + i, gw[l][8 * a + i]);
+            for (int k = 0; k < IN; k++) atomicAdd(gW + l * HID * IN + r * IN + k, g[k]);
+        }
     if (n4 < (uint32_t)OUT)
 #pragma unroll
         for (int i = 0; i < 8; i++) atomicAdd(gW + 4 * HID * IN + n4 * IN + k0 + i, gw4[i]);
@@ -353,7 +391,7 @@ __global__ void __launch_bounds__(TILE, 1) k_train(const GridSpec G, const __hal
     __syncthreads();
     if (r == 0 && sh.failed) atomicOr(errors, ERR_TIMEOUT);
     tc::fence_after_sync();
-    if (r < 32) tc::tmem_dealloc(tmem, 64);
+    if (r < 32) tc::tmem_dealloc(tmem, TRAIN_TMEM_COLS);
 }
 
 /* ---------------------------------------------------------------------------------------------------------

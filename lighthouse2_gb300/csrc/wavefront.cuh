@@ -14,9 +14,9 @@ constexpr int WAVE_BLOCK = 128;
 static_assert(WAVE_BLOCK == LH2G_TRAV_BLOCK, "traversal kernels run LH2G_TRAV_BLOCK threads per block");
 constexpr int NRC_DEPTH = 2;   /* first path length at which radiance-cache frames query the cache */
 #ifndef LH2G_NRC_TRAIN_SHIFT
-#define LH2G_NRC_TRAIN_SHIFT 5
+#define LH2G_NRC_TRAIN_SHIFT 4
 #endif
-/* 1 in 2^LH2G_NRC_TRAIN_SHIFT cached paths trace on and train the cache (about 3 %) */
+/* 1 in 2^LH2G_NRC_TRAIN_SHIFT cached paths trace on and train the cache (1 in 16: the survey's budget) */
 constexpr uint32_t NRC_TRAIN_MASK = (1u << LH2G_NRC_TRAIN_SHIFT) - 1u;
 constexpr uint32_t S_CACHED = 8;   /* radiance-cache frames: the path has recorded its cache vertex */
 

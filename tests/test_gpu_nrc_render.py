@@ -1,7 +1,7 @@
 """Radiance-cache frames (lh2g_render_nrc) against the plain estimator, both measured against a converged plain render.
 
 The plain estimator (1 spp per frame, accumulated) and the cache estimator (paths end into the cache at their first
-diffuse-led vertex from path length 2 on, 1 in 32 trace on and train it online) render the Cornell scene at
+diffuse-led vertex from path length 2 on, 1 in 16 trace on and train it online) render the Cornell scene at
 512 x 512. After the cache has
 been trained for some frames, each gets the same device time (frame counts from measured frame times); the
 cached image must have a clearly lower RMSE against a 1024-spp plain render accumulated in FP64. Frames of the
