@@ -235,7 +235,9 @@ LH2G_API int lh2g_server_destroy(lh2g_server* server);   /* finishes the jobs it
 /* Scheduling settings, applied to jobs admitted afterwards: "expressMaxPaths" (default 0: no express jobs; a
  * path traced whole by one thread is slower than the waves, so express jobs only pay when the GPU is otherwise
  * idle), "expressBudget" (express paths per tick, default 1048576), "tickBudget" (new queue paths per tick,
- * default clamp(capacity, 2^20, 2^22)), "maxWaitSeconds" (0.2). Results do not depend on them. */
+ * default clamp(capacity, 2^20, 2^22)), "maxWaitSeconds" (0.2), "largeJobPaths" (default 2^23; 0 = none: render jobs
+ * of at least this many paths skip the shared queues and run one at a time as plain frames on the server's own
+ * stream beside the ticks, needing no queue memory). Results do not depend on them. */
 LH2G_API int lh2g_server_setting(lh2g_server* server, const char* name, double value);
 LH2G_API const char* lh2g_server_last_error(lh2g_server* server);
 LH2G_API int lh2g_server_add_scene(lh2g_server* server, lh2g_context* scene, int* sceneId);

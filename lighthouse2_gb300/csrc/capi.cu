@@ -277,7 +277,10 @@ struct lh2g_context {
         uint32_t* pixels = nullptr;
         unsigned long long* keys = nullptr;
         float* depth = nullptr;
-        uint32_t *list = nullptr, *big = nullptr, *counters = nullptr;
+        uint32_t *list = nullptr, *counters = nullptr;
+        uint2 *big = nullptr, *owner = nullptr;
+        float4* ck = nullptr;
+        uint32_t ckCap = 0;
         RasterInst* inst = nullptr;
         RasterMat* mats = nullptr;
         int64_t pixCap = 0, triCap = 0;
@@ -509,7 +512,7 @@ int lh2g_destroy(lh2g_context* ctx) {
     dfree(ctx->traceFetch), dfree(ctx->hostRaysDev), dfree(ctx->hostOutDev);
     dfree(ctx->B.capHits), dfree(ctx->B.capSeeds);
     dfree(ctx->rs.pixels), dfree(ctx->rs.keys), dfree(ctx->rs.depth), dfree(ctx->rs.list), dfree(ctx->rs.big), dfree(ctx->rs.counters);
-    dfree(ctx->rs.inst), dfree(ctx->rs.mats);
+    dfree(ctx->rs.inst), dfree(ctx->rs.mats), dfree(ctx->rs.owner), dfree(ctx->rs.ck);
     free_target(ctx);
     if (ctx->hostCounters) cudaFreeHost(ctx->hostCounters);
     if (ctx->ad.hostState) cudaFreeHost(ctx->ad.hostState);
@@ -1793,7 +1796,14 @@ int lh2g_raster_render(lh2g_context* ctx, const lh2g_view* view, uint32_t* pixel
         CK(dalloc(R0.big, total));
         R0.triCap = total;
     }
-    if (!R0.counters) CK(dalloc(R0.counters, 4));
+    /* chunks of the block path: up to 2^20 (88 MB); triangles that find the arrays full are filled one per thread */
+    const uint32_t ckCap = std::min<uint32_t>(1u << 20, std::max<uint32_t>(1u << 14, total));
+    if (ckCap > R0.ckCap) {
+        CK(dalloc(R0.owner, ckCap));
+        CK(dalloc(R0.ck, (size_t)ckCap * 5));
+        R0.ckCap = ckCap;
+    }
+    if (!R0.counters) CK(dalloc(R0.counters, 8));
     if ((int)kept.size() > R0.instCap) {
         CK(dalloc(R0.inst, kept.size()));
         R0.instCap = (int)kept.size();
@@ -1817,12 +1827,13 @@ int lh2g_raster_render(lh2g_context* ctx, const lh2g_view* view, uint32_t* pixel
     CK(cudaMemcpyAsync(R0.mats, mats.data(), sizeof(RasterMat) * mats.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(R0.pixels, 0, sizeof(uint32_t) * WH, st));
     CK(cudaMemsetAsync(R0.keys, 0xff, sizeof(unsigned long long) * WH, st));
-    CK(cudaMemsetAsync(R0.counters, 0, 4 * sizeof(uint32_t), st));
+    CK(cudaMemsetAsync(R0.counters, 0, 8 * sizeof(uint32_t), st));
     RasterFrame F;
     F.W = W, F.H = H, F.nearPlane = fr[0], F.leftPlane = fr[1];
     F.inst = R0.inst, F.nInst = (int)kept.size(), F.total = total;
     F.mats = R0.mats, F.nMats = (uint32_t)ctx->hostMats.size(), F.texels = ctx->texels;
     F.pixels = R0.pixels, F.keys = R0.keys, F.list = R0.list, F.big = R0.big, F.counters = R0.counters;
+    F.owner = R0.owner, F.ck = R0.ck, F.ckCap = R0.ckCap;
     int sms = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
     launch_raster(F, sms, st);

@@ -83,11 +83,22 @@ struct Setup {
     uint32_t shade, mat;
 };
 
+/* the kept instances' first draw-order indices in shared memory (the first RS_SHARED_INST of them), for the
+ * binary search of a triangle's instance; kernels that call setup() fill it first (load_instance_table) */
+constexpr int RS_SHARED_INST = 1024;
+__shared__ uint32_t instFirst[RS_SHARED_INST];
+
+LH2G_DEV void load_instance_table(const RasterFrame& R) {
+    for (int i = threadIdx.x; i < R.nInst && i < RS_SHARED_INST; i += blockDim.x) instFirst[i] = R.inst[i].first;
+    __syncthreads();
+}
+LH2G_DEV uint32_t first_of(const RasterFrame& R, int i) { return i < RS_SHARED_INST ? instFirst[i] : R.inst[i].first; }
+
 LH2G_DEV int find_instance(const RasterFrame& R, uint32_t g) {
     int lo = 0, hi = R.nInst - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (R.inst[mid].first <= g) lo = mid;
+        if (first_of(R, mid) <= g) lo = mid;
         else hi = mid - 1;
     }
     return lo;
@@ -296,22 +307,44 @@ LH2G_DEV void append(uint32_t* list, uint32_t* count, bool take, uint32_t g) {
     if (take) list[base + __popc(m & ((1u << lane) - 1u))] = g;
 }
 
-/* pass 1: every triangle of the kept instances */
+constexpr uint32_t RS_NO_OWNER = 0xffffffffu;
+
+/* pass 1: every triangle of the kept instances. A triangle past the one-thread size takes its chunks from the
+ * chunk arrays; when they are full it is filled here, in one thread (slower, same result). */
 __global__ void __launch_bounds__(128) k_rs_cover(const RasterFrame R) {
+    load_instance_table(R);
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     Setup E;
     bool small = false, big = false;
-    uint32_t offered = 0;
+    uint32_t offered = 0, base = 0;
     if (g < R.total && setup<false>(R, g, E)) {
-        if (work_of(R, E) > RS_SMALL_WORK) big = true;
-        else {
+        if (work_of(R, E) > RS_SMALL_WORK) {
+            const uint32_t n = (uint32_t)(E.maxy - E.miny) / RS_CHUNK + 1u;
+            base = atomicAdd(R.counters + 4, n);
+            if (base < R.ckCap && n <= R.ckCap - base) {
+                big = true;
+                for (uint32_t k = 0; k < n; k++) R.owner[base + k] = make_uint2(g, k);
+            } else {
+                for (uint32_t k = base; k < R.ckCap && k < base + n; k++) R.owner[k] = make_uint2(RS_NO_OWNER, 0u);
+            }
+        }
+        if (!big) {
             Shader none{};
             offered = rasterize<1>(R, E, g, none);
             small = offered > 0;
         }
     }
     append(R.list, R.counters + 0, small, g);
-    append(R.big, R.counters + 1, big, g);
+    {   /* the block-path list, entries (draw order, first chunk) */
+        const uint32_t m = __ballot_sync(0xffffffffu, big);
+        if (m) {
+            const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+            uint32_t b0 = 0;
+            if (lane == leader) b0 = atomicAdd(R.counters + 1, (uint32_t)__popc(m));
+            b0 = __shfl_sync(0xffffffffu, b0, leader);
+            if (big) R.big[b0 + __popc(m & ((1u << lane) - 1u))] = make_uint2(g, base);
+        }
+    }
     unsigned long long o = offered;
 #pragma unroll
     for (int s = 16; s > 0; s >>= 1) o += __shfl_down_sync(0xffffffffu, o, s);
@@ -320,6 +353,7 @@ __global__ void __launch_bounds__(128) k_rs_cover(const RasterFrame R) {
 
 /* pass 2: the small triangles that offered fragments */
 __global__ void __launch_bounds__(128) k_rs_color(const RasterFrame R) {
+    load_instance_table(R);
     const uint32_t n = R.counters[0];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t g = R.list[i];
@@ -395,22 +429,67 @@ LH2G_DEV uint32_t warp_span(const RasterFrame& R, const int y, const float xl, c
     return offered;
 }
 
+/* a warp per block-path triangle: lanes 0..n-1 walk one edge each over its rows and keep its running values at the
+ * first row of every chunk the edge continues into (the chunk then starts from them instead of from the edge's
+ * first row) */
+__global__ void __launch_bounds__(256) k_rs_edges(const RasterFrame R) {
+    load_instance_table(R);
+    const uint32_t n = R.counters[1];
+    const int lane = threadIdx.x & 31;
+    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5) {
+        const uint2 e = R.big[i];
+        Setup E;
+        if (!setup<true>(R, e.x, E)) continue;
+#pragma unroll
+        for (int j = 0; j < RS_MAXV; j++) {
+            if (lane != j || E.iy0[j] > E.iy1[j]) continue;
+            float x = E.x[j], z = E.z[j], u = E.u[j], v = E.v[j];
+            const float dx = E.dx[j], dz = E.dz[j], du = E.du[j], dv = E.dv[j];
+            const int iy0 = E.iy0[j], iy1 = E.iy1[j];
+            /* rows iy0 .. the next chunk start, one step each; then whole chunks of RS_CHUNK steps, storing at each
+             * chunk start (the same additions in the same order as row by row) */
+            int y = iy0;
+            const int first = E.miny + ((iy0 - E.miny) / RS_CHUNK + 1) * RS_CHUNK;
+            for (; y < first && y <= iy1; y++) x += dx, z += dz, u += du, v += dv;
+            for (; y <= iy1; y += RS_CHUNK) {
+                R.ck[(size_t)(e.y + (uint32_t)(y - E.miny) / RS_CHUNK) * RS_MAXV + j] = make_float4(x, z, u, v);
+#pragma unroll
+                for (int k = 0; k < RS_CHUNK; k++) x += dx, z += dz, u += du, v += dv;
+            }
+        }
+    }
+}
+
 /* Triangles past the one-thread size: one block per (triangle, chunk of RS_CHUNK rows, segment of RS_SEG columns).
  * Threads 0..n-1 walk one edge each from its first row to the chunk's end and leave the chunk's values in shared
  * memory; then warp w fills the segment of row w of the chunk (warp_span). */
 constexpr int RS_BIG_WARPS = RS_CHUNK;
 template <int PASS>
-__global__ void __launch_bounds__(32 * RS_BIG_WARPS) k_rs_big(const RasterFrame R, const int chunksPerTri, const int segsPerRow) {
+__global__ void __launch_bounds__(32 * RS_BIG_WARPS) k_rs_big(const RasterFrame R, const int segsPerRow) {
     __shared__ float4 rows[RS_MAXV][RS_CHUNK];   /* x, z, u, v of each edge on each row of the chunk */
-    const uint32_t perTri = (uint32_t)(chunksPerTri * segsPerRow);
-    const uint32_t items = R.counters[1] * perTri;
+    __shared__ Setup shared;                     /* the triangle's set-up, by warp 0 */
+    __shared__ int valid;
+    const uint32_t items = min(R.counters[4], R.ckCap) * (uint32_t)segsPerRow;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     uint32_t offered = 0;
+    load_instance_table(R);
     for (uint32_t item = blockIdx.x; item < items; item += gridDim.x) {
-        const uint32_t g = R.big[item / perTri];
-        const int chunk = (int)(item % perTri) / segsPerRow, seg = (int)(item % perTri) % segsPerRow;
-        Setup E;
-        if (!setup<PASS == 2>(R, g, E)) continue;   /* same outcome in every thread */
+        const uint32_t c = item / (uint32_t)segsPerRow;
+        const int seg = (int)(item % (uint32_t)segsPerRow);
+        const uint2 own = R.owner[c];
+        if (own.x == RS_NO_OWNER) continue;
+        const uint32_t g = own.x;
+        const int chunk = (int)own.y;
+        if (warp == 0) {
+            Setup E0;
+            const bool ok = setup<PASS == 2>(R, g, E0);
+            if (lane == 0) shared = E0, valid = ok;
+        }
+        __syncthreads();
+        const Setup E = shared;
+        const bool ok = valid != 0;
+        __syncthreads();   /* every thread has its copy before warp 0 writes the next item's */
+        if (!ok) continue;
         const int c0 = E.miny + chunk * RS_CHUNK;
         if (c0 > E.maxy) continue;
         const int c1 = min(c0 + RS_CHUNK - 1, E.maxy);
@@ -420,12 +499,21 @@ __global__ void __launch_bounds__(32 * RS_BIG_WARPS) k_rs_big(const RasterFrame 
         }
 #pragma unroll
         for (int j = 0; j < RS_MAXV; j++) {
-            if (t != j || E.iy0[j] > E.iy1[j]) continue;
-            float x = E.x[j], z = E.z[j], u = 0.0f, v = 0.0f;
-            if (PASS == 2) u = E.u[j], v = E.v[j];
+            if (t != j || E.iy0[j] > c1 || E.iy1[j] < c0) continue;
+            /* from the edge's first row, or from its values at the chunk's first row (k_rs_edges) */
+            const int start = max(c0, E.iy0[j]);
+            float x, z, u = 0.0f, v = 0.0f;
+            if (start == E.iy0[j]) {
+                x = E.x[j], z = E.z[j];
+                if (PASS == 2) u = E.u[j], v = E.v[j];
+            } else {
+                const float4 k4 = R.ck[(size_t)c * RS_MAXV + j];
+                x = k4.x, z = k4.y;
+                if (PASS == 2) u = k4.z, v = k4.w;
+            }
             const int last = min(E.iy1[j], c1);
-            for (int y = E.iy0[j]; y <= last; y++) {
-                if (y >= c0) rows[j][y - c0] = make_float4(x, z, u, v);
+            for (int y = start; y <= last; y++) {
+                rows[j][y - c0] = make_float4(x, z, u, v);
                 x += E.dx[j], z += E.dz[j];
                 if (PASS == 2) u += E.du[j], v += E.dv[j];
             }
@@ -471,11 +559,12 @@ __global__ void k_rs_depth(const RasterFrame R, float* zbuffer) {
 }  // namespace
 
 void launch_raster(const RasterFrame& R, int smCount, cudaStream_t st) {
-    const int chunksPerTri = (R.H - 2 + RS_CHUNK - 1) / RS_CHUNK, segsPerRow = (R.W - 2 + RS_SEG - 1) / RS_SEG;
+    const int segsPerRow = (R.W - 2 + RS_SEG - 1) / RS_SEG;
     if (R.total) k_rs_cover<<<(R.total + 127) / 128, 128, 0, st>>>(R);
-    k_rs_big<1><<<smCount * 8, 32 * RS_BIG_WARPS, 0, st>>>(R, chunksPerTri, segsPerRow);
+    k_rs_edges<<<smCount * 2, 256, 0, st>>>(R);
+    k_rs_big<1><<<smCount * 8, 32 * RS_BIG_WARPS, 0, st>>>(R, segsPerRow);
     k_rs_color<<<smCount * 12, 128, 0, st>>>(R);
-    k_rs_big<2><<<smCount * 8, 32 * RS_BIG_WARPS, 0, st>>>(R, chunksPerTri, segsPerRow);
+    k_rs_big<2><<<smCount * 8, 32 * RS_BIG_WARPS, 0, st>>>(R, segsPerRow);
 }
 
 void launch_raster_pack(const float4* tris, uint32_t n, float4* norms, cudaStream_t st) {

@@ -12,7 +12,8 @@
  * Every interpolant is the reference's running sum (x0 += dx per row, u0 += du per pixel, ...), recomputed the
  * same way in both passes, so the GPU's pixels and z-buffer equal the sequential result bit for bit. Triangles
  * covering more than a few dozen pixels are queued instead and run as one block per (triangle, 8-row chunk,
- * 512-column segment) (k_rs_big), a warp per row. */
+ * 512-column segment) (k_rs_big), a warp per row; a warp per queued triangle first walks its edges once and leaves
+ * their running values at every chunk's first row (k_rs_edges), so a chunk starts there. */
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -44,8 +45,11 @@ struct RasterFrame {
     uint32_t* pixels;                /* W x H RGBA8 */
     unsigned long long* keys;        /* W x H depth keys, all ones = empty */
     uint32_t* list;                  /* pass 1 -> pass 2: small triangles that offered fragments */
-    uint32_t* big;                   /* triangles for the block-per-chunk path */
-    uint32_t* counters;              /* [0] list, [1] big, [2] fragments offered, [3] status (bad material) */
+    uint2* big;                      /* triangles for the block path: draw order, first chunk */
+    uint2* owner;                    /* per chunk of RS_CHUNK rows: its triangle's draw order and the chunk's index in it */
+    float4* ck;                      /* per chunk and edge: the edge's running x, z, u, v at the chunk's first row */
+    uint32_t ckCap;                  /* chunks the two arrays above hold */
+    uint32_t* counters;              /* [0] list, [1] big, [2] fragments offered, [3] status (bad material), [4] chunks */
 };
 
 constexpr int RS_CHUNK = 8;          /* rows per block of the big-triangle path (a warp per row) */

@@ -413,6 +413,19 @@ struct lh2g_server {
     /* statistics */
     long long jobsDone = 0;
     unsigned long long raysDone = 0;
+    /* Large jobs (at least largeMin paths; setting "largeJobPaths", 0 = none) skip the shared queues: they run one at a
+     * time as plain frames (the plain core's stages, waves then the tail kernel) on their own stream and buffers,
+     * beside the ticks. A job that fills the GPU alone gains nothing from sharing queues, and in the queues it
+     * lengthens every tick the small jobs need. */
+    long long largeMin = 8ll << 20;
+    std::deque<Job*> largeQ;
+    std::condition_variable lcv;
+    std::thread large;
+    cudaStream_t lst = nullptr;
+    lh2g::WaveBuffers LB{};
+    long long lcap = 0, lpix = 0;
+    lh2g::Counters* lhost = nullptr;   /* pinned copy of a large job's counters */
+    uint32_t largeStatus = 0;          /* traversal status bits of large jobs (reported with the device status) */
 };
 
 namespace lh2g {
@@ -484,6 +497,78 @@ void run_query(lh2g_server* s, Job* j) {
     finish(s, j, ok ? 3 : 4);
 }
 
+/* One large job as a plain frame (the waves of lh2g_render_ex, then the tail kernel and the finalize that leaves the
+ * per-pixel sums), on the server's large-job stream; false on a CUDA error. */
+bool render_large(lh2g_server* s, Job* j, const SceneGPU& S) {
+    const lh2g_render_params& p = j->params;
+    const long long P = (long long)p.width * p.height * p.spp, WH = (long long)p.width * p.height;
+    WaveBuffers& B = s->LB;
+    bool ok = true;
+    if (P > s->lcap) {
+        for (int k = 0; k < 2; k++) cudaFree(B.O[k]), cudaFree(B.D[k]), cudaFree(B.T[k]);
+        cudaFree(B.hits), cudaFree(B.shO), cudaFree(B.shD), cudaFree(B.shE), cudaFree(B.pathAcc), cudaFree(B.order);
+        for (int k = 0; k < 2 && ok; k++)
+            ok = cudaMalloc((void**)&B.O[k], 16 * (size_t)P) == cudaSuccess && cudaMalloc((void**)&B.D[k], 16 * (size_t)P) == cudaSuccess &&
+                 cudaMalloc((void**)&B.T[k], 16 * (size_t)P) == cudaSuccess;
+        ok = ok && cudaMalloc((void**)&B.hits, 16 * (size_t)P) == cudaSuccess && cudaMalloc((void**)&B.shO, 16 * (size_t)P) == cudaSuccess &&
+             cudaMalloc((void**)&B.shD, 16 * (size_t)P) == cudaSuccess && cudaMalloc((void**)&B.shE, 16 * (size_t)P) == cudaSuccess &&
+             cudaMalloc((void**)&B.pathAcc, 16 * (size_t)P) == cudaSuccess && cudaMalloc((void**)&B.order, 4 * (size_t)P) == cudaSuccess;
+        s->lcap = ok ? P : 0;
+    }
+    if (ok && WH > s->lpix) {
+        cudaFree(B.accum), cudaFree(B.frame);
+        ok = cudaMalloc((void**)&B.accum, 16 * (size_t)WH) == cudaSuccess && cudaMalloc((void**)&B.frame, 16 * (size_t)WH) == cudaSuccess;
+        s->lpix = ok ? WH : 0;
+    }
+    if (ok && !B.counters) ok = cudaMalloc((void**)&B.counters, sizeof(Counters)) == cudaSuccess;
+    if (ok && !s->lhost) ok = cudaMallocHost((void**)&s->lhost, sizeof(Counters)) == cudaSuccess;
+    if (!ok) return false;
+    FrameGPU F = frame_of(&j->view, &p);
+    F.stride = s->lcap;
+    cudaStream_t st = s->lst;
+    ok = cudaMemsetAsync(B.counters, 0, sizeof(Counters), st) == cudaSuccess;
+    launch_generate(F, B, st);
+    constexpr int TAIL = 5;   /* the plain core's default waveTail */
+    const int waves = std::min(F.maxDepth, TAIL - 1);
+    for (int d = 1; d <= waves; d++) {
+        launch_extend(S, F, B, d, persistent_blocks_wave(0), st);
+        launch_shade(S, F, B, d, persistent_blocks_wave(2), st);
+        launch_connect(S, F, B, d, persistent_blocks_wave(1), st);
+    }
+    if (waves < F.maxDepth) launch_tail(S, F, B, waves + 1, persistent_blocks_wave(3), st);
+    launch_finalize(F, B, 1.0f / (float)(p.samplesTaken + F.spp), 1, st);
+    ok = ok && cudaGetLastError() == cudaSuccess;
+    ok = ok && cudaMemcpyAsync(j->hostOut, B.accum, 16 * (size_t)WH, cudaMemcpyDeviceToHost, st) == cudaSuccess;
+    ok = ok && cudaMemcpyAsync(s->lhost, B.counters, sizeof(Counters), cudaMemcpyDeviceToHost, st) == cudaSuccess;
+    ok = cudaStreamSynchronize(st) == cudaSuccess && ok;
+    if (ok) {
+        unsigned long long rays = (unsigned long long)P;
+        for (int d = 0; d < F.maxDepth; d++) rays += s->lhost->extension[d] + s->lhost->shadow[d];
+        std::lock_guard<std::mutex> g(s->mu);
+        s->raysDone += rays;
+        s->largeStatus |= s->lhost->status;
+    }
+    return ok;
+}
+
+void large_loop(lh2g_server* s) {
+    cudaSetDevice(s->device);
+    for (;;) {
+        Job* j = nullptr;
+        SceneGPU S;
+        {
+            std::unique_lock<std::mutex> g(s->mu);
+            s->lcv.wait(g, [&] { return s->stop || s->abortLoop || !s->largeQ.empty(); });
+            if (s->largeQ.empty()) return;   /* stopping, nothing held */
+            j = s->largeQ.front();
+            s->largeQ.pop_front();
+            S = s->scenes[j->scene];
+        }
+        const bool ok = render_large(s, j, S);
+        finish(s, j, ok ? 3 : 4);
+    }
+}
+
 /* A path range of a job entering the queues at the next tick. */
 struct Range { Job* job; long long start, count; bool first, express; };
 
@@ -521,6 +606,22 @@ void admit(lh2g_server* s, std::vector<Range>& ranges) {
         else k++;
     }
     const double now = now_s();
+    /* large jobs go to their own lane, in arrival order, without queue memory */
+    if (s->largeMin > 0) {
+        bool moved = false;
+        for (size_t k = 0; k < s->pending.size();) {
+            Job* j = s->pending[k];
+            if (j->kind == 0 && j->paths >= s->largeMin) {
+                s->pending.erase(s->pending.begin() + (long)k);
+                j->state = 1, j->tAdmit = now;
+                s->largeQ.push_back(j);
+                moved = true;
+            } else {
+                k++;
+            }
+        }
+        if (moved) s->lcv.notify_all();
+    }
     while (!s->pending.empty()) {
         size_t pick = 0;
         if (now - s->pending.front()->tSubmit <= s->maxWaitS)
@@ -811,8 +912,14 @@ int lh2g_server_create(int device, long long pathCapacity, lh2g_server** out) {
         lh2g_server_destroy(s);
         return LH2G_ERR_CUDA;
     }
+    ok = ok && cudaStreamCreateWithFlags(&s->lst, cudaStreamNonBlocking) == cudaSuccess;
+    if (!ok) {
+        lh2g_server_destroy(s);
+        return LH2G_ERR_CUDA;
+    }
     s->loop = std::thread(tick_loop, s);
     s->worker = std::thread(worker_loop, s);
+    s->large = std::thread(large_loop, s);
     *out = s;
     return LH2G_OK;
 }
@@ -833,6 +940,11 @@ int lh2g_server_destroy(lh2g_server* s) {
     }
     s->tcv.notify_all();
     if (s->worker.joinable()) s->worker.join();
+    {
+        std::lock_guard<std::mutex> g(s->mu);
+        s->lcv.notify_all();
+    }
+    if (s->large.joinable()) s->large.join();
     cudaSetDevice(s->device);
     if (s->st) cudaStreamSynchronize(s->st);
     if (s->io) cudaStreamSynchronize(s->io);
@@ -843,6 +955,14 @@ int lh2g_server_destroy(lh2g_server* s) {
     for (int k = 0; k < 2; k++) cudaFree(s->Q.O[k]), cudaFree(s->Q.D[k]), cudaFree(s->Q.T[k]);
     cudaFree(s->Q.hits), cudaFree(s->Q.shO), cudaFree(s->Q.shD), cudaFree(s->Q.shE), cudaFree(s->Q.order);
     cudaFree(s->dJobs), cudaFree(s->dAlive), cudaFree(s->dState);
+    if (s->lst) cudaStreamSynchronize(s->lst), cudaStreamDestroy(s->lst);
+    {
+        WaveBuffers& B = s->LB;
+        for (int k = 0; k < 2; k++) cudaFree(B.O[k]), cudaFree(B.D[k]), cudaFree(B.T[k]);
+        cudaFree(B.hits), cudaFree(B.shO), cudaFree(B.shD), cudaFree(B.shE), cudaFree(B.pathAcc), cudaFree(B.order);
+        cudaFree(B.accum), cudaFree(B.frame), cudaFree(B.counters);
+        if (s->lhost) cudaFreeHost(s->lhost);
+    }
     if (s->hAlive) cudaFreeHost(s->hAlive);
     if (s->hTick) cudaFreeHost(s->hTick);
     for (auto& kv : s->jobs) delete kv.second;
@@ -864,6 +984,7 @@ int lh2g_server_setting(lh2g_server* s, const char* name, double value) {
     else if (!strcmp(name, "expressBudget")) s->expressBudget = (long long)value;
     else if (!strcmp(name, "tickBudget")) s->tickBudget = std::max(1ll, (long long)value);
     else if (!strcmp(name, "maxWaitSeconds")) s->maxWaitS = value;
+    else if (!strcmp(name, "largeJobPaths")) s->largeMin = (long long)value;
     else {
         s->err = std::string("unknown server setting ") + name;
         return LH2G_ERR_INVALID;
@@ -901,7 +1022,11 @@ int lh2g_server_submit_render(lh2g_server* s, int sceneId, const lh2g_view* view
     {
         std::lock_guard<std::mutex> g(s->mu);
         if (sceneId < 0 || sceneId >= (int)s->scenes.size()) { delete j; s->err = "submit_render: unknown scene"; return LH2G_ERR_INVALID; }
-        if (P > s->capacity) { delete j; s->err = "submit_render: the job has more paths than the server's capacity"; return LH2G_ERR_OVERFLOW; }
+        if (P > s->capacity && !(s->largeMin > 0 && P >= s->largeMin)) {
+            delete j;
+            s->err = "submit_render: the job has more paths than the server's capacity";
+            return LH2G_ERR_OVERFLOW;
+        }
         j->scene = sceneId;
         j->id = s->nextId++;
         s->jobs[j->id] = j;
@@ -963,7 +1088,7 @@ int lh2g_server_get_stats(lh2g_server* s, lh2g_server_stats* out) {
     out->jobsDone = s->jobsDone;
     out->pathsInFlight = s->pathsInFlight;
     out->pending = (long long)s->pending.size();
-    out->deviceStatus = st.status;
+    out->deviceStatus = st.status | s->largeStatus;
     return LH2G_OK;
 }
 

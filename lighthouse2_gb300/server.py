@@ -39,7 +39,7 @@ class RenderServer:
     server. Results land in numpy arrays owned by the job handles returned by submit_*."""
 
     def __init__(self, path_capacity: int, device: int = 0, **settings):
-        """settings: expressMaxPaths, expressBudget, tickBudget, maxWaitSeconds (lh2g_server_setting)."""
+        """settings: expressMaxPaths, expressBudget, tickBudget, maxWaitSeconds, largeJobPaths (lh2g_server_setting)."""
         self.lib = load_library()
         _bind(self.lib)
         self.srv = C.c_void_p()

@@ -119,3 +119,34 @@ def test_admission_by_path_memory_and_queries(two_scenes, oracle_lib):
     rel = np.abs(srv.result(jid) - ref) / np.maximum(np.abs(ref), 1e-6)
     assert rel.max() <= 1e-4
     srv.close()
+
+
+def test_large_job_lane(two_scenes):
+    """Jobs of at least "largeJobPaths" paths run as plain frames on the server's own stream beside the ticks (and
+    need no queue memory: one is larger than the queue capacity); every image equals the plain core's, in the mix
+    and alone."""
+    from lighthouse2_gb300.server import RenderServer
+    (sa, ca), (sb, cb) = two_scenes
+    cores = [ca, cb]
+    jobs = JOBS + [(1, 320, 240, 1, 6, 3, 7), (0, 256, 256, 2, 5, 2, 2)]   # 76,800 and 131,072 paths
+    expect = []
+    for j in jobs:
+        view, p = job_inputs(*j)
+        expect.append(plain_core_image(cores[j[0]], view, p))
+    srv = RenderServer(path_capacity=1 << 16, largeJobPaths=6000)
+    sid = [srv.add_scene(ca), srv.add_scene(cb)]
+    ids = []
+    for j in jobs:
+        view, p = job_inputs(*j)
+        ids.append(srv.submit_render(sid[j[0]], view, p))
+    for k, jid in enumerate(ids):
+        srv.wait(jid)
+        assert np.array_equal(srv.result(jid).view(np.uint32), expect[k].view(np.uint32)), f"job {k} differs from the plain core"
+        srv.release(jid)
+    view, p = job_inputs(*jobs[-1])
+    jid = srv.submit_render(sid[jobs[-1][0]], view, p)
+    srv.wait(jid)
+    assert np.array_equal(srv.result(jid).view(np.uint32), expect[-1].view(np.uint32))
+    st = srv.stats()
+    assert st["deviceStatus"] == 0 and st["pathsInFlight"] == 0 and st["raysTraced"] > 0
+    srv.close()
