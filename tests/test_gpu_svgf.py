@@ -72,12 +72,13 @@ def test_filter_frame_features_and_halves(scene, oracle_lib, W, H, spp, depth):
     assert (spec == 0).any() and (spec == 1).any()                   # diffuse and via-specular first vertices
 
 
-@pytest.mark.parametrize("taa", [1, 0])
-def test_filtered_render_sequence(scene, oracle_lib, taa):
+@pytest.mark.parametrize("taa,W,H", [(1, 56, 40), (0, 56, 40), (1, 136, 104)])
+def test_filtered_render_sequence(scene, oracle_lib, taa, W, H):
+    """56 x 40: every block of the widest a-trous pass reaches past the image (clamped loads); 136 x 104: each pass
+    has blocks whose tile lies inside the image as well, and partial blocks at the right edge."""
     sc, _, o = scene
     core = RenderCore()           # a fresh core: jitter cycle, previous jitter and camera seed start from their initial values
     core.set_scene(sc)
-    W, H = 56, 40
     core.SetTarget(W, H, 1)
     core.Setting("maxDepth", 5)
     core.Setting("rrStartDepth", 2)
@@ -124,6 +125,7 @@ def test_filtered_render_sequence(scene, oracle_lib, taa):
                 assert_same(f"frame {k} {name}", core.read_filter_buffer(name), st[name])
         fb = core.read_framebuffer()
         assert_same(f"frame {k} frame buffer", fb, st["target"])
+        assert core.GetCoreStats()["deviceStatus"] == 0
         prev_view, pj = view, j
     img = core.read_framebuffer().reshape(H, W, 4)[1:-1, 1:-1, :3]
     assert np.isfinite(img).all() and img.mean() > 0.01
