@@ -179,7 +179,7 @@ LH2G_API int lh2g_trace_host(lh2g_context* ctx, const lh2g_ray* rays, void* out,
  * array's device address (cudaGetSymbolAddress); make that first call before any stream capture. All calls share
  * the array and it keeps the last call's contents: calls whose GPU work overlaps (other streams, threads or
  * contexts on the same device) race. statusHost (may be NULL) receives the frame's LH2G_STATUS_* word (traversal
- * stack overflow or step limit: the frame is then incomplete), copied on the stream: read it after the stream has
+ * stack overflow, step limit, copy timeout: the frame is then incomplete), copied on the stream: read it after the stream has
  * completed (pinned memory) or on return (pageable memory, which makes the copy synchronous). */
 #define LH2G_NOALLOC_MAX_PATHS 32768
 LH2G_API int lh2g_render_noalloc(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_params* params, float* accumDevice,

@@ -168,6 +168,13 @@ typedef struct lh2g_render_params {
  * uses the third random number that lambert.h draws and ignores. */
 #define LH2G_RP_DISNEY     64
 
+/* Bits of the device status word (lh2g_core_stats.deviceStatus, lh2g_render_noalloc's statusHost, the serving
+ * loop's stats): the frame they come with is incomplete. */
+#define LH2G_STATUS_STACK_OVERFLOW 1u    /* a traversal stack was full: entries were dropped */
+#define LH2G_STATUS_TRAVERSAL_LIMIT 2u   /* a traversal exceeded its step limit (a malformed tree) */
+#define LH2G_STATUS_QUEUE_OVERFLOW 4u    /* serving loop: new paths would not have fit the queue (skipped) */
+#define LH2G_STATUS_COPY_TIMEOUT 8u      /* a staged copy of path state did not complete within its bound (batch skipped) */
+
 /* One SVGF pass over the accumulator of a LH2G_RP_FILTER frame (lib/RenderCore_Optix7Filter/rendercore.cpp:
  * 897-935 with the kernels of lib/CUDA/shared_kernel_code/finalize_shared.h:169-600). */
 typedef struct lh2g_filter_params {

@@ -1097,7 +1097,7 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
         if (capSeeds) CK(cudaMemcpy(capSeeds, ctx->B.capSeeds, sizeof(uint32_t) * capN, cudaMemcpyDeviceToHost));
         if (countersOut)
             for (int d = 0; d < F.maxDepth; d++) countersOut[2 * d] = hostCounters->extension[d], countersOut[2 * d + 1] = hostCounters->shadow[d];
-        if (hostCounters->status) return fail(ctx, LH2G_ERR_OVERFLOW, "render: traversal stack overflow or step limit");
+        if (hostCounters->status) return fail(ctx, LH2G_ERR_OVERFLOW, "render: traversal stack overflow, step limit or path-state copy timeout");
     }
     return LH2G_OK;
 }
@@ -1235,7 +1235,7 @@ int render_adaptive(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_
             statsOut->adaptivePaths = a.hostState->pathCount;
             statsOut->requested = a.hostState->requested;
         }
-        if (ctx->hostCounters->status | a.hostCounters2->status) return fail(ctx, LH2G_ERR_OVERFLOW, "render: traversal stack overflow or step limit");
+        if (ctx->hostCounters->status | a.hostCounters2->status) return fail(ctx, LH2G_ERR_OVERFLOW, "render: traversal stack overflow, step limit or path-state copy timeout");
     }
     return LH2G_OK;
 }

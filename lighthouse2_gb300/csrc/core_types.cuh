@@ -19,6 +19,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "lh2g_types.h"
+
 namespace lh2g {
 
 struct BVH8Node {
@@ -113,8 +115,6 @@ constexpr uint32_t S_BOUNCEDTWICE = 8;   /* (S_SPECULAR 1, S_BOUNCED 2 and S_VIA
 constexpr uint32_t MIS_TMIN_SHIFT = 4, MIS_TMIN_EPS = 1u << 4, MIS_TMIN_EPSILON = 2u << 4;
 constexpr int MIS_SLOT_BITS = 26;   /* slots below 2^26 (67M paths) */
 
-#define LH2G_STATUS_STACK_OVERFLOW 1u
-#define LH2G_STATUS_TRAVERSAL_LIMIT 2u
-#define LH2G_STATUS_QUEUE_OVERFLOW 4u   /* serving loop: new paths would not have fit the queue (skipped) */
+/* (the LH2G_STATUS_* bits of the device status word are in lh2g_types.h) */
 
 }  // namespace lh2g

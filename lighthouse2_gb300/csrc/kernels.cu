@@ -89,6 +89,24 @@ __global__ void LH2G_TRAV_BOUNDS k_extend(const SceneGPU S, const FrameGPU F, co
             B.capHits[(size_t)(depth - 1) * F.P + pathIdx] = c;
         }
     };
+#if LH2G_STAGE_RAYS && !LH2G_COOP && !LH2G_REFILL
+    (void)stackBase;
+    if constexpr (MIS) {   /* origins (w: path slot and flags, tmin) and directions */
+        const float4* const src[2] = {O4, D4};
+        trace_queue_staged<false, 2>(S, &C->fetch[depth - 1], count, status, src,
+            [&](uint32_t, const float4 (&v)[2], float3& o, float3& d, float& t0, float& t1) {
+                o = xyz(v[0]), d = xyz(v[1]), t0 = mis_tmin(__float_as_uint(v[0].w), F.eps), t1 = 1e34f;
+            },
+            [&](uint32_t i, const Traversal& tr, bool) { write(i, tr.found, tr.best); }, C->travStats);
+    } else {   /* origins, directions, throughput (w: tmin) */
+        const float4* const src[3] = {O4, D4, T4};
+        trace_queue_staged<false, 3>(S, &C->fetch[depth - 1], count, status, src,
+            [&](uint32_t, const float4 (&v)[3], float3& o, float3& d, float& t0, float& t1) {
+                o = xyz(v[0]), d = xyz(v[1]), t0 = v[2].w, t1 = 1e34f;
+            },
+            [&](uint32_t i, const Traversal& tr, bool) { write(i, tr.found, tr.best); }, C->travStats);
+    }
+#else
     trace_queue_any<false>(S, &C->fetch[depth - 1], count, status, stackBase,
         [&](uint32_t i, float3& o, float3& d, float& t0, float& t1) {
             if (MIS) {
@@ -101,6 +119,7 @@ __global__ void LH2G_TRAV_BOUNDS k_extend(const SceneGPU S, const FrameGPU F, co
         [&](uint32_t i, const Traversal& tr, bool) { write(i, tr.found, tr.best); },
         [&](uint32_t i, const CoopRay& tr, bool) { if ((threadIdx.x & (COOP - 1)) == 0) write(i, tr.found, tr.best); },
         C->travStats);
+#endif
     if (status) atomicOr(&C->status, status);
 }
 
@@ -241,6 +260,15 @@ __global__ void LH2G_TRAV_BOUNDS k_connect(const SceneGPU S, const FrameGPU F, c
         if (optix7) acc.w += 1.0f;
         *accP = acc;
     };
+#if LH2G_STAGE_RAYS && !LH2G_COOP && !LH2G_REFILL
+    (void)stackBase;
+    const float4* const src[2] = {B.shO, B.shD};   /* origins and directions (w: distance to the light) */
+    trace_queue_staged<true, 2>(S, &C->fetch[64 + depth - 1], count, status, src,
+        [&](uint32_t, const float4 (&v)[2], float3& o, float3& d, float& t0, float& t1) {
+            o = xyz(v[0]), d = xyz(v[1]), t0 = optix7 ? F.eps : 0.0f, t1 = v[1].w;
+        },
+        [&](uint32_t i, const Traversal&, bool occluded) { if (!occluded) add(i); }, C->travStats + 2);
+#else
     trace_queue_any<true>(S, &C->fetch[64 + depth - 1], count, status, stackBase,
         [&](uint32_t i, float3& o, float3& d, float& t0, float& t1) {
             const float4 d4 = B.shD[i];
@@ -249,6 +277,7 @@ __global__ void LH2G_TRAV_BOUNDS k_connect(const SceneGPU S, const FrameGPU F, c
         [&](uint32_t i, const Traversal&, bool occluded) { if (!occluded) add(i); },
         [&](uint32_t i, const CoopRay&, bool occluded) { if (!occluded && (threadIdx.x & (COOP - 1)) == 0) add(i); },
         C->travStats + 2);
+#endif
     if (status) atomicOr(&C->status, status);
 }
 
