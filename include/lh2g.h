@@ -60,9 +60,21 @@ LH2G_API int lh2g_set_materials(lh2g_context* ctx, const lh2g_material* material
 LH2G_API int lh2g_pack_materials(const lh2g_material* materials, int count, const lh2g_texture* textures, int textureCount, lh2g_gpu_material* out);
 /* SetTextures (core_api_base.h:103): ARGB32 texels, MIP levels back to back. */
 LH2G_API int lh2g_set_textures(lh2g_context* ctx, const lh2g_texture* textures, int count);
-/* SetLights (core_api_base.h:107-110); at most 64 lights in total. */
+/* SetLights (core_api_base.h:107-110). Frames that select lights by their potentials (every estimator but the OptiX 7
+ * one with its light tree, LH2G_RP_LIGHTTREE) take at most 64 lights in total (the reference's MAXISLIGHTS); the
+ * light tree takes up to LH2G_MAX_TREE_LIGHTS area, point and spot lights. Also builds the light tree
+ * (RenderCore::SetLights calls UpdateLightTree, rendercore_optix7/rendercore.cpp:709). */
+#define LH2G_MAX_TREE_LIGHTS (1 << 20)
 LH2G_API int lh2g_set_lights(lh2g_context* ctx, const lh2g_light_tri* tri, int ntri, const lh2g_point_light* point, int npoint,
                     const lh2g_spot_light* spot, int nspot, const lh2g_dir_light* dir, int ndir);
+/* The light tree that lh2g_set_lights builds for these lights (RenderCore::UpdateLightTree,
+ * rendercore_optix7/rendercore.cpp:625-680), host only: no context or GPU needed. Writes 2 * (ntri + npoint + nspot)
+ * records of 16 32-bit words (the device LightCluster of common_classes.h:522-527: light, left, right, intensity;
+ * box minimum xyz, 0; box maximum xyz, 0; normal xyz, parent) to nodes; record 0 is the root. Returns the record
+ * count, or minus an error code: -LH2G_ERR_INVALID (negative counts, more than LH2G_MAX_TREE_LIGHTS lights) or
+ * -LH2G_ERR_OVERFLOW (capacity, in records, too small). */
+LH2G_API int lh2g_build_light_tree(const lh2g_light_tri* tri, int ntri, const lh2g_point_light* point, int npoint, const lh2g_spot_light* spot,
+                                   int nspot, void* nodes, int capacity);
 /* SetSkyData (core_api_base.h:112): width*height RGB floats; worldToSky16 may be NULL (identity). */
 LH2G_API int lh2g_set_sky(lh2g_context* ctx, const float* rgb, int width, int height, const float* worldToSky16);
 /* Blue-noise tables of the OptiX 7 estimator (LH2G_RP_OPTIX7 and adaptive frames), in the layout of the Lighthouse 2

@@ -167,6 +167,12 @@ typedef struct lh2g_render_params {
  * the BSDF value without lambert.h's ROUGHNESS factor (BSDF_HAS_PURE_SPECULARS is lambert.h's), and the sampler
  * uses the third random number that lambert.h draws and ignores. */
 #define LH2G_RP_DISNEY     64
+/* With LH2G_RP_OPTIX7: stochastic-lightcuts light selection through the binary light tree that lh2g_set_lights builds
+ * (lights_shared.h:120-156 CalculateChildNodeWeights, :198-217 LightPickProbLTree, :322-395 RandomPointOnLightLTree;
+ * the calls the OptiX 7 shading kernel has commented out beside its potential-based ones, pathtracer.h:145,187, with
+ * LIGHTTREE defined). Each tree level draws six numbers from the path's shading seed. Directional lights are not in
+ * the tree. Scenes of more than 64 lights render only with it. */
+#define LH2G_RP_LIGHTTREE  128
 
 /* Bits of the device status word (lh2g_core_stats.deviceStatus, lh2g_render_noalloc's statusHost, the serving
  * loop's stats): the frame they come with is incomplete. */

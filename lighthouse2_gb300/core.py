@@ -34,7 +34,10 @@ STATS_FIELDS = ["totalRays", "totalExtensionRays", "totalShadowRays", "primaryRa
 STATS_DTYPE = np.dtype([(f, "<u4") for f in STATS_FIELDS[:6]] + [(f, "<f4") for f in STATS_FIELDS[6:14]] +
                        [(f, "<u4") for f in STATS_FIELDS[14:18]] + [("probedInstid", "<i4"), ("probedTriid", "<i4"),
                                                                     ("probedDist", "<f4"), ("deviceStatus", "<u4")])
-RP_NEE, RP_DEPTH_W, RP_FILTER, RP_OPTIX7, RP_ADAPTIVE, RP_DISNEY = 1, 2, 4, 16, 32, 64
+RP_NEE, RP_DEPTH_W, RP_FILTER, RP_OPTIX7, RP_ADAPTIVE, RP_DISNEY, RP_LIGHTTREE = 1, 2, 4, 16, 32, 64, 128
+# one light-tree record (lh2g_build_light_tree; the device LightCluster of common_classes.h:522-527)
+LIGHT_TREE_DTYPE = np.dtype([("light", "<i4"), ("left", "<i4"), ("right", "<i4"), ("intensity", "<f4"), ("bmin", "<f4", 4),
+                             ("bmax", "<f4", 4), ("N", "<f4", 3), ("parent", "<i4")])
 # filter buffer slots (LH2G_FB_*): name -> (index, element dtype, components per pixel)
 FILTER_SLOTS = {"features": (0, np.uint32, 4), "worldPos": (1, np.float32, 4), "prevWorldPos": (2, np.float32, 4),
                 "deltaDepth": (3, np.float32, 4), "motion": (4, np.float32, 2), "moments": (5, np.float32, 4),
@@ -51,13 +54,27 @@ C_API = ["lh2g_create", "lh2g_destroy", "lh2g_last_error", "lh2g_set_geometry", 
          "lh2g_nrc_create", "lh2g_nrc_destroy", "lh2g_nrc_last_error", "lh2g_nrc_get_spec", "lh2g_nrc_set_params", "lh2g_nrc_get_params",
          "lh2g_nrc_get_grads", "lh2g_nrc_infer", "lh2g_nrc_train", "lh2g_nrc_apply_update", "lh2g_nrc_infer_counted", "lh2g_nrc_train_counted",
          "lh2g_nrc_last_loss", "lh2g_nrc_wait_selftest", "lh2g_render_nrc", "lh2g_nrc_infer_host", "lh2g_nrc_train_host",
-         "lh2g_set_blue_noise", "lh2g_render_adaptive", "lh2g_set_adaptive_scale", "lh2g_raster_render", "lh2g_raster_pixels_device", "lh2g_raster_read"]
+         "lh2g_set_blue_noise", "lh2g_render_adaptive", "lh2g_set_adaptive_scale", "lh2g_raster_render", "lh2g_raster_pixels_device", "lh2g_raster_read",
+         "lh2g_build_light_tree"]
 
 _lib = None
 
 
 class CoreError(RuntimeError):
     pass
+
+
+def build_light_tree(tri, point, spot, lib=None):
+    """The light tree lh2g_set_lights builds for these lights (structured arrays of the scene's light dtypes),
+    through the host-only lh2g_build_light_tree: an array of LIGHT_TREE_DTYPE records, record 0 the root."""
+    lib = lib or load_library()
+    arrs = [np.ascontiguousarray(a) for a in (tri, point, spot)]
+    cap = 2 * sum(len(a) for a in arrs)
+    out = np.zeros(max(cap, 1), LIGHT_TREE_DTYPE)
+    n = lib.lh2g_build_light_tree(*[x for a in arrs for x in (_p(a) if len(a) else None, len(a))], _p(out), cap)
+    if n < 0:
+        raise CoreError(f"build_light_tree: status {-n}")
+    return out[:n]
 
 
 def load_library(path: str | None = None):
@@ -81,6 +98,7 @@ def load_library(path: str | None = None):
     lib.lh2g_pack_materials.argtypes = [vp, i, vp, i, vp]
     lib.lh2g_set_textures.argtypes = [vp, vp, i]
     lib.lh2g_set_lights.argtypes = [vp, vp, i, vp, i, vp, i, vp, i]
+    lib.lh2g_build_light_tree.argtypes = [vp, i, vp, i, vp, i, vp, i]
     lib.lh2g_set_sky.argtypes = [vp, vp, i, i, vp]
     lib.lh2g_setting.argtypes = [vp, C.c_char_p, f]
     lib.lh2g_set_target.argtypes = [vp, i, i, i]

@@ -27,6 +27,7 @@
 #include "bvh_build.cuh"
 #include "kernels.cuh"
 #include "lh2g.h"
+#include "light_tree.h"
 #include "svgf.cuh"
 #include "raster.cuh"
 
@@ -160,6 +161,9 @@ struct lh2g_context {
     uint32_t* texels = nullptr;
     std::vector<uint32_t> texFirst, texWH;
     float4 *triL = nullptr, *ptL = nullptr, *spL = nullptr, *dirL = nullptr;
+    float4* lightTree = nullptr;       /* 4 float4 per record (light_tree.h) */
+    int nTreeNodes = 0;
+    int lightTreeOn = 0;               /* setting "lightTree": the OptiX 7 estimator selects lights through the tree */
     int nTri = 0, nPt = 0, nSpot = 0, nDir = 0;
     float4* sky = nullptr;
     float4* skySmall = nullptr;       /* the sky's 64x scaled-down copy (OptiX 7 estimator after a bounce) */
@@ -447,6 +451,7 @@ SceneGPU scene_of(const lh2g_context* c) {
     S.nMaterials = (int)std::max<size_t>(c->hostMats.size(), 1);
     S.triLights = c->triL, S.pointLights = c->ptL, S.spotLights = c->spL, S.dirLights = c->dirL;
     S.nTri = c->nTri, S.nPoint = c->nPt, S.nSpot = c->nSpot, S.nDir = c->nDir;
+    S.lightTree = c->lightTree, S.nTreeNodes = c->nTreeNodes;
     S.skyPixels = c->sky, S.skyW = c->skyW, S.skyH = c->skyH;
     S.skySmall = c->skySmall, S.blueNoise = c->blueNoise;
     for (int r = 0; r < 3; r++) S.worldToSky[r] = make_float4(c->w2s[4 * r], c->w2s[4 * r + 1], c->w2s[4 * r + 2], c->w2s[4 * r + 3]);
@@ -507,6 +512,7 @@ int lh2g_destroy(lh2g_context* ctx) {
         if (L.st) cudaStreamSynchronize(L.st);
     for (MeshDev& m : ctx->meshes) dfree(m.verts), dfree(m.tris), dfree(m.rsNorms);
     dfree(ctx->mats), dfree(ctx->texels), dfree(ctx->triL), dfree(ctx->ptL), dfree(ctx->spL), dfree(ctx->dirL), dfree(ctx->sky);
+    dfree(ctx->lightTree);
     dfree(ctx->skySmall), dfree(ctx->blueNoise);
     dfree(ctx->pool), dfree(ctx->triData), dfree(ctx->instGPU), dfree(ctx->tlasPrims), dfree(ctx->instTris), dfree(ctx->instInvRows);
     dfree(ctx->traceFetch), dfree(ctx->hostRaysDev), dfree(ctx->hostOutDev);
@@ -725,9 +731,14 @@ int lh2g_set_materials(lh2g_context* ctx, const lh2g_material* mats, int count) 
 int lh2g_set_lights(lh2g_context* ctx, const lh2g_light_tri* tri, int ntri, const lh2g_point_light* pt, int npt, const lh2g_spot_light* spot, int nspot,
                     const lh2g_dir_light* dir, int ndir) {
     if (!ctx || ntri < 0 || npt < 0 || nspot < 0 || ndir < 0) return LH2G_ERR_INVALID;
-    if (ntri + npt + nspot + ndir > 64) return fail(ctx, LH2G_ERR_INVALID, "set_lights: at most 64 lights (MAXISLIGHTS)");
+    if ((long long)ntri + npt + nspot > LH2G_MAX_TREE_LIGHTS || ndir > 64)
+        return fail(ctx, LH2G_ERR_INVALID, "set_lights: at most LH2G_MAX_TREE_LIGHTS area, point and spot lights and 64 directional lights");
     cudaSetDevice(ctx->device);
     JOIN();
+    const std::vector<LightTreeNode> tree = build_light_tree(tri, ntri, pt, npt, spot, nspot);
+    CK(dalloc(ctx->lightTree, (size_t)4 * std::max<size_t>(tree.size(), 1)));
+    if (!tree.empty()) CK(cudaMemcpyAsync(ctx->lightTree, tree.data(), sizeof(LightTreeNode) * tree.size(), cudaMemcpyHostToDevice, ctx->st));
+    ctx->nTreeNodes = (int)tree.size();
     CK(dalloc(ctx->triL, (size_t)6 * std::max(ntri, 1)));
     CK(dalloc(ctx->ptL, (size_t)2 * std::max(npt, 1)));
     CK(dalloc(ctx->spL, (size_t)3 * std::max(nspot, 1)));
@@ -739,6 +750,16 @@ int lh2g_set_lights(lh2g_context* ctx, const lh2g_light_tri* tri, int ntri, cons
     CK(cudaStreamSynchronize(ctx->st));
     ctx->nTri = ntri, ctx->nPt = npt, ctx->nSpot = nspot, ctx->nDir = ndir;
     return LH2G_OK;
+}
+
+int lh2g_build_light_tree(const lh2g_light_tri* tri, int ntri, const lh2g_point_light* pt, int npt, const lh2g_spot_light* spot, int nspot,
+                          void* nodes, int capacity) {
+    if (ntri < 0 || npt < 0 || nspot < 0 || (long long)ntri + npt + nspot > LH2G_MAX_TREE_LIGHTS || capacity < 0) return -LH2G_ERR_INVALID;
+    if ((ntri && !tri) || (npt && !pt) || (nspot && !spot)) return -LH2G_ERR_INVALID;
+    const std::vector<LightTreeNode> tree = build_light_tree(tri, ntri, pt, npt, spot, nspot);
+    if ((size_t)capacity < tree.size() || (!nodes && !tree.empty())) return -LH2G_ERR_OVERFLOW;
+    if (!tree.empty()) memcpy(nodes, tree.data(), sizeof(LightTreeNode) * tree.size());
+    return (int)tree.size();
 }
 
 int lh2g_set_sky(lh2g_context* ctx, const float* rgb, int w, int h, const float* m16) {
@@ -806,6 +827,9 @@ int lh2g_setting(lh2g_context* ctx, const char* name, float value) {
     else if (!strcmp(name, "bsdf")) {
         if (value != 0.0f && value != 1.0f) return fail(ctx, LH2G_ERR_INVALID, "setting bsdf: 0 (lambert.h) or 1 (disney.h)");
         ctx->bsdf = (int)value;
+    } else if (!strcmp(name, "lightTree")) {
+        if (value != 0.0f && value != 1.0f) return fail(ctx, LH2G_ERR_INVALID, "setting lightTree: 0 (potentials) or 1 (the light tree)");
+        ctx->lightTreeOn = (int)value;
     }
     else if (!strcmp(name, "waveTail")) {
         if (value < 0 || value > 65) return fail(ctx, LH2G_ERR_INVALID, "setting waveTail: 0 (off) or 1..65");
@@ -971,6 +995,10 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
     if (p->flags & LH2G_RP_ADAPTIVE) return fail(ctx, LH2G_ERR_INVALID, "render: adaptive frames go through lh2g_render_adaptive");
     if ((p->flags & LH2G_RP_DISNEY) && !(p->flags & LH2G_RP_OPTIX7))
         return fail(ctx, LH2G_ERR_INVALID, "render: the Disney BSDF belongs to the OptiX 7 estimator and adaptive frames");
+    if ((p->flags & LH2G_RP_LIGHTTREE) && !(p->flags & LH2G_RP_OPTIX7))
+        return fail(ctx, LH2G_ERR_INVALID, "render: the light tree belongs to the OptiX 7 estimator");
+    if (!(p->flags & LH2G_RP_LIGHTTREE) && ctx->nTri + ctx->nPt + ctx->nSpot + ctx->nDir > 64)
+        return fail(ctx, LH2G_ERR_INVALID, "render: more than 64 lights need the OptiX 7 estimator's light tree (LH2G_RP_LIGHTTREE)");
     if ((p->flags & LH2G_RP_OPTIX7) && (filt || nrcFrame || (p->flags & LH2G_RP_DEPTH_W)))
         return fail(ctx, LH2G_ERR_INVALID, "render: the OptiX 7 estimator combines with none of filter, radiance-cache or depth frames");
     if ((p->flags & LH2G_RP_OPTIX7) && ctx->cap >= (1ll << MIS_SLOT_BITS))
@@ -1153,6 +1181,8 @@ int render_adaptive(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_
     if ((p->flags & ~(LH2G_RP_NEE | LH2G_RP_DISNEY)) || p->rowCount != 0)
         return fail(ctx, LH2G_ERR_INVALID, "render_adaptive: only LH2G_RP_NEE and LH2G_RP_DISNEY combine with adaptive frames (whole frames)");
     if (ctx->cap >= (1ll << MIS_SLOT_BITS)) return fail(ctx, LH2G_ERR_INVALID, "render_adaptive: at most 2^26 paths per frame");
+    if (ctx->nTri + ctx->nPt + ctx->nSpot + ctx->nDir > 64)
+        return fail(ctx, LH2G_ERR_INVALID, "render_adaptive: at most 64 lights (the light tree is the OptiX 7 estimator's)");
     if (!ctx->mats) return fail(ctx, LH2G_ERR_STATE, "render: no materials");
     if (!materials_cover_meshes(ctx)) return fail(ctx, LH2G_ERR_INVALID, "render: a triangle's material index exceeds the material count");
     cudaSetDevice(ctx->device);
@@ -1464,7 +1494,7 @@ int lh2g_render(lh2g_context* ctx, const lh2g_view* view, int converge) {
         p.shift = xorshift(ctx->shiftSeed);
         p.cameraR0 = xorshift(ctx->camSeed);
         for (int d = 1; d < p.maxDepth; d++) xorshift(ctx->camSeed);
-        p.flags = (ctx->nee ? LH2G_RP_NEE : 0) | LH2G_RP_OPTIX7 | (ctx->bsdf ? LH2G_RP_DISNEY : 0);
+        p.flags = (ctx->nee ? LH2G_RP_NEE : 0) | LH2G_RP_OPTIX7 | (ctx->bsdf ? LH2G_RP_DISNEY : 0) | (ctx->lightTreeOn ? LH2G_RP_LIGHTTREE : 0);
         r = lh2g_render_ex(ctx, view, &p, ctx->samplesTaken > 0 ? 1 : 0, nullptr, nullptr, nullptr);
     } else {
         p.cameraR0 = xorshift(ctx->camSeed);

@@ -60,6 +60,8 @@ struct SceneGPU {
     const float4* spotLights;        /* 3 float4 */
     const float4* dirLights;         /* 2 float4 */
     int nTri, nPoint, nSpot, nDir;
+    const float4* lightTree;         /* light-tree records, 4 float4 each (light_tree.h); record 0 the root */
+    int nTreeNodes;
     const float4* skyPixels;
     int skyW, skyH;
     float4 worldToSky[3];            /* rows of the 3x3 part */

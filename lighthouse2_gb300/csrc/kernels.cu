@@ -540,7 +540,8 @@ void launch_extend(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, i
 }
 void launch_shade(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int depth, int blocks, cudaStream_t st) {
     if (B.order) k_partition<<<sm_count() * 4, PART_TILE, 0, st>>>(F, B, depth);
-    const int lights = std::max(1, S.nTri + S.nPoint + S.nSpot + S.nDir);   /* at most 64 (lh2g_set_lights) */
+    /* at most 64 lights select by potential (render validation); light-tree frames keep no potentials */
+    const int lights = (F.flags & LH2G_RP_LIGHTTREE) ? 1 : std::max(1, S.nTri + S.nPoint + S.nSpot + S.nDir);
     if (F.flags & MIS_FLAGS) k_shade<true><<<blocks, WAVE_BLOCK, (size_t)lights * WAVE_BLOCK * sizeof(float), st>>>(S, F, B, depth);
     else k_shade<false><<<blocks, WAVE_BLOCK, (size_t)lights * WAVE_BLOCK * sizeof(float), st>>>(S, F, B, depth);
 }

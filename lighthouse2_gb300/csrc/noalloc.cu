@@ -75,7 +75,7 @@ extern "C" LH2G_API int lh2g_render_noalloc(lh2g_context* ctx, const lh2g_view* 
     if (!ctx || !view || !p || !accumDevice) return LH2G_ERR_INVALID;
     if (p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->maxDepth < 1 || p->maxDepth > 64) return LH2G_ERR_INVALID;
     /* filter, radiance-cache and adaptive frames need the context's own buffers; this path renders the plain estimator */
-    if ((p->flags & (LH2G_RP_FILTER | LH2G_RP_NRC | LH2G_RP_OPTIX7 | LH2G_RP_ADAPTIVE | LH2G_RP_DISNEY)) || p->rowCount != 0) return LH2G_ERR_INVALID;
+    if ((p->flags & (LH2G_RP_FILTER | LH2G_RP_NRC | LH2G_RP_OPTIX7 | LH2G_RP_ADAPTIVE | LH2G_RP_DISNEY | LH2G_RP_LIGHTTREE)) || p->rowCount != 0) return LH2G_ERR_INVALID;
     const long long P = (long long)p->width * p->height * p->spp;
     if (P > LH2G_NOALLOC_MAX_PATHS) return LH2G_ERR_OVERFLOW;   /* width * height * spp above the static capacity */
     SceneGPU S;
@@ -83,6 +83,7 @@ extern "C" LH2G_API int lh2g_render_noalloc(lh2g_context* ctx, const lh2g_view* 
     const int r = context_scene(ctx, &S, &device, blocks, &tailDepth);
     if (r != LH2G_OK) return r;
     if (device < 0 || (size_t)device >= MAX_DEVICES) return LH2G_ERR_INVALID;
+    if (S.nTri + S.nPoint + S.nSpot + S.nDir > 64) return LH2G_ERR_INVALID;   /* the plain estimator selects lights by potential */
     int current = -1;
     if (cudaGetDevice(&current) != cudaSuccess) return LH2G_ERR_CUDA;
     if (current != device && cudaSetDevice(device) != cudaSuccess) return LH2G_ERR_CUDA;

@@ -1000,6 +1000,8 @@ int lh2g_server_add_scene(lh2g_server* s, lh2g_context* ctx, int* sceneId) {
     const int r = context_scene(ctx, &S, &dev, blocks, &tail);
     if (r != LH2G_OK) return sfail(s, r, "add_scene: the context has no finalized scene");
     if (dev != s->device) return sfail(s, LH2G_ERR_INVALID, "add_scene: the context is on another device");
+    if (S.nTri + S.nPoint + S.nSpot + S.nDir > 64)
+        return sfail(s, LH2G_ERR_INVALID, "add_scene: at most 64 lights (the serving loop selects lights by their potentials)");
     {
         std::lock_guard<std::mutex> g(s->mu);
         if ((int)s->scenes.size() >= MAX_SCENES) { s->err = "add_scene: at most 16 scenes"; return LH2G_ERR_OVERFLOW; }
@@ -1014,7 +1016,7 @@ int lh2g_server_add_scene(lh2g_server* s, lh2g_context* ctx, int* sceneId) {
 int lh2g_server_submit_render(lh2g_server* s, int sceneId, const lh2g_view* view, const lh2g_render_params* p, float* hostOut, long long* jobId) {
     if (!s || !view || !p || !hostOut || !jobId) return LH2G_ERR_INVALID;
     if (p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->maxDepth < 1 || p->maxDepth > 64 ||
-        (p->flags & (LH2G_RP_FILTER | LH2G_RP_NRC | LH2G_RP_OPTIX7 | LH2G_RP_ADAPTIVE | LH2G_RP_DISNEY)) || p->rowCount != 0)
+        (p->flags & (LH2G_RP_FILTER | LH2G_RP_NRC | LH2G_RP_OPTIX7 | LH2G_RP_ADAPTIVE | LH2G_RP_DISNEY | LH2G_RP_LIGHTTREE)) || p->rowCount != 0)
         return sfail(s, LH2G_ERR_INVALID, "submit_render: bad parameters (filter frames are not served)");
     const long long P = (long long)p->width * p->height * p->spp;
     Job* j = new Job();

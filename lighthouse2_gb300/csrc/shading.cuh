@@ -368,6 +368,127 @@ LH2G_DEV float3 RandomPointOnLight(const SceneGPU& S, float r0, float r1, const 
     }
 }
 
+/* ---- stochastic lightcuts through the light tree (LH2G_RP_LIGHTTREE) ----
+ * Records of 4 float4 (light_tree.h): (light, left, right, intensity), box min, box max, (normal, parent). */
+LH2G_DEV int4 tree_head(const SceneGPU& S, const int node) {
+    const float4 h = __ldg(S.lightTree + (size_t)node * 4);
+    return make_int4(__float_as_int(h.x), __float_as_int(h.y), __float_as_int(h.z), __float_as_int(h.w));
+}
+
+/* CalculateChildNodeWeights (lights_shared.h:120-156): the chance of the left child of node from I with normal N,
+ * the mean of the two bounds the distances to the children's boxes give; six numbers drawn from seed, three for a
+ * random point in each child's box (drawn x, y, z in that order, the order the CUDA compiler evaluates the
+ * reference's make_float3 arguments in). As in the reference, wmax_k takes the left child's F and intensity. */
+LH2G_DEV float light_tree_left_weight(const SceneGPU& S, const int node, const float3& I, const float3& N, uint32_t& seed) {
+    const int4 h = tree_head(S, node);
+    const int left = h.y, right = h.z;
+    const float4* tl = S.lightTree + (size_t)left * 4;
+    const float4* tr = S.lightTree + (size_t)right * 4;
+    const float3 b1j = xyz(__ldg(tl + 1)), b2j = xyz(__ldg(tl + 2));
+    const float3 b1k = xyz(__ldg(tr + 1)), b2k = xyz(__ldg(tr + 2));
+    const float3 diag_j = b2j - b1j, diag_k = b2k - b1k;
+    const float3 LN = xyz(__ldg(S.lightTree + (size_t)node * 4 + 3));
+    const float3 Bj = 0.5f * diag_j, Bk = 0.5f * diag_k;
+    const float3 Cj = (b1j + b2j) * 0.5f, Ck = (b1k + b2k) * 0.5f;
+    const float3 Dj = Cj - I, Dk = Ck - I;
+    const float3 min_j = make_float3(fmaxf(Dj.x - Bj.x, 0.0f), fmaxf(Dj.y - Bj.y, 0.0f), fmaxf(Dj.z - Bj.z, 0.0f));
+    const float3 min_k = make_float3(fmaxf(Dk.x - Bk.x, 0.0f), fmaxf(Dk.y - Bk.y, 0.0f), fmaxf(Dk.z - Bk.z, 0.0f));
+    const float dist2j = dot(min_j, min_j), dist2k = dot(min_k, min_k);
+    const float3 max_j = Dj + Bj, max_k = Dk + Bk;
+    const float dist2j_max = dot(max_j, max_j), dist2k_max = dot(max_k, max_k);
+    const float Ij = __int_as_float(tree_head(S, left).w), Ik = __int_as_float(tree_head(S, right).w);
+    const float rj0 = RandomFloat(seed), rj1 = RandomFloat(seed), rj2 = RandomFloat(seed);
+    const float3 Rj = b1j + (b2j - b1j) * make_float3(rj0, rj1, rj2);
+    const float rk0 = RandomFloat(seed), rk1 = RandomFloat(seed), rk2 = RandomFloat(seed);
+    const float3 Rk = b1k + (b2k - b1k) * make_float3(rk0, rk1, rk2);
+    const float3 Lj = normalize(Rj - I), Lk = normalize(Rk - I);
+    float Fj = fmaxf(0.001f, dot(N, Lj)), Fk = fmaxf(0.001f, dot(N, Lk));
+    if (dot(LN, LN) > 0.001f) Fj *= fmaxf(0.001f, dot(LN, Lj * -1.0f)), Fk *= fmaxf(0.001f, dot(LN, Lk * -1.0f));
+    const bool insideBoth = dist2j == 0 && dist2k == 0;
+    const float wmin_j = (Fj * Ij) / (insideBoth ? 1.0f : fmaxf(0.0001f, dist2j));
+    const float wmin_k = (Fk * Ik) / (insideBoth ? 1.0f : fmaxf(0.0001f, dist2k));
+    const float wmax_j = (Fj * Ij) / fmaxf(0.0001f, dist2j_max);
+    const float wmax_k = (Fj * Ij) / fmaxf(0.0001f, dist2k_max);
+    const float pmin_j = wmin_j / (wmin_j + wmin_k);
+    const float pmax_j = wmax_j / (wmax_j + wmax_k);
+    return 0.5f * (pmin_j + pmax_j);
+}
+
+/* LightPickProbLTree (lights_shared.h:198-217): the chance that the tree picks area light idx, the product of the
+ * branch chances from its leaf (record idx + 1) up to the root, the weights taken at I (the light point, as the
+ * reference passes it) with normal N. A leaf without a parent (a one-light tree: the reference would read
+ * record -1) ends the walk. */
+LH2G_DEV float light_pick_prob_tree(const SceneGPU& S, const int idx, const float3& N, const float3& I, uint32_t& seed) {
+    int node = idx + 1;
+    float pickProb = 1;
+    for (int guard = 0; guard < S.nTreeNodes && node > 0 && node < S.nTreeNodes; guard++) {
+        const int parent = __float_as_int(__ldg(S.lightTree + (size_t)node * 4 + 3).w);
+        if (parent < 0) break;
+        const float p = light_tree_left_weight(S, parent, I, N, seed);
+        if (tree_head(S, parent).y == node) pickProb *= p; else pickProb *= 1 - p;
+        node = parent;
+    }
+    return pickProb;
+}
+
+/* RandomPointOnLightLTree (lights_shared.h:322-395): walk from the root, at each interior node to the left child
+ * with its weight's chance (r1 rescaled to the chosen branch), then a point on the leaf's light as
+ * RandomPointOnLight does. picked: the light's index over area, point and spot lights. A scene without tree lights
+ * gives lightPdf 0. */
+LH2G_DEV float3 RandomPointOnLightTree(const SceneGPU& S, float r0, float r1, uint32_t& seed, const float3& I, const float3& N, float& pickProb,
+                                       float& lightPdf, float3& lightColor, int& picked) {
+    pickProb = 1;
+    if (S.nTreeNodes <= 0) { lightPdf = 0; return mk3(1); }
+    int node = 0, lightIdx = 0;
+    for (int guard = 0; guard <= S.nTreeNodes; guard++) {
+        const int4 h = tree_head(S, node);
+        if (h.y == -1) { lightIdx = h.x; break; }
+        const float p_j = light_tree_left_weight(S, node, I, N, seed);
+        if (r1 < p_j) node = h.y, r1 *= 1.0f / p_j, pickProb *= p_j;
+        else node = h.z, r1 = (r1 - p_j) / (1 - p_j), pickProb *= 1 - p_j;
+    }
+    if (lightIdx & (1 << 30)) {
+        const int k = lightIdx - (1 << 30);
+        picked = S.nTri + k;
+        const float4* l = S.pointLights + (size_t)k * 2;
+        const float4 p = __ldg(l), r = __ldg(l + 1);
+        const float3 P = xyz(p);
+        const float3 L = P - I;
+        const float sqDist = dot(L, L);
+        lightColor = xyz(r) / sqDist;
+        lightPdf = dot(L, N) > 0 ? 1.0f : 0.0f;
+        return P;
+    } else if (lightIdx & (1 << 29)) {
+        const int k = lightIdx - (1 << 29);
+        picked = S.nTri + S.nPoint + k;
+        const float4* l = S.spotLights + (size_t)k * 3;
+        const float4 V0 = __ldg(l), V1 = __ldg(l + 1), Dd = __ldg(l + 2);
+        const float3 P = xyz(V0);
+        float3 L = I - P;
+        const float sqDist = dot(L, L);
+        L = normalize(L);
+        const float d = (fmaxf(0.0f, L.x * Dd.x + L.y * Dd.y + L.z * Dd.z) - V1.w) / (V0.w - V1.w);
+        const float LNdotL = fminf(1.0f, d);
+        lightPdf = (LNdotL > 0 && dot(L, N) < 0) ? (sqDist / LNdotL) : 0;
+        lightColor = xyz(V1);
+        return P;
+    } else {
+        picked = lightIdx;
+        const float3 bary = RandomBarycentrics(r0);
+        const float4* l = S.triLights + (size_t)lightIdx * 6;
+        const float4 n4 = __ldg(l + 1), r4 = __ldg(l + 2), v0 = __ldg(l + 3), v1 = __ldg(l + 4), v2 = __ldg(l + 5);
+        lightColor = xyz(r4);
+        const float3 P = bary.x * xyz(v0) + bary.y * xyz(v1) + bary.z * xyz(v2);
+        float3 L = I - P;
+        const float sqDist = dot(L, L);
+        L = normalize(L);
+        const float LNdotL = L.x * n4.x + L.y * n4.y + L.z * n4.z;
+        const float reciSolidAngle = sqDist / (n4.w * LNdotL);
+        lightPdf = (LNdotL > 0 && dot(L, N) < 0) ? reciSolidAngle : 0;
+        return P;
+    }
+}
+
 LH2G_DEV float3 SampleSkydome(const SceneGPU& S, const float3& Dw) {
     if (S.skyW <= 0 || S.skyH <= 0) return mk3(0);
     const float4 m0 = S.worldToSky[0], m1 = S.worldToSky[1], m2 = S.worldToSky[2];

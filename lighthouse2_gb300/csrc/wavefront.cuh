@@ -486,7 +486,13 @@ __device__ __forceinline__ void shade_mis(const SceneGPU& S, const FrameGPU& F, 
                 const float4 tv = __ldg(S.instTris[INST] + (size_t)PRIM * 13 + 5);   /* T, area */
                 const float lightPdf = (HIT_T * HIT_T) / (fabsf(dot(D, N)) * tv.w);
                 const int ltri = __float_as_int(__ldg(S.instTris[INST] + (size_t)PRIM * 13).w);
-                const float pickProb = light_pick_prob(S, ltri, O, lastN, I);
+                float pickProb;
+                if (F.flags & LH2G_RP_LIGHTTREE) {   /* the shading seed, as the reference draws it before this branch */
+                    uint32_t seed = WangHash(pathIdx * 17u + xorshift_n(F.cameraR0, depth - 1) + (uint32_t)depth * 91771u);
+                    pickProb = light_pick_prob_tree(S, ltri, lastN, I, seed);
+                } else {
+                    pickProb = light_pick_prob(S, ltri, O, lastN, I);
+                }
                 if ((bsdfPdf + lightPdf * pickProb) > 0) contribution = throughput * sd.color * (1.0f / (bsdfPdf + lightPdf * pickProb));
             }
             clamp_intensity(contribution, F.clampValue);
@@ -518,7 +524,9 @@ __device__ __forceinline__ void shade_mis(const SceneGPU& S, const FrameGPU& F, 
         float pickProb = 0, lightPdf = 0;
         float3 lightColor = mk3(0);
         int picked = 0;
-        float3 L = RandomPointOnLight(S, r4.x, r4.y, I, fN * faceDir, pickProb, lightPdf, lightColor, pot, WAVE_BLOCK, picked) - I;
+        float3 L = ((F.flags & LH2G_RP_LIGHTTREE) ? RandomPointOnLightTree(S, r4.x, r4.y, seed, I, fN * faceDir, pickProb, lightPdf, lightColor, picked)
+                                                  : RandomPointOnLight(S, r4.x, r4.y, I, fN * faceDir, pickProb, lightPdf, lightColor, pot, WAVE_BLOCK,
+                                                                       picked)) - I;
         const float dist = length(L);
         L = L * (1.0f / dist);
         const float NdotL = dot(L, fN * faceDir);

@@ -384,6 +384,62 @@ def cornell_sphere(seed=1, subdiv=6):
     return s
 
 
+def lit_room(seed=11, grid=8, n_points=24, n_spots=12, subdiv=3):
+    """The Cornell room and displaced icosphere lit by many lights (for the light tree): a grid x grid array of
+    small ceiling quads (2 grid^2 area lights, seeded colours), n_points point lights and n_spots downward spot
+    lights at seeded positions. The defaults give 164 lights, beyond the 64 that selection by potentials takes."""
+    rng = np.random.default_rng(seed)
+    mats = np.zeros(8 + grid * grid, dtype=MATERIAL_DTYPE)
+    for i in range(8):
+        m = empty_material()
+        m["color"] = rng.uniform(0.1, 0.9, 3)
+        m["roughness"] = 0.75
+        m["flags"] = 1
+        mats[i] = m
+    radiance = rng.uniform(2.0, 12.0, (grid * grid, 3)).astype(np.float32)
+    for k in range(grid * grid):
+        lm = empty_material()
+        lm["color"] = radiance[k]
+        mats[8 + k] = lm
+    q = [add_quad((0, 1, 0), (0, 0, 0), 2, 2, 0), add_quad((0, -1, 0), (0, 2, 0), 2, 2, 1), add_quad((0, 0, 1), (0, 1, -1), 2, 2, 2),
+         add_quad((0, 0, -1), (0, 1, 1), 2, 2, 3), add_quad((1, 0, 0), (-1, 1, 0), 2, 2, 4), add_quad((-1, 0, 0), (1, 1, 0), 2, 2, 5)]
+    cell = 1.6 / grid
+    for gz in range(grid):
+        for gx in range(grid):
+            q.append(add_quad((0, -1, 0), (-0.8 + (gx + 0.5) * cell, 1.98, -0.8 + (gz + 0.5) * cell), 0.5 * cell, 0.5 * cell, 8 + gz * grid + gx))
+    room = _concat(q)
+    first = 12
+    nl = 2 * grid * grid
+    room[3]["ltriIdx"][first:first + nl] = np.arange(nl)
+    verts, faces = icosphere(subdiv)
+    sph = _smooth_mesh(verts, faces, seed + 100, 0.35, np.array([0.3, 0.45, -0.25], np.float32), 0)
+    sph[3]["material"] = rng.integers(0, 8, len(sph[3]))
+    sc = Scene()
+    sc.meshes = [_mesh(*room), _mesh(*sph)]
+    sc.materials = mats
+    ident = np.eye(4, dtype=np.float32)
+    sc.instances = [(0, ident), (1, ident)]
+    lt = make_light_tris(room[0][first:first + nl], room[1][first:first + nl], room[2][first:first + nl], room[3][first:first + nl],
+                         (1.0, 1.0, 1.0), 0, first)
+    lt["radiance"] = np.repeat(radiance, 2, axis=0)
+    lt["energy"] = (lt["radiance"] * lt["area"][:, None]).sum(1)
+    sc.tri_lights = lt
+    pl = np.zeros(n_points, POINT_LIGHT_DTYPE)
+    pl["position"] = rng.uniform((-0.9, 0.2, -0.9), (0.9, 1.8, 0.9), (n_points, 3))
+    pl["radiance"] = rng.uniform(0.05, 0.4, (n_points, 3))
+    pl["energy"] = pl["radiance"].sum(1)
+    sc.point_lights = pl
+    sp = np.zeros(n_spots, SPOT_LIGHT_DTYPE)
+    sp["position"] = rng.uniform((-0.8, 1.5, -0.8), (0.8, 1.9, 0.8), (n_spots, 3))
+    sp["radiance"] = rng.uniform(0.5, 3.0, (n_spots, 3))
+    sp["direction"] = (0.0, -1.0, 0.0)
+    sp["cosInner"], sp["cosOuter"] = 0.95, 0.8
+    sc.spot_lights = sp
+    sc.dir_lights = np.zeros(0, DIR_LIGHT_DTYPE)
+    sc.bounds = (np.array([-1, 0, -1], np.float32), np.array([1, 2, 1], np.float32))
+    return sc
+
+
 def cornell_view(width=512, height=512, frame=0):
     """Camera in the open side of the room; frame > 0 moves it along a short seeded-free dolly (for the filter)."""
     return make_view((0.02 * frame, 1.0 - 0.01 * frame, 0.95), (0.0, 0.9, -1.0), 65.0, width, height)

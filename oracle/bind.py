@@ -26,7 +26,7 @@ PARAMS_DTYPE = np.dtype([("width", "<i4"), ("height", "<i4"), ("spp", "<i4"), ("
 FILTER_PARAMS_DTYPE = np.dtype([("prevView", S.VIEW_DTYPE), ("j0", "<f4"), ("j1", "<f4"), ("prevj0", "<f4"), ("prevj1", "<f4"),
                                 ("clampDirect", "<f4"), ("clampIndirect", "<f4"), ("samplesTaken", "<i4"),
                                 ("camIsStationary", "<i4"), ("taa", "<i4")])
-RP_NEE, RP_DEPTH_W, RP_FILTER, RP_OPTIX7, RP_ADAPTIVE, RP_DISNEY = 1, 2, 4, 16, 32, 64
+RP_NEE, RP_DEPTH_W, RP_FILTER, RP_OPTIX7, RP_ADAPTIVE, RP_DISNEY, RP_LIGHTTREE = 1, 2, 4, 16, 32, 64, 128
 
 
 def build_oracle():
@@ -122,6 +122,17 @@ class Oracle:
             assert L.lh2o_set_sky(s, _p(rgb), w, h, None) == 0
         self.set_blue_noise(sc.blue_noise)
         assert L.lh2o_finalize(s) == 0
+
+    def light_tree(self):
+        """The light tree lh2o_set_lights built for the scene's lights (LIGHT_TREE_DTYPE records, record 0 the root)."""
+        fn = self.lib.lh2o_light_tree
+        fn.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+        n = fn(self.s, None, 0)
+        if n <= 0:
+            return np.zeros(0, LIGHT_TREE_DTYPE)
+        out = np.zeros(n, LIGHT_TREE_DTYPE)
+        assert fn(self.s, _p(out), n) == n
+        return out
 
     def set_blue_noise(self, tables):
         if tables is None:
@@ -484,20 +495,42 @@ def reference_blue_noise():
     return tuple(out)
 
 
+LIGHT_TREE_DTYPE = np.dtype([("light", "<i4"), ("left", "<i4"), ("right", "<i4"), ("intensity", "<f4"), ("bmin", "<f4", 4),
+                             ("bmax", "<f4", 4), ("N", "<f4", 3), ("parent", "<i4")])
+
+
+def ref_light_tree(lib, tri, point, spot):
+    """The light tree the reference's RenderCore::UpdateLightTree (rendercore_optix7/rendercore.cpp:625-680, compiled
+    here by oracle/ref) builds for these lights: LIGHT_TREE_DTYPE records, record 0 the root."""
+    fn = lib.ref_light_tree
+    fn.argtypes = [C.c_void_p, C.c_int] * 3 + [C.c_void_p, C.c_int]
+    cap = 2 * (len(tri) + len(point) + len(spot))
+    out = np.zeros(max(cap, 1), LIGHT_TREE_DTYPE)
+    n = fn(_p(tri) if len(tri) else None, len(tri), _p(point) if len(point) else None, len(point),
+           _p(spot) if len(spot) else None, len(spot), _p(out), cap)
+    assert n >= 0, "ref_light_tree: capacity"
+    return out[:n]
+
+
 class RefOptix7(RefKernels):
     """The OptiX 7 core's shading kernel and ray generation compiled for the host (oracle/ref/ref_optix7.cpp), driven
     through the core's wave loop (lib/rendercore_optix7/rendercore.cpp:874-922) with the oracle answering the ray
     queries. The connection buffer is made large enough that the loop's early flush (rendercore.cpp:906-913) never
     triggers."""
 
-    def __init__(self, disney=False):
-        """disney: the kernel built with the Disney BSDF (ref_o7d_*) instead of lambert.h (ref_o7_*)."""
+    def __init__(self, disney=False, light_tree=False):
+        """disney: the kernel built with the Disney BSDF (ref_o7d_*) instead of lambert.h (ref_o7_*); light_tree: the
+        kernel built with its light-tree calls and LIGHTTREE defined (ref_o7t_*, Lambert BSDF), reading the tree
+        the reference's own UpdateLightTree builds (ref_light_tree)."""
         super().__init__()
         vp, i, f, u = C.c_void_p, C.c_int, C.c_float, C.c_uint32
-        pre = "ref_o7d_" if disney else "ref_o7_"
+        pre = "ref_o7t_" if light_tree else ("ref_o7d_" if disney else "ref_o7_")
+        self.light_tree = light_tree
         sig = {"set_scene": [vp] * 2 + [vp, i] * 4 + [vp, f, f, i, vp, i, i, vp], "init_counters": [i], "next_counters": [],
                "counters": [vp], "generate": [vp, i, i, i, i, i, vp, f, vp, vp, vp, f], "shade": [i, vp, vp, vp, vp, u, u, i, i, i, i, i, f, i],
                "finalize_connections": [i, vp, vp, vp, i], "bluenoise4": [vp, i, i, i, i, vp], "set_shadow_count": [u]}
+        if light_tree:
+            sig["set_light_tree"] = [vp]
 
         class _Fns:
             pass
@@ -522,6 +555,10 @@ class RefOptix7(RefKernels):
         L.set_scene(_p(inst), _p(packed), _p(sc.tri_lights), len(sc.tri_lights), _p(sc.point_lights), len(sc.point_lights),
                            _p(sc.spot_lights), len(sc.spot_lights), _p(sc.dir_lights), len(sc.dir_lights), _p(texels), eps,
                            float(params["clampValue"]), D, _p(sky4), sw, sh, _p(bn))
+        if self.light_tree:
+            tree = ref_light_tree(self.lib, sc.tri_lights, sc.point_lights, sc.spot_lights)
+            self._keep.append(tree)
+            L.set_light_tree(_p(tree))
         ps = np.zeros((3 * P, 4), np.float32)
         hits = np.zeros((P, 4), np.float32)
         conn = np.zeros((6 * P, 4), np.float32)           # O4, D4, E4 at 0, 2 P, 4 P (rendercore.cpp:312)

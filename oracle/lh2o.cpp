@@ -337,6 +337,10 @@ struct Sky { std::vector<f3> px; int w = 0, h = 0; float m[16]; std::vector<f3> 
 
 }  // namespace
 
+/* one record of the light tree (the device LightCluster, common_classes.h:522-527; the parent in the normal's w) */
+struct LtCluster { int light, left, right; float intensity; float bmin[4], bmax[4]; float N[3]; int parent; };
+static_assert(sizeof(LtCluster) == 64, "the device record");
+
 struct lh2o_scene {
     std::vector<Mesh> meshes;
     std::vector<Instance> inst;
@@ -348,6 +352,7 @@ struct lh2o_scene {
     std::vector<lh2g_point_light> pointLights;
     std::vector<lh2g_spot_light> spotLights;
     std::vector<lh2g_dir_light> dirLights;
+    std::vector<LtCluster> lightTree;   /* built by lh2o_set_lights (the light tree) */
     Sky sky;
     BVH2 top;
     bool finalized = false;
@@ -2106,6 +2111,205 @@ float LightPickProb(const lh2o_scene* s, int idx, const f3& O, const f3& N, cons
     return (idx >= 0 && idx < lights) ? potential[idx] / sum : 0.0f;
 }
 
+/* ------------------------------------------------------------------------------------------------------
+ * the stochastic-lightcuts light tree (LH2G_RP_LIGHTTREE)
+ * build: RenderCore::UpdateLightTree / FindBestMatch / UpdateLightTreeNormals, rendercore_optix7/rendercore.cpp:571-680,
+ *   with the LightCluster constructors and Cost of common_classes.h:487-514; a leaf box starts empty (the
+ *   reference grows a box nothing initialised);
+ * use: CalculateChildNodeWeights, LightPickProbLTree, RandomPointOnLightLTree, lights_shared.h:120-156, 198-217,
+ *   322-395 (the three point draws of a child box in x, y, z order, as the CUDA compiler evaluates make_float3's
+ *   arguments); a parentless leaf (a one-light tree) ends LightPickProbLTree's walk.
+ * ---------------------------------------------------------------------------------------------------- */
+
+static LtCluster lt_cluster(int light, float intensity) {
+    LtCluster c;
+    c.light = light, c.left = -1, c.right = -1, c.intensity = intensity;
+    for (int k = 0; k < 4; k++) c.bmin[k] = 1e34f, c.bmax[k] = -1e34f;   /* aabb::Reset */
+    c.N[0] = c.N[1] = c.N[2] = 0, c.parent = -1;
+    return c;
+}
+/* aabb::Grow: _mm_min_ps(bmin, p) / _mm_max_ps(bmax, p), lane by lane, p's w 0 */
+static void lt_grow(LtCluster& c, const float* lo, const float* hi) {
+    for (int k = 0; k < 4; k++) {
+        c.bmin[k] = c.bmin[k] < lo[k] ? c.bmin[k] : lo[k];
+        c.bmax[k] = c.bmax[k] > hi[k] ? c.bmax[k] : hi[k];
+    }
+}
+static void lt_grow_p(LtCluster& c, float x, float y, float z) { const float p[4] = {x, y, z, 0}; lt_grow(c, p, p); }
+static float lt_cost(const LtCluster& c) {
+    const f3 d = mk3(c.bmax[0] - c.bmin[0], c.bmax[1] - c.bmin[1], c.bmax[2] - c.bmin[2]);
+    return c.intensity * dot(d, d);
+}
+static int lt_find_best_match(const std::vector<LtCluster>& t, const int* todo, int idx, int n) {
+    float bestCost = 1e34f;
+    int bestIdx = 0;
+    for (int i = 0; i < n; i++)
+        if (i != idx) {
+            LtCluster tmp = t[todo[idx]];
+            lt_grow(tmp, t[todo[i]].bmin, t[todo[i]].bmax);
+            tmp.intensity += t[todo[i]].intensity;
+            const float cost = lt_cost(tmp);
+            if (cost < bestCost) bestCost = cost, bestIdx = i;
+        }
+    return bestIdx;
+}
+static void lt_normals(std::vector<LtCluster>& t, const lh2o_scene* s, int node) {
+    LtCluster& c = t[node];
+    if (c.left > -1) {
+        lt_normals(t, s, c.left);
+        lt_normals(t, s, c.right);
+        const f3 Nl = ld3(t[c.left].N), Nr = ld3(t[c.right].N);
+        const f3 n = dot(Nl, Nr) > 0.9f ? normalize(Nl + Nr) : mk3(0);
+        c.N[0] = n.x, c.N[1] = n.y, c.N[2] = n.z;
+        t[c.left].parent = t[c.right].parent = node;
+    } else if (c.light & ((1 << 30) + (1 << 29))) {
+        c.N[0] = c.N[1] = c.N[2] = 0;
+    } else {
+        memcpy(c.N, s->triLights[c.light].N, sizeof c.N);
+    }
+}
+static std::vector<LtCluster> lt_build(const lh2o_scene* s) {
+    const int Nt = (int)s->triLights.size(), M = (int)s->pointLights.size(), O = (int)s->spotLights.size();
+    std::vector<LtCluster> t((size_t)(Nt + M + O) * 2, lt_cluster(-1, 0));
+    if (Nt + M + O == 0) return t;
+    std::vector<int> todo((size_t)(Nt + M + O));
+    for (int i = 0; i < Nt; i++) {
+        const lh2g_light_tri& l = s->triLights[i];
+        LtCluster c = lt_cluster(i, l.energy);
+        lt_grow_p(c, l.vertex0[0], l.vertex0[1], l.vertex0[2]);
+        lt_grow_p(c, l.vertex1[0], l.vertex1[1], l.vertex1[2]);
+        lt_grow_p(c, l.vertex2[0], l.vertex2[1], l.vertex2[2]);
+        t[i + 1] = c, todo[i] = i + 1;
+    }
+    for (int i = 0; i < M; i++) {
+        const float* p = s->pointLights[i].position;
+        LtCluster c = lt_cluster(i | (1 << 30), s->pointLights[i].energy);
+        lt_grow_p(c, p[0] - 0.001f, p[1] - 0.001f, p[2] - 0.001f);
+        lt_grow_p(c, p[0] + 0.001f, p[1] + 0.001f, p[2] + 0.001f);
+        t[i + 1 + Nt] = c, todo[i + Nt] = i + 1 + Nt;
+    }
+    for (int i = 0; i < O; i++) {
+        const lh2g_spot_light& l = s->spotLights[i];
+        LtCluster c = lt_cluster(i | (1 << 29), l.radiance[0] + l.radiance[1] + l.radiance[2]);
+        lt_grow_p(c, l.position[0] - 0.001f, l.position[1] - 0.001f, l.position[2] - 0.001f);
+        lt_grow_p(c, l.position[0] + 0.001f, l.position[1] + 0.001f, l.position[2] + 0.001f);
+        t[i + 1 + Nt + M] = c, todo[i + Nt + M] = i + 1 + Nt + M;
+    }
+    int remaining = Nt + M + O, N = Nt + M + O;
+    int A = 0, B = lt_find_best_match(t, todo.data(), A, remaining);
+    while (remaining > 1) {
+        const int C = lt_find_best_match(t, todo.data(), B, remaining);
+        if (A == C) {
+            t[N + 1] = t[todo[A]];
+            lt_grow(t[N + 1], t[todo[B]].bmin, t[todo[B]].bmax);
+            t[N + 1].intensity += t[todo[B]].intensity;
+            t[N + 1].left = todo[A], t[N + 1].right = todo[B];
+            for (int i = A; i < remaining - 1; i++) todo[i] = todo[i + 1];
+            if (B > A) B--;
+            for (int i = B; i < remaining - 2; i++) todo[i] = todo[i + 1];
+            remaining -= 2;
+            todo[remaining] = ++N;
+            A = remaining++;
+            B = lt_find_best_match(t, todo.data(), A, remaining);
+        } else {
+            A = B, B = C;
+        }
+    }
+    t[0] = t[todo[0]];
+    lt_normals(t, s, 0);
+    return t;
+}
+
+static f3 lt_min3(const LtCluster& c) { return mk3(c.bmin[0], c.bmin[1], c.bmin[2]); }
+static f3 lt_max3(const LtCluster& c) { return mk3(c.bmax[0], c.bmax[1], c.bmax[2]); }
+float CalculateChildNodeWeights(const std::vector<LtCluster>& tree, const int node, const f3& I, const f3& N, uint& seed) {
+    const int left = tree[node].left, right = tree[node].right;
+    const f3 b1j = lt_min3(tree[left]), b1k = lt_min3(tree[right]);
+    const f3 b2j = lt_max3(tree[left]), b2k = lt_max3(tree[right]);
+    const f3 diag_j = b2j - b1j, diag_k = b2k - b1k;
+    const f3 LN = ld3(tree[node].N);
+    const f3 Bj = 0.5f * diag_j, Bk = 0.5f * diag_k;
+    const f3 Cj = (b1j + b2j) * 0.5f, Ck = (b1k + b2k) * 0.5f;
+    const f3 Dj = Cj - I, Dk = Ck - I;
+    const f3 min_j = mk3(fmaxr(Dj.x - Bj.x, 0.0f), fmaxr(Dj.y - Bj.y, 0.0f), fmaxr(Dj.z - Bj.z, 0.0f));
+    const f3 min_k = mk3(fmaxr(Dk.x - Bk.x, 0.0f), fmaxr(Dk.y - Bk.y, 0.0f), fmaxr(Dk.z - Bk.z, 0.0f));
+    const float dist2j = dot(min_j, min_j), dist2k = dot(min_k, min_k);
+    const f3 max_j = Dj + Bj, max_k = Dk + Bk;
+    const float dist2j_max = dot(max_j, max_j), dist2k_max = dot(max_k, max_k);
+    const float Ij = tree[left].intensity, Ik = tree[right].intensity;
+    const float a0 = RandomFloat(seed), a1 = RandomFloat(seed), a2 = RandomFloat(seed);
+    const f3 Rj = b1j + (b2j - b1j) * mk3(a0, a1, a2);
+    const float c0 = RandomFloat(seed), c1 = RandomFloat(seed), c2 = RandomFloat(seed);
+    const f3 Rk = b1k + (b2k - b1k) * mk3(c0, c1, c2);
+    const f3 Lj = normalize(Rj - I), Lk = normalize(Rk - I);
+    float Fj = fmaxr(0.001f, dot(N, Lj)), Fk = fmaxr(0.001f, dot(N, Lk));
+    if (dot(LN, LN) > 0.001f) Fj *= fmaxr(0.001f, dot(LN, Lj * -1.0f)), Fk *= fmaxr(0.001f, dot(LN, Lk * -1.0f));
+    const bool insideBoth = dist2j == 0 && dist2k == 0;
+    const float wmin_j = (Fj * Ij) / (insideBoth ? 1.0f : fmaxr(0.0001f, dist2j));
+    const float wmin_k = (Fk * Ik) / (insideBoth ? 1.0f : fmaxr(0.0001f, dist2k));
+    const float wmax_j = (Fj * Ij) / fmaxr(0.0001f, dist2j_max);
+    const float wmax_k = (Fj * Ij) / fmaxr(0.0001f, dist2k_max);   /* sic: the left child's F and I */
+    const float pmin_j = wmin_j / (wmin_j + wmin_k);
+    const float pmax_j = wmax_j / (wmax_j + wmax_k);
+    return 0.5f * (pmin_j + pmax_j);
+}
+float LightPickProbLTree(const std::vector<LtCluster>& tree, int idx, const f3& N, const f3& I, uint& seed) {
+    int node = idx + 1;
+    float pickProb = 1;
+    while (node != 0) {
+        const int parent = tree[node].parent;
+        if (parent < 0) break;
+        const float p = CalculateChildNodeWeights(tree, parent, I, N, seed);
+        if (tree[parent].left == node) pickProb *= p; else pickProb *= 1 - p;
+        node = parent;
+    }
+    return pickProb;
+}
+f3 RandomPointOnLightLTree(const lh2o_scene* s, const std::vector<LtCluster>& tree, float r0, float r1, uint& seed, const f3& I, const f3& N,
+                           float& pickProb, float& lightPdf, f3& lightColor) {
+    pickProb = 1;
+    if (tree.empty()) { lightPdf = 0; return mk3(1); }
+    int node = 0, lightIdx = 0;
+    while (true) {
+        if (tree[node].left == -1) { lightIdx = tree[node].light; break; }
+        const float p_j = CalculateChildNodeWeights(tree, node, I, N, seed);
+        if (r1 < p_j) node = tree[node].left, r1 *= 1.0f / p_j, pickProb *= p_j;
+        else node = tree[node].right, r1 = (r1 - p_j) / (1 - p_j), pickProb *= 1 - p_j;
+    }
+    if (lightIdx & (1 << 30)) {
+        const lh2g_point_light& l = s->pointLights[lightIdx - (1 << 30)];
+        const f3 P = ld3(l.position);
+        const f3 L = P - I;
+        const float sqDist = dot(L, L);
+        lightColor = ld3(l.radiance) / sqDist;
+        lightPdf = dot(L, N) > 0 ? 1.0f : 0.0f;
+        return P;
+    } else if (lightIdx & (1 << 29)) {
+        const lh2g_spot_light& l = s->spotLights[lightIdx - (1 << 29)];
+        const f3 P = ld3(l.position);
+        f3 L = I - P;
+        const float sqDist = dot(L, L);
+        L = normalize(L);
+        const float d = (fmaxr(0.0f, L.x * l.direction[0] + L.y * l.direction[1] + L.z * l.direction[2]) - l.cosOuter) / (l.cosInner - l.cosOuter);
+        const float LNdotL = fminr(1.0f, d);
+        lightPdf = (LNdotL > 0 && dot(L, N) < 0) ? (sqDist / LNdotL) : 0;
+        lightColor = ld3(l.radiance);
+        return P;
+    } else {
+        const f3 bary = RandomBarycentrics(r0);
+        const lh2g_light_tri& l = s->triLights[lightIdx];
+        lightColor = ld3(l.radiance);
+        const f3 P = bary.x * ld3(l.vertex0) + bary.y * ld3(l.vertex1) + bary.z * ld3(l.vertex2);
+        f3 L = I - P;
+        const float sqDist = dot(L, L);
+        L = normalize(L);
+        const float LNdotL = L.x * l.N[0] + L.y * l.N[1] + L.z * l.N[2];
+        const float reciSolidAngle = sqDist / (l.area * LNdotL);
+        lightPdf = (LNdotL > 0 && dot(L, N) < 0) ? reciSolidAngle : 0;
+        return P;
+    }
+}
+
 inline void add4(float* a, const f4& v) { a[0] += v.x, a[1] += v.y, a[2] += v.z, a[3] += v.w; }
 
 /* CLAMPINTENSITY (core_settings.h:191-194) and FIXNAN_FLOAT3 (common_settings.h:66) */
@@ -2191,7 +2395,13 @@ void trace_path_mis(const Frame& F, const int flavor, const uint pathIdx, const 
                 } else {
                     const f3 lastN = UnpackNormal(packedNormal);
                     const float lightPdf = CalculateLightPDF(D, HIT_T, tri.area, N);
-                    const float pickProb = LightPickProb(s, tri.ltriIdx, O, lastN, I);
+                    float pickProb;
+                    if (p.flags & LH2G_RP_LIGHTTREE) {   /* the shading seed, drawn before this branch in the reference */
+                        uint seed = WangHash(pathIdx * 17u + R0(pathLength));
+                        pickProb = LightPickProbLTree(s->lightTree, tri.ltriIdx, lastN, I, seed);
+                    } else {
+                        pickProb = LightPickProb(s, tri.ltriIdx, O, lastN, I);
+                    }
                     if ((bsdfPdf + lightPdf * pickProb) > 0) contribution = throughput * sd.color * (1.0f / (bsdfPdf + lightPdf * pickProb));
                 }
                 clamp_intensity(contribution, p.clampValue);
@@ -2219,7 +2429,8 @@ void trace_path_mis(const Frame& F, const int flavor, const uint pathIdx, const 
         if ((FLAGS & S_SPECULAR) == 0 && nee) {
             float pickProb = 0, lightPdf = 0;
             f3 lightColor = mk3(0);
-            f3 L = RandomPointOnLight(s, r4.x, r4.y, I, fN * faceDir, pickProb, lightPdf, lightColor) - I;
+            f3 L = ((p.flags & LH2G_RP_LIGHTTREE) ? RandomPointOnLightLTree(s, s->lightTree, r4.x, r4.y, seed, I, fN * faceDir, pickProb, lightPdf, lightColor)
+                                                  : RandomPointOnLight(s, r4.x, r4.y, I, fN * faceDir, pickProb, lightPdf, lightColor)) - I;
             const float dist = length(L);
             L = L * (1.0f / dist);
             const float NdotL = dot(L, fN * faceDir);
@@ -2608,12 +2819,24 @@ int lh2o_set_textures(lh2o_scene* s, const lh2g_texture* tex, int count) {
 
 int lh2o_set_lights(lh2o_scene* s, const lh2g_light_tri* tri, int ntri, const lh2g_point_light* pt, int npt,
                     const lh2g_spot_light* spot, int nspot, const lh2g_dir_light* dir, int ndir) {
-    if (!s || ntri + npt + nspot + ndir > 64) return 1;
+    if (!s || ntri < 0 || npt < 0 || nspot < 0 || ndir < 0 || (long long)ntri + npt + nspot > (1 << 20) || ndir > 64) return 1;
     s->triLights.assign(tri, tri + ntri);
     s->pointLights.assign(pt, pt + npt);
     s->spotLights.assign(spot, spot + nspot);
     s->dirLights.assign(dir, dir + ndir);
+    s->lightTree = lt_build(s);
     return 0;
+}
+
+/* the light tree of the scene's lights: 2 * (area + point + spot lights) records of 16 words (the device
+ * LightCluster); returns the record count (out null: only the count), or -1 when out holds fewer than that
+ * (capacity in records) */
+int lh2o_light_tree(const lh2o_scene* s, void* out, int capacity) {
+    if (!s) return -1;
+    if (!out) return (int)s->lightTree.size();
+    if (capacity < (int)s->lightTree.size()) return -1;
+    if (!s->lightTree.empty()) memcpy(out, s->lightTree.data(), sizeof(LtCluster) * s->lightTree.size());
+    return (int)s->lightTree.size();
 }
 
 int lh2o_set_sky(lh2o_scene* s, const float* rgb, int w, int h, const float* m16) {
@@ -2767,6 +2990,8 @@ static int render_optix7(lh2o_scene* s, const lh2g_view* view, const lh2g_render
 int lh2o_render_ex(lh2o_scene* s, const lh2g_view* view, const lh2g_render_params* p, float* pixelAccum, double* pixelAccum64,
                    uint32_t* counters, lh2g_capture* capture, const lh2o_features* feat, int nthreads) {
     if (!s || !s->finalized || !view || !p || p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->maxDepth <= 0 || p->maxDepth > 64) return 1;
+    const size_t lights = s->triLights.size() + s->pointLights.size() + s->spotLights.size() + s->dirLights.size();
+    if ((p->flags & LH2G_RP_LIGHTTREE) ? !(p->flags & LH2G_RP_OPTIX7) : lights > 64) return 1;   /* 64 potentials at most */
     if (p->flags & LH2G_RP_OPTIX7) {
         if ((p->flags & (LH2G_RP_FILTER | LH2G_RP_NRC | LH2G_RP_ADAPTIVE)) || p->rowCount != 0) return 1;
         return render_optix7(s, view, p, pixelAccum, pixelAccum64, counters, capture, nthreads);

@@ -42,6 +42,9 @@ int lh2o_set_materials(lh2o_scene* s, const lh2g_material* mats, int count);
 int lh2o_set_textures(lh2o_scene* s, const lh2g_texture* tex, int count);
 int lh2o_set_lights(lh2o_scene* s, const lh2g_light_tri* tri, int ntri, const lh2g_point_light* pt, int npt,
                     const lh2g_spot_light* spot, int nspot, const lh2g_dir_light* dir, int ndir);
+/* the light tree lh2o_set_lights built (2 * (area + point + spot lights) records of 16 words, record 0 the root);
+ * returns the record count (out NULL: the count only), -1 if capacity (in records) is too small */
+int lh2o_light_tree(const lh2o_scene* s, void* out, int capacity);
 int lh2o_set_sky(lh2o_scene* s, const float* rgb, int width, int height, const float* worldToSky16);
 /* Builds the BVHs (BVH2 per mesh + BVH2 over instances). Must follow the setters, precede tracing. */
 int lh2o_finalize(lh2o_scene* s);

@@ -15,13 +15,23 @@
 #include "common_classes.h"
 #include "common_functions.h"
 
-/* Built twice: as is with the Lambert BSDF (entry points ref_o7_*), and with -DREF_O7_DISNEY with the Disney BSDF
+/* Built three times: as is with the Lambert BSDF (entry points ref_o7_*), and with -DREF_O7_DISNEY with the Disney BSDF
  * (the default branch of the core's kernels/bsdf.h: lib/sharedBSDFs/ggxmdf.h, frosted.h, disney.h; entry points
  * ref_o7d_*). The Disney build reads copies the Makefile makes in $(OUT)/inc_o7d: the three BSDF headers with their
  * CUDA branches selected (the samplers' sincosf form and the adjoint parameter), and pathtracer.h with its unset
  * newBsdfPdf (pathtracer.h:219) zero-initialised, so that a sampler exit that leaves it unset ends the path on the
- * host as the restatement does. logf and powf go to the oracle's own functions, as the other transcendentals do. */
-#ifdef REF_O7_DISNEY
+ * host as the restatement does. logf and powf go to the oracle's own functions, as the other transcendentals do.
+ * The third build (-DREF_O7_LTREE -DLIGHTTREE, entry points ref_o7t_*, Lambert BSDF) selects lights through the light
+ * tree: it reads copies in $(OUT)/inc_o7t of pathtracer.h with its two light-tree calls (pathtracer.h:145,187)
+ * taking the place of the potential-based ones they sit beside as comments, and of
+ * shared_kernel_code/lights_shared.h with the tree typed as the device LightCluster layout (ref_globals.h's
+ * DevLightCluster; the host build of common_classes.h has the host layout) and each child box's three random
+ * numbers drawn x, y, z in that order (the order the CUDA compiler evaluates make_float3's arguments; g++ evaluates
+ * them right to left). */
+#if defined(REF_O7_LTREE)
+#define REF_NS refo7t
+#define O7(name) ref_o7t_##name
+#elif defined(REF_O7_DISNEY)
 #define REF_NS refo7d
 #define O7(name) ref_o7d_##name
 extern "C" float lh2o_logf(float x);
@@ -43,7 +53,10 @@ namespace REF_NS {
             contribution.x *= m_, contribution.y *= m_, contribution.z *= m_;                                                  \
         }                                                                                                                      \
     }
-#ifdef REF_O7_DISNEY
+#if defined(REF_O7_LTREE)
+#include "lambert.h"
+#include "inc_o7t/pathtracer.h"
+#elif defined(REF_O7_DISNEY)
 using std::abs;
 #define logf(x) lh2o_logf(x)
 #define powf(x, y) lh2o_powf(x, y)
@@ -155,6 +168,11 @@ void O7(finalize_connections)(int count, float* accumulator, const float* connec
         if (pixelIdx < stride) acc[pixelIdx] += make_float4(E4.x, E4.y, E4.z, 1);
     }
 }
+
+#if defined(REF_O7_LTREE)
+/* the light tree the light-selection code reads (records of the device LightCluster; owned by the caller) */
+void O7(set_light_tree)(void* records) { lightTree = (DevLightCluster*)records; }
+#endif
 
 /* blueNoiseSampler4 of tools_shared.h:324-337 (the shading kernels' copy) */
 void O7(bluenoise4)(const uint32_t* bn, int x, int y, int sampleIndex, int sampleDimension, float* out4) {
