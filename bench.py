@@ -309,13 +309,14 @@ def decode_launches(lt_all, frames, counts, waves, W, H):
 
 
 def estimators_leg(core, sc, W, H, steps):
-    """The OptiX 7 core's estimator (LH2G_RP_OPTIX7: MIS, blue noise for the first 64 samples, one diffuse bounce)
-    and PrimeAdaptive frames (variance-driven second wave) on the same scene and frame size, seeded synthetic
-    blue-noise tables; device time per frame from CUDA events on the core's stream, rays from the frames' counters."""
+    """The OptiX 7 core's estimator (LH2G_RP_OPTIX7: MIS, blue noise for the first 64 samples, one diffuse bounce),
+    the same with its light tree (LH2G_RP_LIGHTTREE) on this scene and on a room of 2,144 lights, and PrimeAdaptive
+    frames (variance-driven second wave) on the same scene and frame size, seeded synthetic blue-noise tables; device
+    time per frame from CUDA events on the core's stream, rays from the frames' counters."""
     import numpy as np
     import torch
     from lighthouse2_gb300 import scenes as S
-    from lighthouse2_gb300.core import make_params, camera_r0, RP_NEE, RP_OPTIX7
+    from lighthouse2_gb300.core import RenderCore, make_params, camera_r0, RP_NEE, RP_OPTIX7, RP_LIGHTTREE
     core.set_blue_noise(S.synthetic_blue_noise(7))
     stream = torch.cuda.ExternalStream(core.stream_ptr())
     out = {"workload": f"the same scene and camera path, {W}x{H} 1 spp, max depth {MAX_DEPTH}; synthetic blue-noise tables"}
@@ -341,6 +342,40 @@ def estimators_leg(core, sc, W, H, steps):
     rays = [W * H + int(c[:, 0].sum()) + int(c[:, 1].sum()) for c in (o7(k, True)["counters"] for k in range(8))]
     ms = timed(o7, steps)
     out["optix7"] = {"ms_per_frame": ms, "Mrays_per_s": float(np.mean(rays)) / (ms / 1e3) / 1e6, "rays_per_frame": float(np.mean(rays))}
+
+    def o7t(k, counters=False, c=core, view=lambda k: S.spheres_view(W, H, frame=k % 8)):
+        p = make_params(W, H, 1, max_depth=MAX_DEPTH, samples_taken=k, camera_r0=camera_r0(k), flags=RP_NEE | RP_OPTIX7 | RP_LIGHTTREE,
+                        shift=(0x11331445 * (k + 1)) & 0xFFFFFFFF)
+        return c.render_ex(view(k), p, accumulate=k > 0, counters=counters)
+
+    rays = [W * H + int(c[:, 0].sum()) + int(c[:, 1].sum()) for c in (o7t(k, True)["counters"] for k in range(8))]
+    ms = timed(o7t, steps)
+    out["optix7_light_tree"] = {"ms_per_frame": ms, "Mrays_per_s": float(np.mean(rays)) / (ms / 1e3) / 1e6, "rays_per_frame": float(np.mean(rays)),
+                                "lights": len(sc.tri_lights) + len(sc.point_lights) + len(sc.spot_lights)}
+    # a room of 2,144 lights (2,048 area, 64 point, 32 spot): only the light tree renders it
+    room = S.lit_room(seed=29, grid=32, n_points=64, n_spots=32)
+    rc = RenderCore(0)
+    rc.set_scene(room)
+    rc.SetTarget(W, H, 1)
+    rc.set_blue_noise(S.synthetic_blue_noise(7))
+    rstream = torch.cuda.ExternalStream(rc.stream_ptr())
+    room_view = lambda k: S.cornell_view(W, H, frame=k % 4)
+    rays = [W * H + int(c[:, 0].sum()) + int(c[:, 1].sum()) for c in (o7t(k, True, rc, room_view)["counters"] for k in range(4))]
+    rc.WaitForRender()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(rstream):
+        e0.record()
+    n_room = max(4, steps // 4)
+    for k in range(n_room):
+        o7t(k, False, rc, room_view)
+    with torch.cuda.stream(rstream):
+        e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / n_room
+    out["light_tree_2144_lights"] = {"workload": f"lit_room(grid=32): Cornell room + 2,048 area, 64 point and 32 spot lights, {W}x{H} 1 spp, "
+                                                 f"max depth {MAX_DEPTH}; OptiX 7 estimator with the light tree",
+                                     "ms_per_frame": ms, "Mrays_per_s": float(np.mean(rays)) / (ms / 1e3) / 1e6, "rays_per_frame": float(np.mean(rays))}
+    rc.close()
     core.set_adaptive_scale(10.0)
 
     def ad(k):

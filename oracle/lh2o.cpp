@@ -2819,7 +2819,7 @@ int lh2o_set_textures(lh2o_scene* s, const lh2g_texture* tex, int count) {
 
 int lh2o_set_lights(lh2o_scene* s, const lh2g_light_tri* tri, int ntri, const lh2g_point_light* pt, int npt,
                     const lh2g_spot_light* spot, int nspot, const lh2g_dir_light* dir, int ndir) {
-    if (!s || ntri < 0 || npt < 0 || nspot < 0 || ndir < 0 || (long long)ntri + npt + nspot > (1 << 20) || ndir > 64) return 1;
+    if (!s || ntri < 0 || npt < 0 || nspot < 0 || ndir < 0 || (long long)ntri + npt + nspot > (1 << 16) || ndir > 64) return 1;
     s->triLights.assign(tri, tri + ntri);
     s->pointLights.assign(pt, pt + npt);
     s->spotLights.assign(spot, spot + nspot);
