@@ -22,17 +22,44 @@ namespace {
 
 
 /* -------------------------------------------------------------------------------------------------- */
+/* tuning switch: 1 (default) queues a frame's primary rays in 8 x 4 pixel tiles, so that each warp of the first wave
+ * (and, through the compaction that keeps a warp's survivors together, of the later ones) holds a compact patch of
+ * the image instead of a 32-pixel strip of one row; 0 queues them in path order. The queue slot is only where a
+ * path waits: every per-path quantity is indexed by the path, so results do not change. */
+#ifndef LH2G_TILE_PRIMARY
+#define LH2G_TILE_PRIMARY 1
+#endif
+/* the (band-local) path index of primary queue slot q: per sample layer of W x rows pixels, rows in groups of 4,
+ * each group in tiles of 8 columns (the last tile narrower when W is not a multiple of 8, the last group lower when
+ * rows is not a multiple of 4), a tile's pixels row by row */
+__device__ __forceinline__ uint32_t primary_slot_path(const FrameGPU& F, const uint32_t q) {
+#if LH2G_TILE_PRIMARY
+    const uint32_t W = (uint32_t)F.W, rows = F.bandPix ? F.bandPix / W : (uint32_t)F.H, layerSize = W * rows;
+    const uint32_t layer = q / layerSize, r0 = q - layer * layerSize;
+    const uint32_t g = r0 / (4u * W), r = r0 - g * 4u * W;
+    const uint32_t rg = min(4u, rows - 4u * g);
+    const uint32_t t = r / (8u * rg), u = r - t * 8u * rg;
+    const uint32_t wt = min(8u, W - 8u * t);
+    const uint32_t dy = u / wt, dx = u - dy * wt;
+    return layer * layerSize + (4u * g + dy) * W + 8u * t + dx;
+#else
+    (void)F;
+    return q;
+#endif
+}
+
 __global__ void __launch_bounds__(256) k_generate(const FrameGPU F, const WaveBuffers B) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= F.P) return;
+    const uint32_t p = primary_slot_path(F, (uint32_t)i);
     float3 O, D;
-    primary_ray(F, (uint32_t)i, O, D);
-    B.O[0][i] = make_float4(O.x, O.y, O.z, __uint_as_float((uint32_t)i));
+    primary_ray(F, p, O, D);
+    B.O[0][i] = make_float4(O.x, O.y, O.z, __uint_as_float(p));
     B.D[0][i] = make_float4(D.x, D.y, D.z, __uint_as_float(S_SPECULAR));
     B.T[0][i] = make_float4(1.0f, 1.0f, 1.0f, F.eps);
-    B.pathAcc[i] = make_float4(0, 0, 0, 0);
-    if (F.flags & LH2G_RP_FILTER) B.pathAcc[i + F.P] = make_float4(0, 0, 0, 0);
-    if (F.flags & LH2G_RP_NRC) B.nrcRec[i + 4 * F.P] = make_float4(0, 0, 0, 0);   /* no cache query yet */
+    B.pathAcc[p] = make_float4(0, 0, 0, 0);
+    if (F.flags & LH2G_RP_FILTER) B.pathAcc[p + F.P] = make_float4(0, 0, 0, 0);
+    if (F.flags & LH2G_RP_NRC) B.nrcRec[p + 4 * F.P] = make_float4(0, 0, 0, 0);   /* no cache query yet */
 }
 /* primary rays of the OptiX 7 estimator, or the first wave of a PrimeAdaptive frame (sample layers of W*H paths) */
 __global__ void __launch_bounds__(256) k_generate_mis(const SceneGPU S, const FrameGPU F, const WaveBuffers B) {
@@ -40,16 +67,18 @@ __global__ void __launch_bounds__(256) k_generate_mis(const SceneGPU S, const Fr
     if (i >= F.P) return;
     float3 O, D;
     const bool adaptive = (F.flags & LH2G_RP_ADAPTIVE) != 0;
+    uint32_t p = (uint32_t)i;   /* the path's slot (adaptive frames keep path order: their second wave maps slots to layers) */
     if (adaptive) {
         const uint32_t row = (uint32_t)i / (uint32_t)F.W;
         primary_adaptive(S, F, (int)((uint32_t)i % (uint32_t)F.W), (int)(row % (uint32_t)F.H), F.pass + row / (uint32_t)F.H, (uint32_t)i, F.cameraR0, O, D);
     } else {
-        primary_optix7(S, F, (uint32_t)i, O, D);
+        p = primary_slot_path(F, (uint32_t)i);
+        primary_optix7(S, F, p, O, D);
     }
-    B.O[0][i] = make_float4(O.x, O.y, O.z, __uint_as_float(((uint32_t)i << 6) | S_SPECULAR | MIS_TMIN_EPS));
+    B.O[0][i] = make_float4(O.x, O.y, O.z, __uint_as_float((p << 6) | S_SPECULAR | MIS_TMIN_EPS));
     B.D[0][i] = make_float4(D.x, D.y, D.z, __uint_as_float(0u));
     B.T[0][i] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-    B.pathAcc[i] = make_float4(0.0f, 0.0f, 0.0f, adaptive ? 1.0f : 0.0f);   /* PrimeAdaptive: w counts the pixel's samples */
+    B.pathAcc[p] = make_float4(0.0f, 0.0f, 0.0f, adaptive ? 1.0f : 0.0f);   /* PrimeAdaptive: w counts the pixel's samples */
 }
 __device__ __forceinline__ uint32_t queue_count(const FrameGPU& F, const WaveBuffers& B, const Counters* C, int depth) {
     return depth == 1 ? (B.firstCount ? *B.firstCount : (uint32_t)F.P) : C->extension[depth - 2];
