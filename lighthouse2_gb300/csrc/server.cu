@@ -109,8 +109,11 @@ __global__ void __launch_bounds__(256) k_srv_generate(const JobGPU* __restrict__
     for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total && base + g < Q.cap; g += gridDim.x * blockDim.x) {
         uint32_t j = 0;
         while (j + 1 < n && st->newPrefix[j + 1] <= g) j++;
-        const uint32_t slot = st->newSlot[j], i = st->newStart[j] + (g - st->newPrefix[j]);
+        const uint32_t slot = st->newSlot[j];
         const JobGPU& J = jobs[slot];
+        /* a job's ranges run over its primary queue order (pixel tiles, as the plain core queues them); the path
+         * of that position is generated */
+        const uint32_t i = primary_slot_path(J.F, st->newStart[j] + (g - st->newPrefix[j]));
         float3 O, D;
         primary_ray(J.F, i, O, D);
         Q.O[cur][base + g] = make_float4(O.x, O.y, O.z, __uint_as_float(i));

@@ -22,6 +22,37 @@ constexpr uint32_t S_CACHED = 8;   /* radiance-cache frames: the path has record
 
 __device__ __forceinline__ uint32_t lanemask_lt() { uint32_t m; asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m)); return m; }
 
+/* tuning switch: 1 (default) queues a frame's primary rays in 8 x 4 pixel tiles (LH2G_TILE_W), so that each warp of the first wave
+ * (and, through the compaction that keeps a warp's survivors together, of the later ones) holds a compact patch of
+ * the image instead of a 32-pixel strip of one row; 0 queues them in path order. The queue slot is only where a
+ * path waits: every per-path quantity is indexed by the path, so results do not change. */
+#ifndef LH2G_TILE_PRIMARY
+#define LH2G_TILE_PRIMARY 1
+#endif
+#ifndef LH2G_TILE_W
+#define LH2G_TILE_W 8   /* tile width; the height is 32 / width */
+#endif
+/* the (band-local) path index of primary queue slot q: per sample layer of W x rows pixels, rows in groups of TH,
+ * each group in tiles of TW columns (the last tile narrower when W is not a multiple of TW, the last group lower
+ * when rows is not a multiple of TH), a tile's pixels row by row */
+__device__ __forceinline__ uint32_t primary_slot_path(const FrameGPU& F, const uint32_t q) {
+#if LH2G_TILE_PRIMARY
+    constexpr uint32_t TW = LH2G_TILE_W, TH = 32 / LH2G_TILE_W;
+    static_assert(TW * TH == 32, "a tile is a warp");
+    const uint32_t W = (uint32_t)F.W, rows = F.bandPix ? F.bandPix / W : (uint32_t)F.H, layerSize = W * rows;
+    const uint32_t layer = q / layerSize, r0 = q - layer * layerSize;
+    const uint32_t g = r0 / (TH * W), r = r0 - g * TH * W;
+    const uint32_t rg = min(TH, rows - TH * g);
+    const uint32_t t = r / (TW * rg), u = r - t * TW * rg;
+    const uint32_t wt = min(TW, W - TW * t);
+    const uint32_t dy = u / wt, dx = u - dy * wt;
+    return layer * layerSize + (TH * g + dy) * W + TW * t + dx;
+#else
+    (void)F;
+    return q;
+#endif
+}
+
 /* Primary ray of path jobIndex (lib/RenderCore_PrimeRef/kernels/camera.h:39-68; pixel corner without lens for
  * LH2G_RP_FILTER frames, RenderCore_Optix7Filter/optix/.optix.cu:66-100). */
 __device__ __forceinline__ void primary_ray(const FrameGPU& F, const uint32_t local, float3& O, float3& D) {
