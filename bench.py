@@ -600,7 +600,10 @@ def serving_leg(args):
         t_seq = float(service.sum())
         seq_sums = [zlib.crc32(pinned[k]) for k in range(len(jobs))]   # each sequential image's checksum
         cap = max(max(j["W"] * j["H"] * j["spp"] for j in jobs) * 2, args.serving_capacity)
-        srv = RenderServer(path_capacity=cap, **({"tickBudget": args.serving_tick_budget} if args.serving_tick_budget else {}))
+        opts = {"tickBudget": args.serving_tick_budget} if args.serving_tick_budget else {}
+        if args.serving_device_loop >= 0:
+            opts["deviceLoop"] = args.serving_device_loop
+        srv = RenderServer(path_capacity=cap, **opts)
         sids = [srv.add_scene(c) for c in cores]
         for j in jobs[:4]:   # warm-up
             view, p = inputs(j)
@@ -679,6 +682,7 @@ def serving_leg(args):
                           "server_fcfs_p99_within_bound": bool(np.percentile(lat_fcfs, 99) <= bound),
                           "sequential_p99_within_bound": bool(np.percentile(seq_lat, 99) <= bound),
                           "slowdown_vs_standalone": {"p50": float(np.percentile(lat / service, 50)), "p99": float(np.percentile(lat / service, 99))}})
+        sst = srv.stats()
         srv.close()
         ok_srv = [r["rate_jobs_per_s"] for r in sweep if r["server_p99_within_bound"]]
         ok_fcfs = [r["rate_jobs_per_s"] for r in sweep if r["server_fcfs_p99_within_bound"]]
@@ -692,6 +696,7 @@ def serving_leg(args):
                 # the served images equal the sequential ones bit for bit (CRC32 of each image), so both arms are
                 # compared at the same RMSE: that of the plain estimator at each job's spp
                 "images_equal_to_sequential": f"{same_images}/{len(jobs)}",
+                "ticks": int(sst["ticks"]), "device_loop_launches": int(sst["loopLaunches"]),
                 "poisson_sweep": sweep,
                 "rate_at_p99_bound": {"bound_ms": bound * 1e3, "server": max(ok_srv) if ok_srv else None,
                                       "server_fcfs": max(ok_fcfs) if ok_fcfs else None,
@@ -1012,6 +1017,8 @@ def main():
     ap.add_argument("--serving-capacity", type=int, default=SERVING_CAPACITY,
                     help="queue capacity of the serving loop in paths (at least twice the largest job)")
     ap.add_argument("--serving-tick-budget", type=int, default=0, help="new paths per tick of the serving loop (0: the loop's default)")
+    ap.add_argument("--serving-device-loop", type=int, default=-1,
+                    help="1: the serving loop's ticks run in a device-side graph loop (its default), 0: host-driven ticks")
     ap.add_argument("--lanes", type=int, default=LANES, help="frames in flight (0 or 1: one at a time)")
     ap.add_argument("--partition", default="replicas", choices=["replicas", "rows"],
                     help="under torchrun: replicas (every rank renders whole frames) or rows (every frame's rows split over the ranks)")

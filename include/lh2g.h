@@ -241,6 +241,7 @@ typedef struct lh2g_server_stats {
     unsigned long long ticks, raysTraced;
     long long jobsDone, pathsInFlight, pending;
     uint32_t deviceStatus;
+    long long loopLaunches;            /* launches of the device-side tick loop ("deviceLoop"; 0 with host-driven ticks) */
 } lh2g_server_stats;
 LH2G_API int lh2g_server_create(int device, long long pathCapacity, lh2g_server** out);
 LH2G_API int lh2g_server_destroy(lh2g_server* server);   /* finishes the jobs it holds first */
@@ -249,7 +250,10 @@ LH2G_API int lh2g_server_destroy(lh2g_server* server);   /* finishes the jobs it
  * idle), "expressBudget" (express paths per tick, default 1048576), "tickBudget" (new queue paths per tick,
  * default clamp(capacity, 2^20, 2^22)), "maxWaitSeconds" (0.2), "largeJobPaths" (default 2^23; 0 = none: render jobs
  * of at least this many paths skip the shared queues and run one at a time as plain frames on the server's own
- * stream beside the ticks, needing no queue memory). Results do not depend on them. */
+ * stream beside the ticks, needing no queue memory), "deviceLoop" (1 default: one graph launch runs ticks on the
+ * device inside a conditional WHILE node until a job finishes, a job is submitted, the work runs out or "loopTicks"
+ * ticks (default 256) have run, the device admitting the further ranges of jobs already admitted; 0: the host
+ * launches every tick's graph, two in flight). Results do not depend on them. */
 LH2G_API int lh2g_server_setting(lh2g_server* server, const char* name, double value);
 LH2G_API const char* lh2g_server_last_error(lh2g_server* server);
 LH2G_API int lh2g_server_add_scene(lh2g_server* server, lh2g_context* scene, int* sceneId);

@@ -329,6 +329,46 @@ __global__ void k_srv_end(ServerState* st) {
     st->hitCount = st->missCount = 0;
 }
 
+/* ---- the device-side tick loop (setting "deviceLoop") ----
+ * The tick graph's body runs inside a conditional WHILE node: one graph launch runs tick after tick on the device,
+ * and k_srv_loop_end decides at the end of each tick whether another follows. It admits the next ranges of the jobs
+ * whose paths are still entering the queues (the host's admitted-job list, in admission order, within the tick
+ * budget), and ends the launch when a job's live count reached zero (the host finalizes it), when the host has
+ * work waiting (a job submitted since the launch: a mapped host word it reads once per tick, no spinning), when no
+ * work is left, or after `limit` ticks. The host admits new jobs and finalizes finished ones between launches. */
+struct LoopState {
+    uint32_t ticks;                    /* ticks run by the current launch */
+    uint32_t limit;                    /* at most this many per launch */
+    uint32_t budget;                   /* new paths per tick */
+    uint32_t nPart;                    /* jobs with paths still to enter the queues, in admission order */
+    uint32_t partSlot[MAX_SLOTS], partNext[MAX_SLOTS], partEnd[MAX_SLOTS];
+    uint32_t active[MAX_SLOTS];        /* 1: the slot holds a job the host has not finalized */
+    const int* doorbell;               /* mapped host word, nonzero while jobs wait for the host */
+};
+
+__global__ void __launch_bounds__(MAX_SLOTS) k_srv_loop_end(ServerState* st, LoopState* L, const int* __restrict__ alive,
+                                                          cudaGraphConditionalHandle handle) {
+    const int k = threadIdx.x;
+    const int anyDone = __syncthreads_or(L->active[k] && alive[k] <= 0);
+    if (k != 0) return;
+    L->ticks++;
+    bool go = !anyDone && L->ticks < L->limit && *(const volatile int*)L->doorbell == 0;
+    if (go) {
+        uint32_t n = 0, total = 0, budget = L->budget;
+        for (uint32_t p = 0; p < L->nPart && budget > 0 && n < (uint32_t)MAX_NEW; p++) {
+            const uint32_t rem = L->partEnd[p] - L->partNext[p];
+            if (!rem) continue;
+            const uint32_t c = min(rem, budget);
+            st->newSlot[n] = L->partSlot[p], st->newStart[n] = L->partNext[p], st->newPrefix[n] = total;
+            total += c, budget -= c, n++;
+            L->partNext[p] += c;
+        }
+        st->newPrefix[n] = total, st->newCount = n, st->newTotal = total;
+        go = st->qCount[st->cur] > 0 || total > 0;   /* paths in flight or entering */
+    }
+    cudaGraphSetConditional(handle, go ? 1u : 0u);
+}
+
 /* per-pixel sums of a finished job's paths in sample order (as the plain core's finalize) */
 __global__ void k_srv_finalize(const JobGPU J) {
     const int64_t px = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -394,6 +434,17 @@ struct lh2g_server {
     double maxWaitS = 0.2;             /* a job waiting longer than this is admitted before smaller ones */
     cudaGraphExec_t tickExec = nullptr;
     cudaGraph_t tickGraph = nullptr;
+    /* the device-side tick loop (setting "deviceLoop"): a graph whose WHILE node runs the tick body */
+    bool deviceLoop = true;
+    long long loopLimit = 256;         /* ticks per launch at most (setting "loopTicks") */
+    cudaGraphExec_t loopExec = nullptr;
+    cudaGraph_t loopGraph = nullptr;
+    int loopScenes = -1;               /* scene count the loop graph was built with */
+    LoopState* dLoop = nullptr;
+    LoopState* hLoop = nullptr;        /* pinned: [0] staged for a launch, [1] read back after it */
+    int* hDoorbell = nullptr;          /* mapped host word: set when a job is submitted, cleared before a launch */
+    int* dDoorbell = nullptr;
+    long long loopLaunches = 0;
     std::vector<cudaEvent_t> tickEv;   /* ring of tick-completion events */
     long long ticksLaunched = 0, ticksDone = 0;
     int blocksGen = 0, blocksExtend = 0, blocksShade = 0, blocksConnect = 0, blocksTrace0 = 0, blocksTrace1 = 0, blocksExpress = 0, blocksPart = 0;
@@ -676,6 +727,7 @@ void admit(lh2g_server* s, std::vector<Range>& ranges) {
 
 void tick_loop_body(lh2g_server* s);
 int build_tick_graph(lh2g_server* s);
+int build_loop_graph(lh2g_server* s);
 
 void tick_loop(lh2g_server* s) {
     tick_loop_body(s);
@@ -701,6 +753,18 @@ void tick_loop_body(lh2g_server* s) {
             if (n != s->graphScenes && build_tick_graph(s) != LH2G_OK) {
                 std::lock_guard<std::mutex> g(s->mu);
                 s->err = "tick graph capture failed";
+            }
+            bool wantLoop;
+            {
+                std::lock_guard<std::mutex> g(s->mu);
+                wantLoop = s->deviceLoop;
+            }
+            if (wantLoop && n != s->loopScenes && build_loop_graph(s) != LH2G_OK) {
+                cudaGetLastError();
+                if (s->loopExec) cudaGraphExecDestroy(s->loopExec), s->loopExec = nullptr;
+                std::lock_guard<std::mutex> g(s->mu);
+                s->err = "device loop graph build failed: ticks stay host-driven";
+                s->deviceLoop = false;
             }
         }
         admitted.clear();
@@ -763,15 +827,58 @@ void tick_loop_body(lh2g_server* s) {
         tp.expCount = nExp, tp.expPrefix[nExp] = expTotal, tp.expTotal = expTotal;
         cudaMemcpyAsync(&s->dState->newCount, &tp.newCount, offsetof(ServerState, rays) - offsetof(ServerState, newCount), cudaMemcpyHostToDevice,
                         s->st);
-        /* the tick */
-        cudaGraphLaunch(s->tickExec, s->st);
-        cudaEventRecord(s->tickEv[s->ticksLaunched % ring], s->st);
-        s->ticksLaunched++;
-        /* at most two ticks in flight: the host prepares the next tick while the GPU runs the current one; the
-         * live counts on the host are then at least as new as the older of the two */
-        while (s->ticksLaunched - s->ticksDone > 1) {
-            cudaEventSynchronize(s->tickEv[s->ticksDone % ring]);
-            s->ticksDone++;
+        bool loopLaunch;
+        {
+            std::lock_guard<std::mutex> g(s->mu);
+            loopLaunch = s->deviceLoop && s->loopExec && s->loopScenes == s->graphScenes;
+        }
+        if (loopLaunch) {
+            /* the device-side loop: this tick's ranges as staged above, later ticks' ranges of the jobs still
+             * entering the queues from the device; the launch ends when the host is needed */
+            while (s->ticksLaunched > s->ticksDone) {   /* (host-driven ticks still in flight) */
+                cudaEventSynchronize(s->tickEv[s->ticksDone % ring]);
+                s->ticksDone++;
+            }
+            LoopState& L = s->hLoop[0];
+            {
+                std::lock_guard<std::mutex> g(s->mu);
+                L.ticks = 0, L.limit = (uint32_t)std::max(1ll, std::min(s->loopLimit, 1ll << 20));
+                L.budget = (uint32_t)std::min(std::max(s->tickBudget, 1ll), (long long)UINT32_MAX);
+                L.nPart = 0;
+                for (Job* j : s->partial) {
+                    L.partSlot[L.nPart] = (uint32_t)j->slot, L.partNext[L.nPart] = (uint32_t)j->admittedPaths;
+                    L.partEnd[L.nPart] = (uint32_t)j->paths, L.nPart++;
+                }
+                for (int k = 0; k < MAX_SLOTS; k++) L.active[k] = s->slots[k] ? 1u : 0u;
+                L.doorbell = s->dDoorbell;
+                *(volatile int*)s->hDoorbell = 0;   /* jobs submitted from now on end the launch after their tick */
+            }
+            cudaMemcpyAsync(s->dLoop, &L, sizeof(LoopState), cudaMemcpyHostToDevice, s->st);
+            cudaGraphLaunch(s->loopExec, s->st);
+            cudaMemcpyAsync(&s->hLoop[1], s->dLoop, sizeof(LoopState), cudaMemcpyDeviceToHost, s->st);
+            cudaStreamSynchronize(s->st);
+            const LoopState& R = s->hLoop[1];
+            s->ticksLaunched += std::max(R.ticks, 1u);
+            s->ticksDone = s->ticksLaunched;
+            std::lock_guard<std::mutex> g(s->mu);
+            s->loopLaunches++;
+            for (uint32_t p = 0; p < R.nPart; p++) {
+                Job* j = s->slots[R.partSlot[p]];
+                if (j) j->admittedPaths = R.partNext[p];
+            }
+            s->partial.erase(std::remove_if(s->partial.begin(), s->partial.end(), [](const Job* j) { return j->admittedPaths == j->paths; }),
+                             s->partial.end());
+        } else {
+            /* the tick */
+            cudaGraphLaunch(s->tickExec, s->st);
+            cudaEventRecord(s->tickEv[s->ticksLaunched % ring], s->st);
+            s->ticksLaunched++;
+            /* at most two ticks in flight: the host prepares the next tick while the GPU runs the current one; the
+             * live counts on the host are then at least as new as the older of the two */
+            while (s->ticksLaunched - s->ticksDone > 1) {
+                cudaEventSynchronize(s->tickEv[s->ticksDone % ring]);
+                s->ticksDone++;
+            }
         }
         /* jobs with no live path left: finalize, release, copy out */
         std::vector<Job*> done;
@@ -811,18 +918,8 @@ void tick_loop_body(lh2g_server* s) {
     }
 }
 
-int build_tick_graph(lh2g_server* s) {
-    SceneTable T;
-    memset(&T, 0, sizeof(T));
-    int n;
-    {
-        std::lock_guard<std::mutex> g(s->mu);
-        n = (int)s->scenes.size();
-        for (int k = 0; k < n; k++) T.s[k] = s->scenes[k];
-    }
-    if (s->tickExec) cudaGraphExecDestroy(s->tickExec), s->tickExec = nullptr;
-    if (s->tickGraph) cudaGraphDestroy(s->tickGraph), s->tickGraph = nullptr;
-    if (cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return LH2G_ERR_CUDA;
+/* the launches of one tick, on s->st (being captured) */
+void capture_tick_body(lh2g_server* s, const SceneTable& T, int n) {
     k_srv_generate<<<s->blocksGen, 256, 0, s->st>>>(s->dJobs, s->dState, s->Q);
     /* express jobs on a second branch, beside the waves; the tick ends when both are done */
     cudaEventRecord(s->evFork, s->st);
@@ -838,9 +935,56 @@ int build_tick_graph(lh2g_server* s) {
     cudaStreamWaitEvent(s->st, s->evJoin, 0);
     k_srv_end<<<1, 1, 0, s->st>>>(s->dState);
     cudaMemcpyAsync(s->hAlive, s->dAlive, sizeof(int) * MAX_SLOTS, cudaMemcpyDeviceToHost, s->st);
+}
+
+int scene_table(lh2g_server* s, SceneTable& T) {
+    memset(&T, 0, sizeof(T));
+    std::lock_guard<std::mutex> g(s->mu);
+    const int n = (int)s->scenes.size();
+    for (int k = 0; k < n; k++) T.s[k] = s->scenes[k];
+    return n;
+}
+
+int build_tick_graph(lh2g_server* s) {
+    SceneTable T;
+    const int n = scene_table(s, T);
+    if (s->tickExec) cudaGraphExecDestroy(s->tickExec), s->tickExec = nullptr;
+    if (s->tickGraph) cudaGraphDestroy(s->tickGraph), s->tickGraph = nullptr;
+    if (cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return LH2G_ERR_CUDA;
+    capture_tick_body(s, T, n);
     if (cudaStreamEndCapture(s->st, &s->tickGraph) != cudaSuccess) return LH2G_ERR_CUDA;
     if (cudaGraphInstantiate(&s->tickExec, s->tickGraph, 0) != cudaSuccess) return LH2G_ERR_CUDA;
     s->graphScenes = n;
+    return LH2G_OK;
+}
+
+/* the device-side loop: a conditional WHILE node (its condition set to 1 at every launch) whose body is the tick
+ * followed by k_srv_loop_end, which sets the condition for the next iteration */
+int build_loop_graph(lh2g_server* s) {
+    SceneTable T;
+    const int n = scene_table(s, T);
+    if (s->loopExec) cudaGraphExecDestroy(s->loopExec), s->loopExec = nullptr;
+    if (s->loopGraph) cudaGraphDestroy(s->loopGraph), s->loopGraph = nullptr;
+    if (cudaGraphCreate(&s->loopGraph, 0) != cudaSuccess) return LH2G_ERR_CUDA;
+    cudaGraphConditionalHandle handle;
+    if (cudaGraphConditionalHandleCreate(&handle, s->loopGraph, 1, cudaGraphCondAssignDefault) != cudaSuccess) return LH2G_ERR_CUDA;
+    alignas(cudaGraphNodeParams) unsigned char cpBytes[sizeof(cudaGraphNodeParams)];   /* (no default constructor: a union) */
+    memset(cpBytes, 0, sizeof(cpBytes));
+    cudaGraphNodeParams& cp = *reinterpret_cast<cudaGraphNodeParams*>(cpBytes);
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (cudaGraphAddNode(&node, s->loopGraph, nullptr, nullptr, 0, &cp) != cudaSuccess) return LH2G_ERR_CUDA;
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    if (cudaStreamBeginCaptureToGraph(s->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return LH2G_ERR_CUDA;
+    capture_tick_body(s, T, n);
+    k_srv_loop_end<<<1, MAX_SLOTS, 0, s->st>>>(s->dState, s->dLoop, s->dAlive, handle);
+    cudaGraph_t captured = nullptr;
+    if (cudaStreamEndCapture(s->st, &captured) != cudaSuccess) return LH2G_ERR_CUDA;
+    if (cudaGraphInstantiate(&s->loopExec, s->loopGraph, 0) != cudaSuccess) return LH2G_ERR_CUDA;
+    s->loopScenes = n;
     return LH2G_OK;
 }
 
@@ -885,11 +1029,17 @@ int lh2g_server_create(int device, long long pathCapacity, lh2g_server** out) {
     ok = ok && cudaMalloc((void**)&s->dState, sizeof(ServerState)) == cudaSuccess;
     ok = ok && cudaMallocHost((void**)&s->hAlive, sizeof(int) * MAX_SLOTS) == cudaSuccess;
     ok = ok && cudaMallocHost((void**)&s->hTick, sizeof(ServerState) * 4) == cudaSuccess;
+    ok = ok && cudaMalloc((void**)&s->dLoop, sizeof(LoopState)) == cudaSuccess;
+    ok = ok && cudaMallocHost((void**)&s->hLoop, sizeof(LoopState) * 2) == cudaSuccess;
+    ok = ok && cudaHostAlloc((void**)&s->hDoorbell, sizeof(int), cudaHostAllocMapped) == cudaSuccess;
+    ok = ok && cudaHostGetDevicePointer((void**)&s->dDoorbell, s->hDoorbell, 0) == cudaSuccess;
     if (ok) {
         cudaMemset(s->dAlive, 0, sizeof(int) * MAX_SLOTS);
         cudaMemset(s->dState, 0, sizeof(ServerState));
         memset(s->hAlive, 0, sizeof(int) * MAX_SLOTS);
         memset(s->hTick, 0, sizeof(ServerState) * 4);
+        memset(s->hLoop, 0, sizeof(LoopState) * 2);
+        *s->hDoorbell = 0;
         /* per-job memory comes from the stream-ordered pool: keep what it holds between jobs */
         cudaMemPool_t pool;
         if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
@@ -954,6 +1104,11 @@ int lh2g_server_destroy(lh2g_server* s) {
     if (s->side) cudaStreamSynchronize(s->side);
     if (s->tickExec) cudaGraphExecDestroy(s->tickExec);
     if (s->tickGraph) cudaGraphDestroy(s->tickGraph);
+    if (s->loopExec) cudaGraphExecDestroy(s->loopExec);
+    if (s->loopGraph) cudaGraphDestroy(s->loopGraph);
+    cudaFree(s->dLoop);
+    if (s->hLoop) cudaFreeHost(s->hLoop);
+    if (s->hDoorbell) cudaFreeHost(s->hDoorbell);
     for (auto& e : s->tickEv) if (e) cudaEventDestroy(e);
     for (int k = 0; k < 2; k++) cudaFree(s->Q.O[k]), cudaFree(s->Q.D[k]), cudaFree(s->Q.T[k]);
     cudaFree(s->Q.hits), cudaFree(s->Q.shO), cudaFree(s->Q.shD), cudaFree(s->Q.shE), cudaFree(s->Q.order);
@@ -988,6 +1143,8 @@ int lh2g_server_setting(lh2g_server* s, const char* name, double value) {
     else if (!strcmp(name, "tickBudget")) s->tickBudget = std::max(1ll, (long long)value);
     else if (!strcmp(name, "maxWaitSeconds")) s->maxWaitS = value;
     else if (!strcmp(name, "largeJobPaths")) s->largeMin = (long long)value;
+    else if (!strcmp(name, "deviceLoop")) s->deviceLoop = value != 0.0;
+    else if (!strcmp(name, "loopTicks")) s->loopLimit = std::max(1ll, (long long)value);
     else {
         s->err = std::string("unknown server setting ") + name;
         return LH2G_ERR_INVALID;
@@ -1037,6 +1194,7 @@ int lh2g_server_submit_render(lh2g_server* s, int sceneId, const lh2g_view* view
         s->jobs[j->id] = j;
         s->pending.push_back(j);
         *jobId = j->id;
+        *(volatile int*)s->hDoorbell = 1;   /* a running device loop ends after its tick */
     }
     s->cvWork.notify_all();
     return LH2G_OK;
@@ -1054,6 +1212,7 @@ int lh2g_server_submit_trace(lh2g_server* s, int sceneId, const lh2g_ray* hostRa
         s->jobs[j->id] = j;
         s->pending.push_back(j);
         *jobId = j->id;
+        *(volatile int*)s->hDoorbell = 1;   /* a running device loop ends after its tick */
     }
     s->cvWork.notify_all();
     return LH2G_OK;
@@ -1094,6 +1253,7 @@ int lh2g_server_get_stats(lh2g_server* s, lh2g_server_stats* out) {
     out->pathsInFlight = s->pathsInFlight;
     out->pending = (long long)s->pending.size();
     out->deviceStatus = st.status | s->largeStatus;
+    out->loopLaunches = s->loopLaunches;
     return LH2G_OK;
 }
 

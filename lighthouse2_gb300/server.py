@@ -16,7 +16,7 @@ class JobTimes(C.Structure):
 
 class ServerStats(C.Structure):
     _fields_ = [("ticks", C.c_ulonglong), ("raysTraced", C.c_ulonglong), ("jobsDone", C.c_longlong), ("pathsInFlight", C.c_longlong),
-                ("pending", C.c_longlong), ("deviceStatus", C.c_uint32)]
+                ("pending", C.c_longlong), ("deviceStatus", C.c_uint32), ("loopLaunches", C.c_longlong)]
 
 
 def _bind(lib):

@@ -46,8 +46,10 @@ def plain_core_image(core, view, p):
     return core.read_accumulator()
 
 
-@pytest.mark.parametrize("express_max", [None, 5000, 1 << 20])   # all through the queues (default), mixed, all express
-def test_jobs_in_the_mix_equal_plain_core_and_alone(two_scenes, express_max):
+@pytest.mark.parametrize("express_max,device_loop", [(None, 1), (None, 0), (5000, 1), (5000, 0), (1 << 20, 1)])
+def test_jobs_in_the_mix_equal_plain_core_and_alone(two_scenes, express_max, device_loop):
+    """express_max: all jobs through the queues (default), mixed, all express; device_loop: ticks in the device-side
+    graph loop (default) or launched by the host one by one"""
     from lighthouse2_gb300.server import RenderServer
     (sa, ca), (sb, cb) = two_scenes
     cores = [ca, cb]
@@ -55,7 +57,10 @@ def test_jobs_in_the_mix_equal_plain_core_and_alone(two_scenes, express_max):
     for j in JOBS:
         view, p = job_inputs(*j)
         expect.append(plain_core_image(cores[j[0]], view, p))
-    srv = RenderServer(path_capacity=1 << 20, **({} if express_max is None else {"expressMaxPaths": express_max}))
+    opts = {"deviceLoop": device_loop}
+    if express_max is not None:
+        opts["expressMaxPaths"] = express_max
+    srv = RenderServer(path_capacity=1 << 20, **opts)
     sid = [srv.add_scene(ca), srv.add_scene(cb)]
     # all at once: the jobs share ticks
     ids = []
@@ -76,6 +81,7 @@ def test_jobs_in_the_mix_equal_plain_core_and_alone(two_scenes, express_max):
         srv.release(jid)
     st = srv.stats()
     assert st["jobsDone"] == 2 * len(JOBS) and st["deviceStatus"] == 0 and st["pathsInFlight"] == 0
+    assert (st["loopLaunches"] > 0) == bool(device_loop)
     srv.close()
 
 
@@ -149,4 +155,38 @@ def test_large_job_lane(two_scenes):
     assert np.array_equal(srv.result(jid).view(np.uint32), expect[-1].view(np.uint32))
     st = srv.stats()
     assert st["deviceStatus"] == 0 and st["pathsInFlight"] == 0 and st["raysTraced"] > 0
+    srv.close()
+
+
+@pytest.mark.parametrize("tick_budget", [0, 3000])
+def test_device_loop(two_scenes, tick_budget):
+    """"deviceLoop": ticks run on the device inside one graph launch (a conditional WHILE node) until a job finishes
+    or one is submitted; with a small tick budget the device admits the further ranges of the jobs in flight. Every
+    image equals the plain core's, in the mix and with jobs submitted while a loop runs; a launch runs several ticks."""
+    from lighthouse2_gb300.server import RenderServer
+    (sa, ca), (sb, cb) = two_scenes
+    cores = [ca, cb]
+    expect = []
+    for j in JOBS:
+        view, p = job_inputs(*j)
+        expect.append(plain_core_image(cores[j[0]], view, p))
+    opts = {"deviceLoop": 1}
+    if tick_budget:
+        opts["tickBudget"] = tick_budget
+    srv = RenderServer(path_capacity=1 << 16, **opts)
+    sid = [srv.add_scene(ca), srv.add_scene(cb)]
+    for rnd in range(2):
+        ids = []
+        for k, j in enumerate(JOBS):
+            view, p = job_inputs(*j)
+            ids.append(srv.submit_render(sid[j[0]], view, p))
+            if rnd == 1 and k == 1:
+                srv.wait(ids[0])            # later jobs arrive while earlier ones run
+        for k, jid in enumerate(ids):
+            srv.wait(jid)
+            assert np.array_equal(srv.result(jid).view(np.uint32), expect[k].view(np.uint32)), f"job {k} differs (round {rnd})"
+            srv.release(jid)
+    st = srv.stats()
+    assert st["deviceStatus"] == 0 and st["pathsInFlight"] == 0 and st["jobsDone"] == 2 * len(JOBS)
+    assert 0 < st["loopLaunches"] < st["ticks"], st   # launches ran more than one tick each on average
     srv.close()
