@@ -840,7 +840,10 @@ int lh2g_setting(lh2g_context* ctx, const char* name, float value) {
     else if (!strcmp(name, "clampIndirect")) ctx->clampIndirect = value;
     else if (!strcmp(name, "filter")) ctx->filterEnabled = value == 0 ? 0 : 1;
     else if (!strcmp(name, "TAA")) ctx->taaEnabled = value == 0 ? 0 : 1;
-    else if (!strcmp(name, "sortConnections")) ctx->sortConnections = value == 0 ? 0 : 1;
+    else if (!strcmp(name, "sortConnections")) {
+        if (value != 0.0f && value != 1.0f && value != 2.0f) return fail(ctx, LH2G_ERR_INVALID, "setting sortConnections: 0, 1 (by light) or 2 (by light within chunks)");
+        ctx->sortConnections = (int)value;
+    }
     else if (!strcmp(name, "sortRays")) ctx->sortRays = value == 0 ? 0 : 1;
     else if (!strcmp(name, "waveOccupancy")) {
         /* fraction of a full GPU the persistent wave kernels of one frame take (frames in flight share the rest) */
@@ -1089,7 +1092,10 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
         if (ctx->sortConnections) {   /* one timed slot: the regrouping and the any-hit queries */
             WaveBuffers Bs = B;
             Bs.shO = B.sortO, Bs.shD = B.sortD, Bs.shE = B.sortE;
-            mark(), launch_sort_connections(B, d, st), launch_connect(S, F, Bs, d, ctx->blocksConnect, st), mark();
+            mark();
+            if (ctx->sortConnections == 2) launch_sort_connections_local(B, d, st);
+            else launch_sort_connections(B, d, st);
+            launch_connect(S, F, Bs, d, ctx->blocksConnect, st), mark();
         } else {
             mark(), launch_connect(S, F, B, d, ctx->blocksConnect, st), mark();
         }

@@ -337,6 +337,47 @@ __global__ void k_conn_scatter(const WaveBuffers B, const int depth) {
     }
 }
 
+/* Connections grouped by light within chunks of CONN_CHUNK consecutive queue entries (setting "sortConnections" 2):
+ * a counting sort in shared memory per chunk. The queue is in shading order, which follows the primary rays' pixel
+ * tiles, so a chunk's connections start from one region of the image; grouped by light, a warp's shadow rays then
+ * share both their origin region and their target and visit much the same nodes. Entries do not leave their chunk. */
+constexpr uint32_t CONN_CHUNK = 1024;
+__global__ void __launch_bounds__(256) k_conn_local(const WaveBuffers B, const int depth) {
+    __shared__ uint32_t cnt[64], off[64];
+    const uint32_t n = B.counters->shadow[depth - 1];
+    for (uint32_t c0 = blockIdx.x * CONN_CHUNK; c0 < n; c0 += gridDim.x * CONN_CHUNK) {
+        if (threadIdx.x < 64) cnt[threadIdx.x] = 0;
+        __syncthreads();
+        uint32_t bin[4], rank[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const uint32_t i = c0 + threadIdx.x + 256u * k;
+            bin[k] = 64u, rank[k] = 0;
+            if (i < n) bin[k] = (__float_as_uint(B.shE[i].w) >> 1) & 63u, rank[k] = atomicAdd(&cnt[bin[k]], 1u);
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {   /* exclusive prefix over the 64 bins, two per lane */
+            const uint32_t lane = threadIdx.x, a = cnt[2 * lane], b = cnt[2 * lane + 1];
+            uint32_t sum = a + b;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, sum, d);
+                if (lane >= (uint32_t)d) sum += v;
+            }
+            const uint32_t excl = sum - (a + b);
+            off[2 * lane] = excl, off[2 * lane + 1] = excl + a;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (bin[k] == 64u) continue;
+            const uint32_t i = c0 + threadIdx.x + 256u * k, pos = c0 + off[bin[k]] + rank[k];
+            B.sortO[pos] = B.shO[i], B.sortD[pos] = B.shD[i], B.sortE[pos] = B.shE[i];
+        }
+        __syncthreads();
+    }
+}
+
 /* --------------------------------------------------------------------------------------------------
  * Extension rays grouped by direction octant before a bounce wave's closest-hit queries (setting "sortRays"): a
  * counting sort over 8 bins of the queue into sortO/D/E; within a bin, each warp's rays stay together and in order,
@@ -566,6 +607,9 @@ void launch_sort_connections(const WaveBuffers& B, int depth, cudaStream_t st) {
     k_conn_count<<<sm_count() * 4, 256, 0, st>>>(B, depth);
     k_conn_scan<<<1, 64, 0, st>>>(B);
     k_conn_scatter<<<sm_count() * 8, 256, 0, st>>>(B, depth);
+}
+void launch_sort_connections_local(const WaveBuffers& B, int depth, cudaStream_t st) {
+    k_conn_local<<<sm_count() * 8, 256, 0, st>>>(B, depth);
 }
 void launch_sort_rays(const WaveBuffers& B, int depth, cudaStream_t st) {
     k_ray_count<<<sm_count() * 4, 256, 0, st>>>(B, depth);

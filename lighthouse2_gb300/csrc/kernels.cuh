@@ -50,6 +50,8 @@ void launch_tail(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int
 void launch_sort_rays(const WaveBuffers& B, int depth, cudaStream_t st);
 /* the connections of wave `depth` regrouped by light into sortO/D/E (counting sort over 64 bins) */
 void launch_sort_connections(const WaveBuffers& B, int depth, cudaStream_t st);
+/* connections grouped by light within chunks of consecutive queue entries, into sortO/D/E */
+void launch_sort_connections_local(const WaveBuffers& B, int depth, cudaStream_t st);
 /* per-pixel sums of the frame's paths into the accumulator (from zero when overwrite != 0), then the frame */
 void launch_finalize(const FrameGPU& F, const WaveBuffers& B, float scale, int overwrite, cudaStream_t st);
 /* radiance-cache frames: gather queries / training samples (counts[0], counts[1]), then add the predictions */
