@@ -43,9 +43,9 @@ W_DEFAULT, H_DEFAULT = 1920, 1080
 MAX_DEPTH, RR_START = 8, 4
 WAVE_TAIL = 5          # path lengths >= 5 run in the persistent tail kernel (setting "waveTail")
 LANES = 4              # frames in flight (setting "pipelineFrames")
-# ncu dram__bytes_read.sum + dram__bytes_write.sum of two k_extend launches of this workload (waves 2 and 3 of
-# camera pose 1): 196.85 MB + 74.09 MB (profiles/k_extend_spheres_2m_1080p.md)
-EXTEND_CAPTURE = {"pose": 1, "waves": (2, 3), "dram_bytes": 196.84736e6 + 74.086912e6}
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of three k_extend launches of this workload (waves 1, 2 and 3
+# of camera pose 1): 197.65 MB + 197.72 MB + 74.47 MB (profiles/k_extend_spheres_2m_1080p.md)
+EXTEND_CAPTURE = {"pose": 1, "waves": (1, 2, 3), "dram_bytes": (152.189696e6 + 45.460992e6) + (151.02464e6 + 46.699264e6) + (63.042816e6 + 11.42272e6)}
 WORKLOAD = "spheres_2m: 64 x 32k-tri displaced spheres + ground (2,048,002 tris, 66 instances), 16 quad + 4 point lights, " \
            "20 materials (4 textured), sky; 1920x1080 1spp, max depth 8, RR after depth 3, NEE"
 METRIC = "Mrays/s @1080p 1spp"
@@ -947,7 +947,7 @@ def run_gb300(args):
     traffic = None
     if dom == "extend":
         # DRAM bytes per ray from the ncu capture of the same workload, scaled to this run's mean launch
-        rays_captured = sum(int(counts[EXTEND_CAPTURE["pose"]][w - 2, 0]) for w in EXTEND_CAPTURE["waves"])
+        rays_captured = sum(W * H if w == 1 else int(counts[EXTEND_CAPTURE["pose"]][w - 2, 0]) for w in EXTEND_CAPTURE["waves"])
         traffic = EXTEND_CAPTURE["dram_bytes"] / rays_captured * (b_dom / n_dom) / algorithmic_bytes("extend", 1, 0, 0)
     line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "strong" if split else "weak", "vs_baseline": None, "dtype": "f32",
