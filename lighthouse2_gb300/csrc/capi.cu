@@ -844,7 +844,10 @@ int lh2g_setting(lh2g_context* ctx, const char* name, float value) {
         if (value != 0.0f && value != 1.0f && value != 2.0f) return fail(ctx, LH2G_ERR_INVALID, "setting sortConnections: 0, 1 (by light) or 2 (by light within chunks)");
         ctx->sortConnections = (int)value;
     }
-    else if (!strcmp(name, "sortRays")) ctx->sortRays = value == 0 ? 0 : 1;
+    else if (!strcmp(name, "sortRays")) {
+        if (value != 0.0f && value != 1.0f && value != 2.0f) return fail(ctx, LH2G_ERR_INVALID, "setting sortRays: 0, 1 (by octant) or 2 (by octant within chunks)");
+        ctx->sortRays = (int)value;
+    }
     else if (!strcmp(name, "waveOccupancy")) {
         /* fraction of a full GPU the persistent wave kernels of one frame take (frames in flight share the rest) */
         if (!(value > 0.0f && value <= 1.0f)) return fail(ctx, LH2G_ERR_INVALID, "setting waveOccupancy: (0, 1]");
@@ -1084,7 +1087,10 @@ int render_frame(lh2g_context* ctx, const lh2g_view* view, const lh2g_render_par
         if (ctx->sortRays && d >= 2) {
             const int q = (d - 1) & 1;
             Bq.O[q] = B.sortO, Bq.D[q] = B.sortD, Bq.T[q] = B.sortE;
-            mark(), launch_sort_rays(B, d, st), launch_extend(S, F, Bq, d, ctx->blocksExtend, st), mark();
+            mark();
+            if (ctx->sortRays == 2) launch_sort_rays_local(B, d, st);
+            else launch_sort_rays(B, d, st);
+            launch_extend(S, F, Bq, d, ctx->blocksExtend, st), mark();
         } else {
             mark(), launch_extend(S, F, Bq, d, ctx->blocksExtend, st), mark();
         }

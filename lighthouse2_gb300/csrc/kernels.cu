@@ -611,6 +611,42 @@ void launch_sort_connections(const WaveBuffers& B, int depth, cudaStream_t st) {
 void launch_sort_connections_local(const WaveBuffers& B, int depth, cudaStream_t st) {
     k_conn_local<<<sm_count() * 8, 256, 0, st>>>(B, depth);
 }
+/* Extension rays grouped by direction octant within chunks of RAY_CHUNK consecutive queue entries (setting "sortRays"
+ * 2): the queue follows the primary rays' pixel tiles, so a chunk's rays start from one region of the image; grouped
+ * by octant within it, a warp's rays share origin region and direction octant. */
+constexpr uint32_t RAY_CHUNK = 1024;
+__global__ void __launch_bounds__(256) k_ray_local(const WaveBuffers B, const int depth) {
+    __shared__ uint32_t cnt[8], off[8];
+    const int q = (depth - 1) & 1;
+    const uint32_t n = B.counters->extension[depth - 2];
+    for (uint32_t c0 = blockIdx.x * RAY_CHUNK; c0 < n; c0 += gridDim.x * RAY_CHUNK) {
+        if (threadIdx.x < 8) cnt[threadIdx.x] = 0;
+        __syncthreads();
+        uint32_t bin[4], rank[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const uint32_t i = c0 + threadIdx.x + 256u * k;
+            bin[k] = 8u, rank[k] = 0;
+            if (i < n) bin[k] = ray_octant(B.D[q][i]), rank[k] = atomicAdd(&cnt[bin[k]], 1u);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t acc = 0;
+            for (int b = 0; b < 8; b++) off[b] = acc, acc += cnt[b];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (bin[k] == 8u) continue;
+            const uint32_t i = c0 + threadIdx.x + 256u * k, pos = c0 + off[bin[k]] + rank[k];
+            B.sortO[pos] = B.O[q][i], B.sortD[pos] = B.D[q][i], B.sortE[pos] = B.T[q][i];
+        }
+        __syncthreads();
+    }
+}
+void launch_sort_rays_local(const WaveBuffers& B, int depth, cudaStream_t st) {
+    k_ray_local<<<sm_count() * 8, 256, 0, st>>>(B, depth);
+}
 void launch_sort_rays(const WaveBuffers& B, int depth, cudaStream_t st) {
     k_ray_count<<<sm_count() * 4, 256, 0, st>>>(B, depth);
     k_conn_scan<<<1, 64, 0, st>>>(B);

@@ -48,6 +48,8 @@ void launch_connect(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, 
 void launch_tail(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int startDepth, int persistentBlocks, cudaStream_t st);
 /* the extension queue of wave `depth` (>= 2) regrouped by direction octant into sortO/D/E (O, D, T) */
 void launch_sort_rays(const WaveBuffers& B, int depth, cudaStream_t st);
+/* extension rays grouped by direction octant within chunks of consecutive queue entries, into sortO/D/E */
+void launch_sort_rays_local(const WaveBuffers& B, int depth, cudaStream_t st);
 /* the connections of wave `depth` regrouped by light into sortO/D/E (counting sort over 64 bins) */
 void launch_sort_connections(const WaveBuffers& B, int depth, cudaStream_t st);
 /* connections grouped by light within chunks of consecutive queue entries, into sortO/D/E */

@@ -246,10 +246,11 @@ def test_all_rays_miss(spheres_small):
     assert np.isfinite(img).all() and img[:, :3].min() > 0
 
 
-@pytest.mark.parametrize("tail", [0, 5])
-def test_rays_grouped_by_octant_change_nothing(core_lib, oracle_lib, tail):
+@pytest.mark.parametrize("tail,mode", [(0, 1), (5, 1), (0, 2), (5, 2)])
+def test_rays_grouped_by_octant_change_nothing(core_lib, oracle_lib, tail, mode):
     """Regrouping each bounce wave's extension rays by direction octant before the closest-hit queries (setting
-    "sortRays") reorders work only: hit records, RNG states, queue counts and radiance equal the oracle's."""
+    "sortRays": 1 over the whole queue, 2 within chunks of it) reorders work only: hit records, RNG states, queue
+    counts and radiance equal the oracle's."""
     sc = S.spheres_2m(seed=5, n_spheres=6, slices=40, stacks=26, tex_size=64)
     W, H = 160, 96
     view = S.spheres_view(W, H, frame=1)
@@ -258,10 +259,10 @@ def test_rays_grouped_by_octant_change_nothing(core_lib, oracle_lib, tail):
     core.set_scene(sc)
     core.SetTarget(W, H, 2)
     core.Setting("waveTail", tail)
-    core.Setting("sortRays", 1)
+    core.Setting("sortRays", mode)
     o = oracle_lib.Oracle()
     o.set_scene(sc)
     _check_frame(core, o, view, p)
-    core.Setting("sortConnections", 1)   # both regroupings share the sort buffers
+    core.Setting("sortConnections", mode)   # both regroupings share the sort buffers
     _check_frame(core, o, view, p)
     core.close()
