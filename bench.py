@@ -368,6 +368,7 @@ def estimators_leg(core, sc, W, H, steps):
     n_room = max(4, steps // 4)
     for k in range(n_room):
         o7t(k, False, rc, room_view)
+    rc.stream_ptr()   # joins the frames in flight into the core's stream
     with torch.cuda.stream(rstream):
         e1.record()
     torch.cuda.synchronize()
