@@ -127,3 +127,20 @@ def test_live_lighttree(oracle_lib):
         assert not r["flushed"]
         assert np.array_equal(a["counters"], r["counters"])
         assert _close(a["accum"], r["accum"])
+
+
+def test_core_host_build_errors(core_lib):
+    """lh2g_build_light_tree returns minus an error code: -LH2G_ERR_OVERFLOW when the output holds too few records,
+    -LH2G_ERR_INVALID for negative counts."""
+    import ctypes as C
+    from lighthouse2_gb300.core import load_library, LIGHT_TREE_DTYPE
+    lib = load_library()
+    sc = S.lit_room(grid=2, n_points=1, n_spots=1)
+    tri = np.ascontiguousarray(sc.tri_lights)
+    out = np.zeros(4, LIGHT_TREE_DTYPE)
+    p = lambda a: a.ctypes.data_as(C.c_void_p)
+    assert lib.lh2g_build_light_tree(p(tri), len(tri), None, 0, None, 0, p(out), 4) == -5       # needs 16 records
+    assert lib.lh2g_build_light_tree(p(tri), -1, None, 0, None, 0, p(out), 4) == -1
+    n = 2 * len(tri)
+    big = np.zeros(n, LIGHT_TREE_DTYPE)
+    assert lib.lh2g_build_light_tree(p(tri), len(tri), None, 0, None, 0, p(big), n) == n
