@@ -108,19 +108,32 @@ constexpr uint32_t SMEM_SLACK = 1024 + 64;
 /* ---------------------------------------------------------------------------------------------------------
  * inference: out[i] = MLP(encode(query[i])), 4 floats per query (rgb, 0)
  * ------------------------------------------------------------------------------------------------------- */
-constexpr uint32_t INFER_SMEM = WEIGHT_BYTES + ACT_BYTES + SMEM_SLACK;
+/* tuning switch: query tiles per CTA (1 or 2). With 2, a CTA of 256 threads encodes two tiles of 128 queries at
+ * once and issues both tiles' products per layer under one commit: the weights are staged once for both, and more
+ * warps per SM wait on the hash-grid gathers (3 CTAs of 8 warps instead of 4 of 4). Measured 5 % slower (1M queries
+ * in 0.675 against 0.645 ms): the gathers are bound by L2 sector traffic (96 gathers of 4 B per query, each a
+ * 32-byte sector, about 5 TB/s of L2 reads), not by the warps waiting on them. 1 is the default. */
+#ifndef LH2G_NRC_INFER_TILES
+#define LH2G_NRC_INFER_TILES 1
+#endif
+constexpr int INFER_TILES = LH2G_NRC_INFER_TILES;
+static_assert(INFER_TILES == 1 || INFER_TILES == 2, "one or two tiles per CTA");
+constexpr uint32_t INFER_SMEM = WEIGHT_BYTES + INFER_TILES * ACT_BYTES + SMEM_SLACK;
+constexpr uint32_t INFER_TMEM_COLS = 64 * INFER_TILES;
 
-__global__ void __launch_bounds__(TILE) k_infer(const GridSpec G, const __half2* __restrict__ grid, const __nv_bfloat16* __restrict__ W,
-                                                const float4* __restrict__ queries, const long long nMax, const uint32_t* __restrict__ nDev,
-                                                float4* __restrict__ out, uint32_t* errors) {
+__global__ void __launch_bounds__(TILE * INFER_TILES) k_infer(const GridSpec G, const __half2* __restrict__ grid, const __nv_bfloat16* __restrict__ W,
+                                                              const float4* __restrict__ queries, const long long nMax, const uint32_t* __restrict__ nDev,
+                                                              float4* __restrict__ out, uint32_t* errors) {
     /* query count: nMax, or the count a previous kernel left in device memory (at most nMax) */
     const long long n = nDev ? min((long long)*nDev, nMax) : nMax;
     extern __shared__ unsigned char dyn[];
     Shared& sh = *reinterpret_cast<Shared*>(dyn);
     unsigned char* Ws = tiles_base(dyn);
-    unsigned char* A = Ws + WEIGHT_BYTES;
+    /* this thread's tile of the CTA and its row in it; its warp reads TMEM lanes 32 (warp % 4) .. + 31 */
+    const uint32_t sub = threadIdx.x / TILE, row = threadIdx.x % TILE;
+    unsigned char* A = Ws + WEIGHT_BYTES + sub * ACT_BYTES;
     if (threadIdx.x < 32) {
-        tc::tmem_alloc(&sh.tmem, 64);
+        tc::tmem_alloc(&sh.tmem, INFER_TMEM_COLS);
         tc::tmem_relinquish();
     }
     if (threadIdx.x == 0) {
@@ -132,11 +145,12 @@ __global__ void __launch_bounds__(TILE) k_infer(const GridSpec G, const __half2*
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    const uint32_t tmem = sh.tmem, aAddr = tc::smem_u32(A), wAddr = tc::smem_u32(Ws);
+    const uint32_t tmem = sh.tmem, a0 = tc::smem_u32(Ws + WEIGHT_BYTES), wAddr = tc::smem_u32(Ws);
+    const uint32_t myD = tmem + 64u * sub + ((row & ~31u) << 16);
     uint32_t phase = 0;
     const long long tiles = (n + TILE - 1) / TILE;
-    for (long long t = blockIdx.x; t < tiles; t += gridDim.x) {
-        const long long q = t * TILE + threadIdx.x;
+    for (long long t = (long long)blockIdx.x * INFER_TILES; t < tiles; t += (long long)gridDim.x * INFER_TILES) {
+        const long long q = (t + sub) * TILE + row;
         float v[IN];
         if (q < n) {
             float4 qq[4];
@@ -147,23 +161,29 @@ __global__ void __launch_bounds__(TILE) k_infer(const GridSpec G, const __half2*
 #pragma unroll
             for (int i = 0; i < IN; i++) v[i] = 0.0f;
         }
-        store_row64(A, threadIdx.x, v);
+        store_row64(A, row, v);
         for (int l = 0; l < LAYERS; l++) {
             tc::fence_proxy_async();
             tc::fence_before_sync();
             __syncthreads();
-            if (threadIdx.x == 0) issue_gemm(tmem, aAddr, wAddr + layer_offset(l), IN, layer_rows(l), &sh.mbar);
+            if (threadIdx.x == 0) {
+                tc::fence_after_sync();
+                for (int s2 = 0; s2 < INFER_TILES; s2++)
+                    issue_mma(tmem + 64u * (uint32_t)s2, a0 + (uint32_t)s2 * ACT_BYTES, wAddr + layer_offset(l), IN, layer_rows(l), false);
+                tc::mma_commit(&sh.mbar);
+            }
             if (!tc::mbar_wait(&sh.mbar, phase, WAIT_LIMIT)) sh.failed = 1;
             phase ^= 1u;
             tc::fence_after_sync();
             if (l < LAYERS - 1) {
-                read_row(tmem, 4, v);
+#pragma unroll
+                for (int c = 0; c < 4; c++) tc::tmem_ld16(myD + (uint32_t)(16 * c), v + 16 * c);
 #pragma unroll
                 for (int i = 0; i < HID; i++) v[i] = fmaxf(v[i], 0.0f);
-                store_row64(A, threadIdx.x, v);
+                store_row64(A, row, v);
             } else {
                 float y[16];
-                read_row(tmem, 1, y);
+                tc::tmem_ld16(myD, y);
                 if (q < n) out[q] = make_float4(y[0], y[1], y[2], 0.0f);
             }
         }
@@ -174,7 +194,7 @@ __global__ void __launch_bounds__(TILE) k_infer(const GridSpec G, const __half2*
     __syncthreads();
     if (threadIdx.x == 0 && sh.failed) atomicOr(errors, ERR_TIMEOUT);
     tc::fence_after_sync();
-    if (threadIdx.x < 32) tc::tmem_dealloc(tmem, 64);
+    if (threadIdx.x < 32) tc::tmem_dealloc(tmem, INFER_TMEM_COLS);
 }
 
 /* ---------------------------------------------------------------------------------------------------------
@@ -546,12 +566,12 @@ int lh2g_nrc_create(int device, const lh2g_nrc_config* cfg, lh2g_nrc** out) {
     int sms = 1, per = 0, smemSM = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     cudaDeviceGetAttribute(&smemSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_infer, TILE, INFER_SMEM) != cudaSuccess) per = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_infer, TILE * INFER_TILES, INFER_SMEM) != cudaSuccess) per = 0;
     /* resident CTAs per SM: what shared memory allows with the carveout above (1 KB reserved per CTA; the
-     * calculator may assume a smaller carveout), at most 4 (4 x 64 of the SM's 512 TMEM columns). Surplus CTAs
-     * would only wait: the kernel strides over its tiles. */
+     * calculator may assume a smaller carveout), at most what the SM's 512 TMEM columns hold. Surplus CTAs would
+     * only wait: the kernel strides over its tiles. */
     per = std::max(per, smemSM / (int)(INFER_SMEM + 1024));
-    c->blocksInfer = sms * std::max(1, std::min(per, 4));
+    c->blocksInfer = sms * std::max(1, std::min(per, (int)(512 / INFER_TMEM_COLS)));
     c->blocksTrain = sms;
     if (launch_copies(c) != LH2G_OK || cudaStreamSynchronize(c->st) != cudaSuccess) return fail(LH2G_ERR_CUDA);
     *out = c;
@@ -615,8 +635,8 @@ static int infer_launch(lh2g_nrc* c, const float* queries, long long nMax, const
     cudaSetDevice(c->device);
     cudaStream_t st = stream ? (cudaStream_t)stream : c->st;
     const long long tiles = (nMax + TILE - 1) / TILE;
-    const int blocks = (int)std::min<long long>(tiles, c->blocksInfer);
-    k_infer<<<blocks, TILE, INFER_SMEM, st>>>(c->G, reinterpret_cast<const __half2*>(c->grid16), c->Wdev, reinterpret_cast<const float4*>(queries), nMax,
+    const int blocks = (int)std::min<long long>((tiles + INFER_TILES - 1) / INFER_TILES, c->blocksInfer);
+    k_infer<<<blocks, TILE * INFER_TILES, INFER_SMEM, st>>>(c->G, reinterpret_cast<const __half2*>(c->grid16), c->Wdev, reinterpret_cast<const float4*>(queries), nMax,
                                              nDev, reinterpret_cast<float4*>(out), c->dErr);
     NCK(cudaGetLastError());
     return LH2G_OK;
