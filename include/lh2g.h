@@ -91,10 +91,14 @@ LH2G_API int lh2g_set_blue_noise(lh2g_context* ctx, const uint8_t* sobol, const 
  * run to their end in one persistent kernel; 0: one launch per stage and wave throughout) and "pipelineFrames"
  * (frames in flight, 0..4, default 4; 0 and 1 render one frame at a time; see lh2g_get_stream) and "waveOccupancy"
  * (fraction of the GPU the persistent wave kernels of one frame launch, (0, 1], default 1) and "sortConnections"
- * (1: group each wave's light connections by the light they sample before the any-hit queries; default 0).
+ * (1: group each wave's light connections by the light they sample before the any-hit queries, 2: the same within
+ * chunks of 1,024 consecutive connections; default 0) and "sortRays" (1: group each bounce wave's extension rays by
+ * direction octant before the closest-hit queries, 2: within chunks of 1,024; default 0).
  * Estimator of lh2g_render: "estimator" 0 (PrimeRef, default) or 1 (the OptiX 7 core's, LH2G_RP_OPTIX7; one camera
  * seed drawn per wave of maxDepth, where the reference draws only for the waves its loop runs), "adaptive" 1
- * (PrimeAdaptive frames, lh2g_render_adaptive). Both draw a blue-noise shift per frame from seed 0x11331445. */
+ * (PrimeAdaptive frames, lh2g_render_adaptive). Both draw a blue-noise shift per frame from seed 0x11331445.
+ * "bsdf" 1: those estimators with the Disney BSDF (LH2G_RP_DISNEY); "lightTree" 1: the OptiX 7 estimator selects
+ * lights through the light tree (LH2G_RP_LIGHTTREE). */
 LH2G_API int lh2g_setting(lh2g_context* ctx, const char* name, float value);
 /* SetTarget (core_api_base.h:93), headless: the output is a device float4 buffer of width*height pixels. */
 LH2G_API int lh2g_set_target(lh2g_context* ctx, int width, int height, int spp);
