@@ -42,7 +42,7 @@ sys.path.insert(0, ROOT)
 W_DEFAULT, H_DEFAULT = 1920, 1080
 MAX_DEPTH, RR_START = 8, 4
 WAVE_TAIL = 5          # path lengths >= 5 run in the persistent tail kernel (setting "waveTail")
-LANES = 4              # frames in flight (setting "pipelineFrames")
+LANES = 6              # frames in flight (setting "pipelineFrames")
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of three k_extend launches of this workload (waves 1, 2 and 3
 # of camera pose 1): 197.65 MB + 197.72 MB + 74.47 MB (profiles/k_extend_spheres_2m_1080p.md)
 EXTEND_CAPTURE = {"pose": 1, "waves": (1, 2, 3), "dram_bytes": (152.189696e6 + 45.460992e6) + (151.02464e6 + 46.699264e6) + (63.042816e6 + 11.42272e6)}

@@ -89,7 +89,7 @@ LH2G_API int lh2g_set_blue_noise(lh2g_context* ctx, const uint8_t* sobol, const 
  * renders filter-core frames (LH2G_RP_FILTER, Halton-jittered when TAA is on) and denoises them with SVGF.
  * Scheduling settings of this core (results do not change): "waveTail" (default 5; path lengths from this one on
  * run to their end in one persistent kernel; 0: one launch per stage and wave throughout) and "pipelineFrames"
- * (frames in flight, 0..4, default 4; 0 and 1 render one frame at a time; see lh2g_get_stream) and "waveOccupancy"
+ * (frames in flight, 0..8, default 6; 0 and 1 render one frame at a time; see lh2g_get_stream) and "waveOccupancy"
  * (fraction of the GPU the persistent wave kernels of one frame launch, (0, 1], default 1) and "sortConnections"
  * (1: group each wave's light connections by the light they sample before the any-hit queries, 2: the same within
  * chunks of 1,024 consecutive connections; default 0) and "sortRays" (1: group each bounce wave's extension rays by

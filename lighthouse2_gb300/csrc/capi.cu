@@ -224,12 +224,12 @@ struct lh2g_context {
     cudaEvent_t fev[2] = {nullptr, nullptr};   /* around the filter passes: coreStats.filterTime */
     bool filterPending = false;
     lh2g_filter_params lastFilter;
-    NrcBuffers nrcBuf[4];              /* radiance-cache frame buffers per lane (lane 0 also for frames on the context stream) */
+    NrcBuffers nrcBuf[8];              /* radiance-cache frame buffers per lane, MAX_LANES (lane 0 also for frames on the context stream) */
     cudaEvent_t cacheEv = nullptr;     /* the last queued radiance-cache work: the next frame's cache work waits for it */
     bool cacheEvValid = false;
     lh2g_view lastJittered;
     lh2g_render_params lastParams;
-    /* Frame pipelining (setting "pipelineFrames" = frames in flight, default 4): plain frames rotate over lanes,
+    /* Frame pipelining (setting "pipelineFrames" = frames in flight, default 6, at most MAX_LANES): plain frames rotate over lanes,
      * each with its own stream and path-state buffers (lane 0 uses B's, the others their own), so that the sparse
      * last waves of one frame overlap the first waves of the next. The accumulator and the frame are shared: finalizes run
      * in submission order (finEv). A lane frame waits for everything enqueued on the context stream before it
@@ -243,9 +243,10 @@ struct lh2g_context {
         bool pending = false;
         bool ready = false;
     };
-    static constexpr int MAX_LANES = 4;
+    static constexpr int MAX_LANES = 8;
+    static_assert(sizeof(nrcBuf) / sizeof(nrcBuf[0]) == MAX_LANES, "a radiance-cache buffer set per lane");
     Lane lanes[MAX_LANES];
-    int pipelineFrames = 4;            /* lanes in use; 0 or 1: one frame at a time */
+    int pipelineFrames = 6;            /* lanes in use; 0 or 1: one frame at a time */
     int sortConnections = 0;           /* group each wave's connections by light before the any-hit queries */
     int sortRays = 0;                  /* group each bounce wave's extension rays by direction octant before the closest-hit queries */
     int nextLane = 0;
@@ -855,7 +856,7 @@ int lh2g_setting(lh2g_context* ctx, const char* name, float value) {
         int* blocks[3] = {&ctx->blocksExtend, &ctx->blocksConnect, &ctx->blocksShade};
         for (int k = 0; k < 3; k++) *blocks[k] = std::max(1, (int)((float)ctx->fullBlocks[k] * value + 0.5f));
     } else if (!strcmp(name, "pipelineFrames")) {
-        if (value < 0 || value > lh2g_context::MAX_LANES) return fail(ctx, LH2G_ERR_INVALID, "setting pipelineFrames: 0..4 frames in flight");
+        if (value < 0 || value > lh2g_context::MAX_LANES) return fail(ctx, LH2G_ERR_INVALID, "setting pipelineFrames: 0..8 frames in flight");
         JOIN();
         ctx->pipelineFrames = (int)value;
         ctx->nextLane = 0;
