@@ -59,16 +59,6 @@ __device__ __forceinline__ uint32_t queue_count(const FrameGPU& F, const WaveBuf
 }
 
 /* -------------------------------------------------------------------------------------------------- */
-/* tuning switch: resident CTAs per SM the traversal kernels (k_extend, k_connect) are compiled for (register cap);
- * 0 leaves it to the compiler */
-#ifndef LH2G_TRAV_MINBLOCKS
-#define LH2G_TRAV_MINBLOCKS 0
-#endif
-#if LH2G_TRAV_MINBLOCKS > 0
-#define LH2G_TRAV_BOUNDS __launch_bounds__(128, LH2G_TRAV_MINBLOCKS)
-#else
-#define LH2G_TRAV_BOUNDS __launch_bounds__(128)
-#endif
 template <bool MIS>
 __global__ void LH2G_TRAV_BOUNDS k_extend(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int depth) {
     Counters* C = B.counters;

@@ -55,6 +55,17 @@ namespace lh2g {
 #define LH2G_SHORT_STACK 0
 #endif
 constexpr int LH2G_TRAV_BLOCK = 128;
+/* tuning switch: resident CTAs per SM the traversal kernels (k_extend, k_connect and the serving loop's) are compiled
+ * for, a register cap; 0 leaves it to the compiler (56 registers, 9 CTAs). 10 gives 48 registers without spills in
+ * k_extend: 1867 against 1817 Mrays/s on the 1080p frame (11 and 12: 40 registers with spills, 1846 at 12). */
+#ifndef LH2G_TRAV_MINBLOCKS
+#define LH2G_TRAV_MINBLOCKS 10
+#endif
+#if LH2G_TRAV_MINBLOCKS > 0
+#define LH2G_TRAV_BOUNDS __launch_bounds__(LH2G_TRAV_BLOCK, LH2G_TRAV_MINBLOCKS)
+#else
+#define LH2G_TRAV_BOUNDS __launch_bounds__(LH2G_TRAV_BLOCK)
+#endif
 /* LH2G_STAGE_RAYS 1: in the warp-batch loop (LH2G_REFILL 0, LH2G_COOP 0) the next 32 rays' path-state records
  * (the SoA arrays a kernel names: origins, directions, ...) are copied into the warp's shared-memory slot by bulk
  * asynchronous copies (cp.async.bulk, completion on an mbarrier) while the warp traces the current 32; 0 (the
