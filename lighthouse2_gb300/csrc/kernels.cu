@@ -180,12 +180,21 @@ __global__ void __launch_bounds__(WAVE_BLOCK) k_shade(const SceneGPU S, const Fr
  * the connection's any-hit query and its contribution, the next segment. Every per-path quantity (RNG states,
  * hit records, radiance and its order of accumulation, queue counts per path length) is the one the wave loop
  * produces. */
+/* tuning switch: resident CTAs per SM the tail kernel is compiled for (register cap); 0 leaves it to the compiler */
+#ifndef LH2G_TAIL_MINBLOCKS
+#define LH2G_TAIL_MINBLOCKS 0
+#endif
+#if LH2G_TAIL_MINBLOCKS > 0
+#define LH2G_TAIL_BOUNDS __launch_bounds__(WAVE_BLOCK, LH2G_TAIL_MINBLOCKS)
+#else
+#define LH2G_TAIL_BOUNDS __launch_bounds__(WAVE_BLOCK)
+#endif
 template <bool MIS>
-__global__ void __launch_bounds__(WAVE_BLOCK) k_tail(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int startDepth) {
+__global__ void LH2G_TAIL_BOUNDS k_tail(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int startDepth) {
     Counters* C = B.counters;
     const uint32_t count = queue_count(F, B, C, startDepth);
     const int q = (startDepth - 1) & 1;
-    __shared__ float potential[64 * WAVE_BLOCK];
+    extern __shared__ float potential[];   /* light-selection potentials, (lights) x 128 threads, sized at launch */
     float* pot = potential + threadIdx.x;
     uint32_t status = 0;
     unsigned long long cn = 0, ct = 0, an = 0, at = 0;
@@ -557,7 +566,7 @@ int persistent_blocks_wave(int which) {
          * shading loop is grid-stride, blocks beyond what shared memory lets reside simply start later */
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_shade<false>, WAVE_BLOCK, WAVE_BLOCK * sizeof(float));
     }
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_tail<false>, WAVE_BLOCK, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_tail<false>, WAVE_BLOCK, WAVE_BLOCK * sizeof(float));
     return sm_count() * (per > 0 ? per : 1);
 }
 
@@ -583,8 +592,12 @@ void launch_connect(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, 
     k_connect<<<blocks, 128, 0, st>>>(S, F, B, depth);
 }
 void launch_tail(const SceneGPU& S, const FrameGPU& F, const WaveBuffers& B, int startDepth, int blocks, cudaStream_t st) {
-    if (F.flags & MIS_FLAGS) k_tail<true><<<blocks, WAVE_BLOCK, 0, st>>>(S, F, B, startDepth);
-    else k_tail<false><<<blocks, WAVE_BLOCK, 0, st>>>(S, F, B, startDepth);
+    /* the potentials' shared memory as in launch_shade; the loop takes paths from a counter, so blocks beyond what
+     * shared memory lets reside start later */
+    const int lights = (F.flags & LH2G_RP_LIGHTTREE) ? 1 : std::max(1, S.nTri + S.nPoint + S.nSpot + S.nDir);
+    const size_t smem = (size_t)lights * WAVE_BLOCK * sizeof(float);
+    if (F.flags & MIS_FLAGS) k_tail<true><<<blocks, WAVE_BLOCK, smem, st>>>(S, F, B, startDepth);
+    else k_tail<false><<<blocks, WAVE_BLOCK, smem, st>>>(S, F, B, startDepth);
 }
 void launch_nrc_collect(const FrameGPU& F, const WaveBuffers& B, float4* queries, uint32_t* qPath, float4* trainQ, float4* trainT, uint32_t* counts,
                         uint32_t trainCap, cudaStream_t st) {
