@@ -247,7 +247,7 @@ __global__ void LH2G_TAIL_BOUNDS k_tail(const SceneGPU S, const FrameGPU F, cons
 }
 
 /* -------------------------------------------------------------------------------------------------- */
-__global__ void LH2G_TRAV_BOUNDS k_connect(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int depth) {
+__global__ void LH2G_CONNECT_BOUNDS k_connect(const SceneGPU S, const FrameGPU F, const WaveBuffers B, const int depth) {
     Counters* C = B.counters;
     const uint32_t count = C->shadow[depth - 1];
     uint32_t status = 0;

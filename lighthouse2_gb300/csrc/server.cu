@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(PART_TILE) k_srv_partition(ServerState* st, co
 }
 
 /* any hit of every connection; unoccluded ones add their contribution to their path */
-__global__ void LH2G_TRAV_BOUNDS k_srv_connect(const __grid_constant__ SceneTable scenes, const JobGPU* __restrict__ jobs, ServerState* st,
+__global__ void LH2G_CONNECT_BOUNDS k_srv_connect(const __grid_constant__ SceneTable scenes, const JobGPU* __restrict__ jobs, ServerState* st,
                                                      const Queues Q) {
     const uint32_t count = st->shadowCount;
     const uint32_t lane = threadIdx.x & 31u, firstRound = gridDim.x * blockDim.x;

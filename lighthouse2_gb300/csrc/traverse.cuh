@@ -66,6 +66,15 @@ constexpr int LH2G_TRAV_BLOCK = 128;
 #else
 #define LH2G_TRAV_BOUNDS __launch_bounds__(LH2G_TRAV_BLOCK)
 #endif
+/* the any-hit kernels' own cap (default: the same) */
+#ifndef LH2G_CONNECT_MINBLOCKS
+#define LH2G_CONNECT_MINBLOCKS LH2G_TRAV_MINBLOCKS
+#endif
+#if LH2G_CONNECT_MINBLOCKS > 0
+#define LH2G_CONNECT_BOUNDS __launch_bounds__(LH2G_TRAV_BLOCK, LH2G_CONNECT_MINBLOCKS)
+#else
+#define LH2G_CONNECT_BOUNDS __launch_bounds__(LH2G_TRAV_BLOCK)
+#endif
 /* LH2G_STAGE_RAYS 1: in the warp-batch loop (LH2G_REFILL 0, LH2G_COOP 0) the next 32 rays' path-state records
  * (the SoA arrays a kernel names: origins, directions, ...) are copied into the warp's shared-memory slot by bulk
  * asynchronous copies (cp.async.bulk, completion on an mbarrier) while the warp traces the current 32; 0 (the
