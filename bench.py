@@ -830,6 +830,8 @@ def run_gb300(args):
         core.SetTarget(W, H, 1)
     core.Setting("waveTail", args.wave_tail)
     core.Setting("pipelineFrames", args.lanes)
+    if args.wave_occupancy < 1.0:
+        core.Setting("waveOccupancy", args.wave_occupancy)
     core.Setting("sortConnections", args.sort_connections)
     core.Setting("sortRays", args.sort_rays)
     waves = min(MAX_DEPTH, args.wave_tail - 1) if args.wave_tail > 0 else MAX_DEPTH
@@ -1021,6 +1023,7 @@ def main():
     ap.add_argument("--serving-device-loop", type=int, default=-1,
                     help="1: the serving loop's ticks run in a device-side graph loop (its default), 0: host-driven ticks")
     ap.add_argument("--lanes", type=int, default=LANES, help="frames in flight (0 or 1: one at a time)")
+    ap.add_argument("--wave-occupancy", type=float, default=1.0, help="share of the GPU a frame's persistent wave kernels launch (setting waveOccupancy)")
     ap.add_argument("--partition", default="replicas", choices=["replicas", "rows"],
                     help="under torchrun: replicas (every rank renders whole frames) or rows (every frame's rows split over the ranks)")
     ap.add_argument("--sort-connections", type=int, default=0, help="group connections by light before the any-hit queries")
