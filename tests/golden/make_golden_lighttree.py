@@ -37,6 +37,30 @@ def scene():
     return sc
 
 
+# name, scene variant, W, H, depth, samplesTaken, shift
+MIX_FRAMES = [("m_points_spots", "points_spots", 48, 40, 6, 3, 0x5151), ("m_with_directional", "with_directional", 48, 40, 6, 3, 0x5151)]
+
+
+def mix_scene(kind):
+    """An 88-light room (a 3x3 ceiling grid, 40 point and 30 spot lights) in two variants. "points_spots": no area
+    lights, the ceiling tiles no longer emit, so the tree holds only point and spot lights and no path hits an
+    emitter. "with_directional": two directional lights as well, which the tree leaves out (with LIGHTTREE defined
+    the reference never picks a directional light)."""
+    sc = S.lit_room(seed=31, grid=3, n_points=40, n_spots=30)
+    if kind == "points_spots":
+        sc.tri_lights = sc.tri_lights[:0]
+        sc.materials["color"][8:] = (0.5, 0.5, 0.5)
+    else:
+        d = np.zeros(2, S.DIR_LIGHT_DTYPE)
+        d["direction"] = ((0.3, -1.0, 0.2), (-0.5, -0.7, 0.1))
+        d["direction"] /= np.linalg.norm(d["direction"], axis=1, keepdims=True)
+        d["radiance"] = (0.4, 0.4, 0.35)
+        d["energy"] = 1.15
+        sc.dir_lights = d
+    sc.blue_noise = S.synthetic_blue_noise(23)
+    return sc
+
+
 def main():
     from oracle import bind as B
     out = {}
@@ -50,6 +74,16 @@ def main():
     for name, W, H, spp, depth, st, shift in FRAMES:
         p = B.make_params(W, H, spp, max_depth=depth, samples_taken=st, camera_r0=B.camera_r0(st),
                           flags=B.RP_NEE | B.RP_OPTIX7 | B.RP_LIGHTTREE, shift=shift)
+        r = ref.render(o, sc, S.cornell_view(W, H), p)
+        assert not r["flushed"]
+        out[name + "/accum"] = r["accum"]
+        out[name + "/counters"] = r["counters"]
+        print(name, r["counters"][:, 0].tolist(), r["counters"][:, 1].tolist())
+    for name, kind, W, H, depth, st, shift in MIX_FRAMES:
+        sc = mix_scene(kind)
+        o = B.Oracle()
+        o.set_scene(sc)
+        p = B.make_params(W, H, 1, max_depth=depth, samples_taken=st, camera_r0=B.camera_r0(st), flags=B.RP_NEE | B.RP_OPTIX7 | B.RP_LIGHTTREE, shift=shift)
         r = ref.render(o, sc, S.cornell_view(W, H), p)
         assert not r["flushed"]
         out[name + "/accum"] = r["accum"]

@@ -3,7 +3,8 @@ oracle.
 
 The oracle's light tree and light-tree frames are pinned to the reference's own code (tests/test_oracle_lighttree.py).
 Here the GPU must match the oracle on a 164-light room (beyond the 64 lights selection by potentials takes) and on
-the two-light Cornell room: per path and depth the hit record and the RNG state after shading bit-exact (each level
+the two-light Cornell room, and on two light mixes of an 88-light room (point and spot lights only; with directional
+lights): per path and depth the hit record and the RNG state after shading bit-exact (each level
 of the tree draws six numbers from the path's seed, so the states also check the walks), per path length the
 extension and connection counts exact, per-pixel radiance within 1e-4 relative (the arithmetic and the summation
 order are the same, so it is expected to be identical). Frames of more than 64 lights without the tree, and the
@@ -108,4 +109,24 @@ def test_plugin_setting_and_refusals(core_lib):
     fn = core.lib.lh2g_render_noalloc
     rc = fn(core.ctx, view.ctypes.data_as(C.c_void_p), p.ctypes.data_as(C.c_void_p), C.c_void_p(acc.data_ptr()), None, C.byref(status))
     assert rc == 1   # LH2G_ERR_INVALID
+    core.close()
+
+
+@pytest.mark.parametrize("frame", range(2))
+def test_lighttree_light_mixes(core_lib, oracle_lib, frame):
+    """A tree of point and spot lights only (no path hits an emitter), and a room with two directional lights that
+    the tree leaves out: GPU frames equal the oracle's (the oracle's are pinned to the reference's)."""
+    from tests.golden import make_golden_lighttree as G
+    name, kind, W, H, D, st, shift = G.MIX_FRAMES[frame]
+    sc = G.mix_scene(kind)
+    core = RenderCore()
+    core.set_scene(sc)
+    o = oracle_lib.Oracle()
+    o.set_scene(sc)
+    core.SetTarget(W, H, 1)
+    p = make_params(W, H, 1, max_depth=D, samples_taken=st, camera_r0=camera_r0(st), flags=RP_NEE | RP_OPTIX7 | RP_LIGHTTREE, shift=shift)
+    g = core.render_ex(S.cornell_view(W, H), p, capture=True)
+    c = o.render(S.cornell_view(W, H), p, capture=True)
+    _compare(g, c, core.read_accumulator(), c["accum"])
+    assert g["counters"][:, 1].sum() > 0 and core.GetCoreStats()["deviceStatus"] == 0
     core.close()

@@ -94,6 +94,20 @@ def test_lighttree_frames(gold, oracle_lib):
         assert r["counters"][:, 1].sum() > 0
 
 
+def test_lighttree_light_mixes(gold, oracle_lib):
+    """A tree of point and spot lights only, and a room whose directional lights the tree leaves out."""
+    from tests.golden import make_golden_lighttree as G
+    B = oracle_lib
+    for name, kind, W, H, D, st, shift in G.MIX_FRAMES:
+        o = B.Oracle()
+        o.set_scene(G.mix_scene(kind))
+        p = B.make_params(W, H, 1, max_depth=D, samples_taken=st, camera_r0=B.camera_r0(st),
+                          flags=B.RP_NEE | B.RP_OPTIX7 | B.RP_LIGHTTREE, shift=shift)
+        r = o.render(S.cornell_view(W, H), p)
+        assert np.array_equal(r["counters"], gold[name + "/counters"]), name
+        assert _close(r["accum"], gold[name + "/accum"]), name
+
+
 def test_many_lights_need_the_tree(oracle_lib):
     """More than 64 lights: selection by potentials is refused (its arrays hold 64), the light tree renders."""
     B = oracle_lib
