@@ -10,6 +10,7 @@
  *
  * Stack entries are (code, tnear): code bits 31..30 = 00 node index, 01 leaf (bits 29..28 = count - 1,
  * bits 27..0 = first slot), 10 instance index; 0xffffffff marks the return from an instance to the TLAS.
+ * With LH2G_GROUP_STACK an entry holds a node's remaining hit children instead (see there).
  */
 #pragma once
 #include "core_types.cuh"
@@ -48,11 +49,27 @@ namespace lh2g {
 #ifndef LH2G_SORT_ANYHIT
 #define LH2G_SORT_ANYHIT 0
 #endif
+/* LH2G_GROUP_STACK 1: a node's hit children other than the one visited next go on the stack as ONE group entry
+ * (child base, leaf base, the meta bytes of the children not yet taken) instead of one entry each; a pop takes the
+ * group's lowest remaining slot and writes the rest back (after Ylitie, Karras and Laine, "Efficient Incoherent Ray
+ * Traversal on GPUs Through Compressed Wide BVHs", HPG 2017). Closest-hit queries visit the nearest hit child
+ * first and keep one entry distance per group, that of the nearest child, a lower bound of the others' for culling
+ * on pop; any-hit queries take children in slot order, as with LH2G_SORT_ANYHIT 0. No sorting network, no
+ * per-child push. LH2G_GSTACK entries of 20 B (one per level of the descent, plus instance markers). */
+#ifndef LH2G_GROUP_STACK
+#define LH2G_GROUP_STACK 0
+#endif
+#ifndef LH2G_GSTACK
+#define LH2G_GSTACK 32
+#endif
 /* LH2G_SHORT_STACK K (a power of two, 0: off): the top K entries of a lane's stack live in shared memory, a ring of
  * K slots strided by the block size; older entries spill to the local-memory stack when the ring is full and are
  * popped back from there. Every kernel that traverses with it runs LH2G_TRAV_BLOCK threads per block. */
 #ifndef LH2G_SHORT_STACK
 #define LH2G_SHORT_STACK 0
+#endif
+#if LH2G_GROUP_STACK && (LH2G_COOP || LH2G_SHORT_STACK)
+#error "LH2G_GROUP_STACK is a variant of the one-lane-per-ray traversal with the local-memory stack"
 #endif
 constexpr int LH2G_TRAV_BLOCK = 128;
 /* tuning switch: resident CTAs per SM the traversal kernels (k_extend, k_connect and the serving loop's) are compiled
@@ -144,7 +161,14 @@ LH2G_DEV void cx(uint32_t& a, uint32_t& b) { const uint32_t lo = min(a, b), hi =
  * that entry and pops the next; it returns false once the ray is finished. Kernels interleave step() with
  * per-lane refills of finished rays. */
 struct Traversal {
+#if LH2G_GROUP_STACK
+    static constexpr int CAP = LH2G_GSTACK;
+    uint4 stack[LH2G_GSTACK];   /* group {child base, leaf base, meta bytes lo, hi}; single entry {code, 0, 0, 0} */
+    float gnear[LH2G_GSTACK];   /* closest hit: a group's entry distance bound */
+#else
+    static constexpr int CAP = LH2G_STACK;
     uint2 stack[LH2G_STACK];
+#endif
     float3 Ow, Dw, O, D, invD;
     float tmin, tmax;
     int sp, curInst;
@@ -156,7 +180,7 @@ struct Traversal {
         return shortStack + threadIdx.x;
     }
 #endif
-    /* pushes one entry; the caller has checked sp < LH2G_STACK */
+    /* pushes one entry; the caller has checked sp < CAP */
     __device__ __forceinline__ void push(const uint2 e) {
 #if LH2G_SHORT_STACK
         uint2* r = ring();
@@ -166,6 +190,8 @@ struct Traversal {
         }
         r[(sp & (LH2G_SHORT_STACK - 1)) * LH2G_TRAV_BLOCK] = e;
         sp++;
+#elif LH2G_GROUP_STACK
+        stack[sp++] = make_uint4(e.x, 0u, 0u, 0u);
 #else
         stack[sp++] = e;
 #endif
@@ -179,6 +205,8 @@ struct Traversal {
         }
         --sp;
         return ring()[(sp & (LH2G_SHORT_STACK - 1)) * LH2G_TRAV_BLOCK];
+#elif LH2G_GROUP_STACK
+        return make_uint2(stack[--sp].x, 0u);
 #else
         return stack[--sp];
 #endif
@@ -233,6 +261,28 @@ struct Traversal {
     /* pops the next entry that can still hold a closer hit; false when the stack is empty */
     template <bool ANYHIT>
     __device__ __forceinline__ bool pop() {
+#if LH2G_GROUP_STACK
+        for (;;) {
+            if (sp == 0) return false;
+            const uint4 e = stack[sp - 1];
+            if ((e.z | e.w) == 0u) {   /* a single entry: an instance marker or the rest of a TLAS leaf */
+                sp--;
+                entry = e.x;
+                return true;
+            }
+            if (!ANYHIT && found && gnear[sp - 1] > best.t) { sp--; continue; }
+            /* the group's lowest remaining slot: its meta byte, then the rest written back (or the group dropped) */
+            const bool lo = e.z != 0u;
+            const uint32_t w = lo ? e.z : e.w;
+            const uint32_t sh = (uint32_t)(__ffs(w) - 1) & ~7u;
+            const uint32_t m = (w >> sh) & 255u, rest = w & ~(255u << sh);
+            if ((rest | (lo ? e.w : 0u)) == 0u) sp--;
+            else if (lo) stack[sp - 1].z = rest;
+            else stack[sp - 1].w = rest;
+            entry = (m & 0x80u) ? e.x + (m & 7u) : e.y + ((m >> 5) << 28) + (m & 31u);
+            return true;
+        }
+#else
         for (;;) {
             if (sp == 0) return false;
             const uint2 e = take();
@@ -240,6 +290,7 @@ struct Traversal {
             if (entry == ENTRY_MARKER || ANYHIT || (entry >> 30) == 2u) return true;
             if (!found || __uint_as_float(e.y) <= best.t) return true;
         }
+#endif
     }
 
     /* tests the 8 children of interior node `entry`. LH2G_SORT_CHILDREN 1: pushes the hit ones, nearest on top,
@@ -276,6 +327,7 @@ struct Traversal {
         const float limit = (!ANYHIT && found) ? best.t : tmax;
         uint32_t key[8];
         const uint32_t metaLo = n1.z, metaHi = n1.w;
+        uint32_t hlo = 0u, hhi = 0u;   /* LH2G_GROUP_STACK: 0xff in the bytes of the hit children */
 #pragma unroll
         for (int i = 0; i < 8; i++) {
             const uint32_t sel = 0x4440u | (uint32_t)(i & 3);
@@ -291,10 +343,41 @@ struct Traversal {
             const bool hit = meta != 0u && tn <= tf;
             /* key: distance with the low 3 bits replaced by the slot (rounded down: culling stays conservative) */
             key[i] = hit ? ((__float_as_uint(fmaxf(tn, 0.0f)) & ~7u) | (uint32_t)i) : 0xffffffffu;
+            if (LH2G_GROUP_STACK && hit) {
+                if (i < 4) hlo |= 0xffu << (8 * (i & 3));
+                else hhi |= 0xffu << (8 * (i & 3));
+            }
         }
         /* leaf code = kind | (count - 1) << 28 | first slot; the fields do not overlap, so it is a sum */
         const uint32_t leafBase = (curInst < 0 ? 0x80000000u : 0x40000000u) - (1u << 28) + n1.y;
-#if !LH2G_SORT_CHILDREN
+#if LH2G_GROUP_STACK
+        nodes++;
+        /* the hit children's meta bytes (a child's byte is never 0) */
+        uint32_t glo = metaLo & hlo, ghi = metaHi & hhi;
+        if ((glo | ghi) == 0u) return false;
+        uint32_t first, near = 0u;
+        if (ANYHIT) {
+            first = glo ? (uint32_t)(__ffs(glo) - 1) >> 3 : 4u + ((uint32_t)(__ffs(ghi) - 1) >> 3);
+        } else {
+            const uint32_t b = min(min(min(key[0], key[1]), min(key[2], key[3])), min(min(key[4], key[5]), min(key[6], key[7])));
+            first = b & 7u, near = b & ~7u;
+        }
+        const uint32_t sh = (first & 3u) * 8u;
+        const uint32_t m = ((first < 4u ? glo : ghi) >> sh) & 255u;
+        if (first < 4u) glo &= ~(255u << sh);
+        else ghi &= ~(255u << sh);
+        entry = (m & 0x80u) ? n1.x + (m & 7u) : leafBase + ((m >> 5) << 28) + (m & 31u);
+        if ((glo | ghi) != 0u) {
+            if (sp < LH2G_GSTACK) {
+                stack[sp] = make_uint4(n1.x, leafBase, glo, ghi);
+                if (!ANYHIT) gnear[sp] = __uint_as_float(near);
+                sp++;
+            } else {
+                status |= LH2G_STATUS_STACK_OVERFLOW;
+            }
+        }
+        return true;
+#elif !LH2G_SORT_CHILDREN
         const uint32_t best = min(min(min(key[0], key[1]), min(key[2], key[3])), min(min(key[4], key[5]), min(key[6], key[7])));
         nodes++;
         if (best == 0xffffffffu) return false;
@@ -395,15 +478,15 @@ struct Traversal {
             const uint32_t first = entry & 0x0fffffffu, cnt = ((entry >> 28) & 3u) + 1u;
             /* a full stack drops work: the status word says so (the hit record may then be wrong) */
             if (cnt > 1u) {
-                if (sp < LH2G_STACK) push(make_uint2(0x80000000u | ((cnt - 2u) << 28) | (first + 1u), 0u));
+                if (sp < CAP) push(make_uint2(0x80000000u | ((cnt - 2u) << 28) | (first + 1u), 0u));
                 else status |= LH2G_STATUS_STACK_OVERFLOW;
             }
             const int ii = (int)__ldg(S.tlasPrims + first);
             /* an InstanceGPU is four aligned float4: the three rows of the inverse transform, then blasRoot */
             const float4* in = reinterpret_cast<const float4*>(S.inst + ii);
             const uint32_t root = __float_as_uint(__ldg(in + 3).x);
-            if (root != 0xffffffffu && sp >= LH2G_STACK) status |= LH2G_STATUS_STACK_OVERFLOW;
-            if (root != 0xffffffffu && sp < LH2G_STACK) {
+            if (root != 0xffffffffu && sp >= CAP) status |= LH2G_STATUS_STACK_OVERFLOW;
+            if (root != 0xffffffffu && sp < CAP) {
                 const float4 r0 = __ldg(in), r1 = __ldg(in + 1), r2 = __ldg(in + 2);
                 const float m[12] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w};
                 O = xform_point(m, Ow), D = xform_vector(m, Dw);

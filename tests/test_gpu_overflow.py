@@ -1,6 +1,7 @@
 """Traversal that runs out of stack reports it.
 
-A variant of the core built with a 3-entry traversal stack (-DLH2G_STACK=3, in its own build directory) cannot
+A variant of the core built with a 3-entry traversal stack (-DLH2G_STACK=3, or 2 group entries, -DLH2G_GSTACK=2, in
+its own build directory) cannot
 hold the pending children of a two-level traversal through 66 instances (a node a ray crosses often has four or more
 hit children, and entering an instance takes a slot for the return marker), so it drops work; every place where a
 push is refused (sorted children, an instance leaf's remaining instances, the entry into an instance) sets the
@@ -19,7 +20,7 @@ pytestmark = pytest.mark.gpu
 @pytest.fixture(scope="module")
 def small_stack_lib(core_lib):
     from lighthouse2_gb300 import build
-    return build.build(out_dir=os.path.join(build.OUT, "stack3"), defines=["-DLH2G_STACK=3"])
+    return build.build(out_dir=os.path.join(build.OUT, "stack3"), defines=["-DLH2G_STACK=3", "-DLH2G_GSTACK=2"])
 
 
 def _field_rays(scene, n, seed=3):
