@@ -270,7 +270,7 @@ struct Traversal {
                 entry = e.x;
                 return true;
             }
-            if (!ANYHIT && found && gnear[sp - 1] > best.t) { sp--; continue; }
+            if (!ANYHIT && found && gnear[sp - 1] > fmaxf(best.t, 0.0f)) { sp--; continue; }
             /* the group's lowest remaining slot: its meta byte, then the rest written back (or the group dropped) */
             const bool lo = e.z != 0u;
             const uint32_t w = lo ? e.z : e.w;
@@ -288,7 +288,9 @@ struct Traversal {
             const uint2 e = take();
             entry = e.x;
             if (entry == ENTRY_MARKER || ANYHIT || (entry >> 30) == 2u) return true;
-            if (!found || __uint_as_float(e.y) <= best.t) return true;
+            /* e.y is the entry distance clamped to 0 and rounded down, a lower bound of the hits behind the entry
+             * once both sides are clamped: with a negative tmin the best hit may lie behind the origin */
+            if (!found || __uint_as_float(e.y) <= fmaxf(best.t, 0.0f)) return true;
         }
 #endif
     }
@@ -526,7 +528,7 @@ LH2G_DEV bool coop_pop(CoopRay& r, const uint2* stk) {
         const uint2 e = stk[--r.sp];
         r.entry = e.x;
         if (e.x == ENTRY_MARKER || ANYHIT || (e.x >> 30) == 2u) return true;
-        if (!r.found || __uint_as_float(e.y) <= r.best.t) return true;
+        if (!r.found || __uint_as_float(e.y) <= fmaxf(r.best.t, 0.0f)) return true;   /* clamped like the key */
     }
 }
 

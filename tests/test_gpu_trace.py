@@ -73,3 +73,21 @@ def test_empty_and_degenerate_rays(cornell):
     _compare_closest(g, c)
     assert np.array_equal(core.trace_host(rays, 1), o.trace(rays, 1))
     assert len(core.trace_host(rays[:0], 0)) == 0
+
+
+@pytest.mark.parametrize("scene", ["cornell", "spheres"])
+def test_negative_tmin(scene, request):
+    """Rays with tmin < 0 find hits behind their origins: the closest hit is the smallest t above tmin, which may be
+    negative. Once such a hit is found, pending boxes the ray entered before its origin must still be visited."""
+    sc, core, o = request.getfixturevalue(scene)
+    rays = S.random_rays(sc, 100_000, seed=21, kind="incoherent")
+    span = float(np.linalg.norm(np.asarray(sc.bounds[1]) - np.asarray(sc.bounds[0])))
+    rng = np.random.default_rng(5)
+    rays["tmin"] = -rng.uniform(0.0, 0.5, len(rays)) * span
+    rays["tmin"][:1000] = -1e30
+    g = core.trace_host(rays, mode=0)
+    c = o.trace(rays, mode=0)
+    _compare_closest(g, c)
+    behind = (c["prim"] >= 0) & (c["t"] < 0)
+    assert behind.sum() > 1000
+    assert np.array_equal(core.trace_host(rays, mode=1), o.trace(rays, mode=1))
