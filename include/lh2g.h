@@ -177,6 +177,8 @@ LH2G_API int lh2g_get_traversal_stats(lh2g_context* ctx, unsigned long long* out
 /* Ray queries over the scene (the OptiX Prime query interface of lib/RenderCore_PrimeRef/rendercore.cpp:569-605,
  * formats RTP_BUFFER_FORMAT_RAY_ORIGIN_TMIN_DIRECTION_TMAX / hit float4 {u|v<<16, inst, prim, t}).
  * mode 0: closest hit into lh2g_hit[n] (prim = -1 on a miss); mode 1: any hit into uint32 occluded[n].
+ * A hit has tmin < t < tmax; tmin may be negative (hits behind the origin). A ray with a NaN in its origin,
+ * direction, tmin or tmax is a miss and not occluded.
  * lh2g_trace takes device pointers and a CUDA stream (NULL = the context's stream) and returns without waiting;
  * lh2g_trace_host takes host buffers and returns when the results are back on the host. */
 LH2G_API int lh2g_trace(lh2g_context* ctx, const lh2g_ray* rays, void* out, long long n, int mode, void* stream);

@@ -113,6 +113,13 @@ constexpr uint32_t MAX_STEPS = 1u << 20;   /* far beyond any traversal of a well
 
 struct HitRec { float t, u, v; int inst, prim; };
 
+/* A NaN in a ray's origin, direction or interval makes it a miss without traversal: the box tests ignore NaN
+ * operands (min / max return the other one), so such a ray would visit every box along its other axes, and with
+ * an all-NaN direction the whole tree. The triangle test accepts no hit for it either way. */
+LH2G_DEV bool ray_has_nan(const float3 o, const float3 d, const float t0, const float t1) {
+    return o.x != o.x || o.y != o.y || o.z != o.z || d.x != d.x || d.y != d.y || d.z != d.z || t0 != t0 || t1 != t1;
+}
+
 /* 1 / d for the box tests, which only cull: the hardware reciprocal (at most 1 ulp off, which the slab margins
  * cover); |d| below 1e-30 (no denormal reaches rcp) gives +-1e30 */
 LH2G_DEV float safe_rcp(float d) {
@@ -224,7 +231,7 @@ struct Traversal {
 #if LH2G_SHORT_STACK
         base = 0;
 #endif
-        entry = S.tlasRoot;
+        entry = ray_has_nan(o, d, t0, t1) ? ENTRY_MARKER : S.tlasRoot;   /* the marker step ends a NaN ray */
         postponed = 0u;
     }
 
@@ -674,7 +681,7 @@ LH2G_DEV void trace_queue_coop(const SceneGPU& S, uint32_t* fetch, const uint32_
                 r.entry = S.tlasRoot;
                 ray = i;
                 active = true;
-                if (S.tlasRoot == 0xffffffffu) { onFinish(ray, r, false); active = false; }
+                if (S.tlasRoot == 0xffffffffu || ray_has_nan(o, d, t0, t1)) { onFinish(ray, r, false); active = false; }
             } else {
                 exhausted = true;
             }

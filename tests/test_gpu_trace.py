@@ -91,3 +91,24 @@ def test_negative_tmin(scene, request):
     behind = (c["prim"] >= 0) & (c["t"] < 0)
     assert behind.sum() > 1000
     assert np.array_equal(core.trace_host(rays, mode=1), o.trace(rays, mode=1))
+
+
+@pytest.mark.parametrize("scene", ["cornell", "spheres"])
+def test_nan_rays(scene, request):
+    """A NaN in a ray's origin, direction, tmin or tmax makes it a miss (and never occluded), as in the oracle, without
+    a traversal that the box tests' NaN handling would otherwise widen to every box along the ray's other axes."""
+    sc, core, o = request.getfixturevalue(scene)
+    rays = S.random_rays(sc, 20_000, seed=31, kind="incoherent")
+    nan = np.float32(np.nan)
+    rays["o"][0:500, 0] = nan
+    rays["o"][500:1000, 1:] = nan
+    rays["d"][1000:1500] = nan                       # the whole direction
+    rays["d"][1500:2000, 2] = nan
+    rays["tmin"][2000:2500] = nan
+    rays["tmax"][2500:3000] = nan
+    g = core.trace_host(rays, mode=0)
+    c = o.trace(rays, mode=0)
+    _compare_closest(g, c)
+    assert (g["prim"][:3000] < 0).all() and (g["prim"][3000:] >= 0).sum() > 1000
+    ga = core.trace_host(rays, mode=1)
+    assert np.array_equal(ga, o.trace(rays, mode=1)) and not ga[:3000].any()
