@@ -266,7 +266,7 @@ LH2G_API int lh2g_server_add_scene(lh2g_server* server, lh2g_context* scene, int
 /* hostOut: width * height float4. Filter frames (LH2G_RP_FILTER) are not served. */
 LH2G_API int lh2g_server_submit_render(lh2g_server* server, int sceneId, const lh2g_view* view, const lh2g_render_params* params,
                                        float* hostOut, long long* jobId);
-/* ray query as lh2g_trace_host: mode 0 closest hit into lh2g_hit[n], 1 any hit into uint32[n] */
+/* ray query as lh2g_trace_host: mode 0 closest hit into lh2g_hit[n], 1 any hit into uint32[n]; 1 <= n < 2^31 */
 LH2G_API int lh2g_server_submit_trace(lh2g_server* server, int sceneId, const lh2g_ray* hostRays, long long n, int mode, void* hostOut,
                                       long long* jobId);
 /* waits up to timeoutMs for a job: LH2G_OK when done (times filled), LH2G_ERR_STATE on timeout */
