@@ -266,3 +266,21 @@ def test_rays_grouped_by_octant_change_nothing(core_lib, oracle_lib, tail, mode)
     core.Setting("sortConnections", mode)   # both regroupings share the sort buffers
     _check_frame(core, o, view, p)
     core.close()
+
+
+@pytest.mark.parametrize("rr,tail", [(64, 5), (20, 0), (64, 0)])
+def test_deepest_paths(cornell, rr, tail):
+    """maxDepth 64, the largest accepted: without Russian roulette most paths in the closed room live to the last
+    path length, so every per-depth counter, the tail kernel's loop to depth 64 (waveTail 5) or 64 separate waves
+    (waveTail 0), and the 64-deep capture buffers are used; hit records, seeds, counts and radiance equal the
+    oracle's."""
+    sc, core, o = cornell
+    W, H, spp = 32, 24, 2
+    core.SetTarget(W, H, spp)
+    core.Setting("waveTail", tail)
+    try:
+        p = make_params(W, H, spp, max_depth=64, rr_start=rr, samples_taken=5, camera_r0=camera_r0(5), flags=RP_NEE | RP_DEPTH_W)
+        _check_frame(core, o, S.cornell_view(W, H), p)
+        assert core.GetCoreStats()["deviceStatus"] == 0
+    finally:
+        core.Setting("waveTail", 5)

@@ -190,3 +190,26 @@ def test_device_loop(two_scenes, tick_budget):
     assert st["deviceStatus"] == 0 and st["pathsInFlight"] == 0 and st["jobsDone"] == 2 * len(JOBS)
     assert 0 < st["loopLaunches"] < st["ticks"], st   # launches ran more than one tick each on average
     srv.close()
+
+
+@pytest.mark.parametrize("express_max", [None, 1 << 20])
+def test_deepest_paths_served(two_scenes, express_max):
+    """maxDepth 64 without Russian roulette in the closed room: served paths carry their depth up to 64 in their flag
+    word (through the queues, or whole as express jobs), beside a shallow job; images equal the plain core's."""
+    from lighthouse2_gb300.server import RenderServer
+    (sa, ca), (sb, cb) = two_scenes
+    kw = {} if express_max is None else {"expressMaxPaths": express_max}
+    srv = RenderServer(path_capacity=1 << 16, **kw)
+    sid = [srv.add_scene(ca), srv.add_scene(cb)]
+    jobs = [(0, 32, 24, 2, 64, 64, 1), (1, 40, 32, 1, 4, 2, 2), (0, 24, 24, 1, 64, 30, 3)]
+    ids = []
+    for j in jobs:
+        view, p = job_inputs(*j)
+        ids.append(srv.submit_render(sid[j[0]], view, p))
+    for k, jid in enumerate(ids):
+        srv.wait(jid)
+        view, p = job_inputs(*jobs[k])
+        exp = plain_core_image([ca, cb][jobs[k][0]], view, p)
+        assert np.array_equal(srv.result(jid).view(np.uint32), exp.view(np.uint32)), f"job {k} differs"
+    assert srv.stats()["deviceStatus"] == 0
+    srv.close()
