@@ -29,6 +29,49 @@ def test_exports(core_lib):
     C.CDLL(core_lib)  # loads
 
 
+def _signatures():
+    """(return type, argument declarations) of every lh2g_* entry point of include/lh2g.h"""
+    src = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "lh2g.h")).read(), flags=re.S)
+    sigs = {}
+    for m in re.finditer(r"LH2G_API\s+([\w\s\*]+?)\s*\b(lh2g_\w+)\s*\(([^)]*)\)\s*;", src):
+        sigs[m.group(2)] = (m.group(1).strip(), [a.strip() for a in m.group(3).split(",") if a.strip() not in ("", "void")])
+    return sigs
+
+
+def test_null_handles_refused(core_lib):
+    """Every entry point that takes a context, server or cache handle returns an error status for a NULL handle
+    with all other arguments NULL or zero, before any CUDA call (so it runs without a GPU); the two host-only
+    helpers return 0 records for empty input. The constructors and the GPU self-test are left out."""
+    lib = C.CDLL(core_lib)   # a handle of its own: no argument types set elsewhere
+    sigs = _signatures()
+    assert len(sigs) >= 60
+    skip = {"lh2g_create", "lh2g_server_create", "lh2g_nrc_create", "lh2g_nrc_wait_selftest"}
+    for name, (ret, args) in sigs.items():
+        if name in skip:
+            continue
+        f = getattr(lib, name)
+        vals = []
+        for a in args:
+            if "*" in a:
+                vals.append(C.c_void_p(None))
+            elif a.startswith("double"):
+                vals.append(C.c_double(0.0))
+            elif a.startswith("float"):
+                vals.append(C.c_float(0.0))
+            elif "long long" in a:
+                vals.append(C.c_longlong(0))
+            else:
+                vals.append(C.c_int(0))
+        f.restype = C.c_void_p if ret.endswith("*") else C.c_int
+        r = f(*vals)
+        if name.endswith("last_error") or ret.endswith("*"):
+            continue   # a message or a device pointer; it must only not crash
+        if name in ("lh2g_pack_materials", "lh2g_build_light_tree"):
+            assert r == 0, name
+        else:
+            assert r != 0, f"{name} accepted a NULL handle"
+
+
 def test_pack_materials_matches_oracle(core_lib, oracle_lib):
     from lighthouse2_gb300.core import load_library
     lib = load_library()
