@@ -559,6 +559,17 @@ int persistent_blocks_trace(int mode) {
 
 int persistent_blocks_wave(int which) {
     int per = 0;
+    if (LH2G_TRAV_CARVEOUT >= 0 && which <= 1) {   /* on the current device, before the occupancy query */
+        cudaFuncSetAttribute(k_extend<false>, cudaFuncAttributePreferredSharedMemoryCarveout, LH2G_TRAV_CARVEOUT);
+        cudaFuncSetAttribute(k_extend<true>, cudaFuncAttributePreferredSharedMemoryCarveout, LH2G_TRAV_CARVEOUT);
+        cudaFuncSetAttribute(k_connect, cudaFuncAttributePreferredSharedMemoryCarveout, LH2G_TRAV_CARVEOUT);
+    }
+    if (LH2G_SHADE_CARVEOUT >= 0 && which >= 2) {
+        cudaFuncSetAttribute(k_shade<false>, cudaFuncAttributePreferredSharedMemoryCarveout, LH2G_SHADE_CARVEOUT);
+        cudaFuncSetAttribute(k_shade<true>, cudaFuncAttributePreferredSharedMemoryCarveout, LH2G_SHADE_CARVEOUT);
+        cudaFuncSetAttribute(k_tail<false>, cudaFuncAttributePreferredSharedMemoryCarveout, LH2G_SHADE_CARVEOUT);
+        cudaFuncSetAttribute(k_tail<true>, cudaFuncAttributePreferredSharedMemoryCarveout, LH2G_SHADE_CARVEOUT);
+    }
     if (which == 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_extend<false>, 128, 0);
     else if (which == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_connect, 128, 0);
     else if (which == 2) {

@@ -92,6 +92,20 @@ constexpr int LH2G_TRAV_BLOCK = 128;
 #else
 #define LH2G_CONNECT_BOUNDS __launch_bounds__(LH2G_TRAV_BLOCK)
 #endif
+/* tuning switch: the plain core's wave traversal kernels' (k_extend, k_connect) preferred shared-memory carveout,
+ * in percent of the SM's unified L1 / shared storage (-1: the driver's choice); they use no shared memory.
+ * 0 (all of it L1): 1941-1947 against 1862-1868 Mrays/s on the 1080p frame with six frames in flight, where those
+ * kernels run beside other frames' shading kernels (50: 1864); a kernel alone is a little slower with it
+ * (k_extend of frames rendered one at a time 1.64 against 1.60 ms), so the ray-query and serving kernels keep
+ * the driver's choice (with the hint: incoherent closest-hit queries -2.6 %, the small serving mix -2.5 %). */
+#ifndef LH2G_TRAV_CARVEOUT
+#define LH2G_TRAV_CARVEOUT 0
+#endif
+/* the same for the shading kernels (k_shade, k_tail), which hold the light potentials in dynamic shared memory
+ * (100, all of it shared: 1897 Mrays/s, both kernels slower; -1 stays) */
+#ifndef LH2G_SHADE_CARVEOUT
+#define LH2G_SHADE_CARVEOUT -1
+#endif
 /* LH2G_STAGE_RAYS 1: in the warp-batch loop (LH2G_REFILL 0, LH2G_COOP 0) the next 32 rays' path-state records
  * (the SoA arrays a kernel names: origins, directions, ...) are copied into the warp's shared-memory slot by bulk
  * asynchronous copies (cp.async.bulk, completion on an mbarrier) while the warp traces the current 32; 0 (the
