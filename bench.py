@@ -45,7 +45,7 @@ WAVE_TAIL = 5          # path lengths >= 5 run in the persistent tail kernel (se
 LANES = 6              # frames in flight (setting "pipelineFrames")
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of three k_extend launches of this workload (waves 1, 2 and 3
 # of camera pose 1): 197.65 MB + 197.72 MB + 74.47 MB (profiles/k_extend_spheres_2m_1080p.md)
-EXTEND_CAPTURE = {"pose": 1, "waves": (1, 2, 3), "dram_bytes": (152.189696e6 + 45.460992e6) + (151.02464e6 + 46.699264e6) + (63.042816e6 + 11.42272e6)}
+EXTEND_CAPTURE = {"pose": 1, "waves": (1, 2, 3), "dram_bytes": (150.159872e6 + 39.314432e6) + (146.592e6 + 33.778688e6) + (61.080832e6 + 6.445824e6)}
 WORKLOAD = "spheres_2m: 64 x 32k-tri displaced spheres + ground (2,048,002 tris, 66 instances), 16 quad + 4 point lights, " \
            "20 materials (4 textured), sky; 1920x1080 1spp, max depth 8, RR after depth 3, NEE"
 METRIC = "Mrays/s @1080p 1spp"
