@@ -102,7 +102,8 @@ constexpr int LH2G_TRAV_BLOCK = 128;
 #define LH2G_TRAV_CARVEOUT 0
 #endif
 /* the same for the shading kernels (k_shade, k_tail), which hold the light potentials in dynamic shared memory
- * (100, all of it shared: 1897 Mrays/s, both kernels slower; -1 stays) */
+ * (100, all of it shared: 1897 Mrays/s, both kernels slower; 0: 1391-1397, k_shade 2.04 against 0.62 ms with fewer
+ * CTAs resident; -1 stays) */
 #ifndef LH2G_SHADE_CARVEOUT
 #define LH2G_SHADE_CARVEOUT -1
 #endif
